@@ -1,0 +1,300 @@
+// Device-side atmosphere: temperature profile, chemistry, hydrostatic altitude,
+// grey cloud and the opacity-table stencils, one thread block per evaluation.
+//
+// Compiled with --fmad=false: every product and sum is rounded separately,
+// like the reference's host code, so that the discrete decisions made here
+// (temperature clamp, table brackets, cloud layer indices) agree bit for bit
+// with the reference on the same parameters.
+
+#include "model.h"
+
+namespace bgb {
+
+namespace {
+
+// PiecewisePolynomial::getValue src/additional/piecewise_poly.cpp:154-181 and
+// Element::getValue / lagrangeBase :202-229.
+__device__ double poly_value(const AtmosphereConfig& c, const double* dof, double x) {
+  if (x > c.pp_dof_vertices[0] || x < c.pp_dof_vertices[c.pp_ndof - 1]) return 0.0;
+  for (int i = 0; i < c.pp_ndof; ++i)
+    if (c.pp_dof_vertices[i] == x) return dof[i];
+  const int nd = c.pp_ndof_el;
+  int el = 0;
+  for (int e = 0; e < c.pp_nel; ++e)
+    if (c.pp_el_vert[e * nd] > x && c.pp_el_vert[e * nd + nd - 1] < x) {
+      el = e;
+      break;
+    }
+  const double xl = c.pp_el_vert[el * nd], xr = c.pp_el_vert[el * nd + nd - 1];
+  const double r = 2.0 * (x - xl) / (xr - xl) - 1.0;
+  double y = 0;
+  for (int i = 0; i < nd; ++i) {
+    double l = 1;
+    for (int j = 0; j < nd; ++j) {
+      if (i == j) continue;
+      l *= (r - c.pp_ref[j]) / (c.pp_ref[i] - c.pp_ref[j]);
+    }
+    y += dof[el * (nd - 1) + i] * l;
+  }
+  return y;
+}
+
+__device__ __constant__ double kMolWeight[kSpeciesCount] = {
+    0.0,      1.00784, 4.002602, 12.0107, 15.999,   55.845,   55.845,  40.078,  47.867,
+    47.867,   2.01588, 18.01528, 44.01,   28.0101,  16.04246, 27.0253, 17.03052, 26.04,
+    28.0134,  22.98977, 39.0983, 34.09099, 1.00784, 63.8664,  66.9409, 56.853,  34.08,
+    40.3044,  42.981,  56.0774,  54.0040, 26.3209,  41.0859,  48.87484, 17.008,
+    5.4857990907e-4, 50.9415, 50.9415, 54.938044, 28.085, 51.996, 51.996, 44.08, 60.08,
+    64.066,   76.139};
+
+// Chemistry::meanMolecularWeight src/chemistry/chemistry.h:47-59
+__device__ double mean_molecular_weight(const double* n) {
+  double mu = 0;
+  for (int j = 0; j < kSpeciesCount; ++j) mu += n[j] / n[SP_TOTAL] * kMolWeight[j];
+  return mu;
+}
+
+}  // namespace
+
+// One block per evaluation, blockDim.x >= L. Dynamic shared memory: 4 L doubles.
+__global__ void __launch_bounds__(kMaxLevels) atmosphere_kernel(DeviceModel dm, const double* __restrict__ params, int P,
+                                  LevelInfo* __restrict__ lev, LevelSpecies* __restrict__ ls,
+                                  double* __restrict__ ray_n, EvalInfo* __restrict__ ev) {
+  const AtmosphereConfig& c = *dm.cfg;
+  const int b = blockIdx.x;
+  const int l = threadIdx.x;
+  const int L = c.L, S = c.S;
+  extern __shared__ double smem[];
+  double* sT = smem;
+  double* smmw = smem + L;
+  double* sz = smem + 2 * L;
+  double* sH = smem + 3 * L;
+  __shared__ int s_neglect;
+  __shared__ int s_top, s_bottom;
+  __shared__ double s_cloud_layer;
+  if (l == 0) s_neglect = 0;
+  __syncthreads();
+
+  const double* par = params + (size_t)b * P;
+  const double* gen = par;
+  const double* chem = par + c.nparam_general;
+  const double* temp = chem + c.nparam_chem;
+  const double* cloud = temp + c.nparam_temp;
+  // EmissionModel::calcAtmosphereStructure src/forward_model/emission/emission.cpp:158-189,
+  // TransmissionModel::calcAtmosphereStructure src/forward_model/transmission/transmission.cpp:150-194
+  const double g = pow(10.0, gen[0]);
+
+  int neglect = 0;
+  if (l < L) {
+    const double p = dm.pressure[l];
+    // temperature: PiecewisePolynomialTemperature::calcProfile
+    // src/temperature/piecewise_poly_temperature.cpp:49-84, ConstantTemperature
+    // src/temperature/constant_temperature.h:37-44
+    double T;
+    if (c.temp_poly) {
+      double dof[kMaxPolyDof];
+      dof[0] = temp[0];
+      for (int i = 1; i < c.pp_ndof; ++i) dof[i] = dof[i - 1] * temp[i];
+      T = poly_value(c, dof, dm.log10p[l]);
+      if (T < 50) {
+        T = 50;
+        neglect = 1;
+      }
+    } else {
+      T = temp[0];
+    }
+    // chemistry modules in configuration order
+    double n[kSpeciesCount];
+    for (int j = 0; j < kSpeciesCount; ++j) n[j] = 0.0;
+    double mmw = 0.0;
+    int pidx = 0;
+    for (int m = 0; m < c.nchem; ++m) {
+      if (c.chem_kind[m] == 0) {
+        // IsoprofileChemistry::calcChemicalComposition src/chemistry/isoprofile_chemistry.cpp:87-119
+        n[SP_TOTAL] = p * 1.e6 / kBoltzmann / T;
+        for (int j = 0; j < c.chem_nsp[m]; ++j) n[c.chem_sp[m][j]] = n[SP_TOTAL] * chem[pidx + j];
+        if (!c.chem_na_free[m]) n[SP_Na] = n[SP_K] * 16.2181;
+        mmw = mean_molecular_weight(n);
+        // Chemistry::checkMixingRatios src/chemistry/chemistry.h:61-76
+        double sum = 0;
+        for (int j = 1; j < kSpeciesCount; ++j) sum += n[j] / n[SP_TOTAL];
+        if (sum > 1 + 1e-10) neglect = 1;
+        pidx += c.chem_nsp[m];
+      } else {
+        // BackgroundChemistry::calcChemicalComposition src/chemistry/background_chemistry.cpp:72-137
+        const double sh2 = 0.5, she = 0.085114;
+        const double sh2he = sh2 + she;
+        n[SP_TOTAL] = p * 1.e6 / kBoltzmann / T;
+        double bg = 1.0;
+        for (int j = 1; j < kSpeciesCount; ++j) {
+          if (c.chem_bg_h2he[m]) {
+            if (j != SP_H2 && j != SP_He) bg -= n[j] / n[SP_TOTAL];
+          } else if (j != c.chem_bg_sp[m]) {
+            bg -= n[j] / n[SP_TOTAL];
+          }
+        }
+        if (bg < 0) {
+          neglect = 1;
+          bg = 0;
+        }
+        if (c.chem_bg_h2he[m]) {
+          const double xh2 = bg * sh2 / sh2he;
+          const double xhe = bg * she / sh2he;
+          n[SP_H2] = n[SP_TOTAL] * xh2;
+          n[SP_He] = n[SP_TOTAL] * xhe;
+        } else {
+          n[c.chem_bg_sp[m]] = n[SP_TOTAL] * bg;
+        }
+        mmw = mean_molecular_weight(n);
+      }
+    }
+    if (c.transmission && c.fit_mmw) mmw = gen[3];  // Atmosphere::calcAtmosphereStructure :126-187
+    sT[l] = T;
+    smmw[l] = mmw;
+    // number densities of the opacity species (OpacitySpecies::calcTransportCoefficients
+    // src/transport_coeff/opacity_species.cpp:407-410: index species times collision partners)
+    for (int s = 0; s < S; ++s) {
+      double nd = n[c.sp_index[s]];
+      if (c.sp_partner[s][0] >= 0) nd *= n[c.sp_partner[s][0]];
+      if (c.sp_partner[s][1] >= 0) nd *= n[c.sp_partner[s][1]];
+      ls[((size_t)b * L + l) * S + s].n = nd;
+    }
+    for (int r = 0; r < c.R; ++r) ray_n[((size_t)b * L + l) * c.R + r] = n[c.ray_index[r]];
+    if (neglect) atomicOr(&s_neglect, 1);
+  }
+  __syncthreads();
+
+  // hydrostatic altitude: Atmosphere::calcAltitude src/forward_model/atmosphere/atmosphere.cpp:288-307,
+  // calcAltitudeVariableGravity :311-334; scale height calcScaleHeight :353-360.
+  double dz_l = 0.0;
+  if (l >= 1 && l < L && !c.var_g) {
+    const double rho_i = smmw[l] * dm.pressure[l] * 1e6 / (kGasConst * sT[l]);
+    const double rho_m = smmw[l - 1] * dm.pressure[l - 1] * 1e6 / (kGasConst * sT[l - 1]);
+    dz_l = (1.0 / (rho_i * g) + 1.0 / (rho_m * g)) * 0.5 * (dm.pressure[l - 1] * 1e6 - dm.pressure[l] * 1e6);
+  }
+  if (l < L) sH[l] = dz_l;  // staged through sH
+  __syncthreads();
+  if (l == 0) {
+    sz[0] = 0.0;
+    if (!c.var_g) {
+      for (int i = 1; i < L; ++i) sz[i] = sz[i - 1] + sH[i];
+    } else {
+      const double R0 = gen[1];
+      for (int i = 1; i < L; ++i) {
+        const double rho_i = smmw[i] * dm.pressure[i] * 1e6 / (kGasConst * sT[i]);
+        const double rho_m = smmw[i - 1] * dm.pressure[i - 1] * 1e6 / (kGasConst * sT[i - 1]);
+        const double lr = R0 + sz[i - 1];
+        const double ratio = R0 / lr;
+        const double gi = g * (ratio * ratio);
+        const double dz = (1.0 / (rho_i * gi) + 1.0 / (rho_m * gi)) * 0.5 * (dm.pressure[i - 1] * 1e6 - dm.pressure[i] * 1e6);
+        sz[i] = sz[i - 1] + dz;
+      }
+    }
+  }
+  __syncthreads();
+  if (l < L) sH[l] = kGasConst * sT[l] / (smmw[l] * g);
+  __syncthreads();
+
+  // grey cloud: GreyCloudModel::opticalProperties / cloudPosition
+  // src/cloud_model/grey_cloud_model.cpp:59-195
+  if (l == 0) {
+    int top = 0, bottom = 0;
+    double per = 0.0;
+    if (c.cloud) {
+      double tau = cloud[0];
+      const double ptop = cloud[1];
+      const double pbot = c.cloud_fb ? 0.0 : ptop * cloud[2];
+      if (tau < 0) tau = 0;
+      unsigned ti = 0, bi = 0;
+      for (int i = 0; i < L - 1; ++i)
+        if ((dm.pressure[i] > ptop && dm.pressure[i + 1] < ptop) || dm.pressure[i] == ptop) ti = i;
+      if (c.cloud_fb) {
+        if (ptop < dm.pressure[L - 1]) ti = L - 1;
+        double ba = sz[ti] - sH[ti];
+        if (ba < 0) ba = 0;
+        for (int i = 0; i < L - 1; ++i)
+          if ((sz[i] < ba && sz[i + 1] > ba) || sz[i] == ba) bi = i;
+        if (ti == bi) bi -= 2;
+        if (ti == bi) bi -= 2;
+        if (ti < 2) { ti = 2; bi = 0; }
+      } else {
+        for (int i = 0; i < L - 1; ++i)
+          if ((dm.pressure[i] > pbot && dm.pressure[i + 1] < pbot) || dm.pressure[i] == pbot) bi = i;
+        if (ptop <= dm.pressure[L - 1]) ti = L - 1;
+        if (pbot >= dm.pressure[0]) bi = 0;
+        if (ti == bi) bi -= 2;
+        if (ti < 2) { ti = 2; bi = 0; }
+      }
+      per = tau / (double)(ti - bi);
+      top = (int)ti;
+      bottom = (int)bi;
+    }
+    s_top = top;
+    s_bottom = bottom;
+    s_cloud_layer = per;
+    EvalInfo e;
+    // EmissionModel::radiusDistanceScaling src/forward_model/emission/emission.cpp:108-120
+    double sc = kRJupiter / gen[2];
+    e.scaling = sc * sc * gen[1];
+    e.radius = gen[1];
+    e.star_radius = gen[2];
+    // Retrieval::logLikelihood error inflation src/retrieval/retrieval.cpp:332-335
+    e.inflation = c.error_inflation ? pow(10.0, par[P - 1]) : 0.0;
+    e.neglect = s_neglect;
+    e.cloud_top = top;
+    e.cloud_bottom = bottom;
+    e.pad = 0;
+    ev[b] = e;
+  }
+  __syncthreads();
+
+  if (l < L) {
+    const double T = sT[l];
+    LevelInfo li;
+    li.T = T;
+    li.invT = 1.0 / T;
+    li.z = sz[l];
+    li.dz = (l + 1 < L) ? sz[l + 1] - sz[l] : 0.0;
+    double cl = 0.0;
+    if (c.cloud) {
+      // layer l holds tau / (top - bottom) for bottom < l <= top (and l < L - 1)
+      const unsigned top = (unsigned)s_top, bottom = (unsigned)s_bottom;
+      auto layer_tau = [&](int j) -> double {
+        return ((unsigned)j <= top && (unsigned)j > bottom && j < L - 1) ? s_cloud_layer : 0.0;
+      };
+      if (!c.transmission) cl = layer_tau(l);
+      else if (l >= 1) cl = layer_tau(l - 1) / (sz[l] - sz[l - 1]);  // CloudModel::convertOpticalDepth src/cloud_model/cloud_model.h:67-88
+    }
+    li.cloud = cl;
+    li.pad = 0;
+    lev[(size_t)b * L + l] = li;
+    // table stencils: OpacitySpecies::findClosestDataPoints src/transport_coeff/opacity_species.cpp:160-273
+    for (int s = 0; s < S; ++s) {
+      const double* Tn = dm.table_T + c.sp_T_off[s];
+      const int nT = c.sp_nT[s];
+      int lo = 0, up = 0;
+      if (T < Tn[0]) {
+        lo = up = 0;
+      } else if (T > Tn[nT - 1]) {
+        lo = up = nT - 1;
+      } else {
+        for (int i = 0; i < nT; ++i) {
+          if (Tn[i] == T) { lo = up = i; break; }
+          if (Tn[i] < T && Tn[i + 1] > T) { lo = i; up = i + 1; break; }
+        }
+      }
+      LevelSpecies& e = ls[((size_t)b * L + l) * S + s];
+      const int ilo = c.sp_pb_off[s] + lo * L + l;
+      const int iup = c.sp_pb_off[s] + up * L + l;
+      e.row[0] = dm.pb_row0[ilo];
+      e.row[1] = dm.pb_row1[ilo];
+      e.row[2] = dm.pb_row0[iup];
+      e.row[3] = dm.pb_row1[iup];
+      e.wp_lo = dm.pb_w[ilo];
+      e.wp_hi = dm.pb_w[iup];
+      e.wT = (lo != up) ? (T - Tn[lo]) / (Tn[up] - Tn[lo]) : 0.0;
+    }
+  }
+}
+
+}  // namespace bgb

@@ -1,0 +1,315 @@
+// C ABI of the engine (include/bear_gb300.h): argument checking, error
+// translation and the plain-path orchestration around the device kernels.
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/bear_gb300.h"
+#include "model.h"
+
+struct bear_model {
+  bgb::Model m;
+};
+
+namespace {
+
+thread_local std::string g_last_error = "";
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+template <class F>
+int guarded(F&& f) {
+  try {
+    f();
+    return BEAR_OK;
+  } catch (const bgb::Error& e) {
+    return fail(e.code, e.msg);
+  } catch (const std::bad_alloc&) {
+    return fail(BEAR_ERR_INVALID_INPUT, "host allocation failed");
+  } catch (const std::exception& e) {
+    return fail(BEAR_ERR_INVALID_INPUT, e.what());
+  }
+}
+
+void check_cuda(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw bgb::Error(BEAR_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void require_ready(const bear_model* h) {
+  if (!h) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null model");
+  if (!h->m.finalized) throw bgb::Error(BEAR_ERR_STATE, "model is not finalized");
+}
+
+void require_prepared(const bear_model* h) {
+  if (!h) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null model");
+  if (!h->m.prepared) throw bgb::Error(BEAR_ERR_STATE, "model is not prepared");
+}
+
+void require_params(const bear_model* h, int nb_params) {
+  if (nb_params != h->m.acfg.nparam_total)
+    throw bgb::Error(BEAR_ERR_SIZE, "expected " + std::to_string(h->m.acfg.nparam_total) +
+                                        " parameters, got " + std::to_string(nb_params));
+}
+
+// Stage host parameters into the workspace and run one evaluation.
+void run_plain(bear_model* h, const double* params, int nb_params, cudaStream_t st) {
+  bgb::Model& m = h->m;
+  require_params(h, nb_params);
+  if (!params) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null parameters");
+  if ((size_t)nb_params * sizeof(double) > m.h_pinned_bytes)
+    throw bgb::Error(BEAR_ERR_SIZE, "too many parameters for the staging buffer");
+  bgb::ensure_workspace(m, 1);
+  std::memcpy(m.h_pinned, params, nb_params * sizeof(double));
+  check_cuda(cudaMemcpyAsync(m.ws.params, m.h_pinned, nb_params * sizeof(double), cudaMemcpyHostToDevice, st),
+             "parameter upload");
+  bgb::launch_forward(m, m.ws.params, 1, st, true, nullptr, m.ws.loglike);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* bear_last_error(void) { return g_last_error.c_str(); }
+
+int bear_model_create(const char* config_text, int device, bear_model** out) {
+  if (!out) return fail(BEAR_ERR_INVALID_INPUT, "null output handle");
+  *out = nullptr;
+  bear_model* h = new bear_model();
+  int rc = guarded([&] {
+    if (!config_text) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null config text");
+    h->m.device = device;
+    bgb::parse_config(h->m, config_text);
+  });
+  if (rc != BEAR_OK) {
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return BEAR_OK;
+}
+
+int bear_model_add_observation(bear_model* h, const char* name, const char* type, int n,
+                               const double* ce, const double* data, const double* error,
+                               const double* weight, const double* fwhm, int n_filter,
+                               const double* fwl, const double* fresp, const char* detector,
+                               const char* modifier) {
+  return guarded([&] {
+    if (!h) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null model");
+    if (!ce || !data || !error) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "observation arrays missing");
+    if (n_filter > 0 && (!fwl || !fresp)) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "filter arrays missing");
+    bgb::add_observation(h->m, name, type, n, ce, data, error, weight, fwhm, n_filter, fwl, fresp,
+                         detector, modifier);
+  });
+}
+
+int bear_model_prepare(bear_model* h) {
+  return guarded([&] {
+    if (!h) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null model");
+    if (!h->m.prepared) {
+      bgb::finalize_host(h->m);
+      h->m.prepared = true;
+    }
+  });
+}
+
+int bear_model_finalize(bear_model* h) {
+  return guarded([&] {
+    if (!h) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null model");
+    if (h->m.finalized) throw bgb::Error(BEAR_ERR_STATE, "model already finalized");
+    if (!h->m.prepared) {
+      bgb::finalize_host(h->m);
+      h->m.prepared = true;
+    }
+    bgb::upload_model(h->m);
+    h->m.finalized = true;
+  });
+}
+
+int bear_model_observation_setup(const bear_model* h, int k, long long* out, int cap, int* written) {
+  return guarded([&] {
+    require_prepared(h);
+    const bgb::Model& m = h->m;
+    if (k < 0 || k >= (int)m.obs.size()) throw bgb::Error(BEAR_ERR_SIZE, "observation index out of range");
+    const bgb::ObservationSetup& o = m.obs[k];
+    std::vector<long long> v{(long long)o.range_lo, (long long)o.range_hi, (long long)o.n};
+    for (auto& e : o.edge_idx) { v.push_back((long long)e[0]); v.push_back((long long)e[1]); }
+    if (o.has_profile)
+      for (auto& c : o.conv) { v.push_back((long long)c[0]); v.push_back((long long)c[1]); }
+    if ((int)v.size() > cap) throw bgb::Error(BEAR_ERR_SIZE, "capacity too small: need " + std::to_string(v.size()));
+    std::copy(v.begin(), v.end(), out);
+    *written = (int)v.size();
+  });
+}
+
+int bear_model_operator_row(const bear_model* h, int r, int* k0, int* len, const double** weights) {
+  return guarded([&] {
+    require_prepared(h);
+    const bgb::Model& m = h->m;
+    if (r < 0 || r >= m.M) throw bgb::Error(BEAR_ERR_SIZE, "operator row out of range");
+    for (const auto& o : m.obs) {
+      if (r < o.out_offset + o.n) {
+        const int j = r - o.out_offset;
+        *k0 = o.row_k0[j];
+        *len = o.row_len[j];
+        *weights = m.W.data() + o.row_off[j];
+        return;
+      }
+    }
+  });
+}
+
+int bear_model_info(const bear_model* h, int* N, int* M, int* P, int* nobs) {
+  return guarded([&] {
+    require_prepared(h);
+    if (N) *N = (int)h->m.N;
+    if (M) *M = h->m.M;
+    if (P) *P = h->m.acfg.nparam_total;
+    if (nobs) *nobs = (int)h->m.obs.size();
+  });
+}
+
+int bear_model_wavenumbers(const bear_model* h, double* out) {
+  return guarded([&] {
+    require_prepared(h);
+    std::memcpy(out, h->m.nu.data(), h->m.N * sizeof(double));
+  });
+}
+
+int bear_model_observation_size(const bear_model* h, int k, int* n) {
+  return guarded([&] {
+    require_prepared(h);
+    if (k < 0 || k >= (int)h->m.obs.size()) throw bgb::Error(BEAR_ERR_SIZE, "observation index out of range");
+    *n = h->m.obs[k].n;
+  });
+}
+
+int bear_model_device_bytes(const bear_model* h, size_t* bytes) {
+  return guarded([&] {
+    require_ready(h);
+    const bgb::Model& m = h->m;
+    size_t ws = 0;
+    if (m.ws.capacity) {
+      const size_t B = m.ws.capacity, L = m.L, S = std::max(m.acfg.S, 1), N = m.N;
+      ws = B * (L * sizeof(bgb::LevelInfo) + L * S * sizeof(bgb::LevelSpecies) + N * 8 + m.M * 8 + 64);
+      if (m.transmission) ws += B * L * L * 8;
+    }
+    *bytes = m.device_bytes + ws;
+  });
+}
+
+void bear_model_destroy(bear_model* h) {
+  if (!h) return;
+  if (h->m.finalized) bgb::release_model(h->m);
+  delete h;
+}
+
+int bear_model_set_precision(bear_model* h, int fp32_tables) {
+  return guarded([&] {
+    if (!h) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null model");
+    h->m.fp32_tables = fp32_tables != 0;
+  });
+}
+
+int bear_model_set_launch(bear_model* h, int rt_threads, int obs_threads) {
+  return guarded([&] {
+    if (!h) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null model");
+    if (rt_threads < 0 || rt_threads > 256 || rt_threads % 32) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "rt_threads must be a multiple of 32 up to 256");
+    if (obs_threads < 0 || obs_threads > 1024 || obs_threads % 32) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "obs_threads must be a multiple of 32 up to 1024");
+    h->m.rt_threads = rt_threads;
+    h->m.obs_threads = obs_threads;
+  });
+}
+
+int bear_forward(bear_model* h, const double* params, int nb_params, double* spectrum_dev,
+                 double* const* obs_dev, int* neglect, void* stream) {
+  return guarded([&] {
+    require_ready(h);
+    bgb::Model& m = h->m;
+    cudaStream_t st = (cudaStream_t)stream;
+    run_plain(h, params, nb_params, st);
+    if (spectrum_dev) bgb::launch_spectrum_output(m, spectrum_dev, st);
+    if (obs_dev) {
+      for (size_t o = 0; o < m.obs.size(); ++o) {
+        if (!obs_dev[o]) continue;
+        check_cuda(cudaMemcpyAsync(obs_dev[o], m.ws.obs + m.obs[o].out_offset, m.obs[o].n * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, st), "observation output");
+      }
+    }
+    bgb::EvalInfo ev;
+    check_cuda(cudaMemcpyAsync(&ev, m.ws.ev, sizeof ev, cudaMemcpyDeviceToHost, st), "neglect flag");
+    check_cuda(cudaStreamSynchronize(st), "forward model");
+    if (neglect) *neglect = ev.neglect;
+  });
+}
+
+int bear_compute_model(bear_model* h, const double* params, int nb_params, double* spectrum,
+                       double* obs, int* neglect, void* stream) {
+  return guarded([&] {
+    require_ready(h);
+    bgb::Model& m = h->m;
+    cudaStream_t st = (cudaStream_t)stream;
+    run_plain(h, params, nb_params, st);
+    std::vector<double> internal(std::max(m.M, 1));
+    if (spectrum) {
+      bgb::launch_spectrum_output(m, m.ws.spectrum + 0, st);  // in place: plain path owns row 0
+      check_cuda(cudaMemcpyAsync(spectrum, m.ws.spectrum, m.N * sizeof(double), cudaMemcpyDeviceToHost, st),
+                 "spectrum download");
+    }
+    check_cuda(cudaMemcpyAsync(internal.data(), m.ws.obs, m.M * sizeof(double), cudaMemcpyDeviceToHost, st),
+               "observation download");
+    bgb::EvalInfo ev;
+    check_cuda(cudaMemcpyAsync(&ev, m.ws.ev, sizeof ev, cudaMemcpyDeviceToHost, st), "neglect flag");
+    check_cuda(cudaStreamSynchronize(st), "compute model");
+    if (obs) {
+      // ForwardModel::calcModel reverses observations given in ascending wavelength order
+      // (src/forward_model/forward_model.cpp:119-123)
+      for (const auto& o : m.obs)
+        for (int j = 0; j < o.n; ++j)
+          obs[o.out_offset + (o.ascending ? o.n - 1 - j : j)] = internal[o.out_offset + j];
+    }
+    if (neglect) *neglect = ev.neglect;
+  });
+}
+
+int bear_loglike(bear_model* h, const double* params, int nb_params, double* loglike, void* stream) {
+  return guarded([&] {
+    require_ready(h);
+    bgb::Model& m = h->m;
+    cudaStream_t st = (cudaStream_t)stream;
+    run_plain(h, params, nb_params, st);
+    check_cuda(cudaMemcpyAsync(m.h_pinned, m.ws.loglike, sizeof(double), cudaMemcpyDeviceToHost, st),
+               "log-likelihood download");
+    check_cuda(cudaStreamSynchronize(st), "log-likelihood");
+    *loglike = m.h_pinned[0];
+  });
+}
+
+int bear_loglike_batch(bear_model* h, const double* params_dev, int batch, int nb_params,
+                       double* loglike_dev, uint8_t* neglect_dev, void* stream) {
+  return guarded([&] {
+    require_ready(h);
+    require_params(h, nb_params);
+    if (batch < 1) throw bgb::Error(BEAR_ERR_SIZE, "batch must be positive");
+    if (!params_dev || !loglike_dev) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null device buffer");
+    bgb::launch_forward(h->m, params_dev, batch, (cudaStream_t)stream, true, neglect_dev, loglike_dev);
+  });
+}
+
+int bear_loglike_grad_batch(bear_model* h, const double* params_dev, int batch, int nb_params,
+                            double* loglike_dev, double* grad_dev, uint8_t* neglect_dev,
+                            void* stream) {
+  return guarded([&] {
+    require_ready(h);
+    require_params(h, nb_params);
+    if (batch < 1) throw bgb::Error(BEAR_ERR_SIZE, "batch must be positive");
+    if (!params_dev || !loglike_dev || !grad_dev) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null device buffer");
+    bgb::launch_gradient(h->m, params_dev, batch, (cudaStream_t)stream, loglike_dev, grad_dev, neglect_dev);
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,455 @@
+// GB300 kernels of the likelihood engine and their host-side launch code.
+//
+// Data layout in HBM
+//   tables      rows x N, log10 cross sections, wavenumber contiguous (one row
+//               per (species, T, p) table point, sampled on the model grid)
+//   LevelSpecies B x L x S, LevelInfo B x L, EvalInfo B: per-evaluation
+//               atmosphere and stencils written by atmosphere_kernel
+//   spectrum    B x N native units (per cm^-1 flux or ppm transit depth)
+//   W           banded observation operator, one contiguous row per bin
+//
+// Kernels (per batch):
+//   atmosphere_kernel  (atmosphere.cu)  one block per evaluation
+//   emission_kernel    opacity + short-characteristics RT fused per wavenumber;
+//                      the per-level opacities are never materialised
+//   transmission_*     geometry per evaluation, then opacity + tangent-ray
+//                      optical depths + effective height per wavenumber
+//   obs_loglike_kernel banded W . F per bin with warp-shuffle reductions and the
+//                      Gaussian log-likelihood reduced per evaluation
+// Grids put the evaluation index on blockIdx.x and the wavenumber tile on
+// blockIdx.y, so the blocks resident at any time share one wavenumber tile of
+// the tables in L2.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "../../include/bear_gb300.h"
+#include "model.h"
+
+namespace bgb {
+
+#define BGB_CUDA(x)                                                                         \
+  do {                                                                                      \
+    cudaError_t e_ = (x);                                                                   \
+    if (e_ != cudaSuccess)                                                                  \
+      throw Error(BEAR_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));         \
+  } while (0)
+
+__global__ void atmosphere_kernel(DeviceModel dm, const double* __restrict__ params, int P,
+                                  LevelInfo* __restrict__ lev, LevelSpecies* __restrict__ ls,
+                                  double* __restrict__ ray_n, EvalInfo* __restrict__ ev);
+
+// Gauss nodes and weights of ShortCharacteristics (src/radiative_transfer/short_characteristics.h:62-63)
+__device__ __constant__ double kMu[2] = {0.211324865405187, 0.788675134594813};
+__device__ __constant__ double kInvMu[2] = {1.0 / 0.211324865405187, 1.0 / 0.788675134594813};
+
+template <typename TT>
+__device__ __forceinline__ double load_table(const TT* __restrict__ tab, size_t idx) {
+  return (double)__ldg(tab + idx);
+}
+
+// Sum over table species of 10^(bilinear log-p / T interpolation) * n at one
+// level and one wavenumber (OpacitySpecies::calcAbsorptionCrossSections
+// src/transport_coeff/opacity_species.cpp:277-345 and calcTransportCoefficients :400-455).
+template <typename TT>
+__device__ __forceinline__ double level_absorption(const TT* __restrict__ tab, size_t N,
+                                                   const LevelSpecies* __restrict__ d, int S,
+                                                   int k) {
+  double kap = 0.0;
+  for (int s = 0; s < S; ++s) {
+    const int4 r = __ldg(reinterpret_cast<const int4*>(d + s));
+    const double2 w = __ldg(reinterpret_cast<const double2*>(&d[s].wp_lo));
+    const double2 t = __ldg(reinterpret_cast<const double2*>(&d[s].wT));
+    const double v0 = load_table(tab, (size_t)r.x * N + k);
+    const double v1 = load_table(tab, (size_t)r.y * N + k);
+    const double v2 = load_table(tab, (size_t)r.z * N + k);
+    const double v3 = load_table(tab, (size_t)r.w * N + k);
+    const double lo = v0 + (v1 - v0) * w.x;
+    const double hi = v2 + (v3 - v2) * w.y;
+    const double x = lo + (hi - lo) * t.x;
+    kap += exp10(x) * t.y;
+  }
+  return kap;
+}
+
+// Fused opacity assembly + two-stream short characteristics, one thread per
+// wavenumber (ShortCharacteristics::calcSpectrum
+// src/radiative_transfer/short_characteristics.cpp:39-125; Planck function
+// src/additional/aux_functions.cpp:272-278). Writes the flux in W m^-2 cm
+// times the radius-distance scaling.
+template <typename TT>
+__global__ void __launch_bounds__(256) emission_kernel(DeviceModel dm, const TT* __restrict__ tab,
+                                                       const LevelInfo* __restrict__ lev,
+                                                       const LevelSpecies* __restrict__ ls,
+                                                       const EvalInfo* __restrict__ ev,
+                                                       double* __restrict__ spectrum) {
+  const int b = blockIdx.x;
+  const int k = blockIdx.y * blockDim.x + threadIdx.x;
+  if (k >= dm.N) return;
+  const int L = dm.L, S = dm.S;
+  const size_t N = dm.N;
+  const LevelInfo* lv = lev + (size_t)b * L;
+  const LevelSpecies* sp = ls + (size_t)b * L * S;
+  const double c1 = dm.planck_c1[k], c2 = dm.planck_c2[k];
+
+  double kap_prev = level_absorption(tab, N, sp, S, k);
+  double B_prev = c1 / (exp(c2 * __ldg(&lv[0].invT)) - 1.0);
+  double I1 = B_prev, I2 = B_prev;
+  for (int l = 1; l < L; ++l) {
+    const double kap = level_absorption(tab, N, sp + (size_t)l * S, S, k);
+    const double B = c1 / (exp(c2 * __ldg(&lv[l].invT)) - 1.0);
+    const double tau = __ldg(&lv[l - 1].dz) * (kap + kap_prev) / 2. + __ldg(&lv[l - 1].cloud);
+    if (tau != 0) {
+      const double rtau = 1.0 / tau;
+      {
+        const double d = tau * kInvMu[0];
+        const double a = exp(-d);
+        const double q = (a - 1.0) * (kMu[0] * rtau);
+        I1 = I1 * a;
+        I1 += (1.0 + q) * B + (-a - q) * B_prev;
+      }
+      {
+        const double d = tau * kInvMu[1];
+        const double a = exp(-d);
+        const double q = (a - 1.0) * (kMu[1] * rtau);
+        I2 = I2 * a;
+        I2 += (1.0 + q) * B + (-a - q) * B_prev;
+      }
+    }
+    kap_prev = kap;
+    B_prev = B;
+  }
+  const double flux = 2.0 * kPi * (I1 * kMu[0] * 0.5 + I2 * kMu[1] * 0.5) * 1e-3;
+  spectrum[(size_t)b * N + k] = flux * __ldg(&ev[b].scaling);
+}
+
+// Tangent-ray path lengths of every evaluation: geom[b][t][i] for t <= i < L-1 is
+// sqrt((R+z_{i+1})^2 - (R+z_t)^2) - sqrt((R+z_i)^2 - (R+z_t)^2)
+// (TransmissionModel::distanceToTangentCenter src/forward_model/transmission/
+// transmission_spectrum.cpp:145-154). Squares are rounded separately so the
+// tangent level gives exactly zero.
+__global__ void transmission_geometry_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
+                                             const EvalInfo* __restrict__ ev, double* __restrict__ geom) {
+  const int b = blockIdx.x;
+  const int L = dm.L;
+  const LevelInfo* lv = lev + (size_t)b * L;
+  const double R = ev[b].radius;
+  for (int idx = threadIdx.x; idx < L * L; idx += blockDim.x) {
+    const int t = idx / L, i = idx % L;
+    double v = 0.0;
+    if (i >= t && i < L - 1) {
+      const double bt = R + lv[t].z;
+      const double a1 = R + lv[i + 1].z;
+      const double a0 = R + lv[i].z;
+      const double bb = __dmul_rn(bt, bt);
+      v = sqrt(__dsub_rn(__dmul_rn(a1, a1), bb)) - sqrt(__dsub_rn(__dmul_rn(a0, a0), bb));
+    }
+    geom[(size_t)b * L * L + idx] = v;
+  }
+}
+
+// Transit depth per wavenumber (TransmissionModel::calcTransmissionSpectrum ...
+// tangentOpticalDepth src/forward_model/transmission/transmission_spectrum.cpp:32-141).
+// Extinction of every level is staged in shared memory [L][blockDim]; the tangent
+// sums run in FP64 with the reference's tau > 10 cut-off.
+template <typename TT>
+__global__ void __launch_bounds__(128) transmission_kernel(DeviceModel dm, const TT* __restrict__ tab,
+                                                           const LevelInfo* __restrict__ lev,
+                                                           const LevelSpecies* __restrict__ ls,
+                                                           const double* __restrict__ ray_n,
+                                                           const EvalInfo* __restrict__ ev,
+                                                           const double* __restrict__ geom,
+                                                           double* __restrict__ spectrum) {
+  extern __shared__ double chi_s[];
+  const int b = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int k = blockIdx.y * blockDim.x + tid;
+  const int L = dm.L, S = dm.S, R = dm.R;
+  const size_t N = dm.N;
+  const bool active = k < dm.N;
+  const LevelInfo* lv = lev + (size_t)b * L;
+  const LevelSpecies* sp = ls + (size_t)b * L * S;
+  const int TB = blockDim.x;
+  if (active) {
+    for (int l = 0; l < L; ++l) {
+      const double a = level_absorption(tab, N, sp + (size_t)l * S, S, k);
+      double sc = 0.0;
+      for (int r = 0; r < R; ++r) sc += __ldg(&dm.rayleigh[(size_t)r * N + k]) * __ldg(&ray_n[((size_t)b * L + l) * R + r]);
+      chi_s[l * TB + tid] = a + sc + __ldg(&lv[l].cloud);
+    }
+  }
+  if (!active) return;
+  const double Rp = ev[b].radius, Rs = ev[b].star_radius;
+  const double* G = geom + (size_t)b * L * L;
+  // integrateEffectiveTangentHeight :59-77 accumulated from the top down
+  double h = 0.0;
+  double tr_up = 1.0;  // transmission of level t+1; the top level is transparent
+  for (int t = L - 2; t >= 0; --t) {
+    double tau = 0.0;
+    const double* Gt = G + (size_t)t * L;
+    for (int i = t; i < L - 1; ++i) {
+      tau += __ldg(&Gt[i]) * (chi_s[i * TB + tid] + chi_s[(i + 1) * TB + tid]);
+      if (tau > 10.0) break;
+    }
+    const double tr = exp(-tau);
+    const double zt = __ldg(&lv[t].z), zu = __ldg(&lv[t + 1].z);
+    h += 2. * ((Rp + zt) * (1. - tr) + (Rp + zu) * (1. - tr_up)) * (zu - zt) * 0.5;
+    tr_up = tr;
+  }
+  h = sqrt(h + Rp * Rp) - Rp;
+  const double rp = h + Rp;
+  spectrum[(size_t)b * N + k] = rp * rp / Rs / Rs * 1e6;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Observation operator and Gaussian log-likelihood, one block per evaluation
+// (Observation::processModelSpectrum src/observations/observations.cpp:290-304,
+// ForwardModel::applyObservationModifier src/forward_model/forward_model.cpp:161-180,
+// Retrieval::logLikelihood src/retrieval/retrieval.cpp:314-369).
+__global__ void obs_loglike_kernel(DeviceModel dm, const double* __restrict__ spectrum,
+                                   const double* __restrict__ params, int P,
+                                   const EvalInfo* __restrict__ ev, double* __restrict__ obs,
+                                   double* __restrict__ loglike, uint8_t* __restrict__ neglect_out) {
+  const int b = blockIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const double* F = spectrum + (size_t)b * dm.N;
+  const double infl = ev[b].inflation;
+  double acc = 0.0;
+  for (int r = warp; r < dm.M; r += nw) {
+    const int k0 = __ldg(&dm.row_k0[r]), len = __ldg(&dm.row_len[r]);
+    const double* w = dm.W + __ldg(&dm.row_off[r]);
+    double s = 0.0;
+    for (int j = lane; j < len; j += 32) s += __ldg(&w[j]) * F[k0 + j];
+    s = warp_sum(s);
+    if (lane == 0) {
+      const int mp = __ldg(&dm.obs_mod_param[__ldg(&dm.row_obs[r])]);
+      if (mp >= 0) {
+        const double shift = params[(size_t)b * P + mp];
+        if (shift != 0) s += shift;
+      }
+      if (obs) obs[(size_t)b * dm.M + r] = s;
+      const double es = __ldg(&dm.row_err2[r]) + infl;
+      const double d = __ldg(&dm.row_data[r]) - s;
+      const double lt = (infl == 0.0) ? __ldg(&dm.row_logterm[r]) : -0.5 * log(es * 2.0 * kPi);
+      acc += (lt - 0.5 * d * d / es) * __ldg(&dm.row_weight[r]);
+    }
+  }
+  __shared__ double red[32];
+  if (lane == 0) red[warp] = acc;
+  __syncthreads();
+  if (warp == 0) {
+    double v = lane < nw ? red[lane] : 0.0;
+    v = warp_sum(v);
+    if (lane == 0) {
+      const int ng = ev[b].neglect;
+      if (loglike) loglike[b] = ng ? -1e30 : v;
+      if (neglect_out) neglect_out[b] = (uint8_t)ng;
+    }
+  }
+}
+
+// High-resolution output of the plain path (RadiativeTransfer::changeSpectrumUnits
+// src/radiative_transfer/radiative_transfer.h:58-60 for emission; transit depth as is).
+__global__ void spectrum_output_kernel(DeviceModel dm, const double* __restrict__ spectrum,
+                                       int emission, double* __restrict__ out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= dm.N) return;
+  const double f = spectrum[k];
+  out[k] = emission ? f / dm.wl[k] / dm.wl[k] * 10000.0 : f;
+}
+
+// ------------------------------------------------------------------ host side
+template <typename T>
+static T* dev_upload(Model& m, const std::vector<T>& v) {
+  T* p = nullptr;
+  const size_t bytes = std::max<size_t>(v.size(), 1) * sizeof(T);
+  BGB_CUDA(cudaMalloc(&p, bytes));
+  if (!v.empty()) BGB_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  m.allocations.push_back(p);
+  m.device_bytes += bytes;
+  return p;
+}
+
+void upload_model(Model& m) {
+  BGB_CUDA(cudaSetDevice(m.device));
+  const size_t N = m.N;
+  DeviceModel& dm = m.dm;
+  dm.L = m.L;
+  dm.S = m.acfg.S;
+  dm.R = m.acfg.R;
+  dm.N = (int)N;
+  dm.M = m.M;
+  dm.P = m.acfg.nparam_total;
+  dm.nobs = (int)m.obs.size();
+  std::vector<double> c1(N), c2(N);
+  for (size_t k = 0; k < N; ++k) {
+    const double nu = m.nu[k];
+    c1[k] = 2. * kPlanckH * kLightC * kLightC * nu * nu * nu;
+    c2[k] = kPlanckH * nu * kLightC / kBoltzmann;
+  }
+  dm.nu = dev_upload(m, m.nu);
+  dm.wl = dev_upload(m, m.wl);
+  dm.planck_c1 = dev_upload(m, c1);
+  dm.planck_c2 = dev_upload(m, c2);
+  dm.pressure = dev_upload(m, m.p);
+  dm.log10p = dev_upload(m, m.log10p);
+  m.d_table64 = dev_upload(m, m.table_host);
+  dm.table64 = m.d_table64;
+  {
+    std::vector<float> t32(m.table_host.size());
+    for (size_t i = 0; i < t32.size(); ++i) t32[i] = (float)m.table_host[i];
+    m.d_table32 = dev_upload(m, t32);
+    dm.table32 = m.d_table32;
+  }
+  std::vector<double>().swap(m.table_host);
+  dm.table_T = dev_upload(m, m.table_T);
+  dm.pb_row0 = dev_upload(m, m.pb_row0);
+  dm.pb_row1 = dev_upload(m, m.pb_row1);
+  dm.pb_w = dev_upload(m, m.pb_w);
+  std::vector<double> ray;
+  for (int r : m.rayleigh_species) ray.insert(ray.end(), m.opac[r].rayleigh.begin(), m.opac[r].rayleigh.end());
+  dm.rayleigh = dev_upload(m, ray);
+  // observation operator rows in internal order, observations concatenated
+  std::vector<int> k0, len, robs, rout, modp;
+  std::vector<long long> off;
+  std::vector<double> data, err2, wgt, logt;
+  int pidx = m.nparam_general + m.nparam_chem + m.nparam_temp + m.nparam_cloud;
+  for (size_t o = 0; o < m.obs.size(); ++o) {
+    const ObservationSetup& ob = m.obs[o];
+    modp.push_back(ob.nb_modifier ? pidx : -1);
+    pidx += ob.nb_modifier;
+    for (int j = 0; j < ob.n; ++j) {
+      k0.push_back(ob.row_k0[j]);
+      len.push_back(ob.row_len[j]);
+      off.push_back(ob.row_off[j]);
+      robs.push_back((int)o);
+      rout.push_back(ob.out_offset + (ob.ascending ? ob.n - 1 - j : j));
+      data.push_back(ob.data[j]);
+      const double es = ob.error[j] * ob.error[j];
+      err2.push_back(es);
+      wgt.push_back(ob.weight[j]);
+      logt.push_back(-0.5 * std::log(es * 2.0 * kPi));
+    }
+  }
+  dm.row_k0 = dev_upload(m, k0);
+  dm.row_len = dev_upload(m, len);
+  dm.row_off = dev_upload(m, off);
+  dm.W = dev_upload(m, m.W);
+  dm.row_obs = dev_upload(m, robs);
+  dm.row_out = dev_upload(m, rout);
+  dm.row_data = dev_upload(m, data);
+  dm.row_err2 = dev_upload(m, err2);
+  dm.row_weight = dev_upload(m, wgt);
+  dm.row_logterm = dev_upload(m, logt);
+  dm.obs_mod_param = dev_upload(m, modp);
+  std::vector<AtmosphereConfig> cfg{m.acfg};
+  m.d_cfg = dev_upload(m, cfg);
+  dm.cfg = m.d_cfg;
+  BGB_CUDA(cudaMallocHost(&m.h_pinned, 64 * 1024));
+  m.h_pinned_bytes = 64 * 1024;
+}
+
+static void free_workspace(Workspace& w) {
+  cudaFree(w.params);
+  cudaFree(w.lev);
+  cudaFree(w.ls);
+  cudaFree(w.ev);
+  cudaFree(w.spectrum);
+  cudaFree(w.obs);
+  cudaFree(w.loglike);
+  cudaFree(w.geom);
+  cudaFree(w.g_spectrum);
+  cudaFree(w.g_level);
+  cudaFree(w.g_geom);
+  w = Workspace{};
+}
+
+static double* g_ray_n_dummy = nullptr;
+
+void ensure_workspace(Model& m, int batch) {
+  if (batch <= m.ws.capacity) return;
+  BGB_CUDA(cudaSetDevice(m.device));
+  BGB_CUDA(cudaDeviceSynchronize());
+  free_workspace(m.ws);
+  Workspace& w = m.ws;
+  const size_t B = batch, L = m.L, S = std::max(m.acfg.S, 1), N = m.N, M = std::max(m.M, 1);
+  const size_t P = std::max(m.acfg.nparam_total, 1);
+  const size_t R = std::max(m.acfg.R, 1);
+  BGB_CUDA(cudaMalloc(&w.params, B * P * sizeof(double)));
+  BGB_CUDA(cudaMalloc(&w.lev, B * L * sizeof(LevelInfo)));
+  BGB_CUDA(cudaMalloc(&w.ls, B * L * S * sizeof(LevelSpecies) + B * L * R * sizeof(double)));
+  BGB_CUDA(cudaMalloc(&w.ev, B * sizeof(EvalInfo)));
+  BGB_CUDA(cudaMalloc(&w.spectrum, B * N * sizeof(double)));
+  BGB_CUDA(cudaMalloc(&w.obs, B * M * sizeof(double)));
+  BGB_CUDA(cudaMalloc(&w.loglike, B * sizeof(double)));
+  if (m.transmission) BGB_CUDA(cudaMalloc(&w.geom, B * L * L * sizeof(double)));
+  w.capacity = batch;
+}
+
+static inline double* ray_n_ptr(Model& m) {
+  const size_t B = m.ws.capacity, L = m.L, S = std::max(m.acfg.S, 1);
+  return reinterpret_cast<double*>(m.ws.ls + B * L * S);
+}
+
+void launch_forward(Model& m, const double* params_dev, int batch, cudaStream_t st,
+                    bool want_loglike, uint8_t* neglect_dev, double* loglike_dev) {
+  ensure_workspace(m, batch);
+  const DeviceModel& dm = m.dm;
+  Workspace& w = m.ws;
+  const int L = m.L;
+  const int atm_threads = ((L + 31) / 32) * 32;
+  atmosphere_kernel<<<batch, atm_threads, 4 * L * sizeof(double), st>>>(
+      dm, params_dev, dm.P, w.lev, w.ls, ray_n_ptr(m), w.ev);
+  BGB_CUDA(cudaGetLastError());
+  if (!m.transmission) {
+    const int TB = m.rt_threads > 0 ? m.rt_threads : (batch == 1 ? 64 : 128);
+    dim3 grid(batch, (dm.N + TB - 1) / TB);
+    if (m.fp32_tables && batch > 1)
+      emission_kernel<float><<<grid, TB, 0, st>>>(dm, dm.table32, w.lev, w.ls, w.ev, w.spectrum);
+    else
+      emission_kernel<double><<<grid, TB, 0, st>>>(dm, dm.table64, w.lev, w.ls, w.ev, w.spectrum);
+  } else {
+    transmission_geometry_kernel<<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom);
+    const int TB = m.rt_threads > 0 ? std::min(m.rt_threads, 128) : 64;
+    dim3 grid(batch, (dm.N + TB - 1) / TB);
+    const size_t sm = (size_t)L * TB * sizeof(double);
+    if (m.fp32_tables && batch > 1) {
+      BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      transmission_kernel<float><<<grid, TB, sm, st>>>(dm, dm.table32, w.lev, w.ls, ray_n_ptr(m), w.ev, w.geom, w.spectrum);
+    } else {
+      BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      transmission_kernel<double><<<grid, TB, sm, st>>>(dm, dm.table64, w.lev, w.ls, ray_n_ptr(m), w.ev, w.geom, w.spectrum);
+    }
+  }
+  BGB_CUDA(cudaGetLastError());
+  const int OT = m.obs_threads > 0 ? m.obs_threads : 256;
+  obs_loglike_kernel<<<batch, OT, 0, st>>>(dm, w.spectrum, params_dev, dm.P, w.ev, w.obs,
+                                          want_loglike ? (loglike_dev ? loglike_dev : w.loglike) : nullptr,
+                                          neglect_dev);
+  BGB_CUDA(cudaGetLastError());
+}
+
+void launch_spectrum_output(Model& m, double* out_dev, cudaStream_t st) {
+  spectrum_output_kernel<<<(m.dm.N + 255) / 256, 256, 0, st>>>(m.dm, m.ws.spectrum, m.transmission ? 0 : 1, out_dev);
+  BGB_CUDA(cudaGetLastError());
+}
+
+void release_model(Model& m) {
+  cudaSetDevice(m.device);
+  cudaDeviceSynchronize();
+  free_workspace(m.ws);
+  for (void* p : m.allocations) cudaFree(p);
+  m.allocations.clear();
+  if (m.h_pinned) cudaFreeHost(m.h_pinned);
+  m.h_pinned = nullptr;
+  (void)g_ray_n_dummy;
+}
+
+}  // namespace bgb

@@ -1,0 +1,282 @@
+// Internal declarations of the GB300 likelihood engine (host set-up + device
+// kernels). The public boundary is include/bear_gb300.h.
+#pragma once
+
+#include <array>
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+namespace bgb {
+
+// ----------------------------------------------------------------- constants
+// Physical constants in cgs units, src/additional/physical_const.h:28-52.
+constexpr double kPlanckH = 6.62606896e-27;
+constexpr double kLightC = 2.99792458e10;
+constexpr double kBoltzmann = 1.3806504e-16;
+constexpr double kGravConst = 6.673e-8;
+constexpr double kGasConst = 8.314472e7;
+constexpr double kRJupiter = 7.1492e9;
+constexpr double kPi = 3.14159265358979323846;
+
+// Chemical species table, src/chemistry/chem_species.h:30-90. The id order is
+// significant: the mean molecular weight is summed over it in this order.
+constexpr int kSpeciesCount = 46;
+enum SpeciesId : int {
+  SP_TOTAL = 0, SP_H = 1, SP_He = 2, SP_H2 = 10, SP_Na = 19, SP_K = 20, SP_e = 35
+};
+extern const char* const kSpeciesSymbol[kSpeciesCount];
+extern const double kSpeciesMolWeight[kSpeciesCount];
+int species_id(const std::string& symbol);
+
+constexpr int kMaxLevels = 512;
+constexpr int kMaxChemModules = 4;
+constexpr int kMaxTableSpecies = 32;
+constexpr int kMaxRayleigh = 8;
+constexpr int kMaxPolyDof = 64;
+
+// ----------------------------------------------------------------- device-side model description
+// Everything the per-evaluation kernels need that does not depend on the
+// parameters. Lives in device memory; kernels receive a pointer.
+struct AtmosphereConfig {
+  int L;                       // levels, index 0 = bottom (highest pressure)
+  int transmission;            // 0 emission, 1 transmission
+  int nparam_general, nparam_chem, nparam_temp, nparam_cloud, nparam_mod, nparam_total;
+  int error_inflation;
+  // temperature: 0 const, 1 piecewise polynomial in log10 p
+  int temp_poly, pp_nel, pp_ndof_el, pp_ndof;
+  double pp_ref[8];
+  double pp_dof_vertices[kMaxPolyDof];
+  double pp_el_vert[kMaxPolyDof * 8];
+  // chemistry modules applied in order
+  int nchem;
+  int chem_kind[kMaxChemModules];     // 0 isoprofile, 1 background
+  int chem_nsp[kMaxChemModules];
+  int chem_sp[kMaxChemModules][kSpeciesCount];
+  int chem_na_free[kMaxChemModules];
+  int chem_bg_h2he[kMaxChemModules];
+  int chem_bg_sp[kMaxChemModules];
+  // grey cloud
+  int cloud, cloud_fb;
+  // transmission options
+  int fit_mmw, var_g;
+  // opacity species with tables (line lists and CIA)
+  int S;
+  int sp_index[kMaxTableSpecies];
+  int sp_partner[kMaxTableSpecies][2];  // -1 if unused
+  int sp_nT[kMaxTableSpecies];
+  int sp_T_off[kMaxTableSpecies];       // offset into table_T
+  int sp_pb_off[kMaxTableSpecies];      // offset into pb_* arrays: [t][level]
+  // Rayleigh species
+  int R;
+  int ray_index[kMaxRayleigh];
+};
+
+// Per (evaluation, level, table species): the four table rows of the
+// interpolation stencil and its weights, plus the species' number density
+// (product with collision partners for CIA).
+struct __align__(16) LevelSpecies {
+  int row[4];      // (T_lo, p_lo), (T_lo, p_hi), (T_hi, p_lo), (T_hi, p_hi): absolute row numbers
+  double wp_lo;    // log-p weight on the T_lo rows
+  double wp_hi;    // log-p weight on the T_hi rows
+  double wT;       // temperature weight
+  double n;        // number density (cm^-3, or cm^-6 for CIA pairs)
+};
+
+// Per (evaluation, level).
+struct __align__(16) LevelInfo {
+  double T;        // temperature
+  double invT;     // 1 / T
+  double z;        // altitude (cm)
+  double dz;       // z[l+1] - z[l] (0 on the top level)
+  double cloud;    // emission: grey-cloud optical depth of layer l; transmission: cloud extinction at level l
+  double pad;
+};
+
+// Per evaluation.
+struct __align__(16) EvalInfo {
+  double scaling;      // emission: (R_J / d)^2 f
+  double radius;       // transmission: bottom (planet) radius
+  double star_radius;  // transmission: stellar radius
+  double inflation;    // 10^b error inflation (0 if off)
+  int neglect;
+  int cloud_top, cloud_bottom;
+  int pad;
+};
+
+// Device pointers and sizes for the kernels (passed by value).
+struct DeviceModel {
+  const AtmosphereConfig* cfg;
+  int L, S, R, N, M, P, nobs;
+  // grid
+  const double* nu;           // N
+  const double* wl;           // N
+  const double* planck_c1;    // N: 2 h c^2 nu^3
+  const double* planck_c2;    // N: h nu c / k
+  // atmosphere constants
+  const double* pressure;     // L (bar)
+  const double* log10p;       // L
+  // tables
+  const double* table64;      // rows x N, log10 cross sections
+  const float* table32;       // rows x N (optional)
+  const double* table_T;      // all species' temperature nodes
+  const int* pb_row0;         // per species [nT][L]: absolute row of the lower pressure node
+  const int* pb_row1;         // upper pressure node
+  const double* pb_w;         // log-p weight
+  const double* rayleigh;     // R x N
+  // observation operator: M rows, internal (descending-wavelength) order
+  const int* row_k0;
+  const int* row_len;
+  const long long* row_off;
+  const double* W;
+  const int* row_obs;
+  const int* row_out;         // index in the caller-order output
+  const double* row_data;
+  const double* row_err2;
+  const double* row_weight;
+  const double* row_logterm;  // -0.5 log(2 pi sigma^2) (no inflation)
+  const int* obs_mod_param;   // per observation: parameter index of the shift, or -1
+};
+
+// Work buffers for a batch of evaluations.
+struct Workspace {
+  int capacity = 0;
+  double* params = nullptr;    // B x P (plain path staging)
+  LevelInfo* lev = nullptr;    // B x L
+  LevelSpecies* ls = nullptr;  // B x L x S
+  EvalInfo* ev = nullptr;      // B
+  double* spectrum = nullptr;  // B x N native units
+  double* obs = nullptr;       // B x M internal order
+  double* loglike = nullptr;   // B
+  double* geom = nullptr;      // transmission path lengths B x L x L
+  // adjoint
+  double* g_spectrum = nullptr;  // B x N adjoint of the spectrum
+  double* g_level = nullptr;     // B x L x (S + 4) accumulated adjoints
+  double* g_geom = nullptr;      // B x L x L
+};
+
+// ----------------------------------------------------------------- host model
+struct ObservationSetup {
+  std::string name;
+  int type = 0;  // 0 spectroscopy, 1 photometry, 2 band-spectroscopy
+  int n = 0;
+  bool ascending = false;
+  int nb_modifier = 0;
+  int out_offset = 0;   // offset in the concatenated outputs
+  std::vector<double> data, error, weight, fwhm, centers;
+  std::vector<std::array<double, 2>> edges, edge_nu;
+  double wl_edges[2] = {0, 0};
+  double obs_nu_range[2] = {0, 0};
+  size_t range_lo = 0, range_hi = 0;
+  std::vector<std::array<size_t, 2>> edge_idx;
+  bool has_profile = false;
+  std::vector<double> sigma;
+  std::vector<std::array<size_t, 2>> conv;
+  int nfilter = 0;
+  bool photon = false;
+  std::vector<double> filter_wl, filter_resp, filter_grid, filter_weight;
+  double filter_norm = 0;
+  // composite operator rows (internal order)
+  std::vector<int> row_k0, row_len;
+  std::vector<long long> row_off;
+};
+
+struct OpacitySpecies {
+  int kind = 0;  // 0 tabulated (line list / CIA), 1 Rayleigh only
+  int index = 0;
+  std::vector<int> partners;
+  double mass = 0;
+  std::vector<double> T;                    // ascending
+  std::vector<std::vector<double>> P, logP; // per T, ascending
+  std::vector<std::vector<int>> row;        // absolute packed row per (t, q)
+  std::vector<double> rayleigh;             // N (kind 1)
+};
+
+struct ChemModule {
+  int kind = 0;  // 0 iso, 1 background
+  std::vector<int> sp;
+  bool na_free = false;
+  bool bg_h2he = false;
+  int bg_sp = -1;
+};
+
+struct Model {
+  // configuration
+  bool transmission = false;
+  std::string xsec_path, wn_file;
+  int discretisation = 0;
+  double resolution = 1.0;
+  bool error_inflation = false;
+  int L = 0;
+  double pbot = 0, ptop = 0;
+  bool temp_poly = false;
+  int poly_elements = 0, poly_order = 0;
+  std::vector<ChemModule> chem;
+  bool cloud = false, cloud_fb = false;
+  bool fit_mmw = false, fit_sh = false, var_g = false;
+  std::vector<std::pair<std::string, std::string>> opac_cfg;
+  // set-up products
+  std::vector<ObservationSetup> obs;
+  std::vector<double> nu_full, wl_full;
+  std::vector<size_t> index_list;
+  std::vector<double> nu, wl;
+  size_t N = 0;
+  std::vector<double> p, log10p;
+  std::vector<OpacitySpecies> opac;  // config order
+  std::vector<int> table_species;    // indices into opac with kind 0
+  std::vector<int> rayleigh_species; // indices into opac with kind 1
+  long long n_rows = 0;
+  std::vector<double> table_host;    // n_rows x N (freed after upload)
+  std::vector<double> W;             // concatenated operator weights
+  int M = 0;
+  int nparam_general = 0, nparam_chem = 0, nparam_temp = 0, nparam_cloud = 0, nparam_mod = 0;
+  int nparam_total = 0;
+  AtmosphereConfig acfg{};
+  std::vector<int> pb_row0, pb_row1;
+  std::vector<double> pb_w, table_T;
+  bool prepared = false;
+  bool finalized = false;
+  // device
+  int device = 0;
+  bool fp32_tables = false;
+  int rt_threads = 0, obs_threads = 0;
+  DeviceModel dm{};
+  std::vector<void*> allocations;
+  size_t device_bytes = 0;
+  AtmosphereConfig* d_cfg = nullptr;
+  double* d_table64 = nullptr;
+  float* d_table32 = nullptr;
+  Workspace ws;
+  double* h_pinned = nullptr;  // pinned staging for the plain path
+  size_t h_pinned_bytes = 0;
+};
+
+// model_setup.cpp
+void parse_config(Model& m, const std::string& text);
+void add_observation(Model& m, const char* name, const char* type, int n, const double* ce,
+                     const double* data, const double* error, const double* weight,
+                     const double* fwhm, int nfilter, const double* fwl, const double* fresp,
+                     const char* detector, const char* modifier);
+void finalize_host(Model& m);
+
+// engine.cu
+void upload_model(Model& m);
+void ensure_workspace(Model& m, int batch);
+void release_model(Model& m);
+void launch_forward(Model& m, const double* params_dev, int batch, cudaStream_t stream,
+                    bool want_loglike, uint8_t* neglect_dev, double* loglike_dev);
+void launch_spectrum_output(Model& m, double* out_dev, cudaStream_t stream);
+void launch_gradient(Model& m, const double* params_dev, int batch, cudaStream_t stream,
+                     double* loglike_dev, double* grad_dev, uint8_t* neglect_dev);
+
+struct Error : std::exception {
+  int code;
+  std::string msg;
+  Error(int c, std::string s) : code(c), msg(std::move(s)) {}
+  const char* what() const noexcept override { return msg.c_str(); }
+};
+
+}  // namespace bgb

@@ -1,0 +1,806 @@
+// Host-side set-up of the likelihood engine: configuration, spectral grid,
+// observation operators, opacity tables. Everything here is evaluated once per
+// model; the per-evaluation work runs on the GPU (engine.cu).
+//
+// The integer decisions (grid points, band-edge indices, convolution windows,
+// table brackets) must match the reference exactly, so this file is compiled
+// without FMA contraction and follows the reference's operation order.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+
+#include "../../include/bear_gb300.h"
+#include "model.h"
+
+namespace bgb {
+
+const char* const kSpeciesSymbol[kSpeciesCount] = {
+    "Total", "H",   "He",  "C",    "O",   "Fe",  "Fe+", "Ca",  "Ti",   "Ti+", "H2",  "H2O",
+    "CO2",   "CO",  "CH4", "HCN",  "NH3", "C2H2", "N2", "Na",  "K",    "H2S", "H-",  "TiO",
+    "VO",    "FeH", "SH",  "MgO",  "AlO", "CaO", "CrH", "MgH", "CaH",  "TiH", "OH",  "e-",
+    "V",     "V+",  "Mn",  "Si",   "Cr",  "Cr+", "SiO", "SiO2", "SO2", "CS2"};
+const double kSpeciesMolWeight[kSpeciesCount] = {
+    0.0,      1.00784, 4.002602, 12.0107, 15.999,   55.845,   55.845,  40.078,  47.867,
+    47.867,   2.01588, 18.01528, 44.01,   28.0101,  16.04246, 27.0253, 17.03052, 26.04,
+    28.0134,  22.98977, 39.0983, 34.09099, 1.00784, 63.8664,  66.9409, 56.853,  34.08,
+    40.3044,  42.981,  56.0774,  54.0040, 26.3209,  41.0859,  48.87484, 17.008,
+    5.4857990907e-4, 50.9415, 50.9415, 54.938044, 28.085, 51.996, 51.996, 44.08, 60.08,
+    64.066,   76.139};
+
+int species_id(const std::string& s) {
+  for (int i = 0; i < kSpeciesCount; ++i)
+    if (s == kSpeciesSymbol[i]) return i;
+  return -1;
+}
+
+static Error invalid(const std::string& s) { return Error(BEAR_ERR_INVALID_INPUT, s); }
+static Error unsupported(const std::string& s) { return Error(BEAR_ERR_UNSUPPORTED, s); }
+
+// ------------------------------------------------------------------ config text
+void parse_config(Model& m, const std::string& text) {
+  std::istringstream in(text);
+  std::string line;
+  while (std::getline(in, line)) {
+    std::istringstream ls(line);
+    std::vector<std::string> t;
+    std::string w;
+    while (ls >> w) t.push_back(w);
+    if (t.empty() || t[0][0] == '#') continue;
+    const std::string& k = t[0];
+    auto need = [&](size_t n) {
+      if (t.size() < n) throw invalid("config line '" + line + "' is incomplete");
+    };
+    if (k == "forward_model") {
+      need(2);
+      if (t[1] == "emission") m.transmission = false;
+      else if (t[1] == "transmission") m.transmission = true;
+      else throw unsupported("forward model " + t[1] + " is not supported (emission, transmission)");
+    } else if (k == "cross_section_path") {
+      m.xsec_path = t.size() > 1 ? t[1] : "";
+    } else if (k == "wavenumber_file") {
+      m.wn_file = t.size() > 1 ? t[1] : "";
+    } else if (k == "spectral_discretisation") {
+      need(2);
+      // GlobalConfig::GlobalConfig src/config/global_config.cpp:37-74
+      if (t[1] == "const_wavenumber") m.discretisation = 0;
+      else if (t[1] == "const_wavelength") m.discretisation = 1;
+      else if (t[1] == "const_resolution") m.discretisation = 2;
+      else throw invalid("Spectral discretisation parameter: " + t[1] + " unknown!");
+    } else if (k == "spectral_resolution") {
+      need(2);
+      m.resolution = std::stod(t[1]);
+    } else if (k == "error_inflation") {
+      need(2);
+      m.error_inflation = std::stoi(t[1]) != 0;
+    } else if (k == "nb_grid_points") {
+      need(2);
+      m.L = std::stoi(t[1]);
+    } else if (k == "atmos_boundaries") {
+      need(3);
+      m.pbot = std::stod(t[1]);
+      m.ptop = std::stod(t[2]);
+    } else if (k == "temperature_profile") {
+      need(2);
+      // selectTemperatureProfile src/temperature/select_temperature_profile.h:52-161
+      if (t[1] == "poly") {
+        if (t.size() != 4) throw invalid("Piesewise polynomial temperature profile requires exactly two parameters!");
+        m.temp_poly = true;
+        m.poly_elements = std::stoi(t[2]);
+        m.poly_order = std::stoi(t[3]);
+        if (m.poly_order > 6) throw invalid("Piecewise polynomials are only available up to 6th order");
+      } else if (t[1] == "const") {
+        m.temp_poly = false;
+      } else {
+        throw unsupported("temperature profile " + t[1] + " is not supported (poly, const)");
+      }
+    } else if (k == "radiative_transfer") {
+      need(2);
+      if (t[1] != "scm") throw unsupported("radiative transfer " + t[1] + " is not supported (scm)");
+    } else if (k == "chemistry") {
+      need(2);
+      ChemModule c;
+      if (t[1] == "iso" || t[1] == "isoprofile") {
+        // IsoprofileChemistry::IsoprofileChemistry src/chemistry/isoprofile_chemistry.cpp:30-84
+        c.kind = 0;
+        for (size_t i = 2; i < t.size(); ++i) {
+          int id = species_id(t[i]);
+          if (id < 0) throw invalid("Chemical species " + t[i] + " not found in the list of species");
+          c.sp.push_back(id);
+          if (id == SP_Na) c.na_free = true;
+        }
+      } else if (t[1] == "bg" || t[1] == "background") {
+        // BackgroundChemistry::BackgroundChemistry src/chemistry/background_chemistry.cpp:31-69
+        need(3);
+        c.kind = 1;
+        if (t[2] == "H2He") c.bg_h2he = true;
+        else {
+          c.bg_sp = species_id(t[2]);
+          if (c.bg_sp < 0) throw invalid("Chemical species " + t[2] + " not found in the list of species");
+        }
+      } else {
+        throw unsupported("chemistry " + t[1] + " is not supported (iso, bg)");
+      }
+      if (m.chem.size() >= (size_t)kMaxChemModules) throw unsupported("too many chemistry modules");
+      if (c.sp.size() > (size_t)kSpeciesCount) throw invalid("too many species in one chemistry module");
+      m.chem.push_back(c);
+    } else if (k == "cloud") {
+      need(2);
+      if (t[1] == "none") continue;
+      if (t[1] != "grey") throw unsupported("cloud model " + t[1] + " is not supported (grey)");
+      if (m.cloud) throw unsupported("only one cloud model is supported");
+      m.cloud = true;
+      m.cloud_fb = (t.size() == 3 && t[2] == "fb");
+    } else if (k == "opacity") {
+      need(2);
+      m.opac_cfg.emplace_back(t[1], t.size() > 2 ? t[2] : "");
+    } else if (k == "fit_mean_molecular_weight") {
+      need(2);
+      m.fit_mmw = std::stoi(t[1]) != 0;
+    } else if (k == "fit_scale_height") {
+      need(2);
+      m.fit_sh = std::stoi(t[1]) != 0;
+    } else if (k == "variable_gravity") {
+      need(2);
+      m.var_g = std::stoi(t[1]) != 0;
+    } else {
+      throw invalid("unknown config key " + k);
+    }
+  }
+  if (m.fit_sh) throw unsupported("fit_scale_height is not supported");
+  if (m.L < 2 || m.L > kMaxLevels) throw invalid("nb_grid_points must be in [2, 512]");
+  if (!(m.pbot > m.ptop) || !(m.ptop > 0)) throw invalid("atmos_boundaries must be bottom > top > 0");
+}
+
+static void reverse_vec(std::vector<double>& v) { std::reverse(v.begin(), v.end()); }
+
+// ------------------------------------------------------------------ observations
+// Observation::init(ObservationInput) src/observations/observations.cpp:42-111
+void add_observation(Model& m, const char* name, const char* type, int n, const double* ce,
+                     const double* data, const double* error, const double* weight,
+                     const double* fwhm, int nfilter, const double* fwl, const double* fresp,
+                     const char* detector, const char* modifier) {
+  if (m.prepared) throw Error(BEAR_ERR_STATE, "observations must be added before prepare / finalize");
+  if (n < 1) throw invalid("observation without data points");
+  ObservationSetup o;
+  o.name = name ? name : "";
+  std::string mod = modifier ? modifier : "";
+  // setSpectrumModifier :374-392
+  if (mod.empty() || mod == "none") o.nb_modifier = 0;
+  else if (mod == "shift_const") o.nb_modifier = 1;
+  else throw invalid("Observation modifier " + mod + " unknown.");
+  std::string ty = type ? type : "";
+  // selectBandType src/spectral_grid/spectral_band_type.h:49-80
+  if (ty == "spectroscopy" || ty == "Spectroscopy") o.type = 0;
+  else if (ty == "photometry" || ty == "Photometry") o.type = 1;
+  else if (ty == "band-spectroscopy" || ty == "Band-spectroscopy") o.type = 2;
+  else throw invalid("Unsupported band type *" + ty + "* for observation " + o.name);
+  o.n = n;
+  o.data.assign(data, data + n);
+  o.error.assign(error, error + n);
+  o.weight.assign(n, 1.0);
+  if (weight) o.weight.assign(weight, weight + n);
+  if (fwhm) o.fwhm.assign(fwhm, fwhm + n);
+  if (nfilter > 0) {
+    std::string det = detector ? detector : "";
+    if (det == "Energy") det = "energy";
+    if (det == "Photon") det = "photon";
+    if (det != "energy" && det != "photon") throw invalid("Unsupported detector type *" + det + "*");
+    o.photon = det == "photon";
+    o.nfilter = nfilter;
+    o.filter_wl.assign(fwl, fwl + nfilter);
+    o.filter_resp.assign(fresp, fresp + nfilter);
+    if (o.filter_wl.front() < o.filter_wl.back()) {
+      reverse_vec(o.filter_wl);
+      reverse_vec(o.filter_resp);
+    }
+  }
+  o.edges.resize(n);
+  o.centers.resize(n);
+  if (o.type == 0) {
+    std::vector<double> wl(ce, ce + n);
+    // areWavelengthsAscending(vector<double>) :127-151
+    o.ascending = false;
+    if (n > 1 && wl[0] < wl[1]) {
+      o.ascending = true;
+      reverse_vec(wl);
+      reverse_vec(o.data);
+      reverse_vec(o.error);
+      reverse_vec(o.fwhm);
+      reverse_vec(o.weight);
+    }
+    o.centers = wl;
+    // calcBinEdges :188-221
+    for (int i = 0; i < n; ++i) {
+      if (i == 0) {
+        if (n < 2) throw invalid("a spectroscopy observation needs at least two points");
+        o.edges[0][1] = wl[0] - (wl[i] - wl[i + 1]) * 0.5;
+        o.edges[0][0] = wl[0] + (wl[i] - wl[i + 1]) * 0.5;
+      } else if (i == n - 1) {
+        o.edges[n - 1][1] = wl[i] - (wl[i - 1] - wl[i]) * 0.5;
+        o.edges[n - 1][0] = wl[i] + (wl[i - 1] - wl[i]) * 0.5;
+      } else {
+        o.edges[i][0] = wl[i - 1] - (wl[i - 1] - wl[i]) * 0.5;
+        o.edges[i][1] = wl[i] - (wl[i] - wl[i + 1]) * 0.5;
+      }
+    }
+  } else {
+    for (int i = 0; i < n; ++i) o.edges[i] = {ce[2 * i], ce[2 * i + 1]};
+    // areWavelengthsAscending(vector<vector<double>>) :156-184
+    o.ascending = false;
+    if (n > 1 && o.edges.front()[0] < o.edges.back()[0]) {
+      o.ascending = true;
+      std::reverse(o.edges.begin(), o.edges.end());
+      reverse_vec(o.data);
+      reverse_vec(o.error);
+      reverse_vec(o.fwhm);
+      reverse_vec(o.weight);
+    }
+    for (auto& e : o.edges)
+      if (e[0] < e[1]) std::swap(e[0], e[1]);
+    // calcBinCenters :224-233
+    for (int i = 0; i < n; ++i) o.centers[i] = o.edges[i][0] - (o.edges[i][0] - o.edges[i][1]) * 0.5;
+  }
+  // setObservationEdges :237-251
+  if (!o.fwhm.empty()) {
+    o.wl_edges[0] = o.edges.front()[0] + 5.0 * o.fwhm.front() / 2.355;
+    o.wl_edges[1] = o.edges.back()[1] - 5.0 * o.fwhm.back() / 2.355;
+  } else {
+    o.wl_edges[0] = o.edges.front()[0];
+    o.wl_edges[1] = o.edges.back()[1];
+  }
+  // SpectralBands::init src/spectral_grid/spectral_band.cpp:38-63
+  o.edge_nu.resize(n);
+  for (int i = 0; i < n; ++i) o.edge_nu[i] = {1.0 / o.edges[i][0] * 1e4, 1.0 / o.edges[i][1] * 1e4};
+  o.obs_nu_range[0] = 1.0 / o.wl_edges[0] * 1e4;
+  o.obs_nu_range[1] = 1.0 / o.wl_edges[1] * 1e4;
+  m.obs.push_back(std::move(o));
+}
+
+// ------------------------------------------------------------------ spectral grid
+// SpectralGrid::findClosestIndex{,Asc,Desc} src/spectral_grid/spectral_grid.cpp:323-385.
+// Past the end the reference reads beyond its vector; the last index is used here.
+static size_t find_closest(double x, const std::vector<double>& d, size_t start) {
+  const size_t n = d.size();
+  if (n < 2) return 0;
+  size_t it;
+  if (d[0] < d[1]) it = std::lower_bound(d.begin() + start, d.end(), x) - d.begin();
+  else if (d[0] > d[1]) it = std::lower_bound(d.begin() + start, d.end(), x, std::greater<double>()) - d.begin();
+  else return 0;
+  if (it == start) return start;
+  if (it == n) return n - 1;
+  if (std::fabs(x - d[it - 1]) < std::fabs(x - d[it])) return it - 1;
+  return it;
+}
+
+static void load_wavenumbers(Model& m) {
+  // SpectralGrid::loadWavenumberList :87-119; createHeliosWavenumberList :75-84
+  std::ifstream f(m.wn_file);
+  if (!f) {
+    size_t n = (size_t)(90000.0 / 0.01 + 1);
+    m.nu_full.resize(n);
+    for (size_t i = 0; i < n; ++i) m.nu_full[i] = i * 0.01;
+  } else {
+    size_t n = 0;
+    f >> n;
+    m.nu_full.resize(n);
+    for (auto& v : m.nu_full) f >> v;
+    if (!f) throw Error(BEAR_ERR_FILE, "malformed wavenumber file " + m.wn_file);
+  }
+  m.wl_full.resize(m.nu_full.size());
+  for (size_t i = 0; i < m.nu_full.size(); ++i) m.wl_full[i] = 1.0 / m.nu_full[i] * 1e4;
+}
+
+static void sample_grid(Model& m) {
+  // SpectralGrid::sampleSpectralGrid :123-157
+  std::vector<std::array<double, 2>> e;
+  for (auto& o : m.obs) e.push_back({1.0 / o.wl_edges[0] * 1e4, 1.0 / o.wl_edges[1] * 1e4});
+  std::stable_sort(e.begin(), e.end(), [](const std::array<double, 2>& a, const std::array<double, 2>& b) { return a[0] < b[0]; });
+  std::vector<std::array<double, 2>> we{e[0]};
+  for (size_t i = 1; i < e.size(); ++i) {
+    if (e[i][0] > we.back()[0] && e[i][1] < we.back()[1]) continue;
+    if (e[i][0] < we.back()[1] && e[i][1] > we.back()[1]) we.back()[1] = e[i][1];
+    else we.push_back(e[i]);
+  }
+  const size_t nfull = m.nu_full.size();
+  // findBinEdges :390-416
+  std::vector<std::array<size_t, 2>> ei(we.size());
+  for (size_t i = 0; i < we.size(); ++i) {
+    size_t l = std::lower_bound(m.nu_full.begin(), m.nu_full.end(), we[i][0]) - m.nu_full.begin();
+    size_t r = std::lower_bound(m.nu_full.begin(), m.nu_full.end(), we[i][1]) - m.nu_full.begin();
+    if (l >= nfull || r >= nfull)
+      throw invalid("observation range outside of the wavenumber list");
+    ei[i][0] = l;
+    if (m.nu_full[ei[i][0]] > we[i][0]) {
+      if (ei[i][0] == 0) throw invalid("observation range outside of the wavenumber list");
+      ei[i][0] -= 1;
+    }
+    ei[i][1] = r;
+  }
+  // createHighResGrid :239-304 with the three discretisations :161-236
+  std::vector<int> inc(nfull, 0);
+  for (auto& r : ei) {
+    inc[r[0]] = 1;
+    size_t last = r[0];
+    for (size_t j = r[0]; j < r[1]; ++j) {
+      if (m.discretisation == 0) {
+        const double next = m.nu_full[last] + m.resolution;
+        if (next == m.nu_full[j] || m.nu_full[j + 1] > next) { inc[j] = 1; last = j; }
+      } else if (m.discretisation == 1) {
+        const double next = m.wl_full[last] - m.resolution;
+        if (next == m.wl_full[j] || m.wl_full[j + 1] < next) { inc[j] = 1; last = j; }
+      } else {
+        const double next = m.wl_full[last] * (1 - 1. / m.resolution);
+        if (next == m.wl_full[j] || m.wl_full[j + 1] < next) { inc[j] = 1; last = j; }
+      }
+      inc[r[1]] = 1;
+    }
+  }
+  for (auto& o : m.obs) {
+    size_t start = 0;
+    double last_nu = 0;
+    for (int b = 0; b < o.n; ++b) {
+      if (last_nu > o.edge_nu[b][0]) start = 0;
+      size_t i1 = find_closest(o.edge_nu[b][0], m.nu_full, start);
+      size_t i2 = find_closest(o.edge_nu[b][1], m.nu_full, start);
+      inc[i1] = 1;
+      inc[i2] = 1;
+      last_nu = o.edge_nu[b][1];
+      start = i2;
+    }
+  }
+  m.index_list.clear();
+  for (size_t i = 0; i < nfull; ++i)
+    if (inc[i] == 1) m.index_list.push_back(i);
+  m.N = m.index_list.size();
+  m.nu.resize(m.N);
+  m.wl.resize(m.N);
+  for (size_t i = 0; i < m.N; ++i) {
+    m.nu[i] = m.nu_full[m.index_list[i]];
+    m.wl[i] = m.wl_full[m.index_list[i]];
+  }
+  // SpectralBands::setBandEdgeIndices src/spectral_grid/spectral_band.cpp:80-121 and init :66-76
+  for (auto& o : m.obs) {
+    o.edge_idx.resize(o.n);
+    size_t start = 0;
+    double last_nu = 0;
+    for (int b = 0; b < o.n; ++b) {
+      if (last_nu > o.edge_nu[b][0]) start = 0;
+      size_t i1 = find_closest(o.edge_nu[b][0], m.nu, start);
+      size_t i2 = find_closest(o.edge_nu[b][1], m.nu, start);
+      if (i1 > m.N - 1 || i2 > m.N - 1) throw invalid("Edge wavenumber index not found!");
+      if (i1 == i2) throw invalid("The spectral resolution of the opacity grid is too small!");
+      o.edge_idx[b] = {i1, i2};
+      last_nu = o.edge_nu[b][1];
+      start = i2;
+    }
+    o.range_lo = find_closest(o.obs_nu_range[0], m.nu, 0);
+    o.range_hi = find_closest(o.obs_nu_range[1], m.nu, 0);
+  }
+}
+
+// SpectralGrid::interpolateToWavelengthGrid src/spectral_grid/spectral_grid_interpolate.cpp:60-172
+static std::vector<double> interp_to_wavelengths(std::vector<double> x, std::vector<double> y,
+                                                 const double* newx, size_t nn) {
+  if (x.size() > 1 && x[0] < x[1]) {
+    reverse_vec(x);
+    reverse_vec(y);
+  }
+  std::vector<double> out(nn, 0.0);
+  const size_t nd = x.size();
+  size_t x_start = 0;
+  for (size_t i = 0; i < nn; ++i) {
+    if (newx[i] > x.front()) continue;
+    if (newx[i] < x.back()) break;
+    size_t it = x_start;
+    while (it < nd && !(x[it] <= newx[i])) ++it;
+    if (it >= nd) break;
+    const size_t index = it;
+    if (x[it] == newx[i]) out[i] = y[index];
+    else out[i] = y[index - 1] + (y[index] - y[index - 1]) * (newx[i] - x[it - 1]) / (x[it] - x[it - 1]);
+    if (x_start > 0) x_start = index - 1;
+  }
+  return out;
+}
+
+static double normal_dist(double sigma, double x) {
+  // aux::normalDistribution(sigma, x) src/additional/aux_functions.cpp:344-351
+  const double c = std::sqrt(1.0 / (2.0 * kPi));
+  return c / sigma * std::exp(-x * x / (2.0 * sigma * sigma));
+}
+
+// Builds the instrument profile and filter (src/spectral_grid/spectral_band.cpp:127-154,
+// src/spectral_grid/spectral_band_convolve.cpp:44-95, src/observations/
+// observations_filter_response.cpp:122-160) and folds filter, convolution and bin
+// integration into one banded linear operator per bin:
+//   bin_b = sum_k W[b,k] F[k],
+// F being the high-resolution spectrum in native units. The composition is exact for
+// F >= 0 (emission fluxes and transit depths), where the absolute values the reference
+// takes of each convolved point and each wavelength-space bin integral only flip signs.
+static void build_observation_operator(Model& m, ObservationSetup& o) {
+  const size_t N = m.N;
+  o.has_profile = false;
+  if (!o.fwhm.empty() && (int)o.fwhm.size() == o.n) {
+    const size_t nhr = o.range_hi - o.range_lo + 1;
+    std::vector<double> prof = interp_to_wavelengths(o.centers, o.fwhm, m.wl.data() + o.range_lo, nhr);
+    o.sigma.assign(N, 0.0);
+    for (size_t i = 0; i < nhr; ++i) o.sigma[i + o.range_lo] = prof[i] / 2.355;
+    o.conv.resize(nhr);
+    for (size_t i = 0; i < nhr; ++i) {
+      const size_t idx = i + o.range_lo;
+      o.conv[i] = {o.range_lo, o.range_hi};
+      const double cut = 5.0 * o.sigma[idx];
+      if (cut == 0) o.conv[i] = {idx, idx};
+      else {
+        o.conv[i][0] = find_closest(m.wl[idx] + cut, m.wl, 0);
+        o.conv[i][1] = find_closest(m.wl[idx] - cut, m.wl, o.conv[i][0]);
+      }
+    }
+    o.has_profile = true;
+  }
+  if (o.nfilter) {
+    o.filter_grid = interp_to_wavelengths(o.filter_wl, o.filter_resp, m.wl.data(), N);
+    o.filter_weight.assign(N, 1.0);
+    if (o.photon)
+      for (size_t i = 0; i < N; ++i) o.filter_weight[i] = m.wl[i];
+    std::vector<double> y = o.filter_resp;
+    if (o.photon)
+      for (size_t i = 0; i < y.size(); ++i) y[i] *= o.filter_wl[i];
+    double s = 0.0;
+    if (y.size() == 1) s = y[0];
+    else {
+      for (size_t i = 1; i < y.size(); ++i) s += (o.filter_wl[i] - o.filter_wl[i - 1]) * (y[i] + y[i - 1]);
+      s *= 0.5;
+    }
+    if (s < 0) s = std::fabs(s);
+    o.filter_norm = s;
+    if (o.has_profile)
+      for (double r : o.filter_grid)
+        if (r < 0) throw unsupported("negative filter response combined with an instrument profile");
+  }
+  const bool is_flux = !m.transmission;
+  auto filt = [&](size_t k) -> double {
+    return o.nfilter ? o.filter_grid[k] * o.filter_weight[k] / o.filter_norm : 1.0;
+  };
+  o.row_k0.resize(o.n);
+  o.row_len.resize(o.n);
+  o.row_off.resize(o.n);
+  for (int b = 0; b < o.n; ++b) {
+    const size_t i0 = o.edge_idx[b][0], i1 = o.edge_idx[b][1];
+    // band integration weights on the (convolved) points i0..i1
+    std::vector<double> bw(i1 - i0 + 1, 0.0);
+    double scale;
+    if (is_flux) {
+      // bandIntegrateSpectrumFlux src/spectral_grid/spectral_band_integrate.cpp:66-80
+      const double wl_l = 1.0 / m.nu[i0] * 1e4, wl_r = 1.0 / m.nu[i1] * 1e4;
+      for (size_t i = i0 + 1; i < i1 + 1; ++i) {
+        const double d = m.nu[i] - m.nu[i - 1];
+        bw[i - i0] += d;
+        bw[i - 1 - i0] += d;
+      }
+      scale = 0.5 / (wl_l - wl_r);
+    } else {
+      // bandIntegrateSpectrum :85-107 (absolute value of a negative wavelength integral)
+      for (size_t i = i0 + 1; i < i1 + 1; ++i) {
+        const double d = m.wl[i] - m.wl[i - 1];
+        bw[i - i0] += d;
+        bw[i - 1 - i0] += d;
+      }
+      scale = -0.5;
+      if (!o.nfilter) scale /= (m.wl[i0] - m.wl[i1]);
+    }
+    // k range of the composite row
+    size_t klo = i0, khi = i1;
+    if (o.has_profile) {
+      for (size_t i = i0; i <= i1; ++i) {
+        if (i < o.range_lo || i > o.range_hi) continue;
+        const auto& c = o.conv[i - o.range_lo];
+        klo = std::min(klo, c[0]);
+        khi = std::max(khi, c[1]);
+      }
+    }
+    std::vector<double> row(khi - klo + 1, 0.0);
+    for (size_t i = i0; i <= i1; ++i) {
+      const double wb = bw[i - i0] * scale;
+      if (wb == 0.0) continue;
+      if (!o.has_profile) {
+        row[i - klo] += wb * filt(i);
+        continue;
+      }
+      if (i < o.range_lo || i > o.range_hi) continue;  // convolved spectrum is zero outside the range
+      const auto& c = o.conv[i - o.range_lo];
+      // SpectralBands::convolveSpectrum :116-144
+      if (c[0] == c[1] || o.sigma[i] == 0) {
+        row[i - klo] += wb * filt(i);
+        continue;
+      }
+      const size_t s = c[0], e = c[1];
+      if (e - s == 1) {
+        row[s - klo] += wb * filt(s) * normal_dist(o.sigma[i], std::fabs(m.wl[i] - m.wl[s]));
+        continue;
+      }
+      // |0.5 sum (x_j - x_{j-1}) (y_j + y_{j-1})| with x descending -> -0.5 * ...
+      for (size_t j = s; j < e; ++j) {
+        double cw = 0.0;
+        if (j > s) cw += m.wl[j] - m.wl[j - 1];
+        if (j + 1 < e) cw += m.wl[j + 1] - m.wl[j];
+        const double g = normal_dist(o.sigma[i], std::fabs(m.wl[i] - m.wl[j]));
+        row[j - klo] += wb * (-0.5 * cw) * g * filt(j);
+      }
+    }
+    o.row_k0[b] = (int)klo;
+    o.row_len[b] = (int)row.size();
+    o.row_off[b] = (long long)m.W.size();
+    m.W.insert(m.W.end(), row.begin(), row.end());
+  }
+}
+
+// ------------------------------------------------------------------ opacity tables
+// OpacitySpecies::readFileList src/transport_coeff/opacity_species.cpp:66-122,
+// orderDataList :129-156, CrossSectionFile::loadFile
+// src/transport_coeff/cross_section_file.cpp:33-68, SampledData::sampleCrossSections
+// src/transport_coeff/sampled_data.cpp:48-87.
+static void load_table(Model& m, OpacitySpecies& op, const std::string& folder) {
+  const std::string list = m.xsec_path + folder + "/filelist.dat";
+  std::ifstream f(list);
+  if (!f) throw Error(BEAR_ERR_FILE, "No line absorption data found: " + list);
+  std::string line;
+  std::getline(f, line);
+  std::istringstream first(line);
+  std::string storage;
+  op.mass = 0;
+  first >> op.mass >> storage;
+  const bool log_storage = storage == "log";
+  struct Entry { double p, T; std::string file; };
+  std::vector<Entry> entries;
+  while (std::getline(f, line)) {
+    std::istringstream ls(line);
+    Entry e;
+    if (ls >> e.p >> e.T >> e.file) entries.push_back(e);
+  }
+  if (entries.empty()) throw Error(BEAR_ERR_FILE, "empty cross-section list " + list);
+  for (auto& e : entries)
+    if (std::find(op.T.begin(), op.T.end(), e.T) == op.T.end()) op.T.push_back(e.T);
+  std::sort(op.T.begin(), op.T.end());
+  const size_t nT = op.T.size();
+  op.P.assign(nT, {});
+  op.logP.assign(nT, {});
+  op.row.assign(nT, {});
+  std::vector<float> buf;
+  for (size_t t = 0; t < nT; ++t) {
+    std::vector<const Entry*> rows;
+    for (auto& e : entries)
+      if (e.T == op.T[t]) rows.push_back(&e);
+    std::stable_sort(rows.begin(), rows.end(), [](const Entry* a, const Entry* b) { return a->p < b->p; });
+    for (const Entry* e : rows) {
+      op.P[t].push_back(e->p);
+      op.logP[t].push_back(std::log10(e->p));
+      const std::string path = m.xsec_path + folder + "/" + e->file;
+      std::ifstream df(path, std::ios::binary | std::ios::ate);
+      if (!df) throw Error(BEAR_ERR_FILE, "cross section file " + path + " not found");
+      const size_t nd = (size_t)df.tellg() / sizeof(float);
+      df.seekg(0);
+      buf.resize(nd);
+      df.read(reinterpret_cast<char*>(buf.data()), nd * sizeof(float));
+      const int row = (int)m.n_rows++;
+      op.row[t].push_back(row);
+      m.table_host.resize((size_t)m.n_rows * m.N);
+      double* r = m.table_host.data() + (size_t)row * m.N;
+      for (size_t k = 0; k < m.N; ++k) r[k] = 0.0;
+      for (size_t k = 0; k < m.N; ++k) {
+        if (m.index_list[k] > nd - 1) break;
+        double v = buf[m.index_list[k]];
+        if (log_storage) v = std::pow(10.0, v);
+        r[k] = v;
+      }
+      for (size_t k = 0; k < m.N; ++k) {
+        if (op.mass > 0) r[k] *= op.mass / 6.022140857e23;
+        if (r[k] < 1e-200) r[k] = 1e-200;
+      }
+      for (size_t k = 0; k < m.N; ++k) r[k] = std::log10(r[k]);
+    }
+  }
+}
+
+// Rayleigh cross sections src/transport_coeff/species_rayleigh_cross_sections.cpp and
+// OpacitySpecies::generalRayleighCrossSection src/transport_coeff/opacity_species.cpp:528-537
+static void tabulate_rayleigh(Model& m, OpacitySpecies& op) {
+  op.rayleigh.resize(m.N);
+  for (size_t j = 0; j < m.N; ++j) {
+    const double nu = m.nu[j], wl = m.wl[j];
+    double n, nref, king = 1.0;
+    if (op.index == SP_H2) {
+      n = (13.58e-5 * (1. + 7.52e-3 / std::pow(wl, 2))) + 1.;
+      nref = 2.651629e19;
+    } else if (op.index == SP_He) {
+      n = (2283. + 1.8102e13 / (1.5342e10 - nu * nu)) * 1e-8 + 1;
+      nref = 2.546899e19;
+    } else {
+      throw unsupported(std::string("Rayleigh scattering of ") + kSpeciesSymbol[op.index] +
+                        " is not supported (H2, He)");
+    }
+    op.rayleigh[j] = 24. * std::pow(kPi, 3) * std::pow(nu, 4) / (nref * nref) *
+                     std::pow((n * n - 1) / (n * n + 2), 2) * king;
+  }
+}
+
+static void setup_opacity(Model& m) {
+  // TransportCoefficients::addOpacitySpecies src/transport_coeff/transport_coeff.cpp:98-237
+  m.n_rows = 0;
+  m.table_host.clear();
+  for (size_t i = 0; i < m.opac_cfg.size(); ++i) {
+    const std::string& s = m.opac_cfg[i].first;
+    const std::string& fo = m.opac_cfg[i].second;
+    OpacitySpecies op;
+    if (s == "CIA-H2-H2") { op.index = SP_H2; op.partners = {SP_H2}; }
+    else if (s == "CIA-H2-He") { op.index = SP_H2; op.partners = {SP_He}; }
+    else if (s == "CIA-H-He") { op.index = SP_H; op.partners = {SP_He}; }
+    else if (s == "H-") throw unsupported("the H- continuum is not supported");
+    else if (fo == "Rayleigh") {
+      op.index = species_id(s);
+      if (op.index < 0) throw invalid("Opacity species " + s + " has not been found");
+      op.kind = 1;
+      tabulate_rayleigh(m, op);
+      m.rayleigh_species.push_back((int)m.opac.size());
+      m.opac.push_back(std::move(op));
+      continue;
+    } else {
+      op.index = species_id(s);
+      if (op.index < 0) throw invalid("Opacity species " + s + " has not been found");
+    }
+    op.kind = 0;
+    load_table(m, op, fo);
+    m.table_species.push_back((int)m.opac.size());
+    m.opac.push_back(std::move(op));
+  }
+  if ((int)m.table_species.size() > kMaxTableSpecies) throw unsupported("too many opacity species");
+  if ((int)m.rayleigh_species.size() > kMaxRayleigh) throw unsupported("too many Rayleigh species");
+}
+
+// ------------------------------------------------------------------ atmosphere constants
+static void setup_atmosphere(Model& m) {
+  AtmosphereConfig& a = m.acfg;
+  std::memset(&a, 0, sizeof a);
+  const int L = m.L;
+  // Atmosphere::createPressureGrid src/forward_model/atmosphere/atmosphere.cpp:365-383
+  m.p.assign(L, 0.0);
+  const double minp = m.ptop, maxp = m.pbot;
+  m.p[0] = std::log10(maxp);
+  const double step = (std::log10(maxp) - std::log10(minp)) / (L - 1.0);
+  for (int i = 1; i < L - 1; ++i) m.p[i] = m.p[i - 1] - step;
+  for (int i = 0; i < L - 1; ++i) m.p[i] = std::pow(10.0, m.p[i]);
+  m.p[L - 1] = minp;
+  m.log10p.resize(L);
+  for (int i = 0; i < L; ++i) m.log10p[i] = std::log10(m.p[i]);
+  a.L = L;
+  a.transmission = m.transmission;
+  a.temp_poly = m.temp_poly;
+  if (m.temp_poly) {
+    // PiecewisePolynomial src/additional/piecewise_poly.cpp:36-121 (node table :36-44)
+    static const double gl[7][5] = {{0.0},
+                                     {-1.0, 1.0},
+                                     {-1.0, 0.0, 1.0},
+                                     {-1.0, -0.447214, 0.447214, 1.0},
+                                     {-1.0, -0.654654, 0.654654, 1.0},
+                                     {-1.0, -0.654654, 0.0, 0.654654, 1.0},
+                                     {-1.0, -7.65055 - 0.285232, 0.285232, 0.765055, 1.0}};
+    static const int gn[7] = {1, 2, 3, 4, 4, 5, 5};
+    const int order = std::min(std::max(m.poly_order, 1), 6);
+    const int nel = std::max(m.poly_elements, 1);
+    const int nd = gn[order];
+    if (nel * (nd - 1) + 1 > kMaxPolyDof || nel * nd > kMaxPolyDof * 8)
+      throw unsupported("too many piecewise-polynomial elements");
+    a.pp_nel = nel;
+    a.pp_ndof_el = nd;
+    for (int i = 0; i < nd; ++i) a.pp_ref[i] = gl[order][i];
+    const double lb0 = std::log10(m.pbot), lb1 = std::log10(m.ptop);
+    const double size = (lb0 - lb1) / nel;
+    std::vector<double> edges(nel + 1);
+    edges.front() = lb0;
+    edges.back() = lb1;
+    for (int i = 1; i < nel; ++i) edges[i] = edges[i - 1] - size;
+    for (int e = 0; e < nel; ++e)
+      for (int i = 0; i < nd; ++i)
+        a.pp_el_vert[e * nd + i] = edges[e] + (1.0 + a.pp_ref[i]) / 2.0 * (edges[e + 1] - edges[e]);
+    int c = 0;
+    for (int e = 0; e < nel; ++e)
+      for (int i = 0; i < nd - 1; ++i) a.pp_dof_vertices[c++] = a.pp_el_vert[e * nd + i];
+    a.pp_dof_vertices[c++] = a.pp_el_vert[(nel - 1) * nd + nd - 1];
+    a.pp_ndof = c;
+    m.nparam_temp = nel * order + 1;  // PiecewisePolynomialTemperature ctor :33-43
+  } else {
+    m.nparam_temp = 1;
+  }
+  a.nchem = (int)m.chem.size();
+  for (int c = 0; c < a.nchem; ++c) {
+    a.chem_kind[c] = m.chem[c].kind;
+    a.chem_nsp[c] = (int)m.chem[c].sp.size();
+    for (size_t j = 0; j < m.chem[c].sp.size(); ++j) a.chem_sp[c][j] = m.chem[c].sp[j];
+    a.chem_na_free[c] = m.chem[c].na_free;
+    a.chem_bg_h2he[c] = m.chem[c].bg_h2he;
+    a.chem_bg_sp[c] = m.chem[c].bg_sp;
+  }
+  a.cloud = m.cloud;
+  a.cloud_fb = m.cloud_fb;
+  a.fit_mmw = m.fit_mmw;
+  a.var_g = m.var_g;
+  // table species: temperature nodes and the (parameter-independent) pressure bracket of
+  // every level for every temperature row (OpacitySpecies::findClosestDataPoints
+  // src/transport_coeff/opacity_species.cpp:204-269)
+  a.S = (int)m.table_species.size();
+  m.table_T.clear();
+  m.pb_row0.clear();
+  m.pb_row1.clear();
+  m.pb_w.clear();
+  for (int s = 0; s < a.S; ++s) {
+    const OpacitySpecies& op = m.opac[m.table_species[s]];
+    a.sp_index[s] = op.index;
+    a.sp_partner[s][0] = op.partners.size() > 0 ? op.partners[0] : -1;
+    a.sp_partner[s][1] = op.partners.size() > 1 ? op.partners[1] : -1;
+    a.sp_nT[s] = (int)op.T.size();
+    a.sp_T_off[s] = (int)m.table_T.size();
+    a.sp_pb_off[s] = (int)m.pb_row0.size();
+    for (double T : op.T) m.table_T.push_back(T);
+    for (size_t t = 0; t < op.T.size(); ++t) {
+      const std::vector<double>& P = op.P[t];
+      const int np = (int)P.size();
+      for (int l = 0; l < L; ++l) {
+        const double p = m.p[l];
+        int q0 = 0, q1 = 0;
+        if (p < P.front()) q0 = q1 = 0;
+        else if (p > P.back()) q0 = q1 = np - 1;
+        else {
+          for (int i = 0; i < np; ++i) {
+            if (P[i] == p) { q0 = q1 = i; break; }
+            else if (P[i] < p && P[i + 1] > p) { q0 = i; q1 = i + 1; break; }
+          }
+        }
+        m.pb_row0.push_back(op.row[t][q0]);
+        m.pb_row1.push_back(op.row[t][q1]);
+        double w = 0.0;
+        if (q0 != q1) w = (m.log10p[l] - op.logP[t][q0]) / (op.logP[t][q1] - op.logP[t][q0]);
+        m.pb_w.push_back(w);
+      }
+    }
+  }
+  a.R = (int)m.rayleigh_species.size();
+  for (int r = 0; r < a.R; ++r) a.ray_index[r] = m.opac[m.rayleigh_species[r]].index;
+}
+
+void finalize_host(Model& m) {
+  if (m.prepared) throw Error(BEAR_ERR_STATE, "model already prepared");
+  if (m.obs.empty()) throw invalid("No observations given");
+  load_wavenumbers(m);
+  sample_grid(m);
+  m.W.clear();
+  m.M = 0;
+  for (auto& o : m.obs) {
+    o.out_offset = m.M;
+    m.M += o.n;
+  }
+  setup_opacity(m);
+  for (auto& o : m.obs) build_observation_operator(m, o);
+  setup_atmosphere(m);
+  // parameter layout: EmissionModel::extractParameters src/forward_model/emission/emission.cpp:123-153,
+  // TransmissionModel::extractParameters src/forward_model/transmission/transmission.cpp:110-146
+  m.nparam_general = 3 + ((m.transmission && m.fit_mmw) ? 1 : 0);
+  m.nparam_chem = 0;
+  for (auto& c : m.chem) m.nparam_chem += c.kind == 0 ? (int)c.sp.size() : 0;
+  m.nparam_cloud = m.cloud ? (m.cloud_fb ? 2 : 3) : 0;
+  m.nparam_mod = 0;
+  for (auto& o : m.obs) m.nparam_mod += o.nb_modifier;
+  m.nparam_total = m.nparam_general + m.nparam_chem + m.nparam_temp + m.nparam_cloud + m.nparam_mod;
+  AtmosphereConfig& a = m.acfg;
+  a.nparam_general = m.nparam_general;
+  a.nparam_chem = m.nparam_chem;
+  a.nparam_temp = m.nparam_temp;
+  a.nparam_cloud = m.nparam_cloud;
+  a.nparam_mod = m.nparam_mod;
+  a.nparam_total = m.nparam_total + (m.error_inflation ? 1 : 0);
+  a.error_inflation = m.error_inflation;
+}
+
+}  // namespace bgb

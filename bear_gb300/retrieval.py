@@ -1,0 +1,319 @@
+"""pyBeAR-compatible front end of the GB300 engine.
+
+``Retrieval(config, model_config, observations, priors)`` keeps the names and
+semantics of the reference's binding (python/src/bear_python_wrapper.cpp:114-129):
+``computeLikelihood``, ``computeModel``, ``convertCubeParameters``,
+``convertToPhysicalParameters``, ``nbParameters`` and ``spectral_grid``. It adds
+``computeLikelihoodBatch`` / ``computeGradientBatch`` for batches of parameter
+sets evaluated in one launch, and ``BatchEvaluator`` that replays a captured
+CUDA graph for a fixed batch size.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import _lib
+from .config import (Config, GenericConfig, Observation, ObservationArrays, Prior,
+                     observation_arrays, render_config)
+
+PARSEC = 3.08567758135e18
+UNITS = {
+    "": 1.0,
+    "Me": 5.97219e27, "Mearth": 5.97219e27, "Mj": 1.89813e30, "Mjupiter": 1.89813e30,
+    "Ms": 1.9884e33, "Msun": 1.9884e33, "Re": 6.37123e8, "Rearth": 6.37123e8,
+    "Rj": 7.1492e9, "Rjupiter": 7.1492e9, "Rs": 6.96342e10, "Rsun": 6.96342e10,
+    "ly": 9.4607304725808e17, "pc": PARSEC,
+}
+
+
+class Engine:
+    """One device model: config text + observation arrays -> likelihood engine."""
+
+    def __init__(self, config_text: str, observations: Sequence[ObservationArrays], device: int = 0,
+                 prepare_only: bool = False):
+        """prepare_only: run the host-side set-up (grid, observation operators,
+        tables) without a GPU; evaluations are then unavailable."""
+        lib = _lib.load()
+        h = C.c_void_p()
+        _lib.check(lib.bear_model_create(config_text.encode(), int(device), C.byref(h)))
+        self._h = h
+        self._lib = lib
+        self.device = int(device)
+        self._keep = []
+        try:
+            for o in observations:
+                arrs = [None if x is None else np.ascontiguousarray(x, dtype=np.float64)
+                        for x in (o.centers_or_edges, o.data, o.error, o.weight, o.fwhm,
+                                  o.filter_wavelength, o.filter_response)]
+                ce, d, e, w, f, fw, fr = arrs
+                self._keep.append(arrs)
+                nf = 0 if fw is None else int(fw.size)
+                _lib.check(lib.bear_model_add_observation(
+                    h, o.name.encode(), o.type.encode(), int(o.n), _lib.dptr(ce), _lib.dptr(d), _lib.dptr(e),
+                    _lib.dptr(w), _lib.dptr(f), nf, _lib.dptr(fw), _lib.dptr(fr),
+                    (o.detector or "").encode(), (o.modifier or "").encode()))
+            _lib.check(lib.bear_model_prepare(h) if prepare_only else lib.bear_model_finalize(h))
+        except Exception:
+            lib.bear_model_destroy(h)
+            self._h = None
+            raise
+        N, M, P, K = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        _lib.check(lib.bear_model_info(h, C.byref(N), C.byref(M), C.byref(P), C.byref(K)))
+        self.N, self.M, self.P, self.nobs = N.value, M.value, P.value, K.value
+        self.obs_sizes = []
+        for k in range(self.nobs):
+            n = C.c_int()
+            _lib.check(lib.bear_model_observation_size(h, k, C.byref(n)))
+            self.obs_sizes.append(n.value)
+        self.wavenumbers = np.empty(self.N)
+        _lib.check(lib.bear_model_wavenumbers(h, _lib.dptr(self.wavenumbers)))
+
+    def observation_setup(self, k: int) -> dict:
+        """Integer set-up of observation k: observation index range, band-edge
+        indices and convolution windows (as SpectralBands holds them)."""
+        cap = 4 * self.N + 16
+        buf = (C.c_longlong * cap)()
+        n = C.c_int()
+        _lib.check(self._lib.bear_model_observation_setup(self._h, int(k), buf, cap, C.byref(n)))
+        v = list(buf[: n.value])
+        nb = v[2]
+        edges = [(v[3 + 2 * i], v[4 + 2 * i]) for i in range(nb)]
+        rest = v[3 + 2 * nb:]
+        conv = [(rest[2 * i], rest[2 * i + 1]) for i in range(len(rest) // 2)]
+        return {"range": (v[0], v[1]), "edges": edges, "conv": conv}
+
+    def operator_row(self, r: int):
+        """(k0, weights) of row r of the composite observation operator."""
+        k0, ln = C.c_int(), C.c_int()
+        w = C.POINTER(C.c_double)()
+        _lib.check(self._lib.bear_model_operator_row(self._h, int(r), C.byref(k0), C.byref(ln), C.byref(w)))
+        return k0.value, np.ctypeslib.as_array(w, shape=(ln.value,)).copy()
+
+    # ------------------------------------------------------------ plain path
+    def _params(self, params) -> np.ndarray:
+        p = np.ascontiguousarray(params, dtype=np.float64).ravel()
+        if p.size != self.P:
+            raise ValueError(f"expected {self.P} parameters, got {p.size}")
+        return p
+
+    def compute_model(self, params, stream: int = 0):
+        p = self._params(params)
+        spec = np.empty(self.N)
+        obs = np.empty(max(self.M, 1))
+        neg = C.c_int(0)
+        _lib.check(self._lib.bear_compute_model(self._h, _lib.dptr(p), p.size, _lib.dptr(spec), _lib.dptr(obs),
+                                                C.byref(neg), C.c_void_p(stream)))
+        return spec, obs[: self.M], bool(neg.value)
+
+    def loglike(self, params, stream: int = 0) -> float:
+        p = self._params(params)
+        out = C.c_double(0.0)
+        _lib.check(self._lib.bear_loglike(self._h, _lib.dptr(p), p.size, C.byref(out), C.c_void_p(stream)))
+        return out.value
+
+    def forward_device(self, params, spectrum_ptr: int, obs_ptrs: Optional[Sequence[int]], stream: int = 0) -> bool:
+        """ForwardModel::calcModelGPU: device outputs given as raw pointers."""
+        p = self._params(params)
+        arr = None
+        if obs_ptrs is not None:
+            arr = (C.POINTER(C.c_double) * self.nobs)(*[C.cast(C.c_void_p(x), C.POINTER(C.c_double)) for x in obs_ptrs])
+        neg = C.c_int(0)
+        _lib.check(self._lib.bear_forward(self._h, _lib.dptr(p), p.size,
+                                          C.cast(C.c_void_p(spectrum_ptr), C.POINTER(C.c_double)) if spectrum_ptr else C.cast(None, C.POINTER(C.c_double)),
+                                          arr, C.byref(neg), C.c_void_p(stream)))
+        return bool(neg.value)
+
+    # ------------------------------------------------------------ batched path
+    def loglike_batch_ptr(self, params_ptr: int, batch: int, loglike_ptr: int, neglect_ptr: int = 0,
+                          stream: int = 0) -> None:
+        _lib.check(self._lib.bear_loglike_batch(self._h, C.c_void_p(params_ptr), int(batch), self.P,
+                                                C.c_void_p(loglike_ptr), C.c_void_p(neglect_ptr or None),
+                                                C.c_void_p(stream)))
+
+    def grad_batch_ptr(self, params_ptr: int, batch: int, loglike_ptr: int, grad_ptr: int,
+                       neglect_ptr: int = 0, stream: int = 0) -> None:
+        _lib.check(self._lib.bear_loglike_grad_batch(self._h, C.c_void_p(params_ptr), int(batch), self.P,
+                                                     C.c_void_p(loglike_ptr), C.c_void_p(grad_ptr),
+                                                     C.c_void_p(neglect_ptr or None), C.c_void_p(stream)))
+
+    def loglike_batch(self, params):
+        """params: torch float64 CUDA tensor (B, P). Returns (loglike (B,), neglect (B,) uint8)."""
+        import torch
+        t = params.contiguous()
+        assert t.dtype == torch.float64 and t.is_cuda and t.shape[1] == self.P
+        B = t.shape[0]
+        ll = torch.empty(B, dtype=torch.float64, device=t.device)
+        ng = torch.empty(B, dtype=torch.uint8, device=t.device)
+        self.loglike_batch_ptr(t.data_ptr(), B, ll.data_ptr(), ng.data_ptr(),
+                               torch.cuda.current_stream(t.device).cuda_stream)
+        return ll, ng
+
+    def grad_batch(self, params):
+        import torch
+        t = params.contiguous()
+        B = t.shape[0]
+        ll = torch.empty(B, dtype=torch.float64, device=t.device)
+        g = torch.empty(B, self.P, dtype=torch.float64, device=t.device)
+        ng = torch.empty(B, dtype=torch.uint8, device=t.device)
+        self.grad_batch_ptr(t.data_ptr(), B, ll.data_ptr(), g.data_ptr(), ng.data_ptr(),
+                            torch.cuda.current_stream(t.device).cuda_stream)
+        return ll, g, ng
+
+    def set_precision(self, fp32_tables: bool) -> None:
+        _lib.check(self._lib.bear_model_set_precision(self._h, int(bool(fp32_tables))))
+
+    def set_launch(self, rt_threads: int = 0, obs_threads: int = 0) -> None:
+        _lib.check(self._lib.bear_model_set_launch(self._h, int(rt_threads), int(obs_threads)))
+
+    def device_bytes(self) -> int:
+        b = C.c_size_t()
+        _lib.check(self._lib.bear_model_device_bytes(self._h, C.byref(b)))
+        return b.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.bear_model_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class ForwardModelOutput:
+    """src/forward_model/forward_model.h:42-46"""
+
+    neglect_model: bool = False
+    spectrum: List[float] = field(default_factory=list)
+    spectrum_obs: List[List[float]] = field(default_factory=list)
+
+
+class SpectralGrid:
+    """The parts of SpectralGrid the binding exposes (src/spectral_grid/spectral_grid.h:41-63)."""
+
+    def __init__(self, wavenumbers: np.ndarray):
+        self.wavenumber_list = list(wavenumbers)
+        self.wavelength_list = list(1.0 / np.asarray(wavenumbers) * 1e4)
+
+    @staticmethod
+    def wavelengthToWavenumber(wavelength: float) -> float:
+        return 1.0 / wavelength * 1e4
+
+
+def _erfinv(y: float) -> float:
+    from scipy.special import erfinv
+    return float(erfinv(y))
+
+
+class Priors:
+    """Prior transforms of src/retrieval/prior_types.h:89-230 (uniform, log-uniform,
+    Gaussian, delta) with the unit factors of :57-82."""
+
+    def __init__(self, priors: Sequence[Prior]):
+        self.priors = list(priors)
+        for p in self.priors:
+            if p.type not in ("uniform", "log_uniform", "gaussian", "delta"):
+                raise ValueError(f"prior type {p.type} is not supported")
+            if p.unit not in UNITS:
+                raise ValueError(f"Unit {p.unit} for parameter {p.description} unknown!")
+
+    def __len__(self):
+        return len(self.priors)
+
+    def cube_to_parameters(self, cube: Sequence[float]) -> List[float]:
+        out = []
+        for p, u in zip(self.priors, cube):
+            if p.type == "uniform":
+                lo, hi = sorted(p.parameter)
+                out.append(lo + u * (hi - lo))
+            elif p.type == "log_uniform":
+                lo, hi = sorted([math.log10(p.parameter[0]), math.log10(p.parameter[1])])
+                out.append(10.0 ** (lo + u * (hi - lo)))
+            elif p.type == "gaussian":
+                out.append(p.parameter[0] + p.parameter[1] * math.sqrt(2.0) * _erfinv(2.0 * u - 1.0))
+            else:
+                out.append(p.parameter[0])
+        return out
+
+    def to_physical(self, params: Sequence[float]) -> List[float]:
+        return [v * UNITS[p.unit] for p, v in zip(self.priors, params)]
+
+    def cube_to_physical_batch(self, cube: np.ndarray) -> np.ndarray:
+        cube = np.atleast_2d(np.asarray(cube, dtype=np.float64))
+        out = np.empty_like(cube)
+        for j, p in enumerate(self.priors):
+            u = UNITS[p.unit]
+            if p.type == "uniform":
+                lo, hi = sorted(p.parameter)
+                out[:, j] = (lo + cube[:, j] * (hi - lo)) * u
+            elif p.type == "log_uniform":
+                lo, hi = sorted(np.log10(p.parameter))
+                out[:, j] = np.power(10.0, lo + cube[:, j] * (hi - lo)) * u
+            elif p.type == "gaussian":
+                from scipy.special import erfinv
+                out[:, j] = (p.parameter[0] + p.parameter[1] * np.sqrt(2.0) * erfinv(2.0 * cube[:, j] - 1.0)) * u
+            else:
+                out[:, j] = p.parameter[0] * u
+        return out
+
+
+class Retrieval:
+    """Retrieval(GlobalConfig*, GenericConfig*, vector<ObservationInput>, vector<PriorConfig>)
+    (src/retrieval/retrieval.cpp:70-104) on the GB300 engine."""
+
+    def __init__(self, config: Config, model_config: GenericConfig, observations: Sequence[Observation],
+                 priors: Sequence[Prior], device: int = 0):
+        self.config = config
+        self.model_config = model_config
+        self.observations = list(observations)
+        self._arrays = [observation_arrays(o) for o in self.observations]
+        self.engine = Engine(render_config(config, model_config), self._arrays, device)
+        self.priors = Priors(priors)
+        if len(self.priors) != self.engine.P:
+            raise ValueError(f"Found {len(self.priors)} priors config but expected {self.engine.P}")
+        self.spectral_grid = SpectralGrid(self.engine.wavenumbers)
+        self.nb_observations = self.engine.nobs
+
+    def nbParameters(self) -> int:
+        return len(self.priors)
+
+    def convertCubeParameters(self, cube: Sequence[float]) -> Tuple[List[float], List[float]]:
+        params = self.priors.cube_to_parameters(cube)
+        return params, self.priors.to_physical(params)
+
+    def convertToPhysicalParameters(self, params: Sequence[float]) -> List[float]:
+        return self.priors.to_physical(params)
+
+    def computeLikelihood(self, physical_parameters: Sequence[float]) -> float:
+        return self.engine.loglike(physical_parameters)
+
+    def computeModel(self, physical_parameters: Sequence[float], return_high_res_spectrum: bool) -> ForwardModelOutput:
+        spec, obs, neg = self.engine.compute_model(physical_parameters)
+        out = ForwardModelOutput(neglect_model=neg)
+        out.spectrum = list(spec) if return_high_res_spectrum else []
+        off = 0
+        for n in self.engine.obs_sizes:
+            out.spectrum_obs.append(list(obs[off:off + n]))
+            off += n
+        return out
+
+    def computeLikelihoodBatch(self, physical_parameters) -> np.ndarray:
+        import torch
+        t = torch.as_tensor(np.asarray(physical_parameters, dtype=np.float64), device=f"cuda:{self.engine.device}")
+        ll, _ = self.engine.loglike_batch(t)
+        return ll.cpu().numpy()
+
+    def computeGradientBatch(self, physical_parameters) -> Tuple[np.ndarray, np.ndarray]:
+        import torch
+        t = torch.as_tensor(np.asarray(physical_parameters, dtype=np.float64), device=f"cuda:{self.engine.device}")
+        ll, g, _ = self.engine.grad_batch(t)
+        return ll.cpu().numpy(), g.cpu().numpy()

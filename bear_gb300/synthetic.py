@@ -7,9 +7,14 @@ workload here is synthetic. Files follow the reference's loaders exactly:
   (src/spectral_grid/spectral_grid.cpp:87-119).
 * ``<folder>/filelist.dat``: first line ``"<mass> [log]"``, then
   ``"<p_bar> <T_K> <file>"`` rows (src/transport_coeff/opacity_species.cpp:66-122).
-* each data file is raw float32 cross sections over the full global grid
-  (src/transport_coeff/cross_section_file.cpp:33-68). Mass 0 means the values
-  are already cm^2 (no conversion, src/transport_coeff/sampled_data.cpp:68-72).
+* each data file is raw float32 over the full global grid
+  (src/transport_coeff/cross_section_file.cpp:33-68); with the ``log`` flag the
+  values are log10 cross sections, which the loader exponentiates. Mass 0 means
+  cm^2 (no conversion, src/transport_coeff/sampled_data.cpp:68-72).
+
+The generated tables use the ``log`` storage and are built from MT19937
+uniforms (Irwin-Hall sums) with basic IEEE arithmetic only, so a given seed
+produces bit-identical files on x86-64 and aarch64.
 
 Workload shapes (levels, grids, table sizes, observation sizes) are the ones of
 the five benchmark configurations; see ``CONFIGS``.
@@ -127,7 +132,11 @@ def _spec_key(spec: WorkloadSpec) -> str:
     d = dataclasses.asdict(spec)
     d.pop("batch", None)
     d.pop("obs_kind", None)
+    d["format"] = TABLE_FORMAT
     return hashlib.sha1(json.dumps(d, sort_keys=True).encode()).hexdigest()[:16]
+
+
+TABLE_FORMAT = 2  # bump when the generated tables change
 
 
 def write_tables(spec: WorkloadSpec, root: str) -> str:
@@ -139,7 +148,7 @@ def write_tables(spec: WorkloadSpec, root: str) -> str:
     if os.path.exists(done):
         return root
     os.makedirs(root, exist_ok=True)
-    rng = np.random.default_rng(spec.seed)
+    rng = np.random.RandomState(spec.seed % (2**32))
     n_full = int(round((spec.nu_max - spec.nu_min) / spec.nu_step)) + 1
     nu = spec.nu_min + spec.nu_step * np.arange(n_full, dtype=np.float64)
     with open(os.path.join(root, "wavenumber_full.dat"), "w") as f:
@@ -151,39 +160,50 @@ def write_tables(spec: WorkloadSpec, root: str) -> str:
     for s in spec.species:
         folder = os.path.join(root, s)
         os.makedirs(folder, exist_ok=True)
-        shared = rng.standard_normal(n_full)
+        shared = _normal_like(rng, n_full)
         rows = []
         with open(os.path.join(folder, "filelist.dat"), "w") as fl:
-            fl.write("0\n")
+            # mass 0 (cm^2, no conversion); "log": the files hold log10 cross sections
+            fl.write("0 log\n")
             for T in t_nodes:
                 for p in p_nodes:
                     name = f"sigma_{p:.6g}_{T:.6g}.bin"
                     fl.write(f"{_fmt(p)} {_fmt(T)} {name}\n")
                     rows.append(name)
-        n_rows = len(rows)
-        own = rng.standard_normal((n_rows, n_full))
-        x = (0.7 * shared[None, :] + 0.3 * own) / np.sqrt(0.58)
-        x = _boxcar5(x) * np.sqrt(5.0)
-        logsig = spec.table.logsig_mean + spec.table.logsig_std * x
-        sig = np.power(10.0, logsig).astype(np.float32)
-        for r, name in enumerate(rows):
-            sig[r].tofile(os.path.join(folder, name))
-        del own, x, logsig, sig
+        for name in rows:
+            own = _normal_like(rng, n_full)
+            x = (0.7 * shared + 0.3 * own) * (1.0 / 0.7615773105863909)
+            x = _boxcar5(x) * 2.23606797749979
+            logsig = (spec.table.logsig_mean + spec.table.logsig_std * x).astype(np.float32)
+            logsig.tofile(os.path.join(folder, name))
 
     # collision-induced absorption: one pressure row per temperature, smooth in T and nu
-    for cia, amp in (("H2-H2", 1e-46), ("H2-He", 3e-47)):
+    # (log10 sigma = a + 0.2 (T/1000 - 1) - 0.434 ((nu - 4500) / 3500)^2 + ripple)
+    for cia, amp in (("H2-H2", -46.0), ("H2-He", -46.5)):
         folder = os.path.join(root, "CIA", cia)
         os.makedirs(folder, exist_ok=True)
         with open(os.path.join(folder, "filelist.dat"), "w") as fl:
-            fl.write("0\n")
+            fl.write("0 log\n")
             for T in t_nodes:
                 name = f"cia_{T:.6g}.bin"
                 fl.write(f"1 {_fmt(T)} {name}\n")
-                prof = amp * np.sqrt(T / 1000.0) * np.exp(-(((nu - 4500.0) / 3500.0) ** 2))
-                prof = prof * (1.0 + 0.3 * np.sin(nu / 700.0 + T / 500.0) ** 2)
-                prof.astype(np.float32).tofile(os.path.join(folder, name))
+                u = (nu - 4500.0) / 3500.0
+                v = (nu / 700.0 + T / 500.0) * 0.15915494309189535
+                ripple = 0.1 * (v - np.floor(v) - 0.5) ** 2
+                lg = amp + 0.2 * (T / 1000.0 - 1.0) - 0.4342944819032518 * u * u + ripple
+                lg.astype(np.float32).tofile(os.path.join(folder, name))
     open(done, "w").close()
     return root
+
+
+def _normal_like(rng: np.random.RandomState, n: int) -> np.ndarray:
+    """Approximately standard-normal values from four MT19937 uniforms
+    (Irwin-Hall). Uses only integer and basic IEEE arithmetic, so the tables are
+    bit-identical on every platform."""
+    s = rng.random_sample(n)
+    for _ in range(3):
+        s += rng.random_sample(n)
+    return (s - 2.0) * 1.7320508075688772
 
 
 # --------------------------------------------------------------------------- models

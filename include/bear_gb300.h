@@ -1,0 +1,161 @@
+/*
+ * bear_gb300.h -- C ABI of the GB300 likelihood engine (libbeargb300.so).
+ *
+ * The engine evaluates BeAR's per-likelihood forward-model path on one GPU:
+ * opacity assembly from tabulated cross sections, short-characteristics
+ * emission or slant-path transmission radiative transfer, the observation
+ * operator (filter, instrument-profile convolution, bin integration) and the
+ * Gaussian log-likelihood. All signatures use plain pointers and sizes; device
+ * pointers are CUDA device addresses, streams are cudaStream_t passed as void*.
+ *
+ * Each entry point names the reference interface it replaces (paths inside the
+ * BeAR project).
+ *
+ * Status: every function returns 0 on success or a BEAR_ERR_* code; the
+ * message of the last failure on the calling thread is bear_last_error().
+ * No function calls exit(); invalid physics is reported per evaluation through
+ * the neglect flag (the reference then reports log L = -1e30).
+ *
+ * Threading: a model is used by one host thread / one stream at a time. Batch
+ * calls are stream-ordered and allocate nothing once a batch size has been
+ * seen (work buffers grow on first use of a larger batch).
+ */
+#ifndef BEAR_GB300_H
+#define BEAR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  BEAR_OK = 0,
+  BEAR_ERR_INVALID_INPUT = 1, /* reference: InvalidInput (src/additional/exceptions.h:29-50) */
+  BEAR_ERR_FILE = 2,          /* reference: FileNotFound */
+  BEAR_ERR_CUDA = 3,          /* reference: gpuErrchk -> exit (src/CUDA_kernels/error_check.h:29-37) */
+  BEAR_ERR_UNSUPPORTED = 4,   /* module outside the engine's scope */
+  BEAR_ERR_STATE = 5,         /* call order (e.g. evaluation before finalize) */
+  BEAR_ERR_SIZE = 6           /* argument sizes do not match the model */
+};
+
+typedef struct bear_model bear_model;
+
+/* Message of the last failed call on this thread (never NULL). */
+const char* bear_last_error(void);
+
+/* --------------------------------------------------------------- set-up
+ * Replaces the model construction of Retrieval::Retrieval(GlobalConfig*,
+ * GenericConfig*, vector<ObservationInput>, vector<PriorConfig>)
+ * (src/retrieval/retrieval.cpp:70-104): GlobalConfig + Emission/Transmission
+ * ModelConfig are given as line-based text ("key value ..." per line, keys:
+ * forward_model, cross_section_path, wavenumber_file, spectral_discretisation,
+ * spectral_resolution, error_inflation, nb_grid_points, atmos_boundaries,
+ * temperature_profile, radiative_transfer, chemistry, cloud, opacity,
+ * fit_mean_molecular_weight, fit_scale_height, variable_gravity). */
+int bear_model_create(const char* config_text, int device, bear_model** out);
+
+/* One ObservationInput (src/observations/observations.h:42-92,
+ * Observation::init src/observations/observations.cpp:42-111).
+ * type: "spectroscopy" (centers_or_edges = n wavelengths) or "photometry" /
+ * "band-spectroscopy" (centers_or_edges = n x 2 bin edges). weight, fwhm may
+ * be NULL; n_filter = 0 means no filter response. */
+int bear_model_add_observation(bear_model* m, const char* name, const char* type, int n,
+                               const double* centers_or_edges, const double* data,
+                               const double* error, const double* weight, const double* fwhm,
+                               int n_filter, const double* filter_wavelength,
+                               const double* filter_response, const char* detector,
+                               const char* modifier);
+
+/* Builds the spectral grid (SpectralGrid::sampleSpectralGrid,
+ * src/spectral_grid/spectral_grid.cpp:123-157), the observation operators
+ * (src/spectral_grid/spectral_band*.cpp, src/observations/*), loads and
+ * uploads the opacity tables (src/transport_coeff/opacity_species.cpp:44-156,
+ * sampled_data.cpp:48-87) and the device constants. */
+int bear_model_finalize(bear_model* m);
+
+/* The host half of bear_model_finalize (grid, observation operators, tables)
+ * without touching a GPU. bear_model_finalize calls it when needed. After it,
+ * the size and set-up queries below work; evaluations need finalize. */
+int bear_model_prepare(bear_model* m);
+
+/* Set-up of observation k as integers: [obs_index_range.first, .second, n,
+ * n pairs of band-edge indices (SpectralBands::edge_indices), then one pair of
+ * convolution limits per point of the observation range
+ * (SpectralBands::convolution_quadrature_intervals) when an instrument profile
+ * is present]. Returns the number of values written through *written. */
+int bear_model_observation_setup(const bear_model* m, int k, long long* out, int capacity,
+                                 int* written);
+
+/* Row r (internal order, observations concatenated) of the composite
+ * observation operator: bin_r = sum_j weights[j] * spectrum[k0 + j], j < len.
+ * *weights points into the model's host memory (valid until destroy). */
+int bear_model_operator_row(const bear_model* m, int r, int* k0, int* len, const double** weights);
+
+/* Sizes: spectral points N, total observation points M, physical parameters P
+ * (ForwardModel::parametersNumber + 1 with error inflation), observations. */
+int bear_model_info(const bear_model* m, int* nb_spectral_points, int* nb_obs_points,
+                    int* nb_parameters, int* nb_observations);
+/* SpectralGrid::wavenumber_list (src/spectral_grid/spectral_grid.h:41). */
+int bear_model_wavenumbers(const bear_model* m, double* out);
+/* Observation::nbPoints of observation k. */
+int bear_model_observation_size(const bear_model* m, int k, int* n);
+/* Bytes of device memory held by the model (tables, operators, work buffers). */
+int bear_model_device_bytes(const bear_model* m, size_t* bytes);
+void bear_model_destroy(bear_model* m);
+
+/* --------------------------------------------------------------- plain path
+ * ForwardModel::calcModelGPU(params, spectrum_dev, spectrum_obs_dev)
+ * (src/forward_model/forward_model.h:76-79; Emission
+ * src/forward_model/emission/emission.cpp:234-265, Transmission
+ * src/forward_model/transmission/transmission.cpp:257-321).
+ * params: host, nb_params physical parameters. spectrum_dev: device, N
+ * doubles (emission: W m^-2 um^-1 after the unit change; transmission: ppm),
+ * or NULL. obs_dev: array (host memory) of nb_observations device pointers,
+ * each receiving that observation's binned model in the reference's internal
+ * (descending-wavelength) order, or NULL. neglect: host, set to the model's
+ * neglect flag. Synchronises the stream before returning (the reference's
+ * calcModelGPU is synchronous). */
+int bear_forward(bear_model* m, const double* params, int nb_params, double* spectrum_dev,
+                 double* const* obs_dev, int* neglect, void* stream);
+
+/* ForwardModel::calcModel(params, return_high_res) (src/forward_model/
+ * forward_model.cpp:60-127) with host outputs: spectrum (N, may be NULL) and
+ * obs (M, concatenated, each observation in the caller's original order). */
+int bear_compute_model(bear_model* m, const double* params, int nb_params, double* spectrum,
+                       double* obs, int* neglect, void* stream);
+
+/* Retrieval::computeLikelihood (src/retrieval/retrieval.cpp:295-310,
+ * logLikelihoodGPU :374-421): host params, host log-likelihood (-1e30 when
+ * the model is neglected). */
+int bear_loglike(bear_model* m, const double* params, int nb_params, double* loglike,
+                 void* stream);
+
+/* --------------------------------------------------------------- batched path
+ * No reference counterpart (the reference evaluates one point per MultiNest
+ * callback, src/retrieval/multinest_loglike.cpp:152-186). params_dev: device,
+ * batch x nb_params row-major; loglike_dev: device, batch; neglect_dev:
+ * device, batch bytes (NULL allowed). Stream-ordered, no synchronisation. */
+int bear_loglike_batch(bear_model* m, const double* params_dev, int batch, int nb_params,
+                       double* loglike_dev, uint8_t* neglect_dev, void* stream);
+
+/* Gradient of the log-likelihood with respect to the physical parameters by
+ * the engine's adjoint kernels: grad_dev batch x nb_params (device). */
+int bear_loglike_grad_batch(bear_model* m, const double* params_dev, int batch, int nb_params,
+                            double* loglike_dev, double* grad_dev, uint8_t* neglect_dev,
+                            void* stream);
+
+/* Table precision of the batched path: 0 = FP64 tables (default, the plain
+ * path always uses FP64), 1 = FP32 tables with FP64 accumulation. */
+int bear_model_set_precision(bear_model* m, int fp32_tables);
+
+/* Launch configuration of the batched kernels (threads per block along the
+ * spectral axis; 0 = default). Used by the autotuner. */
+int bear_model_set_launch(bear_model* m, int rt_threads, int obs_threads);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BEAR_GB300_H */

@@ -1,0 +1,173 @@
+"""Generates the golden cases under tests/golden/ by running the reference's own
+CPU path (oracle/_ref/bear_ref_harness, built from the reference sources by
+oracle/ref/Makefile) on seeded synthetic inputs.
+
+    make -C oracle/ref && python tests/golden/make_golden.py
+
+Each case: tables from bear_gb300.synthetic (regenerated at test time), a
+config-text template, observations whose data are the reference model at a
+seeded parameter set plus seeded noise, and the reference's outputs for a few
+parameter sets. See tests/goldenlib.py for the file layout.
+"""
+
+from __future__ import annotations
+
+import dataclasses
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+sys.path.insert(0, os.path.dirname(HERE))
+
+import refcase  # noqa: E402
+from bear_gb300 import synthetic as syn  # noqa: E402
+from bear_gb300.config import Observation, observation_arrays, render_config  # noqa: E402
+from goldenlib import GOLDEN_DIR, TABLE_ROOT, save_case, spec_to_meta  # noqa: E402
+
+
+def run_ref(name, template, root, obs, params):
+    d = os.path.join("/tmp", "bear_golden_case_" + name)
+    refcase.write_case(d, template.replace("{ROOT}", root), [observation_arrays(o) for o in obs], params)
+    return refcase.run_case(d)
+
+
+def split_obs(obs, flat):
+    out, off = [], 0
+    for o in obs:
+        out.append(flat[off:off + len(o.data)])
+        off += len(o.data)
+    return out
+
+
+def make(name, spec, kind, template_fn, obs, params, spectrum_rows, attach_kind=None, truth_index=0):
+    root = syn.write_tables(spec, TABLE_ROOT)
+    template = template_fn(render_config(syn.global_config(spec, "{ROOT}", kind), syn.model_config(spec, kind)))
+    # data: the reference model at the truth parameters plus seeded noise
+    first = run_ref(name, template, root, obs, params[truth_index:truth_index + 1])
+    syn.attach_data(obs, split_obs(obs, first["obs"][0]), attach_kind or kind, spec.seed)
+    ref = run_ref(name, template, root, obs, params)
+    arrays = [observation_arrays(o) for o in obs]
+    out = {
+        "ref_loglike": ref["loglike"], "ref_neglect": ref["neglect"], "ref_obs": ref["obs"],
+        "ref_grid": ref["grid"], "spectrum_rows": np.array(spectrum_rows, dtype=np.int64),
+        "ref_spectrum": ref["spectrum"][spectrum_rows],
+    }
+    for k, s in enumerate(ref["setup"]):
+        out[f"ref_setup{k}_range"] = np.array(s["range"], dtype=np.int64)
+        out[f"ref_setup{k}_edges"] = np.array(s["edges"], dtype=np.int64).reshape(-1, 2)
+        out[f"ref_setup{k}_conv"] = np.array(s["conv"], dtype=np.int64).reshape(-1, 2)
+    meta = {"spec": spec_to_meta(spec), "kind": kind, "config_template": template}
+    save_case(os.path.join(GOLDEN_DIR, name + ".npz"), meta, arrays, params, out)
+    print(f"{name}: N={ref['grid'].size} M={ref['obs'].shape[1]} S={params.shape[0]} loglike={ref['loglike']}")
+
+
+def same(t):
+    return t
+
+
+def main():
+    os.makedirs(GOLDEN_DIR, exist_ok=True)
+    which = set(sys.argv[1:])
+
+    # 1. plain emission, the 50-level / 6270-point benchmark workload
+    if not which or "emission_plain" in which:
+        spec = syn.CONFIGS["emission_plain"]
+        obs = syn.observations(spec, "emission")
+        params = np.stack([syn.truth_parameters(spec, "emission", i) for i in range(3)])
+        make("emission_plain", spec, "emission", same, obs, params, [0, 1, 2])
+
+    # 2. plain transmission, 100 levels / 34k points, grey cloud, H2 + He Rayleigh
+    if not which or "transmission_plain" in which:
+        spec = syn.CONFIGS["transmission_plain"]
+        obs = syn.observations(spec, "transmission")
+        params = np.stack([syn.truth_parameters(spec, "transmission", i) for i in range(3)])
+        make("transmission_plain", spec, "transmission", same, obs, params, [0])
+
+    # 3. three observation kinds of the batched workload: R=100 spectrum, bins, 8 filters
+    if not which or "emission_batched" in which:
+        spec = syn.CONFIGS["emission_batched"]
+        obs = syn.observations(spec, "emission")
+        params = np.stack([syn.truth_parameters(spec, "emission", i) for i in range(4)])
+        make("emission_batched", spec, "emission", same, obs, params, [0])
+
+    # 4. emission edge cases: 2 cm^-1 sampling, const T on a table node, grey cloud with
+    #    bottom fraction, K (sodium follows potassium), shift modifier, error inflation,
+    #    ascending / descending / photon-counting observations, a neglected point
+    if not which or "emission_edges" in which:
+        spec = dataclasses.replace(syn.CONFIGS["emission_plain"], name="emission_edges", nb_levels=40,
+                                   species=["H2O", "CO", "K", "Na"], temperature="const", seed=20261210)
+        spec = dataclasses.replace(spec, obs_kind="emission_plain")
+
+        def tmpl(t):
+            t = t.replace("spectral_resolution 1.0", "spectral_resolution 2.0")
+            t = t.replace("error_inflation 0", "error_inflation 1")
+            t = t.replace("temperature_profile poly 5 1", "temperature_profile const")
+            t = t.replace("chemistry iso H2O CO K Na", "chemistry iso H2O CO K")
+            return t + "cloud grey\n"
+        wl = np.linspace(1.4, 4.6, 60)
+        o1 = Observation("asc_spec", "spectroscopy", wl, np.ones(60), np.ones(60))
+        o1.instrument_profile_fwhm = list(wl / 150.0)
+        o1.likelihood_weight = list(np.linspace(0.5, 1.5, 60))
+        o1.spectrum_modifier_id = "shift_const"
+        edges = np.linspace(4.0, 2.2, 21)
+        bins = np.stack([edges[:-1], edges[1:]], axis=1)
+        o2 = Observation("desc_bins", "band-spectroscopy", bins, np.ones(20), np.ones(20))
+        fw = np.linspace(2.05, 2.45, 30)
+        o3 = Observation("photon_filter", "photometry", [[2.45, 2.05]], np.ones(1), np.ones(1))
+        o3.filter_response = [list(fw), list(np.exp(-0.5 * ((fw - 2.25) / 0.08) ** 2))]
+        o3.filter_detector_type = "Photon"
+        obs = [o1, o2, o3]
+        base = [5.0, 1.0, 10 * syn.PARSEC, 3e-4, 1e-4, 2e-7]   # log g, f, d, H2O, CO, K
+        T_node = float(syn.table_nodes(spec.table)[1][8])       # exactly a table temperature
+        rows = []
+        for T, cloud, shift in ((1500.0, [3.0, 0.05, 5.0], 0.0), (T_node, [1.0, 0.3, 3.0], 1e-16),
+                                (2200.0, [0.0, 0.01, 10.0], -2e-16)):
+            rows.append(base + [T] + cloud + [shift, -36.0])
+        bad = list(rows[0])
+        bad[3] = 0.7  # mixing ratios sum above one: neglected, log L = -1e30
+        bad[4] = 0.5
+        rows.append(bad)
+        make("emission_edges", spec, "emission", tmpl, obs, np.array(rows), [0, 1])
+
+    # 5. transmission edge cases: variable gravity, fitted mean molecular weight, poly T,
+    #    ascending bins with an instrument profile, an energy-counting filter, inflation
+    if not which or "transmission_edges" in which:
+        spec = dataclasses.replace(syn.CONFIGS["transmission_plain"], name="transmission_edges", nb_levels=60,
+                                   nu_min=2900.0, nu_max=12100.0, species=["H2O", "CH4", "CO2"],
+                                   temperature="poly", seed=20261211)
+
+        def tmpl(t):
+            t = t.replace("error_inflation 0", "error_inflation 1")
+            t = t.replace("temperature_profile poly 5 1", "temperature_profile poly 3 1")
+            assert "temperature_profile poly 3 1" in t
+            t = t.replace("fit_mean_molecular_weight 0", "fit_mean_molecular_weight 1")
+            t = t.replace("variable_gravity 0", "variable_gravity 1")
+            return t
+        edges = np.geomspace(0.9, 3.3, 41)
+        bins = np.stack([edges[:-1], edges[1:]], axis=1)
+        o1 = Observation("asc_bins", "band-spectroscopy", bins, np.ones(40), np.ones(40))
+        o1.instrument_profile_fwhm = list(np.sqrt(edges[:-1] * edges[1:]) / 200.0)
+        fw = np.linspace(1.1, 1.6, 40)
+        o2 = Observation("energy_filter", "photometry", [[1.1, 1.6]], np.ones(1), np.ones(1))
+        o2.filter_response = [list(fw), list(np.where((fw > 1.2) & (fw < 1.5), 1.0, 0.05))]
+        o2.filter_detector_type = "energy"
+        obs = [o1, o2]
+        rows = []
+        for logg, mmw, T, cl in ((3.0, 2.3, [1400.0, 0.9, 0.95, 0.8], [10.0, 1e-3]),
+                                 (3.3, 2.5, [900.0, 1.1, 0.9, 1.0], [10.0, 1e-2]),
+                                 (2.8, 2.2, [2000.0, 0.8, 0.8, 0.9], [10.0, 3e-4])):
+            rows.append([logg, 1.2 * syn.R_JUPITER, syn.R_SUN, mmw, 1e-4, 1e-5, 1e-6] + T + cl + [2.0])
+        cold = list(rows[0])
+        cold[7] = 60.0   # the profile drops below 50 K: neglected
+        rows.append(cold)
+        make("transmission_edges", spec, "transmission", tmpl, obs, np.array(rows), [0, 1],
+             attach_kind="transmission")
+
+
+if __name__ == "__main__":
+    main()
