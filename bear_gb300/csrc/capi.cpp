@@ -225,6 +225,41 @@ int bear_model_set_launch(bear_model* h, int rt_threads, int obs_threads) {
   });
 }
 
+int bear_model_set_profiling(bear_model* h, int on) {
+  return guarded([&] {
+    require_ready(h);
+    h->m.profiling = on != 0;
+    h->m.ev_recorded = false;
+  });
+}
+
+int bear_model_stage_times(bear_model* h, float* ms3) {
+  return guarded([&] {
+    require_ready(h);
+    if (!ms3) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null output");
+    bgb::stage_times(h->m, ms3);
+  });
+}
+
+int bear_model_table_info(const bear_model* h, int* levels, int* table_species, int* rayleigh_species,
+                          long long* table_rows) {
+  return guarded([&] {
+    require_prepared(h);
+    if (levels) *levels = h->m.L;
+    if (table_species) *table_species = h->m.acfg.S;
+    if (rayleigh_species) *rayleigh_species = h->m.acfg.R;
+    if (table_rows) *table_rows = h->m.n_rows;
+  });
+}
+
+int bear_model_stencil_rows(bear_model* h, int batch, long long* rows) {
+  return guarded([&] {
+    require_ready(h);
+    if (!rows) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null output");
+    *rows = bgb::stencil_rows(h->m, batch);
+  });
+}
+
 int bear_forward(bear_model* h, const double* params, int nb_params, double* spectrum_dev,
                  double* const* obs_dev, int* neglect, void* stream) {
   return guarded([&] {

@@ -405,9 +405,15 @@ void launch_forward(Model& m, const double* params_dev, int batch, cudaStream_t 
   Workspace& w = m.ws;
   const int L = m.L;
   const int atm_threads = ((L + 31) / 32) * 32;
+  if (m.profiling) {
+    for (auto& e : m.ev)
+      if (!e) BGB_CUDA(cudaEventCreate(&e));
+    BGB_CUDA(cudaEventRecord(m.ev[0], st));
+  }
   atmosphere_kernel<<<batch, atm_threads, 4 * L * sizeof(double), st>>>(
       dm, params_dev, dm.P, w.lev, w.ls, ray_n_ptr(m), w.ev);
   BGB_CUDA(cudaGetLastError());
+  if (m.profiling) BGB_CUDA(cudaEventRecord(m.ev[1], st));
   if (!m.transmission) {
     const int TB = m.rt_threads > 0 ? m.rt_threads : (batch == 1 ? 64 : 128);
     dim3 grid(batch, (dm.N + TB - 1) / TB);
@@ -429,11 +435,39 @@ void launch_forward(Model& m, const double* params_dev, int batch, cudaStream_t 
     }
   }
   BGB_CUDA(cudaGetLastError());
+  if (m.profiling) BGB_CUDA(cudaEventRecord(m.ev[2], st));
   const int OT = m.obs_threads > 0 ? m.obs_threads : 256;
   obs_loglike_kernel<<<batch, OT, 0, st>>>(dm, w.spectrum, params_dev, dm.P, w.ev, w.obs,
                                           want_loglike ? (loglike_dev ? loglike_dev : w.loglike) : nullptr,
                                           neglect_dev);
   BGB_CUDA(cudaGetLastError());
+  if (m.profiling) {
+    BGB_CUDA(cudaEventRecord(m.ev[3], st));
+    m.ev_recorded = true;
+  }
+}
+
+void stage_times(Model& m, float* ms3) {
+  if (!m.ev_recorded) throw Error(BEAR_ERR_STATE, "no profiled evaluation recorded");
+  BGB_CUDA(cudaEventSynchronize(m.ev[3]));
+  for (int i = 0; i < 3; ++i) BGB_CUDA(cudaEventElapsedTime(&ms3[i], m.ev[i], m.ev[i + 1]));
+}
+
+long long stencil_rows(Model& m, int batch) {
+  if (batch < 1 || batch > m.ws.capacity) throw Error(BEAR_ERR_SIZE, "batch exceeds the workspace");
+  const size_t n = (size_t)batch * m.L * std::max(m.acfg.S, 1);
+  std::vector<LevelSpecies> h(n);
+  BGB_CUDA(cudaDeviceSynchronize());
+  BGB_CUDA(cudaMemcpy(h.data(), m.ws.ls, n * sizeof(LevelSpecies), cudaMemcpyDeviceToHost));
+  std::vector<char> seen((size_t)m.n_rows, 0);
+  long long count = 0;
+  for (const auto& e : h)
+    for (int r : e.row)
+      if (r >= 0 && r < m.n_rows && !seen[r]) {
+        seen[r] = 1;
+        ++count;
+      }
+  return count;
 }
 
 void launch_spectrum_output(Model& m, double* out_dev, cudaStream_t st) {
@@ -447,6 +481,8 @@ void release_model(Model& m) {
   free_workspace(m.ws);
   for (void* p : m.allocations) cudaFree(p);
   m.allocations.clear();
+  for (auto& e : m.ev)
+    if (e) cudaEventDestroy(e);
   if (m.h_pinned) cudaFreeHost(m.h_pinned);
   m.h_pinned = nullptr;
   (void)g_ray_n_dummy;

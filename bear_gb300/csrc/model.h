@@ -252,6 +252,10 @@ struct Model {
   Workspace ws;
   double* h_pinned = nullptr;  // pinned staging for the plain path
   size_t h_pinned_bytes = 0;
+  // stage timing (bear_model_set_profiling)
+  bool profiling = false;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  bool ev_recorded = false;
 };
 
 // model_setup.cpp
@@ -269,6 +273,8 @@ void release_model(Model& m);
 void launch_forward(Model& m, const double* params_dev, int batch, cudaStream_t stream,
                     bool want_loglike, uint8_t* neglect_dev, double* loglike_dev);
 void launch_spectrum_output(Model& m, double* out_dev, cudaStream_t stream);
+void stage_times(Model& m, float* ms3);
+long long stencil_rows(Model& m, int batch);
 void launch_gradient(Model& m, const double* params_dev, int batch, cudaStream_t stream,
                      double* loglike_dev, double* grad_dev, uint8_t* neglect_dev);
 

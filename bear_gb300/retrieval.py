@@ -171,6 +171,37 @@ class Engine:
     def set_launch(self, rt_threads: int = 0, obs_threads: int = 0) -> None:
         _lib.check(self._lib.bear_model_set_launch(self._h, int(rt_threads), int(obs_threads)))
 
+    def table_info(self) -> dict:
+        L, S, R, rows = C.c_int(), C.c_int(), C.c_int(), C.c_longlong()
+        _lib.check(self._lib.bear_model_table_info(self._h, C.byref(L), C.byref(S), C.byref(R), C.byref(rows)))
+        return {"levels": L.value, "table_species": S.value, "rayleigh_species": R.value, "rows": rows.value}
+
+    @property
+    def table_species(self) -> int:
+        return self.table_info()["table_species"]
+
+    def stencil_row_count(self, batch: int = 1) -> int:
+        """Distinct table rows referenced by the last `batch` evaluations."""
+        n = C.c_longlong()
+        _lib.check(self._lib.bear_model_stencil_rows(self._h, int(batch), C.byref(n)))
+        return n.value
+
+    def stage_times(self, params_ptr: int, batch: int, loglike_ptr: int, stream: int = 0, repeats: int = 3):
+        """Per-stage device times (ms) of a batched evaluation: atmosphere,
+        radiative transfer, observation operator + likelihood (median of repeats)."""
+        _lib.check(self._lib.bear_model_set_profiling(self._h, 1))
+        out = []
+        try:
+            for _ in range(repeats):
+                self.loglike_batch_ptr(params_ptr, batch, loglike_ptr, 0, stream)
+                ms = (C.c_float * 3)()
+                _lib.check(self._lib.bear_model_stage_times(self._h, ms))
+                out.append(list(ms))
+        finally:
+            _lib.check(self._lib.bear_model_set_profiling(self._h, 0))
+        out = np.array(out)
+        return [float(np.median(out[:, i])) for i in range(3)]
+
     def device_bytes(self) -> int:
         b = C.c_size_t()
         _lib.check(self._lib.bear_model_device_bytes(self._h, C.byref(b)))

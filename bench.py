@@ -1,0 +1,410 @@
+"""Benchmark of the GB300 likelihood engine.
+
+Default workload (N=1): batched emission forward model + Gaussian log-likelihood,
+512 live points per launch drawn uniformly over the priors; 80 levels, 6 line
+species + 2 CIA tables on 10 log-p x 20 T, 2000-12000 cm^-1 at 1 cm^-1
+(10257 model points), three observations of 120, 40 and 8 bins (the 8 are
+top-hat / Gaussian bandpass filters). Synthetic seeded tables in the
+reference's on-disk format.
+
+One step = one batch of B likelihood evaluations. ``value`` = evaluations per
+second over the timed steps with parameters resident in HBM; ``e2e`` = the same
+through the host API with the parameter upload and the log-likelihood download
+inside the timed region. L2 is flushed between timed steps (a 512 MiB write)
+outside the per-step event pair.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                    [--workload emission_batched|emission_plain|transmission_plain]
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import platform
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+from bear_gb300 import synthetic as syn  # noqa: E402
+from bear_gb300.config import observation_arrays, render_config  # noqa: E402
+
+WORKLOADS = {
+    "emission_batched": ("emission_batched", "emission"),
+    "emission_adjoint": ("emission_adjoint", "emission"),
+    "emission_plain": ("emission_plain", "emission"),
+    "transmission_plain": ("transmission_plain", "transmission"),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--workload", default="emission_batched", choices=sorted(WORKLOADS))
+    ap.add_argument("--batch", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=0, help="evaluations in the CPU baseline sample")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def synth_dir():
+    return os.environ.get("BEAR_SYNTH_DIR", "/tmp/bear_gb300_synth")
+
+
+def build_case(workload: str):
+    """Tables, config text and observations (data = model at the seeded truth
+    parameters plus 1% noise, computed by the engine itself)."""
+    name, kind = WORKLOADS[workload]
+    spec = syn.CONFIGS[name]
+    root = syn.write_tables(spec, synth_dir())
+    text = render_config(syn.global_config(spec, root, kind), syn.model_config(spec, kind))
+    obs = syn.observations(spec, kind)
+    return spec, kind, text, obs
+
+
+def attach_engine_data(spec, kind, text, obs, device):
+    from bear_gb300.retrieval import Engine
+
+    e0 = Engine(text, [observation_arrays(o) for o in obs], device=device)
+    _, m, _ = e0.compute_model(syn.truth_parameters(spec, kind))
+    e0.close()
+    parts, off = [], 0
+    for o in obs:
+        parts.append(m[off:off + len(o.data)])
+        off += len(o.data)
+    syn.attach_data(obs, parts, kind, spec.seed)
+    return [observation_arrays(o) for o in obs]
+
+
+def live_points(spec, kind, batch, rank):
+    pr = syn.priors(spec, kind)
+    cube = np.random.default_rng(spec.seed + 31 + 1000 * rank).uniform(size=(batch, len(pr)))
+    return syn.cube_to_physical(pr, cube)
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def fp64_peak_tflops(torch, device):
+    """Dense FP64 GEMM rate (cuBLAS) measured here: the FP64 roof of this GPU."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=device)
+    b = torch.randn(n, n, dtype=torch.float64, device=device)
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize(device)
+    best = float("inf")
+    for _ in range(3):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        torch.cuda.synchronize(device)
+        best = min(best, s.elapsed_time(e))
+    del a, b
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def cpu_baseline(text, arrays, params, sample, threads):
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle  # the FP64 CPU restatement of the reference path (a port)
+
+    oracle.set_threads(threads)
+    om = oracle.OracleModel(text, arrays)
+    om.loglike(params[0])  # warm-up
+    t0 = time.perf_counter()
+    for i in range(sample):
+        om.loglike(params[i % len(params)])
+    dt = time.perf_counter() - t0
+    return sample / dt, dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    spec, kind, text, obs = build_case(args.workload)
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    # observation data from the oracle itself (same recipe as the engine arm)
+    arrays0 = [observation_arrays(o) for o in obs]
+    om0 = oracle.OracleModel(text, arrays0)
+    _, m, _ = om0.forward(syn.truth_parameters(spec, kind))
+    parts, off = [], 0
+    for o in obs:
+        parts.append(m[off:off + len(o.data)])
+        off += len(o.data)
+    syn.attach_data(obs, parts, kind, spec.seed)
+    arrays = [observation_arrays(o) for o in obs]
+    om = oracle.OracleModel(text, arrays)
+    B = args.batch or spec.batch
+    params = live_points(spec, kind, B, 0)
+    per_step = max(1, int(os.environ.get("BEAR_REF_EVALS_PER_STEP", "4")))
+    for i in range(args.warmup):
+        om.loglike(params[i % B])
+    times = []
+    idx = 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        for _ in range(per_step):
+            om.loglike(params[idx % B])
+            idx += 1
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = args.steps * per_step / total
+    line = {
+        "impl": "reference", "metric": "likelihood evals/s", "value": value, "unit": "evals/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded tables in the reference format)",
+        "config": {"workload": args.workload, "batch": B, "levels": spec.nb_levels, "spectral_points": om.N,
+                   "bins": om.M, "evals_per_step": per_step},
+        "cpu_baseline": {"value": value, "unit": "evals/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps * per_step} sequential evaluations of the workload's live points"},
+        "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "host": platform.machine(),
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    rank, world, local = dist_env()
+    device = local
+    torch.cuda.set_device(device)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", device))
+
+    from bear_gb300.retrieval import Engine
+
+    spec, kind, text, obs = build_case(args.workload)
+    arrays = attach_engine_data(spec, kind, text, obs, device)
+    eng = Engine(text, arrays, device=device)
+    B = args.batch or spec.batch
+    params_host = live_points(spec, kind, B, rank)
+    P = torch.tensor(params_host, dtype=torch.float64, device=device)
+    ll = torch.empty(B, dtype=torch.float64, device=device)
+    ng = torch.empty(B, dtype=torch.uint8, device=device)
+    stream = torch.cuda.current_stream(device)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+
+    def step():
+        eng.loglike_batch_ptr(P.data_ptr(), B, ll.data_ptr(), ng.data_ptr(), stream.cuda_stream)
+
+    # warm-up
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize(device)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(device)
+
+    # device-resident timing
+    step_ms = []
+    barrier()
+    with ClockSampler(device) as clocks:
+        for _ in range(args.steps):
+            flush.zero_()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            step()
+            e.record(stream)
+            step_ms.append((s, e))
+        barrier()
+    step_ms = [s.elapsed_time(e) for s, e in step_ms]
+    total_ms = sum(step_ms)
+    if dist is not None:
+        t = torch.tensor([total_ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = t.item()
+    value = world * B * args.steps / (total_ms * 1e-3)
+
+    # end-to-end through the host API: pinned params in, log-likelihoods out
+    p_pin = torch.tensor(params_host, dtype=torch.float64).pin_memory()
+    ll_pin = torch.empty(B, dtype=torch.float64).pin_memory()
+    P2 = torch.empty_like(P)
+
+    def e2e_step():
+        P2.copy_(p_pin, non_blocking=True)
+        eng.loglike_batch_ptr(P2.data_ptr(), B, ll.data_ptr(), ng.data_ptr(), stream.cuda_stream)
+        ll_pin.copy_(ll, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    barrier()
+    e2e_ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        e2e_step()
+        e.record(stream)
+        e2e_ms.append((s, e))
+    barrier()
+    e2e_total = sum(s.elapsed_time(e) for s, e in e2e_ms)
+    if dist is not None:
+        t = torch.tensor([e2e_total], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_total = t.item()
+    e2e_value = world * B * args.steps / (e2e_total * 1e-3)
+
+    # plain single-evaluation path (bear_loglike, one host call per evaluation)
+    p0 = params_host[0]
+    for _ in range(3):
+        eng.loglike(p0)
+    n_plain = 50
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    for i in range(n_plain):
+        eng.loglike(params_host[i % B])
+    plain_s = (time.perf_counter() - t0) / n_plain
+
+    # dominant kernel timing for the roofline (CUDA events on the launching stream)
+    stages = eng.stage_times(P.data_ptr(), B, ll.data_ptr(), stream.cuda_stream, repeats=5)
+    kern_ms = stages[1]
+    rows = eng.stencil_row_count(B)
+    N, M, L, S = eng.N, eng.M, spec.nb_levels, eng.table_species
+    # algorithmic bytes of one radiative-transfer launch: every distinct table row the
+    # batch's stencils touch, read once; the per-level stencil records; the spectrum write
+    alg_bytes = rows * N * 8 + B * L * S * 48 + B * N * 8
+    peaks, peak_kind = measured_peaks()
+    achieved_gbs = alg_bytes / (kern_ms * 1e-3) / 1e9
+    fp64_peak = fp64_peak_tflops(torch, device)
+
+    line = None
+    if rank == 0:
+        line = {
+            "metric": "likelihood evals/s", "value": value, "unit": "evals/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded tables in the reference's on-disk format)",
+            "config": {"workload": args.workload, "batch_per_gpu": B, "global_batch": B * world,
+                       "levels": L, "spectral_points": N, "bins": M, "table_species": S,
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                       "l2": "flushed between timed steps (512 MiB write)"},
+            "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": int(P.numel() * 8),
+                    "d2h_bytes_per_step": int(B * 8)},
+            "plain_path": {"evals_per_s": 1.0 / plain_s, "ms_per_eval": plain_s * 1e3,
+                           "api": "bear_loglike (host params in, host log L out)"},
+            "batched_over_plain": value / (1.0 / plain_s),
+            # atmosphere + radiative transfer (+ geometry for transmission) + observation/likelihood
+            "gpu_launches": (3 if kind == "emission" else 4) * args.steps,
+            "roofline": {"bound": "hbm", "kernel": "emission_kernel" if kind == "emission" else "transmission_kernel",
+                         "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": None,
+                         "peak_source": peak_kind, "kernel_ms": kern_ms, "algorithmic_bytes": alg_bytes,
+                         "distinct_table_rows": rows},
+            "stage_ms": {"atmosphere": stages[0], "radiative_transfer": stages[1],
+                         "observation_loglike": stages[2]},
+            "fp64": {"note": "the kernels are bound by FP64 issue, not HBM",
+                     "dgemm_peak_tflops_measured": fp64_peak},
+        }
+    if rank == 0:
+        line["clocks"] = clocks.summary()
+        if not args.no_cpu_baseline:
+            threads = os.cpu_count() or 1
+            sample = args.cpu_sample or (8 if args.workload != "transmission_plain" else 4)
+            v, dt = cpu_baseline(text, arrays, params_host, sample, threads)
+            line["cpu_baseline"] = {"value": v, "unit": "evals/s", "cores": threads, "kind": "port",
+                                    "sample": f"{sample} sequential evaluations of this batch's live points "
+                                              f"({dt:.1f} s), FP64 C oracle with OpenMP"}
+        print(json.dumps(line))
+    eng.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

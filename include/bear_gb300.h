@@ -154,6 +154,22 @@ int bear_model_set_precision(bear_model* m, int fp32_tables);
  * spectral axis; 0 = default). Used by the autotuner. */
 int bear_model_set_launch(bear_model* m, int rt_threads, int obs_threads);
 
+/* --------------------------------------------------------------- measurement
+ * No reference counterpart. With profiling on, every evaluation call records
+ * CUDA events around its three stages (atmosphere, radiative transfer,
+ * observation operator + likelihood) on the launching stream;
+ * bear_model_stage_times waits for the last call's events and returns the
+ * three durations in milliseconds. */
+int bear_model_set_profiling(bear_model* m, int on);
+int bear_model_stage_times(bear_model* m, float* ms3);
+
+/* Table layout and the number of distinct table rows referenced by the
+ * stencils of the last `batch` evaluations (for algorithmic-byte accounting;
+ * copies the stencils to the host and synchronises). */
+int bear_model_table_info(const bear_model* m, int* levels, int* table_species,
+                          int* rayleigh_species, long long* table_rows);
+int bear_model_stencil_rows(bear_model* m, int batch, long long* distinct_rows);
+
 #ifdef __cplusplus
 }
 #endif
