@@ -335,6 +335,16 @@ int bear_loglike_batch(bear_model* h, const double* params_dev, int batch, int n
   });
 }
 
+int bear_loglike_noalloc(bear_model* h, const double* params_dev, int nb_params, double* loglike_dev,
+                         uint8_t* neglect_dev, void* stream) {
+  return guarded([&] {
+    require_ready(h);
+    require_params(h, nb_params);
+    if (!params_dev || !loglike_dev) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null device buffer");
+    bgb::loglike_noalloc(h->m, params_dev, loglike_dev, neglect_dev, (cudaStream_t)stream);
+  });
+}
+
 int bear_loglike_grad_batch(bear_model* h, const double* params_dev, int batch, int nb_params,
                             double* loglike_dev, double* grad_dev, uint8_t* neglect_dev,
                             void* stream) {

@@ -447,6 +447,36 @@ void launch_forward(Model& m, const double* params_dev, int batch, cudaStream_t 
   }
 }
 
+// One evaluation with caller-supplied work buffers (used by the allocation-free
+// entry point): the kernels and launch shapes of the plain path, no workspace
+// growth, no profiling events.
+void launch_forward_into(Model& m, const double* params_dev, const Workspace& w, double* ray_n,
+                         cudaStream_t st, uint8_t* neglect_dev, double* loglike_dev) {
+  const DeviceModel& dm = m.dm;
+  const int L = m.L;
+  const int atm_threads = ((L + 31) / 32) * 32;
+  atmosphere_kernel<<<1, atm_threads, 4 * L * sizeof(double), st>>>(dm, params_dev, dm.P, w.lev, w.ls,
+                                                                    ray_n, w.ev);
+  BGB_CUDA(cudaGetLastError());
+  if (!m.transmission) {
+    const int TB = m.rt_threads > 0 ? m.rt_threads : 64;
+    dim3 grid(1, (dm.N + TB - 1) / TB);
+    emission_kernel<double><<<grid, TB, 0, st>>>(dm, dm.table64, w.lev, w.ls, w.ev, w.spectrum);
+  } else {
+    transmission_geometry_kernel<<<1, 256, 0, st>>>(dm, w.lev, w.ev, w.geom);
+    const int TB = m.rt_threads > 0 ? std::min(m.rt_threads, 128) : 64;
+    dim3 grid(1, (dm.N + TB - 1) / TB);
+    const size_t sm = (size_t)L * TB * sizeof(double);
+    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    transmission_kernel<double><<<grid, TB, sm, st>>>(dm, dm.table64, w.lev, w.ls, ray_n, w.ev, w.geom,
+                                                      w.spectrum);
+  }
+  BGB_CUDA(cudaGetLastError());
+  const int OT = m.obs_threads > 0 ? m.obs_threads : 256;
+  obs_loglike_kernel<<<1, OT, 0, st>>>(dm, w.spectrum, params_dev, dm.P, w.ev, w.obs, loglike_dev, neglect_dev);
+  BGB_CUDA(cudaGetLastError());
+}
+
 void stage_times(Model& m, float* ms3) {
   if (!m.ev_recorded) throw Error(BEAR_ERR_STATE, "no profiled evaluation recorded");
   BGB_CUDA(cudaEventSynchronize(m.ev[3]));

@@ -274,6 +274,9 @@ void launch_forward(Model& m, const double* params_dev, int batch, cudaStream_t 
                     bool want_loglike, uint8_t* neglect_dev, double* loglike_dev);
 void launch_spectrum_output(Model& m, double* out_dev, cudaStream_t stream);
 void stage_times(Model& m, float* ms3);
+// noalloc.cu
+void loglike_noalloc(Model& m, const double* params_dev, double* loglike_dev, uint8_t* neglect_dev,
+                     cudaStream_t stream);
 long long stencil_rows(Model& m, int batch);
 void launch_gradient(Model& m, const double* params_dev, int batch, cudaStream_t stream,
                      double* loglike_dev, double* grad_dev, uint8_t* neglect_dev);

@@ -1,0 +1,117 @@
+// Single-evaluation log-likelihood that allocates no memory at call time.
+//
+// Who needs this: callers that may not allocate device memory while they run --
+// code executing inside a CUDA stream capture (cudaMalloc is not capturable),
+// processes whose device memory is owned by another framework's pool or by a
+// strict budget, and real-time callbacks (for example a sampler's per-point
+// likelihood hook) that must not block on the allocator. The regular entry
+// points grow a per-model workspace with cudaMalloc the first time a batch size
+// is seen; this one instead keeps the per-evaluation work buffers (level and
+// stencil records, the high-resolution spectrum, the binned spectrum, the
+// transmission path lengths) in one fixed array in device memory declared below.
+//
+// The array is a file-scope __device__ variable, so every GPU that loads the
+// library holds kNoAllocScratchBytes of it until the process exits, whether or
+// not this entry point is used. Host code cannot use the array's name as a
+// device address; its address is looked up with cudaGetSymbolAddress once per
+// device (with that device current) on the first call made for a model on that
+// device. Make that first call before any stream capture starts.
+//
+// Every call on a device shares the same array, and each call overwrites what
+// the previous one left there: every element a call reads is written earlier in
+// the same call, so nothing needs clearing. Calls whose executions can overlap
+// on the GPU (different streams without ordering between them, or different
+// models on the same device) race on the array and must be serialised by the
+// caller.
+
+#include <mutex>
+#include <string>
+
+#include "../../include/bear_gb300.h"
+#include "model.h"
+
+namespace bgb {
+
+constexpr size_t kNoAllocScratchBytes = size_t(2) << 20;  // 2 MiB per device
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+void launch_forward_into(Model& m, const double* params_dev, const Workspace& w, double* ray_n,
+                         cudaStream_t st, uint8_t* neglect_dev, double* loglike_dev);
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mutex;
+void* g_scratch_addr[kMaxDevices] = {};
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Carves the single-evaluation work buffers out of the scratch array; returns
+// the bytes needed (and fills w / ray_n when base is not null).
+size_t layout(const Model& m, unsigned char* base, Workspace* w, double** ray_n) {
+  const size_t L = m.L, S = std::max(m.acfg.S, 1), R = std::max(m.acfg.R, 1);
+  const size_t N = m.N, M = std::max(m.M, 1);
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t at = off;
+    off = align256(off + bytes);
+    return base ? base + at : nullptr;
+  };
+  unsigned char* lev = take(L * sizeof(LevelInfo));
+  unsigned char* ls = take(L * S * sizeof(LevelSpecies));
+  unsigned char* rn = take(L * R * sizeof(double));
+  unsigned char* ev = take(sizeof(EvalInfo));
+  unsigned char* spec = take(N * sizeof(double));
+  unsigned char* obs = take(M * sizeof(double));
+  unsigned char* geom = m.transmission ? take(L * L * sizeof(double)) : nullptr;
+  if (base) {
+    *w = Workspace{};
+    w->capacity = 1;
+    w->lev = reinterpret_cast<LevelInfo*>(lev);
+    w->ls = reinterpret_cast<LevelSpecies*>(ls);
+    w->ev = reinterpret_cast<EvalInfo*>(ev);
+    w->spectrum = reinterpret_cast<double*>(spec);
+    w->obs = reinterpret_cast<double*>(obs);
+    w->geom = reinterpret_cast<double*>(geom);
+    *ray_n = reinterpret_cast<double*>(rn);
+  }
+  return off;
+}
+
+unsigned char* scratch_for_device(int device) {
+  if (device < 0 || device >= kMaxDevices) throw Error(BEAR_ERR_INVALID_INPUT, "device index out of range");
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  if (!g_scratch_addr[device]) {
+    int previous = 0;
+    cudaError_t e = cudaGetDevice(&previous);
+    if (e != cudaSuccess) throw Error(BEAR_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) throw Error(BEAR_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+    void* ptr = nullptr;
+    e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    cudaSetDevice(previous);
+    if (e != cudaSuccess || !ptr)
+      throw Error(BEAR_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+    g_scratch_addr[device] = ptr;
+  }
+  return static_cast<unsigned char*>(g_scratch_addr[device]);
+}
+
+}  // namespace
+
+void loglike_noalloc(Model& m, const double* params_dev, double* loglike_dev, uint8_t* neglect_dev,
+                     cudaStream_t st) {
+  const size_t need = layout(m, nullptr, nullptr, nullptr);
+  if (need > kNoAllocScratchBytes)
+    throw Error(BEAR_ERR_SIZE, "this model needs " + std::to_string(need) +
+                                   " bytes of per-evaluation scratch; the allocation-free entry point is limited to " +
+                                   std::to_string(kNoAllocScratchBytes) + " bytes");
+  unsigned char* base = scratch_for_device(m.device);
+  Workspace w;
+  double* ray_n = nullptr;
+  layout(m, base, &w, &ray_n);
+  launch_forward_into(m, params_dev, w, ray_n, st, neglect_dev, loglike_dev);
+}
+
+}  // namespace bgb

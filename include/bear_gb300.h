@@ -154,6 +154,21 @@ int bear_model_set_precision(bear_model* m, int fp32_tables);
  * spectral axis; 0 = default). Used by the autotuner. */
 int bear_model_set_launch(bear_model* m, int rt_threads, int obs_threads);
 
+/* Allocation-free log-likelihood of one parameter set. No counterpart in the
+ * reference. For callers that cannot allocate device memory during the call:
+ * inside a CUDA stream capture, under a foreign memory pool or budget, or in a
+ * latency-bound per-point callback. params_dev: device, nb_params doubles;
+ * loglike_dev: device, 1 double (-1e30 when neglected); neglect_dev: device,
+ * 1 byte (NULL allowed). The per-evaluation work buffers live in a fixed
+ * 2 MiB device array that every GPU loading the library holds until exit;
+ * models needing more scratch than that are rejected with BEAR_ERR_SIZE. The
+ * first call for a model's device looks up the array's address with
+ * cudaGetSymbolAddress: make it before any stream capture. All calls on a
+ * device share the array: calls that may overlap on the GPU race and must be
+ * serialised by the caller. Stream-ordered; does not synchronise. */
+int bear_loglike_noalloc(bear_model* m, const double* params_dev, int nb_params,
+                         double* loglike_dev, uint8_t* neglect_dev, void* stream);
+
 /* --------------------------------------------------------------- measurement
  * No reference counterpart. With profiling on, every evaluation call records
  * CUDA events around its three stages (atmosphere, radiative transfer,
