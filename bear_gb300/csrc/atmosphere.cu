@@ -7,6 +7,7 @@
 // with the reference on the same parameters.
 
 #include "model.h"
+#include "dfloat.cuh"
 
 namespace bgb {
 
@@ -59,7 +60,8 @@ __device__ double mean_molecular_weight(const double* n) {
 // One block per evaluation, blockDim.x >= L. Dynamic shared memory: 4 L doubles.
 __global__ void __launch_bounds__(kMaxLevels) atmosphere_kernel(DeviceModel dm, const double* __restrict__ params, int P,
                                   LevelInfo* __restrict__ lev, LevelSpecies* __restrict__ ls,
-                                  double* __restrict__ ray_n, EvalInfo* __restrict__ ev) {
+                                  LevelSpeciesDF* __restrict__ lsdf, double* __restrict__ ray_n,
+                                  EvalInfo* __restrict__ ev) {
   const AtmosphereConfig& c = *dm.cfg;
   const int b = blockIdx.x;
   const int l = threadIdx.x;
@@ -158,6 +160,17 @@ __global__ void __launch_bounds__(kMaxLevels) atmosphere_kernel(DeviceModel dm, 
       if (c.sp_partner[s][0] >= 0) nd *= n[c.sp_partner[s][0]];
       if (c.sp_partner[s][1] >= 0) nd *= n[c.sp_partner[s][1]];
       ls[((size_t)b * L + l) * S + s].n = nd;
+      // log2 of the density for the double-float path; a zero density skips the
+      // species like the reference's early return (opacity_species.cpp:412)
+      LevelSpeciesDF& f = lsdf[((size_t)b * L + l) * S + s];
+      if (nd > 0) {
+        const df2 lg = df_from_double(log2(nd));
+        f.lg2n_hi = lg.hi;
+        f.lg2n_lo = lg.lo;
+      } else {
+        f.lg2n_hi = kNoSpecies;
+        f.lg2n_lo = 0.0f;
+      }
     }
     for (int r = 0; r < c.R; ++r) ray_n[((size_t)b * L + l) * c.R + r] = n[c.ray_index[r]];
     if (neglect) atomicOr(&s_neglect, 1);
@@ -266,7 +279,9 @@ __global__ void __launch_bounds__(kMaxLevels) atmosphere_kernel(DeviceModel dm, 
       else if (l >= 1) cl = layer_tau(l - 1) / (sz[l] - sz[l - 1]);  // CloudModel::convertOpticalDepth src/cloud_model/cloud_model.h:67-88
     }
     li.cloud = cl;
-    li.pad = 0;
+    const df2 it = df_from_double(li.invT);
+    li.invT_hi = it.hi;
+    li.invT_lo = it.lo;
     lev[(size_t)b * L + l] = li;
     // table stencils: OpacitySpecies::findClosestDataPoints src/transport_coeff/opacity_species.cpp:160-273
     for (int s = 0; s < S; ++s) {
@@ -293,6 +308,14 @@ __global__ void __launch_bounds__(kMaxLevels) atmosphere_kernel(DeviceModel dm, 
       e.wp_lo = dm.pb_w[ilo];
       e.wp_hi = dm.pb_w[iup];
       e.wT = (lo != up) ? (T - Tn[lo]) / (Tn[up] - Tn[lo]) : 0.0;
+      LevelSpeciesDF& f = lsdf[((size_t)b * L + l) * S + s];
+      const df2 a = df_from_double(e.wp_lo), bw = df_from_double(e.wp_hi), t = df_from_double(e.wT);
+      f.wp_lo_hi = a.hi;
+      f.wp_lo_lo = a.lo;
+      f.wp_hi_hi = bw.hi;
+      f.wp_hi_lo = bw.lo;
+      f.wT_hi = t.hi;
+      f.wT_lo = t.lo;
     }
   }
 }

@@ -208,10 +208,11 @@ void bear_model_destroy(bear_model* h) {
   delete h;
 }
 
-int bear_model_set_precision(bear_model* h, int fp32_tables) {
+int bear_model_set_precision(bear_model* h, int mode) {
   return guarded([&] {
     if (!h) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null model");
-    h->m.fp32_tables = fp32_tables != 0;
+    if (mode != 0 && mode != 1) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "precision mode must be 0 or 1");
+    h->m.precision = mode;
   });
 }
 

@@ -1,0 +1,181 @@
+// Double-float arithmetic on the FP32 pipe and table-driven exponentials.
+//
+// On GB300 the FP32 pipe issues ~67x more operations per clock than the FP64
+// pipe (measured: 3.4e13 FFMA/s vs 5.0e11 DFMA/s), so FP64-accurate work that
+// does not need FP64's exponent range is done here in double-float form: a value
+// is an unevaluated sum hi + lo of two floats (about 48 significant bits).
+// Error-free transformations: Knuth's TwoSum, Dekker's Fast2Sum, and the
+// FMA-based TwoProduct. Exponentials use Tang's table-driven method (Tang 1989,
+// ACM TOMS 15:144): 2^y = 2^n * 2^(j/64) * 2^r with |r| <= 1/128 and a short
+// Taylor polynomial for 2^r.
+//
+// Every operation is written with round-to-nearest intrinsics, which the
+// compiler never contracts or reassociates. With BGB_HOST_EMULATION the same
+// code compiles on the host (used to check the routines' accuracy on a CPU).
+#pragma once
+
+#include <cstdint>
+
+#ifdef BGB_HOST_EMULATION
+#include <cmath>
+#include <cstring>
+#define BGB_HD inline
+#define BGB_FADD(a, b) ((float)((a) + (b)))
+#define BGB_FSUB(a, b) ((float)((a) - (b)))
+#define BGB_FMUL(a, b) ((float)((a) * (b)))
+#define BGB_FMA(a, b, c) std::fmaf((a), (b), (c))
+#define BGB_FDIV(a, b) ((float)((a) / (b)))
+#define BGB_RINTF(x) std::rintf(x)
+#define BGB_DMA(a, b, c) std::fma((a), (b), (c))
+static inline float bgb_int_as_float(int i) { float f; std::memcpy(&f, &i, 4); return f; }
+static inline long long bgb_double_as_ll(double d) { long long i; std::memcpy(&i, &d, 8); return i; }
+static inline double bgb_ll_as_double(long long i) { double d; std::memcpy(&d, &i, 8); return d; }
+#else
+#define BGB_HD __device__ __forceinline__
+#define BGB_FADD(a, b) __fadd_rn((a), (b))
+#define BGB_FSUB(a, b) __fsub_rn((a), (b))
+#define BGB_FMUL(a, b) __fmul_rn((a), (b))
+#define BGB_FMA(a, b, c) __fmaf_rn((a), (b), (c))
+#define BGB_FDIV(a, b) __fdiv_rn((a), (b))
+#define BGB_RINTF(x) rintf(x)
+#define BGB_DMA(a, b, c) __fma_rn((a), (b), (c))
+#define bgb_int_as_float(i) __int_as_float(i)
+#define bgb_double_as_ll(d) __double_as_longlong(d)
+#define bgb_ll_as_double(i) __longlong_as_double(i)
+#endif
+
+#include "dfconst.h"
+
+namespace bgb {
+
+struct df2 {
+  float hi, lo;
+};
+
+BGB_HD df2 df_make(float hi) { return {hi, 0.0f}; }
+
+// Split an FP64 value into a double-float (exact for |x| in the float range).
+BGB_HD df2 df_from_double(double x) {
+  const float hi = (float)x;
+  return {hi, (float)(x - (double)hi)};
+}
+
+BGB_HD double df_to_double(df2 a) { return (double)a.hi + (double)a.lo; }
+
+// TwoSum: s + e == a + b exactly.
+BGB_HD df2 two_sum(float a, float b) {
+  const float s = BGB_FADD(a, b);
+  const float bb = BGB_FSUB(s, a);
+  const float e = BGB_FADD(BGB_FSUB(a, BGB_FSUB(s, bb)), BGB_FSUB(b, bb));
+  return {s, e};
+}
+
+// Fast2Sum for |a| >= |b|.
+BGB_HD df2 fast_two_sum(float a, float b) {
+  const float s = BGB_FADD(a, b);
+  return {s, BGB_FSUB(b, BGB_FSUB(s, a))};
+}
+
+BGB_HD df2 df_add(df2 a, df2 b) {
+  const df2 s = two_sum(a.hi, b.hi);
+  return fast_two_sum(s.hi, BGB_FADD(s.lo, BGB_FADD(a.lo, b.lo)));
+}
+
+BGB_HD df2 df_neg(df2 a) { return {-a.hi, -a.lo}; }
+
+BGB_HD df2 df_sub(df2 a, df2 b) { return df_add(a, df_neg(b)); }
+
+BGB_HD df2 df_mul(df2 a, df2 b) {
+  const float p = BGB_FMUL(a.hi, b.hi);
+  float e = BGB_FMA(a.hi, b.hi, -p);
+  e = BGB_FMA(a.hi, b.lo, e);
+  e = BGB_FMA(a.lo, b.hi, e);
+  return fast_two_sum(p, e);
+}
+
+BGB_HD df2 df_mul_f(df2 a, float b) {
+  const float p = BGB_FMUL(a.hi, b);
+  float e = BGB_FMA(a.hi, b, -p);
+  e = BGB_FMA(a.lo, b, e);
+  return fast_two_sum(p, e);
+}
+
+// a / b with three correction steps (quotient digits q1 + q2 + q3).
+BGB_HD df2 df_div(df2 a, df2 b) {
+  const float q1 = BGB_FDIV(a.hi, b.hi);
+  df2 r = df_sub(a, df_mul_f(b, q1));
+  const float q2 = BGB_FDIV(r.hi, b.hi);
+  r = df_sub(r, df_mul_f(b, q2));
+  const float q3 = BGB_FDIV(r.hi, b.hi);
+  return df_add(fast_two_sum(q1, q2), df_make(q3));
+}
+
+// a + (b - a) * w, the reference's linear interpolation step.
+BGB_HD df2 df_lerp(df2 a, df2 b, df2 w) { return df_add(a, df_mul(df_sub(b, a), w)); }
+
+// 2^y for a double-float y, returned as a double-float mantissa m (1/sqrt2 <= m < 2)
+// and an integer exponent: 2^y = m * 2^n. Relative error ~1e-14.
+// tab_hi / tab_lo: 2^(j/64), j = -32..32 (index j + 32).
+BGB_HD df2 df_exp2(df2 y, int& n, const float* tab_hi, const float* tab_lo) {
+  const float nf = BGB_RINTF(y.hi);
+  n = (int)nf;
+  const df2 f = fast_two_sum(BGB_FSUB(y.hi, nf), y.lo);        // |f| <= 1/2, y.hi - nf exact
+  const float jf = BGB_RINTF(BGB_FMUL(f.hi, 64.0f));
+  const int j = (int)jf;
+  const df2 r = fast_two_sum(BGB_FSUB(f.hi, BGB_FMUL(jf, 0.015625f)), f.lo);  // |r| <= 1/128
+  // t = r ln2; 2^r = 1 + t + t^2/2 + t^3/6 + t^4/24 + t^5/120 (+ |t|^6/720 < 3.5e-17)
+  const df2 t = df_mul(r, df2{kLn2Hi, kLn2Lo});
+  const float th = t.hi;
+  const float tail = BGB_FMUL(BGB_FMUL(BGB_FMUL(th, th), th),
+                              BGB_FMA(th, BGB_FMA(th, 1.0f / 120.0f, 1.0f / 24.0f), 1.0f / 6.0f));
+  const float sq = BGB_FMUL(th, th);
+  const float sq_err = BGB_FMA(th, th, -sq);
+  df2 half_t2 = fast_two_sum(BGB_FMUL(sq, 0.5f), BGB_FMUL(BGB_FMA(2.0f * th, t.lo, sq_err), 0.5f));
+  df2 s = df_add(half_t2, df_make(tail));
+  s = df_add(t, s);
+  const df2 p = fast_two_sum(1.0f, s.hi);
+  const df2 e = fast_two_sum(p.hi, BGB_FADD(p.lo, s.lo));
+  const df2 T = {tab_hi[j + 32], tab_lo[j + 32]};
+  return df_mul(T, e);
+}
+
+// 2^(float exponent) as a float, for n in [-126, 127]; 0 below.
+BGB_HD float pow2f(int n) { return n < -126 ? 0.0f : bgb_int_as_float((n + 127) << 23); }
+
+// Multiply a double-float by 2^n (exact unless it under/overflows the float range).
+BGB_HD df2 df_ldexp(df2 a, int n) {
+  if (n >= -126) {
+    const float s = pow2f(n);
+    return {BGB_FMUL(a.hi, s), BGB_FMUL(a.lo, s)};
+  }
+  // two steps for the lowest exponents (flushes below the float range)
+  const float s1 = pow2f(-126), s2 = pow2f(n + 126);
+  return {BGB_FMUL(BGB_FMUL(a.hi, s1), s2), BGB_FMUL(BGB_FMUL(a.lo, s1), s2)};
+}
+
+// 2^n as a double for n in [-1022, 1023]; 0 below.
+BGB_HD double pow2d(int n) { return n < -1022 ? 0.0 : bgb_ll_as_double((long long)(n + 1023) << 52); }
+
+// exp(x) in FP64 by Tang's method: x = k ln2/64 + r (Cody-Waite with a two-part
+// ln2/64 and FMA), |r| <= ln2/128, degree-5 Taylor polynomial, table 2^(j/64)
+// (tab: 64 doubles, j = k mod 64), scaling by 2^(k div 64) in the exponent field.
+// Valid for x in [-700, 700]; about 1 ulp.
+BGB_HD double exp_tang(double x, const double* tab) {
+  const double shifter = 6755399441055744.0;  // 1.5 * 2^52: rounds to an integer
+  const double t = BGB_DMA(x, k64OverLn2, shifter);
+  const double kd = t - shifter;
+  const int k = (int)(bgb_double_as_ll(t) & 0xffffffff);
+  double r = BGB_DMA(-kd, kLn2Over64Hi, x);
+  r = BGB_DMA(-kd, kLn2Over64Lo, r);
+  double p = BGB_DMA(r, 1.0 / 120.0, 1.0 / 24.0);
+  p = BGB_DMA(r, p, 1.0 / 6.0);
+  p = BGB_DMA(r, p, 0.5);
+  p = BGB_DMA(r * r, p, r);
+  const int j = k & 63;
+  const int m = k >> 6;  // arithmetic shift: floor(k / 64)
+  const double T = tab[j];
+  const double scaled = bgb_ll_as_double(bgb_double_as_ll(T) + ((long long)m << 52));
+  return BGB_DMA(scaled, p, scaled);
+}
+
+}  // namespace bgb

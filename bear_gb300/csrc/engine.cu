@@ -1,9 +1,11 @@
 // GB300 kernels of the likelihood engine and their host-side launch code.
 //
 // Data layout in HBM
-//   tables      rows x N, log10 cross sections, wavenumber contiguous (one row
-//               per (species, T, p) table point, sampled on the model grid)
-//   LevelSpecies B x L x S, LevelInfo B x L, EvalInfo B: per-evaluation
+//   tables      rows x N log10 cross sections, wavenumber contiguous (one row per
+//               (species, T, p) table point, sampled on the model grid), stored
+//               twice: as double-floats (float2, the default path) and as FP64
+//               (the validation path)
+//   LevelSpecies(+DF) B x L x S, LevelInfo B x L, EvalInfo B: per-evaluation
 //               atmosphere and stencils written by atmosphere_kernel
 //   spectrum    B x N native units (per cm^-1 flux or ppm transit depth)
 //   W           banded observation operator, one contiguous row per bin
@@ -19,6 +21,14 @@
 // Grids put the evaluation index on blockIdx.x and the wavenumber tile on
 // blockIdx.y, so the blocks resident at any time share one wavenumber tile of
 // the tables in L2.
+//
+// Arithmetic. This GPU issues ~67x more FP32 than FP64 operations per clock.
+// The default kernels therefore assemble opacities in double-float arithmetic
+// on the FP32 pipe (interpolation, 10^x via Tang's table method, accumulation;
+// ~1e-12 relative) and evaluate the Planck function the same way; the
+// short-characteristics recurrence and the tangent-ray sums stay FP64 with a
+// table-driven FP64 exponential. The *_fp64 kernels do every step in FP64 with
+// the CUDA math library and serve as the validation path (precision mode 1).
 
 #include <algorithm>
 #include <cmath>
@@ -28,6 +38,7 @@
 
 #include "../../include/bear_gb300.h"
 #include "model.h"
+#include "physics.cuh"
 
 namespace bgb {
 
@@ -40,33 +51,66 @@ namespace bgb {
 
 __global__ void atmosphere_kernel(DeviceModel dm, const double* __restrict__ params, int P,
                                   LevelInfo* __restrict__ lev, LevelSpecies* __restrict__ ls,
-                                  double* __restrict__ ray_n, EvalInfo* __restrict__ ev);
+                                  LevelSpeciesDF* __restrict__ lsdf, double* __restrict__ ray_n,
+                                  EvalInfo* __restrict__ ev);
 
-// Gauss nodes and weights of ShortCharacteristics (src/radiative_transfer/short_characteristics.h:62-63)
+// Dynamic shared memory the transmission kernels opt into (the per-block maximum of
+// 227 KB less room for their static tables).
+constexpr size_t kTransmissionDynSmem = 225 * 1024;
+
+// Gauss nodes of ShortCharacteristics (src/radiative_transfer/short_characteristics.h:62-63)
 __device__ __constant__ double kMu[2] = {0.211324865405187, 0.788675134594813};
 __device__ __constant__ double kInvMu[2] = {1.0 / 0.211324865405187, 1.0 / 0.788675134594813};
 
-template <typename TT>
-__device__ __forceinline__ double load_table(const TT* __restrict__ tab, size_t idx) {
-  return (double)__ldg(tab + idx);
+__device__ __forceinline__ void load_exp_tables(ExpTables& t) {
+  for (int i = threadIdx.x; i < 65; i += blockDim.x) {
+    t.hi[i] = kExp2TabHi[i];
+    t.lo[i] = kExp2TabLo[i];
+  }
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) t.d[i] = kExp2TabD[i];
 }
 
+// ------------------------------------------------------------------ opacity
 // Sum over table species of 10^(bilinear log-p / T interpolation) * n at one
 // level and one wavenumber (OpacitySpecies::calcAbsorptionCrossSections
-// src/transport_coeff/opacity_species.cpp:277-345 and calcTransportCoefficients :400-455).
-template <typename TT>
-__device__ __forceinline__ double level_absorption(const TT* __restrict__ tab, size_t N,
-                                                   const LevelSpecies* __restrict__ d, int S,
-                                                   int k) {
+// src/transport_coeff/opacity_species.cpp:277-345 and calcTransportCoefficients
+// :400-455), double-float arithmetic; FP64 result.
+__device__ __forceinline__ double level_absorption_df(const float2* __restrict__ tab, size_t N,
+                                                      const LevelSpecies* __restrict__ d,
+                                                      const LevelSpeciesDF* __restrict__ f, int S,
+                                                      int k, const ExpTables& et) {
+  df2 acc = {0.0f, 0.0f};
+  double wide = 0.0;
+  for (int s = 0; s < S; ++s) {
+    const float4 fa = __ldg(reinterpret_cast<const float4*>(f + s));
+    const float4 fb = __ldg(reinterpret_cast<const float4*>(f + s) + 1);
+    if (fb.z == kNoSpecies) continue;  // zero number density: the species adds nothing
+    const int4 r = __ldg(reinterpret_cast<const int4*>(d + s));
+    const float2 t0 = __ldg(tab + (size_t)r.x * N + k);
+    const float2 t1 = __ldg(tab + (size_t)r.y * N + k);
+    const float2 t2 = __ldg(tab + (size_t)r.z * N + k);
+    const float2 t3 = __ldg(tab + (size_t)r.w * N + k);
+    const df2 lo = df_lerp(df2{t0.x, t0.y}, df2{t1.x, t1.y}, df2{fa.x, fa.y});
+    const df2 hi = df_lerp(df2{t2.x, t2.y}, df2{t3.x, t3.y}, df2{fa.z, fa.w});
+    const df2 x = df_lerp(lo, hi, df2{fb.x, fb.y});
+    pow10_times_n(x, df2{fb.z, fb.w}, et.hi, et.lo, acc, wide);
+  }
+  return df_to_double(acc) + wide;
+}
+
+// The same in FP64 with the CUDA math library (validation path).
+__device__ __forceinline__ double level_absorption_fp64(const double* __restrict__ tab, size_t N,
+                                                        const LevelSpecies* __restrict__ d, int S,
+                                                        int k) {
   double kap = 0.0;
   for (int s = 0; s < S; ++s) {
     const int4 r = __ldg(reinterpret_cast<const int4*>(d + s));
     const double2 w = __ldg(reinterpret_cast<const double2*>(&d[s].wp_lo));
     const double2 t = __ldg(reinterpret_cast<const double2*>(&d[s].wT));
-    const double v0 = load_table(tab, (size_t)r.x * N + k);
-    const double v1 = load_table(tab, (size_t)r.y * N + k);
-    const double v2 = load_table(tab, (size_t)r.z * N + k);
-    const double v3 = load_table(tab, (size_t)r.w * N + k);
+    const double v0 = __ldg(tab + (size_t)r.x * N + k);
+    const double v1 = __ldg(tab + (size_t)r.y * N + k);
+    const double v2 = __ldg(tab + (size_t)r.z * N + k);
+    const double v3 = __ldg(tab + (size_t)r.w * N + k);
     const double lo = v0 + (v1 - v0) * w.x;
     const double hi = v2 + (v3 - v2) * w.y;
     const double x = lo + (hi - lo) * t.x;
@@ -75,17 +119,71 @@ __device__ __forceinline__ double level_absorption(const TT* __restrict__ tab, s
   return kap;
 }
 
-// Fused opacity assembly + two-stream short characteristics, one thread per
-// wavenumber (ShortCharacteristics::calcSpectrum
-// src/radiative_transfer/short_characteristics.cpp:39-125; Planck function
-// src/additional/aux_functions.cpp:272-278). Writes the flux in W m^-2 cm
-// times the radius-distance scaling.
-template <typename TT>
-__global__ void __launch_bounds__(256) emission_kernel(DeviceModel dm, const TT* __restrict__ tab,
-                                                       const LevelInfo* __restrict__ lev,
+// One layer of the two-angle short-characteristics recurrence
+// (ShortCharacteristics::calcSpectrum src/radiative_transfer/short_characteristics.cpp:85-115):
+// delta = tau/mu, a = exp(-delta), I <- I a + (1 + (a-1)/delta) B_top + (-a - (a-1)/delta) B_bottom.
+template <bool TANG>
+__device__ __forceinline__ void sc_layer(double tau, double B, double B_prev, double& I1, double& I2,
+                                         const double* tab) {
+  if (tau == 0) return;  // the reference skips exactly transparent layers only
+  const double rtau = 1.0 / tau;
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const double d = tau * kInvMu[i];
+    double a;
+    if (TANG) a = d > 700.0 ? 0.0 : exp_tang(-d, tab);
+    else a = exp(-d);
+    const double q = (a - 1.0) * (kMu[i] * rtau);
+    double& I = i == 0 ? I1 : I2;
+    I = I * a;
+    I += (1.0 + q) * B + (-a - q) * B_prev;
+  }
+}
+
+// Fused opacity assembly + short characteristics, one thread per wavenumber.
+// Writes the flux in W m^-2 cm times the radius-distance scaling.
+__global__ void __launch_bounds__(256) emission_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
                                                        const LevelSpecies* __restrict__ ls,
+                                                       const LevelSpeciesDF* __restrict__ lsdf,
                                                        const EvalInfo* __restrict__ ev,
                                                        double* __restrict__ spectrum) {
+  __shared__ ExpTables et;
+  load_exp_tables(et);
+  __syncthreads();
+  const int b = blockIdx.x;
+  const int k = blockIdx.y * blockDim.x + threadIdx.x;
+  if (k >= dm.N) return;
+  const int L = dm.L, S = dm.S;
+  const size_t N = dm.N;
+  const LevelInfo* lv = lev + (size_t)b * L;
+  const LevelSpecies* sp = ls + (size_t)b * L * S;
+  const LevelSpeciesDF* sf = lsdf + (size_t)b * L * S;
+  const float2 c1f = __ldg(dm.planck_c1_df + k), c2f = __ldg(dm.planck_c2l_df + k);
+  const df2 c1 = {c1f.x, c1f.y}, c2l = {c2f.x, c2f.y};
+  auto planck = [&](int l) {
+    const float2 it = __ldg(reinterpret_cast<const float2*>(&lv[l].invT_hi));
+    return planck_df(c1, c2l, df2{it.x, it.y}, et.hi, et.lo);
+  };
+  double kap_prev = level_absorption_df(dm.table_df, N, sp, sf, S, k, et);
+  double B_prev = planck(0);
+  double I1 = B_prev, I2 = B_prev;
+  for (int l = 1; l < L; ++l) {
+    const double kap = level_absorption_df(dm.table_df, N, sp + (size_t)l * S, sf + (size_t)l * S, S, k, et);
+    const double B = planck(l);
+    const double tau = __ldg(&lv[l - 1].dz) * (kap + kap_prev) / 2. + __ldg(&lv[l - 1].cloud);
+    sc_layer<true>(tau, B, B_prev, I1, I2, et.d);
+    kap_prev = kap;
+    B_prev = B;
+  }
+  const double flux = 2.0 * kPi * (I1 * kMu[0] * 0.5 + I2 * kMu[1] * 0.5) * 1e-3;
+  spectrum[(size_t)b * N + k] = flux * __ldg(&ev[b].scaling);
+}
+
+// Validation path: every step in FP64 with the CUDA math library.
+__global__ void __launch_bounds__(256) emission_kernel_fp64(DeviceModel dm, const LevelInfo* __restrict__ lev,
+                                                            const LevelSpecies* __restrict__ ls,
+                                                            const EvalInfo* __restrict__ ev,
+                                                            double* __restrict__ spectrum) {
   const int b = blockIdx.x;
   const int k = blockIdx.y * blockDim.x + threadIdx.x;
   if (k >= dm.N) return;
@@ -94,31 +192,14 @@ __global__ void __launch_bounds__(256) emission_kernel(DeviceModel dm, const TT*
   const LevelInfo* lv = lev + (size_t)b * L;
   const LevelSpecies* sp = ls + (size_t)b * L * S;
   const double c1 = dm.planck_c1[k], c2 = dm.planck_c2[k];
-
-  double kap_prev = level_absorption(tab, N, sp, S, k);
+  double kap_prev = level_absorption_fp64(dm.table64, N, sp, S, k);
   double B_prev = c1 / (exp(c2 * __ldg(&lv[0].invT)) - 1.0);
   double I1 = B_prev, I2 = B_prev;
   for (int l = 1; l < L; ++l) {
-    const double kap = level_absorption(tab, N, sp + (size_t)l * S, S, k);
+    const double kap = level_absorption_fp64(dm.table64, N, sp + (size_t)l * S, S, k);
     const double B = c1 / (exp(c2 * __ldg(&lv[l].invT)) - 1.0);
     const double tau = __ldg(&lv[l - 1].dz) * (kap + kap_prev) / 2. + __ldg(&lv[l - 1].cloud);
-    if (tau != 0) {
-      const double rtau = 1.0 / tau;
-      {
-        const double d = tau * kInvMu[0];
-        const double a = exp(-d);
-        const double q = (a - 1.0) * (kMu[0] * rtau);
-        I1 = I1 * a;
-        I1 += (1.0 + q) * B + (-a - q) * B_prev;
-      }
-      {
-        const double d = tau * kInvMu[1];
-        const double a = exp(-d);
-        const double q = (a - 1.0) * (kMu[1] * rtau);
-        I2 = I2 * a;
-        I2 += (1.0 + q) * B + (-a - q) * B_prev;
-      }
-    }
+    sc_layer<false>(tau, B, B_prev, I1, I2, nullptr);
     kap_prev = kap;
     B_prev = B;
   }
@@ -126,6 +207,7 @@ __global__ void __launch_bounds__(256) emission_kernel(DeviceModel dm, const TT*
   spectrum[(size_t)b * N + k] = flux * __ldg(&ev[b].scaling);
 }
 
+// ------------------------------------------------------------------ transmission
 // Tangent-ray path lengths of every evaluation: geom[b][t][i] for t <= i < L-1 is
 // sqrt((R+z_{i+1})^2 - (R+z_t)^2) - sqrt((R+z_i)^2 - (R+z_t)^2)
 // (TransmissionModel::distanceToTangentCenter src/forward_model/transmission/
@@ -154,39 +236,42 @@ __global__ void transmission_geometry_kernel(DeviceModel dm, const LevelInfo* __
 // Transit depth per wavenumber (TransmissionModel::calcTransmissionSpectrum ...
 // tangentOpticalDepth src/forward_model/transmission/transmission_spectrum.cpp:32-141).
 // Extinction of every level is staged in shared memory [L][blockDim]; the tangent
-// sums run in FP64 with the reference's tau > 10 cut-off.
-template <typename TT>
-__global__ void __launch_bounds__(128) transmission_kernel(DeviceModel dm, const TT* __restrict__ tab,
-                                                           const LevelInfo* __restrict__ lev,
+// sums run in FP64 with the reference's tau > 10 cut-off; the effective height is
+// accumulated from the top down.
+template <bool DF>
+__global__ void __launch_bounds__(128) transmission_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
                                                            const LevelSpecies* __restrict__ ls,
+                                                           const LevelSpeciesDF* __restrict__ lsdf,
                                                            const double* __restrict__ ray_n,
                                                            const EvalInfo* __restrict__ ev,
                                                            const double* __restrict__ geom,
                                                            double* __restrict__ spectrum) {
   extern __shared__ double chi_s[];
+  __shared__ ExpTables et;
+  if (DF) load_exp_tables(et);
+  __syncthreads();
   const int b = blockIdx.x;
   const int tid = threadIdx.x;
   const int k = blockIdx.y * blockDim.x + tid;
   const int L = dm.L, S = dm.S, R = dm.R;
   const size_t N = dm.N;
-  const bool active = k < dm.N;
+  if (k >= dm.N) return;
   const LevelInfo* lv = lev + (size_t)b * L;
   const LevelSpecies* sp = ls + (size_t)b * L * S;
+  const LevelSpeciesDF* sf = lsdf + (size_t)b * L * S;
   const int TB = blockDim.x;
-  if (active) {
-    for (int l = 0; l < L; ++l) {
-      const double a = level_absorption(tab, N, sp + (size_t)l * S, S, k);
-      double sc = 0.0;
-      for (int r = 0; r < R; ++r) sc += __ldg(&dm.rayleigh[(size_t)r * N + k]) * __ldg(&ray_n[((size_t)b * L + l) * R + r]);
-      chi_s[l * TB + tid] = a + sc + __ldg(&lv[l].cloud);
-    }
+  for (int l = 0; l < L; ++l) {
+    const double a = DF ? level_absorption_df(dm.table_df, N, sp + (size_t)l * S, sf + (size_t)l * S, S, k, et)
+                        : level_absorption_fp64(dm.table64, N, sp + (size_t)l * S, S, k);
+    double sc = 0.0;
+    for (int r = 0; r < R; ++r)
+      sc += __ldg(&dm.rayleigh[(size_t)r * N + k]) * __ldg(&ray_n[((size_t)b * L + l) * R + r]);
+    chi_s[l * TB + tid] = a + sc + __ldg(&lv[l].cloud);
   }
-  if (!active) return;
   const double Rp = ev[b].radius, Rs = ev[b].star_radius;
   const double* G = geom + (size_t)b * L * L;
-  // integrateEffectiveTangentHeight :59-77 accumulated from the top down
   double h = 0.0;
-  double tr_up = 1.0;  // transmission of level t+1; the top level is transparent
+  double tr_up = 1.0;  // the top level is transparent
   for (int t = L - 2; t >= 0; --t) {
     double tau = 0.0;
     const double* Gt = G + (size_t)t * L;
@@ -194,7 +279,7 @@ __global__ void __launch_bounds__(128) transmission_kernel(DeviceModel dm, const
       tau += __ldg(&Gt[i]) * (chi_s[i * TB + tid] + chi_s[(i + 1) * TB + tid]);
       if (tau > 10.0) break;
     }
-    const double tr = exp(-tau);
+    const double tr = DF ? (tau > 700.0 ? 0.0 : exp_tang(-tau, et.d)) : exp(-tau);
     const double zt = __ldg(&lv[t].z), zu = __ldg(&lv[t + 1].z);
     h += 2. * ((Rp + zt) * (1. - tr) + (Rp + zu) * (1. - tr_up)) * (zu - zt) * 0.5;
     tr_up = tr;
@@ -204,6 +289,7 @@ __global__ void __launch_bounds__(128) transmission_kernel(DeviceModel dm, const
   spectrum[(size_t)b * N + k] = rp * rp / Rs / Rs * 1e6;
 }
 
+// ------------------------------------------------------------------ observation + likelihood
 __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
@@ -277,6 +363,11 @@ static T* dev_upload(Model& m, const std::vector<T>& v) {
   return p;
 }
 
+static float2 split_df(double v) {
+  const float hi = (float)v;
+  return make_float2(hi, (float)(v - (double)hi));
+}
+
 void upload_model(Model& m) {
   BGB_CUDA(cudaSetDevice(m.device));
   const size_t N = m.N;
@@ -288,25 +379,34 @@ void upload_model(Model& m) {
   dm.M = m.M;
   dm.P = m.acfg.nparam_total;
   dm.nobs = (int)m.obs.size();
+  // (h nu c / k) log2(e) with log2(e) as a two-part constant
+  const double log2e_hi = 1.4426950408889634, log2e_lo = 2.0355273740931033e-17;
   std::vector<double> c1(N), c2(N);
+  std::vector<float2> c1df(N), c2ldf(N);
   for (size_t k = 0; k < N; ++k) {
     const double nu = m.nu[k];
     c1[k] = 2. * kPlanckH * kLightC * kLightC * nu * nu * nu;
     c2[k] = kPlanckH * nu * kLightC / kBoltzmann;
+    c1df[k] = split_df(c1[k]);
+    const double p = c2[k] * log2e_hi;
+    const double perr = std::fma(c2[k], log2e_hi, -p) + c2[k] * log2e_lo;
+    const float hi = (float)p;
+    c2ldf[k] = make_float2(hi, (float)((p - (double)hi) + perr));
   }
   dm.nu = dev_upload(m, m.nu);
   dm.wl = dev_upload(m, m.wl);
   dm.planck_c1 = dev_upload(m, c1);
   dm.planck_c2 = dev_upload(m, c2);
+  dm.planck_c1_df = dev_upload(m, c1df);
+  dm.planck_c2l_df = dev_upload(m, c2ldf);
   dm.pressure = dev_upload(m, m.p);
   dm.log10p = dev_upload(m, m.log10p);
   m.d_table64 = dev_upload(m, m.table_host);
   dm.table64 = m.d_table64;
   {
-    std::vector<float> t32(m.table_host.size());
-    for (size_t i = 0; i < t32.size(); ++i) t32[i] = (float)m.table_host[i];
-    m.d_table32 = dev_upload(m, t32);
-    dm.table32 = m.d_table32;
+    std::vector<float2> tdf(m.table_host.size());
+    for (size_t i = 0; i < tdf.size(); ++i) tdf[i] = split_df(m.table_host[i]);
+    dm.table_df = dev_upload(m, tdf);
   }
   std::vector<double>().swap(m.table_host);
   dm.table_T = dev_upload(m, m.table_T);
@@ -354,12 +454,32 @@ void upload_model(Model& m) {
   dm.cfg = m.d_cfg;
   BGB_CUDA(cudaMallocHost(&m.h_pinned, 64 * 1024));
   m.h_pinned_bytes = 64 * 1024;
+  // the transmission kernels stage L x blockDim doubles of extinction in shared memory
+  if (m.transmission) {
+    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kTransmissionDynSmem));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kTransmissionDynSmem));
+  }
+}
+
+// Threads per block of the transmission kernel: the requested count, reduced so that
+// L x threads doubles of staged extinction fit the shared memory opted into.
+static int transmission_threads(const Model& m) {
+  int tb = m.rt_threads > 0 ? std::min(m.rt_threads, 128) : 64;
+  const size_t per_thread = (size_t)m.L * sizeof(double);
+  while (tb > 32 && (size_t)tb * per_thread > kTransmissionDynSmem) tb -= 32;
+  if ((size_t)tb * per_thread > kTransmissionDynSmem)
+    throw Error(BEAR_ERR_UNSUPPORTED, "too many levels for the transmission kernel's shared-memory staging");
+  return tb;
 }
 
 static void free_workspace(Workspace& w) {
   cudaFree(w.params);
   cudaFree(w.lev);
   cudaFree(w.ls);
+  cudaFree(w.lsdf);
+  cudaFree(w.ray_n);
   cudaFree(w.ev);
   cudaFree(w.spectrum);
   cudaFree(w.obs);
@@ -370,8 +490,6 @@ static void free_workspace(Workspace& w) {
   cudaFree(w.g_geom);
   w = Workspace{};
 }
-
-static double* g_ray_n_dummy = nullptr;
 
 void ensure_workspace(Model& m, int batch) {
   if (batch <= m.ws.capacity) return;
@@ -384,7 +502,9 @@ void ensure_workspace(Model& m, int batch) {
   const size_t R = std::max(m.acfg.R, 1);
   BGB_CUDA(cudaMalloc(&w.params, B * P * sizeof(double)));
   BGB_CUDA(cudaMalloc(&w.lev, B * L * sizeof(LevelInfo)));
-  BGB_CUDA(cudaMalloc(&w.ls, B * L * S * sizeof(LevelSpecies) + B * L * R * sizeof(double)));
+  BGB_CUDA(cudaMalloc(&w.ls, B * L * S * sizeof(LevelSpecies)));
+  BGB_CUDA(cudaMalloc(&w.lsdf, B * L * S * sizeof(LevelSpeciesDF)));
+  BGB_CUDA(cudaMalloc(&w.ray_n, B * L * R * sizeof(double)));
   BGB_CUDA(cudaMalloc(&w.ev, B * sizeof(EvalInfo)));
   BGB_CUDA(cudaMalloc(&w.spectrum, B * N * sizeof(double)));
   BGB_CUDA(cudaMalloc(&w.obs, B * M * sizeof(double)));
@@ -393,88 +513,60 @@ void ensure_workspace(Model& m, int batch) {
   w.capacity = batch;
 }
 
-static inline double* ray_n_ptr(Model& m) {
-  const size_t B = m.ws.capacity, L = m.L, S = std::max(m.acfg.S, 1);
-  return reinterpret_cast<double*>(m.ws.ls + B * L * S);
+// Kernel sequence of one batch on the given work buffers.
+static void launch_stages(Model& m, const double* params_dev, int batch, const Workspace& w, cudaStream_t st,
+                          bool profile, uint8_t* neglect_dev, double* loglike_dev) {
+  const DeviceModel& dm = m.dm;
+  const int L = m.L;
+  const int atm_threads = ((L + 31) / 32) * 32;
+  if (profile) BGB_CUDA(cudaEventRecord(m.ev[0], st));
+  atmosphere_kernel<<<batch, atm_threads, 4 * L * sizeof(double), st>>>(dm, params_dev, dm.P, w.lev, w.ls,
+                                                                        w.lsdf, w.ray_n, w.ev);
+  BGB_CUDA(cudaGetLastError());
+  if (profile) BGB_CUDA(cudaEventRecord(m.ev[1], st));
+  if (!m.transmission) {
+    const int TB = m.rt_threads > 0 ? m.rt_threads : (batch == 1 ? 64 : 128);
+    dim3 grid(batch, (dm.N + TB - 1) / TB);
+    if (m.precision == 1)
+      emission_kernel_fp64<<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.ev, w.spectrum);
+    else
+      emission_kernel<<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.lsdf, w.ev, w.spectrum);
+  } else {
+    transmission_geometry_kernel<<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom);
+    const int TB = transmission_threads(m);
+    dim3 grid(batch, (dm.N + TB - 1) / TB);
+    const size_t sm = (size_t)L * TB * sizeof(double);
+    if (m.precision == 1)
+      transmission_kernel<false><<<grid, TB, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.spectrum);
+    else
+      transmission_kernel<true><<<grid, TB, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.spectrum);
+  }
+  BGB_CUDA(cudaGetLastError());
+  if (profile) BGB_CUDA(cudaEventRecord(m.ev[2], st));
+  const int OT = m.obs_threads > 0 ? m.obs_threads : 256;
+  obs_loglike_kernel<<<batch, OT, 0, st>>>(dm, w.spectrum, params_dev, dm.P, w.ev, w.obs, loglike_dev,
+                                          neglect_dev);
+  BGB_CUDA(cudaGetLastError());
+  if (profile) BGB_CUDA(cudaEventRecord(m.ev[3], st));
 }
 
 void launch_forward(Model& m, const double* params_dev, int batch, cudaStream_t st,
                     bool want_loglike, uint8_t* neglect_dev, double* loglike_dev) {
   ensure_workspace(m, batch);
-  const DeviceModel& dm = m.dm;
-  Workspace& w = m.ws;
-  const int L = m.L;
-  const int atm_threads = ((L + 31) / 32) * 32;
-  if (m.profiling) {
+  if (m.profiling)
     for (auto& e : m.ev)
       if (!e) BGB_CUDA(cudaEventCreate(&e));
-    BGB_CUDA(cudaEventRecord(m.ev[0], st));
-  }
-  atmosphere_kernel<<<batch, atm_threads, 4 * L * sizeof(double), st>>>(
-      dm, params_dev, dm.P, w.lev, w.ls, ray_n_ptr(m), w.ev);
-  BGB_CUDA(cudaGetLastError());
-  if (m.profiling) BGB_CUDA(cudaEventRecord(m.ev[1], st));
-  if (!m.transmission) {
-    const int TB = m.rt_threads > 0 ? m.rt_threads : (batch == 1 ? 64 : 128);
-    dim3 grid(batch, (dm.N + TB - 1) / TB);
-    if (m.fp32_tables && batch > 1)
-      emission_kernel<float><<<grid, TB, 0, st>>>(dm, dm.table32, w.lev, w.ls, w.ev, w.spectrum);
-    else
-      emission_kernel<double><<<grid, TB, 0, st>>>(dm, dm.table64, w.lev, w.ls, w.ev, w.spectrum);
-  } else {
-    transmission_geometry_kernel<<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom);
-    const int TB = m.rt_threads > 0 ? std::min(m.rt_threads, 128) : 64;
-    dim3 grid(batch, (dm.N + TB - 1) / TB);
-    const size_t sm = (size_t)L * TB * sizeof(double);
-    if (m.fp32_tables && batch > 1) {
-      BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-      transmission_kernel<float><<<grid, TB, sm, st>>>(dm, dm.table32, w.lev, w.ls, ray_n_ptr(m), w.ev, w.geom, w.spectrum);
-    } else {
-      BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-      transmission_kernel<double><<<grid, TB, sm, st>>>(dm, dm.table64, w.lev, w.ls, ray_n_ptr(m), w.ev, w.geom, w.spectrum);
-    }
-  }
-  BGB_CUDA(cudaGetLastError());
-  if (m.profiling) BGB_CUDA(cudaEventRecord(m.ev[2], st));
-  const int OT = m.obs_threads > 0 ? m.obs_threads : 256;
-  obs_loglike_kernel<<<batch, OT, 0, st>>>(dm, w.spectrum, params_dev, dm.P, w.ev, w.obs,
-                                          want_loglike ? (loglike_dev ? loglike_dev : w.loglike) : nullptr,
-                                          neglect_dev);
-  BGB_CUDA(cudaGetLastError());
-  if (m.profiling) {
-    BGB_CUDA(cudaEventRecord(m.ev[3], st));
-    m.ev_recorded = true;
-  }
+  launch_stages(m, params_dev, batch, m.ws, st, m.profiling, neglect_dev,
+                want_loglike ? (loglike_dev ? loglike_dev : m.ws.loglike) : nullptr);
+  if (m.profiling) m.ev_recorded = true;
 }
 
 // One evaluation with caller-supplied work buffers (used by the allocation-free
 // entry point): the kernels and launch shapes of the plain path, no workspace
 // growth, no profiling events.
-void launch_forward_into(Model& m, const double* params_dev, const Workspace& w, double* ray_n,
-                         cudaStream_t st, uint8_t* neglect_dev, double* loglike_dev) {
-  const DeviceModel& dm = m.dm;
-  const int L = m.L;
-  const int atm_threads = ((L + 31) / 32) * 32;
-  atmosphere_kernel<<<1, atm_threads, 4 * L * sizeof(double), st>>>(dm, params_dev, dm.P, w.lev, w.ls,
-                                                                    ray_n, w.ev);
-  BGB_CUDA(cudaGetLastError());
-  if (!m.transmission) {
-    const int TB = m.rt_threads > 0 ? m.rt_threads : 64;
-    dim3 grid(1, (dm.N + TB - 1) / TB);
-    emission_kernel<double><<<grid, TB, 0, st>>>(dm, dm.table64, w.lev, w.ls, w.ev, w.spectrum);
-  } else {
-    transmission_geometry_kernel<<<1, 256, 0, st>>>(dm, w.lev, w.ev, w.geom);
-    const int TB = m.rt_threads > 0 ? std::min(m.rt_threads, 128) : 64;
-    dim3 grid(1, (dm.N + TB - 1) / TB);
-    const size_t sm = (size_t)L * TB * sizeof(double);
-    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    transmission_kernel<double><<<grid, TB, sm, st>>>(dm, dm.table64, w.lev, w.ls, ray_n, w.ev, w.geom,
-                                                      w.spectrum);
-  }
-  BGB_CUDA(cudaGetLastError());
-  const int OT = m.obs_threads > 0 ? m.obs_threads : 256;
-  obs_loglike_kernel<<<1, OT, 0, st>>>(dm, w.spectrum, params_dev, dm.P, w.ev, w.obs, loglike_dev, neglect_dev);
-  BGB_CUDA(cudaGetLastError());
+void launch_forward_into(Model& m, const double* params_dev, const Workspace& w, cudaStream_t st,
+                         uint8_t* neglect_dev, double* loglike_dev) {
+  launch_stages(m, params_dev, 1, w, st, false, neglect_dev, loglike_dev);
 }
 
 void stage_times(Model& m, float* ms3) {
@@ -515,7 +607,6 @@ void release_model(Model& m) {
     if (e) cudaEventDestroy(e);
   if (m.h_pinned) cudaFreeHost(m.h_pinned);
   m.h_pinned = nullptr;
-  (void)g_ray_n_dummy;
 }
 
 }  // namespace bgb

@@ -86,6 +86,15 @@ struct __align__(16) LevelSpecies {
   double n;        // number density (cm^-3, or cm^-6 for CIA pairs)
 };
 
+// Double-float companions of LevelSpecies used by the FP32-pipe opacity path:
+// the same three interpolation weights and log2 of the number density
+// (lg2n_hi = kNoSpecies when the density is zero and the species is skipped).
+struct __align__(16) LevelSpeciesDF {
+  float wp_lo_hi, wp_lo_lo, wp_hi_hi, wp_hi_lo;
+  float wT_hi, wT_lo, lg2n_hi, lg2n_lo;
+};
+constexpr float kNoSpecies = -1.0e30f;
+
 // Per (evaluation, level).
 struct __align__(16) LevelInfo {
   double T;        // temperature
@@ -93,7 +102,7 @@ struct __align__(16) LevelInfo {
   double z;        // altitude (cm)
   double dz;       // z[l+1] - z[l] (0 on the top level)
   double cloud;    // emission: grey-cloud optical depth of layer l; transmission: cloud extinction at level l
-  double pad;
+  float invT_hi, invT_lo;  // 1 / T as a double-float
 };
 
 // Per evaluation.
@@ -116,12 +125,14 @@ struct DeviceModel {
   const double* wl;           // N
   const double* planck_c1;    // N: 2 h c^2 nu^3
   const double* planck_c2;    // N: h nu c / k
+  const float2* planck_c1_df; // N: 2 h c^2 nu^3 as double-float
+  const float2* planck_c2l_df;// N: (h nu c / k) log2(e) as double-float
+  const float2* table_df;     // rows x N, log10 cross sections as double-float
   // atmosphere constants
   const double* pressure;     // L (bar)
   const double* log10p;       // L
   // tables
   const double* table64;      // rows x N, log10 cross sections
-  const float* table32;       // rows x N (optional)
   const double* table_T;      // all species' temperature nodes
   const int* pb_row0;         // per species [nT][L]: absolute row of the lower pressure node
   const int* pb_row1;         // upper pressure node
@@ -147,6 +158,8 @@ struct Workspace {
   double* params = nullptr;    // B x P (plain path staging)
   LevelInfo* lev = nullptr;    // B x L
   LevelSpecies* ls = nullptr;  // B x L x S
+  LevelSpeciesDF* lsdf = nullptr;  // B x L x S
+  double* ray_n = nullptr;     // B x L x R number densities of the Rayleigh species
   EvalInfo* ev = nullptr;      // B
   double* spectrum = nullptr;  // B x N native units
   double* obs = nullptr;       // B x M internal order
@@ -241,14 +254,13 @@ struct Model {
   bool finalized = false;
   // device
   int device = 0;
-  bool fp32_tables = false;
+  int precision = 0;  // 0: double-float opacity + table exponentials, 1: FP64 libm kernels
   int rt_threads = 0, obs_threads = 0;
   DeviceModel dm{};
   std::vector<void*> allocations;
   size_t device_bytes = 0;
   AtmosphereConfig* d_cfg = nullptr;
   double* d_table64 = nullptr;
-  float* d_table32 = nullptr;
   Workspace ws;
   double* h_pinned = nullptr;  // pinned staging for the plain path
   size_t h_pinned_bytes = 0;

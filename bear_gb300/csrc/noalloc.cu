@@ -36,8 +36,8 @@ constexpr size_t kNoAllocScratchBytes = size_t(2) << 20;  // 2 MiB per device
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-void launch_forward_into(Model& m, const double* params_dev, const Workspace& w, double* ray_n,
-                         cudaStream_t st, uint8_t* neglect_dev, double* loglike_dev);
+void launch_forward_into(Model& m, const double* params_dev, const Workspace& w, cudaStream_t st,
+                         uint8_t* neglect_dev, double* loglike_dev);
 
 namespace {
 
@@ -48,8 +48,8 @@ void* g_scratch_addr[kMaxDevices] = {};
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Carves the single-evaluation work buffers out of the scratch array; returns
-// the bytes needed (and fills w / ray_n when base is not null).
-size_t layout(const Model& m, unsigned char* base, Workspace* w, double** ray_n) {
+// the bytes needed (and fills w when base is not null).
+size_t layout(const Model& m, unsigned char* base, Workspace* w) {
   const size_t L = m.L, S = std::max(m.acfg.S, 1), R = std::max(m.acfg.R, 1);
   const size_t N = m.N, M = std::max(m.M, 1);
   size_t off = 0;
@@ -60,6 +60,7 @@ size_t layout(const Model& m, unsigned char* base, Workspace* w, double** ray_n)
   };
   unsigned char* lev = take(L * sizeof(LevelInfo));
   unsigned char* ls = take(L * S * sizeof(LevelSpecies));
+  unsigned char* lsdf = take(L * S * sizeof(LevelSpeciesDF));
   unsigned char* rn = take(L * R * sizeof(double));
   unsigned char* ev = take(sizeof(EvalInfo));
   unsigned char* spec = take(N * sizeof(double));
@@ -70,11 +71,12 @@ size_t layout(const Model& m, unsigned char* base, Workspace* w, double** ray_n)
     w->capacity = 1;
     w->lev = reinterpret_cast<LevelInfo*>(lev);
     w->ls = reinterpret_cast<LevelSpecies*>(ls);
+    w->lsdf = reinterpret_cast<LevelSpeciesDF*>(lsdf);
+    w->ray_n = reinterpret_cast<double*>(rn);
     w->ev = reinterpret_cast<EvalInfo*>(ev);
     w->spectrum = reinterpret_cast<double*>(spec);
     w->obs = reinterpret_cast<double*>(obs);
     w->geom = reinterpret_cast<double*>(geom);
-    *ray_n = reinterpret_cast<double*>(rn);
   }
   return off;
 }
@@ -102,16 +104,15 @@ unsigned char* scratch_for_device(int device) {
 
 void loglike_noalloc(Model& m, const double* params_dev, double* loglike_dev, uint8_t* neglect_dev,
                      cudaStream_t st) {
-  const size_t need = layout(m, nullptr, nullptr, nullptr);
+  const size_t need = layout(m, nullptr, nullptr);
   if (need > kNoAllocScratchBytes)
     throw Error(BEAR_ERR_SIZE, "this model needs " + std::to_string(need) +
                                    " bytes of per-evaluation scratch; the allocation-free entry point is limited to " +
                                    std::to_string(kNoAllocScratchBytes) + " bytes");
   unsigned char* base = scratch_for_device(m.device);
   Workspace w;
-  double* ray_n = nullptr;
-  layout(m, base, &w, &ray_n);
-  launch_forward_into(m, params_dev, w, ray_n, st, neglect_dev, loglike_dev);
+  layout(m, base, &w);
+  launch_forward_into(m, params_dev, w, st, neglect_dev, loglike_dev);
 }
 
 }  // namespace bgb

@@ -1,0 +1,45 @@
+// Per-wavenumber physics helpers shared by the radiative-transfer kernels,
+// written on top of dfloat.cuh (host-compilable for accuracy checks).
+#pragma once
+
+#include "dfloat.cuh"
+
+namespace bgb {
+
+// Exponential tables staged in shared memory (divergent indices).
+struct ExpTables {
+  float hi[65];
+  float lo[65];
+  double d[64];
+};
+
+// Planck function B_nu(T) = 2 h c^2 nu^3 / (exp(h nu c / k T) - 1)
+// (aux::planckFunctionWavenumber, src/additional/aux_functions.cpp:272-278),
+// evaluated as c1 u / (1 - u) with u = 2^(-(h nu c / k) log2(e) / T) in
+// double-float arithmetic. c1 = 2 h c^2 nu^3 and c2l = (h nu c / k) log2(e) as
+// double-floats, invT = 1/T as a double-float. Returns FP64.
+BGB_HD double planck_df(df2 c1, df2 c2l, df2 invT, const float* tab_hi, const float* tab_lo) {
+  const df2 y = df_neg(df_mul(c2l, invT));
+  int n;
+  const df2 m = df_exp2(y, n, tab_hi, tab_lo);  // u = m 2^n, n <= 0
+  if (n < -60) return df_to_double(df_mul(c1, m)) * pow2d(n);  // 1 - u == 1 at this precision
+  const df2 u = df_ldexp(m, n);
+  const df2 d = df_sub(df_make(1.0f), u);
+  return df_to_double(df_div(df_mul(c1, u), d));
+}
+
+// 10^x * n as a double for a double-float log10 cross section x and log2(n):
+// 2^(x log2(10) + log2(n)).
+BGB_HD double pow10_times_n(df2 x, df2 lg2n, const float* tab_hi, const float* tab_lo, df2& acc, double& wide) {
+  const df2 y = df_add(df_mul(x, df2{kLog2_10Hi, kLog2_10Lo}), lg2n);
+  int n;
+  const df2 m = df_exp2(y, n, tab_hi, tab_lo);
+  if (n > -100 && n < 100) {
+    acc = df_add(acc, df_ldexp(m, n));
+  } else {
+    wide += df_to_double(m) * pow2d(n);  // outside the float exponent range: FP64 accumulator
+  }
+  return 0.0;
+}
+
+}  // namespace bgb

@@ -146,9 +146,12 @@ int bear_loglike_grad_batch(bear_model* m, const double* params_dev, int batch, 
                             double* loglike_dev, double* grad_dev, uint8_t* neglect_dev,
                             void* stream);
 
-/* Table precision of the batched path: 0 = FP64 tables (default, the plain
- * path always uses FP64), 1 = FP32 tables with FP64 accumulation. */
-int bear_model_set_precision(bear_model* m, int fp32_tables);
+/* Arithmetic of the opacity assembly (applies to every evaluation path):
+ * 0 (default) = double-float (hi + lo float pairs, ~48 bits) on the FP32 pipe
+ * with table-driven exponentials; radiative-transfer recurrences, tangent-ray
+ * sums and the likelihood stay FP64. 1 = every step in FP64 with the CUDA
+ * math library (the validation path). */
+int bear_model_set_precision(bear_model* m, int mode);
 
 /* Launch configuration of the batched kernels (threads per block along the
  * spectral axis; 0 = default). Used by the autotuner. */

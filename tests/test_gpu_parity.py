@@ -147,18 +147,47 @@ def test_batched_full_size_against_oracle(name, kind):
     e.close()
 
 
-def test_fp32_table_mode_error_is_bounded():
-    """FP32 table storage for the batched path: error against the FP64 path stated."""
+def test_fp64_validation_path_matches_reference(engine_case):
+    """Precision mode 1 (every step in FP64 with the CUDA math library) against the
+    reference's golden outputs: the yardstick for the default double-float path."""
+    c, e = engine_case
+    e.set_precision(1)
+    try:
+        worst = 0.0
+        for i, p in enumerate(c.params):
+            if c.arrays["ref_neglect"][i]:
+                continue
+            ll = e.loglike(p)
+            ref = c.arrays["ref_loglike"][i]
+            worst = max(worst, abs(ll - ref))
+            assert abs(ll - ref) <= ll_tol(ref, i == 0)
+            _, obs, _ = e.compute_model(p)
+            assert goldenlib.rel_err(obs, c.arrays["ref_obs"][i]) < 1e-6
+        _record(c.name, "fp64_path_max_abs_loglike", worst)
+    finally:
+        e.set_precision(0)
+
+
+@pytest.mark.parametrize("name,kind", [("emission_batched", "emission"), ("transmission_plain", "transmission")])
+def test_double_float_path_against_fp64_path(name, kind):
+    """The default path (double-float opacity and Planck on the FP32 pipe) against the
+    all-FP64 path on a batch of live points: spectra and log-likelihoods."""
     import torch
-    spec, text, arrays = _full_case("emission_batched", "emission")
+    spec, text, arrays = _full_case(name, kind)
     e = Engine(text, arrays)
-    pr = syn.priors(spec, "emission")
+    pr = syn.priors(spec, kind)
     cube = np.random.default_rng(3).uniform(size=(32, len(pr)))
-    P = torch.tensor(syn.cube_to_physical(pr, cube), device="cuda")
-    ll64, _ = e.loglike_batch(P)
-    e.set_precision(True)
-    ll32, _ = e.loglike_batch(P)
-    d = (ll32 - ll64).abs().max().item()
-    _record("emission_batched", "fp32_tables_max_abs_loglike_vs_fp64", d)
-    assert d < 1.0
+    phys = syn.cube_to_physical(pr, cube)
+    P = torch.tensor(phys, device="cuda")
+    ll_df, _ = e.loglike_batch(P)
+    spec_df = [e.compute_model(p)[0] for p in phys[:4]]
+    e.set_precision(1)
+    ll_64, _ = e.loglike_batch(P)
+    spec_64 = [e.compute_model(p)[0] for p in phys[:4]]
+    d = (ll_df - ll_64).abs().cpu().numpy()
+    tol = 1e-8 + 1e-12 * ll_64.abs().cpu().numpy()
+    rel_spec = max(goldenlib.rel_err(a, b) for a, b in zip(spec_df, spec_64))
+    _record(name, "df_vs_fp64", {"max_abs_loglike": float(d.max()), "max_rel_spectrum": rel_spec})
+    assert np.all(d <= tol), (d.max(), tol.min())
+    assert rel_spec < 1e-9
     e.close()
