@@ -282,6 +282,12 @@ __global__ void __launch_bounds__(kMaxLevels) atmosphere_kernel(DeviceModel dm, 
     const df2 it = df_from_double(li.invT);
     li.invT_hi = it.hi;
     li.invT_lo = it.lo;
+    const df2 dh = df_from_double(0.5 * li.dz);
+    li.dzh_hi = dh.hi;
+    li.dzh_lo = dh.lo;
+    const df2 cd = df_from_double(cl);
+    li.cloud_hi = cd.hi;
+    li.cloud_lo = cd.lo;
     lev[(size_t)b * L + l] = li;
     // table stencils: OpacitySpecies::findClosestDataPoints src/transport_coeff/opacity_species.cpp:160-273
     for (int s = 0; s < S; ++s) {

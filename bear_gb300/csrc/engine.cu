@@ -98,6 +98,39 @@ __device__ __forceinline__ double level_absorption_df(const float2* __restrict__
   return df_to_double(acc) + wide;
 }
 
+// The same sum kept as a double-float plus an FP64 part for terms outside the float
+// exponent range (zero almost always).
+struct Kappa {
+  df2 v;
+  double wide;
+};
+
+__device__ __forceinline__ Kappa level_kappa_df(const float2* __restrict__ tab, size_t N,
+                                                const LevelSpecies* __restrict__ d,
+                                                const LevelSpeciesDF* __restrict__ f, int S, int k,
+                                                const ExpTables& et) {
+  Kappa r = {{0.0f, 0.0f}, 0.0};
+  for (int s = 0; s < S; ++s) {
+    const float4 fa = __ldg(reinterpret_cast<const float4*>(f + s));
+    const float4 fb = __ldg(reinterpret_cast<const float4*>(f + s) + 1);
+    if (fb.z == kNoSpecies) continue;
+    const int4 rw = __ldg(reinterpret_cast<const int4*>(d + s));
+    const float2 t0 = __ldg(tab + (size_t)rw.x * N + k);
+    const float2 t1 = __ldg(tab + (size_t)rw.y * N + k);
+    const float2 t2 = __ldg(tab + (size_t)rw.z * N + k);
+    const float2 t3 = __ldg(tab + (size_t)rw.w * N + k);
+    const df2 lo = df_lerp(df2{t0.x, t0.y}, df2{t1.x, t1.y}, df2{fa.x, fa.y});
+    const df2 hi = df_lerp(df2{t2.x, t2.y}, df2{t3.x, t3.y}, df2{fa.z, fa.w});
+    const df2 x = df_lerp(lo, hi, df2{fb.x, fb.y});
+    pow10_times_n(x, df2{fb.z, fb.w}, et.hi, et.lo, r.v, r.wide);
+  }
+  return r;
+}
+
+// 700.0 as the bit pattern of a double: for non-negative x, x > 700 <=> bits(x) > bits(700)
+// (an integer comparison, off the FP64 pipe).
+constexpr long long kBits700 = 0x4085E00000000000LL;
+
 // The same in FP64 with the CUDA math library (validation path).
 __device__ __forceinline__ double level_absorption_fp64(const double* __restrict__ tab, size_t N,
                                                         const LevelSpecies* __restrict__ d, int S,
@@ -140,6 +173,25 @@ __device__ __forceinline__ void sc_layer(double tau, double B, double B_prev, do
   }
 }
 
+// The same layer in fewer FP64 operations, used by the default kernel:
+// I a + (1+q) B + (-a-q) B' == a (I - B') + B + q (B - B'), with q = (a-1)/delta and
+// 1/tau supplied by the caller (computed in double-float). The exponential and the
+// recurrence stay FP64.
+__device__ __forceinline__ void sc_layer_fast(double tau, double rtau, double B, double B_prev, double& I1,
+                                              double& I2, const double* tab) {
+  if (tau == 0) return;
+  const double dB = B - B_prev;
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const double d = tau * kInvMu[i];
+    const double a = __double_as_longlong(d) > kBits700 ? 0.0 : exp_tang(-d, tab);
+    const double q = (a - 1.0) * (kMu[i] * rtau);
+    double& I = i == 0 ? I1 : I2;
+    I = fma(a, I - B_prev, B);
+    I = fma(q, dB, I);
+  }
+}
+
 // Fused opacity assembly + short characteristics, one thread per wavenumber.
 // Writes the flux in W m^-2 cm times the radius-distance scaling.
 __global__ void __launch_bounds__(256) emission_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
@@ -164,14 +216,25 @@ __global__ void __launch_bounds__(256) emission_kernel(DeviceModel dm, const Lev
     const float2 it = __ldg(reinterpret_cast<const float2*>(&lv[l].invT_hi));
     return planck_df(c1, c2l, df2{it.x, it.y}, et.hi, et.lo);
   };
-  double kap_prev = level_absorption_df(dm.table_df, N, sp, sf, S, k, et);
+  Kappa kap_prev = level_kappa_df(dm.table_df, N, sp, sf, S, k, et);
   double B_prev = planck(0);
   double I1 = B_prev, I2 = B_prev;
   for (int l = 1; l < L; ++l) {
-    const double kap = level_absorption_df(dm.table_df, N, sp + (size_t)l * S, sf + (size_t)l * S, S, k, et);
+    const Kappa kap = level_kappa_df(dm.table_df, N, sp + (size_t)l * S, sf + (size_t)l * S, S, k, et);
     const double B = planck(l);
-    const double tau = __ldg(&lv[l - 1].dz) * (kap + kap_prev) / 2. + __ldg(&lv[l - 1].cloud);
-    sc_layer<true>(tau, B, B_prev, I1, I2, et.d);
+    // layer optical depth dz (k_l + k_{l-1}) / 2 + cloud, and its reciprocal, in double-float
+    const float4 g = __ldg(reinterpret_cast<const float4*>(&lv[l - 1].dzh_hi));  // dzh, cloud
+    double tau, rtau;
+    const df2 t = df_add(df_mul(df2{g.x, g.y}, df_add(kap.v, kap_prev.v)), df2{g.z, g.w});
+    if (kap.wide == 0.0 && kap_prev.wide == 0.0 && t.hi > 1e-30f && t.hi < 1e30f) {
+      tau = df_to_double(t);
+      rtau = df_to_double(df_div(df_make(1.0f), t));
+    } else {  // optical depths outside the comfortable float range: FP64
+      const double ks = (df_to_double(kap.v) + kap.wide) + (df_to_double(kap_prev.v) + kap_prev.wide);
+      tau = __ldg(&lv[l - 1].dz) * ks / 2. + __ldg(&lv[l - 1].cloud);
+      rtau = 1.0 / tau;
+    }
+    sc_layer_fast(tau, rtau, B, B_prev, I1, I2, et.d);
     kap_prev = kap;
     B_prev = B;
   }
@@ -233,12 +296,17 @@ __global__ void transmission_geometry_kernel(DeviceModel dm, const LevelInfo* __
   }
 }
 
-// Transit depth per wavenumber (TransmissionModel::calcTransmissionSpectrum ...
-// tangentOpticalDepth src/forward_model/transmission/transmission_spectrum.cpp:32-141).
-// Extinction of every level is staged in shared memory [L][blockDim]; the tangent
-// sums run in FP64 with the reference's tau > 10 cut-off; the effective height is
-// accumulated from the top down.
-template <bool DF>
+// Transit depth (TransmissionModel::calcTransmissionSpectrum ... tangentOpticalDepth
+// src/forward_model/transmission/transmission_spectrum.cpp:32-141). A block covers
+// VPB = 128 / TPN wavenumbers with TPN threads each (lane = wavenumber, so table
+// reads stay coalesced). The TPN threads of a wavenumber split the levels' opacities,
+// then share the staged extinction column chi[L][VPB] (FP64) and split the tangent
+// levels. Tangent sums are FP64 with the reference's tau > 10 cut-off; the
+// effective height is summed per level, sum_t (R + z_t)(1 - T_t)(dz_{t-1} + dz_t),
+// which regroups the reference's trapezoid sum.
+constexpr long long kBits10 = 0x4024000000000000LL;  // 10.0 as a double's bit pattern
+
+template <bool DF, int TPN>
 __global__ void __launch_bounds__(128) transmission_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
                                                            const LevelSpecies* __restrict__ ls,
                                                            const LevelSpeciesDF* __restrict__ lsdf,
@@ -246,47 +314,67 @@ __global__ void __launch_bounds__(128) transmission_kernel(DeviceModel dm, const
                                                            const EvalInfo* __restrict__ ev,
                                                            const double* __restrict__ geom,
                                                            double* __restrict__ spectrum) {
-  extern __shared__ double chi_s[];
+  constexpr int VPB = 128 / TPN;
+  extern __shared__ double chi_s[];  // [L][VPB]
   __shared__ ExpTables et;
+  __shared__ double h_part[TPN][VPB];
   if (DF) load_exp_tables(et);
-  __syncthreads();
+  const int v = threadIdx.x % VPB, j = threadIdx.x / VPB;
   const int b = blockIdx.x;
-  const int tid = threadIdx.x;
-  const int k = blockIdx.y * blockDim.x + tid;
+  const int k = blockIdx.y * VPB + v;
   const int L = dm.L, S = dm.S, R = dm.R;
   const size_t N = dm.N;
-  if (k >= dm.N) return;
+  const bool active = k < dm.N;
   const LevelInfo* lv = lev + (size_t)b * L;
   const LevelSpecies* sp = ls + (size_t)b * L * S;
   const LevelSpeciesDF* sf = lsdf + (size_t)b * L * S;
-  const int TB = blockDim.x;
-  for (int l = 0; l < L; ++l) {
-    const double a = DF ? level_absorption_df(dm.table_df, N, sp + (size_t)l * S, sf + (size_t)l * S, S, k, et)
-                        : level_absorption_fp64(dm.table64, N, sp + (size_t)l * S, S, k);
-    double sc = 0.0;
-    for (int r = 0; r < R; ++r)
-      sc += __ldg(&dm.rayleigh[(size_t)r * N + k]) * __ldg(&ray_n[((size_t)b * L + l) * R + r]);
-    chi_s[l * TB + tid] = a + sc + __ldg(&lv[l].cloud);
-  }
-  const double Rp = ev[b].radius, Rs = ev[b].star_radius;
-  const double* G = geom + (size_t)b * L * L;
-  double h = 0.0;
-  double tr_up = 1.0;  // the top level is transparent
-  for (int t = L - 2; t >= 0; --t) {
-    double tau = 0.0;
-    const double* Gt = G + (size_t)t * L;
-    for (int i = t; i < L - 1; ++i) {
-      tau += __ldg(&Gt[i]) * (chi_s[i * TB + tid] + chi_s[(i + 1) * TB + tid]);
-      if (tau > 10.0) break;
+  __syncthreads();
+  // extinction abs + scat + cloud of every level (the TPN threads take every TPN-th level)
+  if (active) {
+    for (int l = j; l < L; l += TPN) {
+      const double a = DF ? level_absorption_df(dm.table_df, N, sp + (size_t)l * S, sf + (size_t)l * S, S, k, et)
+                          : level_absorption_fp64(dm.table64, N, sp + (size_t)l * S, S, k);
+      double sc = 0.0;
+      for (int r = 0; r < R; ++r)
+        sc += __ldg(&dm.rayleigh[(size_t)r * N + k]) * __ldg(&ray_n[((size_t)b * L + l) * R + r]);
+      chi_s[l * VPB + v] = a + sc + __ldg(&lv[l].cloud);
     }
-    const double tr = DF ? (tau > 700.0 ? 0.0 : exp_tang(-tau, et.d)) : exp(-tau);
-    const double zt = __ldg(&lv[t].z), zu = __ldg(&lv[t + 1].z);
-    h += 2. * ((Rp + zt) * (1. - tr) + (Rp + zu) * (1. - tr_up)) * (zu - zt) * 0.5;
-    tr_up = tr;
   }
-  h = sqrt(h + Rp * Rp) - Rp;
-  const double rp = h + Rp;
-  spectrum[(size_t)b * N + k] = rp * rp / Rs / Rs * 1e6;
+  __syncthreads();
+  // neighbour sums chi_i + chi_{i+1}, the bracket of every trapezoid term
+  if (active && j == 0)
+    for (int i = 0; i < L - 1; ++i) chi_s[i * VPB + v] += chi_s[(i + 1) * VPB + v];
+  __syncthreads();
+  double h = 0.0;
+  const double Rp = ev[b].radius;
+  if (active) {
+    const double* G = geom + (size_t)b * L * L;
+    for (int t = L - 2 - j; t >= 0; t -= TPN) {
+      double tau = 0.0;
+      const double* Gt = G + (size_t)t * L;
+      for (int i = t; i < L - 1; ++i) {
+        tau = fma(__ldg(&Gt[i]), chi_s[i * VPB + v], tau);
+        if (__double_as_longlong(tau) > kBits10) break;  // tau > 10 (tau >= 0)
+      }
+      double tr;
+      if (DF) tr = __double_as_longlong(tau) > kBits700 ? 0.0 : exp_tang(-tau, et.d);
+      else tr = exp(-tau);
+      const double zt = __ldg(&lv[t].z);
+      const double wz = (__ldg(&lv[t + 1].z) - zt) + (t >= 1 ? zt - __ldg(&lv[t - 1].z) : 0.0);
+      h = fma((Rp + zt) * (1. - tr), wz, h);
+    }
+  }
+  h_part[j][v] = h;
+  __syncthreads();
+  if (active && j == 0) {
+    double hs = 0.0;
+#pragma unroll
+    for (int q = 0; q < TPN; ++q) hs += h_part[q][v];
+    hs = sqrt(hs + Rp * Rp) - Rp;
+    const double rp = hs + Rp;
+    const double Rs = ev[b].star_radius;
+    spectrum[(size_t)b * N + k] = rp * rp / Rs / Rs * 1e6;
+  }
 }
 
 // ------------------------------------------------------------------ observation + likelihood
@@ -456,22 +544,12 @@ void upload_model(Model& m) {
   m.h_pinned_bytes = 64 * 1024;
   // the transmission kernels stage L x blockDim doubles of extinction in shared memory
   if (m.transmission) {
-    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)kTransmissionDynSmem));
-    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)kTransmissionDynSmem));
+    const int sm = (int)kTransmissionDynSmem;
+    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<true, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<false, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<true, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<false, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
   }
-}
-
-// Threads per block of the transmission kernel: the requested count, reduced so that
-// L x threads doubles of staged extinction fit the shared memory opted into.
-static int transmission_threads(const Model& m) {
-  int tb = m.rt_threads > 0 ? std::min(m.rt_threads, 128) : 64;
-  const size_t per_thread = (size_t)m.L * sizeof(double);
-  while (tb > 32 && (size_t)tb * per_thread > kTransmissionDynSmem) tb -= 32;
-  if ((size_t)tb * per_thread > kTransmissionDynSmem)
-    throw Error(BEAR_ERR_UNSUPPORTED, "too many levels for the transmission kernel's shared-memory staging");
-  return tb;
 }
 
 static void free_workspace(Workspace& w) {
@@ -533,13 +611,22 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
       emission_kernel<<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.lsdf, w.ev, w.spectrum);
   } else {
     transmission_geometry_kernel<<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom);
-    const int TB = transmission_threads(m);
-    dim3 grid(batch, (dm.N + TB - 1) / TB);
-    const size_t sm = (size_t)L * TB * sizeof(double);
-    if (m.precision == 1)
-      transmission_kernel<false><<<grid, TB, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.spectrum);
-    else
-      transmission_kernel<true><<<grid, TB, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.spectrum);
+    // rt_threads selects the wavenumbers per block: 32 (4 threads each, default) or 16 (8 each)
+    const int vpb = (m.rt_threads == 16) ? 16 : 32;
+    dim3 grid(batch, (dm.N + vpb - 1) / vpb);
+    const size_t sm = (size_t)L * vpb * sizeof(double);
+    if (sm > kTransmissionDynSmem) throw Error(BEAR_ERR_UNSUPPORTED, "too many levels for the transmission kernel");
+    if (vpb == 32) {
+      if (m.precision == 1)
+        transmission_kernel<false, 4><<<grid, 128, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.spectrum);
+      else
+        transmission_kernel<true, 4><<<grid, 128, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.spectrum);
+    } else {
+      if (m.precision == 1)
+        transmission_kernel<false, 8><<<grid, 128, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.spectrum);
+      else
+        transmission_kernel<true, 8><<<grid, 128, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.spectrum);
+    }
   }
   BGB_CUDA(cudaGetLastError());
   if (profile) BGB_CUDA(cudaEventRecord(m.ev[2], st));

@@ -102,7 +102,9 @@ struct __align__(16) LevelInfo {
   double z;        // altitude (cm)
   double dz;       // z[l+1] - z[l] (0 on the top level)
   double cloud;    // emission: grey-cloud optical depth of layer l; transmission: cloud extinction at level l
-  float invT_hi, invT_lo;  // 1 / T as a double-float
+  float invT_hi, invT_lo;    // 1 / T as a double-float
+  float dzh_hi, dzh_lo;      // dz / 2 as a double-float
+  float cloud_hi, cloud_lo;  // cloud as a double-float
 };
 
 // Per evaluation.
