@@ -56,7 +56,7 @@ __global__ void atmosphere_kernel(DeviceModel dm, const double* __restrict__ par
 
 // Dynamic shared memory the transmission kernels opt into (the per-block maximum of
 // 227 KB less room for their static tables).
-constexpr size_t kTransmissionDynSmem = 225 * 1024;
+constexpr size_t kTransmissionDynSmem = 220 * 1024;
 
 // Gauss nodes of ShortCharacteristics (src/radiative_transfer/short_characteristics.h:62-63)
 __device__ __constant__ double kMu[2] = {0.211324865405187, 0.788675134594813};
