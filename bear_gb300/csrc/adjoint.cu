@@ -1,13 +1,794 @@
-// Adjoint (reverse-mode) gradient of the log-likelihood.
+// Adjoint (reverse-mode) gradient of the log-likelihood with respect to the
+// physical parameters, emission models.
+//
+// Kernel chain for one chunk of evaluations:
+//   atmosphere_kernel + emission_kernel<STORE> + obs_loglike_kernel
+//       the forward pass, also writing d wT / dT of every table stencil and the
+//       two Gauss-angle intensities after every level (B x L x 2 x N FP64)
+//   obs_adjoint_kernel         d log L / d binned model, the shift and error-
+//                              inflation parameters, sum_k dlogL/dF_k F_k
+//   emission_adjoint_kernel    per wavenumber: the seed W^T dlogL/dbin, then the
+//                              short-characteristics recurrence run backwards from
+//                              the top with every level opacity recomputed (never
+//                              stored); per-level sinks (log number densities,
+//                              temperature, layer thickness, cloud optical depth)
+//                              reduced per block into partial sums
+//   atmosphere_adjoint_kernel  per evaluation: the partial sums reduced in a fixed
+//                              order, then mapped onto the parameters through the
+//                              tangents of the level physics (temperature profile,
+//                              chemistry, hydrostatic layer thickness, grey cloud,
+//                              radius-distance scaling)
+// Every reduction runs in a fixed order, so the gradient is bit-reproducible.
+//
+// Derivative conventions at the model's non-smooth points: discrete decisions
+// are held fixed -- opacity-table brackets (the gradient of the bilinear
+// interpolation on the current cell; zero temperature slope when T is clamped
+// to the table's end), the grey cloud's integer layer indices (so d/d cloud-top
+// pressure and d/d cloud-bottom factor are 0), exactly transparent layers
+// (tau == 0 contributes nothing). A model neglected by the forward pass (50 K
+// temperature clamp, negative background abundance) has log L = -1e30 and a
+// zero gradient.
+//
+// Arithmetic: in precision mode 0 the adjoint runs in double-float on the FP32
+// pipe (about 48 significant bits, ample for a gradient): the level opacities
+// are recomputed with the forward's own double-float routines, the layer adjoint
+// uses a double-float exponential and Taylor series for thin layers, and the
+// per-level sinks are reduced as double-floats. Precision mode 1 does every step
+// in FP64 with the CUDA math library and serves as the reference gradient.
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+
 #include "../../include/bear_gb300.h"
+#include "level_physics.cuh"
 #include "model.h"
+#include "rt_common.cuh"
 
 namespace bgb {
 
-void launch_gradient(Model& m, const double* params_dev, int batch, cudaStream_t st,
-                     double* loglike_dev, double* grad_dev, uint8_t* neglect_dev) {
-  (void)m; (void)params_dev; (void)batch; (void)st; (void)loglike_dev; (void)grad_dev; (void)neglect_dev;
-  throw Error(BEAR_ERR_UNSUPPORTED, "gradient not available");
+#define BGB_CUDA(x)                                                                         \
+  do {                                                                                      \
+    cudaError_t e_ = (x);                                                                   \
+    if (e_ != cudaSuccess)                                                                  \
+      throw Error(BEAR_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));         \
+  } while (0)
+
+constexpr int kAdjThreads = 128;  // threads (wavenumbers) per block of the adjoint kernel
+constexpr double kLn10 = 2.302585092994045684;
+constexpr float kLn10Hi = (float)kLn10, kLn10Lo = (float)(kLn10 - (double)kLn10Hi);
+
+// ------------------------------------------------------------------ accumulators
+// The per-level sinks are summed either as double-floats (FP32 pipe) or in FP64.
+__device__ __forceinline__ df2 acc_add(df2 a, df2 b) { return df_add(a, b); }
+__device__ __forceinline__ double acc_add(double a, double b) { return a + b; }
+__device__ __forceinline__ df2 acc_shfl_xor(df2 v, int o) {
+  return {__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+}
+__device__ __forceinline__ double acc_shfl_xor(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ double acc_to_double(df2 v) { return df_to_double(v); }
+__device__ __forceinline__ double acc_to_double(double v) { return v; }
+
+template <bool DF>
+struct AccType {
+  typedef double type;
+  static __device__ __forceinline__ double from(double x) { return x; }
+  static __device__ __forceinline__ double zero() { return 0.0; }
+};
+template <>
+struct AccType<true> {
+  typedef df2 type;
+  static __device__ __forceinline__ df2 from(double x) { return df_from_double(x); }
+  static __device__ __forceinline__ df2 zero() { return df2{0.0f, 0.0f}; }
+};
+
+// Warp reduce-scatter of VP values (VP = 8, 16 or 32): each halving step keeps
+// half of the values, sends the other half to the partner lane and adds what
+// comes back, so the warp does VP - 1 additions per lane instead of 5 VP.
+// Afterwards lane j holds the warp total of value j / (32 / VP).
+template <int VP, class A>
+__device__ __forceinline__ A warp_reduce_scatter(A (&v)[VP], int lane) {
+#pragma unroll
+  for (int s = 0; s < 5; ++s) {
+    const int o = 16 >> s;
+    const int cnt = VP >> s;
+    if (cnt >= 2) {
+      const int h = cnt / 2;
+      const bool upper = (lane & o) != 0;
+#pragma unroll
+      for (int i = 0; i < h; ++i) {
+        const A send = upper ? v[i] : v[i + h];
+        const A keep = upper ? v[i + h] : v[i];
+        v[i] = acc_add(keep, acc_shfl_xor(send, o));
+      }
+    } else {
+      v[0] = acc_add(v[0], acc_shfl_xor(v[0], o));
+    }
+  }
+  return v[0];
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// ------------------------------------------------------------------ likelihood adjoint
+// log L = sum_r w_r (-0.5 log(2 pi e_r) - 0.5 (d_r - s_r)^2 / e_r), e_r = sigma_r^2 + 10^b
+// (Retrieval::logLikelihood src/retrieval/retrieval.cpp:314-369): writes
+// gS_r = d log L / d s_r, the shift (src/forward_model/forward_model.cpp:161-180) and
+// error-inflation derivatives into the gradient row (zeroing the rest), and per
+// evaluation the seed normaliser 2^-e, its inverse and sum_r gS_r (s_r - shift_r).
+__global__ void __launch_bounds__(256) obs_adjoint_kernel(DeviceModel dm, const double* __restrict__ params, int P,
+                                                          const EvalInfo* __restrict__ ev,
+                                                          const double* __restrict__ obs, double* __restrict__ gS,
+                                                          double* __restrict__ seed, double* __restrict__ grad,
+                                                          int transmission) {
+  __shared__ double red[3][256];
+  const int b = blockIdx.x, tid = threadIdx.x;
+  const int M = dm.M;
+  const bool neg = ev[b].neglect != 0;
+  const double infl = ev[b].inflation;
+  const double* par = params + (size_t)b * P;
+  for (int j = tid; j < P; j += blockDim.x) grad[(size_t)b * P + j] = 0.0;
+  auto row_grad = [&](int r, double& s_out, double& d_out, double& es_out) {
+    const double s = obs[(size_t)b * M + r];
+    const double es = __ldg(&dm.row_err2[r]) + infl;
+    const double d = __ldg(&dm.row_data[r]) - s;
+    s_out = s;
+    d_out = d;
+    es_out = es;
+    return neg ? 0.0 : __ldg(&dm.row_weight[r]) * d / es;
+  };
+  double sgs = 0.0, sinf = 0.0, gmax = 0.0;
+  for (int r = tid; r < M; r += blockDim.x) {
+    double s, d, es;
+    const double g = row_grad(r, s, d, es);
+    gS[(size_t)b * M + r] = g;
+    const int mp = __ldg(&dm.obs_mod_param[__ldg(&dm.row_obs[r])]);
+    double pre = s;
+    if (mp >= 0) {
+      const double sh = par[mp];
+      if (sh != 0) pre = s - sh;
+    }
+    sgs = fma(g, pre, sgs);
+    sinf += __ldg(&dm.row_weight[r]) * 0.5 * (d * d / es - 1.0) / es;
+    gmax = fmax(gmax, fabs(g));
+  }
+  red[0][tid] = sgs;
+  red[1][tid] = sinf;
+  red[2][tid] = gmax;
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if (tid < h) {
+      red[0][tid] += red[0][tid + h];
+      red[1][tid] += red[1][tid + h];
+      red[2][tid] = fmax(red[2][tid], red[2][tid + h]);
+    }
+    __syncthreads();
+  }
+  const double tot_gs = red[0][0], tot_inf = red[1][0], tot_max = red[2][0];
+  __syncthreads();
+  // observation shifts: d log L / d shift_o = sum of gS over the observation's rows
+  for (int o = 0; o < dm.nobs; ++o) {
+    const int mp = __ldg(&dm.obs_mod_param[o]);
+    if (mp < 0) continue;
+    double acc = 0.0;
+    for (int r = __ldg(&dm.obs_row_start[o]) + tid; r < __ldg(&dm.obs_row_start[o + 1]); r += blockDim.x) {
+      double s, d, es;
+      acc += row_grad(r, s, d, es);
+    }
+    red[0][tid] = acc;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+      if (tid < h) red[0][tid] += red[0][tid + h];
+      __syncthreads();
+    }
+    if (tid == 0 && !neg) grad[(size_t)b * P + mp] += red[0][0];
+    __syncthreads();
+  }
+  if (tid == 0) {
+    if (!neg && infl != 0.0) grad[(size_t)b * P + P - 1] += tot_inf * infl * kLn10;
+    // normalise the seed of the spectral adjoint to O(1) so the double-float sinks
+    // stay well inside the float range
+    const double unit = transmission ? 1.0 : ev[b].scaling * kPi * 1e-3;
+    const double mx = tot_max * unit;
+    double nrm = 1.0, inv = 1.0;
+    if (mx > 0.0 && isfinite(mx)) {
+      const int e = ilogb(mx);
+      nrm = ldexp(1.0, -e);
+      inv = ldexp(1.0, e);
+    }
+    seed[b * 3 + 0] = nrm;
+    seed[b * 3 + 1] = inv;
+    seed[b * 3 + 2] = tot_gs;
+  }
+}
+
+// ------------------------------------------------------------------ spectral adjoint (emission)
+struct AdjointArgs {
+  const LevelInfo* lev;
+  const LevelSpecies* ls;
+  const LevelSpeciesDF* lsdf;
+  const EvalInfo* ev;
+  const float2* dwT;
+  const double* istore;
+  const double* gS;
+  const double* seed;
+  double* partial;
+  int V;
+};
+
+// Adjoint of one short-characteristics layer in FP64 (forward: sc_layer):
+// I = a (I' - B') + B + q (B - B'), a = exp(-delta), q = (a - 1) / delta,
+// delta = tau / mu. Given lam = d log L / d I it accumulates d/dB, d/dB', d/dtau and
+// replaces lam by d log L / d I'.
+__device__ __forceinline__ void sc_layer_adjoint_fp64(double tau, double B, double Bp, double Ip1, double Ip2,
+                                                      double& lam1, double& lam2, double& gB, double& gBp,
+                                                      double& gtau) {
+  const double dB = B - Bp;
+  const double rtau = 1.0 / tau;
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const double d = tau * kInvMu[i];
+    const double a = exp(-d);
+    const double rd = kMu[i] * rtau;  // 1 / delta
+    const double q = (a - 1.0) * rd;
+    double& lam = i == 0 ? lam1 : lam2;
+    const double Ip = i == 0 ? Ip1 : Ip2;
+    gB = fma(lam, 1.0 + q, gB);
+    gBp = fma(lam, -a - q, gBp);
+    // dq/ddelta = -(a + q) / delta; Taylor series 1/2 - d/3 + d^2/8 - d^3/30 + d^4/144 below 1e-2
+    const double dq = d < 1e-2 ? fma(d, fma(d, fma(d, fma(d, 1.0 / 144.0, -1.0 / 30.0), 0.125), -1.0 / 3.0), 0.5)
+                               : -(a + q) * rd;
+    const double gd = fma(-a * lam, Ip - Bp, dq * lam * dB);
+    gtau = fma(gd, kInvMu[i], gtau);
+    lam *= a;
+  }
+}
+
+// Gauss nodes and their reciprocals as double-floats
+constexpr double kMu0 = 0.211324865405187, kMu1 = 0.788675134594813;
+constexpr float kMuHi0 = (float)kMu0, kMuLo0 = (float)(kMu0 - (double)kMuHi0);
+constexpr float kMuHi1 = (float)kMu1, kMuLo1 = (float)(kMu1 - (double)kMuHi1);
+constexpr float kInvMuHi0 = (float)(1.0 / kMu0), kInvMuLo0 = (float)(1.0 / kMu0 - (double)kInvMuHi0);
+constexpr float kInvMuHi1 = (float)(1.0 / kMu1), kInvMuLo1 = (float)(1.0 / kMu1 - (double)kInvMuHi1);
+constexpr float kThirdHi = (float)(1.0 / 3.0), kThirdLo = (float)(1.0 / 3.0 - (double)kThirdHi);
+constexpr float kSixthHi = (float)(1.0 / 6.0), kSixthLo = (float)(1.0 / 6.0 - (double)kSixthHi);
+
+// The same layer adjoint in double-float arithmetic (precision mode 0), from the
+// layer's optical depth t and its reciprocal rt as double-floats. Below delta = 1e-2
+// 1 + q, -a - q and dq/ddelta come from their Taylor series (no cancellation):
+// 1 + q = d (1/2 - d/6 + d^2/24 - d^3/120 + d^4/720), dq/dd = 1/2 - d/3 + d^2/8 - d^3/30
+// + d^4/144, -a - q = d dq/dd.
+__device__ __forceinline__ void sc_layer_adjoint_df(df2 t, df2 rt, df2 B, df2 Bp, df2 Ip1, df2 Ip2, df2& lam1,
+                                                    df2& lam2, df2& gB, df2& gBp, df2& gtau, const ExpTables& et) {
+  const df2 dB = df_sub(B, Bp);
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const df2 invmu = i == 0 ? df2{kInvMuHi0, kInvMuLo0} : df2{kInvMuHi1, kInvMuLo1};
+    const df2 mu = i == 0 ? df2{kMuHi0, kMuLo0} : df2{kMuHi1, kMuLo1};
+    const df2 d = df_mul(t, invmu);
+    const df2 a = df_exp_neg(d, et.hi, et.lo);
+    df2 s1, nq, dq;
+    if (d.hi < 1e-2f) {
+      const float df_ = d.hi;
+      const float p1 = BGB_FMA(-df_, BGB_FMA(-df_, 1.0f / 720.0f, 1.0f / 120.0f), 1.0f / 24.0f);
+      df2 P = df_sub(df2{kSixthHi, kSixthLo}, df_mul_f(d, p1));
+      P = df_sub(df_make(0.5f), df_mul(d, P));
+      s1 = df_mul(d, P);
+      const float p2 = BGB_FMA(-df_, BGB_FMA(-df_, 1.0f / 144.0f, 1.0f / 30.0f), 0.125f);
+      df2 Q = df_sub(df2{kThirdHi, kThirdLo}, df_mul_f(d, p2));
+      dq = df_sub(df_make(0.5f), df_mul(d, Q));
+      nq = df_mul(d, dq);
+    } else {
+      const df2 rd = df_mul(rt, mu);  // 1 / delta
+      const df2 q = df_mul(df_sub(a, df_make(1.0f)), rd);
+      s1 = df_add(df_make(1.0f), q);
+      nq = df_neg(df_add(a, q));
+      dq = df_mul(nq, rd);
+    }
+    df2& lam = i == 0 ? lam1 : lam2;
+    const df2 Ip = i == 0 ? Ip1 : Ip2;
+    gB = df_add(gB, df_mul(lam, s1));
+    gBp = df_add(gBp, df_mul(lam, nq));
+    const df2 gd = df_sub(df_mul(dq, df_mul(lam, dB)), df_mul(a, df_mul(lam, df_sub(Ip, Bp))));
+    gtau = df_add(gtau, df_mul(gd, invmu));
+    lam = df_mul(lam, a);
+  }
+}
+
+// One thread per wavenumber (kAdjThreads per block), grid (evaluations, tiles).
+// Dynamic shared memory: per-species opacity terms of two levels,
+// float2 [2][S][kAdjThreads] then double [2][S][kAdjThreads].
+// partial[b][l][v][tile]: v = 0..S-1 d log L / d ln n_s, S temperature, S+1 lev.dz,
+// S+2 lev.cloud (all times the evaluation's seed normaliser).
+template <bool DF, int VP>
+__global__ void __launch_bounds__(kAdjThreads) emission_adjoint_kernel(DeviceModel dm, AdjointArgs a) {
+  typedef AccType<DF> AT;
+  typedef typename AT::type A;
+  constexpr int NW = kAdjThreads / 32;
+  constexpr int G = 32 / VP;
+  __shared__ ExpTables et;
+  __shared__ double red[NW][VP];
+  extern __shared__ __align__(16) unsigned char adj_smem[];
+  const int S = dm.S, L = dm.L;
+  float2* tdf = reinterpret_cast<float2*>(adj_smem);
+  double* twd = reinterpret_cast<double*>(adj_smem + (size_t)2 * S * kAdjThreads * sizeof(float2));
+  if (DF) load_exp_tables(et);
+  __syncthreads();
+  const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int kk = blockIdx.y * kAdjThreads + tid;
+  const bool active = kk < dm.N;
+  const int k = active ? kk : dm.N - 1;  // idle lanes repeat the last wavenumber with a zero seed
+  const size_t N = dm.N;
+  const LevelInfo* lv = a.lev + (size_t)b * L;
+  const LevelSpecies* sp = a.ls + (size_t)b * L * S;
+  const LevelSpeciesDF* sf = a.lsdf + (size_t)b * L * S;
+  const float2* dw = a.dwT + (size_t)b * L * S;
+  const double* Is = a.istore + (size_t)b * L * 2 * N + k;
+
+  // seed: d log L / dF_k = sum_r W_rk gS_r, F = scaling 2 pi 1e-3 (mu1 I1 + mu2 I2) / 2
+  double gF = 0.0;
+  {
+    const double* g = a.gS + (size_t)b * dm.M;
+    const int e1 = __ldg(&dm.col_ptr[k + 1]);
+    for (int e = __ldg(&dm.col_ptr[k]); e < e1; ++e) gF = fma(__ldg(&dm.col_w[e]), g[__ldg(&dm.col_row[e])], gF);
+  }
+  const double sd = active ? gF * a.seed[b * 3] * __ldg(&a.ev[b].scaling) * (kPi * 1e-3) : 0.0;
+
+  // level opacity; per-species terms into buffer q; d kappa / dT (double-float part
+  // and an FP64 part for terms outside the float range)
+  auto kappa_terms = [&](int l, int q, df2& dk_out, double& dkw_out, bool& wide) -> Kappa {
+    float2* td = tdf + (size_t)q * S * kAdjThreads + tid;
+    double* tw = twd + (size_t)q * S * kAdjThreads + tid;
+    const float2* dwl = dw + (size_t)l * S;
+    Kappa kp;
+    if (DF) {
+      df2 dk = {0.0f, 0.0f};
+      double dkw = 0.0;
+      bool wd = false;
+      kp = level_kappa_df_cb(dm.table_df, N, sp + (size_t)l * S, sf + (size_t)l * S, S, k, et,
+                             [&](int s, df2 t, double t_w, bool is_wide, df2 lo, df2 hi) {
+                               const float2 d = __ldg(dwl + s);
+                               td[(size_t)s * kAdjThreads] = make_float2(t.hi, t.lo);
+                               tw[(size_t)s * kAdjThreads] = t_w;
+                               if (d.x != 0.0f) {
+                                 const df2 slope = df_mul(df_sub(hi, lo), df2{d.x, d.y});
+                                 if (is_wide) dkw += t_w * df_to_double(slope);
+                                 else dk = df_add(dk, df_mul(t, slope));
+                               }
+                               wd = wd || is_wide;
+                             });
+      dk_out = df_mul(dk, df2{kLn10Hi, kLn10Lo});
+      dkw_out = dkw * kLn10;
+      wide = wd;
+    } else {
+      double dk = 0.0;
+      kp.v = df2{0.0f, 0.0f};
+      kp.wide = level_absorption_fp64_cb(dm.table64, N, sp + (size_t)l * S, S, k,
+                                         [&](int s, double t, double lo, double hi) {
+                                           const float2 d = __ldg(dwl + s);
+                                           tw[(size_t)s * kAdjThreads] = t;
+                                           dk += t * (hi - lo) * ((double)d.x + (double)d.y);
+                                         });
+      dk_out = df2{0.0f, 0.0f};
+      dkw_out = dk * kLn10;
+      wide = true;
+    }
+    return kp;
+  };
+  // reduce one level's sinks over the block and write the block's partial sums;
+  // gK, gT, gdz, gcl as double-floats (mode 0) or in the .wide-style FP64 arguments (mode 1)
+  auto emit = [&](int l, int q, df2 gK, double gK64, A gT, A gdz, A gcl, bool wide) {
+    const float2* td = tdf + (size_t)q * S * kAdjThreads + tid;
+    const double* tw = twd + (size_t)q * S * kAdjThreads + tid;
+    A v[VP];
+#pragma unroll
+    for (int j = 0; j < VP; ++j) {
+      A x = AT::zero();
+      if (j < S) {
+        if constexpr (DF) {
+          const float2 t = td[(size_t)j * kAdjThreads];
+          x = df_mul(gK, df2{t.x, t.y});
+          if (wide) x = df_add(x, df_from_double(df_to_double(gK) * tw[(size_t)j * kAdjThreads]));
+        } else {
+          x = gK64 * tw[(size_t)j * kAdjThreads];
+        }
+      } else if (j == S) {
+        x = gT;
+      } else if (j == S + 1) {
+        x = gdz;
+      } else if (j == S + 2) {
+        x = gcl;
+      }
+      v[j] = x;
+    }
+    const A r = warp_reduce_scatter<VP>(v, lane);
+    if (lane % G == 0) red[warp][lane / G] = acc_to_double(r);
+    __syncthreads();
+    if (tid < a.V) {
+      double s = 0.0;
+#pragma unroll
+      for (int w = 0; w < NW; ++w) s += red[w][tid];
+      a.partial[(((size_t)b * L + l) * a.V + tid) * gridDim.y + blockIdx.y] = s;
+    }
+    __syncthreads();
+  };
+
+  int q = 0;
+  if constexpr (DF) {
+    // ---------------- double-float recurrence (precision mode 0)
+    const float2 c1f = __ldg(dm.planck_c1_df + k), c2f = __ldg(dm.planck_c2l_df + k);
+    const df2 c1 = {c1f.x, c1f.y}, c2l = {c2f.x, c2f.y};
+    const df2 c2 = df_mul(c2l, df2{kLn2Hi, kLn2Lo});  // h nu c / k
+    const df2 rc1 = df_div(df_make(1.0f), c1);
+    auto invT = [&](int l) {
+      const float2 it = __ldg(reinterpret_cast<const float2*>(&lv[l].invT_hi));
+      return df2{it.x, it.y};
+    };
+    // dB/dT = B (1 + B / c1) x / T with x = c2 / T
+    auto dplanck = [&](int l, df2 B) {
+      const df2 it = invT(l);
+      return df_mul(df_mul(B, df_add(df_make(1.0f), df_mul(B, rc1))), df_mul(df_mul(c2, it), it));
+    };
+    df2 lam1 = df_from_double(sd * kMu[0]), lam2 = df_from_double(sd * kMu[1]);
+    df2 dk_l;
+    double dkw_l;
+    bool wide_l;
+    Kappa kap_l = kappa_terms(L - 1, q, dk_l, dkw_l, wide_l);
+    df2 B_l = planck_df2(c1, c2l, invT(L - 1), et.hi, et.lo);
+    const df2 z = {0.0f, 0.0f};
+    df2 gB_l = z, gK_l = z, gdz_l = z, gcl_l = z;
+    for (int l = L - 1; l >= 1; --l) {
+      df2 dk_m;
+      double dkw_m;
+      bool wide_m;
+      const Kappa kap_m = kappa_terms(l - 1, q ^ 1, dk_m, dkw_m, wide_m);
+      const df2 B_m = planck_df2(c1, c2l, invT(l - 1), et.hi, et.lo);
+      // layer optical depth as in the forward pass (emission_layer_tau_df)
+      const float4 g = __ldg(reinterpret_cast<const float4*>(&lv[l - 1].dzh_hi));  // dzh, cloud
+      const df2 dzh = {g.x, g.y};
+      const bool narrow = kap_l.wide == 0.0 && kap_m.wide == 0.0;
+      df2 t = df_add(df_mul(dzh, df_add(kap_l.v, kap_m.v)), df2{g.z, g.w});
+      bool opaque_layer = t.hi != 0.0f;
+      if (!narrow || !(t.hi > 1e-30f && t.hi < 1e30f)) {
+        const double ks = (df_to_double(kap_l.v) + kap_l.wide) + (df_to_double(kap_m.v) + kap_m.wide);
+        const double tau = __ldg(&lv[l - 1].dz) * ks / 2. + __ldg(&lv[l - 1].cloud);
+        opaque_layer = tau != 0.0;
+        t = df_from_double(fmin(tau, 1e37));
+      }
+      df2 gB_m = z, gtau = z;
+      if (opaque_layer) {
+        const df2 rt = t.hi > 1e-30f ? df_div(df_make(1.0f), t) : z;  // only used above delta = 1e-2
+        const df2 Ip1 = df_from_double(Is[(size_t)(l - 1) * 2 * N]);
+        const df2 Ip2 = df_from_double(Is[(size_t)(l - 1) * 2 * N + N]);
+        sc_layer_adjoint_df(t, rt, B_l, B_m, Ip1, Ip2, lam1, lam2, gB_l, gB_m, gtau, et);
+      }
+      gK_l = df_add(gK_l, df_mul(gtau, dzh));
+      df2 gT = df_add(df_mul(gK_l, dk_l), df_mul(gB_l, dplanck(l, B_l)));
+      if (wide_l) gT = df_add(gT, df_from_double(df_to_double(gK_l) * dkw_l));
+      emit(l, q, gK_l, 0.0, gT, gdz_l, gcl_l, wide_l);
+      // layer l's own sinks belong to lev[l-1] (its dz and cloud)
+      if (narrow) {
+        gdz_l = df_mul(gtau, df_mul_f(df_add(kap_l.v, kap_m.v), 0.5f));
+      } else {
+        const double ks = (df_to_double(kap_l.v) + kap_l.wide) + (df_to_double(kap_m.v) + kap_m.wide);
+        gdz_l = df_from_double(df_to_double(gtau) * 0.5 * ks);
+      }
+      gcl_l = gtau;
+      gK_l = df_mul(gtau, dzh);
+      gB_l = gB_m;
+      B_l = B_m;
+      kap_l = kap_m;
+      dk_l = dk_m;
+      dkw_l = dkw_m;
+      wide_l = wide_m;
+      q ^= 1;
+    }
+    gB_l = df_add(gB_l, df_add(lam1, lam2));  // both angles start from I = B at the bottom level
+    df2 gT = df_add(df_mul(gK_l, dk_l), df_mul(gB_l, dplanck(0, B_l)));
+    if (wide_l) gT = df_add(gT, df_from_double(df_to_double(gK_l) * dkw_l));
+    emit(0, q, gK_l, 0.0, gT, gdz_l, gcl_l, wide_l);
+  } else {
+    // ---------------- FP64 recurrence with the CUDA math library (precision mode 1)
+    const double c1d = __ldg(dm.planck_c1 + k), c2d = __ldg(dm.planck_c2 + k);
+    const double rc1 = 1.0 / c1d;
+    auto planck = [&](int l) { return c1d / (exp(c2d * __ldg(&lv[l].invT)) - 1.0); };
+    auto dplanck = [&](int l, double B) {
+      const double it = __ldg(&lv[l].invT);
+      return B * fma(B, rc1, 1.0) * (c2d * it) * it;
+    };
+    double lam1 = sd * kMu[0], lam2 = sd * kMu[1];
+    df2 unused = {0.0f, 0.0f};
+    double dk_l;
+    bool wide_l;
+    Kappa kap_l = kappa_terms(L - 1, q, unused, dk_l, wide_l);
+    double B_l = planck(L - 1);
+    double gB_l = 0.0, gK_l = 0.0, gdz_l = 0.0, gcl_l = 0.0;
+    for (int l = L - 1; l >= 1; --l) {
+      double dk_m;
+      bool wide_m;
+      const Kappa kap_m = kappa_terms(l - 1, q ^ 1, unused, dk_m, wide_m);
+      const double B_m = planck(l - 1);
+      const double tau = __ldg(&lv[l - 1].dz) * (kap_l.wide + kap_m.wide) / 2. + __ldg(&lv[l - 1].cloud);
+      double gB_m = 0.0, gtau = 0.0;
+      if (tau != 0.0) {
+        const double Ip1 = Is[(size_t)(l - 1) * 2 * N], Ip2 = Is[(size_t)(l - 1) * 2 * N + N];
+        sc_layer_adjoint_fp64(tau, B_l, B_m, Ip1, Ip2, lam1, lam2, gB_l, gB_m, gtau);
+      }
+      const double dzh = 0.5 * __ldg(&lv[l - 1].dz);
+      gK_l = fma(gtau, dzh, gK_l);
+      emit(l, q, unused, gK_l, fma(gK_l, dk_l, gB_l * dplanck(l, B_l)), gdz_l, gcl_l, wide_l);
+      gdz_l = gtau * 0.5 * (kap_l.wide + kap_m.wide);
+      gcl_l = gtau;
+      gK_l = gtau * dzh;
+      gB_l = gB_m;
+      B_l = B_m;
+      kap_l = kap_m;
+      dk_l = dk_m;
+      wide_l = wide_m;
+      q ^= 1;
+    }
+    gB_l += lam1 + lam2;
+    emit(0, q, unused, gK_l, fma(gK_l, dk_l, gB_l * dplanck(0, B_l)), gdz_l, gcl_l, wide_l);
+  }
+}
+
+// ------------------------------------------------------------------ parameter tangents
+// Mixing ratios X_j = n_j / n_total after the chemistry modules (level independent
+// for isoprofile and background chemistry) and their derivative along chemistry
+// parameter tc (-1: none). IsoprofileChemistry::calcChemicalComposition
+// src/chemistry/isoprofile_chemistry.cpp:87-119, BackgroundChemistry
+// src/chemistry/background_chemistry.cpp:72-137, Chemistry::meanMolecularWeight
+// src/chemistry/chemistry.h:47-59.
+__device__ void chemistry_tangent(const AtmosphereConfig& c, const double* chem, int tc, double* X, double* dX,
+                                  double& mmw, double& dmmw) {
+  for (int j = 0; j < kSpeciesCount; ++j) {
+    X[j] = 0.0;
+    dX[j] = 0.0;
+  }
+  X[SP_TOTAL] = 1.0;
+  mmw = dmmw = 0.0;
+  int pidx = 0;
+  for (int m = 0; m < c.nchem; ++m) {
+    if (c.chem_kind[m] == 0) {
+      for (int j = 0; j < c.chem_nsp[m]; ++j) {
+        X[c.chem_sp[m][j]] = chem[pidx + j];
+        dX[c.chem_sp[m][j]] = (tc == pidx + j) ? 1.0 : 0.0;
+      }
+      if (!c.chem_na_free[m]) {
+        X[SP_Na] = X[SP_K] * 16.2181;
+        dX[SP_Na] = dX[SP_K] * 16.2181;
+      }
+      pidx += c.chem_nsp[m];
+    } else {
+      double bg = 1.0, dbg = 0.0;
+      for (int j = 1; j < kSpeciesCount; ++j) {
+        const bool other = c.chem_bg_h2he[m] ? (j != SP_H2 && j != SP_He) : (j != c.chem_bg_sp[m]);
+        if (other) {
+          bg -= X[j];
+          dbg -= dX[j];
+        }
+      }
+      if (bg < 0) bg = dbg = 0.0;
+      if (c.chem_bg_h2he[m]) {
+        const double f2 = kSolarH2 / (kSolarH2 + kSolarHe), fe = kSolarHe / (kSolarH2 + kSolarHe);
+        X[SP_H2] = bg * f2;
+        dX[SP_H2] = dbg * f2;
+        X[SP_He] = bg * fe;
+        dX[SP_He] = dbg * fe;
+      } else {
+        X[c.chem_bg_sp[m]] = bg;
+        dX[c.chem_bg_sp[m]] = dbg;
+      }
+    }
+    mmw = dmmw = 0.0;
+    for (int j = 1; j < kSpeciesCount; ++j) {
+      mmw += X[j] * kMolWeight[j];
+      dmmw += dX[j] * kMolWeight[j];
+    }
+  }
+}
+
+// One block per evaluation. sg[L][V] = the partial sums reduced over the tiles;
+// then thread th < P forms d log L / d param_th = sum over levels of the sinks
+// times the tangents of ln n_s, T, lev.dz and lev.cloud along param_th
+// (EmissionModel::calcAtmosphereStructure src/forward_model/emission/emission.cpp:158-189,
+// Atmosphere::calcAltitude src/forward_model/atmosphere/atmosphere.cpp:288-307,
+// GreyCloudModel src/cloud_model/grey_cloud_model.cpp:59-195,
+// EmissionModel::radiusDistanceScaling emission.cpp:108-120).
+__global__ void __launch_bounds__(kAdjThreads) atmosphere_adjoint_kernel(
+    DeviceModel dm, const double* __restrict__ params, int P, const LevelInfo* __restrict__ lev,
+    const EvalInfo* __restrict__ ev, const double* __restrict__ partial, int V, int tiles,
+    const double* __restrict__ seed, double* __restrict__ grad) {
+  extern __shared__ double sg[];
+  const AtmosphereConfig& c = *dm.cfg;
+  const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  const int L = c.L, S = c.S;
+  if (ev[b].neglect) return;
+  const double inv = seed[b * 3 + 1];
+  for (int idx = warp; idx < L * V; idx += nw) {
+    const double* p = partial + ((size_t)b * L * V + idx) * tiles;
+    double s = 0.0;
+    for (int j = lane; j < tiles; j += 32) s += p[j];
+    s = warp_sum_d(s);
+    if (lane == 0) sg[idx] = s * inv;
+  }
+  __syncthreads();
+  if (tid >= P) return;
+  const int th = tid;
+  const double* par = params + (size_t)b * P;
+  const double* gen = par;
+  const int ng = c.nparam_general, nc = c.nparam_chem, nt = c.nparam_temp;
+  const double* chem = par + ng;
+  const double* temp = chem + nc;
+  const double* cloud = temp + nt;
+
+  double X[kSpeciesCount], dX[kSpeciesCount], mmw, dmmw;
+  chemistry_tangent(c, chem, (th >= ng && th < ng + nc) ? th - ng : -1, X, dX, mmw, dmmw);
+
+  // temperature: T = poly(dof, log10 p), dof_i = temp_0 temp_1 ... temp_i (a constant profile: T = temp_0)
+  const int tm = th - ng - nc;
+  const bool temp_theta = tm >= 0 && tm < nt;
+  double ddof[kMaxPolyDof];
+  if (temp_theta && c.temp_poly) {
+    for (int i = 0; i < c.pp_ndof; ++i) {
+      double v = 0.0;
+      if (i >= tm) {
+        v = 1.0;
+        for (int j = 0; j <= i; ++j)
+          if (j != tm) v *= temp[j];
+      }
+      ddof[i] = v;
+    }
+  }
+  const double g = pow(10.0, gen[0]);
+  const double dlng = th == 0 ? kLn10 : 0.0;  // d ln g / d log g
+  const int ci = ng + nc + nt;                 // cloud optical depth parameter
+  const EvalInfo e = ev[b];
+  double cloud_d = 0.0;
+  if (c.cloud && th == ci && cloud[0] >= 0)
+    cloud_d = 1.0 / (double)((unsigned)e.cloud_top - (unsigned)e.cloud_bottom);
+
+  double acc = 0.0, u_prev = 0.0, du_prev = 0.0;
+  for (int l = 0; l < L; ++l) {
+    const double T = lev[(size_t)b * L + l].T;
+    double dT = 0.0;
+    if (temp_theta) dT = c.temp_poly ? poly_value(c, ddof, dm.log10p[l]) : (tm == 0 ? 1.0 : 0.0);
+    const double dlnT = dT / T;
+    const double* sgl = sg + (size_t)l * V;
+    // n_s = prod over the species and its collision partners of n_total X_j, n_total = p / (k T)
+    for (int s = 0; s < S; ++s) {
+      const double gl = sgl[s];
+      if (gl == 0.0) continue;
+      double dln = 0.0;
+      bool zero = false;
+      const int js[3] = {c.sp_index[s], c.sp_partner[s][0], c.sp_partner[s][1]};
+      for (int u = 0; u < 3; ++u) {
+        if (js[u] < 0) continue;
+        if (X[js[u]] == 0.0) zero = true;
+        else dln += dX[js[u]] / X[js[u]] - dlnT;
+      }
+      if (!zero) acc = fma(gl, dln, acc);
+    }
+    acc = fma(sgl[S], dT, acc);
+    // layer thickness Delta_l = 0.5 (p_{l-1} - p_l) 1e6 (u_l + u_{l-1}) / g, u = R T / (mmw p 1e6)
+    const double p = dm.pressure[l];
+    const double u = kGasConst * T / (mmw * p * 1e6);
+    const double du = u * (dlnT - dmmw / mmw);
+    if (l >= 1) {
+      const double pf = 0.5 * (dm.pressure[l - 1] * 1e6 - p * 1e6) / g;
+      acc = fma(sg[(size_t)(l - 1) * V + S + 1], pf * ((du + du_prev) - (u + u_prev) * dlng), acc);
+    }
+    u_prev = u;
+    du_prev = du;
+    // grey cloud: tau_c / (top - bottom) on layers bottom < l <= top, l < L - 1
+    if (cloud_d != 0.0 && (unsigned)l <= (unsigned)e.cloud_top && (unsigned)l > (unsigned)e.cloud_bottom &&
+        l < L - 1)
+      acc = fma(sgl[S + 2], cloud_d, acc);
+  }
+  // radius-distance scaling (R_J / d)^2 f
+  const double gsc = seed[b * 3 + 2] / e.scaling;
+  if (th == 1) acc += gsc * (kRJupiter / gen[2]) * (kRJupiter / gen[2]);
+  if (th == 2) acc += gsc * (-2.0 * e.scaling / gen[2]);
+  grad[(size_t)b * P + th] += acc;
+}
+
+// ------------------------------------------------------------------ host side
+void free_grad_workspace(Model& m) {
+  GradWorkspace& g = m.gws;
+  cudaFree(g.taps.dwT);
+  cudaFree(g.taps.istore);
+  cudaFree(g.gS);
+  cudaFree(g.seed);
+  cudaFree(g.partial);
+  g = GradWorkspace{};
+}
+
+namespace {
+
+int value_slots(int V) { return V <= 8 ? 8 : V <= 16 ? 16 : 32; }
+
+size_t adjoint_smem(const Model& m) { return (size_t)2 * m.acfg.S * kAdjThreads * (sizeof(float2) + sizeof(double)); }
+
+size_t grad_bytes_per_eval(const Model& m, int tiles, int V) {
+  const size_t L = m.L, N = m.N, S = std::max(m.acfg.S, 1), M = std::max(m.M, 1);
+  return L * 2 * N * 8 + L * S * sizeof(float2) + M * 8 + 3 * 8 + L * (size_t)V * tiles * 8;
+}
+
+void ensure_grad_workspace(Model& m, int chunk, int tiles, int V) {
+  GradWorkspace& g = m.gws;
+  if (chunk <= g.capacity && tiles == g.tiles) return;
+  BGB_CUDA(cudaDeviceSynchronize());
+  free_grad_workspace(m);
+  const size_t B = chunk, L = m.L, N = m.N, S = std::max(m.acfg.S, 1), M = std::max(m.M, 1);
+  BGB_CUDA(cudaMalloc(&g.taps.dwT, B * L * S * sizeof(float2)));
+  BGB_CUDA(cudaMalloc(&g.taps.istore, B * L * 2 * N * sizeof(double)));
+  BGB_CUDA(cudaMalloc(&g.gS, B * M * sizeof(double)));
+  BGB_CUDA(cudaMalloc(&g.seed, B * 3 * sizeof(double)));
+  BGB_CUDA(cudaMalloc(&g.partial, B * L * (size_t)V * tiles * sizeof(double)));
+  g.capacity = chunk;
+  g.tiles = tiles;
+}
+
+template <bool DF, int VP>
+void launch_emission_adjoint(const Model& m, dim3 grid, size_t smem, cudaStream_t st, const AdjointArgs& a) {
+  if (smem > 48 * 1024)
+    BGB_CUDA(cudaFuncSetAttribute(emission_adjoint_kernel<DF, VP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+  emission_adjoint_kernel<DF, VP><<<grid, kAdjThreads, smem, st>>>(m.dm, a);
+}
+
+}  // namespace
+
+void launch_gradient(Model& m, const double* params_dev, int batch, cudaStream_t st, double* loglike_dev,
+                     double* grad_dev, uint8_t* neglect_dev) {
+  if (m.transmission) throw Error(BEAR_ERR_UNSUPPORTED, "gradient of transmission models not available");
+  const int S = m.acfg.S, L = m.L, P = m.acfg.nparam_total;
+  const int V = S + 3;
+  if (V > 32) throw Error(BEAR_ERR_UNSUPPORTED, "the gradient supports at most 29 table species");
+  if (P > kAdjThreads) throw Error(BEAR_ERR_UNSUPPORTED, "the gradient supports at most 128 parameters");
+  const int tiles = (int)((m.N + kAdjThreads - 1) / kAdjThreads);
+  const size_t per_eval = grad_bytes_per_eval(m, tiles, V);
+  const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)batch, m.grad_budget / per_eval));
+  BGB_CUDA(cudaSetDevice(m.device));
+  ensure_workspace(m, chunk);
+  ensure_grad_workspace(m, chunk, tiles, V);
+  const GradWorkspace& g = m.gws;
+  const Workspace& w = m.ws;
+  const size_t smem = adjoint_smem(m);
+  const size_t smem_atm = (size_t)L * V * sizeof(double);
+  if (smem > 227 * 1024 || smem_atm > 227 * 1024)
+    throw Error(BEAR_ERR_UNSUPPORTED, "model too large for the adjoint kernels' shared memory");
+  if (smem_atm > 48 * 1024)
+    BGB_CUDA(cudaFuncSetAttribute(atmosphere_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem_atm));
+  const int VP = value_slots(V);
+  const bool df = m.precision == 0;
+  for (int c0 = 0; c0 < batch; c0 += chunk) {
+    const int nb = std::min(chunk, batch - c0);
+    const double* pc = params_dev + (size_t)c0 * P;
+    double* gc = grad_dev + (size_t)c0 * P;
+    launch_forward_taps(m, pc, nb, st, neglect_dev ? neglect_dev + c0 : nullptr, loglike_dev + c0, g.taps);
+    obs_adjoint_kernel<<<nb, 256, 0, st>>>(m.dm, pc, P, w.ev, w.obs, g.gS, g.seed, gc, 0);
+    BGB_CUDA(cudaGetLastError());
+    AdjointArgs a{w.lev, w.ls, w.lsdf, w.ev, g.taps.dwT, g.taps.istore, g.gS, g.seed, g.partial, V};
+    const dim3 grid(nb, tiles);
+    if (df) {
+      if (VP == 8) launch_emission_adjoint<true, 8>(m, grid, smem, st, a);
+      else if (VP == 16) launch_emission_adjoint<true, 16>(m, grid, smem, st, a);
+      else launch_emission_adjoint<true, 32>(m, grid, smem, st, a);
+    } else {
+      if (VP == 8) launch_emission_adjoint<false, 8>(m, grid, smem, st, a);
+      else if (VP == 16) launch_emission_adjoint<false, 16>(m, grid, smem, st, a);
+      else launch_emission_adjoint<false, 32>(m, grid, smem, st, a);
+    }
+    BGB_CUDA(cudaGetLastError());
+    atmosphere_adjoint_kernel<<<nb, kAdjThreads, smem_atm, st>>>(m.dm, pc, P, w.lev, w.ev, g.partial, V, tiles,
+                                                                 g.seed, gc);
+    BGB_CUDA(cudaGetLastError());
+  }
 }
 
 }  // namespace bgb

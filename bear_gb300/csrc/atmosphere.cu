@@ -8,60 +8,18 @@
 
 #include "model.h"
 #include "dfloat.cuh"
+#include "level_physics.cuh"
 
 namespace bgb {
 
-namespace {
-
-// PiecewisePolynomial::getValue src/additional/piecewise_poly.cpp:154-181 and
-// Element::getValue / lagrangeBase :202-229.
-__device__ double poly_value(const AtmosphereConfig& c, const double* dof, double x) {
-  if (x > c.pp_dof_vertices[0] || x < c.pp_dof_vertices[c.pp_ndof - 1]) return 0.0;
-  for (int i = 0; i < c.pp_ndof; ++i)
-    if (c.pp_dof_vertices[i] == x) return dof[i];
-  const int nd = c.pp_ndof_el;
-  int el = 0;
-  for (int e = 0; e < c.pp_nel; ++e)
-    if (c.pp_el_vert[e * nd] > x && c.pp_el_vert[e * nd + nd - 1] < x) {
-      el = e;
-      break;
-    }
-  const double xl = c.pp_el_vert[el * nd], xr = c.pp_el_vert[el * nd + nd - 1];
-  const double r = 2.0 * (x - xl) / (xr - xl) - 1.0;
-  double y = 0;
-  for (int i = 0; i < nd; ++i) {
-    double l = 1;
-    for (int j = 0; j < nd; ++j) {
-      if (i == j) continue;
-      l *= (r - c.pp_ref[j]) / (c.pp_ref[i] - c.pp_ref[j]);
-    }
-    y += dof[el * (nd - 1) + i] * l;
-  }
-  return y;
-}
-
-__device__ __constant__ double kMolWeight[kSpeciesCount] = {
-    0.0,      1.00784, 4.002602, 12.0107, 15.999,   55.845,   55.845,  40.078,  47.867,
-    47.867,   2.01588, 18.01528, 44.01,   28.0101,  16.04246, 27.0253, 17.03052, 26.04,
-    28.0134,  22.98977, 39.0983, 34.09099, 1.00784, 63.8664,  66.9409, 56.853,  34.08,
-    40.3044,  42.981,  56.0774,  54.0040, 26.3209,  41.0859,  48.87484, 17.008,
-    5.4857990907e-4, 50.9415, 50.9415, 54.938044, 28.085, 51.996, 51.996, 44.08, 60.08,
-    64.066,   76.139};
-
-// Chemistry::meanMolecularWeight src/chemistry/chemistry.h:47-59
-__device__ double mean_molecular_weight(const double* n) {
-  double mu = 0;
-  for (int j = 0; j < kSpeciesCount; ++j) mu += n[j] / n[SP_TOTAL] * kMolWeight[j];
-  return mu;
-}
-
-}  // namespace
 
 // One block per evaluation, blockDim.x >= L. Dynamic shared memory: 4 L doubles.
+// dwT (optional, B x L x S) receives the temperature derivative of each stencil's
+// temperature weight.
 __global__ void __launch_bounds__(kMaxLevels) atmosphere_kernel(DeviceModel dm, const double* __restrict__ params, int P,
                                   LevelInfo* __restrict__ lev, LevelSpecies* __restrict__ ls,
                                   LevelSpeciesDF* __restrict__ lsdf, double* __restrict__ ray_n,
-                                  EvalInfo* __restrict__ ev) {
+                                  EvalInfo* __restrict__ ev, float2* __restrict__ dwT) {
   const AtmosphereConfig& c = *dm.cfg;
   const int b = blockIdx.x;
   const int l = threadIdx.x;
@@ -124,7 +82,7 @@ __global__ void __launch_bounds__(kMaxLevels) atmosphere_kernel(DeviceModel dm, 
         pidx += c.chem_nsp[m];
       } else {
         // BackgroundChemistry::calcChemicalComposition src/chemistry/background_chemistry.cpp:72-137
-        const double sh2 = 0.5, she = 0.085114;
+        const double sh2 = kSolarH2, she = kSolarHe;
         const double sh2he = sh2 + she;
         n[SP_TOTAL] = p * 1.e6 / kBoltzmann / T;
         double bg = 1.0;
@@ -322,6 +280,11 @@ __global__ void __launch_bounds__(kMaxLevels) atmosphere_kernel(DeviceModel dm, 
       f.wp_hi_lo = bw.lo;
       f.wT_hi = t.hi;
       f.wT_lo = t.lo;
+      // d wT / dT for the adjoint (0 when T is clamped to the end of the table)
+      if (dwT) {
+        const df2 dw = df_from_double(lo != up ? 1.0 / (Tn[up] - Tn[lo]) : 0.0);
+        dwT[((size_t)b * L + l) * S + s] = make_float2(dw.hi, dw.lo);
+      }
     }
   }
 }

@@ -216,10 +216,18 @@ int bear_model_set_precision(bear_model* h, int mode) {
   });
 }
 
+int bear_model_set_gradient_memory(bear_model* h, long long bytes) {
+  return guarded([&] {
+    if (!h) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null model");
+    if (bytes < 0) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "bytes must be non-negative");
+    h->m.grad_budget = bytes ? (size_t)bytes : (size_t(16) << 30);
+  });
+}
+
 int bear_model_set_launch(bear_model* h, int rt_threads, int obs_threads) {
   return guarded([&] {
     if (!h) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null model");
-    if (rt_threads < 0 || rt_threads > 256 || rt_threads % 32) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "rt_threads must be a multiple of 32 up to 256");
+    if (rt_threads < 0 || rt_threads > 256 || rt_threads % 16) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "rt_threads must be a multiple of 16 up to 256");
     if (obs_threads < 0 || obs_threads > 1024 || obs_threads % 32) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "obs_threads must be a multiple of 32 up to 1024");
     h->m.rt_threads = rt_threads;
     h->m.obs_threads = obs_threads;

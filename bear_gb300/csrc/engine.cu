@@ -39,6 +39,7 @@
 #include "../../include/bear_gb300.h"
 #include "model.h"
 #include "physics.cuh"
+#include "rt_common.cuh"
 
 namespace bgb {
 
@@ -52,153 +53,22 @@ namespace bgb {
 __global__ void atmosphere_kernel(DeviceModel dm, const double* __restrict__ params, int P,
                                   LevelInfo* __restrict__ lev, LevelSpecies* __restrict__ ls,
                                   LevelSpeciesDF* __restrict__ lsdf, double* __restrict__ ray_n,
-                                  EvalInfo* __restrict__ ev);
+                                  EvalInfo* __restrict__ ev, float2* __restrict__ dwT);
 
 // Dynamic shared memory the transmission kernels opt into (the per-block maximum of
 // 227 KB less room for their static tables).
 constexpr size_t kTransmissionDynSmem = 220 * 1024;
 
-// Gauss nodes of ShortCharacteristics (src/radiative_transfer/short_characteristics.h:62-63)
-__device__ __constant__ double kMu[2] = {0.211324865405187, 0.788675134594813};
-__device__ __constant__ double kInvMu[2] = {1.0 / 0.211324865405187, 1.0 / 0.788675134594813};
-
-__device__ __forceinline__ void load_exp_tables(ExpTables& t) {
-  for (int i = threadIdx.x; i < 65; i += blockDim.x) {
-    t.hi[i] = kExp2TabHi[i];
-    t.lo[i] = kExp2TabLo[i];
-  }
-  for (int i = threadIdx.x; i < 64; i += blockDim.x) t.d[i] = kExp2TabD[i];
-}
-
-// ------------------------------------------------------------------ opacity
-// Sum over table species of 10^(bilinear log-p / T interpolation) * n at one
-// level and one wavenumber (OpacitySpecies::calcAbsorptionCrossSections
-// src/transport_coeff/opacity_species.cpp:277-345 and calcTransportCoefficients
-// :400-455), double-float arithmetic; FP64 result.
-__device__ __forceinline__ double level_absorption_df(const float2* __restrict__ tab, size_t N,
-                                                      const LevelSpecies* __restrict__ d,
-                                                      const LevelSpeciesDF* __restrict__ f, int S,
-                                                      int k, const ExpTables& et) {
-  df2 acc = {0.0f, 0.0f};
-  double wide = 0.0;
-  for (int s = 0; s < S; ++s) {
-    const float4 fa = __ldg(reinterpret_cast<const float4*>(f + s));
-    const float4 fb = __ldg(reinterpret_cast<const float4*>(f + s) + 1);
-    if (fb.z == kNoSpecies) continue;  // zero number density: the species adds nothing
-    const int4 r = __ldg(reinterpret_cast<const int4*>(d + s));
-    const float2 t0 = __ldg(tab + (size_t)r.x * N + k);
-    const float2 t1 = __ldg(tab + (size_t)r.y * N + k);
-    const float2 t2 = __ldg(tab + (size_t)r.z * N + k);
-    const float2 t3 = __ldg(tab + (size_t)r.w * N + k);
-    const df2 lo = df_lerp(df2{t0.x, t0.y}, df2{t1.x, t1.y}, df2{fa.x, fa.y});
-    const df2 hi = df_lerp(df2{t2.x, t2.y}, df2{t3.x, t3.y}, df2{fa.z, fa.w});
-    const df2 x = df_lerp(lo, hi, df2{fb.x, fb.y});
-    pow10_times_n(x, df2{fb.z, fb.w}, et.hi, et.lo, acc, wide);
-  }
-  return df_to_double(acc) + wide;
-}
-
-// The same sum kept as a double-float plus an FP64 part for terms outside the float
-// exponent range (zero almost always).
-struct Kappa {
-  df2 v;
-  double wide;
-};
-
-__device__ __forceinline__ Kappa level_kappa_df(const float2* __restrict__ tab, size_t N,
-                                                const LevelSpecies* __restrict__ d,
-                                                const LevelSpeciesDF* __restrict__ f, int S, int k,
-                                                const ExpTables& et) {
-  Kappa r = {{0.0f, 0.0f}, 0.0};
-  for (int s = 0; s < S; ++s) {
-    const float4 fa = __ldg(reinterpret_cast<const float4*>(f + s));
-    const float4 fb = __ldg(reinterpret_cast<const float4*>(f + s) + 1);
-    if (fb.z == kNoSpecies) continue;
-    const int4 rw = __ldg(reinterpret_cast<const int4*>(d + s));
-    const float2 t0 = __ldg(tab + (size_t)rw.x * N + k);
-    const float2 t1 = __ldg(tab + (size_t)rw.y * N + k);
-    const float2 t2 = __ldg(tab + (size_t)rw.z * N + k);
-    const float2 t3 = __ldg(tab + (size_t)rw.w * N + k);
-    const df2 lo = df_lerp(df2{t0.x, t0.y}, df2{t1.x, t1.y}, df2{fa.x, fa.y});
-    const df2 hi = df_lerp(df2{t2.x, t2.y}, df2{t3.x, t3.y}, df2{fa.z, fa.w});
-    const df2 x = df_lerp(lo, hi, df2{fb.x, fb.y});
-    pow10_times_n(x, df2{fb.z, fb.w}, et.hi, et.lo, r.v, r.wide);
-  }
-  return r;
-}
-
-// 700.0 as the bit pattern of a double: for non-negative x, x > 700 <=> bits(x) > bits(700)
-// (an integer comparison, off the FP64 pipe).
-constexpr long long kBits700 = 0x4085E00000000000LL;
-
-// The same in FP64 with the CUDA math library (validation path).
-__device__ __forceinline__ double level_absorption_fp64(const double* __restrict__ tab, size_t N,
-                                                        const LevelSpecies* __restrict__ d, int S,
-                                                        int k) {
-  double kap = 0.0;
-  for (int s = 0; s < S; ++s) {
-    const int4 r = __ldg(reinterpret_cast<const int4*>(d + s));
-    const double2 w = __ldg(reinterpret_cast<const double2*>(&d[s].wp_lo));
-    const double2 t = __ldg(reinterpret_cast<const double2*>(&d[s].wT));
-    const double v0 = __ldg(tab + (size_t)r.x * N + k);
-    const double v1 = __ldg(tab + (size_t)r.y * N + k);
-    const double v2 = __ldg(tab + (size_t)r.z * N + k);
-    const double v3 = __ldg(tab + (size_t)r.w * N + k);
-    const double lo = v0 + (v1 - v0) * w.x;
-    const double hi = v2 + (v3 - v2) * w.y;
-    const double x = lo + (hi - lo) * t.x;
-    kap += exp10(x) * t.y;
-  }
-  return kap;
-}
-
-// One layer of the two-angle short-characteristics recurrence
-// (ShortCharacteristics::calcSpectrum src/radiative_transfer/short_characteristics.cpp:85-115):
-// delta = tau/mu, a = exp(-delta), I <- I a + (1 + (a-1)/delta) B_top + (-a - (a-1)/delta) B_bottom.
-template <bool TANG>
-__device__ __forceinline__ void sc_layer(double tau, double B, double B_prev, double& I1, double& I2,
-                                         const double* tab) {
-  if (tau == 0) return;  // the reference skips exactly transparent layers only
-  const double rtau = 1.0 / tau;
-#pragma unroll
-  for (int i = 0; i < 2; ++i) {
-    const double d = tau * kInvMu[i];
-    double a;
-    if (TANG) a = d > 700.0 ? 0.0 : exp_tang(-d, tab);
-    else a = exp(-d);
-    const double q = (a - 1.0) * (kMu[i] * rtau);
-    double& I = i == 0 ? I1 : I2;
-    I = I * a;
-    I += (1.0 + q) * B + (-a - q) * B_prev;
-  }
-}
-
-// The same layer in fewer FP64 operations, used by the default kernel:
-// I a + (1+q) B + (-a-q) B' == a (I - B') + B + q (B - B'), with q = (a-1)/delta and
-// 1/tau supplied by the caller (computed in double-float). The exponential and the
-// recurrence stay FP64.
-__device__ __forceinline__ void sc_layer_fast(double tau, double rtau, double B, double B_prev, double& I1,
-                                              double& I2, const double* tab) {
-  if (tau == 0) return;
-  const double dB = B - B_prev;
-#pragma unroll
-  for (int i = 0; i < 2; ++i) {
-    const double d = tau * kInvMu[i];
-    const double a = __double_as_longlong(d) > kBits700 ? 0.0 : exp_tang(-d, tab);
-    const double q = (a - 1.0) * (kMu[i] * rtau);
-    double& I = i == 0 ? I1 : I2;
-    I = fma(a, I - B_prev, B);
-    I = fma(q, dB, I);
-  }
-}
-
 // Fused opacity assembly + short characteristics, one thread per wavenumber.
-// Writes the flux in W m^-2 cm times the radius-distance scaling.
+// Writes the flux in W m^-2 cm times the radius-distance scaling. With STORE the
+// two Gauss-angle intensities after every level are also written to
+// istore[b][l][angle][k] (the adjoint pass reads them back top-down).
+template <bool STORE>
 __global__ void __launch_bounds__(256) emission_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
                                                        const LevelSpecies* __restrict__ ls,
                                                        const LevelSpeciesDF* __restrict__ lsdf,
                                                        const EvalInfo* __restrict__ ev,
-                                                       double* __restrict__ spectrum) {
+                                                       double* __restrict__ spectrum, double* __restrict__ istore) {
   __shared__ ExpTables et;
   load_exp_tables(et);
   __syncthreads();
@@ -210,6 +80,7 @@ __global__ void __launch_bounds__(256) emission_kernel(DeviceModel dm, const Lev
   const LevelInfo* lv = lev + (size_t)b * L;
   const LevelSpecies* sp = ls + (size_t)b * L * S;
   const LevelSpeciesDF* sf = lsdf + (size_t)b * L * S;
+  double* Is = STORE ? istore + (size_t)b * L * 2 * N + k : nullptr;
   const float2 c1f = __ldg(dm.planck_c1_df + k), c2f = __ldg(dm.planck_c2l_df + k);
   const df2 c1 = {c1f.x, c1f.y}, c2l = {c2f.x, c2f.y};
   auto planck = [&](int l) {
@@ -219,22 +90,20 @@ __global__ void __launch_bounds__(256) emission_kernel(DeviceModel dm, const Lev
   Kappa kap_prev = level_kappa_df(dm.table_df, N, sp, sf, S, k, et);
   double B_prev = planck(0);
   double I1 = B_prev, I2 = B_prev;
+  if (STORE) {
+    Is[0] = I1;
+    Is[N] = I2;
+  }
   for (int l = 1; l < L; ++l) {
     const Kappa kap = level_kappa_df(dm.table_df, N, sp + (size_t)l * S, sf + (size_t)l * S, S, k, et);
     const double B = planck(l);
-    // layer optical depth dz (k_l + k_{l-1}) / 2 + cloud, and its reciprocal, in double-float
-    const float4 g = __ldg(reinterpret_cast<const float4*>(&lv[l - 1].dzh_hi));  // dzh, cloud
     double tau, rtau;
-    const df2 t = df_add(df_mul(df2{g.x, g.y}, df_add(kap.v, kap_prev.v)), df2{g.z, g.w});
-    if (kap.wide == 0.0 && kap_prev.wide == 0.0 && t.hi > 1e-30f && t.hi < 1e30f) {
-      tau = df_to_double(t);
-      rtau = df_to_double(df_div(df_make(1.0f), t));
-    } else {  // optical depths outside the comfortable float range: FP64
-      const double ks = (df_to_double(kap.v) + kap.wide) + (df_to_double(kap_prev.v) + kap_prev.wide);
-      tau = __ldg(&lv[l - 1].dz) * ks / 2. + __ldg(&lv[l - 1].cloud);
-      rtau = 1.0 / tau;
-    }
+    emission_layer_tau_df(lv, l, kap, kap_prev, tau, rtau);
     sc_layer_fast(tau, rtau, B, B_prev, I1, I2, et.d);
+    if (STORE) {
+      Is[(size_t)l * 2 * N] = I1;
+      Is[(size_t)l * 2 * N + N] = I2;
+    }
     kap_prev = kap;
     B_prev = B;
   }
@@ -243,10 +112,12 @@ __global__ void __launch_bounds__(256) emission_kernel(DeviceModel dm, const Lev
 }
 
 // Validation path: every step in FP64 with the CUDA math library.
+template <bool STORE>
 __global__ void __launch_bounds__(256) emission_kernel_fp64(DeviceModel dm, const LevelInfo* __restrict__ lev,
                                                             const LevelSpecies* __restrict__ ls,
                                                             const EvalInfo* __restrict__ ev,
-                                                            double* __restrict__ spectrum) {
+                                                            double* __restrict__ spectrum,
+                                                            double* __restrict__ istore) {
   const int b = blockIdx.x;
   const int k = blockIdx.y * blockDim.x + threadIdx.x;
   if (k >= dm.N) return;
@@ -254,15 +125,24 @@ __global__ void __launch_bounds__(256) emission_kernel_fp64(DeviceModel dm, cons
   const size_t N = dm.N;
   const LevelInfo* lv = lev + (size_t)b * L;
   const LevelSpecies* sp = ls + (size_t)b * L * S;
+  double* Is = STORE ? istore + (size_t)b * L * 2 * N + k : nullptr;
   const double c1 = dm.planck_c1[k], c2 = dm.planck_c2[k];
   double kap_prev = level_absorption_fp64(dm.table64, N, sp, S, k);
   double B_prev = c1 / (exp(c2 * __ldg(&lv[0].invT)) - 1.0);
   double I1 = B_prev, I2 = B_prev;
+  if (STORE) {
+    Is[0] = I1;
+    Is[N] = I2;
+  }
   for (int l = 1; l < L; ++l) {
     const double kap = level_absorption_fp64(dm.table64, N, sp + (size_t)l * S, S, k);
     const double B = c1 / (exp(c2 * __ldg(&lv[l].invT)) - 1.0);
     const double tau = __ldg(&lv[l - 1].dz) * (kap + kap_prev) / 2. + __ldg(&lv[l - 1].cloud);
     sc_layer<false>(tau, B, B_prev, I1, I2, nullptr);
+    if (STORE) {
+      Is[(size_t)l * 2 * N] = I1;
+      Is[(size_t)l * 2 * N + N] = I2;
+    }
     kap_prev = kap;
     B_prev = B;
   }
@@ -304,8 +184,6 @@ __global__ void transmission_geometry_kernel(DeviceModel dm, const LevelInfo* __
 // levels. Tangent sums are FP64 with the reference's tau > 10 cut-off; the
 // effective height is summed per level, sum_t (R + z_t)(1 - T_t)(dz_{t-1} + dz_t),
 // which regroups the reference's trapezoid sum.
-constexpr long long kBits10 = 0x4024000000000000LL;  // 10.0 as a double's bit pattern
-
 template <bool DF, int TPN>
 __global__ void __launch_bounds__(128) transmission_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
                                                            const LevelSpecies* __restrict__ ls,
@@ -537,6 +415,28 @@ void upload_model(Model& m) {
   dm.row_weight = dev_upload(m, wgt);
   dm.row_logterm = dev_upload(m, logt);
   dm.obs_mod_param = dev_upload(m, modp);
+  {
+    // first row of each observation, and the operator transposed (rows reading
+    // each wavenumber, in ascending row order) for the adjoint
+    std::vector<int> start(m.obs.size() + 1, 0);
+    for (size_t o = 0; o < m.obs.size(); ++o) start[o + 1] = start[o] + m.obs[o].n;
+    dm.obs_row_start = dev_upload(m, start);
+    std::vector<int> cptr(N + 1, 0);
+    for (size_t r = 0; r < k0.size(); ++r)
+      for (int j = 0; j < len[r]; ++j) ++cptr[(size_t)k0[r] + j + 1];
+    for (size_t k = 0; k < N; ++k) cptr[k + 1] += cptr[k];
+    std::vector<int> crow((size_t)cptr[N]), fill(cptr.begin(), cptr.end() - 1);
+    std::vector<double> cw((size_t)cptr[N]);
+    for (size_t r = 0; r < k0.size(); ++r)
+      for (int j = 0; j < len[r]; ++j) {
+        const int at = fill[(size_t)k0[r] + j]++;
+        crow[at] = (int)r;
+        cw[at] = m.W[(size_t)off[r] + j];
+      }
+    dm.col_ptr = dev_upload(m, cptr);
+    dm.col_row = dev_upload(m, crow);
+    dm.col_w = dev_upload(m, cw);
+  }
   std::vector<AtmosphereConfig> cfg{m.acfg};
   m.d_cfg = dev_upload(m, cfg);
   dm.cfg = m.d_cfg;
@@ -563,9 +463,6 @@ static void free_workspace(Workspace& w) {
   cudaFree(w.obs);
   cudaFree(w.loglike);
   cudaFree(w.geom);
-  cudaFree(w.g_spectrum);
-  cudaFree(w.g_level);
-  cudaFree(w.g_geom);
   w = Workspace{};
 }
 
@@ -592,24 +489,33 @@ void ensure_workspace(Model& m, int batch) {
 }
 
 // Kernel sequence of one batch on the given work buffers.
+// taps (optional, gradient pass): receives d wT / dT of every stencil and the
+// intensities after every level.
 static void launch_stages(Model& m, const double* params_dev, int batch, const Workspace& w, cudaStream_t st,
-                          bool profile, uint8_t* neglect_dev, double* loglike_dev) {
+                          bool profile, uint8_t* neglect_dev, double* loglike_dev,
+                          const ForwardTaps* taps = nullptr) {
   const DeviceModel& dm = m.dm;
   const int L = m.L;
   const int atm_threads = ((L + 31) / 32) * 32;
   if (profile) BGB_CUDA(cudaEventRecord(m.ev[0], st));
   atmosphere_kernel<<<batch, atm_threads, 4 * L * sizeof(double), st>>>(dm, params_dev, dm.P, w.lev, w.ls,
-                                                                        w.lsdf, w.ray_n, w.ev);
+                                                                        w.lsdf, w.ray_n, w.ev,
+                                                                        taps ? taps->dwT : nullptr);
   BGB_CUDA(cudaGetLastError());
   if (profile) BGB_CUDA(cudaEventRecord(m.ev[1], st));
   if (!m.transmission) {
     const int TB = m.rt_threads > 0 ? m.rt_threads : (batch == 1 ? 64 : 128);
     dim3 grid(batch, (dm.N + TB - 1) / TB);
-    if (m.precision == 1)
-      emission_kernel_fp64<<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.ev, w.spectrum);
+    if (taps && m.precision == 1)
+      emission_kernel_fp64<true><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.ev, w.spectrum, taps->istore);
+    else if (taps)
+      emission_kernel<true><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.lsdf, w.ev, w.spectrum, taps->istore);
+    else if (m.precision == 1)
+      emission_kernel_fp64<false><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.ev, w.spectrum, nullptr);
     else
-      emission_kernel<<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.lsdf, w.ev, w.spectrum);
+      emission_kernel<false><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.lsdf, w.ev, w.spectrum, nullptr);
   } else {
+    if (taps) throw Error(BEAR_ERR_UNSUPPORTED, "gradient of transmission models not available");
     transmission_geometry_kernel<<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom);
     // rt_threads selects the wavenumbers per block: 32 (4 threads each, default) or 16 (8 each)
     const int vpb = (m.rt_threads == 16) ? 16 : 32;
@@ -656,6 +562,13 @@ void launch_forward_into(Model& m, const double* params_dev, const Workspace& w,
   launch_stages(m, params_dev, 1, w, st, false, neglect_dev, loglike_dev);
 }
 
+// Forward pass of the gradient: the plain kernel sequence on the model's
+// workspace with the adjoint's taps.
+void launch_forward_taps(Model& m, const double* params_dev, int batch, cudaStream_t st, uint8_t* neglect_dev,
+                         double* loglike_dev, const ForwardTaps& taps) {
+  launch_stages(m, params_dev, batch, m.ws, st, false, neglect_dev, loglike_dev, &taps);
+}
+
 void stage_times(Model& m, float* ms3) {
   if (!m.ev_recorded) throw Error(BEAR_ERR_STATE, "no profiled evaluation recorded");
   BGB_CUDA(cudaEventSynchronize(m.ev[3]));
@@ -688,6 +601,7 @@ void release_model(Model& m) {
   cudaSetDevice(m.device);
   cudaDeviceSynchronize();
   free_workspace(m.ws);
+  free_grad_workspace(m);
   for (void* p : m.allocations) cudaFree(p);
   m.allocations.clear();
   for (auto& e : m.ev)

@@ -152,6 +152,11 @@ struct DeviceModel {
   const double* row_weight;
   const double* row_logterm;  // -0.5 log(2 pi sigma^2) (no inflation)
   const int* obs_mod_param;   // per observation: parameter index of the shift, or -1
+  const int* obs_row_start;   // nobs + 1: first operator row of each observation
+  // transposed observation operator (adjoint): per wavenumber the rows that read it
+  const int* col_ptr;         // N + 1
+  const int* col_row;         // nnz
+  const double* col_w;        // nnz
 };
 
 // Work buffers for a batch of evaluations.
@@ -167,10 +172,22 @@ struct Workspace {
   double* obs = nullptr;       // B x M internal order
   double* loglike = nullptr;   // B
   double* geom = nullptr;      // transmission path lengths B x L x L
-  // adjoint
-  double* g_spectrum = nullptr;  // B x N adjoint of the spectrum
-  double* g_level = nullptr;     // B x L x (S + 4) accumulated adjoints
-  double* g_geom = nullptr;      // B x L x L
+};
+
+// Extra outputs of the forward pass that the adjoint reads back.
+struct ForwardTaps {
+  float2* dwT = nullptr;     // B x L x S: d wT / dT of every stencil (double-float)
+  double* istore = nullptr;  // B x L x 2 x N: Gauss-angle intensities after every level
+};
+
+// Work buffers of the gradient for a chunk of evaluations.
+struct GradWorkspace {
+  int capacity = 0;
+  int tiles = 0;             // wavenumber tiles of the adjoint kernel (partials per level value)
+  ForwardTaps taps;
+  double* gS = nullptr;      // B x M: d log L / d binned model
+  double* seed = nullptr;    // B x 3: seed normaliser, its inverse, sum_r gS_r (s_r - shift_r)
+  double* partial = nullptr; // B x L x V x tiles per-block sinks of the adjoint kernel
 };
 
 // ----------------------------------------------------------------- host model
@@ -264,6 +281,8 @@ struct Model {
   AtmosphereConfig* d_cfg = nullptr;
   double* d_table64 = nullptr;
   Workspace ws;
+  GradWorkspace gws;
+  size_t grad_budget = size_t(16) << 30;  // bytes of gradient work buffers per chunk
   double* h_pinned = nullptr;  // pinned staging for the plain path
   size_t h_pinned_bytes = 0;
   // stage timing (bear_model_set_profiling)
@@ -292,8 +311,12 @@ void stage_times(Model& m, float* ms3);
 void loglike_noalloc(Model& m, const double* params_dev, double* loglike_dev, uint8_t* neglect_dev,
                      cudaStream_t stream);
 long long stencil_rows(Model& m, int batch);
+void launch_forward_taps(Model& m, const double* params_dev, int batch, cudaStream_t stream,
+                         uint8_t* neglect_dev, double* loglike_dev, const ForwardTaps& taps);
+// adjoint.cu
 void launch_gradient(Model& m, const double* params_dev, int batch, cudaStream_t stream,
                      double* loglike_dev, double* grad_dev, uint8_t* neglect_dev);
+void free_grad_workspace(Model& m);
 
 struct Error : std::exception {
   int code;

@@ -28,6 +28,26 @@ BGB_HD double planck_df(df2 c1, df2 c2l, df2 invT, const float* tab_hi, const fl
   return df_to_double(df_div(df_mul(c1, u), d));
 }
 
+// The same Planck function returned as a double-float (values below the float
+// range flush to zero); used by the adjoint, whose arithmetic is double-float.
+BGB_HD df2 planck_df2(df2 c1, df2 c2l, df2 invT, const float* tab_hi, const float* tab_lo) {
+  const df2 y = df_neg(df_mul(c2l, invT));
+  int n;
+  const df2 m = df_exp2(y, n, tab_hi, tab_lo);
+  if (n < -60) return df_ldexp(df_mul(c1, m), n);
+  const df2 u = df_ldexp(m, n);
+  const df2 d = df_sub(df_make(1.0f), u);
+  return df_div(df_mul(c1, u), d);
+}
+
+// exp(-d) for a double-float d >= 0 (0 for d > 700 and below the float range).
+BGB_HD df2 df_exp_neg(df2 d, const float* tab_hi, const float* tab_lo) {
+  if (d.hi > 700.0f) return df2{0.0f, 0.0f};
+  int n;
+  const df2 m = df_exp2(df_neg(df_mul(d, df2{kLog2eHi, kLog2eLo})), n, tab_hi, tab_lo);
+  return df_ldexp(m, n);
+}
+
 // 10^x * n as a double for a double-float log10 cross section x and log2(n):
 // 2^(x log2(10) + log2(n)).
 BGB_HD double pow10_times_n(df2 x, df2 lg2n, const float* tab_hi, const float* tab_lo, df2& acc, double& wide) {

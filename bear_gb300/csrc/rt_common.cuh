@@ -1,0 +1,193 @@
+// Per-wavenumber device helpers shared by the forward kernels (engine.cu) and
+// the adjoint kernels (adjoint.cu): level opacity assembly, the layer optical
+// depth of the emission recurrence and the short-characteristics layer update.
+// The adjoint recomputes level opacities with exactly these functions, so the
+// optical depths it differentiates are bit-identical to the forward pass.
+#pragma once
+
+#include "model.h"
+#include "physics.cuh"
+
+namespace bgb {
+
+// Gauss nodes of ShortCharacteristics (src/radiative_transfer/short_characteristics.h:62-63)
+static __device__ __constant__ double kMu[2] = {0.211324865405187, 0.788675134594813};
+static __device__ __constant__ double kInvMu[2] = {1.0 / 0.211324865405187, 1.0 / 0.788675134594813};
+
+// 700.0 and 10.0 as bit patterns of doubles: for non-negative x, x > 700 <=>
+// bits(x) > bits(700) (an integer comparison, off the FP64 pipe).
+constexpr long long kBits700 = 0x4085E00000000000LL;
+constexpr long long kBits10 = 0x4024000000000000LL;
+
+__device__ __forceinline__ void load_exp_tables(ExpTables& t) {
+  for (int i = threadIdx.x; i < 65; i += blockDim.x) {
+    t.hi[i] = kExp2TabHi[i];
+    t.lo[i] = kExp2TabLo[i];
+  }
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) t.d[i] = kExp2TabD[i];
+}
+
+// Level opacity as a double-float plus an FP64 part for terms outside the float
+// exponent range (zero almost always).
+struct Kappa {
+  df2 v;
+  double wide;
+};
+
+// Sum over table species of 10^(bilinear log-p / T interpolation) * n at one
+// level and one wavenumber (OpacitySpecies::calcAbsorptionCrossSections
+// src/transport_coeff/opacity_species.cpp:277-345 and calcTransportCoefficients
+// :400-455), double-float arithmetic. term(s, t, t_wide, is_wide, lo, hi) is
+// called for every species with its term 10^x n (t as a double-float, or t_wide
+// in FP64 when outside the float range; zero for a skipped species) and the
+// p-interpolated log10 cross sections at the lower and upper temperature nodes.
+template <class F>
+__device__ __forceinline__ Kappa level_kappa_df_cb(const float2* __restrict__ tab, size_t N,
+                                                   const LevelSpecies* __restrict__ d,
+                                                   const LevelSpeciesDF* __restrict__ f, int S, int k,
+                                                   const ExpTables& et, F&& term) {
+  Kappa r = {{0.0f, 0.0f}, 0.0};
+  for (int s = 0; s < S; ++s) {
+    const float4 fa = __ldg(reinterpret_cast<const float4*>(f + s));
+    const float4 fb = __ldg(reinterpret_cast<const float4*>(f + s) + 1);
+    if (fb.z == kNoSpecies) {  // zero number density: the species adds nothing
+      term(s, df2{0.0f, 0.0f}, 0.0, false, df2{0.0f, 0.0f}, df2{0.0f, 0.0f});
+      continue;
+    }
+    const int4 rw = __ldg(reinterpret_cast<const int4*>(d + s));
+    const float2 t0 = __ldg(tab + (size_t)rw.x * N + k);
+    const float2 t1 = __ldg(tab + (size_t)rw.y * N + k);
+    const float2 t2 = __ldg(tab + (size_t)rw.z * N + k);
+    const float2 t3 = __ldg(tab + (size_t)rw.w * N + k);
+    const df2 lo = df_lerp(df2{t0.x, t0.y}, df2{t1.x, t1.y}, df2{fa.x, fa.y});
+    const df2 hi = df_lerp(df2{t2.x, t2.y}, df2{t3.x, t3.y}, df2{fa.z, fa.w});
+    const df2 x = df_lerp(lo, hi, df2{fb.x, fb.y});
+    // 10^x n = 2^(x log2(10) + log2(n))
+    const df2 y = df_add(df_mul(x, df2{kLog2_10Hi, kLog2_10Lo}), df2{fb.z, fb.w});
+    int n;
+    const df2 m = df_exp2(y, n, et.hi, et.lo);
+    if (n > -100 && n < 100) {
+      const df2 t = df_ldexp(m, n);
+      r.v = df_add(r.v, t);
+      term(s, t, 0.0, false, lo, hi);
+    } else {
+      const double w = df_to_double(m) * pow2d(n);
+      r.wide += w;
+      term(s, df2{0.0f, 0.0f}, w, true, lo, hi);
+    }
+  }
+  return r;
+}
+
+struct NoTerm {
+  __device__ __forceinline__ void operator()(int, df2, double, bool, df2, df2) const {}
+};
+
+__device__ __forceinline__ Kappa level_kappa_df(const float2* __restrict__ tab, size_t N,
+                                                const LevelSpecies* __restrict__ d,
+                                                const LevelSpeciesDF* __restrict__ f, int S, int k,
+                                                const ExpTables& et) {
+  return level_kappa_df_cb(tab, N, d, f, S, k, et, NoTerm{});
+}
+
+__device__ __forceinline__ double level_absorption_df(const float2* __restrict__ tab, size_t N,
+                                                      const LevelSpecies* __restrict__ d,
+                                                      const LevelSpeciesDF* __restrict__ f, int S, int k,
+                                                      const ExpTables& et) {
+  const Kappa r = level_kappa_df(tab, N, d, f, S, k, et);
+  return df_to_double(r.v) + r.wide;
+}
+
+// The same sum in FP64 with the CUDA math library (validation path);
+// term(s, t, lo, hi) receives each species' term 10^x n.
+template <class F>
+__device__ __forceinline__ double level_absorption_fp64_cb(const double* __restrict__ tab, size_t N,
+                                                           const LevelSpecies* __restrict__ d, int S, int k,
+                                                           F&& term) {
+  double kap = 0.0;
+  for (int s = 0; s < S; ++s) {
+    const int4 r = __ldg(reinterpret_cast<const int4*>(d + s));
+    const double2 w = __ldg(reinterpret_cast<const double2*>(&d[s].wp_lo));
+    const double2 t = __ldg(reinterpret_cast<const double2*>(&d[s].wT));
+    const double v0 = __ldg(tab + (size_t)r.x * N + k);
+    const double v1 = __ldg(tab + (size_t)r.y * N + k);
+    const double v2 = __ldg(tab + (size_t)r.z * N + k);
+    const double v3 = __ldg(tab + (size_t)r.w * N + k);
+    const double lo = v0 + (v1 - v0) * w.x;
+    const double hi = v2 + (v3 - v2) * w.y;
+    const double x = lo + (hi - lo) * t.x;
+    const double term_s = exp10(x) * t.y;
+    kap += term_s;
+    term(s, term_s, lo, hi);
+  }
+  return kap;
+}
+
+struct NoTerm64 {
+  __device__ __forceinline__ void operator()(int, double, double, double) const {}
+};
+
+__device__ __forceinline__ double level_absorption_fp64(const double* __restrict__ tab, size_t N,
+                                                        const LevelSpecies* __restrict__ d, int S, int k) {
+  return level_absorption_fp64_cb(tab, N, d, S, k, NoTerm64{});
+}
+
+// Optical depth of emission layer l (between levels l-1 and l),
+// dz (k_l + k_{l-1}) / 2 + cloud, and its reciprocal, in double-float; FP64 when
+// an opacity has a term outside the float range or the depth is outside the
+// comfortable float range.
+__device__ __forceinline__ void emission_layer_tau_df(const LevelInfo* __restrict__ lv, int l, const Kappa& kap,
+                                                      const Kappa& kap_prev, double& tau, double& rtau) {
+  const float4 g = __ldg(reinterpret_cast<const float4*>(&lv[l - 1].dzh_hi));  // dzh, cloud
+  const df2 t = df_add(df_mul(df2{g.x, g.y}, df_add(kap.v, kap_prev.v)), df2{g.z, g.w});
+  if (kap.wide == 0.0 && kap_prev.wide == 0.0 && t.hi > 1e-30f && t.hi < 1e30f) {
+    tau = df_to_double(t);
+    rtau = df_to_double(df_div(df_make(1.0f), t));
+  } else {
+    const double ks = (df_to_double(kap.v) + kap.wide) + (df_to_double(kap_prev.v) + kap_prev.wide);
+    tau = __ldg(&lv[l - 1].dz) * ks / 2. + __ldg(&lv[l - 1].cloud);
+    rtau = 1.0 / tau;
+  }
+}
+
+// One layer of the two-angle short-characteristics recurrence
+// (ShortCharacteristics::calcSpectrum src/radiative_transfer/short_characteristics.cpp:85-115):
+// delta = tau/mu, a = exp(-delta), I <- I a + (1 + (a-1)/delta) B_top + (-a - (a-1)/delta) B_bottom.
+template <bool TANG>
+__device__ __forceinline__ void sc_layer(double tau, double B, double B_prev, double& I1, double& I2,
+                                         const double* tab) {
+  if (tau == 0) return;  // the reference skips exactly transparent layers only
+  const double rtau = 1.0 / tau;
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const double d = tau * kInvMu[i];
+    double a;
+    if (TANG) a = d > 700.0 ? 0.0 : exp_tang(-d, tab);
+    else a = exp(-d);
+    const double q = (a - 1.0) * (kMu[i] * rtau);
+    double& I = i == 0 ? I1 : I2;
+    I = I * a;
+    I += (1.0 + q) * B + (-a - q) * B_prev;
+  }
+}
+
+// The same layer in fewer FP64 operations, used by the default kernel:
+// I a + (1+q) B + (-a-q) B' == a (I - B') + B + q (B - B'), with q = (a-1)/delta and
+// 1/tau supplied by the caller (computed in double-float). The exponential and the
+// recurrence stay FP64.
+__device__ __forceinline__ void sc_layer_fast(double tau, double rtau, double B, double B_prev, double& I1,
+                                              double& I2, const double* tab) {
+  if (tau == 0) return;
+  const double dB = B - B_prev;
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const double d = tau * kInvMu[i];
+    const double a = __double_as_longlong(d) > kBits700 ? 0.0 : exp_tang(-d, tab);
+    const double q = (a - 1.0) * (kMu[i] * rtau);
+    double& I = i == 0 ? I1 : I2;
+    I = fma(a, I - B_prev, B);
+    I = fma(q, dB, I);
+  }
+}
+
+}  // namespace bgb

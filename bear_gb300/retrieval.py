@@ -155,8 +155,11 @@ class Engine:
         return ll, ng
 
     def grad_batch(self, params):
+        """params: torch float64 CUDA tensor (B, P). Returns (loglike (B,), d loglike / d params
+        (B, P), neglect (B,) uint8) from the adjoint kernels."""
         import torch
-        t = params.contiguous()
+        t = params.detach().contiguous()
+        assert t.dtype == torch.float64 and t.is_cuda and t.shape[1] == self.P
         B = t.shape[0]
         ll = torch.empty(B, dtype=torch.float64, device=t.device)
         g = torch.empty(B, self.P, dtype=torch.float64, device=t.device)
@@ -165,8 +168,13 @@ class Engine:
                             torch.cuda.current_stream(t.device).cuda_stream)
         return ll, g, ng
 
-    def set_precision(self, fp32_tables: bool) -> None:
-        _lib.check(self._lib.bear_model_set_precision(self._h, int(bool(fp32_tables))))
+    def set_precision(self, mode: int) -> None:
+        """0: double-float opacity assembly (default); 1: every step in FP64."""
+        _lib.check(self._lib.bear_model_set_precision(self._h, int(mode)))
+
+    def set_gradient_memory(self, nbytes: int = 0) -> None:
+        """Device memory the gradient's work buffers may use per chunk (0 = default)."""
+        _lib.check(self._lib.bear_model_set_gradient_memory(self._h, int(nbytes)))
 
     def set_launch(self, rt_threads: int = 0, obs_threads: int = 0) -> None:
         _lib.check(self._lib.bear_model_set_launch(self._h, int(rt_threads), int(obs_threads)))

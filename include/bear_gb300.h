@@ -140,11 +140,22 @@ int bear_loglike(bear_model* m, const double* params, int nb_params, double* log
 int bear_loglike_batch(bear_model* m, const double* params_dev, int batch, int nb_params,
                        double* loglike_dev, uint8_t* neglect_dev, void* stream);
 
-/* Gradient of the log-likelihood with respect to the physical parameters by
- * the engine's adjoint kernels: grad_dev batch x nb_params (device). */
+/* Gradient of the log-likelihood with respect to the physical parameters (the
+ * reference's parameter vector: ratios for the temperature knots, linear mixing
+ * ratios) by the engine's adjoint kernels, with the log-likelihood itself.
+ * No reference counterpart (the reference has no derivatives). grad_dev:
+ * device, batch x nb_params; loglike_dev: device, batch; neglect_dev: device,
+ * batch bytes (NULL allowed). Neglected models get -1e30 and a zero gradient.
+ * Discrete choices of the model (table brackets, cloud layer indices) are held
+ * fixed, so d/d cloud-top pressure is 0. Emission models only. Stream-ordered.
+ * Evaluations run in chunks whose work buffers fit the gradient memory budget. */
 int bear_loglike_grad_batch(bear_model* m, const double* params_dev, int batch, int nb_params,
                             double* loglike_dev, double* grad_dev, uint8_t* neglect_dev,
                             void* stream);
+
+/* Device memory the gradient's work buffers may use per chunk of evaluations
+ * (0 = default, 16 GiB). No reference counterpart. */
+int bear_model_set_gradient_memory(bear_model* m, long long bytes);
 
 /* Arithmetic of the opacity assembly (applies to every evaluation path):
  * 0 (default) = double-float (hi + lo float pairs, ~48 bits) on the FP32 pipe
