@@ -303,8 +303,10 @@ __device__ __forceinline__ void sc_layer_adjoint_df(df2 t, df2 rt, df2 B, df2 Bp
 // float2 [2][S][kAdjThreads] then double [2][S][kAdjThreads].
 // partial[b][l][v][tile]: v = 0..S-1 d log L / d ln n_s, S temperature, S+1 lev.dz,
 // S+2 lev.cloud (all times the evaluation's seed normaliser).
+// Six blocks per SM in the double-float path (80 registers): the sweep is bound by
+// the latency of the table reads, so occupancy beats the few spilled registers.
 template <bool DF, int VP>
-__global__ void __launch_bounds__(kAdjThreads) emission_adjoint_kernel(DeviceModel dm, AdjointArgs a) {
+__global__ void __launch_bounds__(kAdjThreads, DF ? 6 : 4) emission_adjoint_kernel(DeviceModel dm, AdjointArgs a) {
   typedef AccType<DF> AT;
   typedef typename AT::type A;
   constexpr int NW = kAdjThreads / 32;
@@ -616,83 +618,110 @@ __global__ void __launch_bounds__(kAdjThreads) atmosphere_adjoint_kernel(
     if (lane == 0) sg[idx] = s * inv;
   }
   __syncthreads();
-  if (tid >= P) return;
-  const int th = tid;
-  const double* par = params + (size_t)b * P;
-  const double* gen = par;
-  const int ng = c.nparam_general, nc = c.nparam_chem, nt = c.nparam_temp;
-  const double* chem = par + ng;
-  const double* temp = chem + nc;
-  const double* cloud = temp + nt;
+  // thread (th, ch): parameter th, levels of chunk ch; chunk sums added in chunk order
+  __shared__ double part[kAdjThreads];
+  const int nch = max(1, (int)blockDim.x / P);
+  const int th = tid % P, ch = tid / P;
+  double acc = 0.0;
+  if (ch < nch) {
+    const double* par = params + (size_t)b * P;
+    const double* gen = par;
+    const int ng = c.nparam_general, nc = c.nparam_chem, nt = c.nparam_temp;
+    const double* chem = par + ng;
+    const double* temp = chem + nc;
+    const double* cloud = temp + nt;
 
-  double X[kSpeciesCount], dX[kSpeciesCount], mmw, dmmw;
-  chemistry_tangent(c, chem, (th >= ng && th < ng + nc) ? th - ng : -1, X, dX, mmw, dmmw);
-
-  // temperature: T = poly(dof, log10 p), dof_i = temp_0 temp_1 ... temp_i (a constant profile: T = temp_0)
-  const int tm = th - ng - nc;
-  const bool temp_theta = tm >= 0 && tm < nt;
-  double ddof[kMaxPolyDof];
-  if (temp_theta && c.temp_poly) {
-    for (int i = 0; i < c.pp_ndof; ++i) {
-      double v = 0.0;
-      if (i >= tm) {
-        v = 1.0;
-        for (int j = 0; j <= i; ++j)
-          if (j != tm) v *= temp[j];
-      }
-      ddof[i] = v;
-    }
-  }
-  const double g = pow(10.0, gen[0]);
-  const double dlng = th == 0 ? kLn10 : 0.0;  // d ln g / d log g
-  const int ci = ng + nc + nt;                 // cloud optical depth parameter
-  const EvalInfo e = ev[b];
-  double cloud_d = 0.0;
-  if (c.cloud && th == ci && cloud[0] >= 0)
-    cloud_d = 1.0 / (double)((unsigned)e.cloud_top - (unsigned)e.cloud_bottom);
-
-  double acc = 0.0, u_prev = 0.0, du_prev = 0.0;
-  for (int l = 0; l < L; ++l) {
-    const double T = lev[(size_t)b * L + l].T;
-    double dT = 0.0;
-    if (temp_theta) dT = c.temp_poly ? poly_value(c, ddof, dm.log10p[l]) : (tm == 0 ? 1.0 : 0.0);
-    const double dlnT = dT / T;
-    const double* sgl = sg + (size_t)l * V;
-    // n_s = prod over the species and its collision partners of n_total X_j, n_total = p / (k T)
+    double X[kSpeciesCount], dX[kSpeciesCount], mmw, dmmw;
+    chemistry_tangent(c, chem, (th >= ng && th < ng + nc) ? th - ng : -1, X, dX, mmw, dmmw);
+    // per opacity species: n_s = prod over the species and its collision partners of
+    // n_total X_j, n_total = p / (k T): d ln n_s = sum_j dX_j / X_j - np_s dT / T
+    double dlnX[kMaxTableSpecies];
+    int np[kMaxTableSpecies];
     for (int s = 0; s < S; ++s) {
-      const double gl = sgl[s];
-      if (gl == 0.0) continue;
-      double dln = 0.0;
-      bool zero = false;
       const int js[3] = {c.sp_index[s], c.sp_partner[s][0], c.sp_partner[s][1]};
+      double v = 0.0;
+      int n = 0;
+      bool zero = false;
       for (int u = 0; u < 3; ++u) {
         if (js[u] < 0) continue;
+        ++n;
         if (X[js[u]] == 0.0) zero = true;
-        else dln += dX[js[u]] / X[js[u]] - dlnT;
+        else v += dX[js[u]] / X[js[u]];
       }
-      if (!zero) acc = fma(gl, dln, acc);
+      dlnX[s] = v;
+      np[s] = zero ? -1 : n;  // -1: zero density, the species contributes nothing
     }
-    acc = fma(sgl[S], dT, acc);
-    // layer thickness Delta_l = 0.5 (p_{l-1} - p_l) 1e6 (u_l + u_{l-1}) / g, u = R T / (mmw p 1e6)
-    const double p = dm.pressure[l];
-    const double u = kGasConst * T / (mmw * p * 1e6);
-    const double du = u * (dlnT - dmmw / mmw);
-    if (l >= 1) {
-      const double pf = 0.5 * (dm.pressure[l - 1] * 1e6 - p * 1e6) / g;
-      acc = fma(sg[(size_t)(l - 1) * V + S + 1], pf * ((du + du_prev) - (u + u_prev) * dlng), acc);
+    // temperature: T = poly(dof, log10 p), dof_i = temp_0 temp_1 ... temp_i (a constant profile: T = temp_0)
+    const int tm = th - ng - nc;
+    const bool temp_theta = tm >= 0 && tm < nt;
+    double ddof[kMaxPolyDof];
+    if (temp_theta && c.temp_poly) {
+      for (int i = 0; i < c.pp_ndof; ++i) {
+        double v = 0.0;
+        if (i >= tm) {
+          v = 1.0;
+          for (int j = 0; j <= i; ++j)
+            if (j != tm) v *= temp[j];
+        }
+        ddof[i] = v;
+      }
     }
-    u_prev = u;
-    du_prev = du;
-    // grey cloud: tau_c / (top - bottom) on layers bottom < l <= top, l < L - 1
-    if (cloud_d != 0.0 && (unsigned)l <= (unsigned)e.cloud_top && (unsigned)l > (unsigned)e.cloud_bottom &&
-        l < L - 1)
-      acc = fma(sgl[S + 2], cloud_d, acc);
+    auto dT_at = [&](int l) -> double {
+      if (!temp_theta) return 0.0;
+      return c.temp_poly ? poly_value(c, ddof, dm.log10p[l]) : (tm == 0 ? 1.0 : 0.0);
+    };
+    const double g = pow(10.0, gen[0]);
+    const double dlng = th == 0 ? kLn10 : 0.0;  // d ln g / d log g
+    const int ci = ng + nc + nt;                 // cloud optical depth parameter
+    const EvalInfo e = ev[b];
+    double cloud_d = 0.0;
+    if (c.cloud && th == ci && cloud[0] >= 0)
+      cloud_d = 1.0 / (double)((unsigned)e.cloud_top - (unsigned)e.cloud_bottom);
+    // u = R T / (mmw p 1e6) = 1 / rho and its tangent
+    auto u_at = [&](int l, double& du) {
+      const double T = lev[(size_t)b * L + l].T;
+      const double u = kGasConst * T / (mmw * dm.pressure[l] * 1e6);
+      du = u * (dT_at(l) / T - dmmw / mmw);
+      return u;
+    };
+    const int l0 = ch * L / nch, l1 = (ch + 1) * L / nch;
+    double du_prev = 0.0, u_prev = l0 >= 1 ? u_at(l0 - 1, du_prev) : 0.0;
+    for (int l = l0; l < l1; ++l) {
+      const double T = lev[(size_t)b * L + l].T;
+      const double dT = dT_at(l);
+      const double dlnT = dT / T;
+      const double* sgl = sg + (size_t)l * V;
+      for (int s = 0; s < S; ++s)
+        if (np[s] >= 0) acc = fma(sgl[s], dlnX[s] - np[s] * dlnT, acc);
+      acc = fma(sgl[S], dT, acc);
+      // layer thickness Delta_l = 0.5 (p_{l-1} - p_l) 1e6 (u_l + u_{l-1}) / g (lev[l-1].dz)
+      const double u = kGasConst * T / (mmw * dm.pressure[l] * 1e6);
+      const double du = u * (dlnT - dmmw / mmw);
+      if (l >= 1) {
+        const double pf = 0.5 * (dm.pressure[l - 1] * 1e6 - dm.pressure[l] * 1e6) / g;
+        acc = fma(sg[(size_t)(l - 1) * V + S + 1], pf * ((du + du_prev) - (u + u_prev) * dlng), acc);
+      }
+      u_prev = u;
+      du_prev = du;
+      // grey cloud: tau_c / (top - bottom) on layers bottom < l <= top, l < L - 1
+      if (cloud_d != 0.0 && (unsigned)l <= (unsigned)e.cloud_top && (unsigned)l > (unsigned)e.cloud_bottom &&
+          l < L - 1)
+        acc = fma(sgl[S + 2], cloud_d, acc);
+    }
+    // radius-distance scaling (R_J / d)^2 f, once (chunk 0)
+    if (ch == 0) {
+      const double gsc = seed[b * 3 + 2] / e.scaling;
+      if (th == 1) acc += gsc * (kRJupiter / gen[2]) * (kRJupiter / gen[2]);
+      if (th == 2) acc += gsc * (-2.0 * e.scaling / gen[2]);
+    }
   }
-  // radius-distance scaling (R_J / d)^2 f
-  const double gsc = seed[b * 3 + 2] / e.scaling;
-  if (th == 1) acc += gsc * (kRJupiter / gen[2]) * (kRJupiter / gen[2]);
-  if (th == 2) acc += gsc * (-2.0 * e.scaling / gen[2]);
-  grad[(size_t)b * P + th] += acc;
+  part[tid] = acc;
+  __syncthreads();
+  if (tid < P) {
+    double tot = 0.0;
+    for (int q = 0; q < nch; ++q) tot += part[q * P + tid];
+    grad[(size_t)b * P + tid] += tot;
+  }
 }
 
 // ------------------------------------------------------------------ host side

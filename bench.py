@@ -7,14 +7,16 @@ species + 2 CIA tables on 10 log-p x 20 T, 2000-12000 cm^-1 at 1 cm^-1
 top-hat / Gaussian bandpass filters). Synthetic seeded tables in the
 reference's on-disk format.
 
-One step = one batch of B likelihood evaluations. ``value`` = evaluations per
+One step = one batch of B likelihood evaluations. For emission workloads the
+adjoint gradient of the same batch is timed as well (``gradient``: evals/s and
+the ratio of its time to the forward batch). ``value`` = evaluations per
 second over the timed steps with parameters resident in HBM; ``e2e`` = the same
 through the host API with the parameter upload and the log-likelihood download
 inside the timed region. L2 is flushed between timed steps (a 512 MiB write)
 outside the per-step event pair.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-                    [--workload emission_batched|emission_plain|transmission_plain]
+                    [--workload emission_batched|emission_adjoint|emission_plain|transmission_plain]
 """
 
 from __future__ import annotations
@@ -183,18 +185,23 @@ def fp64_peak_tflops(torch, device):
     return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
-def cpu_baseline(text, arrays, params, sample, threads):
+def cpu_baseline(text, arrays, params, sample, threads, budget_s=12.0):
+    """The FP64 C restatement of the reference path (a port) on the host cores:
+    sequential evaluations of the batch's live points until ``budget_s`` seconds
+    have passed (or ``sample`` evaluations, when given)."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
-    import oracle  # the FP64 CPU restatement of the reference path (a port)
+    import oracle
 
     oracle.set_threads(threads)
     om = oracle.OracleModel(text, arrays)
     om.loglike(params[0])  # warm-up
+    n = 0
     t0 = time.perf_counter()
-    for i in range(sample):
-        om.loglike(params[i % len(params)])
+    while (sample and n < sample) or (not sample and time.perf_counter() - t0 < budget_s):
+        om.loglike(params[n % len(params)])
+        n += 1
     dt = time.perf_counter() - t0
-    return sample / dt, dt
+    return n / dt, dt, n
 
 
 def run_reference(args):
@@ -220,7 +227,7 @@ def run_reference(args):
     om = oracle.OracleModel(text, arrays)
     B = args.batch or spec.batch
     params = live_points(spec, kind, B, 0)
-    per_step = max(1, int(os.environ.get("BEAR_REF_EVALS_PER_STEP", "4")))
+    per_step = max(1, int(os.environ.get("BEAR_REF_EVALS_PER_STEP", "16")))
     for i in range(args.warmup):
         om.loglike(params[i % B])
     times = []
@@ -350,6 +357,35 @@ def main():
         eng.loglike(params_host[i % B])
     plain_s = (time.perf_counter() - t0) / n_plain
 
+    # adjoint gradient (emission models): log L and d log L / d params for the batch
+    grad = None
+    if kind == "emission":
+        G = torch.empty(B, eng.P, dtype=torch.float64, device=device)
+
+        def grad_step():
+            eng.grad_batch_ptr(P.data_ptr(), B, ll.data_ptr(), G.data_ptr(), ng.data_ptr(), stream.cuda_stream)
+
+        for _ in range(2):
+            grad_step()
+        barrier()
+        n_grad = max(3, min(args.steps, 10))
+        gev = []
+        for _ in range(n_grad):
+            flush.zero_()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            grad_step()
+            e.record(stream)
+            gev.append((s, e))
+        barrier()
+        grad_ms = sum(s.elapsed_time(e) for s, e in gev) / n_grad
+        fwd_ms = total_ms / args.steps
+        grad = {"evals_per_s": B / (grad_ms * 1e-3), "ms_per_batch": grad_ms, "forward_ms_per_batch": fwd_ms,
+                "grad_over_forward": grad_ms / fwd_ms, "parameters": eng.P, "steps": n_grad,
+                "kernels_per_batch": 6,
+                "api": "bear_loglike_grad_batch (adjoint; forward pass included in the time)"}
+        del G
+
     # dominant kernel timing for the roofline (CUDA events on the launching stream)
     stages = eng.stage_times(P.data_ptr(), B, ll.data_ptr(), stream.cuda_stream, repeats=5)
     kern_ms = stages[1]
@@ -390,15 +426,19 @@ def main():
             "fp64": {"note": "the kernels are bound by FP64 issue, not HBM",
                      "dgemm_peak_tflops_measured": fp64_peak},
         }
+        if grad is not None:
+            line["gradient"] = grad
     if rank == 0:
         line["clocks"] = clocks.summary()
         if not args.no_cpu_baseline:
             threads = os.cpu_count() or 1
-            sample = args.cpu_sample or (8 if args.workload != "transmission_plain" else 4)
-            v, dt = cpu_baseline(text, arrays, params_host, sample, threads)
+            v, dt, n = cpu_baseline(text, arrays, params_host, args.cpu_sample, threads)
             line["cpu_baseline"] = {"value": v, "unit": "evals/s", "cores": threads, "kind": "port",
-                                    "sample": f"{sample} sequential evaluations of this batch's live points "
+                                    "sample": f"{n} sequential evaluations of this batch's live points "
                                               f"({dt:.1f} s), FP64 C oracle with OpenMP"}
+            if "gradient" in line:
+                # the reference has no derivatives: a central-difference gradient costs 2P + 1 evaluations
+                line["gradient"]["cpu_central_difference_evals_per_s"] = v / (2 * eng.P + 1)
         print(json.dumps(line))
     eng.close()
     if dist is not None:
