@@ -178,4 +178,24 @@ BGB_HD double exp_tang(double x, const double* tab) {
   return BGB_DMA(scaled, p, scaled);
 }
 
+// The same method with a 2048-entry table (tab: 2^(j/2048), j = 0..2047): |r| <=
+// ln2/4096, so the degree-3 Taylor polynomial r + r^2/2 + r^3/6 suffices
+// (remainder r^4/24 < 3.5e-17): 8 FP64 operations instead of 10.
+// Valid for x in [-700, 700]; about 1 ulp.
+BGB_HD double exp_tang2048(double x, const double* tab) {
+  const double shifter = 6755399441055744.0;  // 1.5 * 2^52
+  const double t = BGB_DMA(x, k2048OverLn2, shifter);
+  const double kd = t - shifter;
+  const int k = (int)(bgb_double_as_ll(t) & 0xffffffff);
+  double r = BGB_DMA(-kd, kLn2Over2048Hi, x);
+  r = BGB_DMA(-kd, kLn2Over2048Lo, r);
+  double p = BGB_DMA(r, 1.0 / 6.0, 0.5);
+  p = BGB_DMA(r * r, p, r);
+  const int j = k & 2047;
+  const int m = k >> 11;  // floor(k / 2048)
+  const double T = tab[j];
+  const double scaled = bgb_ll_as_double(bgb_double_as_ll(T) + ((long long)m << 52));
+  return BGB_DMA(scaled, p, scaled);
+}
+
 }  // namespace bgb

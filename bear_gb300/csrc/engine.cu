@@ -70,7 +70,9 @@ __global__ void __launch_bounds__(256) emission_kernel(DeviceModel dm, const Lev
                                                        const EvalInfo* __restrict__ ev,
                                                        double* __restrict__ spectrum, double* __restrict__ istore) {
   __shared__ ExpTables et;
+  __shared__ double tab2048[2048];
   load_exp_tables(et);
+  for (int i = threadIdx.x; i < 2048; i += blockDim.x) tab2048[i] = kExp2TabD2048[i];
   __syncthreads();
   const int b = blockIdx.x;
   const int k = blockIdx.y * blockDim.x + threadIdx.x;
@@ -99,7 +101,7 @@ __global__ void __launch_bounds__(256) emission_kernel(DeviceModel dm, const Lev
     const double B = planck(l);
     double tau, rtau;
     emission_layer_tau_df(lv, l, kap, kap_prev, tau, rtau);
-    sc_layer_fast(tau, rtau, B, B_prev, I1, I2, et.d);
+    sc_layer_fast(tau, rtau, B, B_prev, I1, I2, tab2048);
     if (STORE) {
       Is[(size_t)l * 2 * N] = I1;
       Is[(size_t)l * 2 * N + N] = I2;

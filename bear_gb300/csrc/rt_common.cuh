@@ -140,7 +140,9 @@ __device__ __forceinline__ void emission_layer_tau_df(const LevelInfo* __restric
                                                       const Kappa& kap_prev, double& tau, double& rtau) {
   const float4 g = __ldg(reinterpret_cast<const float4*>(&lv[l - 1].dzh_hi));  // dzh, cloud
   const df2 t = df_add(df_mul(df2{g.x, g.y}, df_add(kap.v, kap_prev.v)), df2{g.z, g.w});
-  if (kap.wide == 0.0 && kap_prev.wide == 0.0 && t.hi > 1e-30f && t.hi < 1e30f) {
+  // both wide parts zero (+-0), tested on the bits to stay off the FP64 pipe
+  const bool narrow = ((__double_as_longlong(kap.wide) | __double_as_longlong(kap_prev.wide)) << 1) == 0;
+  if (narrow && t.hi > 1e-30f && t.hi < 1e30f) {
     tau = df_to_double(t);
     rtau = df_to_double(df_div(df_make(1.0f), t));
   } else {
@@ -173,16 +175,16 @@ __device__ __forceinline__ void sc_layer(double tau, double B, double B_prev, do
 
 // The same layer in fewer FP64 operations, used by the default kernel:
 // I a + (1+q) B + (-a-q) B' == a (I - B') + B + q (B - B'), with q = (a-1)/delta and
-// 1/tau supplied by the caller (computed in double-float). The exponential and the
-// recurrence stay FP64.
+// 1/tau supplied by the caller (computed in double-float). The exponential
+// (exp_tang2048; tab2048 = 2^(j/2048)) and the recurrence stay FP64.
 __device__ __forceinline__ void sc_layer_fast(double tau, double rtau, double B, double B_prev, double& I1,
-                                              double& I2, const double* tab) {
-  if (tau == 0) return;
+                                              double& I2, const double* tab2048) {
+  if ((__double_as_longlong(tau) << 1) == 0) return;  // tau == 0 (bit test)
   const double dB = B - B_prev;
 #pragma unroll
   for (int i = 0; i < 2; ++i) {
     const double d = tau * kInvMu[i];
-    const double a = __double_as_longlong(d) > kBits700 ? 0.0 : exp_tang(-d, tab);
+    const double a = __double_as_longlong(d) > kBits700 ? 0.0 : exp_tang2048(-d, tab2048);
     const double q = (a - 1.0) * (kMu[i] * rtau);
     double& I = i == 0 ? I1 : I2;
     I = fma(a, I - B_prev, B);

@@ -1,0 +1,63 @@
+// Host build of the engine's hand-written exponentials (dfloat.cuh / physics.cuh
+// compiled with BGB_HOST_EMULATION: the same operation sequence with IEEE
+// round-to-nearest host arithmetic) measured against long-double references.
+// Prints one "name max_relative_error" line per routine.
+#define BGB_HOST_EMULATION
+#include <cmath>
+#include <cstdio>
+#include <random>
+
+#include "../bear_gb300/csrc/physics.cuh"
+
+using namespace bgb;
+
+int main() {
+  std::mt19937_64 g(20261203);
+  std::uniform_real_distribution<double> U(0.0, 1.0);
+  double e_exp2 = 0, e_tang = 0, e_tang2048 = 0, e_pow10 = 0, e_planck = 0, e_expneg = 0, ulp2048 = 0;
+  for (int i = 0; i < 2000000; ++i) {
+    // double-float 2^y over the exponent range of the opacity terms
+    const double y = -140.0 + 180.0 * U(g);
+    const df2 yd = df_from_double(y);
+    int n;
+    const df2 m = df_exp2(yd, n, kExp2TabHi, kExp2TabLo);
+    const long double ry = exp2l((long double)yd.hi + (long double)yd.lo);
+    e_exp2 = std::fmax(e_exp2, (double)fabsl(((long double)m.hi + m.lo) * exp2l(n) / ry - 1));
+    // FP64 exp(x), x in [-700, 0] (the recurrence's exp(-delta)), with thin layers oversampled
+    double x = -700.0 * U(g);
+    if (i % 4 == 0) x = -1e-3 * U(g);
+    const long double rx = expl((long double)x);
+    e_tang = std::fmax(e_tang, (double)fabsl(exp_tang(x, kExp2TabD) / rx - 1));
+    const double b = exp_tang2048(x, kExp2TabD2048);
+    e_tang2048 = std::fmax(e_tang2048, (double)fabsl(b / rx - 1));
+    const double rd = (double)rx;
+    ulp2048 = std::fmax(ulp2048, (double)fabsl(((long double)b - rx) / (std::nextafter(rd, 1e308) - rd)));
+    // double-float exp(-d) of the adjoint
+    const double d = 60.0 * U(g);
+    const df2 en = df_exp_neg(df_from_double(d), kExp2TabHi, kExp2TabLo);
+    const long double rn = expl(-(long double)(double)df_from_double(d).hi - (long double)df_from_double(d).lo);
+    e_expneg = std::fmax(e_expneg, (double)fabsl(((long double)en.hi + en.lo) / rn - 1));
+  }
+  for (int i = 0; i < 1000000; ++i) {
+    // 10^x for log10 cross sections
+    const double x = -40.0 + 30.0 * U(g);
+    const df2 xd = df_from_double(x);
+    int n;
+    const df2 m = df_exp2(df_mul(xd, df2{kLog2_10Hi, kLog2_10Lo}), n, kExp2TabHi, kExp2TabLo);
+    const long double r = powl(10.0L, (long double)xd.hi + (long double)xd.lo);
+    e_pow10 = std::fmax(e_pow10, (double)fabsl(((long double)m.hi + m.lo) * exp2l(n) / r - 1));
+    // Planck function c1 / (exp(c2 / T) - 1), nu in [1000, 26000] cm^-1, T in [50, 4000] K
+    const double nu = 1000.0 + 25000.0 * U(g), T = 50.0 + 3950.0 * U(g);
+    const double c1 = 2.0 * 6.62606896e-27 * 2.99792458e10 * 2.99792458e10 * nu * nu * nu;
+    const double c2 = 6.62606896e-27 * nu * 2.99792458e10 / 1.3806504e-16;
+    const long double rp = (long double)c1 / expm1l((long double)c2 / T);
+    const double c2l = c2 * 1.4426950408889634;
+    const df2 c2ld = {(float)c2l, (float)(c2l - (double)(float)c2l)};
+    const double Bp = planck_df(df_from_double(c1), c2ld, df_from_double(1.0 / T), kExp2TabHi, kExp2TabLo);
+    if (c2 / T < 690.0) e_planck = std::fmax(e_planck, (double)fabsl(Bp / rp - 1));
+  }
+  std::printf("df_exp2 %.3e\nexp_tang %.3e\nexp_tang2048 %.3e\nexp_tang2048_ulp %.3f\ndf_exp_neg %.3e\n"
+              "df_pow10 %.3e\nplanck_df %.3e\n",
+              e_exp2, e_tang, e_tang2048, ulp2048, e_expneg, e_pow10, e_planck);
+  return 0;
+}

@@ -1,0 +1,52 @@
+"""Accuracy of the engine's hand-written exponentials, measured on the CPU.
+
+dfloat.cuh / physics.cuh compile on the host with BGB_HOST_EMULATION (the same
+operation sequence in IEEE round-to-nearest host arithmetic, FMA where the
+device code uses FMA); tests/numerics_harness.cpp measures each routine
+against long-double references over the argument ranges the kernels use:
+
+* exp_tang / exp_tang2048: Tang's table-driven FP64 exp (64- and 2048-entry
+  tables), the exp(-delta) of the short-characteristics recurrence and the
+  tangent-ray transmission;
+* df_exp2 / 10^x: double-float exponentials of the opacity assembly;
+* planck_df: the double-float Planck function;
+* df_exp_neg: the double-float exp(-delta) of the adjoint.
+
+The bounds are the accuracy figures the kernels rely on (about 1 ulp for the
+FP64 routines; the double-float ones are limited by their ~48-bit inputs).
+"""
+
+import os
+import shutil
+import subprocess
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+BOUNDS = {
+    "exp_tang": 3.4e-16,        # ~1.5 ulp
+    "exp_tang2048": 3.4e-16,
+    "exp_tang2048_ulp": 1.5,
+    "df_exp2": 5e-14,
+    "df_pow10": 2e-12,          # |x| <= 40: 10^x from a 48-bit x log2(10)
+    "df_exp_neg": 1e-12,        # d <= 60
+    "planck_df": 1e-11,         # x = h nu c / k T up to 690: ~x 2^-48 from the 48-bit exponent
+}
+
+
+@pytest.fixture(scope="module")
+def measured(tmp_path_factory):
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        pytest.skip("no C++ compiler")
+    exe = str(tmp_path_factory.mktemp("numerics") / "numerics_harness")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-o", exe,
+                    os.path.join(HERE, "numerics_harness.cpp")], check=True)
+    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
+    return {k: float(v) for k, v in (line.split() for line in out.strip().splitlines())}
+
+
+@pytest.mark.parametrize("name", sorted(BOUNDS))
+def test_exponential_accuracy(measured, name):
+    assert measured[name] <= BOUNDS[name], (name, measured[name])
