@@ -42,6 +42,12 @@ EXPORTS = {
     "bear_model_set_precision": (C.c_int, [C.c_void_p, C.c_int]),
     "bear_model_set_launch": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "bear_model_set_gradient_memory": (C.c_int, [C.c_void_p, C.c_longlong]),
+    "bear_model_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                      C.POINTER(C.c_int)]),
+    "bear_batch_graph_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                          C.POINTER(C.c_void_p)]),
+    "bear_batch_graph_launch": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "bear_batch_graph_destroy": (C.c_int, [C.c_void_p]),
     "bear_loglike_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "bear_model_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "bear_model_stage_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),

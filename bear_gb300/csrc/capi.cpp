@@ -367,3 +367,137 @@ int bear_loglike_grad_batch(bear_model* h, const double* params_dev, int batch, 
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ autotuner and captured batches
+// Not in the reference (it evaluates one point per call). The autotuner times the
+// radiative-transfer kernel's launch shapes on the caller's batch with CUDA events
+// and keeps the fastest for batched calls; the batch graph captures the batched
+// kernel sequence once and replays it.
+
+struct bear_batch_graph {
+  bear_model* h = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  unsigned generation = 0;
+};
+
+extern "C" {
+
+int bear_model_autotune(bear_model* h, const double* params_dev, int batch, int nb_params, void* stream,
+                        int* rt_threads_out) {
+  return guarded([&] {
+    require_ready(h);
+    require_params(h, nb_params);
+    if (batch < 2) throw bgb::Error(BEAR_ERR_SIZE, "autotuning needs a batch of at least 2");
+    if (!params_dev) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null device buffer");
+    bgb::Model& m = h->m;
+    const cudaStream_t st = (cudaStream_t)stream;
+    // emission: threads (wavenumbers) per block; transmission: wavenumbers per block
+    const std::vector<int> cand = m.transmission ? std::vector<int>{32, 16, 64} : std::vector<int>{64, 128, 256};
+    const int saved_rt = m.rt_threads;
+    const bool saved_prof = m.profiling;
+    m.rt_threads = 0;
+    m.profiling = false;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int best = 0;
+    float best_ms = 0.0f;
+    try {
+      check_cuda(cudaEventCreate(&e0), "cudaEventCreate");
+      check_cuda(cudaEventCreate(&e1), "cudaEventCreate");
+      for (int c : cand) {
+        m.tuned_rt = c;
+        bgb::launch_forward(m, params_dev, batch, st, true, nullptr, nullptr);  // warm-up
+        check_cuda(cudaEventRecord(e0, st), "cudaEventRecord");
+        for (int r = 0; r < 3; ++r) bgb::launch_forward(m, params_dev, batch, st, true, nullptr, nullptr);
+        check_cuda(cudaEventRecord(e1, st), "cudaEventRecord");
+        check_cuda(cudaEventSynchronize(e1), "cudaEventSynchronize");
+        float ms = 0.0f;
+        check_cuda(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+        if (best == 0 || ms < best_ms) {
+          best = c;
+          best_ms = ms;
+        }
+      }
+    } catch (...) {
+      if (e0) cudaEventDestroy(e0);
+      if (e1) cudaEventDestroy(e1);
+      m.rt_threads = saved_rt;
+      m.profiling = saved_prof;
+      throw;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    m.tuned_rt = best;
+    m.rt_threads = saved_rt;
+    m.profiling = saved_prof;
+    if (rt_threads_out) *rt_threads_out = best;
+  });
+}
+
+int bear_batch_graph_create(bear_model* h, const double* params_dev, int batch, int nb_params,
+                            double* loglike_dev, uint8_t* neglect_dev, bear_batch_graph** out) {
+  return guarded([&] {
+    require_ready(h);
+    require_params(h, nb_params);
+    if (batch < 1) throw bgb::Error(BEAR_ERR_SIZE, "batch must be positive");
+    if (!params_dev || !loglike_dev || !out) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null buffer");
+    bgb::Model& m = h->m;
+    check_cuda(cudaSetDevice(m.device), "cudaSetDevice");
+    bgb::ensure_workspace(m, batch);  // every allocation happens before the capture
+    const bool saved_prof = m.profiling;
+    m.profiling = false;
+    cudaStream_t s = nullptr;
+    check_cuda(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreateWithFlags");
+    cudaGraph_t graph = nullptr;
+    cudaError_t ce = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (ce != cudaSuccess) {
+      cudaStreamDestroy(s);
+      m.profiling = saved_prof;
+      check_cuda(ce, "cudaStreamBeginCapture");
+    }
+    try {
+      bgb::launch_forward(m, params_dev, batch, s, true, neglect_dev, loglike_dev);
+    } catch (...) {
+      cudaStreamEndCapture(s, &graph);
+      if (graph) cudaGraphDestroy(graph);
+      cudaStreamDestroy(s);
+      m.profiling = saved_prof;
+      throw;
+    }
+    m.profiling = saved_prof;
+    ce = cudaStreamEndCapture(s, &graph);
+    cudaStreamDestroy(s);
+    check_cuda(ce, "cudaStreamEndCapture");
+    auto* g = new bear_batch_graph;
+    g->h = h;
+    g->graph = graph;
+    g->generation = m.ws_generation;
+    ce = cudaGraphInstantiate(&g->exec, graph, 0);
+    if (ce != cudaSuccess) {
+      cudaGraphDestroy(graph);
+      delete g;
+      check_cuda(ce, "cudaGraphInstantiate");
+    }
+    *out = g;
+  });
+}
+
+int bear_batch_graph_launch(bear_batch_graph* g, void* stream) {
+  return guarded([&] {
+    if (!g || !g->exec) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null graph");
+    if (g->generation != g->h->m.ws_generation)
+      throw bgb::Error(BEAR_ERR_STATE, "the model's work buffers were reallocated after the capture; recreate the graph");
+    check_cuda(cudaGraphLaunch(g->exec, (cudaStream_t)stream), "cudaGraphLaunch");
+  });
+}
+
+int bear_batch_graph_destroy(bear_batch_graph* g) {
+  return guarded([&] {
+    if (!g) return;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
+  });
+}
+
+}  // extern "C"

@@ -180,21 +180,24 @@ __global__ void transmission_geometry_kernel(DeviceModel dm, const LevelInfo* __
 
 // Transit depth (TransmissionModel::calcTransmissionSpectrum ... tangentOpticalDepth
 // src/forward_model/transmission/transmission_spectrum.cpp:32-141). A block covers
-// VPB = 128 / TPN wavenumbers with TPN threads each (lane = wavenumber, so table
-// reads stay coalesced). The TPN threads of a wavenumber split the levels' opacities,
+// VPB wavenumbers with TPN = 4 threads each (lane = wavenumber, so table reads stay
+// coalesced; VPB is the tuned launch shape and does not change any sum's order).
+// The TPN threads of a wavenumber split the levels' opacities,
 // then share the staged extinction column chi[L][VPB] (FP64) and split the tangent
 // levels. Tangent sums are FP64 with the reference's tau > 10 cut-off; the
 // effective height is summed per level, sum_t (R + z_t)(1 - T_t)(dz_{t-1} + dz_t),
 // which regroups the reference's trapezoid sum.
-template <bool DF, int TPN>
-__global__ void __launch_bounds__(128) transmission_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
+constexpr int kTPN = 4;
+
+template <bool DF, int VPB>
+__global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
                                                            const LevelSpecies* __restrict__ ls,
                                                            const LevelSpeciesDF* __restrict__ lsdf,
                                                            const double* __restrict__ ray_n,
                                                            const EvalInfo* __restrict__ ev,
                                                            const double* __restrict__ geom,
                                                            double* __restrict__ spectrum) {
-  constexpr int VPB = 128 / TPN;
+  constexpr int TPN = kTPN;
   extern __shared__ double chi_s[];  // [L][VPB]
   __shared__ ExpTables et;
   __shared__ double h_part[TPN][VPB];
@@ -447,10 +450,12 @@ void upload_model(Model& m) {
   // the transmission kernels stage L x blockDim doubles of extinction in shared memory
   if (m.transmission) {
     const int sm = (int)kTransmissionDynSmem;
-    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<true, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<false, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<true, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<false, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<true, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<false, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<true, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<false, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<true, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<false, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
   }
 }
 
@@ -488,6 +493,7 @@ void ensure_workspace(Model& m, int batch) {
   BGB_CUDA(cudaMalloc(&w.loglike, B * sizeof(double)));
   if (m.transmission) BGB_CUDA(cudaMalloc(&w.geom, B * L * L * sizeof(double)));
   w.capacity = batch;
+  ++m.ws_generation;
 }
 
 // Kernel sequence of one batch on the given work buffers.
@@ -505,8 +511,10 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
                                                                         taps ? taps->dwT : nullptr);
   BGB_CUDA(cudaGetLastError());
   if (profile) BGB_CUDA(cudaEventRecord(m.ev[1], st));
+  // launch shape: explicit setting, else the autotuned one for batches, else the default
+  const int rt = m.rt_threads > 0 ? m.rt_threads : (batch > 1 ? m.tuned_rt : 0);
   if (!m.transmission) {
-    const int TB = m.rt_threads > 0 ? m.rt_threads : (batch == 1 ? 64 : 128);
+    const int TB = rt > 0 ? rt : (batch == 1 ? 64 : 128);
     dim3 grid(batch, (dm.N + TB - 1) / TB);
     if (taps && m.precision == 1)
       emission_kernel_fp64<true><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.ev, w.spectrum, taps->istore);
@@ -519,22 +527,18 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
   } else {
     if (taps) throw Error(BEAR_ERR_UNSUPPORTED, "gradient of transmission models not available");
     transmission_geometry_kernel<<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom);
-    // rt_threads selects the wavenumbers per block: 32 (4 threads each, default) or 16 (8 each)
-    const int vpb = (m.rt_threads == 16) ? 16 : 32;
+    // the launch shape selects the wavenumbers per block: 16, 32 (default) or 64, 4 threads each
+    const int vpb = (rt == 16 || rt == 64) ? rt : 32;
     dim3 grid(batch, (dm.N + vpb - 1) / vpb);
     const size_t sm = (size_t)L * vpb * sizeof(double);
     if (sm > kTransmissionDynSmem) throw Error(BEAR_ERR_UNSUPPORTED, "too many levels for the transmission kernel");
-    if (vpb == 32) {
-      if (m.precision == 1)
-        transmission_kernel<false, 4><<<grid, 128, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.spectrum);
-      else
-        transmission_kernel<true, 4><<<grid, 128, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.spectrum);
-    } else {
-      if (m.precision == 1)
-        transmission_kernel<false, 8><<<grid, 128, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.spectrum);
-      else
-        transmission_kernel<true, 8><<<grid, 128, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.spectrum);
-    }
+    const bool df = m.precision != 1;
+    auto go = [&](auto kernel) {
+      kernel<<<grid, kTPN * vpb, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.spectrum);
+    };
+    if (vpb == 16) df ? go(transmission_kernel<true, 16>) : go(transmission_kernel<false, 16>);
+    else if (vpb == 64) df ? go(transmission_kernel<true, 64>) : go(transmission_kernel<false, 64>);
+    else df ? go(transmission_kernel<true, 32>) : go(transmission_kernel<false, 32>);
   }
   BGB_CUDA(cudaGetLastError());
   if (profile) BGB_CUDA(cudaEventRecord(m.ev[2], st));

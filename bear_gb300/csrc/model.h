@@ -275,6 +275,8 @@ struct Model {
   int device = 0;
   int precision = 0;  // 0: double-float opacity + table exponentials, 1: FP64 libm kernels
   int rt_threads = 0, obs_threads = 0;
+  int tuned_rt = 0;           // autotuned radiative-transfer launch shape for batches > 1 (0: default)
+  unsigned ws_generation = 0; // bumped whenever the workspace is reallocated (captured graphs check it)
   DeviceModel dm{};
   std::vector<void*> allocations;
   size_t device_bytes = 0;

@@ -13,6 +13,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import weakref
 from dataclasses import dataclass, field
 from typing import List, Optional, Sequence, Tuple
 
@@ -43,6 +44,7 @@ class Engine:
         h = C.c_void_p()
         _lib.check(lib.bear_model_create(config_text.encode(), int(device), C.byref(h)))
         self._h = h
+        self._graphs = weakref.WeakSet()  # captured batches to destroy before the model
         self._lib = lib
         self.device = int(device)
         self._keep = []
@@ -172,6 +174,18 @@ class Engine:
         """0: double-float opacity assembly (default); 1: every step in FP64."""
         _lib.check(self._lib.bear_model_set_precision(self._h, int(mode)))
 
+    def autotune(self, params) -> int:
+        """Time the radiative-transfer launch shapes on ``params`` (torch float64 CUDA,
+        (B, P), B >= 2) and keep the fastest for batched calls; returns it."""
+        import torch
+        t = params.detach().contiguous()
+        assert t.dtype == torch.float64 and t.is_cuda and t.shape[1] == self.P
+        best = C.c_int()
+        _lib.check(self._lib.bear_model_autotune(self._h, C.c_void_p(t.data_ptr()), int(t.shape[0]), self.P,
+                                                 C.c_void_p(torch.cuda.current_stream(t.device).cuda_stream),
+                                                 C.byref(best)))
+        return best.value
+
     def set_gradient_memory(self, nbytes: int = 0) -> None:
         """Device memory the gradient's work buffers may use per chunk (0 = default)."""
         _lib.check(self._lib.bear_model_set_gradient_memory(self._h, int(nbytes)))
@@ -216,9 +230,61 @@ class Engine:
         return b.value
 
     def close(self) -> None:
+        for g in list(getattr(self, "_graphs", ())):
+            g.close()
         if getattr(self, "_h", None):
             self._lib.bear_model_destroy(self._h)
             self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class BatchEvaluator:
+    """Batched log-likelihoods through a captured CUDA graph.
+
+    Owns device buffers for ``batch`` parameter sets; on creation optionally
+    autotunes the engine's launch shape on ``params`` (B, P) and captures the
+    kernel sequence once. Each call copies the new parameters into the owned
+    buffer and replays the graph on the current stream; the returned tensors are
+    the owned log-likelihood / neglect buffers (overwritten by the next call)."""
+
+    def __init__(self, engine: "Engine", params, autotune: bool = True):
+        import torch
+        t = params.detach().contiguous()
+        assert t.dtype == torch.float64 and t.is_cuda and t.shape[1] == engine.P
+        self.engine = engine
+        self.batch = int(t.shape[0])
+        self.params = t.clone()
+        self.loglike = torch.empty(self.batch, dtype=torch.float64, device=t.device)
+        self.neglect = torch.empty(self.batch, dtype=torch.uint8, device=t.device)
+        self.rt_threads = engine.autotune(self.params) if autotune and self.batch >= 2 else 0
+        torch.cuda.synchronize(t.device)
+        h = C.c_void_p()
+        _lib.check(engine._lib.bear_batch_graph_create(engine._h, C.c_void_p(self.params.data_ptr()), self.batch,
+                                                       engine.P, C.c_void_p(self.loglike.data_ptr()),
+                                                       C.c_void_p(self.neglect.data_ptr()), C.byref(h)))
+        self._g = h
+        engine._graphs.add(self)
+
+    def launch(self, stream: int = 0) -> None:
+        """Replay the graph on the parameters currently in ``self.params``."""
+        _lib.check(self.engine._lib.bear_batch_graph_launch(self._g, C.c_void_p(stream)))
+
+    def __call__(self, params=None):
+        import torch
+        if params is not None:
+            self.params.copy_(params, non_blocking=True)
+        self.launch(torch.cuda.current_stream(self.params.device).cuda_stream)
+        return self.loglike, self.neglect
+
+    def close(self) -> None:
+        if getattr(self, "_g", None):
+            _lib.check(self.engine._lib.bear_batch_graph_destroy(self._g))
+            self._g = None
 
     def __del__(self):
         try:

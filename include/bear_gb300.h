@@ -157,6 +157,31 @@ int bear_loglike_grad_batch(bear_model* m, const double* params_dev, int batch, 
  * (0 = default, 16 GiB). No reference counterpart. */
 int bear_model_set_gradient_memory(bear_model* m, long long bytes);
 
+/* --------------------------------------------------------------- autotuner and captured batches
+ * No reference counterpart. bear_model_autotune times the radiative-transfer
+ * kernel's launch shapes (emission: 64 / 128 / 256 threads per block;
+ * transmission: 16 / 32 / 64 wavenumbers per block) on this batch with CUDA events,
+ * keeps the fastest for later batched calls (an explicit bear_model_set_launch
+ * takes precedence) and reports it. Synchronous; results do not depend on the
+ * choice (each wavenumber is computed by the same code). */
+int bear_model_autotune(bear_model* m, const double* params_dev, int batch, int nb_params, void* stream,
+                        int* rt_threads_out);
+
+/* A captured batch: the batched kernel sequence (atmosphere, radiative transfer,
+ * observation + likelihood) for fixed device buffers params_dev (batch x
+ * nb_params), loglike_dev (batch) and neglect_dev (batch bytes, NULL allowed),
+ * captured once into a CUDA graph. Write new parameters into params_dev, then
+ * bear_batch_graph_launch replays the kernels on the given stream. The graph uses
+ * the model's work buffers as they were at capture: a launch after they were
+ * reallocated (a larger batch or gradient chunk on the same model) fails with
+ * BEAR_ERR_STATE; precision and launch settings changed later do not affect it.
+ * Destroy graphs before their model. */
+typedef struct bear_batch_graph bear_batch_graph;
+int bear_batch_graph_create(bear_model* m, const double* params_dev, int batch, int nb_params,
+                            double* loglike_dev, uint8_t* neglect_dev, bear_batch_graph** out);
+int bear_batch_graph_launch(bear_batch_graph* g, void* stream);
+int bear_batch_graph_destroy(bear_batch_graph* g);
+
 /* Arithmetic of the opacity assembly (applies to every evaluation path):
  * 0 (default) = double-float (hi + lo float pairs, ~48 bits) on the FP32 pipe
  * with table-driven exponentials; radiative-transfer recurrences, tangent-ray
@@ -164,8 +189,11 @@ int bear_model_set_gradient_memory(bear_model* m, long long bytes);
  * math library (the validation path). */
 int bear_model_set_precision(bear_model* m, int mode);
 
-/* Launch configuration of the batched kernels (threads per block along the
- * spectral axis; 0 = default). Used by the autotuner. */
+/* Launch shape of the radiative-transfer kernel (emission: threads =
+ * wavenumbers per block, 64 / 128 / 256; transmission: wavenumbers per block,
+ * 16 / 32 / 64, four threads each; 0 = default or the autotuned shape) and threads
+ * per block of the observation + likelihood kernel (0 = 256). An explicit
+ * setting overrides bear_model_autotune. */
 int bear_model_set_launch(bear_model* m, int rt_threads, int obs_threads);
 
 /* Allocation-free log-likelihood of one parameter set. No counterpart in the
