@@ -56,7 +56,6 @@ namespace bgb {
 
 constexpr int kAdjThreads = 128;  // threads (wavenumbers) per block of the adjoint kernel
 constexpr double kLn10 = 2.302585092994045684;
-constexpr float kLn10Hi = (float)kLn10, kLn10Lo = (float)(kLn10 - (double)kLn10Hi);
 
 // ------------------------------------------------------------------ accumulators
 // The per-level sinks are summed either as double-floats (FP32 pipe) or in FP64.
@@ -350,7 +349,7 @@ __global__ void __launch_bounds__(kAdjThreads, DF ? 6 : 4) emission_adjoint_kern
       df2 dk = {0.0f, 0.0f};
       double dkw = 0.0;
       bool wd = false;
-      kp = level_kappa_df_cb(dm.table_df, N, sp + (size_t)l * S, sf + (size_t)l * S, S, k, et,
+      kp = level_kappa_df_cb(dm.ltab, N, sf + (size_t)l * S, S, k, et,
                              [&](int s, df2 t, double t_w, bool is_wide, df2 lo, df2 hi) {
                                const float2 d = __ldg(dwl + s);
                                td[(size_t)s * kAdjThreads] = make_float2(t.hi, t.lo);
@@ -362,8 +361,9 @@ __global__ void __launch_bounds__(kAdjThreads, DF ? 6 : 4) emission_adjoint_kern
                                }
                                wd = wd || is_wide;
                              });
-      dk_out = df_mul(dk, df2{kLn10Hi, kLn10Lo});
-      dkw_out = dkw * kLn10;
+      // level-table values are log2 cross sections: d(2^y)/dy = 2^y ln 2
+      dk_out = df_mul(dk, df2{kLn2Hi, kLn2Lo});
+      dkw_out = dkw * 0.693147180559945309;
       wide = wd;
     } else {
       double dk = 0.0;

@@ -273,11 +273,10 @@ __global__ void __launch_bounds__(kMaxLevels) atmosphere_kernel(DeviceModel dm, 
       e.wp_hi = dm.pb_w[iup];
       e.wT = (lo != up) ? (T - Tn[lo]) / (Tn[up] - Tn[lo]) : 0.0;
       LevelSpeciesDF& f = lsdf[((size_t)b * L + l) * S + s];
-      const df2 a = df_from_double(e.wp_lo), bw = df_from_double(e.wp_hi), t = df_from_double(e.wT);
-      f.wp_lo_hi = a.hi;
-      f.wp_lo_lo = a.lo;
-      f.wp_hi_hi = bw.hi;
-      f.wp_hi_lo = bw.lo;
+      const df2 t = df_from_double(e.wT);
+      f.lrow[0] = ilo;  // level-table rows: the pressure-bracket indices
+      f.lrow[1] = iup;
+      f.pad[0] = f.pad[1] = 0;
       f.wT_hi = t.hi;
       f.wT_lo = t.lo;
       // d wT / dT for the adjoint (0 when T is clamped to the end of the table)

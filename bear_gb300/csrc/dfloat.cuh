@@ -100,6 +100,16 @@ BGB_HD df2 df_mul_f(df2 a, float b) {
   return fast_two_sum(p, e);
 }
 
+// a * b + c (products and sum as double-floats).
+BGB_HD df2 df_fma(df2 a, df2 b, df2 c) {
+  const float p = BGB_FMUL(a.hi, b.hi);
+  float e = BGB_FMA(a.hi, b.hi, -p);
+  e = BGB_FMA(a.hi, b.lo, e);
+  e = BGB_FMA(a.lo, b.hi, e);
+  const df2 s = two_sum(c.hi, p);
+  return fast_two_sum(s.hi, BGB_FADD(s.lo, BGB_FADD(e, c.lo)));
+}
+
 // a / b with three correction steps (quotient digits q1 + q2 + q3).
 BGB_HD df2 df_div(df2 a, df2 b) {
   const float q1 = BGB_FDIV(a.hi, b.hi);

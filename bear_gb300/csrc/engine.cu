@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(256) emission_kernel(DeviceModel dm, const Lev
     const float2 it = __ldg(reinterpret_cast<const float2*>(&lv[l].invT_hi));
     return planck_df(c1, c2l, df2{it.x, it.y}, et.hi, et.lo);
   };
-  Kappa kap_prev = level_kappa_df(dm.table_df, N, sp, sf, S, k, et);
+  Kappa kap_prev = level_kappa_df(dm.ltab, N, sf, S, k, et);
   double B_prev = planck(0);
   double I1 = B_prev, I2 = B_prev;
   if (STORE) {
@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(256) emission_kernel(DeviceModel dm, const Lev
     Is[N] = I2;
   }
   for (int l = 1; l < L; ++l) {
-    const Kappa kap = level_kappa_df(dm.table_df, N, sp + (size_t)l * S, sf + (size_t)l * S, S, k, et);
+    const Kappa kap = level_kappa_df(dm.ltab, N, sf + (size_t)l * S, S, k, et);
     const double B = planck(l);
     double tau, rtau;
     emission_layer_tau_df(lv, l, kap, kap_prev, tau, rtau);
@@ -157,7 +157,9 @@ __global__ void __launch_bounds__(256) emission_kernel_fp64(DeviceModel dm, cons
 // sqrt((R+z_{i+1})^2 - (R+z_t)^2) - sqrt((R+z_i)^2 - (R+z_t)^2)
 // (TransmissionModel::distanceToTangentCenter src/forward_model/transmission/
 // transmission_spectrum.cpp:145-154). Squares are rounded separately so the
-// tangent level gives exactly zero.
+// tangent level gives exactly zero. Computed in FP64; stored as FP64 (precision
+// mode 1) or as double-floats (DF, the default tangent sums).
+template <bool DF>
 __global__ void transmission_geometry_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
                                              const EvalInfo* __restrict__ ev, double* __restrict__ geom) {
   const int b = blockIdx.x;
@@ -174,7 +176,12 @@ __global__ void transmission_geometry_kernel(DeviceModel dm, const LevelInfo* __
       const double bb = __dmul_rn(bt, bt);
       v = sqrt(__dsub_rn(__dmul_rn(a1, a1), bb)) - sqrt(__dsub_rn(__dmul_rn(a0, a0), bb));
     }
-    geom[(size_t)b * L * L + idx] = v;
+    if (DF) {
+      const df2 d = df_from_double(v);
+      reinterpret_cast<float2*>(geom)[(size_t)b * L * L + idx] = make_float2(d.hi, d.lo);
+    } else {
+      geom[(size_t)b * L * L + idx] = v;
+    }
   }
 }
 
@@ -182,11 +189,15 @@ __global__ void transmission_geometry_kernel(DeviceModel dm, const LevelInfo* __
 // src/forward_model/transmission/transmission_spectrum.cpp:32-141). A block covers
 // VPB wavenumbers with TPN = 4 threads each (lane = wavenumber, so table reads stay
 // coalesced; VPB is the tuned launch shape and does not change any sum's order).
-// The TPN threads of a wavenumber split the levels' opacities,
-// then share the staged extinction column chi[L][VPB] (FP64) and split the tangent
-// levels. Tangent sums are FP64 with the reference's tau > 10 cut-off; the
-// effective height is summed per level, sum_t (R + z_t)(1 - T_t)(dz_{t-1} + dz_t),
-// which regroups the reference's trapezoid sum.
+// The TPN threads of a wavenumber split the levels' opacities, then share the
+// staged extinction column chi[L][VPB] and split the tangent levels. With DF the
+// extinction column and the tangent optical depths are double-floats on the FP32
+// pipe (the reference's tau > 10 cut-off tested on the double-float value); the
+// transmission exp(-tau) and the effective-height (annulus) sum are FP64 in both
+// modes. The effective height is summed per level,
+// sum_t (R + z_t)(1 - T_t)(dz_{t-1} + dz_t), which regroups the reference's
+// trapezoid sum. Dynamic shared memory: chi [L][VPB] (8 B each), then with DF the
+// evaluation's Rayleigh number densities [L][R] as double-floats.
 constexpr int kTPN = 4;
 
 template <bool DF, int VPB>
@@ -199,9 +210,9 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
                                                            double* __restrict__ spectrum) {
   constexpr int TPN = kTPN;
   extern __shared__ double chi_s[];  // [L][VPB]
+  float2* chi_f = reinterpret_cast<float2*>(chi_s);
   __shared__ ExpTables et;
   __shared__ double h_part[TPN][VPB];
-  if (DF) load_exp_tables(et);
   const int v = threadIdx.x % VPB, j = threadIdx.x / VPB;
   const int b = blockIdx.x;
   const int k = blockIdx.y * VPB + v;
@@ -211,33 +222,95 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
   const LevelInfo* lv = lev + (size_t)b * L;
   const LevelSpecies* sp = ls + (size_t)b * L * S;
   const LevelSpeciesDF* sf = lsdf + (size_t)b * L * S;
+  float2* rn_s = chi_f + (size_t)L * VPB;  // [L][R] (DF only)
+  if (DF) {
+    load_exp_tables(et);
+    for (int idx = threadIdx.x; idx < L * R; idx += blockDim.x) {
+      const df2 d = df_from_double(__ldg(&ray_n[(size_t)b * L * R + idx]));
+      rn_s[idx] = make_float2(d.hi, d.lo);
+    }
+  }
   __syncthreads();
   // extinction abs + scat + cloud of every level (the TPN threads take every TPN-th level)
   if (active) {
     for (int l = j; l < L; l += TPN) {
-      const double a = DF ? level_absorption_df(dm.table_df, N, sp + (size_t)l * S, sf + (size_t)l * S, S, k, et)
-                          : level_absorption_fp64(dm.table64, N, sp + (size_t)l * S, S, k);
-      double sc = 0.0;
-      for (int r = 0; r < R; ++r)
-        sc += __ldg(&dm.rayleigh[(size_t)r * N + k]) * __ldg(&ray_n[((size_t)b * L + l) * R + r]);
-      chi_s[l * VPB + v] = a + sc + __ldg(&lv[l].cloud);
+      if (DF) {
+        const Kappa kp = level_kappa_df(dm.ltab, N, sf + (size_t)l * S, S, k, et);
+        df2 x = kp.v;
+        if ((__double_as_longlong(kp.wide) << 1) != 0) x = df_add(x, df_from_double(kp.wide));
+        for (int r = 0; r < R; ++r) {
+          const float2 sr = __ldg(&dm.rayleigh_df[(size_t)r * N + k]);
+          const float2 nr = rn_s[l * R + r];
+          x = df_fma(df2{sr.x, sr.y}, df2{nr.x, nr.y}, x);
+        }
+        const float2 cl = __ldg(reinterpret_cast<const float2*>(&lv[l].cloud_hi));
+        x = df_add(x, df2{cl.x, cl.y});
+        chi_f[l * VPB + v] = make_float2(x.hi, x.lo);
+      } else {
+        const double a = level_absorption_fp64(dm.table64, N, sp + (size_t)l * S, S, k);
+        double sc = 0.0;
+        for (int r = 0; r < R; ++r)
+          sc += __ldg(&dm.rayleigh[(size_t)r * N + k]) * __ldg(&ray_n[((size_t)b * L + l) * R + r]);
+        chi_s[l * VPB + v] = a + sc + __ldg(&lv[l].cloud);
+      }
     }
   }
   __syncthreads();
   // neighbour sums chi_i + chi_{i+1}, the bracket of every trapezoid term
-  if (active && j == 0)
-    for (int i = 0; i < L - 1; ++i) chi_s[i * VPB + v] += chi_s[(i + 1) * VPB + v];
+  if (active && j == 0) {
+    for (int i = 0; i < L - 1; ++i) {
+      if (DF) {
+        const float2 c0 = chi_f[i * VPB + v], c1 = chi_f[(i + 1) * VPB + v];
+        const df2 s2 = df_add(df2{c0.x, c0.y}, df2{c1.x, c1.y});
+        chi_f[i * VPB + v] = make_float2(s2.hi, s2.lo);
+      } else {
+        chi_s[i * VPB + v] += chi_s[(i + 1) * VPB + v];
+      }
+    }
+  }
   __syncthreads();
   double h = 0.0;
   const double Rp = ev[b].radius;
   if (active) {
-    const double* G = geom + (size_t)b * L * L;
     for (int t = L - 2 - j; t >= 0; t -= TPN) {
-      double tau = 0.0;
-      const double* Gt = G + (size_t)t * L;
-      for (int i = t; i < L - 1; ++i) {
-        tau = fma(__ldg(&Gt[i]), chi_s[i * VPB + v], tau);
-        if (__double_as_longlong(tau) > kBits10) break;  // tau > 10 (tau >= 0)
+      double tau;
+      if (DF) {
+        const float2* Gt = reinterpret_cast<const float2*>(geom) + (size_t)b * L * L + (size_t)t * L;
+        df2 ts = {0.0f, 0.0f};
+        auto over = [](df2 x) { return x.hi > 10.0f || (x.hi == 10.0f && x.lo > 0.0f); };  // tau > 10
+        int i = t;
+        bool cut = false;
+        // four terms per iteration with their loads issued together (same sum, same break)
+        for (; i + 3 < L - 1 && !cut; i += 4) {
+          float2 g[4], c[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            g[u] = __ldg(&Gt[i + u]);
+            c[u] = chi_f[(i + u) * VPB + v];
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            ts = df_fma(df2{g[u].x, g[u].y}, df2{c[u].x, c[u].y}, ts);
+            if (over(ts)) {
+              cut = true;
+              break;
+            }
+          }
+        }
+        for (; i < L - 1 && !cut; ++i) {
+          const float2 g = __ldg(&Gt[i]);
+          const float2 c = chi_f[i * VPB + v];
+          ts = df_fma(df2{g.x, g.y}, df2{c.x, c.y}, ts);
+          cut = over(ts);
+        }
+        tau = df_to_double(ts);
+      } else {
+        const double* Gt = geom + (size_t)b * L * L + (size_t)t * L;
+        tau = 0.0;
+        for (int i = t; i < L - 1; ++i) {
+          tau = fma(__ldg(&Gt[i]), chi_s[i * VPB + v], tau);
+          if (__double_as_longlong(tau) > kBits10) break;  // tau > 10 (tau >= 0)
+        }
       }
       double tr;
       if (DF) tr = __double_as_longlong(tau) > kBits700 ? 0.0 : exp_tang(-tau, et.d);
@@ -322,6 +395,29 @@ __global__ void spectrum_output_kernel(DeviceModel dm, const double* __restrict_
   out[k] = emission ? f / dm.wl[k] / dm.wl[k] * 10000.0 : f;
 }
 
+// Level table (set-up): for every pressure-bracket entry (species, temperature
+// node, level) the log-p interpolation of the two table rows at that level,
+// x = t0 + (t1 - t0) w in FP64 as the reference does per evaluation
+// (OpacitySpecies::calcAbsorptionCrossSections src/transport_coeff/opacity_species.cpp:308-338),
+// converted to log2 units with a two-part log2(10) and stored as a double-float.
+constexpr double kLog2_10 = 3.321928094887362348, kLog2_10Tail = 1.661617516973592e-16;
+
+__global__ void level_table_kernel(const double* __restrict__ table64, const int* __restrict__ row0,
+                                   const int* __restrict__ row1, const double* __restrict__ w, long long n_lrows,
+                                   size_t N, float2* __restrict__ ltab) {
+  const size_t total = (size_t)n_lrows * N;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = idx / N, k = idx - r * N;
+    const double t0 = table64[(size_t)__ldg(&row0[r]) * N + k];
+    const double t1 = table64[(size_t)__ldg(&row1[r]) * N + k];
+    const double x = t0 + (t1 - t0) * __ldg(&w[r]);
+    const double p = x * kLog2_10;
+    const double err = fma(x, kLog2_10, -p) + x * kLog2_10Tail;
+    const float hi = (float)p;
+    ltab[idx] = make_float2(hi, (float)((p - (double)hi) + err));
+  }
+}
+
 // ------------------------------------------------------------------ host side
 template <typename T>
 static T* dev_upload(Model& m, const std::vector<T>& v) {
@@ -374,19 +470,34 @@ void upload_model(Model& m) {
   dm.log10p = dev_upload(m, m.log10p);
   m.d_table64 = dev_upload(m, m.table_host);
   dm.table64 = m.d_table64;
-  {
-    std::vector<float2> tdf(m.table_host.size());
-    for (size_t i = 0; i < tdf.size(); ++i) tdf[i] = split_df(m.table_host[i]);
-    dm.table_df = dev_upload(m, tdf);
-  }
   std::vector<double>().swap(m.table_host);
   dm.table_T = dev_upload(m, m.table_T);
   dm.pb_row0 = dev_upload(m, m.pb_row0);
   dm.pb_row1 = dev_upload(m, m.pb_row1);
   dm.pb_w = dev_upload(m, m.pb_w);
+  {
+    // level table: the parameter-independent log-p step of every stencil, built once on the device
+    m.n_lrows = (long long)m.pb_row0.size();
+    float2* lt = nullptr;
+    const size_t bytes = std::max<size_t>((size_t)m.n_lrows * N, 1) * sizeof(float2);
+    BGB_CUDA(cudaMalloc(&lt, bytes));
+    m.allocations.push_back(lt);
+    m.device_bytes += bytes;
+    if (m.n_lrows > 0) {
+      level_table_kernel<<<1184, 256>>>(dm.table64, dm.pb_row0, dm.pb_row1, dm.pb_w, m.n_lrows, N, lt);
+      BGB_CUDA(cudaGetLastError());
+      BGB_CUDA(cudaDeviceSynchronize());
+    }
+    dm.ltab = lt;
+  }
   std::vector<double> ray;
   for (int r : m.rayleigh_species) ray.insert(ray.end(), m.opac[r].rayleigh.begin(), m.opac[r].rayleigh.end());
   dm.rayleigh = dev_upload(m, ray);
+  {
+    std::vector<float2> rdf(ray.size());
+    for (size_t i = 0; i < ray.size(); ++i) rdf[i] = split_df(ray[i]);
+    dm.rayleigh_df = dev_upload(m, rdf);
+  }
   // observation operator rows in internal order, observations concatenated
   std::vector<int> k0, len, robs, rout, modp;
   std::vector<long long> off;
@@ -526,13 +637,14 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
       emission_kernel<false><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.lsdf, w.ev, w.spectrum, nullptr);
   } else {
     if (taps) throw Error(BEAR_ERR_UNSUPPORTED, "gradient of transmission models not available");
-    transmission_geometry_kernel<<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom);
+    if (m.precision == 1) transmission_geometry_kernel<false><<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom);
+    else transmission_geometry_kernel<true><<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom);
     // the launch shape selects the wavenumbers per block: 16, 32 (default) or 64, 4 threads each
     const int vpb = (rt == 16 || rt == 64) ? rt : 32;
     dim3 grid(batch, (dm.N + vpb - 1) / vpb);
-    const size_t sm = (size_t)L * vpb * sizeof(double);
-    if (sm > kTransmissionDynSmem) throw Error(BEAR_ERR_UNSUPPORTED, "too many levels for the transmission kernel");
     const bool df = m.precision != 1;
+    const size_t sm = (size_t)L * vpb * sizeof(double) + (df ? (size_t)L * dm.R * sizeof(float2) : 0);
+    if (sm > kTransmissionDynSmem) throw Error(BEAR_ERR_UNSUPPORTED, "too many levels for the transmission kernel");
     auto go = [&](auto kernel) {
       kernel<<<grid, kTPN * vpb, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.spectrum);
     };
@@ -581,20 +693,37 @@ void stage_times(Model& m, float* ms3) {
   for (int i = 0; i < 3; ++i) BGB_CUDA(cudaEventElapsedTime(&ms3[i], m.ev[i], m.ev[i + 1]));
 }
 
+// Distinct table rows the last batch's stencils read: rows of the level table
+// (2 per species and level, double-float path) or of the FP64 table (4 per
+// species and level, precision mode 1).
 long long stencil_rows(Model& m, int batch) {
   if (batch < 1 || batch > m.ws.capacity) throw Error(BEAR_ERR_SIZE, "batch exceeds the workspace");
   const size_t n = (size_t)batch * m.L * std::max(m.acfg.S, 1);
-  std::vector<LevelSpecies> h(n);
   BGB_CUDA(cudaDeviceSynchronize());
-  BGB_CUDA(cudaMemcpy(h.data(), m.ws.ls, n * sizeof(LevelSpecies), cudaMemcpyDeviceToHost));
-  std::vector<char> seen((size_t)m.n_rows, 0);
   long long count = 0;
-  for (const auto& e : h)
-    for (int r : e.row)
-      if (r >= 0 && r < m.n_rows && !seen[r]) {
-        seen[r] = 1;
-        ++count;
-      }
+  if (m.precision == 0) {
+    std::vector<LevelSpeciesDF> h(n);
+    BGB_CUDA(cudaMemcpy(h.data(), m.ws.lsdf, n * sizeof(LevelSpeciesDF), cudaMemcpyDeviceToHost));
+    std::vector<char> seen((size_t)m.n_lrows, 0);
+    for (const auto& e : h) {
+      if (e.lg2n_hi == kNoSpecies) continue;
+      for (int r : e.lrow)
+        if (r >= 0 && r < m.n_lrows && !seen[r]) {
+          seen[r] = 1;
+          ++count;
+        }
+    }
+  } else {
+    std::vector<LevelSpecies> h(n);
+    BGB_CUDA(cudaMemcpy(h.data(), m.ws.ls, n * sizeof(LevelSpecies), cudaMemcpyDeviceToHost));
+    std::vector<char> seen((size_t)m.n_rows, 0);
+    for (const auto& e : h)
+      for (int r : e.row)
+        if (r >= 0 && r < m.n_rows && !seen[r]) {
+          seen[r] = 1;
+          ++count;
+        }
+  }
   return count;
 }
 

@@ -86,11 +86,14 @@ struct __align__(16) LevelSpecies {
   double n;        // number density (cm^-3, or cm^-6 for CIA pairs)
 };
 
-// Double-float companions of LevelSpecies used by the FP32-pipe opacity path:
-// the same three interpolation weights and log2 of the number density
-// (lg2n_hi = kNoSpecies when the density is zero and the species is skipped).
+// Companion of LevelSpecies for the double-float opacity path: the two rows of
+// the level table (the log-p interpolation at this level is precomputed for every
+// temperature node) at the lower and upper temperature node, the temperature
+// weight and log2 of the number density (lg2n_hi = kNoSpecies when the density is
+// zero and the species is skipped), as double-floats.
 struct __align__(16) LevelSpeciesDF {
-  float wp_lo_hi, wp_lo_lo, wp_hi_hi, wp_hi_lo;
+  int lrow[2];
+  int pad[2];
   float wT_hi, wT_lo, lg2n_hi, lg2n_lo;
 };
 constexpr float kNoSpecies = -1.0e30f;
@@ -129,7 +132,9 @@ struct DeviceModel {
   const double* planck_c2;    // N: h nu c / k
   const float2* planck_c1_df; // N: 2 h c^2 nu^3 as double-float
   const float2* planck_c2l_df;// N: (h nu c / k) log2(e) as double-float
-  const float2* table_df;     // rows x N, log10 cross sections as double-float
+  const float2* ltab;         // level table: per (species, temperature node, level) the
+                              // log-p-interpolated cross section in log2 units, x N, double-float
+                              // (row = the pressure-bracket index sp_pb_off[s] + t L + l)
   // atmosphere constants
   const double* pressure;     // L (bar)
   const double* log10p;       // L
@@ -140,6 +145,7 @@ struct DeviceModel {
   const int* pb_row1;         // upper pressure node
   const double* pb_w;         // log-p weight
   const double* rayleigh;     // R x N
+  const float2* rayleigh_df;  // R x N as double-floats
   // observation operator: M rows, internal (descending-wavelength) order
   const int* row_k0;
   const int* row_len;
@@ -261,6 +267,7 @@ struct Model {
   std::vector<int> table_species;    // indices into opac with kind 0
   std::vector<int> rayleigh_species; // indices into opac with kind 1
   long long n_rows = 0;
+  long long n_lrows = 0;             // rows of the level table
   std::vector<double> table_host;    // n_rows x N (freed after upload)
   std::vector<double> W;             // concatenated operator weights
   int M = 0;

@@ -37,33 +37,29 @@ struct Kappa {
 // Sum over table species of 10^(bilinear log-p / T interpolation) * n at one
 // level and one wavenumber (OpacitySpecies::calcAbsorptionCrossSections
 // src/transport_coeff/opacity_species.cpp:277-345 and calcTransportCoefficients
-// :400-455), double-float arithmetic. term(s, t, t_wide, is_wide, lo, hi) is
-// called for every species with its term 10^x n (t as a double-float, or t_wide
-// in FP64 when outside the float range; zero for a skipped species) and the
-// p-interpolated log10 cross sections at the lower and upper temperature nodes.
+// :400-455), double-float arithmetic. The log-p step of the interpolation depends
+// only on the fixed pressure grid and is read from the level table ltab (log2
+// units), so one evaluation does the temperature step:
+// y = lo + (hi - lo) wT + log2(n), term = 2^y. term(s, t, t_wide, is_wide, lo, hi)
+// is called for every species with its term (t as a double-float, or t_wide in
+// FP64 when outside the float range; zero for a skipped species) and the level
+// table values at the lower and upper temperature nodes (log2 units).
 template <class F>
-__device__ __forceinline__ Kappa level_kappa_df_cb(const float2* __restrict__ tab, size_t N,
-                                                   const LevelSpecies* __restrict__ d,
+__device__ __forceinline__ Kappa level_kappa_df_cb(const float2* __restrict__ ltab, size_t N,
                                                    const LevelSpeciesDF* __restrict__ f, int S, int k,
                                                    const ExpTables& et, F&& term) {
   Kappa r = {{0.0f, 0.0f}, 0.0};
   for (int s = 0; s < S; ++s) {
-    const float4 fa = __ldg(reinterpret_cast<const float4*>(f + s));
-    const float4 fb = __ldg(reinterpret_cast<const float4*>(f + s) + 1);
+    const int4 rw = __ldg(reinterpret_cast<const int4*>(f + s));
+    const float4 fb = __ldg(reinterpret_cast<const float4*>(f + s) + 1);  // wT, log2 n
     if (fb.z == kNoSpecies) {  // zero number density: the species adds nothing
       term(s, df2{0.0f, 0.0f}, 0.0, false, df2{0.0f, 0.0f}, df2{0.0f, 0.0f});
       continue;
     }
-    const int4 rw = __ldg(reinterpret_cast<const int4*>(d + s));
-    const float2 t0 = __ldg(tab + (size_t)rw.x * N + k);
-    const float2 t1 = __ldg(tab + (size_t)rw.y * N + k);
-    const float2 t2 = __ldg(tab + (size_t)rw.z * N + k);
-    const float2 t3 = __ldg(tab + (size_t)rw.w * N + k);
-    const df2 lo = df_lerp(df2{t0.x, t0.y}, df2{t1.x, t1.y}, df2{fa.x, fa.y});
-    const df2 hi = df_lerp(df2{t2.x, t2.y}, df2{t3.x, t3.y}, df2{fa.z, fa.w});
-    const df2 x = df_lerp(lo, hi, df2{fb.x, fb.y});
-    // 10^x n = 2^(x log2(10) + log2(n))
-    const df2 y = df_add(df_mul(x, df2{kLog2_10Hi, kLog2_10Lo}), df2{fb.z, fb.w});
+    const float2 t0 = __ldg(ltab + (size_t)rw.x * N + k);
+    const float2 t1 = __ldg(ltab + (size_t)rw.y * N + k);
+    const df2 lo = {t0.x, t0.y}, hi = {t1.x, t1.y};
+    const df2 y = df_add(df_lerp(lo, hi, df2{fb.x, fb.y}), df2{fb.z, fb.w});
     int n;
     const df2 m = df_exp2(y, n, et.hi, et.lo);
     if (n > -100 && n < 100) {
@@ -83,19 +79,10 @@ struct NoTerm {
   __device__ __forceinline__ void operator()(int, df2, double, bool, df2, df2) const {}
 };
 
-__device__ __forceinline__ Kappa level_kappa_df(const float2* __restrict__ tab, size_t N,
-                                                const LevelSpecies* __restrict__ d,
+__device__ __forceinline__ Kappa level_kappa_df(const float2* __restrict__ ltab, size_t N,
                                                 const LevelSpeciesDF* __restrict__ f, int S, int k,
                                                 const ExpTables& et) {
-  return level_kappa_df_cb(tab, N, d, f, S, k, et, NoTerm{});
-}
-
-__device__ __forceinline__ double level_absorption_df(const float2* __restrict__ tab, size_t N,
-                                                      const LevelSpecies* __restrict__ d,
-                                                      const LevelSpeciesDF* __restrict__ f, int S, int k,
-                                                      const ExpTables& et) {
-  const Kappa r = level_kappa_df(tab, N, d, f, S, k, et);
-  return df_to_double(r.v) + r.wide;
+  return level_kappa_df_cb(ltab, N, f, S, k, et, NoTerm{});
 }
 
 // The same sum in FP64 with the CUDA math library (validation path);

@@ -391,9 +391,10 @@ def main():
     kern_ms = stages[1]
     rows = eng.stencil_row_count(B)
     N, M, L, S = eng.N, eng.M, spec.nb_levels, eng.table_species
-    # algorithmic bytes of one radiative-transfer launch: every distinct table row the
-    # batch's stencils touch, read once; the per-level stencil records; the spectrum write
-    alg_bytes = rows * N * 8 + B * L * S * 48 + B * N * 8
+    # algorithmic bytes of one radiative-transfer launch: every distinct level-table row the
+    # batch's stencils touch (8 B per point), read once; the 32-byte per-level stencil
+    # records; the spectrum write
+    alg_bytes = rows * N * 8 + B * L * S * 32 + B * N * 8
     peaks, peak_kind = measured_peaks()
     achieved_gbs = alg_bytes / (kern_ms * 1e-3) / 1e9
     fp64_peak = fp64_peak_tflops(torch, device)
