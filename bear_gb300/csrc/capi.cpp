@@ -250,6 +250,14 @@ int bear_model_stage_times(bear_model* h, float* ms3) {
   });
 }
 
+int bear_model_table_sharing(const bear_model* h, int* shared, size_t* table_bytes) {
+  return guarded([&] {
+    require_ready(h);
+    if (shared) *shared = h->m.tables_shared ? 1 : 0;
+    if (table_bytes) *table_bytes = bgb::table_bytes(h->m);
+  });
+}
+
 int bear_model_table_info(const bear_model* h, int* levels, int* table_species, int* rayleigh_species,
                           long long* table_rows) {
   return guarded([&] {

@@ -34,6 +34,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
 #include <string>
 
 #include "../../include/bear_gb300.h"
@@ -435,6 +438,110 @@ static float2 split_df(double v) {
   return make_float2(hi, (float)(v - (double)hi));
 }
 
+// ------------------------------------------------------------------ shared opacity tables
+struct TableSet {
+  int device = 0;
+  size_t bytes = 0;
+  std::vector<void*> ptrs;
+  double* table64 = nullptr;
+  float2* ltab = nullptr;
+  double* table_T = nullptr;
+  int* pb_row0 = nullptr;
+  int* pb_row1 = nullptr;
+  double* pb_w = nullptr;
+  ~TableSet() {
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(device);
+    cudaDeviceSynchronize();
+    for (void* p : ptrs) cudaFree(p);
+    cudaSetDevice(prev);
+  }
+  template <typename T>
+  T* upload(const std::vector<T>& v) {
+    T* p = nullptr;
+    const size_t n = std::max<size_t>(v.size(), 1) * sizeof(T);
+    BGB_CUDA(cudaMalloc(&p, n));
+    ptrs.push_back(p);
+    bytes += n;
+    if (!v.empty()) BGB_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return p;
+  }
+};
+
+namespace {
+
+std::mutex g_tables_mutex;
+std::map<std::string, std::weak_ptr<TableSet>> g_tables;
+
+void fnv1a(uint64_t& h, const void* data, size_t n) {
+  const unsigned char* c = static_cast<const unsigned char*>(data);
+  for (size_t i = 0; i < n; ++i) {
+    h ^= c[i];
+    h *= 1099511628211ull;
+  }
+}
+
+// Identity of a table set: device, table directory and species, spectral grid,
+// pressure grid and table shapes.
+std::string table_key(const Model& m) {
+  uint64_t h = 1469598103934665603ull;
+  fnv1a(h, m.xsec_path.data(), m.xsec_path.size());
+  for (const auto& c : m.opac_cfg) {
+    fnv1a(h, c.first.data(), c.first.size());
+    fnv1a(h, "|", 1);
+    fnv1a(h, c.second.data(), c.second.size());
+    fnv1a(h, ";", 1);
+  }
+  fnv1a(h, m.nu.data(), m.nu.size() * sizeof(double));
+  fnv1a(h, m.p.data(), m.p.size() * sizeof(double));
+  fnv1a(h, m.table_T.data(), m.table_T.size() * sizeof(double));
+  fnv1a(h, m.pb_row0.data(), m.pb_row0.size() * sizeof(int));
+  fnv1a(h, m.pb_row1.data(), m.pb_row1.size() * sizeof(int));
+  fnv1a(h, m.pb_w.data(), m.pb_w.size() * sizeof(double));
+  return std::to_string(m.device) + ":" + std::to_string(m.n_rows) + ":" + std::to_string(m.N) + ":" +
+         std::to_string(h);
+}
+
+}  // namespace
+
+// Finds or builds the device tables of the model (FP64 table, level table, brackets).
+static void attach_tables(Model& m) {
+  const std::string key = table_key(m);
+  std::lock_guard<std::mutex> lock(g_tables_mutex);
+  auto it = g_tables.find(key);
+  if (it != g_tables.end()) {
+    if (auto ts = it->second.lock()) {
+      m.tables = ts;
+      m.tables_shared = true;
+      return;
+    }
+  }
+  auto ts = std::make_shared<TableSet>();
+  ts->device = m.device;
+  const size_t N = m.N;
+  ts->table64 = ts->upload(m.table_host);
+  ts->table_T = ts->upload(m.table_T);
+  ts->pb_row0 = ts->upload(m.pb_row0);
+  ts->pb_row1 = ts->upload(m.pb_row1);
+  ts->pb_w = ts->upload(m.pb_w);
+  // level table: the parameter-independent log-p step of every stencil, built once on the device
+  const size_t bytes = std::max<size_t>((size_t)m.n_lrows * N, 1) * sizeof(float2);
+  BGB_CUDA(cudaMalloc(&ts->ltab, bytes));
+  ts->ptrs.push_back(ts->ltab);
+  ts->bytes += bytes;
+  if (m.n_lrows > 0) {
+    level_table_kernel<<<1184, 256>>>(ts->table64, ts->pb_row0, ts->pb_row1, ts->pb_w, m.n_lrows, N, ts->ltab);
+    BGB_CUDA(cudaGetLastError());
+    BGB_CUDA(cudaDeviceSynchronize());
+  }
+  g_tables[key] = ts;
+  m.tables = ts;
+  m.tables_shared = false;
+}
+
+size_t table_bytes(const Model& m) { return m.tables ? m.tables->bytes : 0; }
+
 void upload_model(Model& m) {
   BGB_CUDA(cudaSetDevice(m.device));
   const size_t N = m.N;
@@ -468,28 +575,18 @@ void upload_model(Model& m) {
   dm.planck_c2l_df = dev_upload(m, c2ldf);
   dm.pressure = dev_upload(m, m.p);
   dm.log10p = dev_upload(m, m.log10p);
-  m.d_table64 = dev_upload(m, m.table_host);
-  dm.table64 = m.d_table64;
+  m.n_lrows = (long long)m.pb_row0.size();
+  attach_tables(m);
   std::vector<double>().swap(m.table_host);
-  dm.table_T = dev_upload(m, m.table_T);
-  dm.pb_row0 = dev_upload(m, m.pb_row0);
-  dm.pb_row1 = dev_upload(m, m.pb_row1);
-  dm.pb_w = dev_upload(m, m.pb_w);
-  {
-    // level table: the parameter-independent log-p step of every stencil, built once on the device
-    m.n_lrows = (long long)m.pb_row0.size();
-    float2* lt = nullptr;
-    const size_t bytes = std::max<size_t>((size_t)m.n_lrows * N, 1) * sizeof(float2);
-    BGB_CUDA(cudaMalloc(&lt, bytes));
-    m.allocations.push_back(lt);
-    m.device_bytes += bytes;
-    if (m.n_lrows > 0) {
-      level_table_kernel<<<1184, 256>>>(dm.table64, dm.pb_row0, dm.pb_row1, dm.pb_w, m.n_lrows, N, lt);
-      BGB_CUDA(cudaGetLastError());
-      BGB_CUDA(cudaDeviceSynchronize());
-    }
-    dm.ltab = lt;
-  }
+  const TableSet& ts = *m.tables;
+  m.d_table64 = ts.table64;
+  dm.table64 = ts.table64;
+  dm.ltab = ts.ltab;
+  dm.table_T = ts.table_T;
+  dm.pb_row0 = ts.pb_row0;
+  dm.pb_row1 = ts.pb_row1;
+  dm.pb_w = ts.pb_w;
+  m.device_bytes += ts.bytes;
   std::vector<double> ray;
   for (int r : m.rayleigh_species) ray.insert(ray.end(), m.opac[r].rayleigh.begin(), m.opac[r].rayleigh.end());
   dm.rayleigh = dev_upload(m, ray);
@@ -737,6 +834,7 @@ void release_model(Model& m) {
   cudaDeviceSynchronize();
   free_workspace(m.ws);
   free_grad_workspace(m);
+  m.tables.reset();
   for (void* p : m.allocations) cudaFree(p);
   m.allocations.clear();
   for (auto& e : m.ev)

@@ -5,6 +5,7 @@
 #include <array>
 #include <cstddef>
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -241,6 +242,11 @@ struct ChemModule {
   int bg_sp = -1;
 };
 
+// Device copies of a model's opacity tables (FP64 table, level table, stencil
+// brackets). Models on the same device with the same table files, spectral grid
+// and pressure grid share one set (engine.cu keeps a registry).
+struct TableSet;
+
 struct Model {
   // configuration
   bool transmission = false;
@@ -289,6 +295,8 @@ struct Model {
   size_t device_bytes = 0;
   AtmosphereConfig* d_cfg = nullptr;
   double* d_table64 = nullptr;
+  std::shared_ptr<TableSet> tables;   // shared device tables
+  bool tables_shared = false;         // true when another model created them
   Workspace ws;
   GradWorkspace gws;
   size_t grad_budget = size_t(16) << 30;  // bytes of gradient work buffers per chunk
@@ -315,6 +323,7 @@ void release_model(Model& m);
 void launch_forward(Model& m, const double* params_dev, int batch, cudaStream_t stream,
                     bool want_loglike, uint8_t* neglect_dev, double* loglike_dev);
 void launch_spectrum_output(Model& m, double* out_dev, cudaStream_t stream);
+size_t table_bytes(const Model& m);  // device bytes of the model's (possibly shared) tables
 void stage_times(Model& m, float* ms3);
 // noalloc.cu
 void loglike_noalloc(Model& m, const double* params_dev, double* loglike_dev, uint8_t* neglect_dev,

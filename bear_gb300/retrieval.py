@@ -186,6 +186,12 @@ class Engine:
                                                  C.byref(best)))
         return best.value
 
+    def table_sharing(self) -> Tuple[bool, int]:
+        """(tables shared with another model on this device, their device bytes)."""
+        sh, nb = C.c_int(), C.c_size_t()
+        _lib.check(self._lib.bear_model_table_sharing(self._h, C.byref(sh), C.byref(nb)))
+        return bool(sh.value), int(nb.value)
+
     def set_gradient_memory(self, nbytes: int = 0) -> None:
         """Device memory the gradient's work buffers may use per chunk (0 = default)."""
         _lib.check(self._lib.bear_model_set_gradient_memory(self._h, int(nbytes)))

@@ -367,7 +367,7 @@ def observations(spec: WorkloadSpec, kind: Optional[str] = None) -> List[Observa
         if kind == "emission":
             layout = [("em_vis", 0.405, 2.5, 300, "spectroscopy"), ("em_ir", 2.5, 9.5, 150, "spectroscopy")]
         else:
-            layout = [("tr_vis", 0.4, 3.0, 300, "spectroscopy"), ("tr_ir", 3.0, 9.8, 150, "band-spectroscopy")]
+            layout = [("tr_vis", 0.4, 3.0, 300, "spectroscopy"), ("tr_ir", 3.0, 9.5, 150, "band-spectroscopy")]
         for name, a, b, n, typ in layout:
             if typ == "spectroscopy":
                 wl = np.geomspace(a, b, n)

@@ -44,13 +44,14 @@ WORKLOADS = {
     "emission_adjoint": ("emission_adjoint", "emission"),
     "emission_plain": ("emission_plain", "emission"),
     "transmission_plain": ("transmission_plain", "transmission"),
+    "joint_large": ("joint_large", "joint"),
 }
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=None, help="timed steps (default 20; 4 for joint_large)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--workload", default="emission_batched", choices=sorted(WORKLOADS))
@@ -204,16 +205,72 @@ def cpu_baseline(text, arrays, params, sample, threads, budget_s=12.0):
     return n / dt, dt, n
 
 
+
+def run_reference_joint(args, oracle, threads):
+    """Reference arm of the joint workload: the FP64 oracle of both models
+    (the same observation sets and grid as the engine arm)."""
+    from bear_gb300.joint import joint_observation_sets
+
+    spec = syn.CONFIGS["joint_large"]
+
+    def oracle_data(kind, text, obs):
+        om0 = oracle.OracleModel(text, [observation_arrays(o) for o in obs])
+        _, m, _ = om0.forward(syn.truth_parameters(spec, kind))
+        parts, off = [], 0
+        for o in obs:
+            parts.append(m[off:off + len(o.data)])
+            off += len(o.data)
+        syn.attach_data(obs, parts, kind, spec.seed)
+        return [observation_arrays(o) for o in obs]
+
+    parts = joint_parts(spec, oracle_data)
+    (te, oe), (tt, ot) = parts["emission"], parts["transmission"]
+    em, tr = joint_observation_sets(oe, ot)
+    ome, omt = oracle.OracleModel(te, em), oracle.OracleModel(tt, tr)
+    Pe = ome.P
+    B = args.batch or spec.batch
+    params = joint_params(spec, B, 0)
+    per_step = max(1, int(os.environ.get("BEAR_REF_EVALS_PER_STEP", "2")))
+    for i in range(args.warmup):
+        ome.loglike(params[i % B, :Pe])
+        omt.loglike(params[i % B, Pe:])
+    times, idx = [], 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        for _ in range(per_step):
+            ome.loglike(params[idx % B, :Pe])
+            omt.loglike(params[idx % B, Pe:])
+            idx += 1
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = args.steps * per_step / total
+    print(json.dumps({
+        "impl": "reference", "metric": "likelihood evals/s", "value": value, "unit": "evals/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded tables in the reference format)",
+        "config": {"workload": "joint_large", "batch": B, "levels": spec.nb_levels, "spectral_points": ome.N,
+                   "bins": ome.M // 2 + omt.M // 2, "evals_per_step": per_step},
+        "cpu_baseline": {"value": value, "unit": "evals/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps * per_step} sequential joint evaluations of the workload's live points"},
+        "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "host": platform.machine(),
+    }))
+    return 0
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    spec, kind, text, obs = build_case(args.workload)
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle
 
     threads = os.cpu_count() or 1
     oracle.set_threads(threads)
+    if args.workload == "joint_large":
+        return run_reference_joint(args, oracle, threads)
+    spec, kind, text, obs = build_case(args.workload)
     # observation data from the oracle itself (same recipe as the engine arm)
     arrays0 = [observation_arrays(o) for o in obs]
     om0 = oracle.OracleModel(text, arrays0)
@@ -256,10 +313,208 @@ def run_reference(args):
     return 0
 
 
+
+def joint_parts(spec, data_from):
+    """Config texts and observation arrays of the joint workload's two models, data
+    attached from ``data_from(kind, text, obs)`` (the model at the seeded truth)."""
+    root = syn.write_tables(spec, synth_dir())
+    out = {}
+    for kind in ("emission", "transmission"):
+        text = render_config(syn.global_config(spec, root, kind), syn.model_config(spec, kind))
+        obs = syn.observations(spec, kind)
+        out[kind] = (text, data_from(kind, text, obs))
+    return out
+
+
+def joint_params(spec, B, rank):
+    return np.concatenate([live_points(spec, "emission", B, rank), live_points(spec, "transmission", B, rank)], axis=1)
+
+
+def run_joint(args):
+    """Large joint workload: emission + transmission models on one spectral grid
+    with shared device tables, joint log L = log L_emission + log L_transmission."""
+    import torch
+
+    from bear_gb300.joint import JointBatchEvaluator, JointEngine
+
+    rank, world, local = dist_env()
+    device = local
+    torch.cuda.set_device(device)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", device))
+    spec = syn.CONFIGS["joint_large"]
+    parts = joint_parts(spec, lambda kind, text, obs: attach_engine_data(spec, kind, text, obs, device))
+    (te, oe), (tt, ot) = parts["emission"], parts["transmission"]
+    joint = JointEngine(te, oe, tt, ot, device=device)
+    B = args.batch or spec.batch
+    params_host = joint_params(spec, B, rank)
+    P = torch.tensor(params_host, dtype=torch.float64, device=device)
+    stream = torch.cuda.current_stream(device)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+    ev = JointBatchEvaluator(joint, P, autotune=True)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(device)
+
+    for _ in range(max(args.warmup, 3)):
+        ev()
+    barrier()
+    evs = []
+    with ClockSampler(device) as clocks:
+        for _ in range(args.steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ll, ng = ev()
+            b.record(stream)
+            evs.append((a, b))
+        barrier()
+    total_ms = sum(a.elapsed_time(b) for a, b in evs)
+    if dist is not None:
+        t = torch.tensor([total_ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = t.item()
+    value = world * B * args.steps / (total_ms * 1e-3)
+
+    # end to end: pinned host parameters in, joint log-likelihoods out
+    p_pin = torch.tensor(params_host, dtype=torch.float64).pin_memory()
+    ll_pin = torch.empty(B, dtype=torch.float64).pin_memory()
+    P2 = torch.empty_like(P)
+
+    def e2e_step():
+        P2.copy_(p_pin, non_blocking=True)
+        l, _ = ev(P2)
+        ll_pin.copy_(l, non_blocking=True)
+
+    e2e_step()
+    barrier()
+    e2e = []
+    for _ in range(args.steps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        e2e_step()
+        b.record(stream)
+        e2e.append((a, b))
+    barrier()
+    e2e_ms = sum(a.elapsed_time(b) for a, b in e2e)
+    e2e_value = world * B * args.steps / (e2e_ms * 1e-3)
+
+    # plain path: one host call per model per evaluation
+    n_plain = 6
+    for i in range(2):
+        joint.emission.loglike(params_host[i, :joint.Pe])
+        joint.transmission.loglike(params_host[i, joint.Pe:])
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    for i in range(n_plain):
+        joint.emission.loglike(params_host[i, :joint.Pe])
+        joint.transmission.loglike(params_host[i, joint.Pe:])
+    plain_s = (time.perf_counter() - t0) / n_plain
+
+    # gradient of the joint batch (both adjoints) when both models provide one
+    grad = None
+    try:
+        joint.grad_batch(P[:2])
+        torch.cuda.synchronize(device)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        flush.zero_()
+        a.record(stream)
+        joint.grad_batch(P)
+        b.record(stream)
+        barrier()
+        gms = a.elapsed_time(b)
+        grad = {"evals_per_s": B / (gms * 1e-3), "ms_per_batch": gms, "grad_over_forward": gms / (total_ms / args.steps),
+                "parameters": joint.P, "steps": 1}
+    except Exception as exc:  # the transmission adjoint may be unavailable
+        grad = {"unavailable": str(exc).splitlines()[0]}
+
+    # roofline of the two radiative-transfer kernels (CUDA events) and the FP64 roof
+    peaks, peak_kind = measured_peaks()
+    fp64_peak = fp64_peak_tflops(torch, device)
+    pe, pt = joint._split(P)
+    ll1 = torch.empty(B, dtype=torch.float64, device=device)
+    se = joint.emission.stage_times(pe.data_ptr(), B, ll1.data_ptr(), stream.cuda_stream, repeats=2)
+    rows_e = joint.emission.stencil_row_count(B)
+    st_ = joint.transmission.stage_times(pt.data_ptr(), B, ll1.data_ptr(), stream.cuda_stream, repeats=2)
+    rows_t = joint.transmission.stencil_row_count(B)
+    N, L, S = joint.N, spec.nb_levels, joint.emission.table_species
+    alg = (rows_e + rows_t) * N * 8 + 2 * B * L * S * 32 + 2 * B * N * 8
+    kern_ms = se[1] + st_[1]
+    achieved = alg / (kern_ms * 1e-3) / 1e9
+    em_ops = B * (L - 1) * N * (3 + 3 + 3 + 1 + 2 * (1 + 8 + 3 + 3))
+    shared, table_bytes = joint.transmission.table_sharing()
+    line = {
+        "metric": "likelihood evals/s", "value": value, "unit": "evals/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded tables in the reference's on-disk format)",
+        "config": {"workload": "joint_large", "batch_per_gpu": B, "global_batch": B * world, "levels": L,
+                   "spectral_points": N, "bins": joint.emission.M // 2 + joint.transmission.M // 2,
+                   "observations": joint.n_em_obs + joint.n_tr_obs, "table_species": S,
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "flushed between timed steps (512 MiB write)",
+                   "tables_shared": shared, "table_bytes": table_bytes},
+        "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": int(P.numel() * 8),
+                "d2h_bytes_per_step": int(B * 8)},
+        "plain_path": {"evals_per_s": 1.0 / plain_s, "ms_per_eval": plain_s * 1e3,
+                       "api": "bear_loglike per model (host params in, host log L out)"},
+        "batched_over_plain": value * plain_s,
+        "gpu_launches": 7 * args.steps,
+        "batched_path": {"api": "two bear_batch_graph_launch per step", "autotuned_rt_threads":
+                         [ev.em.rt_threads, ev.tr.rt_threads]},
+        "roofline": {"bound": "hbm", "kernel": "emission_kernel + transmission_kernel", "achieved": achieved,
+                     "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                     "peak_source": peak_kind, "kernel_ms": kern_ms, "algorithmic_bytes": alg,
+                     "distinct_table_rows": rows_e + rows_t},
+        "stage_ms": {"emission": {"atmosphere": se[0], "radiative_transfer": se[1], "observation_loglike": se[2]},
+                     "transmission": {"atmosphere": st_[0], "radiative_transfer": st_[1],
+                                      "observation_loglike": st_[2]}},
+        "fp64": {"bound": "fp64", "unit": "Gop/s", "peak": fp64_peak / 2 * 1e3, "dgemm_tflops_measured": fp64_peak,
+                 "emission_achieved": em_ops / (se[1] * 1e-3) / 1e9,
+                 "emission_frac": em_ops / (se[1] * 1e-3) / 1e9 / (fp64_peak / 2 * 1e3)},
+        "gradient": grad,
+    }
+    if rank == 0:
+        line["clocks"] = clocks.summary()
+        if not args.no_cpu_baseline:
+            sys.path.insert(0, os.path.join(REPO, "oracle"))
+            import oracle
+            from bear_gb300.joint import joint_observation_sets
+
+            threads = os.cpu_count() or 1
+            oracle.set_threads(threads)
+            em, tr = joint_observation_sets(oe, ot)
+            ome, omt = oracle.OracleModel(te, em), oracle.OracleModel(tt, tr)
+            ome.loglike(params_host[0, :joint.Pe])
+            n, t0 = 0, time.perf_counter()
+            while (args.cpu_sample and n < args.cpu_sample) or (not args.cpu_sample and time.perf_counter() - t0 < 12.0):
+                ome.loglike(params_host[n % B, :joint.Pe])
+                omt.loglike(params_host[n % B, joint.Pe:])
+                n += 1
+            dt = time.perf_counter() - t0
+            line["cpu_baseline"] = {"value": n / dt, "unit": "evals/s", "cores": threads, "kind": "port",
+                                    "sample": f"{n} sequential joint evaluations ({dt:.1f} s), FP64 C oracle with OpenMP"}
+        print(json.dumps(line))
+    ev.close()
+    joint.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse()
+    if args.steps is None:
+        args.steps = 4 if args.workload == "joint_large" else 20
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "joint_large":
+        return run_joint(args)
 
     import torch
 

@@ -101,8 +101,13 @@ int bear_model_info(const bear_model* m, int* nb_spectral_points, int* nb_obs_po
 int bear_model_wavenumbers(const bear_model* m, double* out);
 /* Observation::nbPoints of observation k. */
 int bear_model_observation_size(const bear_model* m, int k, int* n);
-/* Bytes of device memory held by the model (tables, operators, work buffers). */
+/* Bytes of device memory held by the model (tables, operators, work buffers;
+ * tables shared with other models are counted in each). */
 int bear_model_device_bytes(const bear_model* m, size_t* bytes);
+/* Whether the model's device opacity tables were created by another model on the
+ * same device (same table files, spectral grid and pressure grid) and are shared,
+ * and their size. No reference counterpart. */
+int bear_model_table_sharing(const bear_model* m, int* shared, size_t* table_bytes);
 void bear_model_destroy(bear_model* m);
 
 /* --------------------------------------------------------------- plain path
