@@ -42,6 +42,7 @@ EXPORTS = {
     "bear_model_set_precision": (C.c_int, [C.c_void_p, C.c_int]),
     "bear_model_set_launch": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "bear_model_set_gradient_memory": (C.c_int, [C.c_void_p, C.c_longlong]),
+    "bear_model_set_tau_cutoff": (C.c_int, [C.c_void_p, C.c_double]),
     "bear_model_table_sharing": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_size_t)]),
     "bear_model_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
                                       C.POINTER(C.c_int)]),

@@ -38,6 +38,7 @@ def _units():
     return [
         ("engine.cu", common_cu),
         ("adjoint.cu", common_cu),
+        ("adjoint_transmission.cu", common_cu),
         ("noalloc.cu", common_cu),
         # bit-faithful host-style arithmetic: no FMA contraction
         ("atmosphere.cu", common_cu + ["--fmad=false"]),

@@ -41,76 +41,12 @@
 #include <string>
 
 #include "../../include/bear_gb300.h"
+#include "adjoint_common.cuh"
 #include "level_physics.cuh"
 #include "model.h"
 #include "rt_common.cuh"
 
 namespace bgb {
-
-#define BGB_CUDA(x)                                                                         \
-  do {                                                                                      \
-    cudaError_t e_ = (x);                                                                   \
-    if (e_ != cudaSuccess)                                                                  \
-      throw Error(BEAR_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));         \
-  } while (0)
-
-constexpr int kAdjThreads = 128;  // threads (wavenumbers) per block of the adjoint kernel
-constexpr double kLn10 = 2.302585092994045684;
-
-// ------------------------------------------------------------------ accumulators
-// The per-level sinks are summed either as double-floats (FP32 pipe) or in FP64.
-__device__ __forceinline__ df2 acc_add(df2 a, df2 b) { return df_add(a, b); }
-__device__ __forceinline__ double acc_add(double a, double b) { return a + b; }
-__device__ __forceinline__ df2 acc_shfl_xor(df2 v, int o) {
-  return {__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
-}
-__device__ __forceinline__ double acc_shfl_xor(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
-__device__ __forceinline__ double acc_to_double(df2 v) { return df_to_double(v); }
-__device__ __forceinline__ double acc_to_double(double v) { return v; }
-
-template <bool DF>
-struct AccType {
-  typedef double type;
-  static __device__ __forceinline__ double from(double x) { return x; }
-  static __device__ __forceinline__ double zero() { return 0.0; }
-};
-template <>
-struct AccType<true> {
-  typedef df2 type;
-  static __device__ __forceinline__ df2 from(double x) { return df_from_double(x); }
-  static __device__ __forceinline__ df2 zero() { return df2{0.0f, 0.0f}; }
-};
-
-// Warp reduce-scatter of VP values (VP = 8, 16 or 32): each halving step keeps
-// half of the values, sends the other half to the partner lane and adds what
-// comes back, so the warp does VP - 1 additions per lane instead of 5 VP.
-// Afterwards lane j holds the warp total of value j / (32 / VP).
-template <int VP, class A>
-__device__ __forceinline__ A warp_reduce_scatter(A (&v)[VP], int lane) {
-#pragma unroll
-  for (int s = 0; s < 5; ++s) {
-    const int o = 16 >> s;
-    const int cnt = VP >> s;
-    if (cnt >= 2) {
-      const int h = cnt / 2;
-      const bool upper = (lane & o) != 0;
-#pragma unroll
-      for (int i = 0; i < h; ++i) {
-        const A send = upper ? v[i] : v[i + h];
-        const A keep = upper ? v[i + h] : v[i];
-        v[i] = acc_add(keep, acc_shfl_xor(send, o));
-      }
-    } else {
-      v[0] = acc_add(v[0], acc_shfl_xor(v[0], o));
-    }
-  }
-  return v[0];
-}
-
-__device__ __forceinline__ double warp_sum_d(double v) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
 
 // ------------------------------------------------------------------ likelihood adjoint
 // log L = sum_r w_r (-0.5 log(2 pi e_r) - 0.5 (d_r - s_r)^2 / e_r), e_r = sigma_r^2 + 10^b
@@ -190,7 +126,9 @@ __global__ void __launch_bounds__(256) obs_adjoint_kernel(DeviceModel dm, const 
     if (!neg && infl != 0.0) grad[(size_t)b * P + P - 1] += tot_inf * infl * kLn10;
     // normalise the seed of the spectral adjoint to O(1) so the double-float sinks
     // stay well inside the float range
-    const double unit = transmission ? 1.0 : ev[b].scaling * kPi * 1e-3;
+    // emission: dF/dI scale; transmission: d depth / dh times R_p^2 (so g_tau ~ wz / R_p)
+    const double unit = transmission ? 1e6 / (ev[b].star_radius * ev[b].star_radius) * ev[b].radius * ev[b].radius
+                                     : ev[b].scaling * kPi * 1e-3;
     const double mx = tot_max * unit;
     double nrm = 1.0, inv = 1.0;
     if (mx > 0.0 && isfinite(mx)) {
@@ -538,61 +476,6 @@ __global__ void __launch_bounds__(kAdjThreads, DF ? 6 : 4) emission_adjoint_kern
 }
 
 // ------------------------------------------------------------------ parameter tangents
-// Mixing ratios X_j = n_j / n_total after the chemistry modules (level independent
-// for isoprofile and background chemistry) and their derivative along chemistry
-// parameter tc (-1: none). IsoprofileChemistry::calcChemicalComposition
-// src/chemistry/isoprofile_chemistry.cpp:87-119, BackgroundChemistry
-// src/chemistry/background_chemistry.cpp:72-137, Chemistry::meanMolecularWeight
-// src/chemistry/chemistry.h:47-59.
-__device__ void chemistry_tangent(const AtmosphereConfig& c, const double* chem, int tc, double* X, double* dX,
-                                  double& mmw, double& dmmw) {
-  for (int j = 0; j < kSpeciesCount; ++j) {
-    X[j] = 0.0;
-    dX[j] = 0.0;
-  }
-  X[SP_TOTAL] = 1.0;
-  mmw = dmmw = 0.0;
-  int pidx = 0;
-  for (int m = 0; m < c.nchem; ++m) {
-    if (c.chem_kind[m] == 0) {
-      for (int j = 0; j < c.chem_nsp[m]; ++j) {
-        X[c.chem_sp[m][j]] = chem[pidx + j];
-        dX[c.chem_sp[m][j]] = (tc == pidx + j) ? 1.0 : 0.0;
-      }
-      if (!c.chem_na_free[m]) {
-        X[SP_Na] = X[SP_K] * 16.2181;
-        dX[SP_Na] = dX[SP_K] * 16.2181;
-      }
-      pidx += c.chem_nsp[m];
-    } else {
-      double bg = 1.0, dbg = 0.0;
-      for (int j = 1; j < kSpeciesCount; ++j) {
-        const bool other = c.chem_bg_h2he[m] ? (j != SP_H2 && j != SP_He) : (j != c.chem_bg_sp[m]);
-        if (other) {
-          bg -= X[j];
-          dbg -= dX[j];
-        }
-      }
-      if (bg < 0) bg = dbg = 0.0;
-      if (c.chem_bg_h2he[m]) {
-        const double f2 = kSolarH2 / (kSolarH2 + kSolarHe), fe = kSolarHe / (kSolarH2 + kSolarHe);
-        X[SP_H2] = bg * f2;
-        dX[SP_H2] = dbg * f2;
-        X[SP_He] = bg * fe;
-        dX[SP_He] = dbg * fe;
-      } else {
-        X[c.chem_bg_sp[m]] = bg;
-        dX[c.chem_bg_sp[m]] = dbg;
-      }
-    }
-    mmw = dmmw = 0.0;
-    for (int j = 1; j < kSpeciesCount; ++j) {
-      mmw += X[j] * kMolWeight[j];
-      dmmw += dX[j] * kMolWeight[j];
-    }
-  }
-}
-
 // One block per evaluation. sg[L][V] = the partial sums reduced over the tiles;
 // then thread th < P forms d log L / d param_th = sum over levels of the sinks
 // times the tangents of ln n_s, T, lev.dz and lev.cloud along param_th
@@ -732,6 +615,15 @@ void free_grad_workspace(Model& m) {
   cudaFree(g.gS);
   cudaFree(g.seed);
   cudaFree(g.partial);
+  cudaFree(g.tr_c);
+  cudaFree(g.tr_gt);
+  cudaFree(g.tr_A);
+  cudaFree(g.tr_z1);
+  cudaFree(g.tr_I);
+  cudaFree(g.tr_gc);
+  cudaFree(g.tr_gz);
+  cudaFree(g.tr_geo);
+  cudaFree(g.tr_rp);
   g = GradWorkspace{};
 }
 
@@ -771,9 +663,55 @@ void launch_emission_adjoint(const Model& m, dim3 grid, size_t smem, cudaStream_
 
 }  // namespace
 
+// adjoint_transmission.cu
+size_t transmission_grad_bytes_per_eval(const Model& m, int V);
+void alloc_transmission_grad(Model& m, int chunk, int V);
+void transmission_adjoint_chunk(Model& m, const double* params_chunk, int nb, cudaStream_t st, double* grad_chunk,
+                                int V);
+
+static void launch_gradient_transmission(Model& m, const double* params_dev, int batch, cudaStream_t st,
+                                         double* loglike_dev, double* grad_dev, uint8_t* neglect_dev) {
+  if (m.precision != 0) throw Error(BEAR_ERR_UNSUPPORTED, "the transmission gradient runs in precision mode 0");
+  if (m.var_g) throw Error(BEAR_ERR_UNSUPPORTED, "the transmission gradient does not support variable gravity");
+  const int S = m.acfg.S, R = m.acfg.R, L = m.L, P = m.acfg.nparam_total;
+  const int V = S + R + 3;
+  if (V > 32) throw Error(BEAR_ERR_UNSUPPORTED, "the gradient supports at most 29 table and Rayleigh species");
+  if (P > 128) throw Error(BEAR_ERR_UNSUPPORTED, "the gradient supports at most 128 parameters");
+  if (L > 32767) throw Error(BEAR_ERR_UNSUPPORTED, "too many levels");
+  const size_t S1 = std::max(S, 1), M = std::max(m.M, 1);
+  const size_t per_eval = transmission_grad_bytes_per_eval(m, V) + L * S1 * sizeof(float2) + M * 8 + 3 * 8;
+  const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)batch, m.grad_budget / per_eval));
+  BGB_CUDA(cudaSetDevice(m.device));
+  ensure_workspace(m, chunk);
+  GradWorkspace& g = m.gws;
+  if (chunk > g.capacity || g.tiles != -1) {
+    BGB_CUDA(cudaDeviceSynchronize());
+    free_grad_workspace(m);
+    BGB_CUDA(cudaMalloc(&g.taps.dwT, (size_t)chunk * L * S1 * sizeof(float2)));
+    BGB_CUDA(cudaMalloc(&g.gS, (size_t)chunk * M * sizeof(double)));
+    BGB_CUDA(cudaMalloc(&g.seed, (size_t)chunk * 3 * sizeof(double)));
+    alloc_transmission_grad(m, chunk, V);
+    g.capacity = chunk;
+    g.tiles = -1;  // transmission layout
+  }
+  const Workspace& w = m.ws;
+  for (int c0 = 0; c0 < batch; c0 += chunk) {
+    const int nb = std::min(chunk, batch - c0);
+    const double* pc = params_dev + (size_t)c0 * P;
+    double* gc = grad_dev + (size_t)c0 * P;
+    launch_forward_taps(m, pc, nb, st, neglect_dev ? neglect_dev + c0 : nullptr, loglike_dev + c0, g.taps);
+    obs_adjoint_kernel<<<nb, 256, 0, st>>>(m.dm, pc, P, w.ev, w.obs, g.gS, g.seed, gc, 1);
+    BGB_CUDA(cudaGetLastError());
+    transmission_adjoint_chunk(m, pc, nb, st, gc, V);
+  }
+}
+
 void launch_gradient(Model& m, const double* params_dev, int batch, cudaStream_t st, double* loglike_dev,
                      double* grad_dev, uint8_t* neglect_dev) {
-  if (m.transmission) throw Error(BEAR_ERR_UNSUPPORTED, "gradient of transmission models not available");
+  if (m.transmission) {
+    launch_gradient_transmission(m, params_dev, batch, st, loglike_dev, grad_dev, neglect_dev);
+    return;
+  }
   const int S = m.acfg.S, L = m.L, P = m.acfg.nparam_total;
   const int V = S + 3;
   if (V > 32) throw Error(BEAR_ERR_UNSUPPORTED, "the gradient supports at most 29 table species");

@@ -1,0 +1,554 @@
+// Adjoint (reverse-mode) gradient of the log-likelihood of transmission models.
+//
+// Forward model per evaluation and wavenumber (TransmissionModel
+// src/forward_model/transmission/transmission_spectrum.cpp:32-154):
+//   chi_l  = kappa_l + sum_r sigma_r n_{r,l} + cloud_l            extinction
+//   c_i    = chi_i + chi_{i+1}
+//   tau_t  = sum_{i=t}^{I_t} G[t][i] c_i                            (I_t: the tau > 10 cut-off)
+//   T_t    = exp(-tau_t),  h = sum_t (R + z_t)(1 - T_t) wz_t,  wz_t = z_{t+1} - z_{t-1} (z_1 - z_0 at t = 0)
+//   depth  = (h + R^2) / R_s^2 1e6
+// with G[t][i] = S_t(i+1) - S_t(i), S_t(j) = sqrt((R + z_j)^2 - (R + z_t)^2) (S_t(t) = 0).
+//
+// Kernel chain for one chunk of evaluations (after the forward pass, the
+// likelihood adjoint and the seed normaliser of adjoint.cu):
+//   tr_geometry_adjoint_kernel  per evaluation: P[t][j] = dG[t][j-1]/dz_j = (R + z_j)/S_t(j),
+//                               Q[t][i] = dG[t][i]/dz_t, U[t][i] = dG[t][i]/dR
+//   tr_adjoint_pass1            per wavenumber (forward layout): opacities recomputed, the
+//                               extinction column, tangent sums with their cut-off index,
+//                               g_tau_t = d log L / d tau_t, the tangent level's direct
+//                               altitude sink and d log L / dR; written per (level, wavenumber)
+//   tr_adjoint_pass2a           per (level j, wavenumber): d log L / d c_j = sum_t g_tau_t G[t][j]
+//                               and the geometry part of d log L / d z_j
+//   tr_adjoint_pass2b           per wavenumber, levels across warps: opacities recomputed for the
+//                               per-level sinks (log number densities of the table and Rayleigh
+//                               species, temperature, altitude, cloud extinction), warp
+//                               reduce-scatter, per-block partial sums
+//   tr_atmosphere_adjoint_kernel per evaluation: partial sums in a fixed order, forward-mode
+//                               tangents of the level physics (temperature, chemistry,
+//                               hydrostatic altitudes as prefix sums, cloud extinction),
+//                               planet and star radii
+// Double-float arithmetic on the FP32 pipe throughout except the transmission
+// exp(-tau), the effective-height terms and the per-evaluation tangents (FP64).
+// Discrete decisions (table brackets, cut-off index, cloud layers) are held fixed.
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+
+#include "adjoint_common.cuh"
+
+namespace bgb {
+
+constexpr int kTrVPB = 32;  // wavenumbers per block of the transmission adjoint kernels
+constexpr int kTrTPN = 4;   // threads per wavenumber
+
+// d log L / d depth_k normalised (the seed): sum_r W_rk gS_r times the evaluation's normaliser
+__device__ __forceinline__ double tr_seed(const DeviceModel& dm, const double* __restrict__ gS,
+                                          const double* __restrict__ seed, int b, int k) {
+  const double* g = gS + (size_t)b * dm.M;
+  double gF = 0.0;
+  const int e1 = __ldg(&dm.col_ptr[k + 1]);
+  for (int e = __ldg(&dm.col_ptr[k]); e < e1; ++e) gF = fma(__ldg(&dm.col_w[e]), g[__ldg(&dm.col_row[e])], gF);
+  return gF * seed[b * 3];
+}
+
+// ------------------------------------------------------------------ geometry derivatives
+__global__ void tr_geometry_adjoint_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
+                                           const EvalInfo* __restrict__ ev, float2* __restrict__ geo) {
+  const int b = blockIdx.x, L = dm.L;
+  const LevelInfo* lv = lev + (size_t)b * L;
+  const double R = ev[b].radius;
+  float2* P = geo + (size_t)b * 3 * L * L;
+  float2* Q = P + (size_t)L * L;
+  float2* U = Q + (size_t)L * L;
+  // 1 / S_t(j) for j > t (0 for j <= t or a degenerate zero path)
+  auto rS = [&](int t, int j) -> double {
+    if (j <= t) return 0.0;
+    const double bt = R + lv[t].z, a = R + lv[j].z;
+    const double s = sqrt(__dsub_rn(__dmul_rn(a, a), __dmul_rn(bt, bt)));
+    return s > 0.0 ? 1.0 / s : 0.0;
+  };
+  auto put = [](float2* p, double v) {
+    const df2 d = df_from_double(v);
+    *p = make_float2(d.hi, d.lo);
+  };
+  for (int idx = threadIdx.x; idx < L * L; idx += blockDim.x) {
+    const int t = idx / L, i = idx % L;
+    const double zt = lv[t].z;
+    put(P + idx, (R + lv[i].z) * rS(t, i));
+    double q = 0.0, u = 0.0;
+    if (i >= t && i < L - 1) {
+      const double r0 = rS(t, i), r1 = rS(t, i + 1);
+      q = (R + zt) * (r0 - r1);
+      u = (lv[i + 1].z - zt) * r1 - (lv[i].z - zt) * r0;
+    }
+    put(Q + idx, q);
+    put(U + idx, u);
+  }
+}
+
+// ------------------------------------------------------------------ pass 1
+struct TrArgs {
+  const LevelInfo* lev;
+  const LevelSpeciesDF* lsdf;
+  const double* ray_n;
+  const EvalInfo* ev;
+  const float2* geom;
+  const float2* geo;
+  const float2* dwT;
+  const double* gS;
+  const double* seed;
+  float2* c;
+  float2* gt;
+  float2* A;
+  float2* z1;
+  short* I;
+  float2* gc;
+  float2* gz;
+  double* rp;
+  double* partial;
+  int V;
+};
+
+// Same layout as transmission_kernel<true, 32>; dynamic shared memory: chi [L][32]
+// then the Rayleigh number densities [L][R] (double-floats).
+__global__ void __launch_bounds__(kTrTPN * kTrVPB) tr_adjoint_pass1(DeviceModel dm, TrArgs a) {
+  constexpr int VPB = kTrVPB, TPN = kTrTPN;
+  extern __shared__ double tr_smem[];
+  float2* chi_f = reinterpret_cast<float2*>(tr_smem);
+  __shared__ ExpTables et;
+  __shared__ double rp_part[TPN * VPB];
+  const int v = threadIdx.x % VPB, j = threadIdx.x / VPB;
+  const int b = blockIdx.x;
+  const int k = blockIdx.y * VPB + v;
+  const int L = dm.L, S = dm.S, R = dm.R;
+  const size_t N = dm.N;
+  const bool active = k < dm.N;
+  const LevelInfo* lv = a.lev + (size_t)b * L;
+  const LevelSpeciesDF* sf = a.lsdf + (size_t)b * L * S;
+  float2* rn_s = chi_f + (size_t)L * VPB;
+  load_exp_tables(et);
+  for (int idx = threadIdx.x; idx < L * R; idx += blockDim.x) {
+    const df2 d = df_from_double(__ldg(&a.ray_n[(size_t)b * L * R + idx]));
+    rn_s[idx] = make_float2(d.hi, d.lo);
+  }
+  __syncthreads();
+  if (active) {
+    for (int l = j; l < L; l += TPN) {
+      const Kappa kp = level_kappa_df(dm.ltab, N, sf + (size_t)l * S, S, k, et);
+      df2 x = kp.v;
+      if ((__double_as_longlong(kp.wide) << 1) != 0) x = df_add(x, df_from_double(kp.wide));
+      for (int r = 0; r < R; ++r) {
+        const float2 sr = __ldg(&dm.rayleigh_df[(size_t)r * N + k]);
+        const float2 nr = rn_s[l * R + r];
+        x = df_fma(df2{sr.x, sr.y}, df2{nr.x, nr.y}, x);
+      }
+      const float2 cl = __ldg(reinterpret_cast<const float2*>(&lv[l].cloud_hi));
+      x = df_add(x, df2{cl.x, cl.y});
+      chi_f[l * VPB + v] = make_float2(x.hi, x.lo);
+    }
+  }
+  __syncthreads();
+  if (active && j == 0) {
+    for (int i = 0; i < L - 1; ++i) {
+      const float2 c0 = chi_f[i * VPB + v], c1 = chi_f[(i + 1) * VPB + v];
+      const df2 s2 = df_add(df2{c0.x, c0.y}, df2{c1.x, c1.y});
+      chi_f[i * VPB + v] = make_float2(s2.hi, s2.lo);
+    }
+  }
+  __syncthreads();
+  const size_t col = (size_t)b * L * N + k;  // [b][l][k] element of level 0
+  double rp = 0.0;
+  if (active) {
+    for (int i = j; i < L - 1; i += TPN) a.c[col + (size_t)i * N] = chi_f[i * VPB + v];
+    const double Rp = a.ev[b].radius, Rs = a.ev[b].star_radius;
+    // g_h = d log L / dh (normalised)
+    const double gh = tr_seed(dm, a.gS, a.seed, b, k) * 1e6 / (Rs * Rs);
+    if (j == 0) rp += gh * 2.0 * Rp;  // the explicit R^2 in depth = (h + R^2) / R_s^2
+    const float2* G = a.geom + (size_t)b * L * L;
+    const float2* Qm = a.geo + (size_t)b * 3 * L * L + (size_t)L * L;
+    const float2* Um = Qm + (size_t)L * L;
+    for (int t = L - 2 - j; t >= 0; t -= TPN) {
+      const float2* Gt = G + (size_t)t * L;
+      const float2* Qt = Qm + (size_t)t * L;
+      const float2* Ut = Um + (size_t)t * L;
+      df2 ts = {0.0f, 0.0f}, qs = {0.0f, 0.0f}, us = {0.0f, 0.0f};
+      int last = L - 2;
+      for (int i = t; i < L - 1; ++i) {
+        const float2 g = __ldg(&Gt[i]), c = chi_f[i * VPB + v];
+        const float2 q = __ldg(&Qt[i]), u = __ldg(&Ut[i]);
+        const df2 cc = {c.x, c.y};
+        ts = df_fma(df2{g.x, g.y}, cc, ts);
+        qs = df_fma(df2{q.x, q.y}, cc, qs);
+        us = df_fma(df2{u.x, u.y}, cc, us);
+        if (ts.hi > dm.tau_cut_hi || (ts.hi == dm.tau_cut_hi && ts.lo > dm.tau_cut_lo)) {  // the forward's cut-off
+          last = i;
+          break;
+        }
+      }
+      const double tau = df_to_double(ts);
+      const double tr = __double_as_longlong(tau) > kBits700 ? 0.0 : exp_tang(-tau, et.d);
+      const double zt = __ldg(&lv[t].z);
+      const double wz = (__ldg(&lv[t + 1].z) - zt) + (t >= 1 ? zt - __ldg(&lv[t - 1].z) : 0.0);
+      const double gtau = gh * (Rp + zt) * wz * tr;  // d log L / d tau_t = -T_t d log L / dT_t
+      const double A = (Rp + zt) * (1.0 - tr);
+      const double z1 = gh * (1.0 - tr) * wz + gtau * df_to_double(qs);
+      rp += gh * (1.0 - tr) * wz + gtau * df_to_double(us);
+      const size_t at = col + (size_t)t * N;
+      const df2 dg = df_from_double(gtau), dA = df_from_double(A), d1 = df_from_double(z1);
+      a.gt[at] = make_float2(dg.hi, dg.lo);
+      a.A[at] = make_float2(dA.hi, dA.lo);
+      a.z1[at] = make_float2(d1.hi, d1.lo);
+      a.I[at] = (short)last;
+    }
+  }
+  // d log L / dR of the block, summed in a fixed order
+  rp_part[threadIdx.x] = rp;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int q = 0; q < TPN * VPB; ++q) s += rp_part[q];
+    a.rp[(size_t)b * gridDim.y + blockIdx.y] = s;
+  }
+}
+
+// ------------------------------------------------------------------ pass 2a
+// One thread per (level j, wavenumber): grid (evaluations, tiles of 128 wavenumbers, L).
+//   g_c_j  = sum_{t <= j <= I_t} g_tau_t G[t][j]                       (j <= L-2)
+//   g_z_j  = sum_{t < j} g_tau_t P[t][j] (c_{j-1} [j-1 <= I_t] - c_j [j <= I_t])
+//          + z1_j + g_h (A_{j-1} - A_{j+1}) (- A_0 at j = 0)           (wz_t = z_{t+1} - z_{t-1})
+__global__ void __launch_bounds__(128) tr_adjoint_pass2a(DeviceModel dm, TrArgs a) {
+  const int b = blockIdx.x, j = blockIdx.z;
+  const int k = blockIdx.y * blockDim.x + threadIdx.x;
+  if (k >= dm.N) return;
+  const int L = dm.L;
+  const size_t N = dm.N;
+  const size_t col = (size_t)b * L * N + k;
+  const float2* G = a.geom + (size_t)b * L * L;
+  const float2* P = a.geo + (size_t)b * 3 * L * L;
+  const df2 z = {0.0f, 0.0f};
+  df2 cj1 = z, cj = z;
+  if (j >= 1) {
+    const float2 v = a.c[col + (size_t)(j - 1) * N];
+    cj1 = df2{v.x, v.y};
+  }
+  if (j <= L - 2) {
+    const float2 v = a.c[col + (size_t)j * N];
+    cj = df2{v.x, v.y};
+  }
+  df2 gc = z, gzp = z;
+  const int tmax = min(j, L - 2);
+  for (int t = 0; t <= tmax; ++t) {
+    const int I = a.I[col + (size_t)t * N];
+    if (I < j - 1) continue;  // the ray of tangent level t stops below level j
+    const float2 gv = a.gt[col + (size_t)t * N];
+    const df2 gtau = {gv.x, gv.y};
+    const bool in_j = I >= j && j <= L - 2;
+    if (in_j) {
+      const float2 g = __ldg(&G[(size_t)t * L + j]);
+      gc = df_fma(gtau, df2{g.x, g.y}, gc);
+    }
+    if (t < j) {
+      const float2 p = __ldg(&P[(size_t)t * L + j]);
+      const df2 d = in_j ? df_sub(cj1, cj) : cj1;  // j - 1 <= I_t holds here
+      gzp = df_fma(df_mul(gtau, df2{p.x, p.y}), d, gzp);
+    }
+  }
+  // direct altitude terms of the effective height
+  const double Rs = a.ev[b].star_radius;
+  const double gh = tr_seed(dm, a.gS, a.seed, b, k) * 1e6 / (Rs * Rs);
+  auto ld = [&](const float2* arr, int t) {
+    const float2 v = arr[col + (size_t)t * N];
+    return df_to_double(df2{v.x, v.y});
+  };
+  double direct = 0.0;
+  if (j <= L - 2) direct += ld(a.z1, j);
+  if (j >= 1) direct += gh * ld(a.A, j - 1);
+  if (j + 1 <= L - 2) direct -= gh * ld(a.A, j + 1);
+  if (j == 0) direct -= gh * ld(a.A, 0);
+  const df2 gzt = df_add(gzp, df_from_double(direct));
+  a.gc[col + (size_t)j * N] = make_float2(gc.hi, gc.lo);
+  a.gz[col + (size_t)j * N] = make_float2(gzt.hi, gzt.lo);
+}
+
+// ------------------------------------------------------------------ pass 2b
+// Block: 32 wavenumbers (lanes) x 4 warps; warp w takes levels w, w+4, ...
+// Dynamic shared memory: per-species terms float2 [S][128] then double [S][128].
+// partial[b][l][v][tile]: v = 0..S-1 d log L / d ln n_s (table species),
+// S..S+R-1 d log L / d ln n_r (Rayleigh species), S+R temperature, S+R+1 z_l,
+// S+R+2 cloud extinction of level l (all times the evaluation's seed normaliser).
+template <int VP>
+__global__ void __launch_bounds__(kTrTPN * kTrVPB) tr_adjoint_pass2b(DeviceModel dm, TrArgs a) {
+  constexpr int G = 32 / VP;
+  __shared__ ExpTables et;
+  extern __shared__ __align__(16) unsigned char tr2_smem[];
+  const int S = dm.S, R = dm.R, L = dm.L;
+  float2* tdf = reinterpret_cast<float2*>(tr2_smem);
+  double* twd = reinterpret_cast<double*>(tr2_smem + (size_t)S * blockDim.x * sizeof(float2));
+  load_exp_tables(et);
+  __syncthreads();
+  const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int kk = blockIdx.y * 32 + lane;
+  const bool active = kk < dm.N;
+  const int k = active ? kk : dm.N - 1;  // idle lanes repeat the last wavenumber with zero sinks
+  const size_t N = dm.N;
+  const size_t col = (size_t)b * L * N + k;
+  const LevelSpeciesDF* sf = a.lsdf + (size_t)b * L * S;
+  const float2* dw = a.dwT + (size_t)b * L * S;
+  float2* td = tdf + tid;
+  double* tw = twd + tid;
+  for (int l = warp; l < L; l += blockDim.x / 32) {
+    // d log L / d chi_l (chi_l enters c_l and c_{l-1})
+    df2 gx = {0.0f, 0.0f};
+    if (active) {
+      if (l <= L - 2) {
+        const float2 v = a.gc[col + (size_t)l * N];
+        gx = df2{v.x, v.y};
+      }
+      if (l >= 1) {
+        const float2 v = a.gc[col + (size_t)(l - 1) * N];
+        gx = df_add(gx, df2{v.x, v.y});
+      }
+    }
+    df2 gzl = {0.0f, 0.0f};
+    if (active) {
+      const float2 v = a.gz[col + (size_t)l * N];
+      gzl = df2{v.x, v.y};
+    }
+    // opacity terms and their temperature slope (level-table values are log2 units)
+    df2 dk = {0.0f, 0.0f};
+    double dkw = 0.0;
+    bool wide = false;
+    const float2* dwl = dw + (size_t)l * S;
+    level_kappa_df_cb(dm.ltab, N, sf + (size_t)l * S, S, k, et,
+                      [&](int s, df2 t, double t_w, bool is_wide, df2 lo, df2 hi) {
+                        const float2 d = __ldg(dwl + s);
+                        td[(size_t)s * blockDim.x] = make_float2(t.hi, t.lo);
+                        tw[(size_t)s * blockDim.x] = t_w;
+                        if (d.x != 0.0f) {
+                          const df2 slope = df_mul(df_sub(hi, lo), df2{d.x, d.y});
+                          if (is_wide) dkw += t_w * df_to_double(slope);
+                          else dk = df_add(dk, df_mul(t, slope));
+                        }
+                        wide = wide || is_wide;
+                      });
+    df2 gT = df_mul(gx, df_mul(dk, df2{kLn2Hi, kLn2Lo}));
+    if (wide) gT = df_add(gT, df_from_double(df_to_double(gx) * dkw * 0.693147180559945309));
+    const double* rn = a.ray_n + ((size_t)b * L + l) * R;
+    df2 v[VP];
+#pragma unroll
+    for (int q = 0; q < VP; ++q) {
+      df2 x = {0.0f, 0.0f};
+      if (q < S) {
+        const float2 t = td[(size_t)q * blockDim.x];
+        x = df_mul(gx, df2{t.x, t.y});
+        if (wide) x = df_add(x, df_from_double(df_to_double(gx) * tw[(size_t)q * blockDim.x]));
+      } else if (q < S + R) {
+        const float2 sr = __ldg(&dm.rayleigh_df[(size_t)(q - S) * N + k]);
+        x = df_mul(gx, df_mul(df2{sr.x, sr.y}, df_from_double(__ldg(&rn[q - S]))));
+      } else if (q == S + R) {
+        x = gT;
+      } else if (q == S + R + 1) {
+        x = gzl;
+      } else if (q == S + R + 2) {
+        x = gx;
+      }
+      v[q] = x;
+    }
+    const df2 r = warp_reduce_scatter<VP>(v, lane);
+    const int idx = lane / G;
+    if (lane % G == 0 && idx < a.V)
+      a.partial[(((size_t)b * L + l) * a.V + idx) * gridDim.y + blockIdx.y] = df_to_double(r);
+  }
+}
+
+// ------------------------------------------------------------------ parameter tangents
+// One block per evaluation. sg[L][V] = the partial sums reduced over the tiles; then
+// thread th < P forms d log L / d param_th = sum over levels of the sinks times the
+// tangents of ln n (table and Rayleigh species), T, z_l and the cloud extinction
+// chi_cloud,l = tau_layer(l-1) / (z_l - z_{l-1}) (CloudModel::convertOpticalDepth
+// src/cloud_model/cloud_model.h:67-88), plus the planet radius (d log L / dR from
+// pass 1) and the stellar radius (depth ~ 1 / R_s^2: -2 / R_s sum_k g_k depth_k).
+// TransmissionModel::calcAtmosphereStructure src/forward_model/transmission/transmission.cpp:150-194,
+// Atmosphere::calcAltitude src/forward_model/atmosphere/atmosphere.cpp:288-307.
+__global__ void __launch_bounds__(128) tr_atmosphere_adjoint_kernel(
+    DeviceModel dm, const double* __restrict__ params, int P, const LevelInfo* __restrict__ lev,
+    const EvalInfo* __restrict__ ev, const double* __restrict__ partial, int V, int tiles,
+    const double* __restrict__ rp, int rp_tiles, const double* __restrict__ seed, double* __restrict__ grad) {
+  extern __shared__ double sg[];
+  __shared__ double s_rp;
+  const AtmosphereConfig& c = *dm.cfg;
+  const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  const int L = c.L, S = c.S, R = c.R;
+  if (ev[b].neglect) return;
+  const double inv = seed[b * 3 + 1];
+  for (int idx = warp; idx < L * V; idx += nw) {
+    const double* p = partial + ((size_t)b * L * V + idx) * tiles;
+    double s = 0.0;
+    for (int q = lane; q < tiles; q += 32) s += p[q];
+    s = warp_sum_d(s);
+    if (lane == 0) sg[idx] = s * inv;
+  }
+  if (warp == 0) {
+    double s = 0.0;
+    for (int q = lane; q < rp_tiles; q += 32) s += rp[(size_t)b * rp_tiles + q];
+    s = warp_sum_d(s);
+    if (lane == 0) s_rp = s * inv;
+  }
+  __syncthreads();
+  if (tid >= P) return;
+  const int th = tid;
+  const double* par = params + (size_t)b * P;
+  const double* gen = par;
+  const int ng = c.nparam_general, nc = c.nparam_chem, nt = c.nparam_temp;
+  const double* chem = par + ng;
+  const double* temp = chem + nc;
+  const double* cloud = temp + nt;
+  double X[kSpeciesCount], dX[kSpeciesCount], mmw, dmmw;
+  chemistry_tangent(c, chem, (th >= ng && th < ng + nc) ? th - ng : -1, X, dX, mmw, dmmw);
+  if (c.fit_mmw) {  // mean molecular weight as a free parameter (general parameter 3)
+    mmw = gen[3];
+    dmmw = th == 3 ? 1.0 : 0.0;
+  }
+  const int tm = th - ng - nc;
+  const bool temp_theta = tm >= 0 && tm < nt;
+  double ddof[kMaxPolyDof];
+  if (temp_theta && c.temp_poly) {
+    for (int i = 0; i < c.pp_ndof; ++i) {
+      double v = 0.0;
+      if (i >= tm) {
+        v = 1.0;
+        for (int q = 0; q <= i; ++q)
+          if (q != tm) v *= temp[q];
+      }
+      ddof[i] = v;
+    }
+  }
+  const double g = pow(10.0, gen[0]);
+  const double dlng = th == 0 ? kLn10 : 0.0;
+  const int ci = ng + nc + nt;
+  const EvalInfo e = ev[b];
+  double cloud_d = 0.0;
+  if (c.cloud && th == ci && cloud[0] >= 0)
+    cloud_d = 1.0 / (double)((unsigned)e.cloud_top - (unsigned)e.cloud_bottom);
+  auto in_cloud = [&](int layer) {
+    return (unsigned)layer <= (unsigned)e.cloud_top && (unsigned)layer > (unsigned)e.cloud_bottom && layer < L - 1;
+  };
+  // per species: d ln n = sum_j dX_j / X_j - (1 + partners) d ln T
+  double dlnX[kMaxTableSpecies];
+  int np[kMaxTableSpecies];
+  for (int s = 0; s < S; ++s) {
+    const int js[3] = {c.sp_index[s], c.sp_partner[s][0], c.sp_partner[s][1]};
+    double v = 0.0;
+    int n = 0;
+    bool zero = false;
+    for (int u = 0; u < 3; ++u) {
+      if (js[u] < 0) continue;
+      ++n;
+      if (X[js[u]] == 0.0) zero = true;
+      else v += dX[js[u]] / X[js[u]];
+    }
+    dlnX[s] = v;
+    np[s] = zero ? -1 : n;
+  }
+  double acc = 0.0, u_prev = 0.0, du_prev = 0.0, dz_prev = 0.0, dz = 0.0;
+  for (int l = 0; l < L; ++l) {
+    const LevelInfo li = lev[(size_t)b * L + l];
+    double dT = 0.0;
+    if (temp_theta) dT = c.temp_poly ? poly_value(c, ddof, dm.log10p[l]) : (tm == 0 ? 1.0 : 0.0);
+    const double dlnT = dT / li.T;
+    const double* sgl = sg + (size_t)l * V;
+    for (int s = 0; s < S; ++s)
+      if (np[s] >= 0) acc = fma(sgl[s], dlnX[s] - np[s] * dlnT, acc);
+    for (int r = 0; r < R; ++r) {
+      const int jr = c.ray_index[r];
+      if (X[jr] != 0.0) acc = fma(sgl[S + r], dX[jr] / X[jr] - dlnT, acc);
+    }
+    acc = fma(sgl[S + R], dT, acc);
+    // z_l = z_{l-1} + Delta_l, Delta_l = 0.5 (p_{l-1} - p_l) 1e6 (u_l + u_{l-1}) / g, u = R T / (mmw p 1e6)
+    const double u = kGasConst * li.T / (mmw * dm.pressure[l] * 1e6);
+    const double du = u * (dlnT - dmmw / mmw);
+    dz_prev = dz;
+    if (l >= 1) {
+      const double pf = 0.5 * (dm.pressure[l - 1] * 1e6 - dm.pressure[l] * 1e6) / g;
+      dz += pf * ((du + du_prev) - (u + u_prev) * dlng);
+    }
+    u_prev = u;
+    du_prev = du;
+    acc = fma(sgl[S + R + 1], dz, acc);
+    // cloud extinction tau_layer(l-1) / (z_l - z_{l-1})
+    if (c.cloud && l >= 1 && in_cloud(l - 1)) {
+      const double zl1 = lev[(size_t)b * L + l - 1].z;
+      const double h = li.z - zl1;
+      double d = -li.cloud * (dz - dz_prev) / h;
+      if (cloud_d != 0.0 && in_cloud(l - 1)) d += cloud_d / h;
+      acc = fma(sgl[S + R + 2], d, acc);
+    }
+  }
+  if (th == 1) acc += s_rp;                                      // planet radius
+  if (th == 2) acc += -2.0 / e.star_radius * seed[b * 3 + 2];    // stellar radius
+  grad[(size_t)b * P + th] += acc;
+}
+
+// ------------------------------------------------------------------ host side
+size_t transmission_grad_bytes_per_eval(const Model& m, int V) {
+  const size_t L = m.L, N = m.N;
+  const size_t tiles2 = (N + 31) / 32, tiles1 = (N + kTrVPB - 1) / kTrVPB;
+  return L * N * (6 * sizeof(float2) + sizeof(short)) + 3 * L * L * sizeof(float2) + L * (size_t)V * tiles2 * 8 +
+         tiles1 * 8;
+}
+
+void alloc_transmission_grad(Model& m, int chunk, int V) {
+  GradWorkspace& g = m.gws;
+  const size_t B = chunk, L = m.L, N = m.N;
+  const size_t n = B * L * N;
+  BGB_CUDA(cudaMalloc(&g.tr_c, n * sizeof(float2)));
+  BGB_CUDA(cudaMalloc(&g.tr_gt, n * sizeof(float2)));
+  BGB_CUDA(cudaMalloc(&g.tr_A, n * sizeof(float2)));
+  BGB_CUDA(cudaMalloc(&g.tr_z1, n * sizeof(float2)));
+  BGB_CUDA(cudaMalloc(&g.tr_I, n * sizeof(short)));
+  BGB_CUDA(cudaMalloc(&g.tr_gc, n * sizeof(float2)));
+  BGB_CUDA(cudaMalloc(&g.tr_gz, n * sizeof(float2)));
+  BGB_CUDA(cudaMalloc(&g.tr_geo, B * 3 * L * L * sizeof(float2)));
+  BGB_CUDA(cudaMalloc(&g.tr_rp, B * ((N + kTrVPB - 1) / kTrVPB) * sizeof(double)));
+  BGB_CUDA(cudaMalloc(&g.partial, B * L * (size_t)V * ((N + 31) / 32) * sizeof(double)));
+}
+
+void transmission_adjoint_chunk(Model& m, const double* params_chunk, int nb, cudaStream_t st, double* grad_chunk,
+                                int V) {
+  const DeviceModel& dm = m.dm;
+  const Workspace& w = m.ws;
+  const GradWorkspace& g = m.gws;
+  const int L = m.L, S = m.acfg.S, R = m.acfg.R, P = m.acfg.nparam_total;
+  const size_t N = m.N;
+  const int tiles1 = (int)((N + kTrVPB - 1) / kTrVPB), tiles2 = (int)((N + 31) / 32);
+  TrArgs a{w.lev, w.lsdf, w.ray_n, w.ev, reinterpret_cast<const float2*>(w.geom), g.tr_geo, g.taps.dwT, g.gS,
+           g.seed, g.tr_c, g.tr_gt, g.tr_A, g.tr_z1, g.tr_I, g.tr_gc, g.tr_gz, g.tr_rp, g.partial, V};
+  tr_geometry_adjoint_kernel<<<nb, 256, 0, st>>>(dm, w.lev, w.ev, g.tr_geo);
+  BGB_CUDA(cudaGetLastError());
+  const size_t sm1 = (size_t)L * kTrVPB * sizeof(float2) + (size_t)L * R * sizeof(float2);
+  if (sm1 > 48 * 1024)
+    BGB_CUDA(cudaFuncSetAttribute(tr_adjoint_pass1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1));
+  tr_adjoint_pass1<<<dim3(nb, tiles1), kTrTPN * kTrVPB, sm1, st>>>(dm, a);
+  BGB_CUDA(cudaGetLastError());
+  tr_adjoint_pass2a<<<dim3(nb, (unsigned)((N + 127) / 128), L), 128, 0, st>>>(dm, a);
+  BGB_CUDA(cudaGetLastError());
+  const size_t sm2 = (size_t)S * kTrTPN * kTrVPB * (sizeof(float2) + sizeof(double));
+  const int VP = V <= 8 ? 8 : V <= 16 ? 16 : 32;
+  auto go2 = [&](auto kernel) {
+    if (sm2 > 48 * 1024) BGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));
+    kernel<<<dim3(nb, tiles2), kTrTPN * kTrVPB, sm2, st>>>(dm, a);
+  };
+  if (VP == 8) go2(tr_adjoint_pass2b<8>);
+  else if (VP == 16) go2(tr_adjoint_pass2b<16>);
+  else go2(tr_adjoint_pass2b<32>);
+  BGB_CUDA(cudaGetLastError());
+  const size_t sma = (size_t)L * V * sizeof(double);
+  if (sma > 48 * 1024)
+    BGB_CUDA(cudaFuncSetAttribute(tr_atmosphere_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sma));
+  tr_atmosphere_adjoint_kernel<<<nb, 128, sma, st>>>(dm, params_chunk, P, w.lev, w.ev, g.partial, V, tiles2, g.tr_rp,
+                                                     tiles1, g.seed, grad_chunk);
+  BGB_CUDA(cudaGetLastError());
+}
+
+}  // namespace bgb

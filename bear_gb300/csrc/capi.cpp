@@ -216,6 +216,14 @@ int bear_model_set_precision(bear_model* h, int mode) {
   });
 }
 
+int bear_model_set_tau_cutoff(bear_model* h, double tau) {
+  return guarded([&] {
+    require_ready(h);
+    if (!(tau > 0)) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "the cut-off must be positive (inf: none)");
+    bgb::set_tau_cutoff(h->m, tau);
+  });
+}
+
 int bear_model_set_gradient_memory(bear_model* h, long long bytes) {
   return guarded([&] {
     if (!h) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null model");

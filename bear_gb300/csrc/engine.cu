@@ -280,7 +280,8 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
       if (DF) {
         const float2* Gt = reinterpret_cast<const float2*>(geom) + (size_t)b * L * L + (size_t)t * L;
         df2 ts = {0.0f, 0.0f};
-        auto over = [](df2 x) { return x.hi > 10.0f || (x.hi == 10.0f && x.lo > 0.0f); };  // tau > 10
+        const float ch = dm.tau_cut_hi, cl = dm.tau_cut_lo;
+        auto over = [ch, cl](df2 x) { return x.hi > ch || (x.hi == ch && x.lo > cl); };  // tau > cut-off
         int i = t;
         bool cut = false;
         // four terms per iteration with their loads issued together (same sum, same break)
@@ -312,7 +313,7 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
         tau = 0.0;
         for (int i = t; i < L - 1; ++i) {
           tau = fma(__ldg(&Gt[i]), chi_s[i * VPB + v], tau);
-          if (__double_as_longlong(tau) > kBits10) break;  // tau > 10 (tau >= 0)
+          if (__double_as_longlong(tau) > dm.tau_cut_bits) break;  // tau > cut-off (tau >= 0)
         }
       }
       double tr;
@@ -542,6 +543,15 @@ static void attach_tables(Model& m) {
 
 size_t table_bytes(const Model& m) { return m.tables ? m.tables->bytes : 0; }
 
+void set_tau_cutoff(Model& m, double tau) {
+  long long bits;
+  std::memcpy(&bits, &tau, sizeof bits);
+  m.dm.tau_cut_bits = bits;
+  const float hi = (float)tau;
+  m.dm.tau_cut_hi = hi;
+  m.dm.tau_cut_lo = std::isinf(tau) ? 0.0f : (float)(tau - (double)hi);
+}
+
 void upload_model(Model& m) {
   BGB_CUDA(cudaSetDevice(m.device));
   const size_t N = m.N;
@@ -553,6 +563,7 @@ void upload_model(Model& m) {
   dm.M = m.M;
   dm.P = m.acfg.nparam_total;
   dm.nobs = (int)m.obs.size();
+  set_tau_cutoff(m, 10.0);  // TransmissionModel::tangentOpticalDepth src/forward_model/transmission/transmission_spectrum.cpp:136-137
   // (h nu c / k) log2(e) with log2(e) as a two-part constant
   const double log2e_hi = 1.4426950408889634, log2e_lo = 2.0355273740931033e-17;
   std::vector<double> c1(N), c2(N);
@@ -733,7 +744,6 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
     else
       emission_kernel<false><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.lsdf, w.ev, w.spectrum, nullptr);
   } else {
-    if (taps) throw Error(BEAR_ERR_UNSUPPORTED, "gradient of transmission models not available");
     if (m.precision == 1) transmission_geometry_kernel<false><<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom);
     else transmission_geometry_kernel<true><<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom);
     // the launch shape selects the wavenumbers per block: 16, 32 (default) or 64, 4 threads each

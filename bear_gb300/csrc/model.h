@@ -160,6 +160,10 @@ struct DeviceModel {
   const double* row_logterm;  // -0.5 log(2 pi sigma^2) (no inflation)
   const int* obs_mod_param;   // per observation: parameter index of the shift, or -1
   const int* obs_row_start;   // nobs + 1: first operator row of each observation
+  // tangent-ray cut-off of the transmission sums (the reference's tau > 10): FP64 bit
+  // pattern (tau >= 0 compares as an integer) and double-float split
+  long long tau_cut_bits;
+  float tau_cut_hi, tau_cut_lo;
   // transposed observation operator (adjoint): per wavenumber the rows that read it
   const int* col_ptr;         // N + 1
   const int* col_row;         // nnz
@@ -195,6 +199,16 @@ struct GradWorkspace {
   double* gS = nullptr;      // B x M: d log L / d binned model
   double* seed = nullptr;    // B x 3: seed normaliser, its inverse, sum_r gS_r (s_r - shift_r)
   double* partial = nullptr; // B x L x V x tiles per-block sinks of the adjoint kernel
+  // transmission adjoint (double-floats unless noted), per (evaluation, level, wavenumber)
+  float2* tr_c = nullptr;     // extinction pair sums chi_i + chi_{i+1}
+  float2* tr_gt = nullptr;    // d log L / d tau_t
+  float2* tr_A = nullptr;     // (R + z_t)(1 - T_t)
+  float2* tr_z1 = nullptr;    // direct altitude sink of tangent level t
+  short* tr_I = nullptr;      // last level index inside the tau > 10 cut-off
+  float2* tr_gc = nullptr;    // d log L / d (chi_j + chi_{j+1})
+  float2* tr_gz = nullptr;    // d log L / d z_j
+  float2* tr_geo = nullptr;   // per evaluation 3 x L x L: dG/dz_j (P), dG/dz_t (Q), dG/dR (U)
+  double* tr_rp = nullptr;    // per (evaluation, tile) partial d log L / d R_p
 };
 
 // ----------------------------------------------------------------- host model
@@ -324,6 +338,7 @@ void launch_forward(Model& m, const double* params_dev, int batch, cudaStream_t 
                     bool want_loglike, uint8_t* neglect_dev, double* loglike_dev);
 void launch_spectrum_output(Model& m, double* out_dev, cudaStream_t stream);
 size_t table_bytes(const Model& m);  // device bytes of the model's (possibly shared) tables
+void set_tau_cutoff(Model& m, double tau);
 void stage_times(Model& m, float* ms3);
 // noalloc.cu
 void loglike_noalloc(Model& m, const double* params_dev, double* loglike_dev, uint8_t* neglect_dev,

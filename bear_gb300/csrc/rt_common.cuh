@@ -14,10 +14,9 @@ namespace bgb {
 static __device__ __constant__ double kMu[2] = {0.211324865405187, 0.788675134594813};
 static __device__ __constant__ double kInvMu[2] = {1.0 / 0.211324865405187, 1.0 / 0.788675134594813};
 
-// 700.0 and 10.0 as bit patterns of doubles: for non-negative x, x > 700 <=>
+// 700.0 as the bit pattern of a double: for non-negative x, x > 700 <=>
 // bits(x) > bits(700) (an integer comparison, off the FP64 pipe).
 constexpr long long kBits700 = 0x4085E00000000000LL;
-constexpr long long kBits10 = 0x4024000000000000LL;
 
 __device__ __forceinline__ void load_exp_tables(ExpTables& t) {
   for (int i = threadIdx.x; i < 65; i += blockDim.x) {

@@ -192,6 +192,10 @@ class Engine:
         _lib.check(self._lib.bear_model_table_sharing(self._h, C.byref(sh), C.byref(nb)))
         return bool(sh.value), int(nb.value)
 
+    def set_tau_cutoff(self, tau: float = 10.0) -> None:
+        """Optical depth at which transmission tangent sums stop (10, the reference's; inf: none)."""
+        _lib.check(self._lib.bear_model_set_tau_cutoff(self._h, float(tau)))
+
     def set_gradient_memory(self, nbytes: int = 0) -> None:
         """Device memory the gradient's work buffers may use per chunk (0 = default)."""
         _lib.check(self._lib.bear_model_set_gradient_memory(self._h, int(nbytes)))

@@ -614,7 +614,7 @@ def main():
 
     # adjoint gradient (emission models): log L and d log L / d params for the batch
     grad = None
-    if kind == "emission":
+    if True:  # emission and transmission models both have an adjoint
         G = torch.empty(B, eng.P, dtype=torch.float64, device=device)
 
         def grad_step():
@@ -637,7 +637,7 @@ def main():
         fwd_ms = total_ms / args.steps
         grad = {"evals_per_s": B / (grad_ms * 1e-3), "ms_per_batch": grad_ms, "forward_ms_per_batch": fwd_ms,
                 "grad_over_forward": grad_ms / fwd_ms, "parameters": eng.P, "steps": n_grad,
-                "kernels_per_batch": 6,
+                "kernels_per_batch": 6 if kind == "emission" else 10,
                 "api": "bear_loglike_grad_batch (adjoint; forward pass included in the time)"}
         del G
 

@@ -158,6 +158,14 @@ int bear_loglike_grad_batch(bear_model* m, const double* params_dev, int batch, 
                             double* loglike_dev, double* grad_dev, uint8_t* neglect_dev,
                             void* stream);
 
+/* Optical depth at which a transmission tangent-ray sum stops (the reference's
+ * tau > 10, src/forward_model/transmission/transmission_spectrum.cpp:136-137,
+ * the default; INFINITY: no cut-off). The cut-off makes log L a step function of
+ * the parameters wherever a ray's partial sum crosses it; gradient checks by
+ * finite differences therefore use the smooth model without it. Applies to
+ * later launches (not to graphs captured before). */
+int bear_model_set_tau_cutoff(bear_model* m, double tau);
+
 /* Device memory the gradient's work buffers may use per chunk of evaluations
  * (0 = default, 16 GiB). No reference counterpart. */
 int bear_model_set_gradient_memory(bear_model* m, long long bytes);

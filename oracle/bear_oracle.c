@@ -133,6 +133,7 @@ typedef struct orc_model {
   int nparam_general, nparam_chem, nparam_temp, nparam_cloud, nparam_mod, nparam_total;
   int M;                     /* total obs points */
   int finalized;
+  double tau_cut;            /* tangent-ray cut-off (the reference's 10) */
 } orc_model;
 
 /* ------------------------------------------------------------------ config parsing */
@@ -151,6 +152,7 @@ static int tokenize(char* line, char** tok, int maxtok) {
 orc_model* orc_create(const char* text) {
   orc_model* m = (orc_model*)calloc(1, sizeof(orc_model));
   m->resolution = 1.0;
+  m->tau_cut = 10;
   char* buf = strdup(text);
   char* save = NULL;
   for (char* line = strtok_r(buf, "\n", &save); line; line = strtok_r(NULL, "\n", &save)) {
@@ -967,7 +969,7 @@ static double transit_point(const orc_model* m, const double* chi, const atm_t* 
       const double a1 = R + a->z[i + 1], a0 = R + a->z[i];
       const double path = sqrt(a1 * a1 - b * b) - sqrt(a0 * a0 - b * b);
       tau += path * (chi[i] + chi[i + 1]);
-      if (tau > 10) break;
+      if (tau > m->tau_cut) break;
     }
     trans[t] = exp(-tau);
   }
@@ -1149,6 +1151,15 @@ int orc_loglike(const orc_model* m, const double* par, int P, double* loglike, d
   if (neglect) ll = -1e30;
   *loglike = ll;
   if (!obs_out) free(obs);
+  return 0;
+}
+
+/* Optical depth at which tangent-ray sums stop (the reference's 10; INFINITY:
+ * none). Test infrastructure: gradient checks by central differences use the
+ * smooth model without the cut-off. */
+int orc_set_tau_cutoff(orc_model* m, double tau) {
+  if (!m || !(tau > 0)) return 1;
+  m->tau_cut = tau;
   return 0;
 }
 

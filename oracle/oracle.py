@@ -52,6 +52,8 @@ def lib():
         L.orc_last_error.restype = C.c_char_p
         L.orc_set_threads.restype = C.c_int
         L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_set_tau_cutoff.restype = C.c_int
+        L.orc_set_tau_cutoff.argtypes = [C.c_void_p, C.c_double]
         L.orc_obs_setup.restype = C.c_int
         L.orc_obs_setup.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_long), C.c_int]
         _lib = L
@@ -106,6 +108,11 @@ class OracleModel:
         if lib().orc_forward(self.h, _ptr(p), p.size, _ptr(spec), _ptr(obs), C.byref(neg)):
             raise RuntimeError("oracle: " + lib().orc_last_error().decode())
         return spec, obs[: self.M], bool(neg.value)
+
+    def set_tau_cutoff(self, tau: float) -> None:
+        """Optical depth at which transmission tangent sums stop (10, the reference's; inf: none)."""
+        if lib().orc_set_tau_cutoff(self.h, float(tau)):
+            raise RuntimeError("oracle: invalid cut-off")
 
     def loglike(self, params) -> float:
         p = np.ascontiguousarray(params, dtype=np.float64)
