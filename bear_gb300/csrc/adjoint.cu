@@ -615,14 +615,14 @@ void free_grad_workspace(Model& m) {
   cudaFree(g.gS);
   cudaFree(g.seed);
   cudaFree(g.partial);
-  cudaFree(g.tr_c);
-  cudaFree(g.tr_gt);
-  cudaFree(g.tr_A);
-  cudaFree(g.tr_z1);
-  cudaFree(g.tr_I);
+  cudaFree(g.taps.tr_geo);
+  cudaFree(g.taps.tr_c);
+  cudaFree(g.taps.tr_T);
+  cudaFree(g.taps.tr_qs);
+  cudaFree(g.taps.tr_us);
+  cudaFree(g.taps.tr_I);
   cudaFree(g.tr_gc);
   cudaFree(g.tr_gz);
-  cudaFree(g.tr_geo);
   cudaFree(g.tr_rp);
   g = GradWorkspace{};
 }

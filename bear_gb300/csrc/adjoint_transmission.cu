@@ -9,16 +9,18 @@
 //   depth  = (h + R^2) / R_s^2 1e6
 // with G[t][i] = S_t(i+1) - S_t(i), S_t(j) = sqrt((R + z_j)^2 - (R + z_t)^2) (S_t(t) = 0).
 //
-// Kernel chain for one chunk of evaluations (after the forward pass, the
-// likelihood adjoint and the seed normaliser of adjoint.cu):
-//   tr_geometry_adjoint_kernel  per evaluation: P[t][j] = dG[t][j-1]/dz_j = (R + z_j)/S_t(j),
+// Kernel chain for one chunk of evaluations (the likelihood adjoint and the seed
+// normaliser come from adjoint.cu):
+//   tr_geometry_adjoint_kernel  per evaluation, before the forward radiative transfer:
+//                               P[t][j] = dG[t][j-1]/dz_j = (R + z_j)/S_t(j),
 //                               Q[t][i] = dG[t][i]/dz_t, U[t][i] = dG[t][i]/dR
-//   tr_adjoint_pass1            per wavenumber (forward layout): opacities recomputed, the
-//                               extinction column, tangent sums with their cut-off index,
-//                               g_tau_t = d log L / d tau_t, the tangent level's direct
-//                               altitude sink and d log L / dR; written per (level, wavenumber)
-//   tr_adjoint_pass2a           per (level j, wavenumber): d log L / d c_j = sum_t g_tau_t G[t][j]
-//                               and the geometry part of d log L / d z_j
+//   transmission_kernel<STORE>  (engine.cu) the forward pass itself also stores, per (level,
+//                               wavenumber), the ray transmission T_t, the cut-off index, the
+//                               pair sums c and the ray sums of c dG/dz_t and c dG/dR
+//   tr_adjoint_pass2a           per (level j, wavenumber), g_tau_t = d log L / d tau_t and the
+//                               cut-off indices staged in shared memory: d log L / d c_j =
+//                               sum_t g_tau_t G[t][j], d log L / d z_j (geometry and effective
+//                               height) and d log L / dR
 //   tr_adjoint_pass2b           per wavenumber, levels across warps: opacities recomputed for the
 //                               per-level sinks (log number densities of the table and Rayleigh
 //                               species, temperature, altitude, cloud extinction), warp
@@ -87,7 +89,7 @@ __global__ void tr_geometry_adjoint_kernel(DeviceModel dm, const LevelInfo* __re
   }
 }
 
-// ------------------------------------------------------------------ pass 1
+// ------------------------------------------------------------------ pass 2a
 struct TrArgs {
   const LevelInfo* lev;
   const LevelSpeciesDF* lsdf;
@@ -98,11 +100,11 @@ struct TrArgs {
   const float2* dwT;
   const double* gS;
   const double* seed;
-  float2* c;
-  float2* gt;
-  float2* A;
-  float2* z1;
-  short* I;
+  const float2* c;
+  const float2* T;
+  float2* qs;  // read, then overwritten with the direct altitude sink z1_t
+  float2* us;  // read, then overwritten with A_t = (R + z_t)(1 - T_t)
+  const short* I;
   float2* gc;
   float2* gz;
   double* rp;
@@ -110,165 +112,114 @@ struct TrArgs {
   int V;
 };
 
-// Same layout as transmission_kernel<true, 32>; dynamic shared memory: chi [L][32]
-// then the Rayleigh number densities [L][R] (double-floats).
-__global__ void __launch_bounds__(kTrTPN * kTrVPB) tr_adjoint_pass1(DeviceModel dm, TrArgs a) {
-  constexpr int VPB = kTrVPB, TPN = kTrTPN;
-  extern __shared__ double tr_smem[];
-  float2* chi_f = reinterpret_cast<float2*>(tr_smem);
-  __shared__ ExpTables et;
-  __shared__ double rp_part[TPN * VPB];
-  const int v = threadIdx.x % VPB, j = threadIdx.x / VPB;
-  const int b = blockIdx.x;
-  const int k = blockIdx.y * VPB + v;
-  const int L = dm.L, S = dm.S, R = dm.R;
+// Block: 32 wavenumbers (lanes) x 4 groups; group w takes levels j = w, w+4, ...
+// From the forward pass's stores, with g_h = d log L / dh (the normalised seed times
+// 1e6 / R_s^2) and F_t = (R + z_t) wz_t:
+//   g_tau_t = g_h F_t T_t                 staged with the cut-off indices in shared
+//                                          memory (float2 [L][32] then short [L][32])
+//   g_c_j   = sum_{t <= j <= I_t} g_tau_t G[t][j]                      (j <= L-2)
+//   g_z_j   = sum_{t < j} g_tau_t P[t][j] (c_{j-1} [j-1 <= I_t] - c_j [j <= I_t])
+//           + g_h (1 - T_j) wz_j + g_tau_j qs_j + g_h (A_{j-1} - A_{j+1}) (- A_0 at j = 0),
+//             A_t = (R + z_t)(1 - T_t)   (wz_t = z_{t+1} - z_{t-1}; z_1 - z_0 at t = 0)
+//   dlogL/dR += g_h (1 - T_j) wz_j + g_tau_j us_j (+ 2 R g_h once: depth = (h + R^2) / R_s^2)
+__global__ void __launch_bounds__(128) tr_adjoint_pass2a(DeviceModel dm, TrArgs a) {
+  extern __shared__ __align__(16) unsigned char tr2a_smem[];
+  __shared__ float2 rp_part[128];
+  const int L = dm.L;
+  float2* gt_s = reinterpret_cast<float2*>(tr2a_smem);               // [L][32]
+  float2* fz_s = gt_s + (size_t)L * 32;                                // [L]: R + z_t
+  float2* fw_s = fz_s + L;                                             // [L]: wz_t
+  float2* ff_s = fw_s + L;                                             // [L]: (R + z_t) wz_t
+  short* I_s = reinterpret_cast<short*>(ff_s + L);                     // [L][32]
+  const int b = blockIdx.x, lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
+  const int kk = blockIdx.y * 32 + lane;
+  const bool active = kk < dm.N;
+  const int k = active ? kk : dm.N - 1;
   const size_t N = dm.N;
-  const bool active = k < dm.N;
+  const size_t col = (size_t)b * L * N + k;
   const LevelInfo* lv = a.lev + (size_t)b * L;
-  const LevelSpeciesDF* sf = a.lsdf + (size_t)b * L * S;
-  float2* rn_s = chi_f + (size_t)L * VPB;
-  load_exp_tables(et);
-  for (int idx = threadIdx.x; idx < L * R; idx += blockDim.x) {
-    const df2 d = df_from_double(__ldg(&a.ray_n[(size_t)b * L * R + idx]));
-    rn_s[idx] = make_float2(d.hi, d.lo);
+  const double Rp = a.ev[b].radius, Rs = a.ev[b].star_radius;
+  // per-level geometry factors of the effective height (FP64 once per block)
+  for (int t = threadIdx.x; t < L - 1; t += blockDim.x) {
+    const double zt = __ldg(&lv[t].z);
+    const double wz = (__ldg(&lv[t + 1].z) - zt) + (t >= 1 ? zt - __ldg(&lv[t - 1].z) : 0.0);
+    const df2 z = df_from_double(Rp + zt), w = df_from_double(wz), f = df_from_double((Rp + zt) * wz);
+    fz_s[t] = make_float2(z.hi, z.lo);
+    fw_s[t] = make_float2(w.hi, w.lo);
+    ff_s[t] = make_float2(f.hi, f.lo);
   }
   __syncthreads();
-  if (active) {
-    for (int l = j; l < L; l += TPN) {
-      const Kappa kp = level_kappa_df(dm.ltab, N, sf + (size_t)l * S, S, k, et);
-      df2 x = kp.v;
-      if ((__double_as_longlong(kp.wide) << 1) != 0) x = df_add(x, df_from_double(kp.wide));
-      for (int r = 0; r < R; ++r) {
-        const float2 sr = __ldg(&dm.rayleigh_df[(size_t)r * N + k]);
-        const float2 nr = rn_s[l * R + r];
-        x = df_fma(df2{sr.x, sr.y}, df2{nr.x, nr.y}, x);
-      }
-      const float2 cl = __ldg(reinterpret_cast<const float2*>(&lv[l].cloud_hi));
-      x = df_add(x, df2{cl.x, cl.y});
-      chi_f[l * VPB + v] = make_float2(x.hi, x.lo);
+  const df2 gh = df_from_double(active ? tr_seed(dm, a.gS, a.seed, b, k) * 1e6 / (Rs * Rs) : 0.0);
+  const df2 one = df_make(1.0f);
+  auto ld = [&](const float2* arr, int t) {
+    const float2 v = arr[col + (size_t)t * N];
+    return df2{v.x, v.y};
+  };
+  auto sm = [](const float2* arr, int i) {
+    const float2 v = arr[i];
+    return df2{v.x, v.y};
+  };
+  // per tangent level: g_tau_t = g_h F_t T_t (staged), A_t = (R + z_t)(1 - T_t) and the direct
+  // sink z1_t = g_h (1 - T_t) wz_t + g_tau_t qs_t, written over the ray sums they replace
+  df2 rp = {0.0f, 0.0f};
+  for (int t = grp; t < L - 1; t += 4) {
+    const df2 T = ld(a.T, t), omT = df_sub(one, T);
+    const df2 gt = df_mul(df_mul(gh, sm(ff_s, t)), T);
+    const df2 base = df_mul(df_mul(gh, omT), sm(fw_s, t));
+    const df2 z1 = df_add(base, df_mul(gt, ld(a.qs, t)));
+    rp = df_add(rp, df_add(base, df_mul(gt, ld(a.us, t))));
+    const df2 A = df_mul(sm(fz_s, t), omT);
+    gt_s[t * 32 + lane] = make_float2(gt.hi, gt.lo);
+    I_s[t * 32 + lane] = a.I[col + (size_t)t * N];
+    if (active) {
+      a.qs[col + (size_t)t * N] = make_float2(z1.hi, z1.lo);
+      a.us[col + (size_t)t * N] = make_float2(A.hi, A.lo);
     }
   }
+  if (grp == 0) rp = df_add(rp, df_mul(gh, df_from_double(2.0 * Rp)));  // depth = (h + R^2) / R_s^2
   __syncthreads();
-  if (active && j == 0) {
-    for (int i = 0; i < L - 1; ++i) {
-      const float2 c0 = chi_f[i * VPB + v], c1 = chi_f[(i + 1) * VPB + v];
-      const df2 s2 = df_add(df2{c0.x, c0.y}, df2{c1.x, c1.y});
-      chi_f[i * VPB + v] = make_float2(s2.hi, s2.lo);
-    }
-  }
-  __syncthreads();
-  const size_t col = (size_t)b * L * N + k;  // [b][l][k] element of level 0
-  double rp = 0.0;
   if (active) {
-    for (int i = j; i < L - 1; i += TPN) a.c[col + (size_t)i * N] = chi_f[i * VPB + v];
-    const double Rp = a.ev[b].radius, Rs = a.ev[b].star_radius;
-    // g_h = d log L / dh (normalised)
-    const double gh = tr_seed(dm, a.gS, a.seed, b, k) * 1e6 / (Rs * Rs);
-    if (j == 0) rp += gh * 2.0 * Rp;  // the explicit R^2 in depth = (h + R^2) / R_s^2
     const float2* G = a.geom + (size_t)b * L * L;
-    const float2* Qm = a.geo + (size_t)b * 3 * L * L + (size_t)L * L;
-    const float2* Um = Qm + (size_t)L * L;
-    for (int t = L - 2 - j; t >= 0; t -= TPN) {
-      const float2* Gt = G + (size_t)t * L;
-      const float2* Qt = Qm + (size_t)t * L;
-      const float2* Ut = Um + (size_t)t * L;
-      df2 ts = {0.0f, 0.0f}, qs = {0.0f, 0.0f}, us = {0.0f, 0.0f};
-      int last = L - 2;
-      for (int i = t; i < L - 1; ++i) {
-        const float2 g = __ldg(&Gt[i]), c = chi_f[i * VPB + v];
-        const float2 q = __ldg(&Qt[i]), u = __ldg(&Ut[i]);
-        const df2 cc = {c.x, c.y};
-        ts = df_fma(df2{g.x, g.y}, cc, ts);
-        qs = df_fma(df2{q.x, q.y}, cc, qs);
-        us = df_fma(df2{u.x, u.y}, cc, us);
-        if (ts.hi > dm.tau_cut_hi || (ts.hi == dm.tau_cut_hi && ts.lo > dm.tau_cut_lo)) {  // the forward's cut-off
-          last = i;
-          break;
+    const float2* P = a.geo + (size_t)b * 3 * L * L;
+    const df2 z = {0.0f, 0.0f};
+    for (int j = grp; j < L; j += 4) {
+      const df2 cj1 = j >= 1 ? ld(a.c, j - 1) : z;
+      const df2 cj = j <= L - 2 ? ld(a.c, j) : z;
+      const df2 dcc = df_sub(cj1, cj);
+      df2 gc = z, gzp = z;
+      const int tmax = min(j, L - 2);
+      for (int t = 0; t <= tmax; ++t) {
+        const int I = I_s[t * 32 + lane];
+        if (I < j - 1) continue;  // the ray of tangent level t stops below level j
+        const df2 gtau = sm(gt_s, t * 32 + lane);
+        const bool in_j = I >= j && j <= L - 2;
+        if (in_j) {
+          const float2 g = __ldg(&G[(size_t)t * L + j]);
+          gc = df_fma(gtau, df2{g.x, g.y}, gc);
+        }
+        if (t < j) {
+          const float2 p = __ldg(&P[(size_t)t * L + j]);
+          gzp = df_fma(df_mul(gtau, df2{p.x, p.y}), in_j ? dcc : cj1, gzp);  // j - 1 <= I_t holds here
         }
       }
-      const double tau = df_to_double(ts);
-      const double tr = __double_as_longlong(tau) > kBits700 ? 0.0 : exp_tang(-tau, et.d);
-      const double zt = __ldg(&lv[t].z);
-      const double wz = (__ldg(&lv[t + 1].z) - zt) + (t >= 1 ? zt - __ldg(&lv[t - 1].z) : 0.0);
-      const double gtau = gh * (Rp + zt) * wz * tr;  // d log L / d tau_t = -T_t d log L / dT_t
-      const double A = (Rp + zt) * (1.0 - tr);
-      const double z1 = gh * (1.0 - tr) * wz + gtau * df_to_double(qs);
-      rp += gh * (1.0 - tr) * wz + gtau * df_to_double(us);
-      const size_t at = col + (size_t)t * N;
-      const df2 dg = df_from_double(gtau), dA = df_from_double(A), d1 = df_from_double(z1);
-      a.gt[at] = make_float2(dg.hi, dg.lo);
-      a.A[at] = make_float2(dA.hi, dA.lo);
-      a.z1[at] = make_float2(d1.hi, d1.lo);
-      a.I[at] = (short)last;
+      // direct terms of the effective height: z1_j + g_h (A_{j-1} - A_{j+1}) (- A_0 at j = 0)
+      df2 nb = z;
+      if (j >= 1) nb = ld(a.us, j - 1);
+      if (j + 1 <= L - 2) nb = df_sub(nb, ld(a.us, j + 1));
+      if (j == 0) nb = df_sub(nb, ld(a.us, 0));
+      df2 gzt = df_fma(gh, nb, gzp);
+      if (j <= L - 2) gzt = df_add(gzt, ld(a.qs, j));
+      a.gc[col + (size_t)j * N] = make_float2(gc.hi, gc.lo);
+      a.gz[col + (size_t)j * N] = make_float2(gzt.hi, gzt.lo);
     }
   }
-  // d log L / dR of the block, summed in a fixed order
-  rp_part[threadIdx.x] = rp;
+  rp_part[threadIdx.x] = make_float2(rp.hi, rp.lo);
   __syncthreads();
   if (threadIdx.x == 0) {
     double s = 0.0;
-    for (int q = 0; q < TPN * VPB; ++q) s += rp_part[q];
+    for (int q = 0; q < 128; ++q) s += df_to_double(sm(rp_part, q));
     a.rp[(size_t)b * gridDim.y + blockIdx.y] = s;
   }
-}
-
-// ------------------------------------------------------------------ pass 2a
-// One thread per (level j, wavenumber): grid (evaluations, tiles of 128 wavenumbers, L).
-//   g_c_j  = sum_{t <= j <= I_t} g_tau_t G[t][j]                       (j <= L-2)
-//   g_z_j  = sum_{t < j} g_tau_t P[t][j] (c_{j-1} [j-1 <= I_t] - c_j [j <= I_t])
-//          + z1_j + g_h (A_{j-1} - A_{j+1}) (- A_0 at j = 0)           (wz_t = z_{t+1} - z_{t-1})
-__global__ void __launch_bounds__(128) tr_adjoint_pass2a(DeviceModel dm, TrArgs a) {
-  const int b = blockIdx.x, j = blockIdx.z;
-  const int k = blockIdx.y * blockDim.x + threadIdx.x;
-  if (k >= dm.N) return;
-  const int L = dm.L;
-  const size_t N = dm.N;
-  const size_t col = (size_t)b * L * N + k;
-  const float2* G = a.geom + (size_t)b * L * L;
-  const float2* P = a.geo + (size_t)b * 3 * L * L;
-  const df2 z = {0.0f, 0.0f};
-  df2 cj1 = z, cj = z;
-  if (j >= 1) {
-    const float2 v = a.c[col + (size_t)(j - 1) * N];
-    cj1 = df2{v.x, v.y};
-  }
-  if (j <= L - 2) {
-    const float2 v = a.c[col + (size_t)j * N];
-    cj = df2{v.x, v.y};
-  }
-  df2 gc = z, gzp = z;
-  const int tmax = min(j, L - 2);
-  for (int t = 0; t <= tmax; ++t) {
-    const int I = a.I[col + (size_t)t * N];
-    if (I < j - 1) continue;  // the ray of tangent level t stops below level j
-    const float2 gv = a.gt[col + (size_t)t * N];
-    const df2 gtau = {gv.x, gv.y};
-    const bool in_j = I >= j && j <= L - 2;
-    if (in_j) {
-      const float2 g = __ldg(&G[(size_t)t * L + j]);
-      gc = df_fma(gtau, df2{g.x, g.y}, gc);
-    }
-    if (t < j) {
-      const float2 p = __ldg(&P[(size_t)t * L + j]);
-      const df2 d = in_j ? df_sub(cj1, cj) : cj1;  // j - 1 <= I_t holds here
-      gzp = df_fma(df_mul(gtau, df2{p.x, p.y}), d, gzp);
-    }
-  }
-  // direct altitude terms of the effective height
-  const double Rs = a.ev[b].star_radius;
-  const double gh = tr_seed(dm, a.gS, a.seed, b, k) * 1e6 / (Rs * Rs);
-  auto ld = [&](const float2* arr, int t) {
-    const float2 v = arr[col + (size_t)t * N];
-    return df_to_double(df2{v.x, v.y});
-  };
-  double direct = 0.0;
-  if (j <= L - 2) direct += ld(a.z1, j);
-  if (j >= 1) direct += gh * ld(a.A, j - 1);
-  if (j + 1 <= L - 2) direct -= gh * ld(a.A, j + 1);
-  if (j == 0) direct -= gh * ld(a.A, 0);
-  const df2 gzt = df_add(gzp, df_from_double(direct));
-  a.gc[col + (size_t)j * N] = make_float2(gc.hi, gc.lo);
-  a.gz[col + (size_t)j * N] = make_float2(gzt.hi, gzt.lo);
 }
 
 // ------------------------------------------------------------------ pass 2b
@@ -278,7 +229,7 @@ __global__ void __launch_bounds__(128) tr_adjoint_pass2a(DeviceModel dm, TrArgs 
 // S..S+R-1 d log L / d ln n_r (Rayleigh species), S+R temperature, S+R+1 z_l,
 // S+R+2 cloud extinction of level l (all times the evaluation's seed normaliser).
 template <int VP>
-__global__ void __launch_bounds__(kTrTPN * kTrVPB) tr_adjoint_pass2b(DeviceModel dm, TrArgs a) {
+__global__ void __launch_bounds__(kTrTPN * kTrVPB, VP == 32 ? 4 : 6) tr_adjoint_pass2b(DeviceModel dm, TrArgs a) {
   constexpr int G = 32 / VP;
   __shared__ ExpTables et;
   extern __shared__ __align__(16) unsigned char tr2_smem[];
@@ -493,51 +444,49 @@ __global__ void __launch_bounds__(128) tr_atmosphere_adjoint_kernel(
 // ------------------------------------------------------------------ host side
 size_t transmission_grad_bytes_per_eval(const Model& m, int V) {
   const size_t L = m.L, N = m.N;
-  const size_t tiles2 = (N + 31) / 32, tiles1 = (N + kTrVPB - 1) / kTrVPB;
-  return L * N * (6 * sizeof(float2) + sizeof(short)) + 3 * L * L * sizeof(float2) + L * (size_t)V * tiles2 * 8 +
-         tiles1 * 8;
+  const size_t tiles = (N + 31) / 32;
+  return L * N * (6 * sizeof(float2) + sizeof(short)) + 3 * L * L * sizeof(float2) + L * (size_t)V * tiles * 8 +
+         tiles * 8;
 }
 
 void alloc_transmission_grad(Model& m, int chunk, int V) {
   GradWorkspace& g = m.gws;
   const size_t B = chunk, L = m.L, N = m.N;
-  const size_t n = B * L * N;
-  BGB_CUDA(cudaMalloc(&g.tr_c, n * sizeof(float2)));
-  BGB_CUDA(cudaMalloc(&g.tr_gt, n * sizeof(float2)));
-  BGB_CUDA(cudaMalloc(&g.tr_A, n * sizeof(float2)));
-  BGB_CUDA(cudaMalloc(&g.tr_z1, n * sizeof(float2)));
-  BGB_CUDA(cudaMalloc(&g.tr_I, n * sizeof(short)));
+  const size_t n = B * L * N, tiles = (N + 31) / 32;
+  BGB_CUDA(cudaMalloc(&g.taps.tr_c, n * sizeof(float2)));
+  BGB_CUDA(cudaMalloc(&g.taps.tr_T, n * sizeof(float2)));
+  BGB_CUDA(cudaMalloc(&g.taps.tr_qs, n * sizeof(float2)));
+  BGB_CUDA(cudaMalloc(&g.taps.tr_us, n * sizeof(float2)));
+  BGB_CUDA(cudaMalloc(&g.taps.tr_I, n * sizeof(short)));
+  BGB_CUDA(cudaMalloc(&g.taps.tr_geo, B * 3 * L * L * sizeof(float2)));
   BGB_CUDA(cudaMalloc(&g.tr_gc, n * sizeof(float2)));
   BGB_CUDA(cudaMalloc(&g.tr_gz, n * sizeof(float2)));
-  BGB_CUDA(cudaMalloc(&g.tr_geo, B * 3 * L * L * sizeof(float2)));
-  BGB_CUDA(cudaMalloc(&g.tr_rp, B * ((N + kTrVPB - 1) / kTrVPB) * sizeof(double)));
-  BGB_CUDA(cudaMalloc(&g.partial, B * L * (size_t)V * ((N + 31) / 32) * sizeof(double)));
+  BGB_CUDA(cudaMalloc(&g.tr_rp, B * tiles * sizeof(double)));
+  BGB_CUDA(cudaMalloc(&g.partial, B * L * (size_t)V * tiles * sizeof(double)));
 }
 
+// The adjoint kernels of one chunk, after the storing forward pass and the likelihood adjoint.
 void transmission_adjoint_chunk(Model& m, const double* params_chunk, int nb, cudaStream_t st, double* grad_chunk,
                                 int V) {
   const DeviceModel& dm = m.dm;
   const Workspace& w = m.ws;
   const GradWorkspace& g = m.gws;
-  const int L = m.L, S = m.acfg.S, R = m.acfg.R, P = m.acfg.nparam_total;
+  const ForwardTaps& tp = g.taps;
+  const int L = m.L, S = m.acfg.S, P = m.acfg.nparam_total;
   const size_t N = m.N;
-  const int tiles1 = (int)((N + kTrVPB - 1) / kTrVPB), tiles2 = (int)((N + 31) / 32);
-  TrArgs a{w.lev, w.lsdf, w.ray_n, w.ev, reinterpret_cast<const float2*>(w.geom), g.tr_geo, g.taps.dwT, g.gS,
-           g.seed, g.tr_c, g.tr_gt, g.tr_A, g.tr_z1, g.tr_I, g.tr_gc, g.tr_gz, g.tr_rp, g.partial, V};
-  tr_geometry_adjoint_kernel<<<nb, 256, 0, st>>>(dm, w.lev, w.ev, g.tr_geo);
-  BGB_CUDA(cudaGetLastError());
-  const size_t sm1 = (size_t)L * kTrVPB * sizeof(float2) + (size_t)L * R * sizeof(float2);
-  if (sm1 > 48 * 1024)
-    BGB_CUDA(cudaFuncSetAttribute(tr_adjoint_pass1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1));
-  tr_adjoint_pass1<<<dim3(nb, tiles1), kTrTPN * kTrVPB, sm1, st>>>(dm, a);
-  BGB_CUDA(cudaGetLastError());
-  tr_adjoint_pass2a<<<dim3(nb, (unsigned)((N + 127) / 128), L), 128, 0, st>>>(dm, a);
+  const int tiles = (int)((N + 31) / 32);
+  TrArgs a{w.lev, w.lsdf, w.ray_n, w.ev, reinterpret_cast<const float2*>(w.geom), tp.tr_geo, tp.dwT, g.gS,
+           g.seed, tp.tr_c, tp.tr_T, tp.tr_qs, tp.tr_us, tp.tr_I, g.tr_gc, g.tr_gz, g.tr_rp, g.partial, V};
+  const size_t sm2a = (size_t)L * 32 * (sizeof(float2) + sizeof(short)) + (size_t)3 * L * sizeof(float2);
+  if (sm2a > 48 * 1024)
+    BGB_CUDA(cudaFuncSetAttribute(tr_adjoint_pass2a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2a));
+  tr_adjoint_pass2a<<<dim3(nb, tiles), 128, sm2a, st>>>(dm, a);
   BGB_CUDA(cudaGetLastError());
   const size_t sm2 = (size_t)S * kTrTPN * kTrVPB * (sizeof(float2) + sizeof(double));
   const int VP = V <= 8 ? 8 : V <= 16 ? 16 : 32;
   auto go2 = [&](auto kernel) {
     if (sm2 > 48 * 1024) BGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));
-    kernel<<<dim3(nb, tiles2), kTrTPN * kTrVPB, sm2, st>>>(dm, a);
+    kernel<<<dim3(nb, tiles), kTrTPN * kTrVPB, sm2, st>>>(dm, a);
   };
   if (VP == 8) go2(tr_adjoint_pass2b<8>);
   else if (VP == 16) go2(tr_adjoint_pass2b<16>);
@@ -546,8 +495,8 @@ void transmission_adjoint_chunk(Model& m, const double* params_chunk, int nb, cu
   const size_t sma = (size_t)L * V * sizeof(double);
   if (sma > 48 * 1024)
     BGB_CUDA(cudaFuncSetAttribute(tr_atmosphere_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sma));
-  tr_atmosphere_adjoint_kernel<<<nb, 128, sma, st>>>(dm, params_chunk, P, w.lev, w.ev, g.partial, V, tiles2, g.tr_rp,
-                                                     tiles1, g.seed, grad_chunk);
+  tr_atmosphere_adjoint_kernel<<<nb, 128, sma, st>>>(dm, params_chunk, P, w.lev, w.ev, g.partial, V, tiles, g.tr_rp,
+                                                     tiles, g.seed, grad_chunk);
   BGB_CUDA(cudaGetLastError());
 }
 

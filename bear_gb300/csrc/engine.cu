@@ -201,16 +201,23 @@ __global__ void transmission_geometry_kernel(DeviceModel dm, const LevelInfo* __
 // sum_t (R + z_t)(1 - T_t)(dz_{t-1} + dz_t), which regroups the reference's
 // trapezoid sum. Dynamic shared memory: chi [L][VPB] (8 B each), then with DF the
 // evaluation's Rayleigh number densities [L][R] as double-floats.
+// With STORE (double-float path, gradient pass) the kernel also writes, per
+// (evaluation, level, wavenumber), the pair sums c, the ray transmissions T_t, the
+// last index inside the cut-off and the sums of c_i dG[t][i]/dz_t and c_i dG[t][i]/dR
+// over each ray (taps.tr_*; dG from taps.tr_geo, computed before this kernel).
 constexpr int kTPN = 4;
 
-template <bool DF, int VPB>
+__global__ void tr_geometry_adjoint_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
+                                           const EvalInfo* __restrict__ ev, float2* __restrict__ geo);
+
+template <bool DF, int VPB, bool STORE = false>
 __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
                                                            const LevelSpecies* __restrict__ ls,
                                                            const LevelSpeciesDF* __restrict__ lsdf,
                                                            const double* __restrict__ ray_n,
                                                            const EvalInfo* __restrict__ ev,
                                                            const double* __restrict__ geom,
-                                                           double* __restrict__ spectrum) {
+                                                           double* __restrict__ spectrum, ForwardTaps taps) {
   constexpr int TPN = kTPN;
   extern __shared__ double chi_s[];  // [L][VPB]
   float2* chi_f = reinterpret_cast<float2*>(chi_s);
@@ -274,10 +281,34 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
   __syncthreads();
   double h = 0.0;
   const double Rp = ev[b].radius;
+  const size_t col = (size_t)b * L * N + k;  // [b][level][k] of level 0 (gradient pass stores)
+  if (STORE && active)
+    for (int i = j; i < L - 1; i += TPN) taps.tr_c[col + (size_t)i * N] = chi_f[i * VPB + v];
   if (active) {
     for (int t = L - 2 - j; t >= 0; t -= TPN) {
       double tau;
-      if (DF) {
+      df2 qs = {0.0f, 0.0f}, us = {0.0f, 0.0f};
+      int last = L - 2;
+      if (DF && STORE) {
+        const float2* Gt = reinterpret_cast<const float2*>(geom) + (size_t)b * L * L + (size_t)t * L;
+        const float2* Qt = taps.tr_geo + (size_t)b * 3 * L * L + (size_t)L * L + (size_t)t * L;
+        const float2* Ut = Qt + (size_t)L * L;
+        const float ch = dm.tau_cut_hi, cl = dm.tau_cut_lo;
+        df2 ts = {0.0f, 0.0f};
+        for (int i = t; i < L - 1; ++i) {
+          const float2 g = __ldg(&Gt[i]), c = chi_f[i * VPB + v];
+          const float2 q = __ldg(&Qt[i]), u = __ldg(&Ut[i]);
+          const df2 cc = {c.x, c.y};
+          ts = df_fma(df2{g.x, g.y}, cc, ts);
+          qs = df_fma(df2{q.x, q.y}, cc, qs);
+          us = df_fma(df2{u.x, u.y}, cc, us);
+          if (ts.hi > ch || (ts.hi == ch && ts.lo > cl)) {  // tau > cut-off
+            last = i;
+            break;
+          }
+        }
+        tau = df_to_double(ts);
+      } else if (DF) {
         const float2* Gt = reinterpret_cast<const float2*>(geom) + (size_t)b * L * L + (size_t)t * L;
         df2 ts = {0.0f, 0.0f};
         const float ch = dm.tau_cut_hi, cl = dm.tau_cut_lo;
@@ -319,6 +350,14 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
       double tr;
       if (DF) tr = __double_as_longlong(tau) > kBits700 ? 0.0 : exp_tang(-tau, et.d);
       else tr = exp(-tau);
+      if (STORE) {
+        const size_t at = col + (size_t)t * N;
+        const df2 dT = df_from_double(tr);
+        taps.tr_T[at] = make_float2(dT.hi, dT.lo);
+        taps.tr_qs[at] = make_float2(qs.hi, qs.lo);
+        taps.tr_us[at] = make_float2(us.hi, us.lo);
+        taps.tr_I[at] = (short)last;
+      }
       const double zt = __ldg(&lv[t].z);
       const double wz = (__ldg(&lv[t + 1].z) - zt) + (t >= 1 ? zt - __ldg(&lv[t - 1].z) : 0.0);
       h = fma((Rp + zt) * (1. - tr), wz, h);
@@ -675,6 +714,7 @@ void upload_model(Model& m) {
     BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<false, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<true, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<false, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<true, 32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
   }
 }
 
@@ -752,10 +792,20 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
     const bool df = m.precision != 1;
     const size_t sm = (size_t)L * vpb * sizeof(double) + (df ? (size_t)L * dm.R * sizeof(float2) : 0);
     if (sm > kTransmissionDynSmem) throw Error(BEAR_ERR_UNSUPPORTED, "too many levels for the transmission kernel");
+    const ForwardTaps none{};
     auto go = [&](auto kernel) {
-      kernel<<<grid, kTPN * vpb, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.spectrum);
+      kernel<<<grid, kTPN * vpb, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.spectrum, none);
     };
-    if (vpb == 16) df ? go(transmission_kernel<true, 16>) : go(transmission_kernel<false, 16>);
+    if (taps) {
+      // gradient pass: double-float kernel, 32 wavenumbers per block, storing the ray data
+      if (!df) throw Error(BEAR_ERR_UNSUPPORTED, "the transmission gradient runs in precision mode 0");
+      tr_geometry_adjoint_kernel<<<batch, 256, 0, st>>>(dm, w.lev, w.ev, taps->tr_geo);
+      BGB_CUDA(cudaGetLastError());
+      const dim3 g32(batch, (dm.N + 31) / 32);
+      const size_t sm32 = (size_t)L * 32 * sizeof(double) + (size_t)L * dm.R * sizeof(float2);
+      transmission_kernel<true, 32, true><<<g32, kTPN * 32, sm32, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev,
+                                                                        w.geom, w.spectrum, *taps);
+    } else if (vpb == 16) df ? go(transmission_kernel<true, 16>) : go(transmission_kernel<false, 16>);
     else if (vpb == 64) df ? go(transmission_kernel<true, 64>) : go(transmission_kernel<false, 64>);
     else df ? go(transmission_kernel<true, 32>) : go(transmission_kernel<false, 32>);
   }

@@ -188,7 +188,14 @@ struct Workspace {
 // Extra outputs of the forward pass that the adjoint reads back.
 struct ForwardTaps {
   float2* dwT = nullptr;     // B x L x S: d wT / dT of every stencil (double-float)
-  double* istore = nullptr;  // B x L x 2 x N: Gauss-angle intensities after every level
+  double* istore = nullptr;  // emission, B x L x 2 x N: Gauss-angle intensities after every level
+  // transmission, per (evaluation, level, wavenumber) as double-floats unless noted
+  float2* tr_geo = nullptr;  // per evaluation 3 x L x L: dG/dz_j (P), dG/dz_t (Q), dG/dR (U)
+  float2* tr_c = nullptr;    // extinction pair sums chi_i + chi_{i+1}
+  float2* tr_T = nullptr;    // tangent-ray transmission T_t
+  float2* tr_qs = nullptr;   // sum_i c_i Q[t][i] over the ray's terms
+  float2* tr_us = nullptr;   // sum_i c_i U[t][i]
+  short* tr_I = nullptr;     // last level index inside the cut-off
 };
 
 // Work buffers of the gradient for a chunk of evaluations.
@@ -199,15 +206,9 @@ struct GradWorkspace {
   double* gS = nullptr;      // B x M: d log L / d binned model
   double* seed = nullptr;    // B x 3: seed normaliser, its inverse, sum_r gS_r (s_r - shift_r)
   double* partial = nullptr; // B x L x V x tiles per-block sinks of the adjoint kernel
-  // transmission adjoint (double-floats unless noted), per (evaluation, level, wavenumber)
-  float2* tr_c = nullptr;     // extinction pair sums chi_i + chi_{i+1}
-  float2* tr_gt = nullptr;    // d log L / d tau_t
-  float2* tr_A = nullptr;     // (R + z_t)(1 - T_t)
-  float2* tr_z1 = nullptr;    // direct altitude sink of tangent level t
-  short* tr_I = nullptr;      // last level index inside the tau > 10 cut-off
+  // transmission adjoint, per (evaluation, level, wavenumber), double-floats
   float2* tr_gc = nullptr;    // d log L / d (chi_j + chi_{j+1})
   float2* tr_gz = nullptr;    // d log L / d z_j
-  float2* tr_geo = nullptr;   // per evaluation 3 x L x L: dG/dz_j (P), dG/dz_t (Q), dG/dR (U)
   double* tr_rp = nullptr;    // per (evaluation, tile) partial d log L / d R_p
 };
 
