@@ -38,6 +38,7 @@ sys.path.insert(0, REPO)
 
 from bear_gb300 import synthetic as syn  # noqa: E402
 from bear_gb300.config import observation_arrays, render_config  # noqa: E402
+from bear_gb300.replicas import max_over_ranks  # noqa: E402
 
 WORKLOADS = {
     "emission_batched": ("emission_batched", "emission"),
@@ -375,9 +376,7 @@ def run_joint(args):
         barrier()
     total_ms = sum(a.elapsed_time(b) for a, b in evs)
     if dist is not None:
-        t = torch.tensor([total_ms], dtype=torch.float64, device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = t.item()
+        total_ms = max_over_ranks(total_ms, dist, device)
     value = world * B * args.steps / (total_ms * 1e-3)
 
     # end to end: pinned host parameters in, joint log-likelihoods out
@@ -402,6 +401,8 @@ def run_joint(args):
         e2e.append((a, b))
     barrier()
     e2e_ms = sum(a.elapsed_time(b) for a, b in e2e)
+    if dist is not None:
+        e2e_ms = max_over_ranks(e2e_ms, dist, device)
     e2e_value = world * B * args.steps / (e2e_ms * 1e-3)
 
     # plain path: one host call per model per evaluation
@@ -568,9 +569,7 @@ def main():
     step_ms = [s.elapsed_time(e) for s, e in step_ms]
     total_ms = sum(step_ms)
     if dist is not None:
-        t = torch.tensor([total_ms], dtype=torch.float64, device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = t.item()
+        total_ms = max_over_ranks(total_ms, dist, device)
     value = world * B * args.steps / (total_ms * 1e-3)
 
     # end-to-end through the host API: pinned params in, log-likelihoods out
@@ -596,9 +595,7 @@ def main():
     barrier()
     e2e_total = sum(s.elapsed_time(e) for s, e in e2e_ms)
     if dist is not None:
-        t = torch.tensor([e2e_total], dtype=torch.float64, device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_total = t.item()
+        e2e_total = max_over_ranks(e2e_total, dist, device)
     e2e_value = world * B * args.steps / (e2e_total * 1e-3)
 
     # plain single-evaluation path (bear_loglike, one host call per evaluation)
