@@ -55,6 +55,12 @@ EXPORTS = {
     "bear_model_stage_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     "bear_model_table_info": (C.c_int, [C.c_void_p, _ip, _ip, _ip, C.POINTER(C.c_longlong)]),
     "bear_model_stencil_rows": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_longlong)]),
+    "bear_model_set_priors": (C.c_int, [C.c_void_p, C.c_int, _ip, _dp, _dp, _dp, _ip]),
+    "bear_prior_transform_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
+    "bear_loglike_cube_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                          C.c_void_p, C.c_void_p]),
+    "bear_batch_graph_create_cube": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                               C.c_void_p, C.POINTER(C.c_void_p)]),
 }
 
 

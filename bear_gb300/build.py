@@ -40,6 +40,7 @@ def _units():
         ("adjoint.cu", common_cu),
         ("adjoint_transmission.cu", common_cu),
         ("noalloc.cu", common_cu),
+        ("priors.cu", common_cu),
         # bit-faithful host-style arithmetic: no FMA contraction
         ("atmosphere.cu", common_cu + ["--fmad=false"]),
         ("model_setup.cpp", common_cpp + ["-Xcompiler", "-ffp-contract=off"]),
@@ -51,7 +52,7 @@ def _sources_digest() -> str:
     h = hashlib.sha1()
     for d in (CSRC, INCLUDE):
         for f in sorted(os.listdir(d)):
-            if f.endswith((".cu", ".cpp", ".h")):
+            if f.endswith((".cu", ".cuh", ".cpp", ".h")):
                 with open(os.path.join(d, f), "rb") as fh:
                     h.update(f.encode())
                     h.update(fh.read())

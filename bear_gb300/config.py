@@ -5,8 +5,9 @@ the reference's Python binding (python/src/bear_python_wrapper.cpp:28-300):
 ``Config`` (GlobalConfig, src/config/global_config.h:27-71), ``Observation``
 (ObservationInput, src/observations/observations.h:42-92), ``Prior``
 (PriorConfig, src/retrieval/priors.h:32-49), ``EmissionModelConfig``
-(src/forward_model/emission/emission.h:44-100) and ``TransmissionModelConfig``
-(src/forward_model/transmission/transmission.h:47-110).
+(src/forward_model/emission/emission.h:44-100), ``TransmissionModelConfig``
+(src/forward_model/transmission/transmission.h:47-110) and ``OccultationConfig``
+(src/forward_model/secondary_eclipse/secondary_eclipse.h:53-105).
 
 The engine itself is configured through a line-based ``key value...`` text
 (``render_config``) plus per-observation arrays, which is what crosses the
@@ -166,6 +167,50 @@ class TransmissionModelConfig(GenericConfig):
         self.modules_parameters = [list(p) for p in modp]
 
 
+class OccultationConfig(GenericConfig):
+    """Secondary-eclipse model, src/forward_model/secondary_eclipse/secondary_eclipse.h:53-105;
+    constructor argument order of secondary_eclipse_model_config.cpp:76-112 (the one pyBeAR
+    binds, python/src/bear_python_wrapper.cpp:203-221), clouds optional.
+
+    stellar_spectrum_model: "blackbody" (no parameters; T_eff is fitted), "file" [path]
+    ("wavelength flux" lines, W m^-2 um^-1) or "grid" [folder/] (T_eff, log g, [M/H] fitted)."""
+
+    forward_model_type = "secondary_eclipse"
+
+    def __init__(
+        self,
+        nb_grid_points: int,
+        atmos_bottom_pressure: float,
+        atmos_top_pressure: float,
+        temperature_profile_model: str,
+        temperature_profile_parameters: Sequence[str],
+        radiative_transfer_model: str,
+        radiative_transfer_parameters: Sequence[str],
+        chemistry_model: Sequence[str],
+        chemistry_parameters: Sequence[Sequence[str]],
+        opacity_species_symbol: Sequence[str],
+        opacity_species_folder: Sequence[str],
+        stellar_spectrum_model: str,
+        stellar_model_parameters: Sequence[str],
+        cloud_model: Sequence[str] = (),
+        cloud_model_parameters: Sequence[Sequence[str]] = (),
+    ):
+        self.nb_grid_points = int(nb_grid_points)
+        self.atmos_boundaries = [float(atmos_bottom_pressure), float(atmos_top_pressure)]
+        self.temperature_profile_model = temperature_profile_model
+        self.temperature_profile_parameters = list(temperature_profile_parameters)
+        self.radiative_transfer_model = radiative_transfer_model
+        self.radiative_transfer_parameters = list(radiative_transfer_parameters)
+        self.chemistry_model = list(chemistry_model)
+        self.chemistry_parameters = [list(p) for p in chemistry_parameters]
+        self.opacity_species_symbol = list(opacity_species_symbol)
+        self.opacity_species_folder = list(opacity_species_folder)
+        self.stellar_spectrum_model = stellar_spectrum_model
+        self.stellar_model_parameters = list(stellar_model_parameters)
+        self.cloud_model = list(cloud_model)
+        self.cloud_model_parameters = [list(p) for p in cloud_model_parameters]
+
+
 def _fmt(x: float) -> str:
     return repr(float(x))
 
@@ -189,9 +234,12 @@ def render_config(config: Config, model_config: GenericConfig) -> str:
         " ".join(["temperature_profile", model_config.temperature_profile_model]
                  + list(model_config.temperature_profile_parameters)),
     ]
-    if mt == "emission":
+    if mt in ("emission", "secondary_eclipse", "Secondary_eclipse", "se"):
         lines.append(" ".join(["radiative_transfer", model_config.radiative_transfer_model]
                               + list(model_config.radiative_transfer_parameters)))
+        if mt != "emission":
+            lines.append(" ".join(["stellar_spectrum", model_config.stellar_spectrum_model]
+                                  + list(model_config.stellar_model_parameters)))
     else:
         lines.append(f"fit_mean_molecular_weight {int(model_config.fit_mean_molecular_weight)}")
         lines.append(f"fit_scale_height {int(model_config.fit_scale_height)}")

@@ -45,6 +45,7 @@
 #include "level_physics.cuh"
 #include "model.h"
 #include "rt_common.cuh"
+#include "star.cuh"
 
 namespace bgb {
 
@@ -54,12 +55,21 @@ namespace bgb {
 // gS_r = d log L / d s_r, the shift (src/forward_model/forward_model.cpp:161-180) and
 // error-inflation derivatives into the gradient row (zeroing the rest), and per
 // evaluation the seed normaliser 2^-e, its inverse and sum_r gS_r (s_r - shift_r).
+//
+// Secondary eclipse: s_r = p_r / q_r (R_p/R_s)^2 1e6 + shift with p_r the binned planet
+// flux and q_r the binned stellar flux. gS_r then receives d log L / d p_r =
+// d log L / d s_r (R_p/R_s)^2 1e6 / q_r (the seed of the emission adjoint), and the
+// gradient row d/d(R_p/R_s) = sum_r d log L / d s_r 2 (s_r - shift_r) / (R_p/R_s) and
+// d/d(stellar parameters) = -sum_r d log L / d s_r (s_r - shift_r) / q_r dq_r/d theta
+// (blackbody: q_r and dq_r/dT_eff in FP64 from the row's points; grid: the trilinear
+// weights' derivatives, zero where a parameter is clamped or on a node).
 __global__ void __launch_bounds__(256) obs_adjoint_kernel(DeviceModel dm, const double* __restrict__ params, int P,
                                                           const EvalInfo* __restrict__ ev,
                                                           const double* __restrict__ obs, double* __restrict__ gS,
                                                           double* __restrict__ seed, double* __restrict__ grad,
                                                           int transmission) {
-  __shared__ double red[3][256];
+  __shared__ double red[7][256];
+  __shared__ StarCell cell;
   const int b = blockIdx.x, tid = threadIdx.x;
   const int M = dm.M;
   const bool neg = ev[b].neglect != 0;
@@ -75,34 +85,73 @@ __global__ void __launch_bounds__(256) obs_adjoint_kernel(DeviceModel dm, const 
     es_out = es;
     return neg ? 0.0 : __ldg(&dm.row_weight[r]) * d / es;
   };
-  double sgs = 0.0, sinf = 0.0, gmax = 0.0;
+  const int star = dm.star_model;
+  if (star == 3 && tid == 0) cell = star_grid_cell(dm, par + 2);
+  __syncthreads();
+  const double rr = ev[b].radius;
+  double sgs = 0.0, sinf = 0.0, gmax = 0.0, grr = 0.0, gst[3] = {0.0, 0.0, 0.0};
   for (int r = tid; r < M; r += blockDim.x) {
     double s, d, es;
     const double g = row_grad(r, s, d, es);
-    gS[(size_t)b * M + r] = g;
     const int mp = __ldg(&dm.obs_mod_param[__ldg(&dm.row_obs[r])]);
     double pre = s;
     if (mp >= 0) {
       const double sh = par[mp];
       if (sh != 0) pre = s - sh;
     }
-    sgs = fma(g, pre, sgs);
     sinf += __ldg(&dm.row_weight[r]) * 0.5 * (d * d / es - 1.0) / es;
-    gmax = fmax(gmax, fabs(g));
+    if (star) {
+      double q = 0.0, dq[3] = {0.0, 0.0, 0.0};
+      if (star == 1) {
+        const int k0 = __ldg(&dm.row_k0[r]), len = __ldg(&dm.row_len[r]);
+        const double* w = dm.W + __ldg(&dm.row_off[r]);
+        const double teff = par[2];
+        for (int j = 0; j < len; ++j) {
+          const double wj = __ldg(&w[j]);
+          q = fma(wj, star_blackbody_fp64(dm, k0 + j, teff), q);
+          dq[0] = fma(wj, star_blackbody_dT(dm, k0 + j, teff), dq[0]);
+        }
+      } else if (star == 2) {
+        q = __ldg(&dm.star_bin[r]);
+      } else {
+        double v[8], dv[3];
+        for (int i = 0; i < 8; ++i) v[i] = __ldg(&dm.star_bin[(size_t)cell.c[i] * M + r]);
+        q = star_trilinear(v, cell.w);
+        star_trilinear_dw(v, cell.w, dv);
+        for (int a = 0; a < 3; ++a) dq[a] = dv[a] * cell.dw[a];
+      }
+      const double gp = g * rr * rr * 1e6 / q;
+      gS[(size_t)b * M + r] = gp;
+      gmax = fmax(gmax, fabs(gp));
+      grr = fma(g, 2.0 * pre / rr, grr);
+      for (int a = 0; a < 3; ++a) gst[a] = fma(-g * pre / q, dq[a], gst[a]);
+    } else {
+      gS[(size_t)b * M + r] = g;
+      sgs = fma(g, pre, sgs);
+      gmax = fmax(gmax, fabs(g));
+    }
   }
   red[0][tid] = sgs;
   red[1][tid] = sinf;
   red[2][tid] = gmax;
+  red[3][tid] = grr;
+  for (int a = 0; a < 3; ++a) red[4 + a][tid] = gst[a];
   __syncthreads();
   for (int h = blockDim.x / 2; h > 0; h >>= 1) {
     if (tid < h) {
       red[0][tid] += red[0][tid + h];
       red[1][tid] += red[1][tid + h];
       red[2][tid] = fmax(red[2][tid], red[2][tid + h]);
+      for (int a = 3; a < 7; ++a) red[a][tid] += red[a][tid + h];
     }
     __syncthreads();
   }
   const double tot_gs = red[0][0], tot_inf = red[1][0], tot_max = red[2][0];
+  if (tid == 0 && star && !neg) {
+    grad[(size_t)b * P + 1] += red[3][0];
+    const int nst = star == 1 ? 1 : star == 3 ? 3 : 0;
+    for (int a = 0; a < nst; ++a) grad[(size_t)b * P + 2 + a] += red[4 + a][0];
+  }
   __syncthreads();
   // observation shifts: d log L / d shift_o = sum of gS over the observation's rows
   for (int o = 0; o < dm.nobs; ++o) {
@@ -591,8 +640,9 @@ __global__ void __launch_bounds__(kAdjThreads) atmosphere_adjoint_kernel(
           l < L - 1)
         acc = fma(sgl[S + 2], cloud_d, acc);
     }
-    // radius-distance scaling (R_J / d)^2 f, once (chunk 0)
-    if (ch == 0) {
+    // radius-distance scaling (R_J / d)^2 f, once (chunk 0); the secondary eclipse has
+    // none (its R_p / R_s and stellar derivatives come from the likelihood adjoint)
+    if (ch == 0 && dm.star_model == 0) {
       const double gsc = seed[b * 3 + 2] / e.scaling;
       if (th == 1) acc += gsc * (kRJupiter / gen[2]) * (kRJupiter / gen[2]);
       if (th == 2) acc += gsc * (-2.0 * e.scaling / gen[2]);

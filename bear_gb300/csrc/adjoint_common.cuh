@@ -12,13 +12,6 @@
 
 namespace bgb {
 
-#define BGB_CUDA(x)                                                                         \
-  do {                                                                                      \
-    cudaError_t e_ = (x);                                                                   \
-    if (e_ != cudaSuccess)                                                                  \
-      throw Error(BEAR_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));         \
-  } while (0)
-
 constexpr int kAdjThreads = 128;  // threads (wavenumbers) per block of the emission adjoint kernel
 constexpr double kLn10 = 2.302585092994045684;
 

@@ -204,11 +204,19 @@ __global__ void __launch_bounds__(kMaxLevels) atmosphere_kernel(DeviceModel dm, 
     s_bottom = bottom;
     s_cloud_layer = per;
     EvalInfo e;
-    // EmissionModel::radiusDistanceScaling src/forward_model/emission/emission.cpp:108-120
-    double sc = kRJupiter / gen[2];
-    e.scaling = sc * sc * gen[1];
-    e.radius = gen[1];
-    e.star_radius = gen[2];
+    if (c.occultation) {
+      // OccultationModel::calcModelGPU src/forward_model/secondary_eclipse/secondary_eclipse.cpp:262-285:
+      // the planet's spectrum unscaled; radius holds R_p / R_s
+      e.scaling = 1.0;
+      e.radius = gen[1];
+      e.star_radius = 0.0;
+    } else {
+      // EmissionModel::radiusDistanceScaling src/forward_model/emission/emission.cpp:108-120
+      double sc = kRJupiter / gen[2];
+      e.scaling = sc * sc * gen[1];
+      e.radius = gen[1];
+      e.star_radius = gen[2];
+    }
     // Retrieval::logLikelihood error inflation src/retrieval/retrieval.cpp:332-335
     e.inflation = c.error_inflation ? pow(10.0, par[P - 1]) : 0.0;
     e.neglect = s_neglect;

@@ -370,6 +370,39 @@ int bear_loglike_noalloc(bear_model* h, const double* params_dev, int nb_params,
   });
 }
 
+int bear_model_set_priors(bear_model* h, int n, const int* type, const double* a, const double* b,
+                          const double* unit, const int* link) {
+  return guarded([&] {
+    require_ready(h);
+    if (n < 0 || (n > 0 && !type)) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null prior table");
+    bgb::set_priors(h->m, n, type, a, b, unit, link);
+  });
+}
+
+int bear_prior_transform_batch(bear_model* h, const double* cube_dev, int batch, int nb_params,
+                               double* params_dev, void* stream) {
+  return guarded([&] {
+    require_ready(h);
+    require_params(h, nb_params);
+    if (batch < 1) throw bgb::Error(BEAR_ERR_SIZE, "batch must be positive");
+    if (!cube_dev || !params_dev) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null device buffer");
+    bgb::launch_prior_transform(h->m, cube_dev, batch, params_dev, (cudaStream_t)stream);
+  });
+}
+
+int bear_loglike_cube_batch(bear_model* h, const double* cube_dev, int batch, int nb_params, double* params_dev,
+                            double* loglike_dev, uint8_t* neglect_dev, void* stream) {
+  return guarded([&] {
+    require_ready(h);
+    require_params(h, nb_params);
+    if (batch < 1) throw bgb::Error(BEAR_ERR_SIZE, "batch must be positive");
+    if (!cube_dev || !params_dev || !loglike_dev) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null device buffer");
+    const cudaStream_t st = (cudaStream_t)stream;
+    bgb::launch_prior_transform(h->m, cube_dev, batch, params_dev, st);
+    bgb::launch_forward(h->m, params_dev, batch, st, true, neglect_dev, loglike_dev);
+  });
+}
+
 int bear_loglike_grad_batch(bear_model* h, const double* params_dev, int batch, int nb_params,
                             double* loglike_dev, double* grad_dev, uint8_t* neglect_dev,
                             void* stream) {
@@ -450,6 +483,58 @@ int bear_model_autotune(bear_model* h, const double* params_dev, int batch, int 
   });
 }
 
+}  // extern "C"
+
+namespace {
+
+// Captures launch(stream) for a batch of the model into a graph (every allocation
+// happens before the capture).
+template <class F>
+void capture_batch(bear_model* h, int batch, bear_batch_graph** out, F&& launch) {
+  bgb::Model& m = h->m;
+  check_cuda(cudaSetDevice(m.device), "cudaSetDevice");
+  bgb::ensure_workspace(m, batch);  // every allocation happens before the capture
+  const bool saved_prof = m.profiling;
+  m.profiling = false;
+  cudaStream_t s = nullptr;
+  check_cuda(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreateWithFlags");
+  cudaGraph_t graph = nullptr;
+  cudaError_t ce = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (ce != cudaSuccess) {
+    cudaStreamDestroy(s);
+    m.profiling = saved_prof;
+    check_cuda(ce, "cudaStreamBeginCapture");
+  }
+  try {
+    launch(s);
+  } catch (...) {
+    cudaStreamEndCapture(s, &graph);
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamDestroy(s);
+    m.profiling = saved_prof;
+    throw;
+  }
+  m.profiling = saved_prof;
+  ce = cudaStreamEndCapture(s, &graph);
+  cudaStreamDestroy(s);
+  check_cuda(ce, "cudaStreamEndCapture");
+  auto* g = new bear_batch_graph;
+  g->h = h;
+  g->graph = graph;
+  g->generation = m.ws_generation;
+  ce = cudaGraphInstantiate(&g->exec, graph, 0);
+  if (ce != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    delete g;
+    check_cuda(ce, "cudaGraphInstantiate");
+  }
+  *out = g;
+}
+
+}  // namespace
+
+extern "C" {
+
 int bear_batch_graph_create(bear_model* h, const double* params_dev, int batch, int nb_params,
                             double* loglike_dev, uint8_t* neglect_dev, bear_batch_graph** out) {
   return guarded([&] {
@@ -457,44 +542,25 @@ int bear_batch_graph_create(bear_model* h, const double* params_dev, int batch, 
     require_params(h, nb_params);
     if (batch < 1) throw bgb::Error(BEAR_ERR_SIZE, "batch must be positive");
     if (!params_dev || !loglike_dev || !out) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null buffer");
-    bgb::Model& m = h->m;
-    check_cuda(cudaSetDevice(m.device), "cudaSetDevice");
-    bgb::ensure_workspace(m, batch);  // every allocation happens before the capture
-    const bool saved_prof = m.profiling;
-    m.profiling = false;
-    cudaStream_t s = nullptr;
-    check_cuda(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreateWithFlags");
-    cudaGraph_t graph = nullptr;
-    cudaError_t ce = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
-    if (ce != cudaSuccess) {
-      cudaStreamDestroy(s);
-      m.profiling = saved_prof;
-      check_cuda(ce, "cudaStreamBeginCapture");
-    }
-    try {
-      bgb::launch_forward(m, params_dev, batch, s, true, neglect_dev, loglike_dev);
-    } catch (...) {
-      cudaStreamEndCapture(s, &graph);
-      if (graph) cudaGraphDestroy(graph);
-      cudaStreamDestroy(s);
-      m.profiling = saved_prof;
-      throw;
-    }
-    m.profiling = saved_prof;
-    ce = cudaStreamEndCapture(s, &graph);
-    cudaStreamDestroy(s);
-    check_cuda(ce, "cudaStreamEndCapture");
-    auto* g = new bear_batch_graph;
-    g->h = h;
-    g->graph = graph;
-    g->generation = m.ws_generation;
-    ce = cudaGraphInstantiate(&g->exec, graph, 0);
-    if (ce != cudaSuccess) {
-      cudaGraphDestroy(graph);
-      delete g;
-      check_cuda(ce, "cudaGraphInstantiate");
-    }
-    *out = g;
+    capture_batch(h, batch, out, [&](cudaStream_t s) {
+      bgb::launch_forward(h->m, params_dev, batch, s, true, neglect_dev, loglike_dev);
+    });
+  });
+}
+
+int bear_batch_graph_create_cube(bear_model* h, const double* cube_dev, int batch, int nb_params,
+                                 double* params_dev, double* loglike_dev, uint8_t* neglect_dev,
+                                 bear_batch_graph** out) {
+  return guarded([&] {
+    require_ready(h);
+    require_params(h, nb_params);
+    if (batch < 1) throw bgb::Error(BEAR_ERR_SIZE, "batch must be positive");
+    if (!cube_dev || !params_dev || !loglike_dev || !out) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null buffer");
+    if (h->m.n_priors != h->m.acfg.nparam_total) throw bgb::Error(BEAR_ERR_STATE, "no priors set (bear_model_set_priors)");
+    capture_batch(h, batch, out, [&](cudaStream_t s) {
+      bgb::launch_prior_transform(h->m, cube_dev, batch, params_dev, s);
+      bgb::launch_forward(h->m, params_dev, batch, s, true, neglect_dev, loglike_dev);
+    });
   });
 }
 

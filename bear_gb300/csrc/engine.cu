@@ -43,15 +43,9 @@
 #include "model.h"
 #include "physics.cuh"
 #include "rt_common.cuh"
+#include "star.cuh"
 
 namespace bgb {
-
-#define BGB_CUDA(x)                                                                         \
-  do {                                                                                      \
-    cudaError_t e_ = (x);                                                                   \
-    if (e_ != cudaSuccess)                                                                  \
-      throw Error(BEAR_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));         \
-  } while (0)
 
 __global__ void atmosphere_kernel(DeviceModel dm, const double* __restrict__ params, int P,
                                   LevelInfo* __restrict__ lev, LevelSpecies* __restrict__ ls,
@@ -386,22 +380,58 @@ __device__ __forceinline__ double warp_sum(double v) {
 // (Observation::processModelSpectrum src/observations/observations.cpp:290-304,
 // ForwardModel::applyObservationModifier src/forward_model/forward_model.cpp:161-180,
 // Retrieval::logLikelihood src/retrieval/retrieval.cpp:314-369).
+//
+// Secondary eclipse (OccultationModel::calcModelGPU src/forward_model/secondary_eclipse/
+// secondary_eclipse.cpp:262-335, OccultationDevice src/CUDA_kernels/secondary_eclipse_kernels.cu:35-51):
+// each row is binned planet flux / binned stellar flux x (R_p / R_s)^2 x 1e6 before the shift.
+// The blackbody star is binned here from its point values (double-float, or FP64 when fp64
+// is set); file and grid stars use their precomputed binned rows (the grid's eight corners
+// interpolated per evaluation).
 __global__ void obs_loglike_kernel(DeviceModel dm, const double* __restrict__ spectrum,
                                    const double* __restrict__ params, int P,
                                    const EvalInfo* __restrict__ ev, double* __restrict__ obs,
-                                   double* __restrict__ loglike, uint8_t* __restrict__ neglect_out) {
+                                   double* __restrict__ loglike, uint8_t* __restrict__ neglect_out, int fp64) {
   const int b = blockIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const double* F = spectrum + (size_t)b * dm.N;
   const double infl = ev[b].inflation;
+  const int star = dm.star_model;
+  __shared__ ExpTables et;
+  __shared__ StarCell cell;
+  double teff = 0.0;
+  df2 invT = {0.0f, 0.0f};
+  if (star == 1) {
+    load_exp_tables(et);
+    teff = params[(size_t)b * P + 2];
+    const double it = 1.0 / teff;
+    invT.hi = (float)it;
+    invT.lo = (float)(it - (double)invT.hi);
+  } else if (star == 3 && threadIdx.x == 0) {
+    cell = star_grid_cell(dm, params + (size_t)b * P + 2);
+  }
+  if (star) __syncthreads();
   double acc = 0.0;
   for (int r = warp; r < dm.M; r += nw) {
     const int k0 = __ldg(&dm.row_k0[r]), len = __ldg(&dm.row_len[r]);
     const double* w = dm.W + __ldg(&dm.row_off[r]);
-    double s = 0.0;
+    double s = 0.0, ss = 0.0;
     for (int j = lane; j < len; j += 32) s += __ldg(&w[j]) * F[k0 + j];
+    if (star == 1)
+      for (int j = lane; j < len; j += 32)
+        ss += __ldg(&w[j]) * (fp64 ? star_blackbody_fp64(dm, k0 + j, teff) : star_blackbody_df(dm, k0 + j, invT, et));
     s = warp_sum(s);
+    if (star == 1) ss = warp_sum(ss);
     if (lane == 0) {
+      if (star) {
+        if (star == 2) ss = __ldg(&dm.star_bin[r]);
+        else if (star == 3) {
+          double v[8];
+          for (int i = 0; i < 8; ++i) v[i] = __ldg(&dm.star_bin[(size_t)cell.c[i] * dm.M + r]);
+          ss = star_trilinear(v, cell.w);
+        }
+        const double rr = ev[b].radius;
+        s = s / ss * rr * rr * 1e6;
+      }
       const int mp = __ldg(&dm.obs_mod_param[__ldg(&dm.row_obs[r])]);
       if (mp >= 0) {
         const double shift = params[(size_t)b * P + mp];
@@ -429,12 +459,29 @@ __global__ void obs_loglike_kernel(DeviceModel dm, const double* __restrict__ sp
 }
 
 // High-resolution output of the plain path (RadiativeTransfer::changeSpectrumUnits
-// src/radiative_transfer/radiative_transfer.h:58-60 for emission; transit depth as is).
+// src/radiative_transfer/radiative_transfer.h:58-60 for emission; transit depth as is;
+// for the secondary eclipse planet / star x (R_p / R_s)^2 x 1e6,
+// src/forward_model/secondary_eclipse/secondary_eclipse.cpp:326-332). Evaluation 0.
 __global__ void spectrum_output_kernel(DeviceModel dm, const double* __restrict__ spectrum,
-                                       int emission, double* __restrict__ out) {
+                                       int emission, const double* __restrict__ params,
+                                       const EvalInfo* __restrict__ ev, double* __restrict__ out) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= dm.N) return;
   const double f = spectrum[k];
+  if (dm.star_model) {
+    double st;
+    if (dm.star_model == 1) st = star_blackbody_fp64(dm, k, params[2]);
+    else if (dm.star_model == 2) st = dm.star_hr[k];
+    else {
+      const StarCell c = star_grid_cell(dm, params + 2);
+      double v[8];
+      for (int i = 0; i < 8; ++i) v[i] = dm.star_hr[(size_t)c.c[i] * dm.N + k];
+      st = star_trilinear(v, c.w);
+    }
+    const double rr = ev[0].radius;
+    out[k] = f / st * rr * rr * 1e6;
+    return;
+  }
   out[k] = emission ? f / dm.wl[k] / dm.wl[k] * 10000.0 : f;
 }
 
@@ -678,6 +725,11 @@ void upload_model(Model& m) {
   dm.row_weight = dev_upload(m, wgt);
   dm.row_logterm = dev_upload(m, logt);
   dm.obs_mod_param = dev_upload(m, modp);
+  dm.star_model = m.occultation ? m.star_model : 0;
+  for (int a = 0; a < 3; ++a) dm.star_n[a] = m.star_n[a];
+  dm.star_axes = m.star_axes.empty() ? nullptr : dev_upload(m, m.star_axes);
+  dm.star_hr = m.star_hr.empty() ? nullptr : dev_upload(m, m.star_hr);
+  dm.star_bin = m.star_bin.empty() ? nullptr : dev_upload(m, m.star_bin);
   {
     // first row of each observation, and the operator transposed (rows reading
     // each wavenumber, in ascending row order) for the adjoint
@@ -813,7 +865,7 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
   if (profile) BGB_CUDA(cudaEventRecord(m.ev[2], st));
   const int OT = m.obs_threads > 0 ? m.obs_threads : 256;
   obs_loglike_kernel<<<batch, OT, 0, st>>>(dm, w.spectrum, params_dev, dm.P, w.ev, w.obs, loglike_dev,
-                                          neglect_dev);
+                                          neglect_dev, m.precision == 1);
   BGB_CUDA(cudaGetLastError());
   if (profile) BGB_CUDA(cudaEventRecord(m.ev[3], st));
 }
@@ -885,7 +937,8 @@ long long stencil_rows(Model& m, int batch) {
 }
 
 void launch_spectrum_output(Model& m, double* out_dev, cudaStream_t st) {
-  spectrum_output_kernel<<<(m.dm.N + 255) / 256, 256, 0, st>>>(m.dm, m.ws.spectrum, m.transmission ? 0 : 1, out_dev);
+  spectrum_output_kernel<<<(m.dm.N + 255) / 256, 256, 0, st>>>(m.dm, m.ws.spectrum, m.transmission ? 0 : 1,
+                                                              m.ws.params, m.ws.ev, out_dev);
   BGB_CUDA(cudaGetLastError());
 }
 

@@ -45,6 +45,7 @@ constexpr int kMaxPolyDof = 64;
 struct AtmosphereConfig {
   int L;                       // levels, index 0 = bottom (highest pressure)
   int transmission;            // 0 emission, 1 transmission
+  int occultation;             // 1: secondary eclipse (emission with spectrum scaling 1)
   int nparam_general, nparam_chem, nparam_temp, nparam_cloud, nparam_mod, nparam_total;
   int error_inflation;
   // temperature: 0 const, 1 piecewise polynomial in log10 p
@@ -122,6 +123,17 @@ struct __align__(16) EvalInfo {
   int pad;
 };
 
+// One parameter's prior on the device (Retrieval's PriorConfig list). a, b: uniform
+// bounds (ordered), log10 of the log-uniform bounds (ordered), Gaussian mean and
+// standard deviation, or the delta value; link: the linked parameter (linked priors).
+enum PriorType : int { kPriorUniform = 0, kPriorLogUniform = 1, kPriorGaussian = 2, kPriorDelta = 3, kPriorLinked = 4 };
+constexpr int kMaxPriors = 256;
+struct DevicePrior {
+  int type;
+  int link;
+  double a, b, unit;
+};
+
 // Device pointers and sizes for the kernels (passed by value).
 struct DeviceModel {
   const AtmosphereConfig* cfg;
@@ -168,6 +180,13 @@ struct DeviceModel {
   const int* col_ptr;         // N + 1
   const int* col_row;         // nnz
   const double* col_w;        // nnz
+  // secondary eclipse: the stellar spectrum (star_model 1 blackbody at T_eff = params[2],
+  // 2 file, 3 grid over (T_eff, log g, [M/H]) = params[2..4]); 0 for other models
+  int star_model;
+  int star_n[3];              // grid: nodes per axis
+  const double* star_axes;    // grid: star_n[0] + star_n[1] + star_n[2] ascending nodes
+  const double* star_hr;      // file: N; grid: spectra x N, spectrum (t, g, m) at (t n1 + g) n2 + m
+  const double* star_bin;     // file: M; grid: spectra x M: the stellar spectrum through each row
 };
 
 // Work buffers for a batch of evaluations.
@@ -276,6 +295,9 @@ struct Model {
   std::vector<ChemModule> chem;
   bool cloud = false, cloud_fb = false;
   bool fit_mmw = false, fit_sh = false, var_g = false;
+  bool occultation = false;
+  int star_model = 0;             // 1 blackbody, 2 file, 3 grid
+  std::string star_path;          // file path (2) or grid folder (3)
   std::vector<std::pair<std::string, std::string>> opac_cfg;
   // set-up products
   std::vector<ObservationSetup> obs;
@@ -291,6 +313,11 @@ struct Model {
   long long n_lrows = 0;             // rows of the level table
   std::vector<double> table_host;    // n_rows x N (freed after upload)
   std::vector<double> W;             // concatenated operator weights
+  // stellar spectrum of the secondary-eclipse model (file: 1 spectrum; grid: all)
+  std::vector<double> star_hr;       // spectra x N on the model grid
+  std::vector<double> star_bin;      // spectra x M through the observation rows
+  std::vector<double> star_axes;
+  int star_n[3] = {0, 0, 0};
   int M = 0;
   int nparam_general = 0, nparam_chem = 0, nparam_temp = 0, nparam_cloud = 0, nparam_mod = 0;
   int nparam_total = 0;
@@ -315,6 +342,8 @@ struct Model {
   Workspace ws;
   GradWorkspace gws;
   size_t grad_budget = size_t(16) << 30;  // bytes of gradient work buffers per chunk
+  DevicePrior* d_priors = nullptr;  // prior table (bear_model_set_priors)
+  int n_priors = 0;
   double* h_pinned = nullptr;  // pinned staging for the plain path
   size_t h_pinned_bytes = 0;
   // stage timing (bear_model_set_profiling)
@@ -347,6 +376,10 @@ void loglike_noalloc(Model& m, const double* params_dev, double* loglike_dev, ui
 long long stencil_rows(Model& m, int batch);
 void launch_forward_taps(Model& m, const double* params_dev, int batch, cudaStream_t stream,
                          uint8_t* neglect_dev, double* loglike_dev, const ForwardTaps& taps);
+// priors.cu
+void set_priors(Model& m, int n, const int* type, const double* a, const double* b, const double* unit,
+                const int* link);
+void launch_prior_transform(Model& m, const double* cube_dev, int batch, double* params_dev, cudaStream_t stream);
 // adjoint.cu
 void launch_gradient(Model& m, const double* params_dev, int batch, cudaStream_t stream,
                      double* loglike_dev, double* grad_dev, uint8_t* neglect_dev);
@@ -358,5 +391,15 @@ struct Error : std::exception {
   Error(int c, std::string s) : code(c), msg(std::move(s)) {}
   const char* what() const noexcept override { return msg.c_str(); }
 };
+
+// Throws Error(BEAR_ERR_CUDA) with the failing call and CUDA's message (the
+// BEAR_ERR_* codes come from include/bear_gb300.h, which users of the macro include).
+#define BGB_CUDA(x)                                                                         \
+  do {                                                                                      \
+    cudaError_t e_ = (x);                                                                   \
+    if (e_ != cudaSuccess)                                                                  \
+      throw Error(BEAR_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));         \
+  } while (0)
+
 
 }  // namespace bgb

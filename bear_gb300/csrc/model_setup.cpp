@@ -56,9 +56,12 @@ void parse_config(Model& m, const std::string& text) {
     };
     if (k == "forward_model") {
       need(2);
+      // Retrieval::selectForwardModel src/retrieval/select_forward_model.cpp:38-150
       if (t[1] == "emission") m.transmission = false;
       else if (t[1] == "transmission") m.transmission = true;
-      else throw unsupported("forward model " + t[1] + " is not supported (emission, transmission)");
+      else if (t[1] == "secondary_eclipse" || t[1] == "Secondary_eclipse" || t[1] == "se") m.occultation = true;
+      else
+        throw unsupported("forward model " + t[1] + " is not supported (emission, transmission, secondary_eclipse)");
     } else if (k == "cross_section_path") {
       m.xsec_path = t.size() > 1 ? t[1] : "";
     } else if (k == "wavenumber_file") {
@@ -96,6 +99,21 @@ void parse_config(Model& m, const std::string& text) {
         m.temp_poly = false;
       } else {
         throw unsupported("temperature profile " + t[1] + " is not supported (poly, const)");
+      }
+    } else if (k == "stellar_spectrum") {
+      need(2);
+      // selectStellarModel src/forward_model/stellar_spectrum/select_stellar_model.h:52-122
+      if (t[1] == "blackbody") {
+        if (t.size() != 2) throw invalid("Stellar blackbody model requires no parameters!");
+        m.star_model = 1;
+      } else if (t[1] == "file" || t[1] == "grid") {
+        if (t.size() != 3)
+          throw invalid(t[1] == "file" ? "Stellar model requires one parameter (the file path)!"
+                                       : "Stellar grid model requires one parameter (the parameter file path)!");
+        m.star_model = t[1] == "file" ? 2 : 3;
+        m.star_path = t[2];
+      } else {
+        throw invalid("Stellar model " + t[1] + " unknown!");
       }
     } else if (k == "radiative_transfer") {
       need(2);
@@ -151,6 +169,8 @@ void parse_config(Model& m, const std::string& text) {
     }
   }
   if (m.fit_sh) throw unsupported("fit_scale_height is not supported");
+  if (m.occultation && m.star_model == 0) throw invalid("the secondary-eclipse model needs a stellar_spectrum");
+  if (!m.occultation && m.star_model != 0) throw invalid("stellar_spectrum applies to the secondary-eclipse model only");
   if (m.L < 2 || m.L > kMaxLevels) throw invalid("nb_grid_points must be in [2, 512]");
   if (!(m.pbot > m.ptop) || !(m.ptop > 0)) throw invalid("atmos_boundaries must be bottom > top > 0");
 }
@@ -677,6 +697,7 @@ static void setup_atmosphere(Model& m) {
   for (int i = 0; i < L; ++i) m.log10p[i] = std::log10(m.p[i]);
   a.L = L;
   a.transmission = m.transmission;
+  a.occultation = m.occultation;
   a.temp_poly = m.temp_poly;
   if (m.temp_poly) {
     // PiecewisePolynomial src/additional/piecewise_poly.cpp:36-121 (node table :36-44)
@@ -770,6 +791,129 @@ static void setup_atmosphere(Model& m) {
   for (int r = 0; r < a.R; ++r) a.ray_index[r] = m.opac[m.rayleigh_species[r]].index;
 }
 
+// ------------------------------------------------------------------ stellar spectrum
+static std::vector<float> read_floats(const std::string& path, const char* what) {
+  std::ifstream f(path, std::ios::binary | std::ios::ate);
+  if (!f) throw Error(BEAR_ERR_FILE, std::string(what) + " " + path + " not found");
+  const std::streamoff n = f.tellg() / (std::streamoff)sizeof(float);
+  std::vector<float> v((size_t)n);
+  f.seekg(0);
+  f.read(reinterpret_cast<char*>(v.data()), n * (std::streamoff)sizeof(float));
+  return v;
+}
+
+// StarSpectrumFile::readSpectrum src/forward_model/stellar_spectrum/star_file_spectrum.cpp:85-130:
+// "wavelength flux" lines (W m^-2 um^-1), converted to W m^-2 cm (x wl^2 / 1e4) and
+// interpolated linearly onto the model's wavelengths (zero outside the file's range).
+static void load_star_file(Model& m) {
+  std::ifstream f(m.star_path);
+  if (!f) throw Error(BEAR_ERR_FILE, "stellar spectrum file " + m.star_path + " not found");
+  std::vector<double> x, y;
+  std::string line;
+  while (std::getline(f, line)) {
+    std::istringstream ls(line);
+    double a, b;
+    if (!(ls >> a >> b)) continue;
+    x.push_back(a);
+    y.push_back(b);
+  }
+  if (x.size() < 2) throw invalid("stellar spectrum file " + m.star_path + " has fewer than two points");
+  for (size_t i = 0; i < y.size(); ++i) y[i] = y[i] * x[i] * x[i] / 10000.;
+  m.star_hr = interp_to_wavelengths(x, y, m.wl.data(), m.N);
+}
+
+// StellarSpectrumGrid src/forward_model/stellar_spectrum/stellar_spectrum_grid.cpp:42-210:
+// <folder>grid_parameters.dat holds the T_eff, log g and [M/H] nodes (one line each), the
+// name of the float32 wavelength file, then one "T_eff log_g [M/H] file" line per spectrum
+// (float32 fluxes). Every spectrum is sampled onto the model grid here
+// (SampledStellarSpectrum::sampleSpectrum sampled_stellar_spectrum.cpp:47-80: x wl^2 / 1e4,
+// linear interpolation, values below 1e-37 raised to 1e-37), once, instead of on first use.
+// As in the reference, a folder path without a trailing '/' is extended with '+'.
+static void load_star_grid(Model& m) {
+  std::string folder = m.star_path;
+  if (folder.empty() || folder.back() != '/') folder += "+";
+  const std::string pfile = folder + "grid_parameters.dat";
+  std::ifstream f(pfile);
+  if (!f) throw Error(BEAR_ERR_FILE, "stellar grid parameter file " + pfile + " not found");
+  std::vector<double> axis[3];
+  std::string line;
+  for (int a = 0; a < 3; ++a) {
+    std::getline(f, line);
+    std::istringstream ls(line);
+    double v;
+    while (ls >> v) axis[a].push_back(v);
+    if (axis[a].empty()) throw invalid("stellar grid " + pfile + ": an empty parameter line");
+    for (size_t i = 1; i < axis[a].size(); ++i)
+      if (!(axis[a][i] > axis[a][i - 1])) throw invalid("stellar grid " + pfile + ": nodes must ascend");
+  }
+  std::string wl_name;
+  f >> wl_name;
+  std::getline(f, line);
+  std::vector<std::string> entries;
+  while (std::getline(f, line)) entries.push_back(line);
+  const size_t n0 = axis[0].size(), n1 = axis[1].size(), n2 = axis[2].size();
+  if (entries.size() != n0 * n1 * n2)
+    throw invalid("Stellar spectrum grid is inconsistent. The number of files does not correspond to the number "
+                  "of given effective temperatures, log g, and metallicities!");
+  const std::vector<float> wlf = read_floats(folder + wl_name, "stellar grid wavelength file");
+  std::vector<double> gwl(wlf.begin(), wlf.end());
+  m.star_hr.assign(n0 * n1 * n2 * m.N, 0.0);
+  std::vector<char> seen(n0 * n1 * n2, 0);
+  for (const std::string& e : entries) {
+    std::istringstream ls(e);
+    double v[3];
+    std::string name;
+    if (!(ls >> v[0] >> v[1] >> v[2] >> name)) throw invalid("stellar grid " + pfile + ": bad line '" + e + "'");
+    size_t idx[3];
+    for (int a = 0; a < 3; ++a) {
+      auto it = std::find(axis[a].begin(), axis[a].end(), v[a]);
+      if (it == axis[a].end()) throw invalid("stellar grid " + pfile + ": a spectrum off the parameter nodes");
+      idx[a] = (size_t)(it - axis[a].begin());
+    }
+    const size_t c = (idx[0] * n1 + idx[1]) * n2 + idx[2];
+    if (seen[c]) throw invalid("Stellar spectra grid seems to be incomplete. Possibly duplicates?");
+    seen[c] = 1;
+    const std::vector<float> fl = read_floats(folder + name, "stellar grid spectrum");
+    if (fl.size() != gwl.size())
+      throw invalid("spectrum file " + folder + name + " has an incorrect number of spectral points");
+    std::vector<double> y(fl.size());
+    for (size_t i = 0; i < y.size(); ++i) y[i] = (double)fl[i] * gwl[i] * gwl[i] / 10000.;
+    std::vector<double> s = interp_to_wavelengths(gwl, y, m.wl.data(), m.N);
+    for (double& q : s)
+      if (q < 1e-37) q = 1e-37;
+    std::copy(s.begin(), s.end(), m.star_hr.begin() + c * m.N);
+  }
+  m.star_axes.clear();
+  for (int a = 0; a < 3; ++a) {
+    m.star_n[a] = (int)axis[a].size();
+    m.star_axes.insert(m.star_axes.end(), axis[a].begin(), axis[a].end());
+  }
+}
+
+// Stellar spectra through the observation operator: the binned stellar flux of every
+// operator row (the binning is linear, so the grid model interpolates these instead of
+// binning an interpolated spectrum).
+static void setup_star(Model& m) {
+  m.star_hr.clear();
+  m.star_bin.clear();
+  if (m.star_model == 2) load_star_file(m);
+  else if (m.star_model == 3) load_star_grid(m);
+  else return;
+  const size_t ns = m.star_hr.size() / m.N;
+  m.star_bin.assign(ns * (size_t)m.M, 0.0);
+  for (size_t c = 0; c < ns; ++c) {
+    const double* F = m.star_hr.data() + c * m.N;
+    size_t r = 0;
+    for (const auto& o : m.obs)
+      for (int b = 0; b < o.n; ++b, ++r) {
+        double s = 0.0;
+        const double* w = m.W.data() + o.row_off[b];
+        for (int j = 0; j < o.row_len[b]; ++j) s += w[j] * F[o.row_k0[b] + j];
+        m.star_bin[c * m.M + r] = s;
+      }
+  }
+}
+
 void finalize_host(Model& m) {
   if (m.prepared) throw Error(BEAR_ERR_STATE, "model already prepared");
   if (m.obs.empty()) throw invalid("No observations given");
@@ -783,10 +927,14 @@ void finalize_host(Model& m) {
   }
   setup_opacity(m);
   for (auto& o : m.obs) build_observation_operator(m, o);
+  setup_star(m);
   setup_atmosphere(m);
   // parameter layout: EmissionModel::extractParameters src/forward_model/emission/emission.cpp:123-153,
-  // TransmissionModel::extractParameters src/forward_model/transmission/transmission.cpp:110-146
+  // TransmissionModel::extractParameters src/forward_model/transmission/transmission.cpp:110-146,
+  // OccultationModel::extractParameters src/forward_model/secondary_eclipse/secondary_eclipse.cpp:115-150
+  // ([log g, R_p / R_s] and the stellar model's parameters; both counted as general here)
   m.nparam_general = 3 + ((m.transmission && m.fit_mmw) ? 1 : 0);
+  if (m.occultation) m.nparam_general = 2 + (m.star_model == 1 ? 1 : m.star_model == 3 ? 3 : 0);
   m.nparam_chem = 0;
   for (auto& c : m.chem) m.nparam_chem += c.kind == 0 ? (int)c.sp.size() : 0;
   m.nparam_cloud = m.cloud ? (m.cloud_fb ? 2 : 3) : 0;

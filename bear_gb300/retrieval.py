@@ -61,6 +61,7 @@ class Engine:
                     _lib.dptr(w), _lib.dptr(f), nf, _lib.dptr(fw), _lib.dptr(fr),
                     (o.detector or "").encode(), (o.modifier or "").encode()))
             _lib.check(lib.bear_model_prepare(h) if prepare_only else lib.bear_model_finalize(h))
+            self.finalized = not prepare_only
         except Exception:
             lib.bear_model_destroy(h)
             self._h = None
@@ -155,6 +156,58 @@ class Engine:
         self.loglike_batch_ptr(t.data_ptr(), B, ll.data_ptr(), ng.data_ptr(),
                                torch.cuda.current_stream(t.device).cuda_stream)
         return ll, ng
+
+    # ------------------------------------------------------------ priors on the device
+    _PRIOR_TYPES = {"uniform": 0, "log_uniform": 1, "gaussian": 2, "delta": 3, "linked": 4}
+
+    def set_priors(self, priors: Sequence[Prior]) -> None:
+        """Upload one prior per parameter (pyBeAR Prior objects; "linked" priors take the
+        1-based index of the parameter they follow, as the reference's config)."""
+        n = len(priors)
+        typ = np.zeros(n, dtype=np.int32)
+        a, b, u = np.zeros(n), np.zeros(n), np.ones(n)
+        link = np.full(n, -1, dtype=np.int32)
+        for i, p in enumerate(priors):
+            if p.type not in self._PRIOR_TYPES:
+                raise ValueError(f"Prior type {p.type} for {p.description} unknown!")
+            typ[i] = self._PRIOR_TYPES[p.type]
+            if p.type == "linked":
+                link[i] = int(p.parameter[0]) - 1
+                continue
+            a[i] = p.parameter[0]
+            b[i] = p.parameter[1] if len(p.parameter) > 1 else 0.0
+            if p.unit not in UNITS:
+                raise ValueError(f"Unit {p.unit} for parameter {p.description} unknown!")
+            u[i] = UNITS[p.unit]
+        ip = C.POINTER(C.c_int)
+        _lib.check(self._lib.bear_model_set_priors(self._h, n, typ.ctypes.data_as(ip), _lib.dptr(a), _lib.dptr(b),
+                                                   _lib.dptr(u), link.ctypes.data_as(ip)))
+
+    def prior_transform_batch(self, cube):
+        """cube: torch float64 CUDA tensor (B, P) in [0, 1]. Returns the physical parameters."""
+        import torch
+        t = cube.contiguous()
+        assert t.dtype == torch.float64 and t.is_cuda and t.shape[1] == self.P
+        out = torch.empty_like(t)
+        _lib.check(self._lib.bear_prior_transform_batch(self._h, C.c_void_p(t.data_ptr()), t.shape[0], self.P,
+                                                        C.c_void_p(out.data_ptr()),
+                                                        C.c_void_p(torch.cuda.current_stream(t.device).cuda_stream)))
+        return out
+
+    def loglike_cube_batch(self, cube):
+        """cube: torch float64 CUDA tensor (B, P). Returns (loglike, neglect, physical parameters)."""
+        import torch
+        t = cube.contiguous()
+        assert t.dtype == torch.float64 and t.is_cuda and t.shape[1] == self.P
+        B = t.shape[0]
+        par = torch.empty_like(t)
+        ll = torch.empty(B, dtype=torch.float64, device=t.device)
+        ng = torch.empty(B, dtype=torch.uint8, device=t.device)
+        _lib.check(self._lib.bear_loglike_cube_batch(self._h, C.c_void_p(t.data_ptr()), B, self.P,
+                                                     C.c_void_p(par.data_ptr()), C.c_void_p(ll.data_ptr()),
+                                                     C.c_void_p(ng.data_ptr()),
+                                                     C.c_void_p(torch.cuda.current_stream(t.device).cuda_stream)))
+        return ll, ng, par
 
     def grad_batch(self, params):
         """params: torch float64 CUDA tensor (B, P). Returns (loglike (B,), d loglike / d params
@@ -330,15 +383,27 @@ def _erfinv(y: float) -> float:
 
 
 class Priors:
-    """Prior transforms of src/retrieval/prior_types.h:89-230 (uniform, log-uniform,
-    Gaussian, delta) with the unit factors of :57-82."""
+    """Prior transforms of src/retrieval/prior_types.h:89-256 (uniform, log-uniform,
+    Gaussian, delta, linked) with the unit factors of :57-82. A linked prior
+    (parameter = 1-based index of another, non-linked parameter; Priors::setupLinkedPriors
+    src/retrieval/priors.cpp:246-280) takes that parameter's prior at that parameter's
+    cube coordinate and carries no unit (Retrieval::convertHypercubeParameters
+    src/retrieval/multinest_loglike.cpp:59-97)."""
 
     def __init__(self, priors: Sequence[Prior]):
         self.priors = list(priors)
-        for p in self.priors:
-            if p.type not in ("uniform", "log_uniform", "gaussian", "delta"):
-                raise ValueError(f"prior type {p.type} is not supported")
-            if p.unit not in UNITS:
+        self.links = [-1] * len(self.priors)
+        for i, p in enumerate(self.priors):
+            if p.type not in ("uniform", "log_uniform", "gaussian", "delta", "linked"):
+                raise ValueError(f"Prior type {p.type} for {p.description} unknown!")
+            if p.type == "linked":
+                j = int(p.parameter[0]) - 1
+                if not 0 <= j < len(self.priors):
+                    raise ValueError(f"Linked prior {p.description} wrong index for link!")
+                if self.priors[j].type == "linked":
+                    raise ValueError(f"Linked prior {p.description} Can not link prior to another linked prior!")
+                self.links[i] = j
+            elif p.unit not in UNITS:
                 raise ValueError(f"Unit {p.unit} for parameter {p.description} unknown!")
 
     def __len__(self):
@@ -346,7 +411,10 @@ class Priors:
 
     def cube_to_parameters(self, cube: Sequence[float]) -> List[float]:
         out = []
-        for p, u in zip(self.priors, cube):
+        for i, p in enumerate(self.priors):
+            u = cube[i]
+            if self.links[i] >= 0:
+                p, u = self.priors[self.links[i]], cube[self.links[i]]
             if p.type == "uniform":
                 lo, hi = sorted(p.parameter)
                 out.append(lo + u * (hi - lo))
@@ -360,22 +428,25 @@ class Priors:
         return out
 
     def to_physical(self, params: Sequence[float]) -> List[float]:
-        return [v * UNITS[p.unit] for p, v in zip(self.priors, params)]
+        return [v * (1.0 if p.type == "linked" else UNITS[p.unit]) for p, v in zip(self.priors, params)]
 
     def cube_to_physical_batch(self, cube: np.ndarray) -> np.ndarray:
         cube = np.atleast_2d(np.asarray(cube, dtype=np.float64))
         out = np.empty_like(cube)
         for j, p in enumerate(self.priors):
-            u = UNITS[p.unit]
+            c = cube[:, j]
+            u = UNITS[p.unit] if p.type != "linked" else 1.0
+            if self.links[j] >= 0:
+                p, c = self.priors[self.links[j]], cube[:, self.links[j]]
             if p.type == "uniform":
                 lo, hi = sorted(p.parameter)
-                out[:, j] = (lo + cube[:, j] * (hi - lo)) * u
+                out[:, j] = (lo + c * (hi - lo)) * u
             elif p.type == "log_uniform":
                 lo, hi = sorted(np.log10(p.parameter))
-                out[:, j] = np.power(10.0, lo + cube[:, j] * (hi - lo)) * u
+                out[:, j] = np.power(10.0, lo + c * (hi - lo)) * u
             elif p.type == "gaussian":
                 from scipy.special import erfinv
-                out[:, j] = (p.parameter[0] + p.parameter[1] * np.sqrt(2.0) * erfinv(2.0 * cube[:, j] - 1.0)) * u
+                out[:, j] = (p.parameter[0] + p.parameter[1] * np.sqrt(2.0) * erfinv(2.0 * c - 1.0)) * u
             else:
                 out[:, j] = p.parameter[0] * u
         return out
@@ -395,6 +466,8 @@ class Retrieval:
         self.priors = Priors(priors)
         if len(self.priors) != self.engine.P:
             raise ValueError(f"Found {len(self.priors)} priors config but expected {self.engine.P}")
+        if self.engine.finalized:
+            self.engine.set_priors(self.priors.priors)
         self.spectral_grid = SpectralGrid(self.engine.wavenumbers)
         self.nb_observations = self.engine.nobs
 
@@ -420,6 +493,17 @@ class Retrieval:
             out.spectrum_obs.append(list(obs[off:off + n]))
             off += n
         return out
+
+    def computeLikelihoodCubeBatch(self, cube):
+        """Log L of a batch of hypercube points (B x P, a torch CUDA tensor or an array):
+        the prior transform runs on the device. Returns (log L, physical parameters) as
+        torch tensors on the device."""
+        import torch
+        t = torch.as_tensor(cube, dtype=torch.float64)
+        if not t.is_cuda:
+            t = t.to(f"cuda:{self.engine.device}")
+        ll, ng, par = self.engine.loglike_cube_batch(t)
+        return ll, par
 
     def computeLikelihoodBatch(self, physical_parameters) -> np.ndarray:
         import torch

@@ -31,7 +31,8 @@ from typing import Callable, Dict, List, Optional, Sequence, Tuple
 
 import numpy as np
 
-from .config import Config, EmissionModelConfig, Observation, Prior, TransmissionModelConfig
+from .config import (Config, EmissionModelConfig, Observation, OccultationConfig, Prior,
+                     TransmissionModelConfig)
 
 PARSEC = 3.08567758135e18
 R_JUPITER = 7.1492e9
@@ -402,3 +403,104 @@ def attach_data(obs: List[Observation], model_obs: Sequence[np.ndarray], kind: s
             data = m + 50.0 * rng.standard_normal(m.shape)
         o.data = list(data)
         o.data_error = list(err)
+
+
+# --------------------------------------------------------------------------- secondary eclipse
+# Stellar spectra for the secondary-eclipse model: surface flux in W m^-2 um^-1 (the
+# reference's stellar file unit), pi B_lambda(T_eff) with seeded absorption lines whose
+# depth grows with [M/H] and whose width grows with log g.
+
+_H, _C, _K = 6.62606896e-34, 2.99792458e8, 1.3806504e-23   # SI
+
+
+def star_spectrum(teff: float, log_g: float = 4.5, metallicity: float = 0.0, n: int = 3000,
+                  wl_min: float = 0.3, wl_max: float = 30.0, seed: int = 5) -> Tuple[np.ndarray, np.ndarray]:
+    """(wavelengths in um ascending, flux in W m^-2 um^-1) of a synthetic star."""
+    wl = np.geomspace(wl_min, wl_max, n)
+    lam = wl * 1e-6
+    b_lambda = 2.0 * _H * _C**2 / lam**5 / np.expm1(_H * _C / (lam * _K * teff)) * 1e-6
+    rng = np.random.default_rng(seed)
+    centres = np.geomspace(wl_min, wl_max, 60) * np.exp(rng.uniform(-0.02, 0.02, 60))
+    depth = rng.uniform(0.05, 0.3, 60) * (1.0 + 0.5 * metallicity)
+    width = rng.uniform(0.002, 0.01, 60) * (1.0 + 0.2 * (log_g - 4.5))
+    lines = np.ones_like(wl)
+    for c, d, w in zip(centres, depth, width):
+        lines *= 1.0 - d * np.exp(-0.5 * ((np.log(wl) - np.log(c)) / w) ** 2)
+    return wl, np.pi * b_lambda * lines
+
+
+def write_star_file(path: str, wl: np.ndarray, flux: np.ndarray) -> None:
+    """Stellar spectrum file of the "file" model: one "wavelength flux" line per point."""
+    tmp = path + ".tmp"
+    with open(tmp, "w") as f:
+        for a, b in zip(wl, flux):
+            f.write(f"{_fmt(a)} {_fmt(b)}\n")
+    os.replace(tmp, path)
+
+
+def star_grid(teff: Sequence[float], log_g: Sequence[float], metallicity: Sequence[float],
+              n: int = 2000) -> Tuple[List[np.ndarray], np.ndarray, np.ndarray]:
+    """Axes, float32 wavelengths and float32 spectra (T_eff, log g, [M/H] row-major) of a
+    synthetic stellar grid."""
+    axes = [np.asarray(teff, dtype=np.float64), np.asarray(log_g, dtype=np.float64),
+            np.asarray(metallicity, dtype=np.float64)]
+    spectra = []
+    for t in axes[0]:
+        for g in axes[1]:
+            for m in axes[2]:
+                wl, fl = star_spectrum(float(t), float(g), float(m), n=n)
+                spectra.append(fl)
+    return axes, wl.astype(np.float32), np.asarray(spectra, dtype=np.float32)
+
+
+def write_star_grid(folder: str, axes: Sequence[np.ndarray], wl: np.ndarray, spectra: np.ndarray) -> None:
+    """Stellar grid folder of the "grid" model: grid_parameters.dat (three node lines, the
+    wavelength file name, then "T_eff log_g [M/H] file" per spectrum) and float32 files."""
+    os.makedirs(folder, exist_ok=True)
+    np.asarray(wl, dtype=np.float32).tofile(os.path.join(folder, "wavelengths.bin"))
+    lines = [" ".join(_fmt(v) for v in a) for a in axes] + ["wavelengths.bin"]
+    i = 0
+    for t in axes[0]:
+        for g in axes[1]:
+            for m in axes[2]:
+                name = f"spectrum_{i:03d}.bin"
+                np.asarray(spectra[i], dtype=np.float32).tofile(os.path.join(folder, name))
+                lines.append(f"{_fmt(t)} {_fmt(g)} {_fmt(m)} {name}")
+                i += 1
+    tmp = os.path.join(folder, "grid_parameters.dat.tmp")
+    with open(tmp, "w") as f:
+        f.write("\n".join(lines) + "\n")
+    os.replace(tmp, os.path.join(folder, "grid_parameters.dat"))
+
+
+def eclipse_model_config(spec: WorkloadSpec, star_model: str, star_params: Sequence[str]) -> OccultationConfig:
+    """The emission workload's atmosphere as a secondary-eclipse model."""
+    sym, fold = _opacity_lists(spec)
+    temp = ("poly", ["5", "1"]) if spec.temperature == "poly" else ("const", [])
+    cloud = (["grey"], [["fb"]]) if spec.cloud else ([], [])
+    return OccultationConfig(spec.nb_levels, spec.p_bottom, spec.p_top, temp[0], temp[1], "scm", [],
+                             ["iso", "bg"], [list(spec.species), ["H2He"]], sym, fold, star_model,
+                             list(star_params), cloud[0], cloud[1])
+
+
+def eclipse_priors(spec: WorkloadSpec, star_model: str, axes: Optional[Sequence[np.ndarray]] = None) -> List[Prior]:
+    """[log g, R_p / R_s, stellar parameters, abundances, temperature, cloud] of an eclipse workload."""
+    pr = [Prior("uniform", "log g", [3.0, 3.6]), Prior("uniform", "R_p/R_s", [0.08, 0.14])]
+    if star_model == "blackbody":
+        pr.append(Prior("uniform", "T_eff", [4500.0, 6500.0]))
+    elif star_model == "grid":
+        for name, a in zip(("T_eff", "stellar log g", "[M/H]"), axes):
+            pr.append(Prior("uniform", name, [float(a[0]), float(a[-1])]))
+    for sp in spec.species:
+        pr.append(Prior("log_uniform", sp, [1e-8, 1e-3]))
+    if spec.temperature == "poly":
+        pr.append(Prior("uniform", "T0", [1200.0, 2800.0]))
+        for k in range(5):
+            pr.append(Prior("uniform", f"T ratio {k+1}", [0.6, 1.0]))
+    else:
+        pr.append(Prior("uniform", "T", [900.0, 2500.0]))
+    if spec.cloud:
+        pr.append(Prior("log_uniform", "cloud optical depth", [0.1, 10.0]))
+        pr.append(Prior("log_uniform", "cloud top pressure", [max(spec.p_top * 10.0, 1e-5),
+                                                              min(spec.p_bottom / 10.0, 10.0)]))
+    return pr

@@ -48,12 +48,14 @@ const char* bear_last_error(void);
 /* --------------------------------------------------------------- set-up
  * Replaces the model construction of Retrieval::Retrieval(GlobalConfig*,
  * GenericConfig*, vector<ObservationInput>, vector<PriorConfig>)
- * (src/retrieval/retrieval.cpp:70-104): GlobalConfig + Emission/Transmission
- * ModelConfig are given as line-based text ("key value ..." per line, keys:
- * forward_model, cross_section_path, wavenumber_file, spectral_discretisation,
- * spectral_resolution, error_inflation, nb_grid_points, atmos_boundaries,
- * temperature_profile, radiative_transfer, chemistry, cloud, opacity,
- * fit_mean_molecular_weight, fit_scale_height, variable_gravity). */
+ * (src/retrieval/retrieval.cpp:70-104): GlobalConfig + Emission/Transmission/
+ * Occultation ModelConfig are given as line-based text ("key value ..." per line,
+ * keys: forward_model (emission, transmission, secondary_eclipse), cross_section_path,
+ * wavenumber_file, spectral_discretisation, spectral_resolution, error_inflation,
+ * nb_grid_points, atmos_boundaries, temperature_profile, radiative_transfer,
+ * chemistry, cloud, opacity, fit_mean_molecular_weight, fit_scale_height,
+ * variable_gravity, stellar_spectrum (secondary eclipse: blackbody | file <path> |
+ * grid <folder/>, src/forward_model/stellar_spectrum/select_stellar_model.h:52-122)). */
 int bear_model_create(const char* config_text, int device, bear_model** out);
 
 /* One ObservationInput (src/observations/observations.h:42-92,
@@ -145,6 +147,32 @@ int bear_loglike(bear_model* m, const double* params, int nb_params, double* log
 int bear_loglike_batch(bear_model* m, const double* params_dev, int batch, int nb_params,
                        double* loglike_dev, uint8_t* neglect_dev, void* stream);
 
+/* --------------------------------------------------------------- priors on the device
+ * The reference converts MultiNest's hypercube coordinates to parameters on the host,
+ * one point at a time (Retrieval::convertHypercubeParameters
+ * src/retrieval/multinest_loglike.cpp:59-97, prior classes src/retrieval/prior_types.h:89-256).
+ * Here a batch of live points stays in device memory: cube -> parameters -> log L.
+ *
+ * bear_model_set_priors: one prior per model parameter (n = the model's parameter
+ * count, the error exponent included when error inflation is on), as the PriorConfig
+ * list of Retrieval::Retrieval: type[i] 0 uniform (a, b = bounds), 1 log-uniform
+ * (a, b = bounds > 0), 2 Gaussian (a = mean, b = standard deviation; erf_inv as the
+ * reference), 3 delta (a = value), 4 linked (link[i] = the 0-based parameter whose
+ * prior and cube coordinate it takes; never another linked one; the value is used
+ * without a unit, as in the reference). unit[i]: the unit factor (NULL: all 1), e.g.
+ * 7.1492e9 for "Rj" (src/retrieval/prior_types.h:57-82). a, b, link may be NULL
+ * where no prior needs them.
+ * bear_prior_transform_batch: cube (batch x nb_params, device, in [0, 1]) to physical
+ * parameters (batch x nb_params, device).
+ * bear_loglike_cube_batch: the transform, then bear_loglike_batch on the result
+ * (params_dev receives the physical parameters). */
+int bear_model_set_priors(bear_model* m, int n, const int* type, const double* a, const double* b,
+                          const double* unit, const int* link);
+int bear_prior_transform_batch(bear_model* m, const double* cube_dev, int batch, int nb_params,
+                               double* params_dev, void* stream);
+int bear_loglike_cube_batch(bear_model* m, const double* cube_dev, int batch, int nb_params, double* params_dev,
+                            double* loglike_dev, uint8_t* neglect_dev, void* stream);
+
 /* Gradient of the log-likelihood with respect to the physical parameters (the
  * reference's parameter vector: ratios for the temperature knots, linear mixing
  * ratios) by the engine's adjoint kernels, with the log-likelihood itself.
@@ -192,6 +220,10 @@ int bear_model_autotune(bear_model* m, const double* params_dev, int batch, int 
 typedef struct bear_batch_graph bear_batch_graph;
 int bear_batch_graph_create(bear_model* m, const double* params_dev, int batch, int nb_params,
                             double* loglike_dev, uint8_t* neglect_dev, bear_batch_graph** out);
+/* The same captured from the hypercube: prior transform (into params_dev) + forward. */
+int bear_batch_graph_create_cube(bear_model* m, const double* cube_dev, int batch, int nb_params,
+                                 double* params_dev, double* loglike_dev, uint8_t* neglect_dev,
+                                 bear_batch_graph** out);
 int bear_batch_graph_launch(bear_batch_graph* g, void* stream);
 int bear_batch_graph_destroy(bear_batch_graph* g);
 

@@ -108,6 +108,13 @@ typedef struct {
 typedef struct orc_model {
   /* global */
   int transmission;
+  int occultation;           /* secondary eclipse (OccultationModel) */
+  int star_model;            /* 1 blackbody (T_eff parameter), 2 file, 3 grid (T_eff, log g, [M/H]) */
+  char star_file[1024];      /* file path (2) or grid folder (3) */
+  double* star_flux;         /* N, file stellar spectrum on the model grid */
+  double* star_grid;         /* spectra x N, grid spectra on the model grid, (t, g, m) row-major */
+  double* star_axis[3];
+  int star_n[3];
   char xsec_path[1024], wn_file[1024];
   int discretisation; double resolution; int error_inflation;
   /* model */
@@ -162,6 +169,8 @@ orc_model* orc_create(const char* text) {
     if (!strcmp(k, "forward_model")) {
       if (nt < 2) goto bad;
       if (!strcmp(tok[1], "transmission")) m->transmission = 1;
+      else if (!strcmp(tok[1], "secondary_eclipse") || !strcmp(tok[1], "Secondary_eclipse") || !strcmp(tok[1], "se"))
+        m->occultation = 1;  /* selectForwardModel src/retrieval/select_forward_model.cpp:69 */
       else if (strcmp(tok[1], "emission")) { set_err("unsupported forward model %s", tok[1]); goto fail; }
     } else if (!strcmp(k, "cross_section_path")) { snprintf(m->xsec_path, sizeof m->xsec_path, "%s", nt > 1 ? tok[1] : ""); }
     else if (!strcmp(k, "wavenumber_file")) { snprintf(m->wn_file, sizeof m->wn_file, "%s", nt > 1 ? tok[1] : ""); }
@@ -179,6 +188,15 @@ orc_model* orc_create(const char* text) {
       if (!strcmp(tok[1], "poly")) { m->temp_poly = 1; m->poly_elements = atoi(tok[2]); m->poly_order = atoi(tok[3]); }
       else if (!strcmp(tok[1], "const")) m->temp_poly = 0;
       else { set_err("unsupported temperature profile %s", tok[1]); goto fail; }
+    } else if (!strcmp(k, "stellar_spectrum")) {
+      /* selectStellarModel src/forward_model/stellar_spectrum/select_stellar_model.h */
+      if (nt < 2) goto bad;
+      if (!strcmp(tok[1], "blackbody")) m->star_model = 1;
+      else if ((!strcmp(tok[1], "file") || !strcmp(tok[1], "grid")) && nt >= 3) {
+        m->star_model = !strcmp(tok[1], "file") ? 2 : 3;
+        snprintf(m->star_file, sizeof m->star_file, "%s", tok[2]);
+      }
+      else { set_err("unsupported stellar spectrum %s", tok[1]); goto fail; }
     } else if (!strcmp(k, "radiative_transfer")) {
       if (strcmp(tok[1], "scm")) { set_err("unsupported radiative transfer %s", tok[1]); goto fail; }
     } else if (!strcmp(k, "chemistry")) {
@@ -690,6 +708,144 @@ static void setup_atmosphere(orc_model* m) {
   }
 }
 
+/* StarSpectrumFile src/forward_model/stellar_spectrum/star_file_spectrum.cpp:40-120:
+ * "wavelength(um) flux(W m-2 um-1)" lines, flux * wl^2 / 1e4, interpolated to the grid */
+static int load_star_file(orc_model* m) {
+  FILE* f = fopen(m->star_file, "r");
+  if (!f) { set_err("stellar spectrum file %s not found", m->star_file); return -1; }
+  size_t cap = 1024, n = 0;
+  double* x = (double*)malloc(cap * sizeof(double));
+  double* y = (double*)malloc(cap * sizeof(double));
+  char line[512];
+  while (fgets(line, sizeof line, f)) {
+    double a, b;
+    if (sscanf(line, "%lf %lf", &a, &b) != 2) continue;
+    if (n == cap) { cap *= 2; x = (double*)realloc(x, cap * sizeof(double)); y = (double*)realloc(y, cap * sizeof(double)); }
+    x[n] = a; y[n] = b * a * a / 10000.; ++n;
+  }
+  fclose(f);
+  if (n < 2) { free(x); free(y); set_err("stellar spectrum file %s has fewer than two points", m->star_file); return -1; }
+  m->star_flux = (double*)calloc(m->N, sizeof(double));
+  interp_to_wavelengths(x, y, (int)n, m->wl, m->N, m->star_flux);
+  free(x); free(y);
+  return 0;
+}
+
+static float* read_float_file(const char* path, size_t* n) {
+  FILE* f = fopen(path, "rb");
+  if (!f) return NULL;
+  fseek(f, 0, SEEK_END);
+  long bytes = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  *n = (size_t)bytes / sizeof(float);
+  float* v = (float*)malloc((*n ? *n : 1) * sizeof(float));
+  if (fread(v, sizeof(float), *n, f) != *n) { free(v); fclose(f); return NULL; }
+  fclose(f);
+  return v;
+}
+
+/* StellarSpectrumGrid src/forward_model/stellar_spectrum/stellar_spectrum_grid.cpp:42-210 and
+ * SampledStellarSpectrum::sampleSpectrum sampled_stellar_spectrum.cpp:47-80: every grid
+ * spectrum (float32, W m-2 um-1 on the grid's float32 wavelengths) x wl^2 / 1e4, interpolated
+ * to the model grid, values below 1e-37 raised to 1e-37. A folder without a trailing '/' gets
+ * a '+' appended, as in the reference. */
+static int load_star_grid(orc_model* m) {
+  char folder[1100], path[2200], line[4096];
+  snprintf(folder, sizeof folder, "%s%s", m->star_file,
+           (m->star_file[0] && m->star_file[strlen(m->star_file) - 1] == '/') ? "" : "+");
+  snprintf(path, sizeof path, "%sgrid_parameters.dat", folder);
+  FILE* f = fopen(path, "r");
+  if (!f) { set_err("stellar grid parameter file %s not found", path); return -1; }
+  for (int a = 0; a < 3; ++a) {
+    if (!fgets(line, sizeof line, f)) { fclose(f); set_err("stellar grid %s truncated", path); return -1; }
+    m->star_axis[a] = (double*)malloc(256 * sizeof(double));
+    int n = 0, used = 0; double v; char* c = line;
+    while (n < 256 && sscanf(c, "%lf%n", &v, &used) == 1) { m->star_axis[a][n++] = v; c += used; }
+    m->star_n[a] = n;
+  }
+  char wlname[1024];
+  if (fscanf(f, "%1023s", wlname) != 1) { fclose(f); set_err("stellar grid %s truncated", path); return -1; }
+  if (!fgets(line, sizeof line, f)) line[0] = 0;
+  const int n0 = m->star_n[0], n1 = m->star_n[1], n2 = m->star_n[2];
+  snprintf(path, sizeof path, "%s%s", folder, wlname);
+  size_t nwl = 0;
+  float* wlf = read_float_file(path, &nwl);
+  if (!wlf) { fclose(f); set_err("stellar grid wavelength file %s not found", path); return -1; }
+  double* gwl = (double*)malloc(nwl * sizeof(double));
+  double* y = (double*)malloc(nwl * sizeof(double));
+  for (size_t i = 0; i < nwl; ++i) gwl[i] = wlf[i];
+  m->star_grid = (double*)calloc((size_t)n0 * n1 * n2 * m->N, sizeof(double));
+  int count = 0;
+  while (fgets(line, sizeof line, f)) {
+    double t, g, q; char name[1024];
+    if (sscanf(line, "%lf %lf %lf %1023s", &t, &g, &q, name) != 4) continue;
+    int it = -1, ig = -1, iq = -1;
+    for (int i = 0; i < n0; ++i) if (m->star_axis[0][i] == t) it = i;
+    for (int i = 0; i < n1; ++i) if (m->star_axis[1][i] == g) ig = i;
+    for (int i = 0; i < n2; ++i) if (m->star_axis[2][i] == q) iq = i;
+    if (it < 0 || ig < 0 || iq < 0) { fclose(f); set_err("stellar grid: spectrum off the nodes"); return -1; }
+    snprintf(path, sizeof path, "%s%s", folder, name);
+    size_t nf = 0;
+    float* fl = read_float_file(path, &nf);
+    if (!fl || nf != nwl) { fclose(f); set_err("stellar grid spectrum %s missing or of the wrong size", path); return -1; }
+    for (size_t i = 0; i < nwl; ++i) y[i] = (double)fl[i] * gwl[i] * gwl[i] / 10000.;
+    free(fl);
+    double* out = m->star_grid + ((size_t)(it * n1 + ig) * n2 + iq) * m->N;
+    interp_to_wavelengths(gwl, y, (int)nwl, m->wl, m->N, out);
+    for (size_t i = 0; i < m->N; ++i) if (out[i] < 1e-37) out[i] = 1e-37;
+    ++count;
+  }
+  fclose(f);
+  free(wlf); free(gwl); free(y);
+  if (count != n0 * n1 * n2) { set_err("stellar grid is inconsistent"); return -1; }
+  return 0;
+}
+
+/* StellarSpectrumGrid::findClosestGridPoints stellar_spectrum_grid.cpp:245-270 */
+static void star_closest(const double* g, int n, double x, int* i0, int* i1) {
+  if (x <= g[0]) { *i0 = *i1 = 0; return; }
+  if (x >= g[n - 1]) { *i0 = *i1 = n - 1; return; }
+  int j = 0;
+  while (g[j] < x) ++j;
+  *i1 = j;
+  *i0 = g[j] != x ? j - 1 : j;
+}
+
+/* StellarSpectrumGrid::calcFlux stellar_spectrum_grid.cpp:275-330 with
+ * aux::triLinearInterpolation src/additional/aux_functions.cpp:290-318 */
+static void star_grid_flux(const orc_model* m, const double* sp, double* out) {
+  double x[3]; int lo[3], hi[3];
+  for (int a = 0; a < 3; ++a) {
+    const double* g = m->star_axis[a]; const int n = m->star_n[a];
+    x[a] = sp[a];
+    if (x[a] < g[0]) x[a] = g[0];
+    if (x[a] > g[n - 1]) x[a] = g[n - 1];
+    star_closest(g, n, x[a], &lo[a], &hi[a]);
+  }
+  const int n1 = m->star_n[1], n2 = m->star_n[2];
+  #define ORC_SG(t, g, q) (m->star_grid + ((size_t)((t) * n1 + (g)) * n2 + (q)) * m->N)
+  const double* c000 = ORC_SG(lo[0], lo[1], lo[2]); const double* c100 = ORC_SG(hi[0], lo[1], lo[2]);
+  const double* c010 = ORC_SG(lo[0], hi[1], lo[2]); const double* c110 = ORC_SG(hi[0], hi[1], lo[2]);
+  const double* c001 = ORC_SG(lo[0], lo[1], hi[2]); const double* c101 = ORC_SG(hi[0], lo[1], hi[2]);
+  const double* c011 = ORC_SG(lo[0], hi[1], hi[2]); const double* c111 = ORC_SG(hi[0], hi[1], hi[2]);
+  #undef ORC_SG
+  const double x0 = m->star_axis[0][lo[0]], x1 = m->star_axis[0][hi[0]];
+  const double y0 = m->star_axis[1][lo[1]], y1 = m->star_axis[1][hi[1]];
+  const double z0 = m->star_axis[2][lo[2]], z1 = m->star_axis[2][hi[2]];
+  double xd = (x[0] - x0) / (x1 - x0); if (x[0] == x0) xd = 0;
+  double yd = (x[1] - y0) / (y1 - y0); if (x[1] == y0) yd = 0;
+  double zd = (x[2] - z0) / (z1 - z0); if (x[2] == z0) zd = 0;
+  for (size_t i = 0; i < m->N; ++i) {
+    const double c00 = c000[i] * (1. - xd) + c100[i] * xd;
+    const double c01 = c001[i] * (1. - xd) + c101[i] * xd;
+    const double c10 = c010[i] * (1. - xd) + c110[i] * xd;
+    const double c11 = c011[i] * (1. - xd) + c111[i] * xd;
+    const double c0 = c00 * (1. - yd) + c10 * yd;
+    const double c1 = c01 * (1. - yd) + c11 * yd;
+    out[i] = c0 * (1. - zd) + c1 * zd;
+  }
+}
+
 int orc_finalize(orc_model* m) {
   if (m->nobs == 0) { set_err("no observations"); return -1; }
   if (load_wavenumbers(m)) return -1;
@@ -698,6 +854,14 @@ int orc_finalize(orc_model* m) {
   if (setup_opacity(m)) return -1;
   setup_atmosphere(m);
   m->nparam_general = 3 + (m->transmission && (m->fit_mmw || m->fit_sh) ? 1 : 0);
+  if (m->occultation) {
+    /* OccultationModel: [log g, R_p / R_s] then the stellar model's parameters
+     * (src/forward_model/secondary_eclipse/secondary_eclipse.cpp:72,115-150) */
+    if (m->star_model == 0) { set_err("the secondary-eclipse model needs a stellar spectrum"); return -1; }
+    m->nparam_general = 2 + (m->star_model == 1 ? 1 : m->star_model == 3 ? 3 : 0);
+    if (m->star_model == 2 && load_star_file(m)) return -1;
+    if (m->star_model == 3 && load_star_grid(m)) return -1;
+  }
   m->nparam_chem = 0;
   for (int c = 0; c < m->nchem; ++c) m->nparam_chem += m->chem_kind[c] == 0 ? m->chem_nsp[c] : 0;
   m->nparam_cloud = m->cloud ? (m->cloud_fb ? 2 : 3) : 0;
@@ -1088,7 +1252,18 @@ int orc_forward(const orc_model* m, const double* par, int P, double* spectrum, 
   }
 
   double* spec = (double*)malloc(N * sizeof(double));
-  if (!m->transmission) {
+  double* star = NULL;
+  if (m->occultation) {
+    /* OccultationModel::calcModelCPU src/forward_model/secondary_eclipse/secondary_eclipse.cpp:183-246:
+     * planet emission without the radius-distance scaling, stellar spectrum from the model */
+    #pragma omp parallel for schedule(dynamic, 16)
+    for (long i = 0; i < (long)N; ++i) spec[i] = sc_point(m, absorption + (size_t)i * L, cloud_tau, &a, (size_t)i);
+    star = (double*)malloc(N * sizeof(double));
+    if (m->star_model == 3) star_grid_flux(m, gen + 2, star);
+    else
+      for (size_t i = 0; i < N; ++i)  /* StarBlackBody::calcFlux star_blackbody.cpp:35-47 */
+        star[i] = m->star_model == 1 ? planck_wn(gen[2], m->nu[i]) * K_PI * 1e-3 : m->star_flux[i];
+  } else if (!m->transmission) {
     const double scaling = (K_RJUP / gen[2]) * (K_RJUP / gen[2]) * gen[1];
     #pragma omp parallel for schedule(dynamic, 16)
     for (long i = 0; i < (long)N; ++i) spec[i] = sc_point(m, absorption + (size_t)i * L, cloud_tau, &a, (size_t)i);
@@ -1116,14 +1291,24 @@ int orc_forward(const orc_model* m, const double* par, int P, double* spectrum, 
     const obs_t* o = &m->obs[k];
     double* bands = (double*)malloc((o->n ? o->n : 1) * sizeof(double));
     process_observation(m, o, spec, !m->transmission, bands);
+    if (m->occultation) {
+      /* occultation depth: binned planet / binned star x (R_p / R_s)^2 x 1e6 */
+      double* sb = (double*)malloc((o->n ? o->n : 1) * sizeof(double));
+      process_observation(m, o, star, 1, sb);
+      for (int b = 0; b < o->n; ++b) bands[b] = bands[b] / sb[b] * gen[1] * gen[1] * 1e6;
+      free(sb);
+    }
     if (o->nb_modifier) { const double c = mods[mi]; if (c != 0) for (int b = 0; b < o->n; ++b) bands[b] += c; mi += o->nb_modifier; }
     for (int b = 0; b < o->n; ++b) obs_out[o->out_offset + b] = o->ascending ? bands[o->n - 1 - b] : bands[b];
     free(bands);
   }
-  if (!m->transmission) {
+  if (m->occultation) {
+    for (size_t i = 0; i < N; ++i) spec[i] = spec[i] / star[i] * gen[1] * gen[1] * 1e6;
+  } else if (!m->transmission) {
     /* RadiativeTransfer::changeSpectrumUnits src/radiative_transfer/radiative_transfer.h:58-60 */
     for (size_t i = 0; i < N; ++i) spec[i] = spec[i] / m->wl[i] / m->wl[i] * 10000.0;
   }
+  free(star);
   if (spectrum) memcpy(spectrum, spec, N * sizeof(double));
   *neglect_out = neglect;
   free(spec); free(absorption); free(scattering); free(cloud_tau);

@@ -33,6 +33,7 @@
 #include "forward_model/emission/emission.h"
 #include "forward_model/forward_model.h"
 #include "forward_model/transmission/transmission.h"
+#include "forward_model/secondary_eclipse/secondary_eclipse.h"
 #include "observations/observations.h"
 #include "retrieval/priors.h"
 #include "retrieval/retrieval.h"
@@ -182,7 +183,17 @@ int main(int argc, char** argv) {
   bear::GenericConfig* model_cfg = nullptr;
   bear::EmissionModelConfig* em = nullptr;
   bear::TransmissionModelConfig* tm = nullptr;
-  if (model == "emission") {
+  bear::OccultationConfig* om = nullptr;
+  if (model == "secondary_eclipse" || model == "Secondary_eclipse" || model == "se") {
+    auto rt = kv.get("radiative_transfer");
+    if (rt.empty()) rt = {"scm"};
+    auto star = kv.get("stellar_spectrum");
+    om = new bear::OccultationConfig(nb_grid, std::stod(bounds[0]), std::stod(bounds[1]), temp[0],
+                                     tail(temp, 1), rt[0], tail(rt, 1), chem_models, chem_params,
+                                     op_symbol, op_folder, star[0], tail(star, 1), cloud_models,
+                                     cloud_params);
+    model_cfg = om;
+  } else if (model == "emission") {
     auto rt = kv.get("radiative_transfer");
     if (rt.empty()) rt = {"scm"};
     em = new bear::EmissionModelConfig(nb_grid, std::stod(bounds[0]), std::stod(bounds[1]),
@@ -258,5 +269,6 @@ int main(int argc, char** argv) {
 
   delete em;
   delete tm;
+  delete om;
   return 0;
 }

@@ -27,12 +27,13 @@ sys.path.insert(0, os.path.dirname(HERE))
 import refcase  # noqa: E402
 from bear_gb300 import synthetic as syn  # noqa: E402
 from bear_gb300.config import Observation, observation_arrays, render_config  # noqa: E402
-from goldenlib import GOLDEN_DIR, TABLE_ROOT, save_case, spec_to_meta  # noqa: E402
+from goldenlib import GOLDEN_DIR, TABLE_ROOT, save_case, spec_to_meta, write_star  # noqa: E402
 
 
-def run_ref(name, template, root, obs, params):
+def run_ref(name, template, root, obs, params, star_dir=""):
     d = os.path.join("/tmp", "bear_golden_case_" + name)
-    refcase.write_case(d, template.replace("{ROOT}", root), [observation_arrays(o) for o in obs], params)
+    refcase.write_case(d, template.replace("{ROOT}", root).replace("{STAR}", star_dir),
+                       [observation_arrays(o) for o in obs], params)
     return refcase.run_case(d)
 
 
@@ -44,13 +45,17 @@ def split_obs(obs, flat):
     return out
 
 
-def make(name, spec, kind, template_fn, obs, params, spectrum_rows, attach_kind=None, truth_index=0):
+def make(name, spec, kind, template_fn, obs, params, spectrum_rows, attach_kind=None, truth_index=0,
+         model_cfg=None, star=None):
+    """star: (kind, arrays) of a secondary-eclipse case's stellar file or grid."""
     root = syn.write_tables(spec, TABLE_ROOT)
-    template = template_fn(render_config(syn.global_config(spec, "{ROOT}", kind), syn.model_config(spec, kind)))
+    mc = model_cfg if model_cfg is not None else syn.model_config(spec, kind)
+    template = template_fn(render_config(syn.global_config(spec, "{ROOT}", kind), mc))
+    star_dir = write_star(star[0], star[1], os.path.join(TABLE_ROOT, "star_" + name) + "/") if star else ""
     # data: the reference model at the truth parameters plus seeded noise
-    first = run_ref(name, template, root, obs, params[truth_index:truth_index + 1])
+    first = run_ref(name, template, root, obs, params[truth_index:truth_index + 1], star_dir)
     syn.attach_data(obs, split_obs(obs, first["obs"][0]), attach_kind or kind, spec.seed)
-    ref = run_ref(name, template, root, obs, params)
+    ref = run_ref(name, template, root, obs, params, star_dir)
     arrays = [observation_arrays(o) for o in obs]
     out = {
         "ref_loglike": ref["loglike"], "ref_neglect": ref["neglect"], "ref_obs": ref["obs"],
@@ -62,6 +67,9 @@ def make(name, spec, kind, template_fn, obs, params, spectrum_rows, attach_kind=
         out[f"ref_setup{k}_edges"] = np.array(s["edges"], dtype=np.int64).reshape(-1, 2)
         out[f"ref_setup{k}_conv"] = np.array(s["conv"], dtype=np.int64).reshape(-1, 2)
     meta = {"spec": spec_to_meta(spec), "kind": kind, "config_template": template}
+    if star:
+        meta["star"] = star[0]
+        out.update(star[1])
     save_case(os.path.join(GOLDEN_DIR, name + ".npz"), meta, arrays, params, out)
     print(f"{name}: N={ref['grid'].size} M={ref['obs'].shape[1]} S={params.shape[0]} loglike={ref['loglike']}")
 
@@ -167,6 +175,57 @@ def main():
         rows.append(cold)
         make("transmission_edges", spec, "transmission", tmpl, obs, np.array(rows), [0, 1],
              attach_kind="transmission")
+
+    # 6-8. secondary eclipse (occultation depth, ppm) with a blackbody, a file and a grid star:
+    #      40 levels, 2 cm^-1 sampling from 1.0 to 6.7 um, an R=100 spectrum with an instrument
+    #      profile and a shift modifier, descending bins, two photon-counting filters
+    for star_kind in ("blackbody", "file", "grid"):
+        name = "eclipse_" + star_kind
+        if which and name not in which:
+            continue
+        spec = dataclasses.replace(syn.CONFIGS["emission_plain"], name=name, model="emission", nb_levels=40,
+                                   nu_min=1500.0, nu_max=10000.0, nu_step=2.0, species=["H2O", "CO", "CH4"],
+                                   temperature="poly", cloud=(star_kind == "file"), seed=20261220)
+        star = None
+        star_params = []
+        axes = None
+        if star_kind == "file":
+            wl, fl = syn.star_spectrum(5200.0, 4.4, 0.1)
+            star = ("file", {"star_wl": wl[::-1].copy(), "star_flux": fl[::-1].copy()})  # descending file
+            star_params = ["{STAR}star.dat"]
+        elif star_kind == "grid":
+            axes, gwl, gsp = syn.star_grid([4000.0, 4600.0, 5300.0, 6000.0], [4.0, 4.5], [-0.5, 0.0, 0.5])
+            star = ("grid", {"star_axis0": axes[0], "star_axis1": axes[1], "star_axis2": axes[2],
+                             "star_grid_wl": gwl, "star_grid_spectra": gsp})
+            star_params = ["{STAR}"]
+        mc = syn.eclipse_model_config(spec, star_kind, star_params)
+        wl = np.geomspace(1.1, 5.0, 40)
+        o1 = Observation("nirspec_like", "spectroscopy", wl, np.ones(40), np.ones(40))
+        o1.instrument_profile_fwhm = list(wl / 100.0)
+        o1.spectrum_modifier_id = "shift_const"
+        edges = np.linspace(1.7, 1.1, 13)
+        o2 = Observation("wfc3_bins", "band-spectroscopy", np.stack([edges[:-1], edges[1:]], axis=1),
+                         np.ones(12), np.ones(12))
+        obs = [o1, o2]
+        for i, (c, w) in enumerate(((3.6, 0.75), (4.5, 1.0))):
+            fw = np.linspace(c - 0.6 * w, c + 0.6 * w, 50)
+            o = Observation(f"irac{i + 1}", "photometry", [[c - 0.5 * w, c + 0.5 * w]], np.ones(1), np.ones(1))
+            o.filter_response = [list(fw), list(np.where(np.abs(fw - c) <= 0.5 * w, 1.0, 0.02))]
+            o.filter_detector_type = "photon"
+            obs.append(o)
+        pr = syn.eclipse_priors(spec, star_kind, axes)
+        rng = np.random.default_rng(spec.seed + (0 if star_kind == "blackbody" else 1 if star_kind == "file" else 2))
+        rows = syn.cube_to_physical(pr, rng.uniform(0.05, 0.95, (3, len(pr))))
+        rows = np.concatenate([rows, np.zeros((3, 1))], axis=1)   # shift
+        rows[1, -1] = 15.0
+        if star_kind == "grid":
+            rows[1, 2:5] = [4600.0, 4.5, 0.0]       # exactly on grid nodes
+            rows[2, 2:5] = [6500.0, 3.0, 0.25]      # T_eff and log g outside: clamped to the edges
+        bad = rows[0].copy()
+        bad[[p.description for p in pr].index("T0")] = 40.0  # the profile below 50 K: neglected
+        params = np.vstack([rows, bad])
+        make(name, spec, "secondary_eclipse", same, obs, params, [0, 1, 2], attach_kind="transmission",
+             model_cfg=mc, star=star)
 
 
 if __name__ == "__main__":

@@ -9,8 +9,11 @@ A golden case is one .npz under tests/golden/ holding
               ref_loglike (S), ref_neglect (S), ref_obs (S x M, caller order),
               ref_spectrum (rows listed in spectrum_rows x N), ref_grid (N)
   ref_setup_* per-observation integer set-up (index range, band edges, windows)
+  star_*      secondary-eclipse cases: the stellar spectrum file (star_wl, star_flux)
+              or stellar grid (star_axis0..2, star_grid_wl, star_grid_spectra) the
+              config template names as {STAR}; meta "star" is "file" or "grid"
 The tables are regenerated from the spec (bear_gb300.synthetic, bit-identical
-on every platform) into a temporary directory.
+on every platform) into a temporary directory, the star files from the arrays.
 """
 
 from __future__ import annotations
@@ -74,8 +77,15 @@ class Case:
     def table_root(self) -> str:
         return syn.write_tables(self.spec, TABLE_ROOT)
 
+    def star_root(self) -> str:
+        """Directory holding this case's stellar spectrum file or grid ("" if none)."""
+        kind = self.meta.get("star", "")
+        if not kind:
+            return ""
+        return write_star(kind, self.arrays, os.path.join(TABLE_ROOT, "star_" + self.name) + "/")
+
     def config_text(self) -> str:
-        return self.meta["config_template"].replace("{ROOT}", self.table_root())
+        return self.meta["config_template"].replace("{ROOT}", self.table_root()).replace("{STAR}", self.star_root())
 
     def observations(self) -> List[ObservationArrays]:
         out = []
@@ -97,6 +107,20 @@ class Case:
         return {"range": tuple(int(x) for x in a[f"ref_setup{k}_range"]),
                 "edges": [tuple(int(x) for x in r) for r in a[f"ref_setup{k}_edges"]],
                 "conv": [tuple(int(x) for x in r) for r in a[f"ref_setup{k}_conv"].reshape(-1, 2)]}
+
+
+def write_star(kind: str, arrays: dict, folder: str) -> str:
+    """Write a case's stellar spectrum ("file": folder/star.dat) or grid ("grid": the grid
+    folder) from its arrays; returns the folder."""
+    os.makedirs(folder, exist_ok=True)
+    if kind == "file":
+        syn.write_star_file(os.path.join(folder, "star.dat"), arrays["star_wl"], arrays["star_flux"])
+    elif kind == "grid":
+        axes = [arrays[f"star_axis{i}"] for i in range(3)]
+        syn.write_star_grid(folder, axes, arrays["star_grid_wl"], arrays["star_grid_spectra"])
+    else:
+        raise ValueError(kind)
+    return folder
 
 
 def golden_cases() -> List[str]:

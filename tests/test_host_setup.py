@@ -48,7 +48,11 @@ def test_observation_operator_reproduces_binning(prepared):
     the reference's filtered, convolved and bin-integrated spectrum."""
     c, e = prepared
     emission = c.meta["kind"] == "emission"
+    eclipse = c.meta["kind"] == "secondary_eclipse"
+    if eclipse and c.meta.get("star"):
+        pytest.skip("file and grid stars: the binned stellar flux is not recoverable from the outputs")
     wl = 1e4 / e.wavenumbers
+    nu = e.wavenumbers
     obs_arrays = c.observations()
     for j, i in enumerate(c.arrays["spectrum_rows"]):
         if c.arrays["ref_neglect"][i]:
@@ -56,10 +60,18 @@ def test_observation_operator_reproduces_binning(prepared):
         F = c.arrays["ref_spectrum"][j].copy()
         if emission:
             F = F * wl * wl / 1e4  # undo the per-micron conversion of the returned spectrum
+        if eclipse:
+            # blackbody star pi B_nu(T_eff) 1e-3; the returned spectrum is F_p / F_s (R_p/R_s)^2 1e6
+            h, cl, kb = 6.62606896e-27, 2.99792458e10, 1.3806504e-16
+            rr, teff = c.params[i][1], c.params[i][2]
+            Fs = 2.0 * h * cl * cl * nu**3 / np.expm1(h * nu * cl / kb / teff) * np.pi * 1e-3
+            F = F * Fs / (rr * rr * 1e6)
         internal = np.empty(e.M)
         for r in range(e.M):
             k0, w = e.operator_row(r)
             internal[r] = w @ F[k0:k0 + w.size]
+            if eclipse:
+                internal[r] = internal[r] / (w @ Fs[k0:k0 + w.size]) * rr * rr * 1e6
         # shift modifiers are applied after binning
         got = goldenlib.user_order_from_internal(obs_arrays, internal)
         ref = c.arrays["ref_obs"][i].copy()
@@ -96,3 +108,39 @@ def test_missing_table_file_is_reported(tmp_path):
     with pytest.raises(_lib.EngineError) as ei:
         Engine(text, c.observations(), prepare_only=True)
     assert ei.value.code in (1, 2)
+
+
+def test_eclipse_configuration_errors(tmp_path):
+    """Secondary-eclipse set-up: the stellar model is required and checked (the
+    reference's selectStellarModel messages), files must exist, grids must be complete."""
+    c = [goldenlib.Case(p) for p in CASES if p.endswith("eclipse_blackbody.npz")][0]
+    text = c.config_text()
+    obs = c.observations()
+    no_star = "\n".join(l for l in text.splitlines() if not l.startswith("stellar_spectrum")) + "\n"
+    for bad, code in ((no_star, 1), (text.replace("stellar_spectrum blackbody", "stellar_spectrum blackbody 5000"), 1),
+                      (text.replace("stellar_spectrum blackbody", "stellar_spectrum phoenix"), 1),
+                      (text.replace("stellar_spectrum blackbody", f"stellar_spectrum file {tmp_path}/none.dat"), 2),
+                      (text.replace("stellar_spectrum blackbody", f"stellar_spectrum grid {tmp_path}/"), 2),
+                      (text.replace("forward_model secondary_eclipse", "forward_model emission"), 1)):
+        with pytest.raises(_lib.EngineError) as ei:
+            Engine(bad, obs, prepare_only=True)
+        assert ei.value.code == code, (bad.splitlines()[-1], ei.value)
+    # an incomplete grid: one spectrum line missing
+    from bear_gb300 import synthetic as syn
+    axes, wl, sp = syn.star_grid([4000.0, 5000.0], [4.5], [0.0], n=200)
+    syn.write_star_grid(str(tmp_path / "g") + "/", axes, wl, sp)
+    pf = tmp_path / "g" / "grid_parameters.dat"
+    lines = pf.read_text().splitlines()
+    pf.write_text("\n".join(lines[:-1]) + "\n")
+    with pytest.raises(_lib.EngineError) as ei:
+        Engine(text.replace("stellar_spectrum blackbody", f"stellar_spectrum grid {tmp_path}/g/"), obs,
+               prepare_only=True)
+    assert "inconsistent" in str(ei.value)
+    # the short name and the parameter count of a file star: [log g, R_p/R_s] + chemistry ...
+    wl2, fl2 = syn.star_spectrum(5000.0, n=300)
+    syn.write_star_file(str(tmp_path / "s.dat"), wl2, fl2)
+    e = Engine(text.replace("forward_model secondary_eclipse", "forward_model se")
+               .replace("stellar_spectrum blackbody", f"stellar_spectrum file {tmp_path}/s.dat"), obs,
+               prepare_only=True)
+    assert e.P == c.params.shape[1] - 1
+    e.close()
