@@ -27,7 +27,8 @@ constexpr double kPi = 3.14159265358979323846;
 // significant: the mean molecular weight is summed over it in this order.
 constexpr int kSpeciesCount = 46;
 enum SpeciesId : int {
-  SP_TOTAL = 0, SP_H = 1, SP_He = 2, SP_H2 = 10, SP_Na = 19, SP_K = 20, SP_e = 35
+  SP_TOTAL = 0, SP_H = 1, SP_He = 2, SP_H2 = 10, SP_H2O = 11, SP_CO2 = 12, SP_CO = 13, SP_CH4 = 14,
+  SP_Na = 19, SP_K = 20, SP_Hm = 22, SP_e = 35
 };
 extern const char* const kSpeciesSymbol[kSpeciesCount];
 extern const double kSpeciesMolWeight[kSpeciesCount];

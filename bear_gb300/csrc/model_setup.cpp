@@ -625,22 +625,52 @@ static void load_table(Model& m, OpacitySpecies& op, const std::string& folder) 
   }
 }
 
-// Rayleigh cross sections src/transport_coeff/species_rayleigh_cross_sections.cpp and
-// OpacitySpecies::generalRayleighCrossSection src/transport_coeff/opacity_species.cpp:528-537
+// Rayleigh cross sections src/transport_coeff/species_rayleigh_cross_sections.cpp:25-234 and
+// OpacitySpecies::generalRayleighCrossSection src/transport_coeff/opacity_species.cpp:528-537:
+// H2, He (all wavelengths), H (Lee & Kim 2002 expansion), CO, CO2, CH4, H2O (zero beyond
+// 2 micron; H2O from the refractive index of water at standard conditions).
 static void tabulate_rayleigh(Model& m, OpacitySpecies& op) {
-  op.rayleigh.resize(m.N);
+  const int sp = op.index;
+  if (sp != SP_H2 && sp != SP_He && sp != SP_H && sp != SP_CO && sp != SP_CO2 && sp != SP_CH4 && sp != SP_H2O)
+    throw unsupported(std::string("Rayleigh scattering of ") + kSpeciesSymbol[sp] +
+                      " is not supported (H2, He, H, CO, CO2, CH4, H2O)");
+  op.rayleigh.assign(m.N, 0.0);
   for (size_t j = 0; j < m.N; ++j) {
     const double nu = m.nu[j], wl = m.wl[j];
-    double n, nref, king = 1.0;
-    if (op.index == SP_H2) {
+    double n = 1.0, nref = 2.546899e19, king = 1.0;
+    if (sp == SP_H2) {
       n = (13.58e-5 * (1. + 7.52e-3 / std::pow(wl, 2))) + 1.;
       nref = 2.651629e19;
-    } else if (op.index == SP_He) {
+    } else if (sp == SP_He) {
       n = (2283. + 1.8102e13 / (1.5342e10 - nu * nu)) * 1e-8 + 1;
-      nref = 2.546899e19;
+    } else if (sp == SP_H) {
+      const double f = 0.0912 / wl;  // Lyman limit / wavelength
+      op.rayleigh[j] = 8.41e-25 * std::pow(f, 4) + 3.37e-24 * std::pow(f, 6) + 4.71e-22 * std::pow(f, 14);
+      continue;
     } else {
-      throw unsupported(std::string("Rayleigh scattering of ") + kSpeciesSymbol[op.index] +
-                        " is not supported (H2, He)");
+      if (wl > 2.0) continue;
+      const double nu2 = nu * nu;
+      if (sp == SP_CO) {
+        n = (22851. + 0.456e14 / (71427.0 * 71427.0 - nu2)) * 1e-8 + 1;
+      } else if (sp == SP_CO2) {
+        king = 1.1364 + 25.3e-12 * nu2;
+        n = (5799.25 / (128908.9 * 128908.9 - nu2) + 120.05 / (89223.8 * 89223.8 - nu2) +
+             5.3334 / (75037.5 * 75037.5 - nu2) + 4.3244 / (67837.7 * 67837.7 - nu2) +
+             0.1218145e-6 / (2418.136 * 2418.136 - nu2)) * 1.1427e3 + 1.0;
+      } else if (sp == SP_CH4) {
+        n = (46662. + 4.02e-6 * nu2) * 1e-8 + 1;
+      } else {  // H2O
+        static const double a[8] = {0.244257733, 0.974634476e-2, -0.373234996e-2, 0.268678472e-3,
+                                    0.158920570e-2, 0.245934259e-2, 0.900704920, -0.166626219e-1};
+        const double delta = 1.0, theta = 1.0, luv = 0.229202, lir = 5.432937;
+        nref = 3.34279671749673e+22;
+        king = (6 + 3 * 3e-4) / (6 - 7 * 3e-4);
+        const double lam = wl / 0.589;
+        const double af = delta * (a[0] + a[1] * delta + a[2] * theta + a[3] * lam * lam * theta +
+                                   a[4] * std::pow(lam, -2) + a[5] / (lam * lam - luv * luv) +
+                                   a[6] / (lam * lam - lir * lir) + a[7] * delta * delta);
+        n = std::pow(((2 * af + 1) / (1 - af)), 0.5);
+      }
     }
     op.rayleigh[j] = 24. * std::pow(kPi, 3) * std::pow(nu, 4) / (nref * nref) *
                      std::pow((n * n - 1) / (n * n + 2), 2) * king;

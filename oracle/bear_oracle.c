@@ -612,7 +612,7 @@ static int load_rows(orc_model* m, opac_t* op, const char* folder) {
   return 0;
 }
 
-/* Rayleigh cross sections, src/transport_coeff/species_rayleigh_cross_sections.cpp and
+/* Rayleigh cross sections, src/transport_coeff/species_rayleigh_cross_sections.cpp:25-234 and
  * generalRayleighCrossSection src/transport_coeff/opacity_species.cpp:528-537 */
 static double rayleigh_general(double nref, double n, double king, double nu) {
   return 24. * pow(K_PI, 3) * pow(nu, 4) / (nref * nref) * pow((n * n - 1) / (n * n + 2), 2) * king;
@@ -628,6 +628,38 @@ static int tabulate_rayleigh(orc_model* m, opac_t* op, int sp) {
     } else if (sp == SP_He) {
       n = (2283. + 1.8102e13 / (1.5342e10 - nu * nu)) * 1e-8 + 1;
       nref = 2.546899e19;
+    } else if (sp == SP_H) {
+      /* GasHRayleigh: Lee & Kim 2002 low-energy expansion */
+      const double f = 0.0912 / wl;
+      op->rayleigh[j] = 8.41e-25 * pow(f, 4) + 3.37e-24 * pow(f, 6) + 4.71e-22 * pow(f, 14);
+      continue;
+    } else if (sp == SP_CO || sp == SP_CO2 || sp == SP_CH4 || sp == SP_H2O) {
+      op->rayleigh[j] = 0.0;
+      if (wl > 2.0) continue;  /* these are zero beyond 2 micron */
+      const double nu2 = nu * nu;
+      nref = 2.546899e19;
+      if (sp == SP_CO) {
+        n = (22851. + 0.456e14 / (71427.0 * 71427.0 - nu2)) * 1e-8 + 1;
+      } else if (sp == SP_CO2) {
+        king = 1.1364 + 25.3e-12 * nu2;
+        n = (5799.25 / (128908.9 * 128908.9 - nu2) + 120.05 / (89223.8 * 89223.8 - nu2)
+             + 5.3334 / (75037.5 * 75037.5 - nu2) + 4.3244 / (67837.7 * 67837.7 - nu2)
+             + 0.1218145e-6 / (2418.136 * 2418.136 - nu2)) * 1.1427e3 + 1.0;
+      } else if (sp == SP_CH4) {
+        n = (46662. + 4.02e-6 * nu2) * 1e-8 + 1;
+      } else {
+        /* GasH2ORayleigh: water at STP (delta = theta = 1) */
+        static const double a[8] = {0.244257733, 0.974634476e-2, -0.373234996e-2, 0.268678472e-3,
+                                    0.158920570e-2, 0.245934259e-2, 0.900704920, -0.166626219e-1};
+        const double delta = 1.0, theta = 1.0, luv = 0.229202, lir = 5.432937;
+        nref = 3.34279671749673e+22;
+        king = (6 + 3 * 3e-4) / (6 - 7 * 3e-4);
+        const double lam = wl / 0.589;
+        const double af = delta * (a[0] + a[1] * delta + a[2] * theta + a[3] * lam * lam * theta
+                                   + a[4] * pow(lam, -2) + a[5] / (lam * lam - luv * luv)
+                                   + a[6] / (lam * lam - lir * lir) + a[7] * delta * delta);
+        n = pow(((2 * af + 1) / (1 - af)), 0.5);
+      }
     } else {
       set_err("Rayleigh scattering for this species is not restated in the oracle");
       return -1;

@@ -176,6 +176,27 @@ def main():
         make("transmission_edges", spec, "transmission", tmpl, obs, np.array(rows), [0, 1],
              attach_kind="transmission")
 
+    # 9. transmission with every Rayleigh species of the reference (H2, He, H, CO, CO2, CH4,
+    #    H2O; the last four vanish beyond 2 micron), atomic H in the chemistry, 0.45-3.4 um
+    if not which or "transmission_rayleigh" in which:
+        spec = dataclasses.replace(syn.CONFIGS["transmission_plain"], name="transmission_rayleigh", nb_levels=50,
+                                   nu_min=2900.0, nu_max=22500.0, nu_step=2.0, species=["H2O", "CO", "CO2", "CH4"],
+                                   temperature="const", cloud=False, seed=20261230,
+                                   rayleigh=("H2", "He", "H", "CO", "CO2", "CH4", "H2O"))
+
+        def tmpl(t):
+            assert "chemistry iso H2O CO CO2 CH4\n" in t
+            return t.replace("chemistry iso H2O CO CO2 CH4\n", "chemistry iso H2O CO CO2 CH4 H\n")
+        edges = np.geomspace(0.46, 3.3, 61)
+        obs = [Observation("transit_bins", "band-spectroscopy", np.stack([edges[:-1], edges[1:]], axis=1),
+                           np.ones(60), np.ones(60))]
+        rows = []
+        for T, xs, xh in ((1200.0, [1e-4, 1e-4, 1e-6, 1e-5], 1e-3), (800.0, [1e-3, 1e-5, 1e-7, 1e-4], 1e-5),
+                          (2200.0, [1e-6, 1e-3, 1e-5, 1e-8], 0.05)):
+            rows.append([3.2, 1.1 * syn.R_JUPITER, 0.9 * syn.R_SUN] + xs + [xh, T])
+        make("transmission_rayleigh", spec, "transmission", tmpl, obs, np.array(rows), [0, 2],
+             attach_kind="transmission")
+
     # 6-8. secondary eclipse (occultation depth, ppm) with a blackbody, a file and a grid star:
     #      40 levels, 2 cm^-1 sampling from 1.0 to 6.7 um, an R=100 spectrum with an instrument
     #      profile and a shift modifier, descending bins, two photon-counting filters

@@ -46,10 +46,13 @@ def test_device_transform_matches_host(case):
     cube[1] = 1.0
     dev = e.prior_transform_batch(torch.tensor(cube, device="cuda")).cpu().numpy()
     host = Priors(pr).cube_to_physical_batch(cube)
-    err = np.abs(dev - host) / np.maximum(np.abs(host), 1e-300)
     finite = np.isfinite(host)
     assert np.array_equal(np.isfinite(dev), finite)
-    assert err[finite].max() < 4e-16, err[finite].max()
+    assert np.array_equal(dev[~finite], host[~finite])  # erfinv(+-1) = +-inf on both sides
+    err = np.abs(dev[finite] - host[finite]) / np.maximum(np.abs(host[finite]), 1e-300)
+    # one rounding of the log-uniform exponent x (the device contracts a + u (b - a) into
+    # an FMA) moves 10^x by ln(10) |x| 2^-53 relative: ~2e-15 at x = -8
+    assert err.max() < 1e-14, err.max()
 
 
 def test_cube_batch_equals_transform_then_batch(case):
