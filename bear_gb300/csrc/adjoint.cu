@@ -758,6 +758,8 @@ static void launch_gradient_transmission(Model& m, const double* params_dev, int
 
 void launch_gradient(Model& m, const double* params_dev, int batch, cudaStream_t st, double* loglike_dev,
                      double* grad_dev, uint8_t* neglect_dev) {
+  if (m.hm) throw Error(BEAR_ERR_UNSUPPORTED, "no gradient for models with the H- continuum");
+  if (m.acfg.cloud_kind) throw Error(BEAR_ERR_UNSUPPORTED, "no gradient for the power-law and KH clouds");
   if (m.transmission) {
     launch_gradient_transmission(m, params_dev, batch, st, loglike_dev, grad_dev, neglect_dev);
     return;

@@ -130,7 +130,17 @@ __global__ void __launch_bounds__(kMaxLevels) atmosphere_kernel(DeviceModel dm, 
         f.lg2n_lo = 0.0f;
       }
     }
-    for (int r = 0; r < c.R; ++r) ray_n[((size_t)b * L + l) * c.R + r] = n[c.ray_index[r]];
+    double* rn = ray_n + ((size_t)b * L + l) * c.R;
+    for (int r = 0; r < c.R_ray; ++r) rn[r] = n[c.ray_index[r]];
+    if (c.hm) {
+      // H- continuum coefficients (GasHm::calcContinuumAbsorption src/transport_coeff/h_m.cpp:36-53:
+      // kappa_bf n(H-) + kappa_ff P_e n(H), P_e = n(e-) k T; nothing when n(H-) = 0)
+      double* hc = rn + c.R_ray;
+      const double nhm = n[SP_Hm];
+      hc[0] = nhm;
+      const double pn = n[SP_e] * kBoltzmann * T * n[SP_H];
+      for (int i = 1; i < kHmTerms; ++i) hc[i] = nhm == 0.0 ? 0.0 : pow(5040.0 / T, (i + 1) / 2.0) * pn;
+    }
     if (neglect) atomicOr(&s_neglect, 1);
   }
   __syncthreads();
@@ -172,9 +182,12 @@ __global__ void __launch_bounds__(kMaxLevels) atmosphere_kernel(DeviceModel dm, 
     int top = 0, bottom = 0;
     double per = 0.0;
     if (c.cloud) {
+      // power law and KH clouds place the layers like the grey cloud
+      // (src/cloud_model/power_law_cloud_model.cpp:69-121, kh_cloud_model.cpp:69-133)
+      const int it = c.cloud_kind == 0 ? 1 : c.cloud_kind == 1 ? 2 : 4;
       double tau = cloud[0];
-      const double ptop = cloud[1];
-      const double pbot = c.cloud_fb ? 0.0 : ptop * cloud[2];
+      const double ptop = cloud[it];
+      const double pbot = c.cloud_fb ? 0.0 : ptop * cloud[it + 1];
       if (tau < 0) tau = 0;
       unsigned ti = 0, bi = 0;
       for (int i = 0; i < L - 1; ++i)
@@ -223,6 +236,18 @@ __global__ void __launch_bounds__(kMaxLevels) atmosphere_kernel(DeviceModel dm, 
     e.cloud_top = top;
     e.cloud_bottom = bottom;
     e.pad = 0;
+    for (int i = 0; i < 4; ++i) e.cs[i] = 0.0;
+    if (c.cloud && c.cloud_kind == 1) {
+      e.cs[0] = cloud[1];                          // exponent
+      e.cs[3] = pow(c.cloud_ref_wl, cloud[1]);     // reference_value
+    } else if (c.cloud && c.cloud_kind == 2) {
+      const double q0 = cloud[1], a0 = cloud[2];
+      e.cs[0] = q0;
+      e.cs[1] = a0;
+      e.cs[2] = 2 * kPi * cloud[3];                // 2 pi particle size
+      const double xr = e.cs[2] / c.cloud_ref_wl;  // reference size parameter
+      e.cs[3] = q0 * pow(xr, -a0) + pow(xr, 0.2);  // reference_q
+    }
     ev[b] = e;
   }
   __syncthreads();

@@ -60,16 +60,30 @@ constexpr size_t kTransmissionDynSmem = 220 * 1024;
 // Writes the flux in W m^-2 cm times the radius-distance scaling. With STORE the
 // two Gauss-angle intensities after every level are also written to
 // istore[b][l][angle][k] (the adjoint pass reads them back top-down).
-template <bool STORE>
+//
+// EXT (models with the H- continuum or a non-grey cloud): the H- continuum (rows R_ray
+// .. R-1 of the linear-term table, coefficients in ray_n) has its level coefficients
+// staged in dynamic shared memory as double-floats (L x kHmTerms float2) and added to
+// the level absorption; a non-grey cloud scales the cloud depths by its wavelength factor.
+template <bool STORE, bool EXT = false>
 __global__ void __launch_bounds__(256) emission_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
                                                        const LevelSpecies* __restrict__ ls,
                                                        const LevelSpeciesDF* __restrict__ lsdf,
+                                                       const double* __restrict__ ray_n,
                                                        const EvalInfo* __restrict__ ev,
                                                        double* __restrict__ spectrum, double* __restrict__ istore) {
   __shared__ ExpTables et;
   __shared__ double tab2048[2048];
+  extern __shared__ float2 hm_s[];  // [L][kHmTerms] when the H- continuum is on
   load_exp_tables(et);
   for (int i = threadIdx.x; i < 2048; i += blockDim.x) tab2048[i] = kExp2TabD2048[i];
+  const bool hm = EXT && dm.R > dm.R_ray;
+  if (hm)
+    for (int i = threadIdx.x; i < dm.L * kHmTerms; i += blockDim.x) {
+      const int l = i / kHmTerms, c = i - l * kHmTerms;
+      const df2 d = df_from_double(__ldg(&ray_n[((size_t)blockIdx.x * dm.L + l) * dm.R + dm.R_ray + c]));
+      hm_s[i] = make_float2(d.hi, d.lo);
+    }
   __syncthreads();
   const int b = blockIdx.x;
   const int k = blockIdx.y * blockDim.x + threadIdx.x;
@@ -86,7 +100,22 @@ __global__ void __launch_bounds__(256) emission_kernel(DeviceModel dm, const Lev
     const float2 it = __ldg(reinterpret_cast<const float2*>(&lv[l].invT_hi));
     return planck_df(c1, c2l, df2{it.x, it.y}, et.hi, et.lo);
   };
-  Kappa kap_prev = level_kappa_df(dm.ltab, N, sf, S, k, et);
+  auto kappa = [&](int l) {
+    Kappa kp = level_kappa_df(dm.ltab, N, sf + (size_t)l * S, S, k, et);
+    if (hm) {
+      df2 x = kp.v;
+      for (int c = 0; c < kHmTerms; ++c) {
+        const float2 r = __ldg(&dm.rayleigh_df[(size_t)(dm.R_ray + c) * N + k]);
+        const float2 q = hm_s[l * kHmTerms + c];
+        x = df_fma(df2{r.x, r.y}, df2{q.x, q.y}, x);
+      }
+      kp.v = x;
+    }
+    return kp;
+  };
+  const double csh = (EXT && dm.cloud_kind) ? cloud_shape(dm, ev[b], k) : 1.0;
+  const df2 csd = df_from_double(csh);
+  Kappa kap_prev = kappa(0);
   double B_prev = planck(0);
   double I1 = B_prev, I2 = B_prev;
   if (STORE) {
@@ -94,10 +123,10 @@ __global__ void __launch_bounds__(256) emission_kernel(DeviceModel dm, const Lev
     Is[N] = I2;
   }
   for (int l = 1; l < L; ++l) {
-    const Kappa kap = level_kappa_df(dm.ltab, N, sf + (size_t)l * S, S, k, et);
+    const Kappa kap = kappa(l);
     const double B = planck(l);
     double tau, rtau;
-    emission_layer_tau_df(lv, l, kap, kap_prev, tau, rtau);
+    emission_layer_tau_df<EXT>(lv, l, kap, kap_prev, tau, rtau, csh, csd);
     sc_layer_fast(tau, rtau, B, B_prev, I1, I2, tab2048);
     if (STORE) {
       Is[(size_t)l * 2 * N] = I1;
@@ -114,6 +143,7 @@ __global__ void __launch_bounds__(256) emission_kernel(DeviceModel dm, const Lev
 template <bool STORE>
 __global__ void __launch_bounds__(256) emission_kernel_fp64(DeviceModel dm, const LevelInfo* __restrict__ lev,
                                                             const LevelSpecies* __restrict__ ls,
+                                                            const double* __restrict__ ray_n,
                                                             const EvalInfo* __restrict__ ev,
                                                             double* __restrict__ spectrum,
                                                             double* __restrict__ istore) {
@@ -126,7 +156,14 @@ __global__ void __launch_bounds__(256) emission_kernel_fp64(DeviceModel dm, cons
   const LevelSpecies* sp = ls + (size_t)b * L * S;
   double* Is = STORE ? istore + (size_t)b * L * 2 * N + k : nullptr;
   const double c1 = dm.planck_c1[k], c2 = dm.planck_c2[k];
-  double kap_prev = level_absorption_fp64(dm.table64, N, sp, S, k);
+  auto kappa = [&](int l) {
+    double kp = level_absorption_fp64(dm.table64, N, sp + (size_t)l * S, S, k);
+    const double* rn = ray_n + ((size_t)b * L + l) * dm.R;
+    for (int r = dm.R_ray; r < dm.R; ++r) kp += __ldg(&dm.rayleigh[(size_t)r * N + k]) * __ldg(&rn[r]);
+    return kp;
+  };
+  const double csh = dm.cloud_kind ? cloud_shape(dm, ev[b], k) : 1.0;
+  double kap_prev = kappa(0);
   double B_prev = c1 / (exp(c2 * __ldg(&lv[0].invT)) - 1.0);
   double I1 = B_prev, I2 = B_prev;
   if (STORE) {
@@ -134,9 +171,9 @@ __global__ void __launch_bounds__(256) emission_kernel_fp64(DeviceModel dm, cons
     Is[N] = I2;
   }
   for (int l = 1; l < L; ++l) {
-    const double kap = level_absorption_fp64(dm.table64, N, sp + (size_t)l * S, S, k);
+    const double kap = kappa(l);
     const double B = c1 / (exp(c2 * __ldg(&lv[l].invT)) - 1.0);
-    const double tau = __ldg(&lv[l - 1].dz) * (kap + kap_prev) / 2. + __ldg(&lv[l - 1].cloud);
+    const double tau = __ldg(&lv[l - 1].dz) * (kap + kap_prev) / 2. + __ldg(&lv[l - 1].cloud) * csh;
     sc_layer<false>(tau, B, B_prev, I1, I2, nullptr);
     if (STORE) {
       Is[(size_t)l * 2 * N] = I1;
@@ -227,6 +264,8 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
   const LevelSpecies* sp = ls + (size_t)b * L * S;
   const LevelSpeciesDF* sf = lsdf + (size_t)b * L * S;
   float2* rn_s = chi_f + (size_t)L * VPB;  // [L][R] (DF only)
+  // non-grey cloud: the extinction of every level scaled by the wavelength factor
+  const double csh = (dm.cloud_kind && active) ? cloud_shape(dm, ev[b], k) : 1.0;
   if (DF) {
     load_exp_tables(et);
     for (int idx = threadIdx.x; idx < L * R; idx += blockDim.x) {
@@ -248,14 +287,14 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
           x = df_fma(df2{sr.x, sr.y}, df2{nr.x, nr.y}, x);
         }
         const float2 cl = __ldg(reinterpret_cast<const float2*>(&lv[l].cloud_hi));
-        x = df_add(x, df2{cl.x, cl.y});
+        x = dm.cloud_kind ? df_fma(df2{cl.x, cl.y}, df_from_double(csh), x) : df_add(x, df2{cl.x, cl.y});
         chi_f[l * VPB + v] = make_float2(x.hi, x.lo);
       } else {
         const double a = level_absorption_fp64(dm.table64, N, sp + (size_t)l * S, S, k);
         double sc = 0.0;
         for (int r = 0; r < R; ++r)
           sc += __ldg(&dm.rayleigh[(size_t)r * N + k]) * __ldg(&ray_n[((size_t)b * L + l) * R + r]);
-        chi_s[l * VPB + v] = a + sc + __ldg(&lv[l].cloud);
+        chi_s[l * VPB + v] = a + sc + __ldg(&lv[l].cloud) * csh;
       }
     }
   }
@@ -686,6 +725,9 @@ void upload_model(Model& m) {
   m.device_bytes += ts.bytes;
   std::vector<double> ray;
   for (int r : m.rayleigh_species) ray.insert(ray.end(), m.opac[r].rayleigh.begin(), m.opac[r].rayleigh.end());
+  ray.insert(ray.end(), m.hm_rows.begin(), m.hm_rows.end());  // H- continuum rows follow the Rayleigh rows
+  dm.R_ray = m.acfg.R_ray;
+  dm.cloud_kind = m.acfg.cloud_kind;
   dm.rayleigh = dev_upload(m, ray);
   {
     std::vector<float2> rdf(ray.size());
@@ -827,14 +869,19 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
   if (!m.transmission) {
     const int TB = rt > 0 ? rt : (batch == 1 ? 64 : 128);
     dim3 grid(batch, (dm.N + TB - 1) / TB);
+    const size_t hm_smem = m.hm ? (size_t)L * kHmTerms * sizeof(float2) : 0;
     if (taps && m.precision == 1)
-      emission_kernel_fp64<true><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.ev, w.spectrum, taps->istore);
-    else if (taps)
-      emission_kernel<true><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.lsdf, w.ev, w.spectrum, taps->istore);
+      emission_kernel_fp64<true><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.ray_n, w.ev, w.spectrum, taps->istore);
+    else if (taps)  // the gradient rejects H- models
+      emission_kernel<true><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.spectrum,
+                                                taps->istore);
     else if (m.precision == 1)
-      emission_kernel_fp64<false><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.ev, w.spectrum, nullptr);
+      emission_kernel_fp64<false><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.ray_n, w.ev, w.spectrum, nullptr);
+    else if (m.hm || m.acfg.cloud_kind)
+      emission_kernel<false, true><<<grid, TB, hm_smem, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev,
+                                                             w.spectrum, nullptr);
     else
-      emission_kernel<false><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.lsdf, w.ev, w.spectrum, nullptr);
+      emission_kernel<false><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.spectrum, nullptr);
   } else {
     if (m.precision == 1) transmission_geometry_kernel<false><<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom);
     else transmission_geometry_kernel<true><<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom);

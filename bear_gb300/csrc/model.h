@@ -62,8 +62,10 @@ struct AtmosphereConfig {
   int chem_na_free[kMaxChemModules];
   int chem_bg_h2he[kMaxChemModules];
   int chem_bg_sp[kMaxChemModules];
-  // grey cloud
-  int cloud, cloud_fb;
+  // cloud: grey placement (kind 0), times a wavelength shape for the power-law (1) and
+  // KH non-grey (2) clouds; parameters [tau, (exponent | q0, a0, size), p_top, (bottom factor)]
+  int cloud, cloud_fb, cloud_kind;
+  double cloud_ref_wl;
   // transmission options
   int fit_mmw, var_g;
   // opacity species with tables (line lists and CIA)
@@ -73,10 +75,16 @@ struct AtmosphereConfig {
   int sp_nT[kMaxTableSpecies];
   int sp_T_off[kMaxTableSpecies];       // offset into table_T
   int sp_pb_off[kMaxTableSpecies];      // offset into pb_* arrays: [t][level]
-  // Rayleigh species
-  int R;
+  // linear opacity terms: R_ray Rayleigh species (scattering), then, with hm, the kHmTerms
+  // terms of the H- continuum (absorption); R = R_ray + (hm ? kHmTerms : 0)
+  int R, R_ray, hm;
   int ray_index[kMaxRayleigh];
 };
+
+// H- continuum (GasHm src/transport_coeff/h_m.cpp:36-137) as kHmTerms linear terms: row 0
+// the bound-free cross section (coefficient n(H-)), rows 1-6 the free-free polynomials
+// in wavelength (coefficients (5040/T)^((i+1)/2) 1e-29 P_e n(H)); all zero when n(H-) = 0.
+constexpr int kHmTerms = 7;
 
 // Per (evaluation, level, table species): the four table rows of the
 // interpolation stencil and its weights, plus the species' number density
@@ -122,6 +130,9 @@ struct __align__(16) EvalInfo {
   int neglect;
   int cloud_top, cloud_bottom;
   int pad;
+  // non-grey cloud shape: power law {exponent, -, -, ref_wl^exponent};
+  // KH {q0, a0, 2 pi size, Q(reference size parameter)}
+  double cs[4];
 };
 
 // One parameter's prior on the device (Retrieval's PriorConfig list). a, b: uniform
@@ -158,8 +169,10 @@ struct DeviceModel {
   const int* pb_row0;         // per species [nT][L]: absolute row of the lower pressure node
   const int* pb_row1;         // upper pressure node
   const double* pb_w;         // log-p weight
-  const double* rayleigh;     // R x N
+  const double* rayleigh;     // R x N: Rayleigh cross sections, then the H- continuum rows
   const float2* rayleigh_df;  // R x N as double-floats
+  int R_ray;                  // Rayleigh rows (the rest, R - R_ray, are H- continuum rows)
+  int cloud_kind;             // 0 grey (or no cloud), 1 power law, 2 KH non-grey
   // observation operator: M rows, internal (descending-wavelength) order
   const int* row_k0;
   const int* row_len;
@@ -295,8 +308,11 @@ struct Model {
   int poly_elements = 0, poly_order = 0;
   std::vector<ChemModule> chem;
   bool cloud = false, cloud_fb = false;
+  int cloud_kind = 0;             // 0 grey, 1 power_law, 2 KHnongrey
+  double cloud_ref_wl = 0.0;      // reference wavelength (micron) of the non-grey clouds
   bool fit_mmw = false, fit_sh = false, var_g = false;
   bool occultation = false;
+  bool hm = false;                // H- continuum configured
   int star_model = 0;             // 1 blackbody, 2 file, 3 grid
   std::string star_path;          // file path (2) or grid folder (3)
   std::vector<std::pair<std::string, std::string>> opac_cfg;
@@ -314,6 +330,7 @@ struct Model {
   long long n_lrows = 0;             // rows of the level table
   std::vector<double> table_host;    // n_rows x N (freed after upload)
   std::vector<double> W;             // concatenated operator weights
+  std::vector<double> hm_rows;       // kHmTerms x N wavelength parts of the H- continuum
   // stellar spectrum of the secondary-eclipse model (file: 1 spectrum; grid: all)
   std::vector<double> star_hr;       // spectra x N on the model grid
   std::vector<double> star_bin;      // spectra x M through the observation rows

@@ -148,10 +148,22 @@ void parse_config(Model& m, const std::string& text) {
     } else if (k == "cloud") {
       need(2);
       if (t[1] == "none") continue;
-      if (t[1] != "grey") throw unsupported("cloud model " + t[1] + " is not supported (grey)");
+      // selectCloudModel src/cloud_model/select_cloud_model.h:42-100
       if (m.cloud) throw unsupported("only one cloud model is supported");
+      if (t[1] == "grey") {
+        m.cloud_kind = 0;
+        m.cloud_fb = (t.size() == 3 && t[2] == "fb");
+      } else if (t[1] == "power_law" || t[1] == "KHnongrey") {
+        // PowerLawCloudModel / KHCloudModel ctors: the reference wavelength, then optionally "fb"
+        if (t.size() < 3)
+          throw invalid("Expected at least one parameter for the " + t[1] + " cloud model, but only found 0");
+        m.cloud_kind = t[1] == "power_law" ? 1 : 2;
+        m.cloud_ref_wl = std::stod(t[2]);
+        m.cloud_fb = (t.size() == 4 && t[3] == "fb");
+      } else {
+        throw unsupported("cloud model " + t[1] + " is not supported (grey, power_law, KHnongrey)");
+      }
       m.cloud = true;
-      m.cloud_fb = (t.size() == 3 && t[2] == "fb");
     } else if (k == "opacity") {
       need(2);
       m.opac_cfg.emplace_back(t[1], t.size() > 2 ? t[2] : "");
@@ -677,8 +689,49 @@ static void tabulate_rayleigh(Model& m, OpacitySpecies& op) {
   }
 }
 
+// GasHm::boundFreeAbsorption and freeFreeAbsorption src/transport_coeff/h_m.cpp:56-137: the
+// wavelength-dependent parts. Row 0: the photo-detachment cross section (threshold 1.6419 um,
+// valid above 0.125 um); rows 1-6: the free-free polynomials lambda^2 A + B + C/lambda + ...
+// + F/lambda^4 of each power (5040/T)^((i+1)/2), with the coefficient set above 0.3645 um or
+// from 0.1823 to 0.3645 um, times 1e-29 (zero outside).
+static void tabulate_hm(Model& m) {
+  static const double lambda_0 = 1.6419;
+  static const double Cn[7] = {0.0, 152.519, 49.534, -118.858, 92.536, -34.194, 4.982};
+  static const double A1[7] = {0.0, 0.0, 2483.3460, -3449.8890, 2200.0400, -696.2710, 88.2830};
+  static const double B1[7] = {0.0, 0.0, 285.8270, -1158.3820, 2427.7190, -1841.4000, 444.5170};
+  static const double C1[7] = {0.0, 0.0, -2054.2910, 8746.5230, -13651.1050, 8624.9700, -1863.8650};
+  static const double D1[7] = {0.0, 0.0, 2827.7760, -11485.6320, 16755.5240, -10051.5300, 2095.2880};
+  static const double E1[7] = {0.0, 0.0, -1341.5370, 5303.6090, -7510.4940, 4400.0670, -901.7880};
+  static const double F1[7] = {0.0, 0.0, 208.9520, -812.9390, 1132.7380, -655.0200, 132.9850};
+  static const double A2[7] = {0.0, 518.1021, 473.2636, -482.2089, 115.5291, 0.0, 0.0};
+  static const double B2[7] = {0.0, -734.8666, 1443.4137, -737.1616, 169.6374, 0.0, 0.0};
+  static const double C2[7] = {0.0, 1021.1775, -1977.3395, 1096.8827, -245.6490, 0.0, 0.0};
+  static const double D2[7] = {0.0, -479.0721, 922.3575, -521.1341, 114.2430, 0.0, 0.0};
+  static const double E2[7] = {0.0, 93.1373, -178.9275, 101.7963, -21.9972, 0.0, 0.0};
+  static const double F2[7] = {0.0, -6.4285, 12.3600, -7.0571, 1.5097, 0.0, 0.0};
+  const size_t N = m.N;
+  m.hm_rows.assign((size_t)kHmTerms * N, 0.0);
+  for (size_t k = 0; k < N; ++k) {
+    const double l = m.wl[k];
+    if (l <= lambda_0 && l >= 0.125) {
+      double f = 0;
+      for (int i = 1; i < 7; ++i) f += Cn[i] * std::pow((1.0 / l - 1.0 / lambda_0), (i - 1) / 2.0);
+      m.hm_rows[k] = 1e-18 * l * l * l * std::pow(1.0 / l - 1.0 / lambda_0, 1.5) * f;
+    }
+    const double *A = nullptr, *B = nullptr, *C = nullptr, *D = nullptr, *E = nullptr, *F = nullptr;
+    if (l > 0.3645) { A = A1; B = B1; C = C1; D = D1; E = E1; F = F1; }
+    else if (l >= 0.1823) { A = A2; B = B2; C = C2; D = D2; E = E2; F = F2; }
+    if (!A) continue;
+    for (int i = 1; i < 7; ++i)
+      m.hm_rows[(size_t)i * N + k] =
+          (l * l * A[i] + B[i] + C[i] / l + D[i] / l / l + E[i] / l / l / l + F[i] / l / l / l / l) * 1e-29;
+  }
+}
+
 static void setup_opacity(Model& m) {
   // TransportCoefficients::addOpacitySpecies src/transport_coeff/transport_coeff.cpp:98-237
+  m.hm = false;
+  m.hm_rows.clear();
   m.n_rows = 0;
   m.table_host.clear();
   for (size_t i = 0; i < m.opac_cfg.size(); ++i) {
@@ -688,7 +741,13 @@ static void setup_opacity(Model& m) {
     if (s == "CIA-H2-H2") { op.index = SP_H2; op.partners = {SP_H2}; }
     else if (s == "CIA-H2-He") { op.index = SP_H2; op.partners = {SP_He}; }
     else if (s == "CIA-H-He") { op.index = SP_H; op.partners = {SP_He}; }
-    else if (s == "H-") throw unsupported("the H- continuum is not supported");
+    else if (s == "H-") {
+      // GasHm: no tables, a continuum computed from T, n(H-), n(H) and n(e-)
+      if (m.hm) throw invalid("the H- continuum is listed twice");
+      m.hm = true;
+      tabulate_hm(m);
+      continue;
+    }
     else if (fo == "Rayleigh") {
       op.index = species_id(s);
       if (op.index < 0) throw invalid("Opacity species " + s + " has not been found");
@@ -776,6 +835,8 @@ static void setup_atmosphere(Model& m) {
   }
   a.cloud = m.cloud;
   a.cloud_fb = m.cloud_fb;
+  a.cloud_kind = m.cloud ? m.cloud_kind : 0;
+  a.cloud_ref_wl = m.cloud_ref_wl;
   a.fit_mmw = m.fit_mmw;
   a.var_g = m.var_g;
   // table species: temperature nodes and the (parameter-independent) pressure bracket of
@@ -817,8 +878,10 @@ static void setup_atmosphere(Model& m) {
       }
     }
   }
-  a.R = (int)m.rayleigh_species.size();
-  for (int r = 0; r < a.R; ++r) a.ray_index[r] = m.opac[m.rayleigh_species[r]].index;
+  a.R_ray = (int)m.rayleigh_species.size();
+  for (int r = 0; r < a.R_ray; ++r) a.ray_index[r] = m.opac[m.rayleigh_species[r]].index;
+  a.hm = m.hm;
+  a.R = a.R_ray + (m.hm ? kHmTerms : 0);
 }
 
 // ------------------------------------------------------------------ stellar spectrum
@@ -967,7 +1030,7 @@ void finalize_host(Model& m) {
   if (m.occultation) m.nparam_general = 2 + (m.star_model == 1 ? 1 : m.star_model == 3 ? 3 : 0);
   m.nparam_chem = 0;
   for (auto& c : m.chem) m.nparam_chem += c.kind == 0 ? (int)c.sp.size() : 0;
-  m.nparam_cloud = m.cloud ? (m.cloud_fb ? 2 : 3) : 0;
+  m.nparam_cloud = m.cloud ? (m.cloud_fb ? 2 : 3) + (m.cloud_kind == 1 ? 1 : m.cloud_kind == 2 ? 3 : 0) : 0;
   m.nparam_mod = 0;
   for (auto& o : m.obs) m.nparam_mod += o.nb_modifier;
   m.nparam_total = m.nparam_general + m.nparam_chem + m.nparam_temp + m.nparam_cloud + m.nparam_mod;

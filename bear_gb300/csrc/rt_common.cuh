@@ -118,14 +118,31 @@ __device__ __forceinline__ double level_absorption_fp64(const double* __restrict
   return level_absorption_fp64_cb(tab, N, d, S, k, NoTerm64{});
 }
 
+// Wavelength factor of the non-grey clouds at wavenumber k (1 for grey):
+// power law wl^a / wl_ref^a (PowerLawCloudModel::opticalProperties
+// src/cloud_model/power_law_cloud_model.cpp:113-119), KH non-grey
+// Q_ref / (q0 x^-a0 + x^0.2) with x = 2 pi r / wl (KHCloudModel::opticalProperties
+// src/cloud_model/kh_cloud_model.cpp:115-132), FP64.
+__device__ __forceinline__ double cloud_shape(const DeviceModel& dm, const EvalInfo& e, int k) {
+  const double wl = __ldg(&dm.wl[k]);
+  if (dm.cloud_kind == 1) return pow(wl, e.cs[0]) / e.cs[3];
+  const double x = e.cs[2] / wl;
+  return e.cs[3] / (e.cs[0] * pow(x, -e.cs[1]) + pow(x, 0.2));
+}
+
 // Optical depth of emission layer l (between levels l-1 and l),
 // dz (k_l + k_{l-1}) / 2 + cloud, and its reciprocal, in double-float; FP64 when
 // an opacity has a term outside the float range or the depth is outside the
 // comfortable float range.
+// SHAPE: the cloud depth is scaled by the non-grey cloud factor (csh, FP64, and its
+// double-float split csd).
+template <bool SHAPE = false>
 __device__ __forceinline__ void emission_layer_tau_df(const LevelInfo* __restrict__ lv, int l, const Kappa& kap,
-                                                      const Kappa& kap_prev, double& tau, double& rtau) {
+                                                      const Kappa& kap_prev, double& tau, double& rtau,
+                                                      double csh = 1.0, df2 csd = df2{1.0f, 0.0f}) {
   const float4 g = __ldg(reinterpret_cast<const float4*>(&lv[l - 1].dzh_hi));  // dzh, cloud
-  const df2 t = df_add(df_mul(df2{g.x, g.y}, df_add(kap.v, kap_prev.v)), df2{g.z, g.w});
+  const df2 cl = SHAPE ? df_mul(df2{g.z, g.w}, csd) : df2{g.z, g.w};
+  const df2 t = df_add(df_mul(df2{g.x, g.y}, df_add(kap.v, kap_prev.v)), cl);
   // both wide parts zero (+-0), tested on the bits to stay off the FP64 pipe
   const bool narrow = ((__double_as_longlong(kap.wide) | __double_as_longlong(kap_prev.wide)) << 1) == 0;
   if (narrow && t.hi > 1e-30f && t.hi < 1e30f) {
@@ -133,7 +150,7 @@ __device__ __forceinline__ void emission_layer_tau_df(const LevelInfo* __restric
     rtau = df_to_double(df_div(df_make(1.0f), t));
   } else {
     const double ks = (df_to_double(kap.v) + kap.wide) + (df_to_double(kap_prev.v) + kap_prev.wide);
-    tau = __ldg(&lv[l - 1].dz) * ks / 2. + __ldg(&lv[l - 1].cloud);
+    tau = __ldg(&lv[l - 1].dz) * ks / 2. + (SHAPE ? __ldg(&lv[l - 1].cloud) * csh : __ldg(&lv[l - 1].cloud));
     rtau = 1.0 / tau;
   }
 }

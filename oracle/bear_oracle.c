@@ -95,7 +95,7 @@ typedef struct {
 } obs_t;
 
 typedef struct {
-  int kind;                  /* 0 line/CIA table, 1 Rayleigh only */
+  int kind;                  /* 0 line/CIA table, 1 Rayleigh only, 2 H- continuum */
   int index;                 /* species_index */
   int partner[2]; int npartner;
   double mass;
@@ -103,6 +103,8 @@ typedef struct {
   int* nP; double** P; double** logP;  /* per T, ascending */
   double*** rows;            /* rows[t][p] -> N log10 cross sections */
   double* rayleigh;          /* N */
+  double* hm_bf;             /* N: H- bound-free cross section (kind 2) */
+  double* hm_ff[7];          /* [1..6] x N: the free-free polynomials in wavelength (kind 2) */
 } opac_t;
 
 typedef struct orc_model {
@@ -123,6 +125,8 @@ typedef struct orc_model {
   int nchem; int chem_kind[8]; int chem_nsp[8]; int chem_sp[8][SP_COUNT]; int chem_bg_h2he[8]; int chem_bg_sp[8];
   int chem_na_free[8];
   int cloud; int cloud_fb;
+  int cloud_kind;            /* 0 grey, 1 power_law, 2 KHnongrey */
+  double cloud_ref_wl;       /* reference wavelength (um) of the non-grey clouds */
   int fit_mmw, fit_sh, var_g;
   int nopac; opac_t opac[64];
   char opac_sym[64][64], opac_folder[64][512];
@@ -216,8 +220,17 @@ orc_model* orc_create(const char* text) {
       } else { set_err("unsupported chemistry %s", tok[1]); goto fail; }
     } else if (!strcmp(k, "cloud")) {
       if (!strcmp(tok[1], "none")) continue;
-      if (strcmp(tok[1], "grey")) { set_err("unsupported cloud %s", tok[1]); goto fail; }
-      m->cloud = 1; m->cloud_fb = (nt >= 3 && !strcmp(tok[2], "fb"));
+      /* selectCloudModel src/cloud_model/select_cloud_model.h:42-100 */
+      if (!strcmp(tok[1], "grey")) {
+        m->cloud_kind = 0; m->cloud_fb = (nt >= 3 && !strcmp(tok[2], "fb"));
+      } else if (!strcmp(tok[1], "power_law") || !strcmp(tok[1], "KHnongrey")) {
+        /* PowerLawCloudModel / KHCloudModel ctors: reference wavelength, optional "fb" */
+        if (nt < 3) { set_err("the %s cloud needs a reference wavelength", tok[1]); goto fail; }
+        m->cloud_kind = !strcmp(tok[1], "power_law") ? 1 : 2;
+        m->cloud_ref_wl = atof(tok[2]);
+        m->cloud_fb = (nt == 4 && !strcmp(tok[3], "fb"));
+      } else { set_err("unsupported cloud %s", tok[1]); goto fail; }
+      m->cloud = 1;
     } else if (!strcmp(k, "opacity")) {
       int o = m->nopac++;
       snprintf(m->opac_sym[o], 64, "%s", tok[1]);
@@ -669,6 +682,44 @@ static int tabulate_rayleigh(orc_model* m, opac_t* op, int sp) {
   return 0;
 }
 
+/* GasHm src/transport_coeff/h_m.cpp:36-137: the wavelength-dependent parts of the H-
+ * bound-free cross section (photo-detachment threshold 1.6419 um, valid above 0.125 um)
+ * and of the free-free polynomials (two coefficient sets, above 0.3645 um and from
+ * 0.1823 to 0.3645 um); the temperature factors are applied per level. */
+static void tabulate_hm(orc_model* m, opac_t* op) {
+  static const double lambda_0 = 1.6419;
+  static const double Cn[7] = {0.0, 152.519, 49.534, -118.858, 92.536, -34.194, 4.982};
+  static const double A1[7] = {0.0, 0.0, 2483.3460, -3449.8890, 2200.0400, -696.2710, 88.2830};
+  static const double B1[7] = {0.0, 0.0, 285.8270, -1158.3820, 2427.7190, -1841.4000, 444.5170};
+  static const double C1[7] = {0.0, 0.0, -2054.2910, 8746.5230, -13651.1050, 8624.9700, -1863.8650};
+  static const double D1[7] = {0.0, 0.0, 2827.7760, -11485.6320, 16755.5240, -10051.5300, 2095.2880};
+  static const double E1[7] = {0.0, 0.0, -1341.5370, 5303.6090, -7510.4940, 4400.0670, -901.7880};
+  static const double F1[7] = {0.0, 0.0, 208.9520, -812.9390, 1132.7380, -655.0200, 132.9850};
+  static const double A2[7] = {0.0, 518.1021, 473.2636, -482.2089, 115.5291, 0.0, 0.0};
+  static const double B2[7] = {0.0, -734.8666, 1443.4137, -737.1616, 169.6374, 0.0, 0.0};
+  static const double C2[7] = {0.0, 1021.1775, -1977.3395, 1096.8827, -245.6490, 0.0, 0.0};
+  static const double D2[7] = {0.0, -479.0721, 922.3575, -521.1341, 114.2430, 0.0, 0.0};
+  static const double E2[7] = {0.0, 93.1373, -178.9275, 101.7963, -21.9972, 0.0, 0.0};
+  static const double F2[7] = {0.0, -6.4285, 12.3600, -7.0571, 1.5097, 0.0, 0.0};
+  const size_t N = m->N;
+  op->hm_bf = (double*)calloc(N, sizeof(double));
+  for (int i = 1; i < 7; ++i) op->hm_ff[i] = (double*)calloc(N, sizeof(double));
+  for (size_t k = 0; k < N; ++k) {
+    const double l = m->wl[k];
+    if (l <= lambda_0 && l >= 0.125) {
+      double f = 0;
+      for (int i = 1; i < 7; ++i) f += Cn[i] * pow((1.0 / l - 1.0 / lambda_0), (i - 1) / 2.0);
+      op->hm_bf[k] = 1e-18 * l * l * l * pow(1.0 / l - 1.0 / lambda_0, 1.5) * f;
+    }
+    const double *A = NULL, *B = NULL, *C = NULL, *D = NULL, *E = NULL, *F = NULL;
+    if (l > 0.3645) { A = A1; B = B1; C = C1; D = D1; E = E1; F = F1; }
+    else if (l >= 0.1823) { A = A2; B = B2; C = C2; D = D2; E = E2; F = F2; }
+    if (A)
+      for (int i = 1; i < 7; ++i)
+        op->hm_ff[i][k] = l * l * A[i] + B[i] + C[i] / l + D[i] / l / l + E[i] / l / l / l + F[i] / l / l / l / l;
+  }
+}
+
 static int setup_opacity(orc_model* m) {
   /* TransportCoefficients::addOpacitySpecies src/transport_coeff/transport_coeff.cpp:98-237 */
   for (int i = 0; i < m->nopac; ++i) {
@@ -678,7 +729,7 @@ static int setup_opacity(orc_model* m) {
     if (!strcmp(s, "CIA-H2-H2")) { op->kind = 0; op->index = SP_H2; op->partner[op->npartner++] = SP_H2; }
     else if (!strcmp(s, "CIA-H2-He")) { op->kind = 0; op->index = SP_H2; op->partner[op->npartner++] = SP_He; }
     else if (!strcmp(s, "CIA-H-He")) { op->kind = 0; op->index = SP_H; op->partner[op->npartner++] = SP_He; }
-    else if (!strcmp(s, "H-")) { set_err("H- continuum is not restated in the oracle"); return -1; }
+    else if (!strcmp(s, "H-")) { op->kind = 2; op->index = SP_Hm; tabulate_hm(m, op); continue; }
     else if (!strcmp(fo, "Rayleigh")) {
       int sp = species_id(s);
       if (sp < 0) { set_err("unknown Rayleigh species %s", s); return -1; }
@@ -896,7 +947,9 @@ int orc_finalize(orc_model* m) {
   }
   m->nparam_chem = 0;
   for (int c = 0; c < m->nchem; ++c) m->nparam_chem += m->chem_kind[c] == 0 ? m->chem_nsp[c] : 0;
-  m->nparam_cloud = m->cloud ? (m->cloud_fb ? 2 : 3) : 0;
+  /* grey [tau, p_top, (bottom factor)]; power_law [tau, exponent, p_top, (...)];
+   * KHnongrey [tau, q0, a0, particle size, p_top, (...)] */
+  m->nparam_cloud = m->cloud ? (m->cloud_fb ? 2 : 3) + (m->cloud_kind == 1 ? 1 : m->cloud_kind == 2 ? 3 : 0) : 0;
   m->nparam_mod = 0; m->M = 0;
   for (int k = 0; k < m->nobs; ++k) { m->nparam_mod += m->obs[k].nb_modifier; m->obs[k].out_offset = m->M; m->M += m->obs[k].n; }
   m->nparam_total = m->nparam_general + m->nparam_chem + m->nparam_temp + m->nparam_cloud + m->nparam_mod;
@@ -1114,6 +1167,19 @@ static void species_coefficients(const orc_model* m, const opac_t* op, const dou
     #pragma omp parallel for
     for (long i = 0; i < (long)N; ++i) scattering[i * L + level] += op->rayleigh[i] * ns;
   }
+  if (op->kind == 2) {
+    /* GasHm::calcContinuumAbsorption h_m.cpp:36-53 with freeFreeAbsorption :88-137 */
+    double pw[7];
+    for (int i = 1; i < 7; ++i) pw[i] = pow(5040.0 / T, (i + 1) / 2.0);
+    const double pe = n[SP_e] * K_BOLTZMANN * T, nh = n[SP_H], nhm = n[SP_Hm];
+    #pragma omp parallel for
+    for (long i = 0; i < (long)N; ++i) {
+      double x = 0;
+      for (int j = 1; j < 7; ++j) x += pw[j] * op->hm_ff[j][i];
+      const double kff = x * 1e-29;
+      absorption[i * L + level] += op->hm_bf[i] * nhm + kff * pe * nh;
+    }
+  }
 }
 
 /* ------------------------------------------------------------------ radiative transfer */
@@ -1124,13 +1190,15 @@ static double planck_wn(double T, double nu) {
 }
 
 /* ShortCharacteristics::calcSpectrum src/radiative_transfer/short_characteristics.cpp:39-125 */
-static double sc_point(const orc_model* m, const double* kappa, const double* cloud_tau, const atm_t* a, size_t nu_i) {
+static double sc_point(const orc_model* m, const double* kappa, const double* cloud_tau, const double* cnum,
+                       const double* cden, const atm_t* a, size_t nu_i) {
   const int L = m->L;
   const double mu[2] = {0.211324865405187, 0.788675134594813};
   const double w[2] = {0.5, 0.5};
   double tau[512], B[512];
   for (int i = 0; i < L - 1; ++i) tau[i] = (a->z[i + 1] - a->z[i]) * (kappa[i + 1] + kappa[i]) / 2.;
-  if (cloud_tau) for (int i = 0; i < L - 1; ++i) tau[i] += cloud_tau[i];
+  if (cloud_tau)
+    for (int i = 0; i < L - 1; ++i) tau[i] += cnum ? cloud_tau[i] * cnum[nu_i] / cden[nu_i] : cloud_tau[i];
   for (int i = 0; i < L; ++i) B[i] = planck_wn(a->T[i], m->nu[nu_i]);
   double I1 = B[0], I2 = B[0];
   for (int i = 0; i < L - 1; ++i) {
@@ -1270,11 +1338,31 @@ int orc_forward(const orc_model* m, const double* par, int P, double* spectrum, 
     for (int s = 0; s < m->nopac; ++s)
       species_coefficients(m, &m->opac[s], a.nd + (size_t)l * SP_COUNT, a.T[l], m->p[l], l, absorption, scattering);
 
-  double* cloud_tau = NULL;   /* [L-1] identical for every nu (grey) */
+  double* cloud_tau = NULL;   /* [L-1] layer optical depth of the grey placement */
+  double *cnum = NULL, *cden = NULL;  /* non-grey clouds: layer depth x cnum / cden per nu */
   if (m->cloud) {
-    /* GreyCloudModel::opticalProperties src/cloud_model/grey_cloud_model.cpp:59-106 */
-    double tau_c = cloud[0], ptop = cloud[1], pbot = 0;
-    if (!m->cloud_fb) pbot = ptop * cloud[2];
+    /* GreyCloudModel::opticalProperties src/cloud_model/grey_cloud_model.cpp:59-106;
+     * PowerLawCloudModel::opticalProperties power_law_cloud_model.cpp:69-121 and
+     * KHCloudModel::opticalProperties kh_cloud_model.cpp:69-133 place the cloud the same way */
+    const int it = m->cloud_kind == 0 ? 1 : m->cloud_kind == 1 ? 2 : 4;
+    double tau_c = cloud[0], ptop = cloud[it], pbot = 0;
+    if (!m->cloud_fb) pbot = ptop * cloud[it + 1];
+    if (m->cloud_kind) {
+      cnum = (double*)malloc(N * sizeof(double)); cden = (double*)malloc(N * sizeof(double));
+      if (m->cloud_kind == 1) {
+        const double expo = cloud[1], ref = pow(m->cloud_ref_wl, expo);
+        for (size_t i = 0; i < N; ++i) { cnum[i] = pow(m->wl[i], expo); cden[i] = ref; }
+      } else {
+        const double q0 = cloud[1], a0 = cloud[2], r = cloud[3];
+        const double xr = 2 * K_PI * r / m->cloud_ref_wl;
+        const double refq = q0 * pow(xr, -a0) + pow(xr, 0.2);
+        for (size_t i = 0; i < N; ++i) {
+          const double x = 2 * K_PI * r / m->wl[i];
+          cnum[i] = refq;
+          cden[i] = q0 * pow(x, -a0) + pow(x, 0.2);
+        }
+      }
+    }
     if (tau_c < 0) tau_c = 0;
     unsigned ti, bi;
     cloud_position(m, &a, ptop, pbot, m->cloud_fb, &ti, &bi);
@@ -1289,7 +1377,7 @@ int orc_forward(const orc_model* m, const double* par, int P, double* spectrum, 
     /* OccultationModel::calcModelCPU src/forward_model/secondary_eclipse/secondary_eclipse.cpp:183-246:
      * planet emission without the radius-distance scaling, stellar spectrum from the model */
     #pragma omp parallel for schedule(dynamic, 16)
-    for (long i = 0; i < (long)N; ++i) spec[i] = sc_point(m, absorption + (size_t)i * L, cloud_tau, &a, (size_t)i);
+    for (long i = 0; i < (long)N; ++i) spec[i] = sc_point(m, absorption + (size_t)i * L, cloud_tau, cnum, cden, &a, (size_t)i);
     star = (double*)malloc(N * sizeof(double));
     if (m->star_model == 3) star_grid_flux(m, gen + 2, star);
     else
@@ -1298,7 +1386,7 @@ int orc_forward(const orc_model* m, const double* par, int P, double* spectrum, 
   } else if (!m->transmission) {
     const double scaling = (K_RJUP / gen[2]) * (K_RJUP / gen[2]) * gen[1];
     #pragma omp parallel for schedule(dynamic, 16)
-    for (long i = 0; i < (long)N; ++i) spec[i] = sc_point(m, absorption + (size_t)i * L, cloud_tau, &a, (size_t)i);
+    for (long i = 0; i < (long)N; ++i) spec[i] = sc_point(m, absorption + (size_t)i * L, cloud_tau, cnum, cden, &a, (size_t)i);
     for (size_t i = 0; i < N; ++i) spec[i] *= scaling;
   } else {
     const double R = gen[1], Rs = gen[2];
@@ -1311,7 +1399,11 @@ int orc_forward(const orc_model* m, const double* par, int P, double* spectrum, 
     #pragma omp parallel for schedule(dynamic, 16)
     for (long i = 0; i < (long)N; ++i) {
       double chi[512];
-      for (int l = 0; l < L; ++l) chi[l] = absorption[(size_t)i * L + l] + scattering[(size_t)i * L + l] + (ext ? ext[l] : 0.0);
+      for (int l = 0; l < L; ++l) {
+        double e = ext ? ext[l] : 0.0;
+        if (cnum && l > 0) e = cloud_tau[l - 1] * cnum[i] / cden[i] / (a.z[l] - a.z[l - 1]);
+        chi[l] = absorption[(size_t)i * L + l] + scattering[(size_t)i * L + l] + e;
+      }
       spec[i] = transit_point(m, chi, &a, R, Rs);
     }
     free(ext);
@@ -1343,7 +1435,7 @@ int orc_forward(const orc_model* m, const double* par, int P, double* spectrum, 
   free(star);
   if (spectrum) memcpy(spectrum, spec, N * sizeof(double));
   *neglect_out = neglect;
-  free(spec); free(absorption); free(scattering); free(cloud_tau);
+  free(spec); free(absorption); free(scattering); free(cloud_tau); free(cnum); free(cden);
   free(a.T); free(a.z); free(a.H); free(a.mmw); free(a.nd);
   return 0;
 }

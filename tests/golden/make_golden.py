@@ -197,6 +197,74 @@ def main():
         make("transmission_rayleigh", spec, "transmission", tmpl, obs, np.array(rows), [0, 2],
              attach_kind="transmission")
 
+    # 10-11. the H- bound-free + free-free continuum (GasHm) with H, H- and e- in the chemistry,
+    #        in a hot emission model and a transmission model, 0.33-3.3 um
+    for kind in ("emission", "transmission"):
+        name = f"{kind}_hminus"
+        if which and name not in which:
+            continue
+        base = syn.CONFIGS["emission_plain" if kind == "emission" else "transmission_plain"]
+        spec = dataclasses.replace(base, name=name, model=kind, nb_levels=45, nu_min=3000.0, nu_max=30500.0,
+                                   nu_step=4.0, species=["H2O", "CO"],
+                                   temperature="poly" if kind == "emission" else "const", cloud=False,
+                                   seed=20261240 + (kind == "transmission"),
+                                   rayleigh=() if kind == "emission" else ("H2",))
+
+        def tmpl(t):
+            assert "chemistry iso H2O CO\n" in t
+            t = t.replace("chemistry iso H2O CO\n", "chemistry iso H2O CO H H- e-\n")
+            return t + "opacity H-\n"
+        edges = np.geomspace(0.34, 3.2, 51)
+        o1 = Observation("bins", "band-spectroscopy", np.stack([edges[:-1], edges[1:]], axis=1), np.ones(50),
+                         np.ones(50))
+        wl = np.geomspace(0.5, 1.6, 30)
+        o2 = Observation("spec", "spectroscopy", wl, np.ones(30), np.ones(30))
+        o2.instrument_profile_fwhm = list(wl / 300.0)
+        obs = [o1, o2]
+        rows = []
+        for T, xs in ((2600.0, [1e-4, 3e-4, 1e-3, 3e-9, 1e-6]), (3400.0, [1e-5, 1e-4, 1e-2, 1e-8, 1e-5]),
+                      (1900.0, [1e-3, 1e-3, 1e-5, 1e-10, 1e-8])):
+            if kind == "emission":  # an inverted-free profile falling from T to 0.55 T at the top
+                rows.append([4.5, 1.0, 10 * syn.PARSEC] + xs + [T, 0.95, 0.9, 0.85, 0.8, 0.85])
+            else:
+                rows.append([3.0, 1.4 * syn.R_JUPITER, syn.R_SUN] + xs + [T])
+        zero = list(rows[0])
+        zero[6] = 0.0   # no H-: the reference skips the whole continuum (free-free included)
+        rows.append(zero)
+        make(name, spec, kind, tmpl, obs, np.array(rows), [0, 1], attach_kind=kind)
+
+    # 12-13. non-grey clouds: a power-law cloud (reference wavelength 1 um, free bottom) in
+    #        emission and a KH non-grey cloud (reference 1.5 um, fixed bottom) in transmission
+    for name, kind, cl in (("emission_powerlaw_cloud", "emission", "cloud power_law 1.0\n"),
+                           ("transmission_kh_cloud", "transmission", "cloud KHnongrey 1.5 fb\n")):
+        if which and name not in which:
+            continue
+        base = syn.CONFIGS["emission_plain" if kind == "emission" else "transmission_plain"]
+        spec = dataclasses.replace(base, name=name, model=kind, nb_levels=50, nu_min=2500.0, nu_max=16500.0,
+                                   nu_step=2.0, species=["H2O", "CO", "CH4"], cloud=False, seed=20261250 + len(kind),
+                                   temperature="poly" if kind == "emission" else "const")
+
+        def tmpl(t, cl=cl):
+            return t + cl
+        edges = np.geomspace(0.65, 3.8, 49)
+        o1 = Observation("bins", "band-spectroscopy", np.stack([edges[:-1], edges[1:]], axis=1), np.ones(48),
+                         np.ones(48))
+        wl = np.geomspace(1.0, 2.5, 40)
+        o2 = Observation("spec", "spectroscopy", wl, np.ones(40), np.ones(40))
+        o2.instrument_profile_fwhm = list(wl / 200.0)
+        obs = [o1, o2]
+        rows = []
+        if kind == "emission":
+            for tau, a, ptop, frac, T in ((2.0, -2.0, 0.3, 8.0, 1600.0), (8.0, -4.0, 1.0, 3.0, 2100.0),
+                                          (0.5, 1.0, 0.05, 20.0, 1200.0)):
+                rows.append([4.8, 1.0, 10 * syn.PARSEC, 1e-4, 3e-4, 1e-6, T, 0.9, 0.85, 0.8, 0.85, 0.9,
+                             tau, a, ptop, frac])
+        else:
+            for tau, q0, a0, r, ptop, T in ((5.0, 10.0, 4.0, 0.5, 0.01, 1300.0), (20.0, 3.0, 6.0, 1.5, 1e-3, 900.0),
+                                            (1.0, 30.0, 2.0, 0.1, 0.1, 1900.0)):
+                rows.append([3.1, 1.3 * syn.R_JUPITER, syn.R_SUN, 1e-4, 1e-4, 1e-5, T, tau, q0, a0, r, ptop])
+        make(name, spec, kind, tmpl, obs, np.array(rows), [0, 1], attach_kind=kind)
+
     # 6-8. secondary eclipse (occultation depth, ppm) with a blackbody, a file and a grid star:
     #      40 levels, 2 cm^-1 sampling from 1.0 to 6.7 um, an R=100 spectrum with an instrument
     #      profile and a shift modifier, descending bins, two photon-counting filters
