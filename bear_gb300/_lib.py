@@ -56,6 +56,7 @@ EXPORTS = {
     "bear_model_table_info": (C.c_int, [C.c_void_p, _ip, _ip, _ip, C.POINTER(C.c_longlong)]),
     "bear_model_stencil_rows": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_longlong)]),
     "bear_model_set_priors": (C.c_int, [C.c_void_p, C.c_int, _ip, _dp, _dp, _dp, _ip]),
+    "bear_contribution_functions": (C.c_int, [C.c_void_p, _dp, C.c_int, _dp, _dp, C.c_void_p]),
     "bear_prior_transform_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     "bear_loglike_cube_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                           C.c_void_p, C.c_void_p]),

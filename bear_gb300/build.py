@@ -41,6 +41,7 @@ def _units():
         ("adjoint_transmission.cu", common_cu),
         ("noalloc.cu", common_cu),
         ("priors.cu", common_cu),
+        ("contribution.cu", common_cu),
         # bit-faithful host-style arithmetic: no FMA contraction
         ("atmosphere.cu", common_cu + ["--fmad=false"]),
         ("model_setup.cpp", common_cpp + ["-Xcompiler", "-ffp-contract=off"]),

@@ -272,7 +272,7 @@ int bear_model_table_info(const bear_model* h, int* levels, int* table_species, 
     require_prepared(h);
     if (levels) *levels = h->m.L;
     if (table_species) *table_species = h->m.acfg.S;
-    if (rayleigh_species) *rayleigh_species = h->m.acfg.R;
+    if (rayleigh_species) *rayleigh_species = h->m.acfg.R_ray;
     if (table_rows) *table_rows = h->m.n_rows;
   });
 }
@@ -367,6 +367,18 @@ int bear_loglike_noalloc(bear_model* h, const double* params_dev, int nb_params,
     require_params(h, nb_params);
     if (!params_dev || !loglike_dev) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null device buffer");
     bgb::loglike_noalloc(h->m, params_dev, loglike_dev, neglect_dev, (cudaStream_t)stream);
+  });
+}
+
+int bear_contribution_functions(bear_model* h, const double* params, int nb_params, double* cf_bins,
+                                double* cf_spectrum, void* stream) {
+  return guarded([&] {
+    require_ready(h);
+    if (h->m.transmission)
+      throw bgb::Error(BEAR_ERR_UNSUPPORTED, "contribution functions exist for emission and secondary-eclipse models");
+    const cudaStream_t st = (cudaStream_t)stream;
+    run_plain(h, params, nb_params, st);
+    bgb::contribution_functions(h->m, st, cf_spectrum, cf_bins);
   });
 }
 

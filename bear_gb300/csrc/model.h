@@ -361,6 +361,12 @@ struct Model {
   GradWorkspace gws;
   size_t grad_budget = size_t(16) << 30;  // bytes of gradient work buffers per chunk
   DevicePrior* d_priors = nullptr;  // prior table (bear_model_set_priors)
+  // contribution functions: device L x N buffer and the wavelength-integration operator
+  // (rows in internal order, cf_out = caller-order index), built on first use
+  double* d_cf = nullptr;
+  std::vector<double> cf_W;
+  std::vector<int> cf_k0, cf_len, cf_out;
+  std::vector<long long> cf_off;
   int n_priors = 0;
   double* h_pinned = nullptr;  // pinned staging for the plain path
   size_t h_pinned_bytes = 0;
@@ -377,6 +383,8 @@ void add_observation(Model& m, const char* name, const char* type, int n, const 
                      const double* fwhm, int nfilter, const double* fwl, const double* fresp,
                      const char* detector, const char* modifier);
 void finalize_host(Model& m);
+void compose_operator_rows(const Model& m, const ObservationSetup& o, bool is_flux, std::vector<double>& W,
+                           std::vector<int>& row_k0, std::vector<int>& row_len, std::vector<long long>& row_off);
 
 // engine.cu
 void upload_model(Model& m);
@@ -394,6 +402,8 @@ void loglike_noalloc(Model& m, const double* params_dev, double* loglike_dev, ui
 long long stencil_rows(Model& m, int batch);
 void launch_forward_taps(Model& m, const double* params_dev, int batch, cudaStream_t stream,
                          uint8_t* neglect_dev, double* loglike_dev, const ForwardTaps& taps);
+// contribution.cu
+void contribution_functions(Model& m, cudaStream_t stream, double* spectrum, double* bins);
 // priors.cu
 void set_priors(Model& m, int n, const int* type, const double* a, const double* b, const double* unit,
                 const int* link);

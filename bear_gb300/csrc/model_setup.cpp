@@ -493,13 +493,20 @@ static void build_observation_operator(Model& m, ObservationSetup& o) {
       for (double r : o.filter_grid)
         if (r < 0) throw unsupported("negative filter response combined with an instrument profile");
   }
-  const bool is_flux = !m.transmission;
+  compose_operator_rows(m, o, !m.transmission, m.W, o.row_k0, o.row_len, o.row_off);
+}
+
+// The rows of one observation's composite operator (filter, convolution, bin integration)
+// for flux (is_flux: wavenumber integral over the band) or wavelength integration,
+// appended to W; k0 / len / off receive each row's first wavenumber, length and offset.
+void compose_operator_rows(const Model& m, const ObservationSetup& o, bool is_flux, std::vector<double>& W,
+                           std::vector<int>& row_k0, std::vector<int>& row_len, std::vector<long long>& row_off) {
   auto filt = [&](size_t k) -> double {
     return o.nfilter ? o.filter_grid[k] * o.filter_weight[k] / o.filter_norm : 1.0;
   };
-  o.row_k0.resize(o.n);
-  o.row_len.resize(o.n);
-  o.row_off.resize(o.n);
+  row_k0.resize(o.n);
+  row_len.resize(o.n);
+  row_off.resize(o.n);
   for (int b = 0; b < o.n; ++b) {
     const size_t i0 = o.edge_idx[b][0], i1 = o.edge_idx[b][1];
     // band integration weights on the (convolved) points i0..i1
@@ -563,10 +570,10 @@ static void build_observation_operator(Model& m, ObservationSetup& o) {
         row[j - klo] += wb * (-0.5 * cw) * g * filt(j);
       }
     }
-    o.row_k0[b] = (int)klo;
-    o.row_len[b] = (int)row.size();
-    o.row_off[b] = (long long)m.W.size();
-    m.W.insert(m.W.end(), row.begin(), row.end());
+    row_k0[b] = (int)klo;
+    row_len[b] = (int)row.size();
+    row_off[b] = (long long)W.size();
+    W.insert(W.end(), row.begin(), row.end());
   }
 }
 

@@ -114,6 +114,18 @@ class Engine:
                                                 C.byref(neg), C.c_void_p(stream)))
         return spec, obs[: self.M], bool(neg.value)
 
+    def contribution_functions(self, params, stream: int = 0):
+        """Contribution functions of one parameter set (emission and secondary-eclipse
+        models): (binned, levels x M in compute_model's observation order; high-resolution,
+        levels x N). Level 0 is the bottom of the atmosphere."""
+        p = self._params(params)
+        L = self.table_info()["levels"]
+        bins = np.empty((L, max(self.M, 1)))
+        hr = np.empty((L, self.N))
+        _lib.check(self._lib.bear_contribution_functions(self._h, _lib.dptr(p), p.size, _lib.dptr(bins),
+                                                         _lib.dptr(hr), C.c_void_p(stream)))
+        return bins[:, : self.M], hr
+
     def loglike(self, params, stream: int = 0) -> float:
         p = self._params(params)
         out = C.c_double(0.0)

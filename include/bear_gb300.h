@@ -147,6 +147,18 @@ int bear_loglike(bear_model* m, const double* params, int nb_params, double* log
 int bear_loglike_batch(bear_model* m, const double* params_dev, int batch, int nb_params,
                        double* loglike_dev, uint8_t* neglect_dev, void* stream);
 
+/* Contribution functions of one parameter set (emission and secondary-eclipse models;
+ * EmissionModel::postProcessContributionFunctions
+ * src/forward_model/emission/emission_post_process.cpp:330-376, kernel
+ * src/CUDA_kernels/contribution_function_kernels.cu:21-66): per level i the share
+ * 2 pi B(T_i) (1 - exp(-dtau_i)) exp(-sum of dtau above) of the gas absorption layer
+ * below it (level 0: 0). cf_spectrum (host, levels x spectral points) and cf_bins
+ * (host, levels x observation points, each level in the order of bear_compute_model's
+ * observations, binned by wavelength integration as the reference does) may be NULL.
+ * Level 0 is the bottom of the atmosphere. Transmission models: BEAR_ERR_UNSUPPORTED. */
+int bear_contribution_functions(bear_model* m, const double* params, int nb_params, double* cf_bins,
+                                double* cf_spectrum, void* stream);
+
 /* --------------------------------------------------------------- priors on the device
  * The reference converts MultiNest's hypercube coordinates to parameters on the host,
  * one point at a time (Retrieval::convertHypercubeParameters

@@ -1440,6 +1440,60 @@ int orc_forward(const orc_model* m, const double* par, int P, double* spectrum, 
   return 0;
 }
 
+/* Contribution functions: contributionFunctionDevice
+ * src/CUDA_kernels/contribution_function_kernels.cu:21-66 as driven by
+ * EmissionModel::postProcessContributionFunctions src/forward_model/emission/emission_post_process.cpp:330-376
+ * (secondary eclipse: secondary_eclipse_post_process.cpp:255-305): gas absorption only, from
+ * the top down, CF_i = 2 pi B(T_i) (1 - exp(-dtau_i)) x the transmission above; level 0 is
+ * left 0 here (never written by the reference). hr: L x N; bins: L x M, each level binned with
+ * wavelength integration (is_flux = false) and in the caller's order. The reference keeps its
+ * opacities as floats on the GPU; this restatement is FP64 throughout. */
+int orc_contribution(const orc_model* m, const double* par, int P, double* hr, double* bins) {
+  if (!m->finalized) { set_err("model not finalized"); return -1; }
+  if (m->transmission) { set_err("contribution functions exist for emission models only"); return -1; }
+  if (P < m->nparam_total) { set_err("expected %d parameters, got %d", m->nparam_total, P); return -1; }
+  const int L = m->L; const size_t N = m->N;
+  const double* gen = par;
+  const double* chem = par + m->nparam_general;
+  const double* temp = chem + m->nparam_chem;
+  atm_t a;
+  a.T = (double*)malloc(L * sizeof(double)); a.z = (double*)malloc(L * sizeof(double));
+  a.H = (double*)malloc(L * sizeof(double)); a.mmw = (double*)malloc(L * sizeof(double));
+  a.nd = (double*)malloc((size_t)L * SP_COUNT * sizeof(double));
+  atmosphere(m, temp, chem, pow(10, gen[0]), 1.0, 0.0, &a);
+  double* absorption = (double*)calloc(N * L, sizeof(double));
+  double* scattering = (double*)calloc(N * L, sizeof(double));
+  for (int l = 0; l < L; ++l)
+    for (int s = 0; s < m->nopac; ++s)
+      species_coefficients(m, &m->opac[s], a.nd + (size_t)l * SP_COUNT, a.T[l], m->p[l], l, absorption, scattering);
+  double* cf = (double*)calloc(N * L, sizeof(double));
+  #pragma omp parallel for
+  for (long k = 0; k < (long)N; ++k) {
+    double tcum = 1.0;
+    for (int i = L - 1; i > 0; --i) {
+      const double dz = a.z[i] - a.z[i - 1];
+      const double dtau = dz * (absorption[(size_t)k * L + i] + absorption[(size_t)k * L + i - 1]) / 2.;
+      const double t = exp(-dtau);
+      cf[(size_t)i * N + k] = 2 * K_PI * planck_wn(a.T[i], m->nu[k]) * (1.0 - t) * tcum;
+      tcum *= t;
+    }
+  }
+  if (hr) memcpy(hr, cf, N * L * sizeof(double));
+  if (bins) {
+    for (int l = 0; l < L; ++l)
+      for (int k = 0; k < m->nobs; ++k) {
+        const obs_t* o = &m->obs[k];
+        double* bands = (double*)malloc((o->n ? o->n : 1) * sizeof(double));
+        process_observation(m, o, cf + (size_t)l * N, 0, bands);
+        for (int b = 0; b < o->n; ++b) bins[(size_t)l * m->M + o->out_offset + b] = o->ascending ? bands[o->n - 1 - b] : bands[b];
+        free(bands);
+      }
+  }
+  free(cf); free(absorption); free(scattering);
+  free(a.T); free(a.z); free(a.H); free(a.mmw); free(a.nd);
+  return 0;
+}
+
 /* Retrieval::logLikelihood src/retrieval/retrieval.cpp:314-369 */
 int orc_loglike(const orc_model* m, const double* par, int P, double* loglike, double* obs_out) {
   double* obs = obs_out ? obs_out : (double*)malloc((m->M ? m->M : 1) * sizeof(double));

@@ -47,6 +47,8 @@ def lib():
         L.orc_grid.argtypes = [C.c_void_p, _dp]
         L.orc_forward.restype = C.c_int
         L.orc_forward.argtypes = [C.c_void_p, _dp, C.c_int, _dp, _dp, C.POINTER(C.c_int)]
+        L.orc_contribution.restype = C.c_int
+        L.orc_contribution.argtypes = [C.c_void_p, _dp, C.c_int, _dp, _dp]
         L.orc_loglike.restype = C.c_int
         L.orc_loglike.argtypes = [C.c_void_p, _dp, C.c_int, _dp, _dp]
         L.orc_last_error.restype = C.c_char_p
@@ -108,6 +110,15 @@ class OracleModel:
         if lib().orc_forward(self.h, _ptr(p), p.size, _ptr(spec), _ptr(obs), C.byref(neg)):
             raise RuntimeError("oracle: " + lib().orc_last_error().decode())
         return spec, obs[: self.M], bool(neg.value)
+
+    def contribution(self, params, levels: int):
+        """Contribution functions: (levels x N high-resolution, levels x M binned)."""
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        hr = np.empty((levels, self.N))
+        bins = np.empty((levels, max(self.M, 1)))
+        if lib().orc_contribution(self.h, _ptr(p), p.size, _ptr(hr), _ptr(bins)):
+            raise RuntimeError("oracle: " + lib().orc_last_error().decode())
+        return hr, bins[:, : self.M]
 
     def set_tau_cutoff(self, tau: float) -> None:
         """Optical depth at which transmission tangent sums stop (10, the reference's; inf: none)."""
