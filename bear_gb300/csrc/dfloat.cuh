@@ -30,6 +30,8 @@
 static inline float bgb_int_as_float(int i) { float f; std::memcpy(&f, &i, 4); return f; }
 static inline long long bgb_double_as_ll(double d) { long long i; std::memcpy(&i, &d, 8); return i; }
 static inline double bgb_ll_as_double(long long i) { double d; std::memcpy(&d, &i, 8); return d; }
+static inline unsigned bgb_float_as_uint(float f) { unsigned u; std::memcpy(&u, &f, 4); return u; }
+static inline int bgb_clz(unsigned x) { return __builtin_clz(x); }
 #else
 #define BGB_HD __device__ __forceinline__
 #define BGB_FADD(a, b) __fadd_rn((a), (b))
@@ -42,6 +44,8 @@ static inline double bgb_ll_as_double(long long i) { double d; std::memcpy(&d, &
 #define bgb_int_as_float(i) __int_as_float(i)
 #define bgb_double_as_ll(d) __double_as_longlong(d)
 #define bgb_ll_as_double(i) __longlong_as_double(i)
+#define bgb_float_as_uint(f) __float_as_uint(f)
+#define bgb_clz(x) __clz((int)(x))
 #endif
 
 #include "dfconst.h"
@@ -60,7 +64,33 @@ BGB_HD df2 df_from_double(double x) {
   return {hi, (float)(x - (double)hi)};
 }
 
-BGB_HD double df_to_double(df2 a) { return (double)a.hi + (double)a.lo; }
+// float -> double by moving the sign, exponent (rebiased by 1023 - 127) and mantissa into
+// place with integer operations (exact for normal numbers and zero, which is all a
+// conversion does): keeps the conversion off the FP64 pipe, where an F2F would issue.
+// Subnormals, infinities and NaN take the ordinary conversion.
+BGB_HD double f2d_bits(float f) {
+  const unsigned u = bgb_float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+  if (e - 1u < 254u)
+    return bgb_ll_as_double((long long)(sign | ((unsigned long long)(e + 896u) << 52) |
+                                        ((unsigned long long)(u & 0x7fffffu) << 29)));
+  if ((u & 0x7fffffffu) == 0u) return bgb_ll_as_double((long long)sign);
+  return (double)f;
+}
+
+// int -> double with integer operations (exact; |k| < 2^31).
+BGB_HD double i2d_bits(int k) {
+  if (k == 0) return 0.0;
+  const unsigned long long sign = k < 0 ? 0x8000000000000000ull : 0ull;
+  const unsigned a = k < 0 ? 0u - (unsigned)k : (unsigned)k;
+  const int msb = 31 - bgb_clz(a);
+  const unsigned long long mant = ((unsigned long long)a << (52 - msb)) & 0xfffffffffffffull;
+  return bgb_ll_as_double((long long)(sign | ((unsigned long long)(1023 + msb) << 52) | mant));
+}
+
+// hi + lo in FP64: the two conversions on the integer pipe, one FP64 add.
+BGB_HD double df_to_double(df2 a) { return f2d_bits(a.hi) + f2d_bits(a.lo); }
 
 // TwoSum: s + e == a + b exactly.
 BGB_HD df2 two_sum(float a, float b) {
@@ -173,8 +203,8 @@ BGB_HD double pow2d(int n) { return n < -1022 ? 0.0 : bgb_ll_as_double((long lon
 BGB_HD double exp_tang(double x, const double* tab) {
   const double shifter = 6755399441055744.0;  // 1.5 * 2^52: rounds to an integer
   const double t = BGB_DMA(x, k64OverLn2, shifter);
-  const double kd = t - shifter;
   const int k = (int)(bgb_double_as_ll(t) & 0xffffffff);
+  const double kd = i2d_bits(k);  // == t - shifter
   double r = BGB_DMA(-kd, kLn2Over64Hi, x);
   r = BGB_DMA(-kd, kLn2Over64Lo, r);
   double p = BGB_DMA(r, 1.0 / 120.0, 1.0 / 24.0);
@@ -195,8 +225,8 @@ BGB_HD double exp_tang(double x, const double* tab) {
 BGB_HD double exp_tang2048(double x, const double* tab) {
   const double shifter = 6755399441055744.0;  // 1.5 * 2^52
   const double t = BGB_DMA(x, k2048OverLn2, shifter);
-  const double kd = t - shifter;
   const int k = (int)(bgb_double_as_ll(t) & 0xffffffff);
+  const double kd = i2d_bits(k);  // == t - shifter, formed on the integer pipe
   double r = BGB_DMA(-kd, kLn2Over2048Hi, x);
   r = BGB_DMA(-kd, kLn2Over2048Lo, r);
   double p = BGB_DMA(r, 1.0 / 6.0, 0.5);

@@ -66,7 +66,7 @@ constexpr size_t kTransmissionDynSmem = 220 * 1024;
 // staged in dynamic shared memory as double-floats (L x kHmTerms float2) and added to
 // the level absorption; a non-grey cloud scales the cloud depths by its wavelength factor.
 template <bool STORE, bool EXT = false>
-__global__ void __launch_bounds__(256) emission_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
+__global__ void __launch_bounds__(256, 6) emission_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
                                                        const LevelSpecies* __restrict__ ls,
                                                        const LevelSpeciesDF* __restrict__ lsdf,
                                                        const double* __restrict__ ray_n,

@@ -652,11 +652,12 @@ def main():
     fp64_peak = fp64_peak_tflops(torch, device)
 
     # The binding roof is FP64 issue: FP64-pipe instructions per wavenumber and layer
-    # counted from the kernel source (emission: tau and 1/tau and B_nu converted from
-    # double-float, 3 each; two Gauss angles of delta, exp_tang2048 (8), q (3) and the
-    # update (3); dB), against the DFMA rate implied by a measured DGEMM.
+    # counted from the kernel source (emission: the double-float -> double conversions of
+    # tau, 1/tau and B_nu, one FP64 add each (the float -> double steps run on the integer
+    # pipe); dB; per Gauss angle delta (1), exp_tang2048 (7), q (3) and the update (3)),
+    # against the DFMA rate implied by a measured DGEMM.
     if kind == "emission":
-        ops_per_point_layer = 3 + 3 + 3 + 1 + 2 * (1 + 8 + 3 + 3)
+        ops_per_point_layer = 3 + 1 + 2 * (1 + 7 + 3 + 3)
         fp64_ops = B * (L - 1) * N * ops_per_point_layer
     else:
         ops_per_point_layer = None

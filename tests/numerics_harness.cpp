@@ -5,6 +5,7 @@
 #define BGB_HOST_EMULATION
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <random>
 
 #include "../bear_gb300/csrc/physics.cuh"
@@ -56,8 +57,26 @@ int main() {
     const double Bp = planck_df(df_from_double(c1), c2ld, df_from_double(1.0 / T), kExp2TabHi, kExp2TabLo);
     if (c2 / T < 690.0) e_planck = std::fmax(e_planck, (double)fabsl(Bp / rp - 1));
   }
+  // integer-pipe conversions: bit-identical to the FP64 conversions they replace
+  long long conv_mismatch = 0;
+  std::uniform_int_distribution<unsigned> bits(0u, 0xffffffffu);
+  auto same = [](double a, double b) {
+    return (std::isnan(a) && std::isnan(b)) || bgb_double_as_ll(a) == bgb_double_as_ll(b);
+  };
+  for (int i = 0; i < 4000000; ++i) {
+    unsigned u = bits(g);
+    if (i < 512) u = (i & 1) ? (0x80000000u | (unsigned)(i >> 1)) : (unsigned)(i >> 1);  // zeros, subnormals
+    if (i >= 512 && i < 1024) u = ((unsigned)(i & 255) << 23) | (u & 0x807fffffu);        // every exponent
+    float f;
+    std::memcpy(&f, &u, 4);
+    if (!same(f2d_bits(f), (double)f)) ++conv_mismatch;
+  }
+  for (int k = -3000000; k <= 3000000; ++k)
+    if (!same(i2d_bits(k), (double)k)) ++conv_mismatch;
+  for (int k : {2147483647, -2147483647, 1 << 30, -(1 << 30)})
+    if (!same(i2d_bits(k), (double)k)) ++conv_mismatch;
   std::printf("df_exp2 %.3e\nexp_tang %.3e\nexp_tang2048 %.3e\nexp_tang2048_ulp %.3f\ndf_exp_neg %.3e\n"
-              "df_pow10 %.3e\nplanck_df %.3e\n",
-              e_exp2, e_tang, e_tang2048, ulp2048, e_expneg, e_pow10, e_planck);
+              "df_pow10 %.3e\nplanck_df %.3e\nconversion_mismatches %lld\n",
+              e_exp2, e_tang, e_tang2048, ulp2048, e_expneg, e_pow10, e_planck, conv_mismatch);
   return 0;
 }

@@ -10,7 +10,9 @@ against long-double references over the argument ranges the kernels use:
   tangent-ray transmission;
 * df_exp2 / 10^x: double-float exponentials of the opacity assembly;
 * planck_df: the double-float Planck function;
-* df_exp_neg: the double-float exp(-delta) of the adjoint.
+* df_exp_neg: the double-float exp(-delta) of the adjoint;
+* f2d_bits / i2d_bits: float and int to double built with integer operations
+  (bit-identical to the conversions, checked on every exponent, zeros and subnormals).
 
 The bounds are the accuracy figures the kernels rely on (about 1 ulp for the
 FP64 routines; the double-float ones are limited by their ~48-bit inputs).
@@ -32,6 +34,7 @@ BOUNDS = {
     "df_pow10": 2e-12,          # |x| <= 40: 10^x from a 48-bit x log2(10)
     "df_exp_neg": 1e-12,        # d <= 60
     "planck_df": 1e-11,         # x = h nu c / k T up to 690: ~x 2^-48 from the 48-bit exponent
+    "conversion_mismatches": 0,  # float / int -> double on the integer pipe: bit-identical
 }
 
 
