@@ -58,12 +58,6 @@ struct df2 {
 
 BGB_HD df2 df_make(float hi) { return {hi, 0.0f}; }
 
-// Split an FP64 value into a double-float (exact for |x| in the float range).
-BGB_HD df2 df_from_double(double x) {
-  const float hi = (float)x;
-  return {hi, (float)(x - (double)hi)};
-}
-
 // float -> double by moving the sign, exponent (rebiased by 1023 - 127) and mantissa into
 // place with integer operations (exact for normal numbers and zero, which is all a
 // conversion does): keeps the conversion off the FP64 pipe, where an F2F would issue.
@@ -87,6 +81,12 @@ BGB_HD double i2d_bits(int k) {
   const int msb = 31 - bgb_clz(a);
   const unsigned long long mant = ((unsigned long long)a << (52 - msb)) & 0xfffffffffffffull;
   return bgb_ll_as_double((long long)(sign | ((unsigned long long)(1023 + msb) << 52) | mant));
+}
+
+// Split an FP64 value into a double-float (exact for |x| in the float range).
+BGB_HD df2 df_from_double(double x) {
+  const float hi = (float)x;
+  return {hi, (float)(x - (double)hi)};
 }
 
 // hi + lo in FP64: the two conversions on the integer pipe, one FP64 add.

@@ -178,20 +178,21 @@ __device__ __forceinline__ void sc_layer(double tau, double B, double B_prev, do
 
 // The same layer in fewer FP64 operations, used by the default kernel:
 // I a + (1+q) B + (-a-q) B' == a (I - B') + B + q (B - B'), with q = (a-1)/delta and
-// 1/tau supplied by the caller (computed in double-float). The exponential
+// 1/tau supplied by the caller (computed in double-float); q (B - B') is formed as
+// (a - 1) (mu ((B - B') / tau)). The exponential
 // (exp_tang2048; tab2048 = 2^(j/2048)) and the recurrence stay FP64.
 __device__ __forceinline__ void sc_layer_fast(double tau, double rtau, double B, double B_prev, double& I1,
                                               double& I2, const double* tab2048) {
   if ((__double_as_longlong(tau) << 1) == 0) return;  // tau == 0 (bit test)
-  const double dB = B - B_prev;
+  // q dB = (a - 1) mu (dB / tau): dB / tau shared by both angles
+  const double u = (B - B_prev) * rtau;
 #pragma unroll
   for (int i = 0; i < 2; ++i) {
     const double d = tau * kInvMu[i];
     const double a = __double_as_longlong(d) > kBits700 ? 0.0 : exp_tang2048(-d, tab2048);
-    const double q = (a - 1.0) * (kMu[i] * rtau);
     double& I = i == 0 ? I1 : I2;
     I = fma(a, I - B_prev, B);
-    I = fma(q, dB, I);
+    I = fma(a - 1.0, kMu[i] * u, I);
   }
 }
 
