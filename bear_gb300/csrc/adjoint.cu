@@ -524,6 +524,203 @@ __global__ void __launch_bounds__(kAdjThreads, DF ? 6 : 4) emission_adjoint_kern
   }
 }
 
+// ------------------------------------------------------------------ split adjoint (precision mode 0)
+// The default gradient splits the emission adjoint in two kernels so that the
+// opacity recomputation and the per-level reductions run with full occupancy:
+//
+// emission_adjoint_sweep_kernel   one thread per (evaluation, wavenumber): the reverse
+//     short-characteristics recurrence from the forward's stored intensities, layer
+//     optical depths and half opacity sums (so no opacities are recomputed here), the
+//     Planck function recomputed per level; writes d log L / d kappa of every level and
+//     reduces the level sinks that need no opacity: temperature through B_nu, layer
+//     thickness and cloud depth (values S, S+1, S+2 of the partial sums).
+// emission_adjoint_sinks_kernel   one block per (evaluation, level, 512 wavenumbers), four
+//     wavenumbers per thread: recomputes the species terms of the level opacity and their
+//     temperature slope, accumulates d log L / d ln n_s and the opacity part of
+//     d log L / dT in registers over the four wavenumbers, then one warp reduce-scatter and
+//     one block reduction (values 0 .. S).
+// The two write disjoint tile slots of the (zeroed) partial sums, which
+// atmosphere_adjoint_kernel reduces as before.
+struct SweepArgs {
+  const LevelInfo* lev;
+  const EvalInfo* ev;
+  const double* istore;
+  const float4* layer;  // forward's layer optical depth and half opacity sum
+  const double* gS;
+  const double* seed;
+  float2* gK;           // out: d log L / d kappa per (evaluation, level, wavenumber)
+  double* partial;
+  int V, tiles_total;
+};
+
+__global__ void __launch_bounds__(kAdjThreads) emission_adjoint_sweep_kernel(DeviceModel dm, SweepArgs a) {
+  constexpr int NW = kAdjThreads / 32;
+  __shared__ ExpTables et;
+  __shared__ double red[NW][4];
+  load_exp_tables(et);
+  __syncthreads();
+  const int S = dm.S, L = dm.L;
+  const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int kk = blockIdx.y * kAdjThreads + tid;
+  const bool active = kk < dm.N;
+  const int k = active ? kk : dm.N - 1;  // idle lanes repeat the last wavenumber with a zero seed
+  const size_t N = dm.N;
+  const LevelInfo* lv = a.lev + (size_t)b * L;
+  const double* Is = a.istore + (size_t)b * L * 2 * N + k;
+  const float4* lay = a.layer + (size_t)b * L * N + k;
+  float2* gKo = a.gK + (size_t)b * L * N + k;
+
+  // seed: d log L / dF_k = sum_r W_rk gS_r, F = scaling 2 pi 1e-3 (mu1 I1 + mu2 I2) / 2
+  double gF = 0.0;
+  {
+    const double* g = a.gS + (size_t)b * dm.M;
+    const int e1 = __ldg(&dm.col_ptr[k + 1]);
+    for (int e = __ldg(&dm.col_ptr[k]); e < e1; ++e) gF = fma(__ldg(&dm.col_w[e]), g[__ldg(&dm.col_row[e])], gF);
+  }
+  const double sd = active ? gF * a.seed[b * 3] * __ldg(&a.ev[b].scaling) * (kPi * 1e-3) : 0.0;
+
+  const float2 c1f = __ldg(dm.planck_c1_df + k), c2f = __ldg(dm.planck_c2l_df + k);
+  const df2 c1 = {c1f.x, c1f.y}, c2l = {c2f.x, c2f.y};
+  const df2 c2 = df_mul(c2l, df2{kLn2Hi, kLn2Lo});  // h nu c / k
+  const df2 rc1 = df_div(df_make(1.0f), c1);
+  auto invT = [&](int l) {
+    const float2 it = __ldg(reinterpret_cast<const float2*>(&lv[l].invT_hi));
+    return df2{it.x, it.y};
+  };
+  // dB/dT = B (1 + B / c1) x / T with x = c2 / T
+  auto dplanck = [&](int l, df2 B) {
+    const df2 it = invT(l);
+    return df_mul(df_mul(B, df_add(df_make(1.0f), df_mul(B, rc1))), df_mul(df_mul(c2, it), it));
+  };
+  // the three opacity-free sinks of level l, reduced over the block
+  auto emit3 = [&](int l, df2 gBT, df2 gdz, df2 gcl) {
+    df2 v[4] = {gBT, gdz, gcl, df2{0.0f, 0.0f}};
+    const df2 r = warp_reduce_scatter<4>(v, lane);
+    if ((lane & 7) == 0) red[warp][lane >> 3] = df_to_double(r);
+    __syncthreads();
+    if (tid < 3) {
+      double sum = 0.0;
+#pragma unroll
+      for (int w = 0; w < NW; ++w) sum += red[w][tid];
+      a.partial[(((size_t)b * L + l) * a.V + S + tid) * a.tiles_total + blockIdx.y] = sum;
+    }
+    __syncthreads();
+  };
+
+  const df2 z = {0.0f, 0.0f};
+  df2 lam1 = df_from_double(sd * kMu[0]), lam2 = df_from_double(sd * kMu[1]);
+  df2 B_l = planck_df2(c1, c2l, invT(L - 1), et.hi, et.lo);
+  df2 gB_l = z, gK_l = z, gdz_l = z, gcl_l = z;
+  for (int l = L - 1; l >= 1; --l) {
+    const df2 B_m = planck_df2(c1, c2l, invT(l - 1), et.hi, et.lo);
+    const float4 tk = lay[(size_t)l * N];
+    const df2 t = {tk.x, tk.y}, ksh = {tk.z, tk.w};
+    const float2 gz = __ldg(reinterpret_cast<const float2*>(&lv[l - 1].dzh_hi));
+    const df2 dzh = {gz.x, gz.y};
+    df2 gB_m = z, gtau = z;
+    if (t.hi != 0.0f) {
+      const df2 rt = t.hi > 1e-30f ? df_div(df_make(1.0f), t) : z;  // only used above delta = 1e-2
+      const df2 Ip1 = df_from_double(Is[(size_t)(l - 1) * 2 * N]);
+      const df2 Ip2 = df_from_double(Is[(size_t)(l - 1) * 2 * N + N]);
+      sc_layer_adjoint_df(t, rt, B_l, B_m, Ip1, Ip2, lam1, lam2, gB_l, gB_m, gtau, et);
+    }
+    gK_l = df_add(gK_l, df_mul(gtau, dzh));
+    if (active) gKo[(size_t)l * N] = make_float2(gK_l.hi, gK_l.lo);
+    emit3(l, df_mul(gB_l, dplanck(l, B_l)), gdz_l, gcl_l);
+    // layer l's own sinks belong to lev[l-1] (its dz and cloud)
+    gdz_l = df_mul(gtau, ksh);
+    gcl_l = gtau;
+    gK_l = df_mul(gtau, dzh);
+    gB_l = gB_m;
+    B_l = B_m;
+  }
+  gB_l = df_add(gB_l, df_add(lam1, lam2));  // both angles start from I = B at the bottom level
+  if (active) gKo[0] = make_float2(gK_l.hi, gK_l.lo);
+  emit3(0, df_mul(gB_l, dplanck(0, B_l)), gdz_l, gcl_l);
+}
+
+struct SinkArgs {
+  const LevelSpeciesDF* lsdf;
+  const float2* dwT;
+  const float2* gK;
+  double* partial;
+  int V, tiles_total, tile0;  // this kernel's slots start at tile0
+};
+
+constexpr int kSinkKPT = 4;  // wavenumbers per thread of the sink kernel
+
+template <int VP>
+__global__ void __launch_bounds__(kAdjThreads) emission_adjoint_sinks_kernel(DeviceModel dm, SinkArgs a) {
+  constexpr int NW = kAdjThreads / 32;
+  constexpr int G = 32 / VP;
+  __shared__ ExpTables et;
+  __shared__ double red[NW][VP];
+  load_exp_tables(et);
+  __syncthreads();
+  const int S = dm.S, L = dm.L;
+  const int b = blockIdx.x, l = blockIdx.y, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const size_t N = dm.N;
+  const LevelSpeciesDF* sf = a.lsdf + ((size_t)b * L + l) * S;
+  const float2* dwl = a.dwT + ((size_t)b * L + l) * S;
+  const float2* gKl = a.gK + ((size_t)b * L + l) * N;
+  const df2 z = {0.0f, 0.0f};
+  df2 acc[VP];
+#pragma unroll
+  for (int j = 0; j < VP; ++j) acc[j] = z;
+#pragma unroll 1
+  for (int j = 0; j < kSinkKPT; ++j) {
+    const int k = (blockIdx.z * kSinkKPT + j) * kAdjThreads + tid;
+    if (k >= dm.N) break;
+    const float2 gk = gKl[k];
+    if (gk.x == 0.0f) continue;
+    const df2 gK = {gk.x, gk.y};
+    double gK64 = 0.0;
+    df2 dk = z;
+    double dkw = 0.0;
+#pragma unroll
+    for (int s = 0; s < VP - 1; ++s) {
+      if (s >= S) break;
+      // species term 2^y of the level opacity (level_kappa_df_cb) and its temperature slope
+      const int4 rw = __ldg(reinterpret_cast<const int4*>(sf + s));
+      const float4 fb = __ldg(reinterpret_cast<const float4*>(sf + s) + 1);  // wT, log2 n
+      if (fb.z == kNoSpecies) continue;
+      const float2 t0 = __ldg(dm.ltab + (size_t)rw.x * N + k);
+      const float2 t1 = __ldg(dm.ltab + (size_t)rw.y * N + k);
+      const df2 lo = {t0.x, t0.y}, hi = {t1.x, t1.y};
+      const df2 y = df_add(df_lerp(lo, hi, df2{fb.x, fb.y}), df2{fb.z, fb.w});
+      int n;
+      const df2 m = df_exp2(y, n, et.hi, et.lo);
+      const float2 d = __ldg(dwl + s);
+      const bool narrow = n > -100 && n < 100;
+      const df2 slope = df_mul(df_sub(hi, lo), df2{d.x, d.y});
+      if (narrow) {
+        const df2 t = df_ldexp(m, n);
+        acc[s] = df_add(acc[s], df_mul(gK, t));
+        if (d.x != 0.0f) dk = df_add(dk, df_mul(t, slope));
+      } else {
+        const double tw = df_to_double(m) * pow2d(n);
+        if (gK64 == 0.0) gK64 = df_to_double(gK);
+        acc[s] = df_add(acc[s], df_from_double(gK64 * tw));
+        if (d.x != 0.0f) dkw += tw * df_to_double(slope);
+      }
+    }
+    // opacity part of d log L / dT: gK d kappa / dT (level-table values are log2: d 2^y / dy = 2^y ln 2)
+    acc[VP - 1] = df_add(acc[VP - 1], df_mul(gK, df_mul(dk, df2{kLn2Hi, kLn2Lo})));
+    if (dkw != 0.0) acc[VP - 1] = df_add(acc[VP - 1], df_from_double(df_to_double(gK) * dkw * 0.693147180559945309));
+  }
+  const df2 r = warp_reduce_scatter<VP>(acc, lane);
+  if (lane % G == 0) red[warp][lane / G] = df_to_double(r);
+  __syncthreads();
+  // value slot j < S: species j; slot VP-1: temperature (value S of the partial sums)
+  if (tid < VP && (tid < S || tid == VP - 1)) {
+    double sum = 0.0;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) sum += red[w][tid];
+    const int v = tid < S ? tid : S;
+    a.partial[(((size_t)b * L + l) * a.V + v) * a.tiles_total + a.tile0 + blockIdx.z] = sum;
+  }
+}
+
 // ------------------------------------------------------------------ parameter tangents
 // One block per evaluation. sg[L][V] = the partial sums reduced over the tiles;
 // then thread th < P forms d log L / d param_th = sum over levels of the sinks
@@ -662,6 +859,8 @@ void free_grad_workspace(Model& m) {
   GradWorkspace& g = m.gws;
   cudaFree(g.taps.dwT);
   cudaFree(g.taps.istore);
+  cudaFree(g.taps.em_layer);
+  cudaFree(g.em_gK);
   cudaFree(g.gS);
   cudaFree(g.seed);
   cudaFree(g.partial);
@@ -683,19 +882,25 @@ int value_slots(int V) { return V <= 8 ? 8 : V <= 16 ? 16 : 32; }
 
 size_t adjoint_smem(const Model& m) { return (size_t)2 * m.acfg.S * kAdjThreads * (sizeof(float2) + sizeof(double)); }
 
-size_t grad_bytes_per_eval(const Model& m, int tiles, int V) {
+// split: the double-float path's per-(level, wavenumber) layer data and d log L / d kappa
+size_t grad_bytes_per_eval(const Model& m, int tiles, int V, bool split) {
   const size_t L = m.L, N = m.N, S = std::max(m.acfg.S, 1), M = std::max(m.M, 1);
-  return L * 2 * N * 8 + L * S * sizeof(float2) + M * 8 + 3 * 8 + L * (size_t)V * tiles * 8;
+  return L * 2 * N * 8 + L * S * sizeof(float2) + M * 8 + 3 * 8 + L * (size_t)V * tiles * 8 +
+         (split ? L * N * (sizeof(float4) + sizeof(float2)) : 0);
 }
 
-void ensure_grad_workspace(Model& m, int chunk, int tiles, int V) {
+void ensure_grad_workspace(Model& m, int chunk, int tiles, int V, bool split) {
   GradWorkspace& g = m.gws;
-  if (chunk <= g.capacity && tiles == g.tiles) return;
+  if (chunk <= g.capacity && tiles == g.tiles && (!split || g.em_gK)) return;
   BGB_CUDA(cudaDeviceSynchronize());
   free_grad_workspace(m);
   const size_t B = chunk, L = m.L, N = m.N, S = std::max(m.acfg.S, 1), M = std::max(m.M, 1);
   BGB_CUDA(cudaMalloc(&g.taps.dwT, B * L * S * sizeof(float2)));
   BGB_CUDA(cudaMalloc(&g.taps.istore, B * L * 2 * N * sizeof(double)));
+  if (split) {
+    BGB_CUDA(cudaMalloc(&g.taps.em_layer, B * L * N * sizeof(float4)));
+    BGB_CUDA(cudaMalloc(&g.em_gK, B * L * N * sizeof(float2)));
+  }
   BGB_CUDA(cudaMalloc(&g.gS, B * M * sizeof(double)));
   BGB_CUDA(cudaMalloc(&g.seed, B * 3 * sizeof(double)));
   BGB_CUDA(cudaMalloc(&g.partial, B * L * (size_t)V * tiles * sizeof(double)));
@@ -768,12 +973,17 @@ void launch_gradient(Model& m, const double* params_dev, int batch, cudaStream_t
   const int V = S + 3;
   if (V > 32) throw Error(BEAR_ERR_UNSUPPORTED, "the gradient supports at most 29 table species");
   if (P > kAdjThreads) throw Error(BEAR_ERR_UNSUPPORTED, "the gradient supports at most 128 parameters");
-  const int tiles = (int)((m.N + kAdjThreads - 1) / kAdjThreads);
-  const size_t per_eval = grad_bytes_per_eval(m, tiles, V);
+  const bool df = m.precision == 0;
+  // tile slots of the partial sums: the fused / sweep kernel's (128 wavenumbers each), then
+  // in the double-float path the sink kernel's (kSinkKPT x 128 wavenumbers each)
+  const int tiles_a = (int)((m.N + kAdjThreads - 1) / kAdjThreads);
+  const int tiles_b = df ? (int)((m.N + kSinkKPT * kAdjThreads - 1) / (kSinkKPT * kAdjThreads)) : 0;
+  const int tiles = tiles_a + tiles_b;
+  const size_t per_eval = grad_bytes_per_eval(m, tiles, V, df);
   const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)batch, m.grad_budget / per_eval));
   BGB_CUDA(cudaSetDevice(m.device));
   ensure_workspace(m, chunk);
-  ensure_grad_workspace(m, chunk, tiles, V);
+  ensure_grad_workspace(m, chunk, tiles, V, df);
   const GradWorkspace& g = m.gws;
   const Workspace& w = m.ws;
   const size_t smem = adjoint_smem(m);
@@ -784,7 +994,7 @@ void launch_gradient(Model& m, const double* params_dev, int batch, cudaStream_t
     BGB_CUDA(cudaFuncSetAttribute(atmosphere_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem_atm));
   const int VP = value_slots(V);
-  const bool df = m.precision == 0;
+  const int VPB = value_slots(S + 1);
   for (int c0 = 0; c0 < batch; c0 += chunk) {
     const int nb = std::min(chunk, batch - c0);
     const double* pc = params_dev + (size_t)c0 * P;
@@ -793,11 +1003,19 @@ void launch_gradient(Model& m, const double* params_dev, int batch, cudaStream_t
     obs_adjoint_kernel<<<nb, 256, 0, st>>>(m.dm, pc, P, w.ev, w.obs, g.gS, g.seed, gc, 0);
     BGB_CUDA(cudaGetLastError());
     AdjointArgs a{w.lev, w.ls, w.lsdf, w.ev, g.taps.dwT, g.taps.istore, g.gS, g.seed, g.partial, V};
-    const dim3 grid(nb, tiles);
+    const dim3 grid(nb, tiles_a);
     if (df) {
-      if (VP == 8) launch_emission_adjoint<true, 8>(m, grid, smem, st, a);
-      else if (VP == 16) launch_emission_adjoint<true, 16>(m, grid, smem, st, a);
-      else launch_emission_adjoint<true, 32>(m, grid, smem, st, a);
+      BGB_CUDA(cudaMemsetAsync(g.partial, 0, (size_t)nb * L * V * tiles * sizeof(double), st));
+      SweepArgs sa{w.lev, w.ev, g.taps.istore, g.taps.em_layer, g.gS, g.seed, g.em_gK, g.partial, V, tiles};
+      emission_adjoint_sweep_kernel<<<grid, kAdjThreads, 0, st>>>(m.dm, sa);
+      BGB_CUDA(cudaGetLastError());
+      if (S > 0) {
+        SinkArgs ka{w.lsdf, g.taps.dwT, g.em_gK, g.partial, V, tiles, tiles_a};
+        const dim3 gridb(nb, L, tiles_b);
+        if (VPB == 8) emission_adjoint_sinks_kernel<8><<<gridb, kAdjThreads, 0, st>>>(m.dm, ka);
+        else if (VPB == 16) emission_adjoint_sinks_kernel<16><<<gridb, kAdjThreads, 0, st>>>(m.dm, ka);
+        else emission_adjoint_sinks_kernel<32><<<gridb, kAdjThreads, 0, st>>>(m.dm, ka);
+      }
     } else {
       if (VP == 8) launch_emission_adjoint<false, 8>(m, grid, smem, st, a);
       else if (VP == 16) launch_emission_adjoint<false, 16>(m, grid, smem, st, a);

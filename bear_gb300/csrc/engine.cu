@@ -59,7 +59,9 @@ constexpr size_t kTransmissionDynSmem = 220 * 1024;
 // Fused opacity assembly + short characteristics, one thread per wavenumber.
 // Writes the flux in W m^-2 cm times the radius-distance scaling. With STORE the
 // two Gauss-angle intensities after every level are also written to
-// istore[b][l][angle][k] (the adjoint pass reads them back top-down).
+// istore[b][l][angle][k] (the adjoint pass reads them back top-down), and, when
+// layer_store is given, each layer's optical depth and half opacity sum as
+// double-floats to layer_store[b][l][k] (layer l between levels l-1 and l).
 //
 // EXT (models with the H- continuum or a non-grey cloud): the H- continuum (rows R_ray
 // .. R-1 of the linear-term table, coefficients in ray_n) has its level coefficients
@@ -71,7 +73,8 @@ __global__ void __launch_bounds__(256, 6) emission_kernel(DeviceModel dm, const 
                                                        const LevelSpeciesDF* __restrict__ lsdf,
                                                        const double* __restrict__ ray_n,
                                                        const EvalInfo* __restrict__ ev,
-                                                       double* __restrict__ spectrum, double* __restrict__ istore) {
+                                                       double* __restrict__ spectrum, double* __restrict__ istore,
+                                                       float4* __restrict__ layer_store = nullptr) {
   __shared__ ExpTables et;
   __shared__ double tab2048[2048];
   extern __shared__ float2 hm_s[];  // [L][kHmTerms] when the H- continuum is on
@@ -126,7 +129,13 @@ __global__ void __launch_bounds__(256, 6) emission_kernel(DeviceModel dm, const 
     const Kappa kap = kappa(l);
     const double B = planck(l);
     double tau, rtau;
-    emission_layer_tau_df<EXT>(lv, l, kap, kap_prev, tau, rtau, csh, csd);
+    if (STORE) {
+      float4 tk;
+      emission_layer_tau_df<EXT, true>(lv, l, kap, kap_prev, tau, rtau, csh, csd, &tk);
+      layer_store[((size_t)b * L + l) * N + k] = tk;
+    } else {
+      emission_layer_tau_df<EXT>(lv, l, kap, kap_prev, tau, rtau, csh, csd);
+    }
     sc_layer_fast(tau, rtau, B, B_prev, I1, I2, tab2048);
     if (STORE) {
       Is[(size_t)l * 2 * N] = I1;
@@ -874,7 +883,7 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
       emission_kernel_fp64<true><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.ray_n, w.ev, w.spectrum, taps->istore);
     else if (taps)  // the gradient rejects H- models
       emission_kernel<true><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.spectrum,
-                                                taps->istore);
+                                                taps->istore, taps->em_layer);
     else if (m.precision == 1)
       emission_kernel_fp64<false><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.ray_n, w.ev, w.spectrum, nullptr);
     else if (m.hm || m.acfg.cloud_kind)

@@ -222,6 +222,8 @@ struct Workspace {
 struct ForwardTaps {
   float2* dwT = nullptr;     // B x L x S: d wT / dT of every stencil (double-float)
   double* istore = nullptr;  // emission, B x L x 2 x N: Gauss-angle intensities after every level
+  float4* em_layer = nullptr;  // emission, B x L x N: layer optical depth and (k_l + k_{l-1}) / 2
+                               // as double-floats (layer l between levels l-1 and l; l = 0 unused)
   // transmission, per (evaluation, level, wavenumber) as double-floats unless noted
   float2* tr_geo = nullptr;  // per evaluation 3 x L x L: dG/dz_j (P), dG/dz_t (Q), dG/dR (U)
   float2* tr_c = nullptr;    // extinction pair sums chi_i + chi_{i+1}
@@ -238,7 +240,8 @@ struct GradWorkspace {
   ForwardTaps taps;
   double* gS = nullptr;      // B x M: d log L / d binned model
   double* seed = nullptr;    // B x 3: seed normaliser, its inverse, sum_r gS_r (s_r - shift_r)
-  double* partial = nullptr; // B x L x V x tiles per-block sinks of the adjoint kernel
+  double* partial = nullptr; // B x L x V x tiles per-block sinks of the adjoint kernel(s)
+  float2* em_gK = nullptr;   // emission, B x L x N: d log L / d kappa per level (double-float)
   // transmission adjoint, per (evaluation, level, wavenumber), double-floats
   float2* tr_gc = nullptr;    // d log L / d (chi_j + chi_{j+1})
   float2* tr_gz = nullptr;    // d log L / d z_j

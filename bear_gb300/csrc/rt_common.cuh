@@ -136,10 +136,13 @@ __device__ __forceinline__ double cloud_shape(const DeviceModel& dm, const EvalI
 // comfortable float range.
 // SHAPE: the cloud depth is scaled by the non-grey cloud factor (csh, FP64, and its
 // double-float split csd).
-template <bool SHAPE = false>
+// OUT (gradient pass): tk receives the layer optical depth as a double-float (FP64 values
+// clamped to 1e37) and (k_l + k_{l-1}) / 2, as the adjoint uses them.
+template <bool SHAPE = false, bool OUT = false>
 __device__ __forceinline__ void emission_layer_tau_df(const LevelInfo* __restrict__ lv, int l, const Kappa& kap,
                                                       const Kappa& kap_prev, double& tau, double& rtau,
-                                                      double csh = 1.0, df2 csd = df2{1.0f, 0.0f}) {
+                                                      double csh = 1.0, df2 csd = df2{1.0f, 0.0f},
+                                                      float4* tk = nullptr) {
   const float4 g = __ldg(reinterpret_cast<const float4*>(&lv[l - 1].dzh_hi));  // dzh, cloud
   const df2 cl = SHAPE ? df_mul(df2{g.z, g.w}, csd) : df2{g.z, g.w};
   const df2 t = df_add(df_mul(df2{g.x, g.y}, df_add(kap.v, kap_prev.v)), cl);
@@ -148,10 +151,18 @@ __device__ __forceinline__ void emission_layer_tau_df(const LevelInfo* __restric
   if (narrow && t.hi > 1e-30f && t.hi < 1e30f) {
     tau = df_to_double(t);
     rtau = df_to_double(df_div(df_make(1.0f), t));
+    if (OUT) {
+      const df2 ksh = df_mul_f(df_add(kap.v, kap_prev.v), 0.5f);
+      *tk = make_float4(t.hi, t.lo, ksh.hi, ksh.lo);
+    }
   } else {
     const double ks = (df_to_double(kap.v) + kap.wide) + (df_to_double(kap_prev.v) + kap_prev.wide);
     tau = __ldg(&lv[l - 1].dz) * ks / 2. + (SHAPE ? __ldg(&lv[l - 1].cloud) * csh : __ldg(&lv[l - 1].cloud));
     rtau = 1.0 / tau;
+    if (OUT) {
+      const df2 td = df_from_double(fmin(tau, 1e37)), kd = df_from_double(fmin(0.5 * ks, 1e37));
+      *tk = make_float4(td.hi, td.lo, kd.hi, kd.lo);
+    }
   }
 }
 
