@@ -287,7 +287,7 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
   if (active) {
     for (int l = j; l < L; l += TPN) {
       if (DF) {
-        const Kappa kp = level_kappa_df(dm.ltab, N, sf + (size_t)l * S, S, k, et);
+        const Kappa kp = level_kappa_df<4>(dm.ltab, N, sf + (size_t)l * S, S, k, et);
         df2 x = kp.v;
         if ((__double_as_longlong(kp.wide) << 1) != 0) x = df_add(x, df_from_double(kp.wide));
         for (int r = 0; r < R; ++r) {

@@ -43,32 +43,49 @@ struct Kappa {
 // is called for every species with its term (t as a double-float, or t_wide in
 // FP64 when outside the float range; zero for a skipped species) and the level
 // table values at the lower and upper temperature nodes (log2 units).
-template <class F>
+// GRP: species handled per group; a group's table reads are issued together before its
+// arithmetic (the accumulation order is unchanged), which hides memory latency where
+// registers allow.
+template <int GRP = 1, class F>
 __device__ __forceinline__ Kappa level_kappa_df_cb(const float2* __restrict__ ltab, size_t N,
                                                    const LevelSpeciesDF* __restrict__ f, int S, int k,
                                                    const ExpTables& et, F&& term) {
   Kappa r = {{0.0f, 0.0f}, 0.0};
-  for (int s = 0; s < S; ++s) {
-    const int4 rw = __ldg(reinterpret_cast<const int4*>(f + s));
-    const float4 fb = __ldg(reinterpret_cast<const float4*>(f + s) + 1);  // wT, log2 n
-    if (fb.z == kNoSpecies) {  // zero number density: the species adds nothing
-      term(s, df2{0.0f, 0.0f}, 0.0, false, df2{0.0f, 0.0f}, df2{0.0f, 0.0f});
-      continue;
+  for (int s0 = 0; s0 < S; s0 += GRP) {
+    int4 rw[GRP];
+    float4 fb[GRP];
+    float2 t0[GRP], t1[GRP];
+#pragma unroll
+    for (int g = 0; g < GRP; ++g) {
+      if (s0 + g >= S) break;
+      rw[g] = __ldg(reinterpret_cast<const int4*>(f + s0 + g));
+      fb[g] = __ldg(reinterpret_cast<const float4*>(f + s0 + g) + 1);  // wT, log2 n
+      if (fb[g].z != kNoSpecies) {
+        t0[g] = __ldg(ltab + (size_t)rw[g].x * N + k);
+        t1[g] = __ldg(ltab + (size_t)rw[g].y * N + k);
+      }
     }
-    const float2 t0 = __ldg(ltab + (size_t)rw.x * N + k);
-    const float2 t1 = __ldg(ltab + (size_t)rw.y * N + k);
-    const df2 lo = {t0.x, t0.y}, hi = {t1.x, t1.y};
-    const df2 y = df_add(df_lerp(lo, hi, df2{fb.x, fb.y}), df2{fb.z, fb.w});
-    int n;
-    const df2 m = df_exp2(y, n, et.hi, et.lo);
-    if (n > -100 && n < 100) {
-      const df2 t = df_ldexp(m, n);
-      r.v = df_add(r.v, t);
-      term(s, t, 0.0, false, lo, hi);
-    } else {
-      const double w = df_to_double(m) * pow2d(n);
-      r.wide += w;
-      term(s, df2{0.0f, 0.0f}, w, true, lo, hi);
+#pragma unroll
+    for (int g = 0; g < GRP; ++g) {
+      const int s = s0 + g;
+      if (s >= S) break;
+      if (fb[g].z == kNoSpecies) {  // zero number density: the species adds nothing
+        term(s, df2{0.0f, 0.0f}, 0.0, false, df2{0.0f, 0.0f}, df2{0.0f, 0.0f});
+        continue;
+      }
+      const df2 lo = {t0[g].x, t0[g].y}, hi = {t1[g].x, t1[g].y};
+      const df2 y = df_add(df_lerp(lo, hi, df2{fb[g].x, fb[g].y}), df2{fb[g].z, fb[g].w});
+      int n;
+      const df2 m = df_exp2(y, n, et.hi, et.lo);
+      if (n > -100 && n < 100) {
+        const df2 t = df_ldexp(m, n);
+        r.v = df_add(r.v, t);
+        term(s, t, 0.0, false, lo, hi);
+      } else {
+        const double w = df_to_double(m) * pow2d(n);
+        r.wide += w;
+        term(s, df2{0.0f, 0.0f}, w, true, lo, hi);
+      }
     }
   }
   return r;
@@ -78,10 +95,11 @@ struct NoTerm {
   __device__ __forceinline__ void operator()(int, df2, double, bool, df2, df2) const {}
 };
 
+template <int GRP = 1>
 __device__ __forceinline__ Kappa level_kappa_df(const float2* __restrict__ ltab, size_t N,
                                                 const LevelSpeciesDF* __restrict__ f, int S, int k,
                                                 const ExpTables& et) {
-  return level_kappa_df_cb(ltab, N, f, S, k, et, NoTerm{});
+  return level_kappa_df_cb<GRP>(ltab, N, f, S, k, et, NoTerm{});
 }
 
 // The same sum in FP64 with the CUDA math library (validation path);
