@@ -677,31 +677,43 @@ __global__ void __launch_bounds__(kAdjThreads) emission_adjoint_sinks_kernel(Dev
     double gK64 = 0.0;
     df2 dk = z;
     double dkw = 0.0;
+    // species in groups of four: a group's table reads are issued before its arithmetic
 #pragma unroll
-    for (int s = 0; s < VP - 1; ++s) {
-      if (s >= S) break;
-      // species term 2^y of the level opacity (level_kappa_df_cb) and its temperature slope
-      const int4 rw = __ldg(reinterpret_cast<const int4*>(sf + s));
-      const float4 fb = __ldg(reinterpret_cast<const float4*>(sf + s) + 1);  // wT, log2 n
-      if (fb.z == kNoSpecies) continue;
-      const float2 t0 = __ldg(dm.ltab + (size_t)rw.x * N + k);
-      const float2 t1 = __ldg(dm.ltab + (size_t)rw.y * N + k);
-      const df2 lo = {t0.x, t0.y}, hi = {t1.x, t1.y};
-      const df2 y = df_add(df_lerp(lo, hi, df2{fb.x, fb.y}), df2{fb.z, fb.w});
-      int n;
-      const df2 m = df_exp2(y, n, et.hi, et.lo);
-      const float2 d = __ldg(dwl + s);
-      const bool narrow = n > -100 && n < 100;
-      const df2 slope = df_mul(df_sub(hi, lo), df2{d.x, d.y});
-      if (narrow) {
-        const df2 t = df_ldexp(m, n);
-        acc[s] = df_add(acc[s], df_mul(gK, t));
-        if (d.x != 0.0f) dk = df_add(dk, df_mul(t, slope));
-      } else {
-        const double tw = df_to_double(m) * pow2d(n);
-        if (gK64 == 0.0) gK64 = df_to_double(gK);
-        acc[s] = df_add(acc[s], df_from_double(gK64 * tw));
-        if (d.x != 0.0f) dkw += tw * df_to_double(slope);
+    for (int s0 = 0; s0 < VP - 1; s0 += 4) {
+      if (s0 >= S) break;
+      float2 t0[4], t1[4];
+#pragma unroll
+      for (int g = 0; g < 4; ++g) {
+        const int s = s0 + g;
+        if (s >= S || s >= VP - 1) break;
+        const int4 rw = __ldg(reinterpret_cast<const int4*>(sf + s));
+        t0[g] = __ldg(dm.ltab + (size_t)rw.x * N + k);
+        t1[g] = __ldg(dm.ltab + (size_t)rw.y * N + k);
+      }
+#pragma unroll
+      for (int g = 0; g < 4; ++g) {
+        const int s = s0 + g;
+        if (s >= S || s >= VP - 1) break;
+        // species term 2^y of the level opacity (level_kappa_df_cb) and its temperature slope
+        const float4 fb = __ldg(reinterpret_cast<const float4*>(sf + s) + 1);  // wT, log2 n
+        if (fb.z == kNoSpecies) continue;
+        const df2 lo = {t0[g].x, t0[g].y}, hi = {t1[g].x, t1[g].y};
+        const df2 y = df_add(df_lerp(lo, hi, df2{fb.x, fb.y}), df2{fb.z, fb.w});
+        int n;
+        const df2 m = df_exp2(y, n, et.hi, et.lo);
+        const float2 d = __ldg(dwl + s);
+        const bool narrow = n > -100 && n < 100;
+        const df2 slope = df_mul(df_sub(hi, lo), df2{d.x, d.y});
+        if (narrow) {
+          const df2 t = df_ldexp(m, n);
+          acc[s] = df_add(acc[s], df_mul(gK, t));
+          if (d.x != 0.0f) dk = df_add(dk, df_mul(t, slope));
+        } else {
+          const double tw = df_to_double(m) * pow2d(n);
+          if (gK64 == 0.0) gK64 = df_to_double(gK);
+          acc[s] = df_add(acc[s], df_from_double(gK64 * tw));
+          if (d.x != 0.0f) dkw += tw * df_to_double(slope);
+        }
       }
     }
     // opacity part of d log L / dT: gK d kappa / dT (level-table values are log2: d 2^y / dy = 2^y ln 2)

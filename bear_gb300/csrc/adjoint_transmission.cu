@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(kTrTPN * kTrVPB, VP == 32 ? 4 : 6) tr_adjoint_
     double dkw = 0.0;
     bool wide = false;
     const float2* dwl = dw + (size_t)l * S;
-    level_kappa_df_cb(dm.ltab, N, sf + (size_t)l * S, S, k, et,
+    level_kappa_df_cb<2>(dm.ltab, N, sf + (size_t)l * S, S, k, et,
                       [&](int s, df2 t, double t_w, bool is_wide, df2 lo, df2 hi) {
                         const float2 d = __ldg(dwl + s);
                         td[(size_t)s * blockDim.x] = make_float2(t.hi, t.lo);
