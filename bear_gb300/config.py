@@ -165,6 +165,9 @@ class TransmissionModelConfig(GenericConfig):
         self.cloud_model_parameters = [list(p) for p in clp]
         self.modules = list(mods)
         self.modules_parameters = [list(p) for p in modp]
+        # impact parameters per atmospheric layer (not in the reference: 1 is its tangent
+        # ray per level; A > 1 adds A - 1 rays inside every layer, extinction linear in z)
+        self.transmission_annuli = 1
 
 
 class OccultationConfig(GenericConfig):
@@ -246,6 +249,9 @@ def render_config(config: Config, model_config: GenericConfig) -> str:
         lines.append(f"variable_gravity {int(model_config.use_variable_gravity)}")
         if getattr(model_config, "modules", []):
             raise ValueError("transmission spectrum modules are not supported by this engine")
+        annuli = int(getattr(model_config, "transmission_annuli", 1))
+        if annuli != 1:
+            lines.append(f"transmission_annuli {annuli}")
     for m, p in zip(model_config.chemistry_model, model_config.chemistry_parameters):
         lines.append(" ".join(["chemistry", m] + list(p)))
     for m, p in zip(model_config.cloud_model, model_config.cloud_model_parameters):

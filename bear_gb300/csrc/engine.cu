@@ -250,6 +250,42 @@ constexpr int kTPN = 4;
 __global__ void tr_geometry_adjoint_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
                                            const EvalInfo* __restrict__ ev, float2* __restrict__ geo);
 
+// Extinction abs + scat + cloud of every level of wavenumber k into the staged column
+// chi[l][VPB] (double-floats with DF, FP64 otherwise); thread j of the wavenumber's kTPN
+// takes every kTPN-th level. rn_s: the Rayleigh / continuum coefficients as double-floats (DF).
+template <bool DF, int VPB>
+__device__ __forceinline__ void tr_extinction(const DeviceModel& dm, const LevelInfo* __restrict__ lv,
+                                              const LevelSpecies* __restrict__ sp,
+                                              const LevelSpeciesDF* __restrict__ sf,
+                                              const double* __restrict__ ray_n, int b, int k, int v, int j,
+                                              const ExpTables& et, const float2* rn_s, double csh,
+                                              double* chi_s) {
+  float2* chi_f = reinterpret_cast<float2*>(chi_s);
+  const int L = dm.L, S = dm.S, R = dm.R;
+  const size_t N = dm.N;
+  for (int l = j; l < L; l += kTPN) {
+    if (DF) {
+      const Kappa kp = level_kappa_df<4>(dm.ltab, N, sf + (size_t)l * S, S, k, et);
+      df2 x = kp.v;
+      if ((__double_as_longlong(kp.wide) << 1) != 0) x = df_add(x, df_from_double(kp.wide));
+      for (int r = 0; r < R; ++r) {
+        const float2 sr = __ldg(&dm.rayleigh_df[(size_t)r * N + k]);
+        const float2 nr = rn_s[l * R + r];
+        x = df_fma(df2{sr.x, sr.y}, df2{nr.x, nr.y}, x);
+      }
+      const float2 cl = __ldg(reinterpret_cast<const float2*>(&lv[l].cloud_hi));
+      x = dm.cloud_kind ? df_fma(df2{cl.x, cl.y}, df_from_double(csh), x) : df_add(x, df2{cl.x, cl.y});
+      chi_f[l * VPB + v] = make_float2(x.hi, x.lo);
+    } else {
+      const double a = level_absorption_fp64(dm.table64, N, sp + (size_t)l * S, S, k);
+      double sc = 0.0;
+      for (int r = 0; r < R; ++r)
+        sc += __ldg(&dm.rayleigh[(size_t)r * N + k]) * __ldg(&ray_n[((size_t)b * L + l) * R + r]);
+      chi_s[l * VPB + v] = a + sc + __ldg(&lv[l].cloud) * csh;
+    }
+  }
+}
+
 template <bool DF, int VPB, bool STORE = false>
 __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
                                                            const LevelSpecies* __restrict__ ls,
@@ -284,29 +320,7 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
   }
   __syncthreads();
   // extinction abs + scat + cloud of every level (the TPN threads take every TPN-th level)
-  if (active) {
-    for (int l = j; l < L; l += TPN) {
-      if (DF) {
-        const Kappa kp = level_kappa_df<4>(dm.ltab, N, sf + (size_t)l * S, S, k, et);
-        df2 x = kp.v;
-        if ((__double_as_longlong(kp.wide) << 1) != 0) x = df_add(x, df_from_double(kp.wide));
-        for (int r = 0; r < R; ++r) {
-          const float2 sr = __ldg(&dm.rayleigh_df[(size_t)r * N + k]);
-          const float2 nr = rn_s[l * R + r];
-          x = df_fma(df2{sr.x, sr.y}, df2{nr.x, nr.y}, x);
-        }
-        const float2 cl = __ldg(reinterpret_cast<const float2*>(&lv[l].cloud_hi));
-        x = dm.cloud_kind ? df_fma(df2{cl.x, cl.y}, df_from_double(csh), x) : df_add(x, df2{cl.x, cl.y});
-        chi_f[l * VPB + v] = make_float2(x.hi, x.lo);
-      } else {
-        const double a = level_absorption_fp64(dm.table64, N, sp + (size_t)l * S, S, k);
-        double sc = 0.0;
-        for (int r = 0; r < R; ++r)
-          sc += __ldg(&dm.rayleigh[(size_t)r * N + k]) * __ldg(&ray_n[((size_t)b * L + l) * R + r]);
-        chi_s[l * VPB + v] = a + sc + __ldg(&lv[l].cloud) * csh;
-      }
-    }
-  }
+  if (active) tr_extinction<DF, VPB>(dm, lv, sp, sf, ray_n, b, k, v, j, et, rn_s, csh, chi_s);
   __syncthreads();
   // neighbour sums chi_i + chi_{i+1}, the bracket of every trapezoid term
   if (active && j == 0) {
@@ -403,6 +417,160 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
       const double zt = __ldg(&lv[t].z);
       const double wz = (__ldg(&lv[t + 1].z) - zt) + (t >= 1 ? zt - __ldg(&lv[t - 1].z) : 0.0);
       h = fma((Rp + zt) * (1. - tr), wz, h);
+    }
+  }
+  h_part[j][v] = h;
+  __syncthreads();
+  if (active && j == 0) {
+    double hs = 0.0;
+#pragma unroll
+    for (int q = 0; q < TPN; ++q) hs += h_part[q][v];
+    hs = sqrt(hs + Rp * Rp) - Rp;
+    const double rp = hs + Rp;
+    const double Rs = ev[b].star_radius;
+    spectrum[(size_t)b * N + k] = rp * rp / Rs / Rs * 1e6;
+  }
+}
+
+// ------------------------------------------------------------------ transmission with annuli
+// Transit depth with A = dm.annuli impact parameters per layer (not in the reference, whose
+// rays touch the levels only; A = 1 is that formula and uses transmission_kernel): in layer t
+// the rays' altitudes are zb = z_t + (z_{t+1} - z_t) j / A, j = 0..A-1, plus the top level. A
+// ray's first, partial segment (from its tangent point to level t+1) takes the extinction
+// interpolated linearly in altitude, chi_t + (chi_{t+1} - chi_t) j / A; the other segments,
+// the tau > cut-off rule, exp(-tau) and the effective-height trapezoid (over the finer grid of
+// impact parameters) are those of transmission_kernel.
+//
+// Geometry per evaluation: geom[b][k][i], k < K = (L-1) A, the path length through level
+// pair (i, i+1) of ray k (i == t: the partial segment), and rays[b] = {zb[K+1], wz[K+1]}
+// (altitude, trapezoid weight (zb_{k+1} - zb_k) + (zb_k - zb_{k-1})).
+template <bool DF>
+__global__ void transmission_annuli_geometry_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
+                                                    const EvalInfo* __restrict__ ev, double* __restrict__ geom,
+                                                    double* __restrict__ rays) {
+  const int b = blockIdx.x;
+  const int L = dm.L, A = dm.annuli, K = (L - 1) * A;
+  const LevelInfo* lv = lev + (size_t)b * L;
+  const double R = ev[b].radius;
+  double* zb = rays + (size_t)b * 2 * (K + 1);
+  double* wz = zb + (K + 1);
+  for (int kr = threadIdx.x; kr <= K; kr += blockDim.x) {
+    double z = lv[L - 1].z;
+    if (kr < K) {
+      const int t = kr / A, jj = kr - t * A;
+      const double z0 = lv[t].z, z1 = lv[t + 1].z;
+      z = __dadd_rn(z0, __ddiv_rn(__dmul_rn(__dsub_rn(z1, z0), (double)jj), (double)A));
+    }
+    zb[kr] = z;
+  }
+  __syncthreads();
+  for (int kr = threadIdx.x; kr <= K; kr += blockDim.x)
+    wz[kr] = (kr < K ? zb[kr + 1] - zb[kr] : 0.0) + (kr >= 1 ? zb[kr] - zb[kr - 1] : 0.0);
+  for (int idx = threadIdx.x; idx < K * L; idx += blockDim.x) {
+    const int kr = idx / L, i = idx - kr * L, t = kr / A;
+    double v = 0.0;
+    if (i >= t && i < L - 1) {
+      const double bt = R + zb[kr];
+      const double bb = __dmul_rn(bt, bt);
+      const double a1 = R + lv[i + 1].z;
+      v = sqrt(__dsub_rn(__dmul_rn(a1, a1), bb));
+      if (i > t) {
+        const double a0 = R + lv[i].z;
+        v -= sqrt(__dsub_rn(__dmul_rn(a0, a0), bb));
+      }
+    }
+    if (DF) {
+      const df2 d = df_from_double(v);
+      reinterpret_cast<float2*>(geom)[(size_t)b * K * L + idx] = make_float2(d.hi, d.lo);
+    } else {
+      geom[(size_t)b * K * L + idx] = v;
+    }
+  }
+}
+
+// Dynamic shared memory: the extinction pair sums [L][VPB], their differences
+// chi_{i+1} - chi_i [L][VPB] (double-floats with DF, FP64 otherwise), then (DF) the
+// Rayleigh / continuum coefficients [L][R].
+template <bool DF, int VPB>
+__global__ void __launch_bounds__(kTPN * VPB) transmission_annuli_kernel(
+    DeviceModel dm, const LevelInfo* __restrict__ lev, const LevelSpecies* __restrict__ ls,
+    const LevelSpeciesDF* __restrict__ lsdf, const double* __restrict__ ray_n, const EvalInfo* __restrict__ ev,
+    const double* __restrict__ geom, const double* __restrict__ rays, double* __restrict__ spectrum) {
+  constexpr int TPN = kTPN;
+  extern __shared__ double chi_s[];
+  const int L = dm.L, S = dm.S, R = dm.R, A = dm.annuli, K = (L - 1) * A;
+  float2* chi_f = reinterpret_cast<float2*>(chi_s);
+  double* dif_s = chi_s + (size_t)L * VPB;
+  float2* dif_f = reinterpret_cast<float2*>(dif_s);
+  float2* rn_s = reinterpret_cast<float2*>(dif_s + (size_t)L * VPB);
+  __shared__ ExpTables et;
+  __shared__ double h_part[TPN][VPB];
+  const int v = threadIdx.x % VPB, j = threadIdx.x / VPB;
+  const int b = blockIdx.x;
+  const int k = blockIdx.y * VPB + v;
+  const size_t N = dm.N;
+  const bool active = k < dm.N;
+  const LevelInfo* lv = lev + (size_t)b * L;
+  const LevelSpecies* sp = ls + (size_t)b * L * S;
+  const LevelSpeciesDF* sf = lsdf + (size_t)b * L * S;
+  const double csh = (dm.cloud_kind && active) ? cloud_shape(dm, ev[b], k) : 1.0;
+  if (DF) {
+    load_exp_tables(et);
+    for (int idx = threadIdx.x; idx < L * R; idx += blockDim.x) {
+      const df2 d = df_from_double(__ldg(&ray_n[(size_t)b * L * R + idx]));
+      rn_s[idx] = make_float2(d.hi, d.lo);
+    }
+  }
+  __syncthreads();
+  if (active) tr_extinction<DF, VPB>(dm, lv, sp, sf, ray_n, b, k, v, j, et, rn_s, csh, chi_s);
+  __syncthreads();
+  // pair sums chi_i + chi_{i+1} (in place) and differences chi_{i+1} - chi_i
+  if (active && j == 0) {
+    for (int i = 0; i < L - 1; ++i) {
+      if (DF) {
+        const float2 c0 = chi_f[i * VPB + v], c1 = chi_f[(i + 1) * VPB + v];
+        const df2 x0 = {c0.x, c0.y}, x1 = {c1.x, c1.y};
+        const df2 s2 = df_add(x0, x1), d2 = df_sub(x1, x0);
+        chi_f[i * VPB + v] = make_float2(s2.hi, s2.lo);
+        dif_f[i * VPB + v] = make_float2(d2.hi, d2.lo);
+      } else {
+        const double c0 = chi_s[i * VPB + v], c1 = chi_s[(i + 1) * VPB + v];
+        chi_s[i * VPB + v] = c0 + c1;
+        dif_s[i * VPB + v] = c1 - c0;
+      }
+    }
+  }
+  __syncthreads();
+  const double Rp = ev[b].radius;
+  const double* zb = rays + (size_t)b * 2 * (K + 1);
+  const double* wz = zb + (K + 1);
+  double h = 0.0;
+  if (active) {
+    for (int kr = K - 1 - j; kr >= 0; kr -= TPN) {
+      const int t = kr / A, jj = kr - t * A;
+      double tau;
+      if (DF) {
+        const float2* Gk = reinterpret_cast<const float2*>(geom) + ((size_t)b * K + kr) * L;
+        const float ch = dm.tau_cut_hi, cl = dm.tau_cut_lo;
+        auto over = [ch, cl](df2 x) { return x.hi > ch || (x.hi == ch && x.lo > cl); };  // tau > cut-off
+        const float2 g0 = __ldg(&Gk[t]), c0 = chi_f[t * VPB + v], d0 = dif_f[t * VPB + v];
+        const df2 seg = df_add(df2{c0.x, c0.y}, df_mul(df_from_double((double)jj / A), df2{d0.x, d0.y}));
+        df2 ts = df_mul(df2{g0.x, g0.y}, seg);
+        for (int i = t + 1; i < L - 1 && !over(ts); ++i) {
+          const float2 g = __ldg(&Gk[i]), c = chi_f[i * VPB + v];
+          ts = df_fma(df2{g.x, g.y}, df2{c.x, c.y}, ts);
+        }
+        tau = df_to_double(ts);
+      } else {
+        const double* Gk = geom + ((size_t)b * K + kr) * L;
+        tau = __ldg(&Gk[t]) * (chi_s[t * VPB + v] + (double)jj / A * dif_s[t * VPB + v]);
+        for (int i = t + 1; i < L - 1 && !(__double_as_longlong(tau) > dm.tau_cut_bits); ++i)
+          tau = fma(__ldg(&Gk[i]), chi_s[i * VPB + v], tau);
+      }
+      double tr;
+      if (DF) tr = __double_as_longlong(tau) > kBits700 ? 0.0 : exp_tang(-tau, et.d);
+      else tr = exp(-tau);
+      h = fma((Rp + __ldg(&zb[kr])) * (1. - tr), __ldg(&wz[kr]), h);
     }
   }
   h_part[j][v] = h;
@@ -736,6 +904,7 @@ void upload_model(Model& m) {
   for (int r : m.rayleigh_species) ray.insert(ray.end(), m.opac[r].rayleigh.begin(), m.opac[r].rayleigh.end());
   ray.insert(ray.end(), m.hm_rows.begin(), m.hm_rows.end());  // H- continuum rows follow the Rayleigh rows
   dm.R_ray = m.acfg.R_ray;
+  dm.annuli = m.transmission ? m.annuli : 1;
   dm.cloud_kind = m.acfg.cloud_kind;
   dm.rayleigh = dev_upload(m, ray);
   {
@@ -818,6 +987,8 @@ void upload_model(Model& m) {
     BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<true, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<false, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<true, 32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_annuli_kernel<true, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_annuli_kernel<false, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
   }
 }
 
@@ -832,6 +1003,7 @@ static void free_workspace(Workspace& w) {
   cudaFree(w.obs);
   cudaFree(w.loglike);
   cudaFree(w.geom);
+  cudaFree(w.rays);
   w = Workspace{};
 }
 
@@ -853,7 +1025,11 @@ void ensure_workspace(Model& m, int batch) {
   BGB_CUDA(cudaMalloc(&w.spectrum, B * N * sizeof(double)));
   BGB_CUDA(cudaMalloc(&w.obs, B * M * sizeof(double)));
   BGB_CUDA(cudaMalloc(&w.loglike, B * sizeof(double)));
-  if (m.transmission) BGB_CUDA(cudaMalloc(&w.geom, B * L * L * sizeof(double)));
+  if (m.transmission) {
+    const size_t K = transmission_rays(m);
+    BGB_CUDA(cudaMalloc(&w.geom, B * std::max(K, L) * L * sizeof(double)));
+    if (m.annuli > 1) BGB_CUDA(cudaMalloc(&w.rays, B * 2 * (K + 1) * sizeof(double)));
+  }
   w.capacity = batch;
   ++m.ws_generation;
 }
@@ -891,6 +1067,24 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
                                                              w.spectrum, nullptr);
     else
       emission_kernel<false><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.spectrum, nullptr);
+  } else if (m.annuli > 1) {
+    // A impact parameters per layer: 32 wavenumbers per block, extinction sums and differences staged
+    if (taps) throw Error(BEAR_ERR_UNSUPPORTED, "the transmission gradient needs one impact parameter per level");
+    const bool df = m.precision != 1;
+    const size_t sm = 2 * (size_t)L * 32 * sizeof(double) + (df ? (size_t)L * dm.R * sizeof(float2) : 0);
+    if (sm > kTransmissionDynSmem) throw Error(BEAR_ERR_UNSUPPORTED, "too many levels for the transmission kernel");
+    const dim3 grid(batch, (dm.N + 31) / 32);
+    if (df) {
+      transmission_annuli_geometry_kernel<true><<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom, w.rays);
+      BGB_CUDA(cudaGetLastError());
+      transmission_annuli_kernel<true, 32><<<grid, kTPN * 32, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev,
+                                                                       w.geom, w.rays, w.spectrum);
+    } else {
+      transmission_annuli_geometry_kernel<false><<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom, w.rays);
+      BGB_CUDA(cudaGetLastError());
+      transmission_annuli_kernel<false, 32><<<grid, kTPN * 32, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev,
+                                                                        w.geom, w.rays, w.spectrum);
+    }
   } else {
     if (m.precision == 1) transmission_geometry_kernel<false><<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom);
     else transmission_geometry_kernel<true><<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom);

@@ -2,6 +2,7 @@
 // kernels). The public boundary is include/bear_gb300.h.
 #pragma once
 
+#include <algorithm>
 #include <array>
 #include <cstddef>
 #include <cstdint>
@@ -173,6 +174,7 @@ struct DeviceModel {
   const float2* rayleigh_df;  // R x N as double-floats
   int R_ray;                  // Rayleigh rows (the rest, R - R_ray, are H- continuum rows)
   int cloud_kind;             // 0 grey (or no cloud), 1 power law, 2 KH non-grey
+  int annuli;                 // transmission: impact parameters per layer (1: the reference's tangent rays)
   // observation operator: M rows, internal (descending-wavelength) order
   const int* row_k0;
   const int* row_len;
@@ -215,7 +217,8 @@ struct Workspace {
   double* spectrum = nullptr;  // B x N native units
   double* obs = nullptr;       // B x M internal order
   double* loglike = nullptr;   // B
-  double* geom = nullptr;      // transmission path lengths B x L x L
+  double* geom = nullptr;      // transmission path lengths B x L x L (B x K x L with K = (L-1) A annuli)
+  double* rays = nullptr;      // transmission with annuli: B x 2 (K + 1): ray altitude, trapezoid weight
 };
 
 // Extra outputs of the forward pass that the adjoint reads back.
@@ -314,6 +317,7 @@ struct Model {
   int cloud_kind = 0;             // 0 grey, 1 power_law, 2 KHnongrey
   double cloud_ref_wl = 0.0;      // reference wavelength (micron) of the non-grey clouds
   bool fit_mmw = false, fit_sh = false, var_g = false;
+  int annuli = 1;                 // transmission impact parameters per layer (not in the reference)
   bool occultation = false;
   bool hm = false;                // H- continuum configured
   int star_model = 0;             // 1 blackbody, 2 file, 3 grid
@@ -390,6 +394,8 @@ void compose_operator_rows(const Model& m, const ObservationSetup& o, bool is_fl
                            std::vector<int>& row_k0, std::vector<int>& row_len, std::vector<long long>& row_off);
 
 // engine.cu
+// transmission rays per evaluation: L - 1 tangent rays, (L - 1) A with annuli
+inline int transmission_rays(const Model& m) { return (m.L - 1) * std::max(m.annuli, 1); }
 void upload_model(Model& m);
 void ensure_workspace(Model& m, int batch);
 void release_model(Model& m);

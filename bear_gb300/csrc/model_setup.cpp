@@ -176,6 +176,10 @@ void parse_config(Model& m, const std::string& text) {
     } else if (k == "variable_gravity") {
       need(2);
       m.var_g = std::stoi(t[1]) != 0;
+    } else if (k == "transmission_annuli") {
+      need(2);
+      m.annuli = std::stoi(t[1]);
+      if (m.annuli < 1 || m.annuli > 64) throw invalid("transmission_annuli must be in [1, 64]");
     } else {
       throw invalid("unknown config key " + k);
     }

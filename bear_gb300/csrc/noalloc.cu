@@ -65,7 +65,9 @@ size_t layout(const Model& m, unsigned char* base, Workspace* w) {
   unsigned char* ev = take(sizeof(EvalInfo));
   unsigned char* spec = take(N * sizeof(double));
   unsigned char* obs = take(M * sizeof(double));
-  unsigned char* geom = m.transmission ? take(L * L * sizeof(double)) : nullptr;
+  const size_t K = m.transmission ? (size_t)transmission_rays(m) : 0;
+  unsigned char* geom = m.transmission ? take(std::max(K, L) * L * sizeof(double)) : nullptr;
+  unsigned char* rays = (m.transmission && m.annuli > 1) ? take(2 * (K + 1) * sizeof(double)) : nullptr;
   if (base) {
     *w = Workspace{};
     w->capacity = 1;
@@ -77,6 +79,7 @@ size_t layout(const Model& m, unsigned char* base, Workspace* w) {
     w->spectrum = reinterpret_cast<double*>(spec);
     w->obs = reinterpret_cast<double*>(obs);
     w->geom = reinterpret_cast<double*>(geom);
+    w->rays = reinterpret_cast<double*>(rays);
   }
   return off;
 }

@@ -7,16 +7,18 @@ species + 2 CIA tables on 10 log-p x 20 T, 2000-12000 cm^-1 at 1 cm^-1
 top-hat / Gaussian bandpass filters). Synthetic seeded tables in the
 reference's on-disk format.
 
-One step = one batch of B likelihood evaluations. For emission workloads the
-adjoint gradient of the same batch is timed as well (``gradient``: evals/s and
-the ratio of its time to the forward batch). ``value`` = evaluations per
+One step = one batch of B likelihood evaluations. The adjoint gradient of the
+same batch is timed as well (``gradient``: evals/s and the ratio of its time to
+the forward batch), except for transmission_annuli (10 impact parameters per
+layer, which the adjoint does not cover). ``value`` = evaluations per
 second over the timed steps with parameters resident in HBM; ``e2e`` = the same
 through the host API with the parameter upload and the log-likelihood download
 inside the timed region. L2 is flushed between timed steps (a 512 MiB write)
 outside the per-step event pair.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-                    [--workload emission_batched|emission_adjoint|emission_plain|transmission_plain]
+                    [--workload emission_batched|emission_adjoint|emission_plain|transmission_plain|
+                                transmission_annuli|joint_large]
 """
 
 from __future__ import annotations
@@ -45,8 +47,11 @@ WORKLOADS = {
     "emission_adjoint": ("emission_adjoint", "emission"),
     "emission_plain": ("emission_plain", "emission"),
     "transmission_plain": ("transmission_plain", "transmission"),
+    "transmission_annuli": ("transmission_plain", "transmission"),
     "joint_large": ("joint_large", "joint"),
 }
+# impact parameters per layer of the transit integral (1: the reference's tangent rays)
+ANNULI = {"transmission_annuli": 10}
 
 
 def parse():
@@ -80,6 +85,8 @@ def build_case(workload: str):
     spec = syn.CONFIGS[name]
     root = syn.write_tables(spec, synth_dir())
     text = render_config(syn.global_config(spec, root, kind), syn.model_config(spec, kind))
+    if workload in ANNULI:
+        text += f"transmission_annuli {ANNULI[workload]}\n"
     obs = syn.observations(spec, kind)
     return spec, kind, text, obs
 
@@ -611,7 +618,7 @@ def main():
 
     # adjoint gradient (emission models): log L and d log L / d params for the batch
     grad = None
-    if True:  # emission and transmission models both have an adjoint
+    if args.workload not in ANNULI:  # the adjoint covers one tangent ray per level
         G = torch.empty(B, eng.P, dtype=torch.float64, device=device)
 
         def grad_step():
@@ -680,7 +687,8 @@ def main():
             "config": {"workload": args.workload, "batch_per_gpu": B, "global_batch": B * world,
                        "levels": L, "spectral_points": N, "bins": M, "table_species": S,
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                       "l2": "flushed between timed steps (512 MiB write)"},
+                       "l2": "flushed between timed steps (512 MiB write)",
+                       "annuli_per_layer": ANNULI.get(args.workload, 1)},
             "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": int(P.numel() * 8),
                     "d2h_bytes_per_step": int(B * 8)},
             "plain_path": {"evals_per_s": 1.0 / plain_s, "ms_per_eval": plain_s * 1e3,
@@ -691,7 +699,8 @@ def main():
             "gpu_launches": (3 if kind == "emission" else 4) * args.steps,
             "batched_path": {"api": "bear_batch_graph_launch (CUDA graph of the batched kernels)",
                              "autotuned_rt_threads": ev.rt_threads},
-            "roofline": {"bound": "hbm", "kernel": "emission_kernel" if kind == "emission" else "transmission_kernel",
+            "roofline": {"bound": "hbm", "kernel": "emission_kernel" if kind == "emission" else
+                         ("transmission_annuli_kernel" if args.workload in ANNULI else "transmission_kernel"),
                          "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": None,
                          "peak_source": peak_kind, "kernel_ms": kern_ms, "algorithmic_bytes": alg_bytes,
@@ -702,6 +711,8 @@ def main():
         }
         if grad is not None:
             line["gradient"] = grad
+        elif args.workload in ANNULI:
+            line["gradient"] = {"unavailable": "the adjoint covers one tangent ray per level"}
     if rank == 0:
         line["clocks"] = clocks.summary()
         if not args.no_cpu_baseline:

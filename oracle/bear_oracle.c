@@ -111,6 +111,7 @@ typedef struct orc_model {
   /* global */
   int transmission;
   int occultation;           /* secondary eclipse (OccultationModel) */
+  int annuli;                /* impact parameters per layer of the transit integral (1: the reference) */
   int star_model;            /* 1 blackbody (T_eff parameter), 2 file, 3 grid (T_eff, log g, [M/H]) */
   char star_file[1024];      /* file path (2) or grid folder (3) */
   double* star_flux;         /* N, file stellar spectrum on the model grid */
@@ -238,6 +239,7 @@ orc_model* orc_create(const char* text) {
     } else if (!strcmp(k, "fit_mean_molecular_weight")) m->fit_mmw = atoi(tok[1]);
     else if (!strcmp(k, "fit_scale_height")) m->fit_sh = atoi(tok[1]);
     else if (!strcmp(k, "variable_gravity")) m->var_g = atoi(tok[1]);
+    else if (!strcmp(k, "transmission_annuli")) m->annuli = atoi(tok[1]);
     continue;
   bad:
     set_err("malformed config line for %s", k); goto fail;
@@ -931,6 +933,7 @@ static void star_grid_flux(const orc_model* m, const double* sp, double* out) {
 
 int orc_finalize(orc_model* m) {
   if (m->nobs == 0) { set_err("no observations"); return -1; }
+  if (m->annuli < 0 || m->annuli > 64) { set_err("transmission_annuli must be in [1, 64]"); return -1; }
   if (load_wavenumbers(m)) return -1;
   if (sample_grid(m)) return -1;
   setup_observation_operators(m);
@@ -1222,7 +1225,48 @@ static double sc_point(const orc_model* m, const double* kappa, const double* cl
 /* TransmissionModel::tangentPathsTransmission / tangentOpticalDepth /
  * integrateEffectiveTangentHeight / distanceToTangentCenter
  * src/forward_model/transmission/transmission_spectrum.cpp:32-154 */
+/* The transit depth with A impact parameters per layer (A = 1 is the reference's
+ * formula, transit_point below): in layer t, b_k = R + zb_k with
+ * zb_k = z_t + (z_{t+1} - z_t) j / A, j = 0..A-1, plus the top level. A ray's first,
+ * partial segment from its tangent point to level t+1 uses the extinction interpolated
+ * linearly in altitude at zb_k, chi_t + (chi_{t+1} - chi_t) j / A; the other segments
+ * and the tau > cut-off rule are the reference's; the effective height is the same
+ * trapezoid over the finer grid of impact parameters. Not in the reference. */
+static double transit_point_annuli(const orc_model* m, const double* chi, const atm_t* a, double R, double Rs) {
+  const int L = m->L, A = m->annuli, K = (L - 1) * A;
+  double* zb = (double*)malloc((K + 1) * sizeof(double));
+  double* trans = (double*)malloc((K + 1) * sizeof(double));
+  for (int k = 0; k < K; ++k) {
+    const int t = k / A, j = k % A;
+    zb[k] = a->z[t] + (a->z[t + 1] - a->z[t]) * j / A;
+  }
+  zb[K] = a->z[L - 1];
+  trans[K] = 1;
+  for (int k = K - 1; k >= 0; --k) {
+    const int t = k / A, j = k % A;
+    const double b = R + zb[k];
+    const double chib = chi[t] + (chi[t + 1] - chi[t]) * j / A;
+    const double a1 = R + a->z[t + 1];
+    double tau = sqrt(a1 * a1 - b * b) * (chib + chi[t + 1]);
+    if (!(tau > m->tau_cut))
+      for (int i = t + 1; i < L - 1; ++i) {
+        const double u1 = R + a->z[i + 1], u0 = R + a->z[i];
+        tau += (sqrt(u1 * u1 - b * b) - sqrt(u0 * u0 - b * b)) * (chi[i] + chi[i + 1]);
+        if (tau > m->tau_cut) break;
+      }
+    trans[k] = exp(-tau);
+  }
+  double h = 0;
+  for (int k = 0; k < K; ++k)
+    h += 2. * ((R + zb[k]) * (1. - trans[k]) + (R + zb[k + 1]) * (1. - trans[k + 1])) * (zb[k + 1] - zb[k]) * 0.5;
+  free(zb); free(trans);
+  h = sqrt(h + R * R) - R;
+  const double rp = h + R;
+  return rp * rp / Rs / Rs * 1e6;
+}
+
 static double transit_point(const orc_model* m, const double* chi, const atm_t* a, double R, double Rs) {
+  if (m->annuli > 1) return transit_point_annuli(m, chi, a, R, Rs);
   const int L = m->L;
   double trans[512];
   trans[L - 1] = 1;
