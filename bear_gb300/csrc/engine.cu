@@ -94,7 +94,6 @@ __global__ void __launch_bounds__(256, 6) emission_kernel(DeviceModel dm, const 
   const int L = dm.L, S = dm.S;
   const size_t N = dm.N;
   const LevelInfo* lv = lev + (size_t)b * L;
-  const LevelSpecies* sp = ls + (size_t)b * L * S;
   const LevelSpeciesDF* sf = lsdf + (size_t)b * L * S;
   double* Is = STORE ? istore + (size_t)b * L * 2 * N + k : nullptr;
   const float2 c1f = __ldg(dm.planck_c1_df + k), c2f = __ldg(dm.planck_c2l_df + k);
@@ -251,9 +250,9 @@ __global__ void tr_geometry_adjoint_kernel(DeviceModel dm, const LevelInfo* __re
                                            const EvalInfo* __restrict__ ev, float2* __restrict__ geo);
 
 // Extinction abs + scat + cloud of every level of wavenumber k into the staged column
-// chi[l][VPB] (double-floats with DF, FP64 otherwise); thread j of the wavenumber's kTPN
-// takes every kTPN-th level. rn_s: the Rayleigh / continuum coefficients as double-floats (DF).
-template <bool DF, int VPB>
+// chi[l][VPB] (double-floats with DF, FP64 otherwise); thread j of the wavenumber's TPN
+// takes every TPN-th level. rn_s: the Rayleigh / continuum coefficients as double-floats (DF).
+template <bool DF, int VPB, int TPN = kTPN>
 __device__ __forceinline__ void tr_extinction(const DeviceModel& dm, const LevelInfo* __restrict__ lv,
                                               const LevelSpecies* __restrict__ sp,
                                               const LevelSpeciesDF* __restrict__ sf,
@@ -263,7 +262,7 @@ __device__ __forceinline__ void tr_extinction(const DeviceModel& dm, const Level
   float2* chi_f = reinterpret_cast<float2*>(chi_s);
   const int L = dm.L, S = dm.S, R = dm.R;
   const size_t N = dm.N;
-  for (int l = j; l < L; l += kTPN) {
+  for (int l = j; l < L; l += TPN) {
     if (DF) {
       const Kappa kp = level_kappa_df<4>(dm.ltab, N, sf + (size_t)l * S, S, k, et);
       df2 x = kp.v;
@@ -438,12 +437,16 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
 // the rays' altitudes are zb = z_t + (z_{t+1} - z_t) j / A, j = 0..A-1, plus the top level. A
 // ray's first, partial segment (from its tangent point to level t+1) takes the extinction
 // interpolated linearly in altitude, chi_t + (chi_{t+1} - chi_t) j / A; the other segments,
-// the tau > cut-off rule, exp(-tau) and the effective-height trapezoid (over the finer grid of
-// impact parameters) are those of transmission_kernel.
+// the tau > cut-off rule and the effective-height trapezoid (over the finer grid of impact
+// parameters) are those of transmission_kernel. The double-float path forms exp(-tau) and
+// 1 - T in double-float (relative error ~1e-14) and adds rw_k (1 - T_k) into h in FP64, so
+// a ray costs one FP64 FMA and one conversion add on the FP64 pipe.
 //
-// Geometry per evaluation: geom[b][k][i], k < K = (L-1) A, the path length through level
-// pair (i, i+1) of ray k (i == t: the partial segment), and rays[b] = {zb[K+1], wz[K+1]}
-// (altitude, trapezoid weight (zb_{k+1} - zb_k) + (zb_k - zb_{k-1})).
+// Geometry per evaluation: geom[b][t][i][j], the path length through level pair (i, i+1)
+// of ray k = t A + j of layer t (i == t: the partial segment; the A rays of a layer are
+// contiguous for each i), and rays[b] = {zb[K+1], rw[K+1]}, K = (L-1) A: the altitudes
+// and rw_k = (R + zb_k) ((zb_{k+1} - zb_k) + (zb_k - zb_{k-1})), so that the effective
+// height is h = sum_k rw_k (1 - T_k).
 template <bool DF>
 __global__ void transmission_annuli_geometry_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
                                                     const EvalInfo* __restrict__ ev, double* __restrict__ geom,
@@ -453,7 +456,7 @@ __global__ void transmission_annuli_geometry_kernel(DeviceModel dm, const LevelI
   const LevelInfo* lv = lev + (size_t)b * L;
   const double R = ev[b].radius;
   double* zb = rays + (size_t)b * 2 * (K + 1);
-  double* wz = zb + (K + 1);
+  double* rw = zb + (K + 1);
   for (int kr = threadIdx.x; kr <= K; kr += blockDim.x) {
     double z = lv[L - 1].z;
     if (kr < K) {
@@ -465,9 +468,9 @@ __global__ void transmission_annuli_geometry_kernel(DeviceModel dm, const LevelI
   }
   __syncthreads();
   for (int kr = threadIdx.x; kr <= K; kr += blockDim.x)
-    wz[kr] = (kr < K ? zb[kr + 1] - zb[kr] : 0.0) + (kr >= 1 ? zb[kr] - zb[kr - 1] : 0.0);
+    rw[kr] = (R + zb[kr]) * ((kr < K ? zb[kr + 1] - zb[kr] : 0.0) + (kr >= 1 ? zb[kr] - zb[kr - 1] : 0.0));
   for (int idx = threadIdx.x; idx < K * L; idx += blockDim.x) {
-    const int kr = idx / L, i = idx - kr * L, t = kr / A;
+    const int t = idx / (L * A), rem = idx - t * (L * A), i = rem / A, kr = t * A + (rem - i * A);
     double v = 0.0;
     if (i >= t && i < L - 1) {
       const double bt = R + zb[kr];
@@ -491,12 +494,18 @@ __global__ void transmission_annuli_geometry_kernel(DeviceModel dm, const LevelI
 // Dynamic shared memory: the extinction pair sums [L][VPB], their differences
 // chi_{i+1} - chi_i [L][VPB] (double-floats with DF, FP64 otherwise), then (DF) the
 // Rayleigh / continuum coefficients [L][R].
-template <bool DF, int VPB>
-__global__ void __launch_bounds__(kTPN * VPB) transmission_annuli_kernel(
+constexpr int kMaxAnnuli = 64;  // transmission_annuli upper bound
+
+// dynamic shared memory of transmission_annuli_kernel (32 wavenumbers per block)
+inline size_t annuli_dyn_smem(int L, int R, bool df) {
+  return 2 * (size_t)L * 32 * sizeof(double) + (df ? (size_t)L * R * sizeof(float2) : 0);
+}
+
+template <bool DF, int VPB, int TPN, int RG>
+__global__ void __launch_bounds__(TPN * VPB, 4) transmission_annuli_kernel(
     DeviceModel dm, const LevelInfo* __restrict__ lev, const LevelSpecies* __restrict__ ls,
     const LevelSpeciesDF* __restrict__ lsdf, const double* __restrict__ ray_n, const EvalInfo* __restrict__ ev,
     const double* __restrict__ geom, const double* __restrict__ rays, double* __restrict__ spectrum) {
-  constexpr int TPN = kTPN;
   extern __shared__ double chi_s[];
   const int L = dm.L, S = dm.S, R = dm.R, A = dm.annuli, K = (L - 1) * A;
   float2* chi_f = reinterpret_cast<float2*>(chi_s);
@@ -505,6 +514,7 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_annuli_kernel(
   float2* rn_s = reinterpret_cast<float2*>(dif_s + (size_t)L * VPB);
   __shared__ ExpTables et;
   __shared__ double h_part[TPN][VPB];
+  __shared__ float2 wj_s[kMaxAnnuli];  // j / A as double-floats
   const int v = threadIdx.x % VPB, j = threadIdx.x / VPB;
   const int b = blockIdx.x;
   const int k = blockIdx.y * VPB + v;
@@ -516,13 +526,17 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_annuli_kernel(
   const double csh = (dm.cloud_kind && active) ? cloud_shape(dm, ev[b], k) : 1.0;
   if (DF) {
     load_exp_tables(et);
+    for (int q = threadIdx.x; q < A; q += blockDim.x) {
+      const df2 d = df_from_double((double)q / A);
+      wj_s[q] = make_float2(d.hi, d.lo);
+    }
     for (int idx = threadIdx.x; idx < L * R; idx += blockDim.x) {
       const df2 d = df_from_double(__ldg(&ray_n[(size_t)b * L * R + idx]));
       rn_s[idx] = make_float2(d.hi, d.lo);
     }
   }
   __syncthreads();
-  if (active) tr_extinction<DF, VPB>(dm, lv, sp, sf, ray_n, b, k, v, j, et, rn_s, csh, chi_s);
+  if (active) tr_extinction<DF, VPB, TPN>(dm, lv, sp, sf, ray_n, b, k, v, j, et, rn_s, csh, chi_s);
   __syncthreads();
   // pair sums chi_i + chi_{i+1} (in place) and differences chi_{i+1} - chi_i
   if (active && j == 0) {
@@ -542,35 +556,70 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_annuli_kernel(
   }
   __syncthreads();
   const double Rp = ev[b].radius;
-  const double* zb = rays + (size_t)b * 2 * (K + 1);
-  const double* wz = zb + (K + 1);
+  const double* rw = rays + (size_t)b * 2 * (K + 1) + (K + 1);
   double h = 0.0;
   if (active) {
-    for (int kr = K - 1 - j; kr >= 0; kr -= TPN) {
-      const int t = kr / A, jj = kr - t * A;
-      double tau;
-      if (DF) {
-        const float2* Gk = reinterpret_cast<const float2*>(geom) + ((size_t)b * K + kr) * L;
-        const float ch = dm.tau_cut_hi, cl = dm.tau_cut_lo;
-        auto over = [ch, cl](df2 x) { return x.hi > ch || (x.hi == ch && x.lo > cl); };  // tau > cut-off
-        const float2 g0 = __ldg(&Gk[t]), c0 = chi_f[t * VPB + v], d0 = dif_f[t * VPB + v];
-        const df2 seg = df_add(df2{c0.x, c0.y}, df_mul(df_from_double((double)jj / A), df2{d0.x, d0.y}));
-        df2 ts = df_mul(df2{g0.x, g0.y}, seg);
-        for (int i = t + 1; i < L - 1 && !over(ts); ++i) {
-          const float2 g = __ldg(&Gk[i]), c = chi_f[i * VPB + v];
-          ts = df_fma(df2{g.x, g.y}, df2{c.x, c.y}, ts);
+    // each thread takes every TPN-th layer and walks its A rays in groups of at most RG:
+    // per level pair, the group's path lengths (contiguous, the same for the warp's
+    // wavenumbers) are loaded together; every ray keeps its own sum, in level order, and
+    // stops at its own cut-off
+    const int ng = (A + RG - 1) / RG, gs = (A + ng - 1) / ng;
+    for (int t = L - 2 - j; t >= 0; t -= TPN) {
+      for (int a0 = 0; a0 < A; a0 += gs) {
+        const int na = min(gs, A - a0);
+        if (DF) {
+          const float2* Gt = reinterpret_cast<const float2*>(geom) + ((size_t)b * (L - 1) + t) * L * A + a0;
+          const float ch = dm.tau_cut_hi, cl = dm.tau_cut_lo;
+          auto over = [ch, cl](df2 x) { return x.hi > ch || (x.hi == ch && x.lo > cl); };  // tau > cut-off
+          const float2 c0 = chi_f[t * VPB + v], d0 = dif_f[t * VPB + v];
+          df2 ts[RG];
+          unsigned live = 0;
+#pragma unroll
+          for (int u = 0; u < RG; ++u) {
+            ts[u] = df2{0.0f, 0.0f};
+            if (u < na) {
+              const float2 g = __ldg(&Gt[(size_t)t * A + u]), w = wj_s[a0 + u];
+              const df2 seg = df_add(df2{c0.x, c0.y}, df_mul(df2{w.x, w.y}, df2{d0.x, d0.y}));
+              ts[u] = df_mul(df2{g.x, g.y}, seg);
+              if (!over(ts[u])) live |= 1u << u;
+            }
+          }
+          for (int i = t + 1; i < L - 1 && live; ++i) {
+            const float2 c = chi_f[i * VPB + v];
+            float2 g[RG];
+#pragma unroll
+            for (int u = 0; u < RG; ++u)
+              if (u < na) g[u] = __ldg(&Gt[(size_t)i * A + u]);
+            // branch-free over the group (a finished ray's sum is kept, not advanced), so
+            // that the group's independent sums overlap
+#pragma unroll
+            for (int u = 0; u < RG; ++u)
+              if (u < na) {
+                const df2 n = df_fma(df2{g[u].x, g[u].y}, df2{c.x, c.y}, ts[u]);
+                const bool l = (live >> u) & 1u;
+                ts[u].hi = l ? n.hi : ts[u].hi;
+                ts[u].lo = l ? n.lo : ts[u].lo;
+                live &= ~((unsigned)(l && over(n)) << u);
+              }
+          }
+          // T = exp(-tau) and 1 - T in double-float; one FP64 FMA per ray into h
+#pragma unroll
+          for (int u = 0; u < RG; ++u)
+            if (u < na) {
+              const df2 T = df_exp_neg(ts[u], et.hi, et.lo);
+              h = fma(__ldg(&rw[t * A + a0 + u]), df_to_double(df_sub(df_make(1.0f), T)), h);
+            }
+        } else {
+          const double* Gt = geom + ((size_t)b * (L - 1) + t) * L * A;
+          for (int u = 0; u < na; ++u) {
+            const int jj = a0 + u;
+            double tau = __ldg(&Gt[(size_t)t * A + jj]) * (chi_s[t * VPB + v] + (double)jj / A * dif_s[t * VPB + v]);
+            for (int i = t + 1; i < L - 1 && !(__double_as_longlong(tau) > dm.tau_cut_bits); ++i)
+              tau = fma(__ldg(&Gt[(size_t)i * A + jj]), chi_s[i * VPB + v], tau);
+            h = fma(__ldg(&rw[t * A + jj]), 1. - exp(-tau), h);
+          }
         }
-        tau = df_to_double(ts);
-      } else {
-        const double* Gk = geom + ((size_t)b * K + kr) * L;
-        tau = __ldg(&Gk[t]) * (chi_s[t * VPB + v] + (double)jj / A * dif_s[t * VPB + v]);
-        for (int i = t + 1; i < L - 1 && !(__double_as_longlong(tau) > dm.tau_cut_bits); ++i)
-          tau = fma(__ldg(&Gk[i]), chi_s[i * VPB + v], tau);
       }
-      double tr;
-      if (DF) tr = __double_as_longlong(tau) > kBits700 ? 0.0 : exp_tang(-tau, et.d);
-      else tr = exp(-tau);
-      h = fma((Rp + __ldg(&zb[kr])) * (1. - tr), __ldg(&wz[kr]), h);
     }
   }
   h_part[j][v] = h;
@@ -987,8 +1036,10 @@ void upload_model(Model& m) {
     BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<true, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<false, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<true, 32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-    BGB_CUDA(cudaFuncSetAttribute(transmission_annuli_kernel<true, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-    BGB_CUDA(cudaFuncSetAttribute(transmission_annuli_kernel<false, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_annuli_kernel<true, 32, 4, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_annuli_kernel<true, 32, 8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_annuli_kernel<true, 32, 8, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_annuli_kernel<false, 32, 4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
   }
 }
 
@@ -1068,22 +1119,27 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
     else
       emission_kernel<false><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.spectrum, nullptr);
   } else if (m.annuli > 1) {
-    // A impact parameters per layer: 32 wavenumbers per block, extinction sums and differences staged
+    // A impact parameters per layer: 32 wavenumbers per block, extinction sums and
+    // differences staged; the launch shape selects threads per wavenumber x rays summed
+    // together: 16 -> 4 x 4, 32 (default) -> 8 x 4, 64 -> 8 x 8 (FP64 path: 4 threads)
     if (taps) throw Error(BEAR_ERR_UNSUPPORTED, "the transmission gradient needs one impact parameter per level");
     const bool df = m.precision != 1;
-    const size_t sm = 2 * (size_t)L * 32 * sizeof(double) + (df ? (size_t)L * dm.R * sizeof(float2) : 0);
+    const size_t sm = annuli_dyn_smem(L, dm.R, df);
     if (sm > kTransmissionDynSmem) throw Error(BEAR_ERR_UNSUPPORTED, "too many levels for the transmission kernel");
     const dim3 grid(batch, (dm.N + 31) / 32);
+    auto go = [&](auto kernel, int tpn) {
+      kernel<<<grid, tpn * 32, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.rays, w.spectrum);
+    };
     if (df) {
       transmission_annuli_geometry_kernel<true><<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom, w.rays);
       BGB_CUDA(cudaGetLastError());
-      transmission_annuli_kernel<true, 32><<<grid, kTPN * 32, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev,
-                                                                       w.geom, w.rays, w.spectrum);
+      if (rt == 16) go(transmission_annuli_kernel<true, 32, 4, 4>, 4);
+      else if (rt == 64) go(transmission_annuli_kernel<true, 32, 8, 8>, 8);
+      else go(transmission_annuli_kernel<true, 32, 8, 4>, 8);
     } else {
       transmission_annuli_geometry_kernel<false><<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom, w.rays);
       BGB_CUDA(cudaGetLastError());
-      transmission_annuli_kernel<false, 32><<<grid, kTPN * 32, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev,
-                                                                        w.geom, w.rays, w.spectrum);
+      go(transmission_annuli_kernel<false, 32, 4, 1>, 4);
     }
   } else {
     if (m.precision == 1) transmission_geometry_kernel<false><<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom);
