@@ -200,14 +200,21 @@ __global__ void __launch_bounds__(256) emission_kernel_fp64(DeviceModel dm, cons
 // (TransmissionModel::distanceToTangentCenter src/forward_model/transmission/
 // transmission_spectrum.cpp:145-154). Squares are rounded separately so the
 // tangent level gives exactly zero. Computed in FP64; stored as FP64 (precision
-// mode 1) or as double-floats (DF, the default tangent sums).
+// mode 1) or as double-floats (DF, the default tangent sums). Also the effective-height
+// weights rw_t = (R + z_t)((z_{t+1} - z_t) + (z_t - z_{t-1})), t < L-1, into
+// rays[b][L + t] (the layout of the annuli geometry with one ray per level).
 template <bool DF>
 __global__ void transmission_geometry_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
-                                             const EvalInfo* __restrict__ ev, double* __restrict__ geom) {
+                                             const EvalInfo* __restrict__ ev, double* __restrict__ geom,
+                                             double* __restrict__ rays) {
   const int b = blockIdx.x;
   const int L = dm.L;
   const LevelInfo* lv = lev + (size_t)b * L;
   const double R = ev[b].radius;
+  for (int t = threadIdx.x; t < L - 1; t += blockDim.x) {
+    const double zt = lv[t].z;
+    rays[(size_t)b * 2 * L + L + t] = (R + zt) * ((lv[t + 1].z - zt) + (t >= 1 ? zt - lv[t - 1].z : 0.0));
+  }
   for (int idx = threadIdx.x; idx < L * L; idx += blockDim.x) {
     const int t = idx / L, i = idx % L;
     double v = 0.0;
@@ -234,10 +241,11 @@ __global__ void transmission_geometry_kernel(DeviceModel dm, const LevelInfo* __
 // The TPN threads of a wavenumber split the levels' opacities, then share the
 // staged extinction column chi[L][VPB] and split the tangent levels. With DF the
 // extinction column and the tangent optical depths are double-floats on the FP32
-// pipe (the reference's tau > 10 cut-off tested on the double-float value); the
-// transmission exp(-tau) and the effective-height (annulus) sum are FP64 in both
-// modes. The effective height is summed per level,
-// sum_t (R + z_t)(1 - T_t)(dz_{t-1} + dz_t), which regroups the reference's
+// pipe (the reference's tau > 10 cut-off tested on the double-float value), and so are
+// exp(-tau) and 1 - T (relative error ~1e-14); the effective-height (annulus) sum is
+// FP64 in both modes. The effective height is summed per level,
+// sum_t rw_t (1 - T_t), rw_t = (R + z_t)(dz_{t-1} + dz_t) (from the geometry
+// kernel), which regroups the reference's
 // trapezoid sum. Dynamic shared memory: chi [L][VPB] (8 B each), then with DF the
 // evaluation's Rayleigh number densities [L][R] as double-floats.
 // With STORE (double-float path, gradient pass) the kernel also writes, per
@@ -292,6 +300,7 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
                                                            const double* __restrict__ ray_n,
                                                            const EvalInfo* __restrict__ ev,
                                                            const double* __restrict__ geom,
+                                                           const double* __restrict__ rays,
                                                            double* __restrict__ spectrum, ForwardTaps taps) {
   constexpr int TPN = kTPN;
   extern __shared__ double chi_s[];  // [L][VPB]
@@ -336,12 +345,14 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
   __syncthreads();
   double h = 0.0;
   const double Rp = ev[b].radius;
+  const double* rw = rays + (size_t)b * 2 * L + L;  // effective-height weights
   const size_t col = (size_t)b * L * N + k;  // [b][level][k] of level 0 (gradient pass stores)
   if (STORE && active)
     for (int i = j; i < L - 1; i += TPN) taps.tr_c[col + (size_t)i * N] = chi_f[i * VPB + v];
   if (active) {
     for (int t = L - 2 - j; t >= 0; t -= TPN) {
-      double tau;
+      double tau = 0.0;
+      df2 tsd = {0.0f, 0.0f};  // the tangent sum as a double-float (DF)
       df2 qs = {0.0f, 0.0f}, us = {0.0f, 0.0f};
       int last = L - 2;
       if (DF && STORE) {
@@ -362,7 +373,7 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
             break;
           }
         }
-        tau = df_to_double(ts);
+        tsd = ts;
       } else if (DF) {
         const float2* Gt = reinterpret_cast<const float2*>(geom) + (size_t)b * L * L + (size_t)t * L;
         df2 ts = {0.0f, 0.0f};
@@ -393,7 +404,7 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
           ts = df_fma(df2{g.x, g.y}, df2{c.x, c.y}, ts);
           cut = over(ts);
         }
-        tau = df_to_double(ts);
+        tsd = ts;
       } else {
         const double* Gt = geom + (size_t)b * L * L + (size_t)t * L;
         tau = 0.0;
@@ -402,20 +413,23 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
           if (__double_as_longlong(tau) > dm.tau_cut_bits) break;  // tau > cut-off (tau >= 0)
         }
       }
-      double tr;
-      if (DF) tr = __double_as_longlong(tau) > kBits700 ? 0.0 : exp_tang(-tau, et.d);
-      else tr = exp(-tau);
-      if (STORE) {
-        const size_t at = col + (size_t)t * N;
-        const df2 dT = df_from_double(tr);
-        taps.tr_T[at] = make_float2(dT.hi, dT.lo);
-        taps.tr_qs[at] = make_float2(qs.hi, qs.lo);
-        taps.tr_us[at] = make_float2(us.hi, us.lo);
-        taps.tr_I[at] = (short)last;
+      // 1 - T: with DF, T = exp(-tau) and 1 - T in double-float (relative error ~1e-14),
+      // so the ray costs one conversion add and one FMA on the FP64 pipe
+      double omt;
+      if (DF) {
+        const df2 T = df_exp_neg(tsd, et.hi, et.lo);
+        if (STORE) {
+          const size_t at = col + (size_t)t * N;
+          taps.tr_T[at] = make_float2(T.hi, T.lo);
+          taps.tr_qs[at] = make_float2(qs.hi, qs.lo);
+          taps.tr_us[at] = make_float2(us.hi, us.lo);
+          taps.tr_I[at] = (short)last;
+        }
+        omt = df_to_double(df_sub(df_make(1.0f), T));
+      } else {
+        omt = 1. - exp(-tau);
       }
-      const double zt = __ldg(&lv[t].z);
-      const double wz = (__ldg(&lv[t + 1].z) - zt) + (t >= 1 ? zt - __ldg(&lv[t - 1].z) : 0.0);
-      h = fma((Rp + zt) * (1. - tr), wz, h);
+      h = fma(__ldg(&rw[t]), omt, h);
     }
   }
   h_part[j][v] = h;
@@ -1079,7 +1093,7 @@ void ensure_workspace(Model& m, int batch) {
   if (m.transmission) {
     const size_t K = transmission_rays(m);
     BGB_CUDA(cudaMalloc(&w.geom, B * std::max(K, L) * L * sizeof(double)));
-    if (m.annuli > 1) BGB_CUDA(cudaMalloc(&w.rays, B * 2 * (K + 1) * sizeof(double)));
+    BGB_CUDA(cudaMalloc(&w.rays, B * 2 * (K + 1) * sizeof(double)));
   }
   w.capacity = batch;
   ++m.ws_generation;
@@ -1142,8 +1156,8 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
       go(transmission_annuli_kernel<false, 32, 4, 1>, 4);
     }
   } else {
-    if (m.precision == 1) transmission_geometry_kernel<false><<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom);
-    else transmission_geometry_kernel<true><<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom);
+    if (m.precision == 1) transmission_geometry_kernel<false><<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom, w.rays);
+    else transmission_geometry_kernel<true><<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom, w.rays);
     // the launch shape selects the wavenumbers per block: 16, 32 (default) or 64, 4 threads each
     const int vpb = (rt == 16 || rt == 64) ? rt : 32;
     dim3 grid(batch, (dm.N + vpb - 1) / vpb);
@@ -1152,7 +1166,7 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
     if (sm > kTransmissionDynSmem) throw Error(BEAR_ERR_UNSUPPORTED, "too many levels for the transmission kernel");
     const ForwardTaps none{};
     auto go = [&](auto kernel) {
-      kernel<<<grid, kTPN * vpb, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.spectrum, none);
+      kernel<<<grid, kTPN * vpb, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.rays, w.spectrum, none);
     };
     if (taps) {
       // gradient pass: double-float kernel, 32 wavenumbers per block, storing the ray data
@@ -1162,7 +1176,7 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
       const dim3 g32(batch, (dm.N + 31) / 32);
       const size_t sm32 = (size_t)L * 32 * sizeof(double) + (size_t)L * dm.R * sizeof(float2);
       transmission_kernel<true, 32, true><<<g32, kTPN * 32, sm32, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev,
-                                                                        w.geom, w.spectrum, *taps);
+                                                                        w.geom, w.rays, w.spectrum, *taps);
     } else if (vpb == 16) df ? go(transmission_kernel<true, 16>) : go(transmission_kernel<false, 16>);
     else if (vpb == 64) df ? go(transmission_kernel<true, 64>) : go(transmission_kernel<false, 64>);
     else df ? go(transmission_kernel<true, 32>) : go(transmission_kernel<false, 32>);

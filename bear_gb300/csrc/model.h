@@ -218,7 +218,7 @@ struct Workspace {
   double* obs = nullptr;       // B x M internal order
   double* loglike = nullptr;   // B
   double* geom = nullptr;      // transmission path lengths B x L x L (B x K x L with K = (L-1) A annuli)
-  double* rays = nullptr;      // transmission with annuli: B x 2 (K + 1): ray altitude, trapezoid weight
+  double* rays = nullptr;      // transmission: B x 2 (K + 1): ray altitudes, effective-height weights
 };
 
 // Extra outputs of the forward pass that the adjoint reads back.

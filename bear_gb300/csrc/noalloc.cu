@@ -67,7 +67,7 @@ size_t layout(const Model& m, unsigned char* base, Workspace* w) {
   unsigned char* obs = take(M * sizeof(double));
   const size_t K = m.transmission ? (size_t)transmission_rays(m) : 0;
   unsigned char* geom = m.transmission ? take(std::max(K, L) * L * sizeof(double)) : nullptr;
-  unsigned char* rays = (m.transmission && m.annuli > 1) ? take(2 * (K + 1) * sizeof(double)) : nullptr;
+  unsigned char* rays = m.transmission ? take(2 * (K + 1) * sizeof(double)) : nullptr;
   if (base) {
     *w = Workspace{};
     w->capacity = 1;
