@@ -29,8 +29,9 @@
 //                               tangents of the level physics (temperature, chemistry,
 //                               hydrostatic altitudes as prefix sums, cloud extinction),
 //                               planet and star radii
-// Double-float arithmetic on the FP32 pipe throughout except the transmission
-// exp(-tau), the effective-height terms and the per-evaluation tangents (FP64).
+// Double-float arithmetic on the FP32 pipe throughout except the effective-height
+// terms and the per-evaluation tangents (FP64); the ray transmissions T_t are the
+// forward pass's double-float values.
 // Discrete decisions (table brackets, cut-off index, cloud layers) are held fixed.
 
 #include <algorithm>
@@ -74,7 +75,8 @@ __global__ void tr_geometry_adjoint_kernel(DeviceModel dm, const LevelInfo* __re
     const df2 d = df_from_double(v);
     *p = make_float2(d.hi, d.lo);
   };
-  for (int idx = threadIdx.x; idx < L * L; idx += blockDim.x) {
+  // grid: evaluations x blocks of elements
+  for (int idx = blockIdx.y * blockDim.x + threadIdx.x; idx < L * L; idx += gridDim.y * blockDim.x) {
     const int t = idx / L, i = idx % L;
     const double zt = lv[t].z;
     put(P + idx, (R + lv[i].z) * rS(t, i));

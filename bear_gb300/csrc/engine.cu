@@ -211,11 +211,13 @@ __global__ void transmission_geometry_kernel(DeviceModel dm, const LevelInfo* __
   const int L = dm.L;
   const LevelInfo* lv = lev + (size_t)b * L;
   const double R = ev[b].radius;
-  for (int t = threadIdx.x; t < L - 1; t += blockDim.x) {
-    const double zt = lv[t].z;
-    rays[(size_t)b * 2 * L + L + t] = (R + zt) * ((lv[t + 1].z - zt) + (t >= 1 ? zt - lv[t - 1].z : 0.0));
-  }
-  for (int idx = threadIdx.x; idx < L * L; idx += blockDim.x) {
+  if (blockIdx.y == 0)
+    for (int t = threadIdx.x; t < L - 1; t += blockDim.x) {
+      const double zt = lv[t].z;
+      rays[(size_t)b * 2 * L + L + t] = (R + zt) * ((lv[t + 1].z - zt) + (t >= 1 ? zt - lv[t - 1].z : 0.0));
+    }
+  // grid: evaluations x blocks of elements
+  for (int idx = blockIdx.y * blockDim.x + threadIdx.x; idx < L * L; idx += gridDim.y * blockDim.x) {
     const int t = idx / L, i = idx % L;
     double v = 0.0;
     if (i >= t && i < L - 1) {
@@ -465,42 +467,42 @@ template <bool DF>
 __global__ void transmission_annuli_geometry_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
                                                     const EvalInfo* __restrict__ ev, double* __restrict__ geom,
                                                     double* __restrict__ rays) {
+  // one thread per ray kr (grid: evaluations x ray blocks); kr == K is the top level
   const int b = blockIdx.x;
   const int L = dm.L, A = dm.annuli, K = (L - 1) * A;
+  const int kr = blockIdx.y * blockDim.x + threadIdx.x;
+  if (kr > K) return;
   const LevelInfo* lv = lev + (size_t)b * L;
   const double R = ev[b].radius;
+  auto zb_of = [&](int q) {
+    if (q >= K) return lv[L - 1].z;
+    const int t = q / A, jj = q - t * A;
+    const double z0 = lv[t].z, z1 = lv[t + 1].z;
+    return __dadd_rn(z0, __ddiv_rn(__dmul_rn(__dsub_rn(z1, z0), (double)jj), (double)A));
+  };
+  const double z = zb_of(kr);
+  const double wz = (kr < K ? zb_of(kr + 1) - z : 0.0) + (kr >= 1 ? z - zb_of(kr - 1) : 0.0);
   double* zb = rays + (size_t)b * 2 * (K + 1);
-  double* rw = zb + (K + 1);
-  for (int kr = threadIdx.x; kr <= K; kr += blockDim.x) {
-    double z = lv[L - 1].z;
-    if (kr < K) {
-      const int t = kr / A, jj = kr - t * A;
-      const double z0 = lv[t].z, z1 = lv[t + 1].z;
-      z = __dadd_rn(z0, __ddiv_rn(__dmul_rn(__dsub_rn(z1, z0), (double)jj), (double)A));
-    }
-    zb[kr] = z;
-  }
-  __syncthreads();
-  for (int kr = threadIdx.x; kr <= K; kr += blockDim.x)
-    rw[kr] = (R + zb[kr]) * ((kr < K ? zb[kr + 1] - zb[kr] : 0.0) + (kr >= 1 ? zb[kr] - zb[kr - 1] : 0.0));
-  for (int idx = threadIdx.x; idx < K * L; idx += blockDim.x) {
-    const int t = idx / (L * A), rem = idx - t * (L * A), i = rem / A, kr = t * A + (rem - i * A);
-    double v = 0.0;
-    if (i >= t && i < L - 1) {
-      const double bt = R + zb[kr];
-      const double bb = __dmul_rn(bt, bt);
-      const double a1 = R + lv[i + 1].z;
-      v = sqrt(__dsub_rn(__dmul_rn(a1, a1), bb));
-      if (i > t) {
-        const double a0 = R + lv[i].z;
-        v -= sqrt(__dsub_rn(__dmul_rn(a0, a0), bb));
-      }
-    }
+  zb[kr] = z;
+  zb[K + 1 + kr] = (R + z) * wz;
+  if (kr == K) return;
+  // path lengths through level pairs (i, i+1), i = t..L-2: s_{i+1} - s_i with
+  // s_i = sqrt((R + z_i)^2 - b^2), each root taken once; the partial segment is s_{t+1}
+  const int t = kr / A, jj = kr - t * A;
+  const double bt = R + z;
+  const double bb = __dmul_rn(bt, bt);
+  double s_prev = 0.0;
+  for (int i = t; i < L - 1; ++i) {
+    const double a1 = R + lv[i + 1].z;
+    const double s_next = sqrt(__dsub_rn(__dmul_rn(a1, a1), bb));
+    const double v = s_next - s_prev;
+    s_prev = s_next;
+    const size_t at = (((size_t)b * (L - 1) + t) * L + i) * A + jj;  // [b][t][i][j]
     if (DF) {
       const df2 d = df_from_double(v);
-      reinterpret_cast<float2*>(geom)[(size_t)b * K * L + idx] = make_float2(d.hi, d.lo);
+      reinterpret_cast<float2*>(geom)[at] = make_float2(d.hi, d.lo);
     } else {
-      geom[(size_t)b * K * L + idx] = v;
+      geom[at] = v;
     }
   }
 }
@@ -1141,23 +1143,25 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
     const size_t sm = annuli_dyn_smem(L, dm.R, df);
     if (sm > kTransmissionDynSmem) throw Error(BEAR_ERR_UNSUPPORTED, "too many levels for the transmission kernel");
     const dim3 grid(batch, (dm.N + 31) / 32);
+    const dim3 ggrid(batch, (transmission_rays(m) + 1 + 127) / 128);  // one thread per ray + the top level
     auto go = [&](auto kernel, int tpn) {
       kernel<<<grid, tpn * 32, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.rays, w.spectrum);
     };
     if (df) {
-      transmission_annuli_geometry_kernel<true><<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom, w.rays);
+      transmission_annuli_geometry_kernel<true><<<ggrid, 128, 0, st>>>(dm, w.lev, w.ev, w.geom, w.rays);
       BGB_CUDA(cudaGetLastError());
       if (rt == 16) go(transmission_annuli_kernel<true, 32, 4, 4>, 4);
       else if (rt == 64) go(transmission_annuli_kernel<true, 32, 8, 8>, 8);
       else go(transmission_annuli_kernel<true, 32, 8, 4>, 8);
     } else {
-      transmission_annuli_geometry_kernel<false><<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom, w.rays);
+      transmission_annuli_geometry_kernel<false><<<ggrid, 128, 0, st>>>(dm, w.lev, w.ev, w.geom, w.rays);
       BGB_CUDA(cudaGetLastError());
       go(transmission_annuli_kernel<false, 32, 4, 1>, 4);
     }
   } else {
-    if (m.precision == 1) transmission_geometry_kernel<false><<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom, w.rays);
-    else transmission_geometry_kernel<true><<<batch, 256, 0, st>>>(dm, w.lev, w.ev, w.geom, w.rays);
+    const dim3 ggrid(batch, (L * L + 255) / 256);
+    if (m.precision == 1) transmission_geometry_kernel<false><<<ggrid, 256, 0, st>>>(dm, w.lev, w.ev, w.geom, w.rays);
+    else transmission_geometry_kernel<true><<<ggrid, 256, 0, st>>>(dm, w.lev, w.ev, w.geom, w.rays);
     // the launch shape selects the wavenumbers per block: 16, 32 (default) or 64, 4 threads each
     const int vpb = (rt == 16 || rt == 64) ? rt : 32;
     dim3 grid(batch, (dm.N + vpb - 1) / vpb);
@@ -1171,7 +1175,7 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
     if (taps) {
       // gradient pass: double-float kernel, 32 wavenumbers per block, storing the ray data
       if (!df) throw Error(BEAR_ERR_UNSUPPORTED, "the transmission gradient runs in precision mode 0");
-      tr_geometry_adjoint_kernel<<<batch, 256, 0, st>>>(dm, w.lev, w.ev, taps->tr_geo);
+      tr_geometry_adjoint_kernel<<<dim3(batch, (L * L + 255) / 256), 256, 0, st>>>(dm, w.lev, w.ev, taps->tr_geo);
       BGB_CUDA(cudaGetLastError());
       const dim3 g32(batch, (dm.N + 31) / 32);
       const size_t sm32 = (size_t)L * 32 * sizeof(double) + (size_t)L * dm.R * sizeof(float2);
