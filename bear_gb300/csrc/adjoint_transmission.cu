@@ -133,6 +133,7 @@ __global__ void __launch_bounds__(128) tr_adjoint_pass2a(DeviceModel dm, TrArgs 
   float2* fw_s = fz_s + L;                                             // [L]: wz_t
   float2* ff_s = fw_s + L;                                             // [L]: (R + z_t) wz_t
   short* I_s = reinterpret_cast<short*>(ff_s + L);                     // [L][32]
+  short* m_s = I_s + (size_t)L * 32;                                   // [L][32]
   const int b = blockIdx.x, lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
   const int kk = blockIdx.y * 32 + lane;
   const bool active = kk < dm.N;
@@ -180,6 +181,17 @@ __global__ void __launch_bounds__(128) tr_adjoint_pass2a(DeviceModel dm, TrArgs 
   }
   if (grp == 0) rp = df_add(rp, df_mul(gh, df_from_double(2.0 * Rp)));  // depth = (h + R^2) / R_s^2
   __syncthreads();
+  // m(j): the lowest tangent level whose ray reaches level j. Ray t covers levels
+  // t..I_t + 1 (I_t >= t), so in ascending t the covered levels form a growing prefix.
+  if (grp == 0) {
+    int cov = -1;
+    for (int t = 0; t < L - 1; ++t) {
+      const int hi = min((int)I_s[t * 32 + lane] + 1, L - 1);
+      for (int j = cov + 1; j <= hi; ++j) m_s[j * 32 + lane] = (short)t;
+      cov = max(cov, hi);
+    }
+  }
+  __syncthreads();
   if (active) {
     const float2* G = a.geom + (size_t)b * L * L;
     const float2* P = a.geo + (size_t)b * 3 * L * L;
@@ -188,22 +200,25 @@ __global__ void __launch_bounds__(128) tr_adjoint_pass2a(DeviceModel dm, TrArgs 
       const df2 cj1 = j >= 1 ? ld(a.c, j - 1) : z;
       const df2 cj = j <= L - 2 ? ld(a.c, j) : z;
       const df2 dcc = df_sub(cj1, cj);
-      df2 gc = z, gzp = z;
+      // g_z part: sum over rays through j of g_tau P (x dcc), over rays ending at j - 1 (x c_{j-1})
+      df2 gc = z, pin = z, pend = z;
       const int tmax = min(j, L - 2);
-      for (int t = 0; t <= tmax; ++t) {
+      // from the lowest m(j) of the warp's wavenumbers, so the path-length loads stay uniform
+      const unsigned mask = __activemask();
+      const int t0 = (int)__reduce_min_sync(mask, (unsigned)m_s[j * 32 + lane]);
+      for (int t = t0; t <= tmax; ++t) {
         const int I = I_s[t * 32 + lane];
+        const float2 g = __ldg(&G[(size_t)t * L + j]), p = __ldg(&P[(size_t)t * L + j]);
         if (I < j - 1) continue;  // the ray of tangent level t stops below level j
         const df2 gtau = sm(gt_s, t * 32 + lane);
         const bool in_j = I >= j && j <= L - 2;
-        if (in_j) {
-          const float2 g = __ldg(&G[(size_t)t * L + j]);
-          gc = df_fma(gtau, df2{g.x, g.y}, gc);
-        }
+        if (in_j) gc = df_fma(gtau, df2{g.x, g.y}, gc);
         if (t < j) {
-          const float2 p = __ldg(&P[(size_t)t * L + j]);
-          gzp = df_fma(df_mul(gtau, df2{p.x, p.y}), in_j ? dcc : cj1, gzp);  // j - 1 <= I_t holds here
+          if (in_j) pin = df_fma(gtau, df2{p.x, p.y}, pin);
+          else pend = df_fma(gtau, df2{p.x, p.y}, pend);  // j - 1 <= I_t holds here
         }
       }
+      const df2 gzp = df_fma(pin, dcc, df_mul(pend, cj1));
       // direct terms of the effective height: z1_j + g_h (A_{j-1} - A_{j+1}) (- A_0 at j = 0)
       df2 nb = z;
       if (j >= 1) nb = ld(a.us, j - 1);
@@ -315,8 +330,27 @@ __global__ void __launch_bounds__(kTrTPN * kTrVPB, VP == 32 ? 4 : 6) tr_adjoint_
   }
 }
 
+// ------------------------------------------------------------------ partial-sum reduction
+// One warp per (evaluation, level, sink) row: the row's per-tile partial sums added in a
+// fixed order (lane-strided, then a warp tree), the total written over the row's first
+// entry. Grid: evaluations x row blocks of kReduceWarps rows.
+constexpr int kReduceWarps = 8;
+
+__global__ void __launch_bounds__(kReduceWarps * 32) tr_partial_reduce_kernel(double* __restrict__ partial, int rows,
+                                                                              int tiles) {
+  const int lane = threadIdx.x & 31;
+  const int row = blockIdx.y * kReduceWarps + (threadIdx.x >> 5);
+  if (row >= rows) return;
+  double* p = partial + ((size_t)blockIdx.x * rows + row) * tiles;
+  double s = 0.0;
+  for (int q = lane; q < tiles; q += 32) s += p[q];
+  s = warp_sum_d(s);
+  if (lane == 0) p[0] = s;
+}
+
 // ------------------------------------------------------------------ parameter tangents
-// One block per evaluation. sg[L][V] = the partial sums reduced over the tiles; then
+// One block per evaluation. sg[L][V] = the partial sums reduced over the tiles (by
+// tr_partial_reduce_kernel, first entry of each row); then
 // thread th < P forms d log L / d param_th = sum over levels of the sinks times the
 // tangents of ln n (table and Rayleigh species), T, z_l and the cloud extinction
 // chi_cloud,l = tau_layer(l-1) / (z_l - z_{l-1}) (CloudModel::convertOpticalDepth
@@ -331,17 +365,11 @@ __global__ void __launch_bounds__(128) tr_atmosphere_adjoint_kernel(
   extern __shared__ double sg[];
   __shared__ double s_rp;
   const AtmosphereConfig& c = *dm.cfg;
-  const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int L = c.L, S = c.S, R = c.R;
   if (ev[b].neglect) return;
   const double inv = seed[b * 3 + 1];
-  for (int idx = warp; idx < L * V; idx += nw) {
-    const double* p = partial + ((size_t)b * L * V + idx) * tiles;
-    double s = 0.0;
-    for (int q = lane; q < tiles; q += 32) s += p[q];
-    s = warp_sum_d(s);
-    if (lane == 0) sg[idx] = s * inv;
-  }
+  for (int idx = tid; idx < L * V; idx += blockDim.x) sg[idx] = partial[((size_t)b * L * V + idx) * tiles] * inv;
   if (warp == 0) {
     double s = 0.0;
     for (int q = lane; q < rp_tiles; q += 32) s += rp[(size_t)b * rp_tiles + q];
@@ -479,7 +507,7 @@ void transmission_adjoint_chunk(Model& m, const double* params_chunk, int nb, cu
   const int tiles = (int)((N + 31) / 32);
   TrArgs a{w.lev, w.lsdf, w.ray_n, w.ev, reinterpret_cast<const float2*>(w.geom), tp.tr_geo, tp.dwT, g.gS,
            g.seed, tp.tr_c, tp.tr_T, tp.tr_qs, tp.tr_us, tp.tr_I, g.tr_gc, g.tr_gz, g.tr_rp, g.partial, V};
-  const size_t sm2a = (size_t)L * 32 * (sizeof(float2) + sizeof(short)) + (size_t)3 * L * sizeof(float2);
+  const size_t sm2a = (size_t)L * 32 * (sizeof(float2) + 2 * sizeof(short)) + (size_t)3 * L * sizeof(float2);
   if (sm2a > 48 * 1024)
     BGB_CUDA(cudaFuncSetAttribute(tr_adjoint_pass2a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2a));
   tr_adjoint_pass2a<<<dim3(nb, tiles), 128, sm2a, st>>>(dm, a);
@@ -497,6 +525,9 @@ void transmission_adjoint_chunk(Model& m, const double* params_chunk, int nb, cu
   const size_t sma = (size_t)L * V * sizeof(double);
   if (sma > 48 * 1024)
     BGB_CUDA(cudaFuncSetAttribute(tr_atmosphere_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sma));
+  tr_partial_reduce_kernel<<<dim3(nb, (L * V + kReduceWarps - 1) / kReduceWarps), kReduceWarps * 32, 0, st>>>(
+      g.partial, L * V, tiles);
+  BGB_CUDA(cudaGetLastError());
   tr_atmosphere_adjoint_kernel<<<nb, 128, sma, st>>>(dm, params_chunk, P, w.lev, w.ev, g.partial, V, tiles, g.tr_rp,
                                                      tiles, g.seed, grad_chunk);
   BGB_CUDA(cudaGetLastError());

@@ -1052,6 +1052,7 @@ void upload_model(Model& m) {
     BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<true, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<false, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<true, 32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<true, 64, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_annuli_kernel<true, 32, 4, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_annuli_kernel<true, 32, 8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_annuli_kernel<true, 32, 8, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
@@ -1173,13 +1174,19 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
       kernel<<<grid, kTPN * vpb, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.rays, w.spectrum, none);
     };
     if (taps) {
-      // gradient pass: double-float kernel, 32 wavenumbers per block, storing the ray data
+      // gradient pass: double-float kernel storing the ray data
       if (!df) throw Error(BEAR_ERR_UNSUPPORTED, "the transmission gradient runs in precision mode 0");
       tr_geometry_adjoint_kernel<<<dim3(batch, (L * L + 255) / 256), 256, 0, st>>>(dm, w.lev, w.ev, taps->tr_geo);
       BGB_CUDA(cudaGetLastError());
-      const dim3 g32(batch, (dm.N + 31) / 32);
-      const size_t sm32 = (size_t)L * 32 * sizeof(double) + (size_t)L * dm.R * sizeof(float2);
-      transmission_kernel<true, 32, true><<<g32, kTPN * 32, sm32, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev,
+      // the tuned wavenumbers per block when it is 64, else 32
+      const int sv = vpb == 64 ? 64 : 32;
+      const dim3 gs(batch, (dm.N + sv - 1) / sv);
+      const size_t sms = (size_t)L * sv * sizeof(double) + (size_t)L * dm.R * sizeof(float2);
+      if (sv == 64)
+        transmission_kernel<true, 64, true><<<gs, kTPN * 64, sms, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev,
+                                                                        w.geom, w.rays, w.spectrum, *taps);
+      else
+        transmission_kernel<true, 32, true><<<gs, kTPN * 32, sms, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev,
                                                                         w.geom, w.rays, w.spectrum, *taps);
     } else if (vpb == 16) df ? go(transmission_kernel<true, 16>) : go(transmission_kernel<false, 16>);
     else if (vpb == 64) df ? go(transmission_kernel<true, 64>) : go(transmission_kernel<false, 64>);
