@@ -882,6 +882,8 @@ void free_grad_workspace(Model& m) {
   cudaFree(g.taps.tr_qs);
   cudaFree(g.taps.tr_us);
   cudaFree(g.taps.tr_I);
+  cudaFree(g.taps.tr_ts);
+  cudaFree(g.taps.tr_dk);
   cudaFree(g.tr_gc);
   cudaFree(g.tr_gz);
   cudaFree(g.tr_rp);
@@ -931,8 +933,8 @@ void launch_emission_adjoint(const Model& m, dim3 grid, size_t smem, cudaStream_
 }  // namespace
 
 // adjoint_transmission.cu
-size_t transmission_grad_bytes_per_eval(const Model& m, int V);
-void alloc_transmission_grad(Model& m, int chunk, int V);
+size_t transmission_grad_bytes_per_eval(const Model& m, int V, bool store);
+void alloc_transmission_grad(Model& m, int chunk, int V, bool store);
 void transmission_adjoint_chunk(Model& m, const double* params_chunk, int nb, cudaStream_t st, double* grad_chunk,
                                 int V);
 
@@ -947,18 +949,23 @@ static void launch_gradient_transmission(Model& m, const double* params_dev, int
   if (P > 128) throw Error(BEAR_ERR_UNSUPPORTED, "the gradient supports at most 128 parameters");
   if (L > 32767) throw Error(BEAR_ERR_UNSUPPORTED, "too many levels");
   const size_t S1 = std::max(S, 1), M = std::max(m.M, 1);
-  const size_t per_eval = transmission_grad_bytes_per_eval(m, V) + L * S1 * sizeof(float2) + M * 8 + 3 * 8;
+  // the forward pass stores the opacity terms for the adjoint when chunks of at least
+  // min(batch, 8) evaluations still fit the memory budget; else the adjoint recomputes them
+  const size_t extra = L * S1 * sizeof(float2) + M * 8 + 3 * 8;
+  const size_t per_store = transmission_grad_bytes_per_eval(m, V, true) + extra;
+  const bool store = m.grad_budget / per_store >= std::min<size_t>((size_t)batch, 8);
+  const size_t per_eval = store ? per_store : transmission_grad_bytes_per_eval(m, V, false) + extra;
   const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)batch, m.grad_budget / per_eval));
   BGB_CUDA(cudaSetDevice(m.device));
   ensure_workspace(m, chunk);
   GradWorkspace& g = m.gws;
-  if (chunk > g.capacity || g.tiles != -1) {
+  if (chunk > g.capacity || g.tiles != -1 || g.tr_store != store) {
     BGB_CUDA(cudaDeviceSynchronize());
     free_grad_workspace(m);
     BGB_CUDA(cudaMalloc(&g.taps.dwT, (size_t)chunk * L * S1 * sizeof(float2)));
     BGB_CUDA(cudaMalloc(&g.gS, (size_t)chunk * M * sizeof(double)));
     BGB_CUDA(cudaMalloc(&g.seed, (size_t)chunk * 3 * sizeof(double)));
-    alloc_transmission_grad(m, chunk, V);
+    alloc_transmission_grad(m, chunk, V, store);
     g.capacity = chunk;
     g.tiles = -1;  // transmission layout
   }

@@ -112,6 +112,8 @@ struct TrArgs {
   double* rp;
   double* partial;
   int V;
+  const float2* ts;  // stored opacity terms (nullptr: recompute them)
+  const float2* dk;  // stored temperature-slope sums
 };
 
 // Block: 32 wavenumbers (lanes) x 4 groups; group w takes levels j = w, w+4, ...
@@ -241,7 +243,8 @@ __global__ void __launch_bounds__(128) tr_adjoint_pass2a(DeviceModel dm, TrArgs 
 
 // ------------------------------------------------------------------ pass 2b
 // Block: 32 wavenumbers (lanes) x 4 warps; warp w takes levels w, w+4, ...
-// Dynamic shared memory: per-species terms float2 [S][128] then double [S][128].
+// Dynamic shared memory: per-species terms float2 [S][128], double [S][128], then the
+// evaluation's Rayleigh number densities float2 [L][R].
 // partial[b][l][v][tile]: v = 0..S-1 d log L / d ln n_s (table species),
 // S..S+R-1 d log L / d ln n_r (Rayleigh species), S+R temperature, S+R+1 z_l,
 // S+R+2 cloud extinction of level l (all times the evaluation's seed normaliser).
@@ -253,7 +256,12 @@ __global__ void __launch_bounds__(kTrTPN * kTrVPB, VP == 32 ? 4 : 6) tr_adjoint_
   const int S = dm.S, R = dm.R, L = dm.L;
   float2* tdf = reinterpret_cast<float2*>(tr2_smem);
   double* twd = reinterpret_cast<double*>(tr2_smem + (size_t)S * blockDim.x * sizeof(float2));
+  float2* rn_s = reinterpret_cast<float2*>(twd + (size_t)S * blockDim.x);  // [L][R] Rayleigh n as double-floats
   load_exp_tables(et);
+  for (int idx = threadIdx.x; idx < L * R; idx += blockDim.x) {
+    const df2 d = df_from_double(__ldg(&a.ray_n[(size_t)blockIdx.x * L * R + idx]));
+    rn_s[idx] = make_float2(d.hi, d.lo);
+  }
   __syncthreads();
   const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int kk = blockIdx.y * 32 + lane;
@@ -283,37 +291,46 @@ __global__ void __launch_bounds__(kTrTPN * kTrVPB, VP == 32 ? 4 : 6) tr_adjoint_
       const float2 v = a.gz[col + (size_t)l * N];
       gzl = df2{v.x, v.y};
     }
-    // opacity terms and their temperature slope (level-table values are log2 units)
+    // opacity terms and their temperature slope (level-table values are log2 units): from the
+    // forward pass's stores where it kept them, else recomputed in the same order
     df2 dk = {0.0f, 0.0f};
     double dkw = 0.0;
     bool wide = false;
-    const float2* dwl = dw + (size_t)l * S;
-    level_kappa_df_cb<2>(dm.ltab, N, sf + (size_t)l * S, S, k, et,
-                      [&](int s, df2 t, double t_w, bool is_wide, df2 lo, df2 hi) {
-                        const float2 d = __ldg(dwl + s);
-                        td[(size_t)s * blockDim.x] = make_float2(t.hi, t.lo);
-                        tw[(size_t)s * blockDim.x] = t_w;
-                        if (d.x != 0.0f) {
-                          const df2 slope = df_mul(df_sub(hi, lo), df2{d.x, d.y});
-                          if (is_wide) dkw += t_w * df_to_double(slope);
-                          else dk = df_add(dk, df_mul(t, slope));
-                        }
-                        wide = wide || is_wide;
-                      });
+    const float2 dks = a.ts ? a.dk[col + (size_t)l * N] : make_float2(__int_as_float(0x7fc00000), 0.0f);
+    const bool stored = !isnan(dks.x);
+    const float2* tsl = a.ts + ((size_t)b * L + l) * S * N + k;  // [s][N] (stored mode)
+    if (stored) {
+      dk = df2{dks.x, dks.y};
+    } else {
+      const float2* dwl = dw + (size_t)l * S;
+      level_kappa_df_cb<2>(dm.ltab, N, sf + (size_t)l * S, S, k, et,
+                           [&](int s, df2 t, double t_w, bool is_wide, df2 lo, df2 hi) {
+                             const float2 d = __ldg(dwl + s);
+                             td[(size_t)s * blockDim.x] = make_float2(t.hi, t.lo);
+                             tw[(size_t)s * blockDim.x] = t_w;
+                             if (d.x != 0.0f) {
+                               const df2 slope = df_mul(df_sub(hi, lo), df2{d.x, d.y});
+                               if (is_wide) dkw += t_w * df_to_double(slope);
+                               else dk = df_add(dk, df_mul(t, slope));
+                             }
+                             wide = wide || is_wide;
+                           });
+    }
     df2 gT = df_mul(gx, df_mul(dk, df2{kLn2Hi, kLn2Lo}));
     if (wide) gT = df_add(gT, df_from_double(df_to_double(gx) * dkw * 0.693147180559945309));
-    const double* rn = a.ray_n + ((size_t)b * L + l) * R;
+    const float2* rn = rn_s + (size_t)l * R;
     df2 v[VP];
 #pragma unroll
     for (int q = 0; q < VP; ++q) {
       df2 x = {0.0f, 0.0f};
       if (q < S) {
-        const float2 t = td[(size_t)q * blockDim.x];
+        const float2 t = stored ? __ldg(tsl + (size_t)q * N) : td[(size_t)q * blockDim.x];
         x = df_mul(gx, df2{t.x, t.y});
         if (wide) x = df_add(x, df_from_double(df_to_double(gx) * tw[(size_t)q * blockDim.x]));
       } else if (q < S + R) {
         const float2 sr = __ldg(&dm.rayleigh_df[(size_t)(q - S) * N + k]);
-        x = df_mul(gx, df_mul(df2{sr.x, sr.y}, df_from_double(__ldg(&rn[q - S]))));
+        const float2 nr = rn[q - S];
+        x = df_mul(gx, df_mul(df2{sr.x, sr.y}, df2{nr.x, nr.y}));
       } else if (q == S + R) {
         x = gT;
       } else if (q == S + R + 1) {
@@ -472,16 +489,22 @@ __global__ void __launch_bounds__(128) tr_atmosphere_adjoint_kernel(
 }
 
 // ------------------------------------------------------------------ host side
-size_t transmission_grad_bytes_per_eval(const Model& m, int V) {
+size_t transmission_grad_bytes_per_eval(const Model& m, int V, bool store) {
   const size_t L = m.L, N = m.N;
   const size_t tiles = (N + 31) / 32;
+  const size_t terms = store ? L * N * ((size_t)m.acfg.S + 1) * sizeof(float2) : 0;
   return L * N * (6 * sizeof(float2) + sizeof(short)) + 3 * L * L * sizeof(float2) + L * (size_t)V * tiles * 8 +
-         tiles * 8;
+         tiles * 8 + terms;
 }
 
-void alloc_transmission_grad(Model& m, int chunk, int V) {
+void alloc_transmission_grad(Model& m, int chunk, int V, bool store) {
   GradWorkspace& g = m.gws;
   const size_t B = chunk, L = m.L, N = m.N;
+  g.tr_store = store;
+  if (store) {
+    BGB_CUDA(cudaMalloc(&g.taps.tr_ts, B * L * (size_t)m.acfg.S * N * sizeof(float2)));
+    BGB_CUDA(cudaMalloc(&g.taps.tr_dk, B * L * N * sizeof(float2)));
+  }
   const size_t n = B * L * N, tiles = (N + 31) / 32;
   BGB_CUDA(cudaMalloc(&g.taps.tr_c, n * sizeof(float2)));
   BGB_CUDA(cudaMalloc(&g.taps.tr_T, n * sizeof(float2)));
@@ -506,13 +529,14 @@ void transmission_adjoint_chunk(Model& m, const double* params_chunk, int nb, cu
   const size_t N = m.N;
   const int tiles = (int)((N + 31) / 32);
   TrArgs a{w.lev, w.lsdf, w.ray_n, w.ev, reinterpret_cast<const float2*>(w.geom), tp.tr_geo, tp.dwT, g.gS,
-           g.seed, tp.tr_c, tp.tr_T, tp.tr_qs, tp.tr_us, tp.tr_I, g.tr_gc, g.tr_gz, g.tr_rp, g.partial, V};
+           g.seed, tp.tr_c, tp.tr_T, tp.tr_qs, tp.tr_us, tp.tr_I, g.tr_gc, g.tr_gz, g.tr_rp, g.partial, V,
+           tp.tr_ts, tp.tr_dk};
   const size_t sm2a = (size_t)L * 32 * (sizeof(float2) + 2 * sizeof(short)) + (size_t)3 * L * sizeof(float2);
   if (sm2a > 48 * 1024)
     BGB_CUDA(cudaFuncSetAttribute(tr_adjoint_pass2a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2a));
   tr_adjoint_pass2a<<<dim3(nb, tiles), 128, sm2a, st>>>(dm, a);
   BGB_CUDA(cudaGetLastError());
-  const size_t sm2 = (size_t)S * kTrTPN * kTrVPB * (sizeof(float2) + sizeof(double));
+  const size_t sm2 = (size_t)S * kTrTPN * kTrVPB * (sizeof(float2) + sizeof(double)) + (size_t)L * m.acfg.R * sizeof(float2);
   const int VP = V <= 8 ? 8 : V <= 16 ? 16 : 32;
   auto go2 = [&](auto kernel) {
     if (sm2 > 48 * 1024) BGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));

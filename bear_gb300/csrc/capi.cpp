@@ -228,7 +228,7 @@ int bear_model_set_gradient_memory(bear_model* h, long long bytes) {
   return guarded([&] {
     if (!h) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null model");
     if (bytes < 0) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "bytes must be non-negative");
-    h->m.grad_budget = bytes ? (size_t)bytes : (size_t(16) << 30);
+    h->m.grad_budget = bytes ? (size_t)bytes : (size_t(32) << 30);
   });
 }
 

@@ -295,6 +295,46 @@ __device__ __forceinline__ void tr_extinction(const DeviceModel& dm, const Level
   }
 }
 
+// The same double-float extinction for the gradient's forward pass when it stores the
+// opacity terms: each table species' term into taps.tr_ts and the temperature-slope sum
+// sum_s term_s (hi_s - lo_s) d wT_s / dT into taps.tr_dk (NaN where a term lies outside
+// the float range), in the order the transmission adjoint would recompute them.
+template <int VPB>
+__device__ __forceinline__ void tr_extinction_terms(const DeviceModel& dm, const LevelInfo* __restrict__ lv,
+                                                    const LevelSpeciesDF* __restrict__ sf, int b, int k, int v,
+                                                    int j, const ExpTables& et, const float2* rn_s, double csh,
+                                                    double* chi_s, const ForwardTaps& taps) {
+  float2* chi_f = reinterpret_cast<float2*>(chi_s);
+  const int L = dm.L, S = dm.S, R = dm.R;
+  const size_t N = dm.N;
+  for (int l = j; l < L; l += kTPN) {
+    const float2* dwl = taps.dwT + ((size_t)b * L + l) * S;
+    float2* tso = taps.tr_ts + ((size_t)b * L + l) * S * N + k;
+    df2 dk = {0.0f, 0.0f};
+    bool wide = false;
+    const Kappa kp = level_kappa_df_cb<4>(dm.ltab, N, sf + (size_t)l * S, S, k, et,
+                                          [&](int s, df2 t, double, bool is_wide, df2 lo, df2 hi) {
+                                            tso[(size_t)s * N] = make_float2(t.hi, t.lo);
+                                            const float2 d = __ldg(dwl + s);
+                                            if (d.x != 0.0f && !is_wide)
+                                              dk = df_add(dk, df_mul(t, df_mul(df_sub(hi, lo), df2{d.x, d.y})));
+                                            wide = wide || is_wide;
+                                          });
+    taps.tr_dk[((size_t)b * L + l) * N + k] = wide ? make_float2(__int_as_float(0x7fc00000), 0.0f)
+                                                   : make_float2(dk.hi, dk.lo);
+    df2 x = kp.v;
+    if ((__double_as_longlong(kp.wide) << 1) != 0) x = df_add(x, df_from_double(kp.wide));
+    for (int r = 0; r < R; ++r) {
+      const float2 sr = __ldg(&dm.rayleigh_df[(size_t)r * N + k]);
+      const float2 nr = rn_s[l * R + r];
+      x = df_fma(df2{sr.x, sr.y}, df2{nr.x, nr.y}, x);
+    }
+    const float2 cl = __ldg(reinterpret_cast<const float2*>(&lv[l].cloud_hi));
+    x = dm.cloud_kind ? df_fma(df2{cl.x, cl.y}, df_from_double(csh), x) : df_add(x, df2{cl.x, cl.y});
+    chi_f[l * VPB + v] = make_float2(x.hi, x.lo);
+  }
+}
+
 template <bool DF, int VPB, bool STORE = false>
 __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
                                                            const LevelSpecies* __restrict__ ls,
@@ -330,7 +370,10 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
   }
   __syncthreads();
   // extinction abs + scat + cloud of every level (the TPN threads take every TPN-th level)
-  if (active) tr_extinction<DF, VPB>(dm, lv, sp, sf, ray_n, b, k, v, j, et, rn_s, csh, chi_s);
+  if (active) {
+    if (STORE && DF && taps.tr_ts) tr_extinction_terms<VPB>(dm, lv, sf, b, k, v, j, et, rn_s, csh, chi_s, taps);
+    else tr_extinction<DF, VPB>(dm, lv, sp, sf, ray_n, b, k, v, j, et, rn_s, csh, chi_s);
+  }
   __syncthreads();
   // neighbour sums chi_i + chi_{i+1}, the bracket of every trapezoid term
   if (active && j == 0) {

@@ -234,6 +234,10 @@ struct ForwardTaps {
   float2* tr_qs = nullptr;   // sum_i c_i Q[t][i] over the ray's terms
   float2* tr_us = nullptr;   // sum_i c_i U[t][i]
   short* tr_I = nullptr;     // last level index inside the cut-off
+  // transmission, when the gradient's memory budget allows (else the adjoint recomputes them):
+  float2* tr_ts = nullptr;   // B x L x S x N: each table species' opacity term n_s sigma_s
+  float2* tr_dk = nullptr;   // B x L x N: sum_s term_s (hi_s - lo_s) d wT_s / dT; x = NaN where a
+                             // term lies outside the float range (the adjoint recomputes there)
 };
 
 // Work buffers of the gradient for a chunk of evaluations.
@@ -249,6 +253,7 @@ struct GradWorkspace {
   float2* tr_gc = nullptr;    // d log L / d (chi_j + chi_{j+1})
   float2* tr_gz = nullptr;    // d log L / d z_j
   double* tr_rp = nullptr;    // per (evaluation, tile) partial d log L / d R_p
+  bool tr_store = false;      // the forward pass stores the opacity terms (taps.tr_ts, tr_dk)
 };
 
 // ----------------------------------------------------------------- host model
@@ -366,7 +371,7 @@ struct Model {
   bool tables_shared = false;         // true when another model created them
   Workspace ws;
   GradWorkspace gws;
-  size_t grad_budget = size_t(16) << 30;  // bytes of gradient work buffers per chunk
+  size_t grad_budget = size_t(32) << 30;  // bytes of gradient work buffers per chunk
   DevicePrior* d_priors = nullptr;  // prior table (bear_model_set_priors)
   // contribution functions: device L x N buffer and the wavelength-integration operator
   // (rows in internal order, cf_out = caller-order index), built on first use

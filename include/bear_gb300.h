@@ -207,7 +207,7 @@ int bear_loglike_grad_batch(bear_model* m, const double* params_dev, int batch, 
 int bear_model_set_tau_cutoff(bear_model* m, double tau);
 
 /* Device memory the gradient's work buffers may use per chunk of evaluations
- * (0 = default, 16 GiB). No reference counterpart. */
+ * (0 = default, 32 GiB). No reference counterpart. */
 int bear_model_set_gradient_memory(bear_model* m, long long bytes);
 
 /* --------------------------------------------------------------- autotuner and captured batches
