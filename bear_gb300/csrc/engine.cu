@@ -119,30 +119,31 @@ __global__ void __launch_bounds__(256, 6) emission_kernel(DeviceModel dm, const 
   const df2 csd = df_from_double(csh);
   Kappa kap_prev = kappa(0);
   double B_prev = planck(0);
-  double I1 = B_prev, I2 = B_prev;
+  double J1 = 0.0, J2 = 0.0;  // I - B: the bottom boundary is I = B
   if (STORE) {
-    Is[0] = I1;
-    Is[N] = I2;
+    Is[0] = B_prev;
+    Is[N] = B_prev;
   }
   for (int l = 1; l < L; ++l) {
     const Kappa kap = kappa(l);
     const double B = planck(l);
-    double tau, rtau;
+    double d1, d2, rtau;
     if (STORE) {
       float4 tk;
-      emission_layer_tau_df<EXT, true>(lv, l, kap, kap_prev, tau, rtau, csh, csd, &tk);
+      emission_layer_tau_df<EXT, true>(lv, l, kap, kap_prev, d1, d2, rtau, csh, csd, &tk);
       layer_store[((size_t)b * L + l) * N + k] = tk;
     } else {
-      emission_layer_tau_df<EXT>(lv, l, kap, kap_prev, tau, rtau, csh, csd);
+      emission_layer_tau_df<EXT>(lv, l, kap, kap_prev, d1, d2, rtau, csh, csd);
     }
-    sc_layer_fast(tau, rtau, B, B_prev, I1, I2, tab2048);
+    sc_layer_j(d1, d2, rtau, B, B_prev, J1, J2, tab2048);
     if (STORE) {
-      Is[(size_t)l * 2 * N] = I1;
-      Is[(size_t)l * 2 * N + N] = I2;
+      Is[(size_t)l * 2 * N] = J1 + B;
+      Is[(size_t)l * 2 * N + N] = J2 + B;
     }
     kap_prev = kap;
     B_prev = B;
   }
+  const double I1 = J1 + B_prev, I2 = J2 + B_prev;
   const double flux = 2.0 * kPi * (I1 * kMu[0] * 0.5 + I2 * kMu[1] * 0.5) * 1e-3;
   spectrum[(size_t)b * N + k] = flux * __ldg(&ev[b].scaling);
 }

@@ -156,9 +156,16 @@ __device__ __forceinline__ double cloud_shape(const DeviceModel& dm, const EvalI
 // double-float split csd).
 // OUT (gradient pass): tk receives the layer optical depth as a double-float (FP64 values
 // clamped to 1e37) and (k_l + k_{l-1}) / 2, as the adjoint uses them.
+// The per-angle optical depths delta_i = tau / mu_i as FP64 values of double-float products
+// (one conversion add each) and 1 / tau.
+constexpr float kInvMuF[2][2] = {{(float)(1.0 / 0.211324865405187),
+                                  (float)(1.0 / 0.211324865405187 - (double)(float)(1.0 / 0.211324865405187))},
+                                 {(float)(1.0 / 0.788675134594813),
+                                  (float)(1.0 / 0.788675134594813 - (double)(float)(1.0 / 0.788675134594813))}};
+
 template <bool SHAPE = false, bool OUT = false>
 __device__ __forceinline__ void emission_layer_tau_df(const LevelInfo* __restrict__ lv, int l, const Kappa& kap,
-                                                      const Kappa& kap_prev, double& tau, double& rtau,
+                                                      const Kappa& kap_prev, double& d1, double& d2, double& rtau,
                                                       double csh = 1.0, df2 csd = df2{1.0f, 0.0f},
                                                       float4* tk = nullptr) {
   const float4 g = __ldg(reinterpret_cast<const float4*>(&lv[l - 1].dzh_hi));  // dzh, cloud
@@ -167,7 +174,8 @@ __device__ __forceinline__ void emission_layer_tau_df(const LevelInfo* __restric
   // both wide parts zero (+-0), tested on the bits to stay off the FP64 pipe
   const bool narrow = ((__double_as_longlong(kap.wide) | __double_as_longlong(kap_prev.wide)) << 1) == 0;
   if (narrow && t.hi > 1e-30f && t.hi < 1e30f) {
-    tau = df_to_double(t);
+    d1 = df_to_double(df_mul(t, df2{kInvMuF[0][0], kInvMuF[0][1]}));
+    d2 = df_to_double(df_mul(t, df2{kInvMuF[1][0], kInvMuF[1][1]}));
     rtau = df_to_double(df_div(df_make(1.0f), t));
     if (OUT) {
       const df2 ksh = df_mul_f(df_add(kap.v, kap_prev.v), 0.5f);
@@ -175,7 +183,10 @@ __device__ __forceinline__ void emission_layer_tau_df(const LevelInfo* __restric
     }
   } else {
     const double ks = (df_to_double(kap.v) + kap.wide) + (df_to_double(kap_prev.v) + kap_prev.wide);
-    tau = __ldg(&lv[l - 1].dz) * ks / 2. + (SHAPE ? __ldg(&lv[l - 1].cloud) * csh : __ldg(&lv[l - 1].cloud));
+    const double tau =
+        __ldg(&lv[l - 1].dz) * ks / 2. + (SHAPE ? __ldg(&lv[l - 1].cloud) * csh : __ldg(&lv[l - 1].cloud));
+    d1 = tau * kInvMu[0];
+    d2 = tau * kInvMu[1];
     rtau = 1.0 / tau;
     if (OUT) {
       const df2 td = df_from_double(fmin(tau, 1e37)), kd = df_from_double(fmin(0.5 * ks, 1e37));
@@ -205,23 +216,32 @@ __device__ __forceinline__ void sc_layer(double tau, double B, double B_prev, do
   }
 }
 
-// The same layer in fewer FP64 operations, used by the default kernel:
-// I a + (1+q) B + (-a-q) B' == a (I - B') + B + q (B - B'), with q = (a-1)/delta and
-// 1/tau supplied by the caller (computed in double-float); q (B - B') is formed as
-// (a - 1) (mu ((B - B') / tau)). The exponential
-// (exp_tang2048; tab2048 = 2^(j/2048)) and the recurrence stay FP64.
-__device__ __forceinline__ void sc_layer_fast(double tau, double rtau, double B, double B_prev, double& I1,
-                                              double& I2, const double* tab2048) {
-  if ((__double_as_longlong(tau) << 1) == 0) return;  // tau == 0 (bit test)
-  // q dB = (a - 1) mu (dB / tau): dB / tau shared by both angles
+// The same layer in fewer FP64 operations, used by the default kernel, carried as
+// J = I - B (the intensity less the source function of the level just passed):
+// I = a (I' - B') + B + q (B - B'), q = (a - 1) / delta, becomes J = a J' + (a - 1) w with
+// w = mu u, u = (B - B') / tau (shared by the angles): four FP64 operations per angle.
+// (a - 1) w is rounded as the reference rounds q (B - B'); in particular a layer thin
+// enough that a rounds to 1 leaves J unchanged, as the reference leaves I - B.
+// delta_i = tau / mu_i and 1 / tau come from the caller (double-float products); the
+// exponential (exp_tang2048_f, table index chosen in FP32; tab2048 = 2^(j/2048)) and
+// the recurrence are FP64. An exactly transparent layer (tau == 0) is skipped as in the
+// reference: I stays, so J moves by B' - B.
+__device__ __forceinline__ void sc_layer_j(double d1, double d2, double rtau, double B, double B_prev, double& J1,
+                                           double& J2, const double* tab2048) {
+  if ((__double_as_longlong(d1) << 1) == 0) {  // tau == 0 (bit test)
+    const double s = B_prev - B;
+    J1 += s;
+    J2 += s;
+    return;
+  }
   const double u = (B - B_prev) * rtau;
 #pragma unroll
   for (int i = 0; i < 2; ++i) {
-    const double d = tau * kInvMu[i];
-    const double a = __double_as_longlong(d) > kBits700 ? 0.0 : exp_tang2048(-d, tab2048);
-    double& I = i == 0 ? I1 : I2;
-    I = fma(a, I - B_prev, B);
-    I = fma(a - 1.0, kMu[i] * u, I);
+    const double d = i == 0 ? d1 : d2;
+    const double a = __double_as_longlong(d) > kBits700 ? 0.0 : exp_tang2048_f(-d, -d2f_trunc(d), tab2048);
+    const double w = kMu[i] * u;
+    double& J = i == 0 ? J1 : J2;
+    J = fma(a, J, (a - 1.0) * w);
   }
 }
 

@@ -16,6 +16,7 @@ int main() {
   std::mt19937_64 g(20261203);
   std::uniform_real_distribution<double> U(0.0, 1.0);
   double e_exp2 = 0, e_tang = 0, e_tang2048 = 0, e_pow10 = 0, e_planck = 0, e_expneg = 0, ulp2048 = 0;
+  double e_tang2048f = 0, ulp2048f = 0;
   for (int i = 0; i < 2000000; ++i) {
     // double-float 2^y over the exponent range of the opacity terms
     const double y = -140.0 + 180.0 * U(g);
@@ -33,6 +34,11 @@ int main() {
     e_tang2048 = std::fmax(e_tang2048, (double)fabsl(b / rx - 1));
     const double rd = (double)rx;
     ulp2048 = std::fmax(ulp2048, (double)fabsl(((long double)b - rx) / (std::nextafter(rd, 1e308) - rd)));
+    // the same with the table index from a float estimate of x (the kernels' d2f_trunc of -x)
+    const double bf = exp_tang2048_f(x, -d2f_trunc(-x), kExp2TabD2048);
+    e_tang2048f = std::fmax(e_tang2048f, (double)fabsl(bf / rx - 1));
+    if (x >= -40.0)  // a >= 4e-18: the range where a's last bits can reach the intensities
+      ulp2048f = std::fmax(ulp2048f, (double)fabsl(((long double)bf - rx) / (std::nextafter(rd, 1e308) - rd)));
     // double-float exp(-d) of the adjoint
     const double d = 60.0 * U(g);
     const df2 en = df_exp_neg(df_from_double(d), kExp2TabHi, kExp2TabLo);
@@ -75,8 +81,18 @@ int main() {
     if (!same(i2d_bits(k), (double)k)) ++conv_mismatch;
   for (int k : {2147483647, -2147483647, 1 << 30, -(1 << 30)})
     if (!same(i2d_bits(k), (double)k)) ++conv_mismatch;
+  // d2f_trunc: below the float range 0, else within 2^-23 of the value
+  double e_trunc = 0;
+  for (int i = 0; i < 1000000; ++i) {
+    const double d = std::ldexp(U(g), (int)(277.0 * U(g)) - 150);  // up to 2^127
+    const float f = d2f_trunc(d);
+    if (d < std::ldexp(1.0, -126)) e_trunc = std::fmax(e_trunc, f == 0.0f ? 0.0 : 1.0);
+    else e_trunc = std::fmax(e_trunc, std::fabs((double)f / d - 1));
+  }
   std::printf("df_exp2 %.3e\nexp_tang %.3e\nexp_tang2048 %.3e\nexp_tang2048_ulp %.3f\ndf_exp_neg %.3e\n"
-              "df_pow10 %.3e\nplanck_df %.3e\nconversion_mismatches %lld\n",
-              e_exp2, e_tang, e_tang2048, ulp2048, e_expneg, e_pow10, e_planck, conv_mismatch);
+              "df_pow10 %.3e\nplanck_df %.3e\nconversion_mismatches %lld\nexp_tang2048_f %.3e\n"
+              "exp_tang2048_f_ulp %.3f\nd2f_trunc %.3e\n",
+              e_exp2, e_tang, e_tang2048, ulp2048, e_expneg, e_pow10, e_planck, conv_mismatch, e_tang2048f,
+              ulp2048f, e_trunc);
   return 0;
 }

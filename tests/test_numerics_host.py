@@ -6,8 +6,11 @@ device code uses FMA); tests/numerics_harness.cpp measures each routine
 against long-double references over the argument ranges the kernels use:
 
 * exp_tang / exp_tang2048: Tang's table-driven FP64 exp (64- and 2048-entry
-  tables), the exp(-delta) of the short-characteristics recurrence and the
-  tangent-ray transmission;
+  tables; the FP64 reference forms of the recurrence's exponential);
+* exp_tang2048_f: the same with the table index chosen in FP32 from d2f_trunc,
+  the exp(-delta) of the short-characteristics recurrence (ulp bound over
+  delta <= 40, where a >= 4e-18; relative bound over delta <= 700);
+* d2f_trunc: float estimate of a double from its bits (2^-23);
 * df_exp2 / 10^x: double-float exponentials of the opacity assembly;
 * planck_df: the double-float Planck function;
 * df_exp_neg: the double-float exp(-delta) of the adjoint;
@@ -30,6 +33,9 @@ BOUNDS = {
     "exp_tang": 3.4e-16,        # ~1.5 ulp
     "exp_tang2048": 3.4e-16,
     "exp_tang2048_ulp": 1.5,
+    "exp_tang2048_f": 3.4e-16,
+    "exp_tang2048_f_ulp": 1.5,
+    "d2f_trunc": 1.2e-7,        # 2^-23
     "df_exp2": 5e-14,
     "df_pow10": 2e-12,          # |x| <= 40: 10^x from a 48-bit x log2(10)
     "df_exp_neg": 1e-12,        # d <= 60
