@@ -660,11 +660,12 @@ def main():
 
     # The binding roof is FP64 issue: FP64-pipe instructions per wavenumber and layer
     # counted from the kernel source (emission: the double-float -> double conversions of
-    # tau, 1/tau and B_nu, one FP64 add each (the float -> double steps run on the integer
-    # pipe); (B - B') / tau (2); per Gauss angle delta (1), exp_tang2048 (7), mu u (1), a - 1
-    # (1) and the update (3)), against the DFMA rate implied by a measured DGEMM.
+    # delta_1, delta_2, 1/tau and B_nu, one FP64 add each (the float -> double steps run on
+    # the integer pipe); (B - B') / tau (2); per Gauss angle exp_tang2048_f (6), mu u (1),
+    # a - 1 (1), (a - 1) w (1) and the update (1)), against the DFMA rate implied by a
+    # measured DGEMM.
     if kind == "emission":
-        ops_per_point_layer = 3 + 2 + 2 * (1 + 7 + 1 + 1 + 3)
+        ops_per_point_layer = 4 + 2 + 2 * (6 + 1 + 1 + 1 + 1)
         fp64_ops = B * (L - 1) * N * ops_per_point_layer
     else:
         ops_per_point_layer = None
