@@ -26,6 +26,8 @@
 #define BGB_FMA(a, b, c) std::fmaf((a), (b), (c))
 #define BGB_FDIV(a, b) ((float)((a) / (b)))
 #define BGB_RINTF(x) std::rintf(x)
+#define BGB_FMINF(a, b) std::fmin((a), (b))
+#define BGB_FMAXF(a, b) std::fmax((a), (b))
 #define BGB_DMA(a, b, c) std::fma((a), (b), (c))
 static inline float bgb_int_as_float(int i) { float f; std::memcpy(&f, &i, 4); return f; }
 static inline long long bgb_double_as_ll(double d) { long long i; std::memcpy(&i, &d, 8); return i; }
@@ -40,6 +42,8 @@ static inline int bgb_clz(unsigned x) { return __builtin_clz(x); }
 #define BGB_FMA(a, b, c) __fmaf_rn((a), (b), (c))
 #define BGB_FDIV(a, b) __fdiv_rn((a), (b))
 #define BGB_RINTF(x) rintf(x)
+#define BGB_FMINF(a, b) fminf((a), (b))
+#define BGB_FMAXF(a, b) fmaxf((a), (b))
 #define BGB_DMA(a, b, c) __fma_rn((a), (b), (c))
 #define bgb_int_as_float(i) __int_as_float(i)
 #define bgb_double_as_ll(d) __double_as_longlong(d)
@@ -154,29 +158,33 @@ BGB_HD df2 df_div(df2 a, df2 b) {
 BGB_HD df2 df_lerp(df2 a, df2 b, df2 w) { return df_add(a, df_mul(df_sub(b, a), w)); }
 
 // 2^y for a double-float y, returned as a double-float mantissa m (1/sqrt2 <= m < 2)
-// and an integer exponent: 2^y = m * 2^n. Relative error ~1e-14.
+// and an integer exponent: 2^y = m * 2^n. Relative error ~1e-14. y.hi is clamped to
+// [-16000, 16000] (the callers' 2^n is 0 or infinite well inside that; NaN propagates).
 // tab_hi / tab_lo: 2^(j/64), j = -32..32 (index j + 32).
+// k = round(64 y.hi) by the float shifter 1.5 * 2^23 (n = floor((k + 32) / 64) and j = k - 64 n
+// in [-32, 31]); r = y - k/64 exactly as a double-float (|r| <= 1/128 + |y.lo|), t = r ln2,
+// 2^r = 1 + t + t^2/2 + t^3 (1/6 + t/24 + t^2/120) with t^2 as an exact float product plus
+// its error and the cubic tail in float (|t| <= 5.5e-3: tail error below 1e-15 relative),
+// m = T_j (1 + s) as one double-float FMA.
 BGB_HD df2 df_exp2(df2 y, int& n, const float* tab_hi, const float* tab_lo) {
-  const float nf = BGB_RINTF(y.hi);
-  n = (int)nf;
-  const df2 f = fast_two_sum(BGB_FSUB(y.hi, nf), y.lo);        // |f| <= 1/2, y.hi - nf exact
-  const float jf = BGB_RINTF(BGB_FMUL(f.hi, 64.0f));
-  const int j = (int)jf;
-  const df2 r = fast_two_sum(BGB_FSUB(f.hi, BGB_FMUL(jf, 0.015625f)), f.lo);  // |r| <= 1/128
-  // t = r ln2; 2^r = 1 + t + t^2/2 + t^3/6 + t^4/24 + t^5/120 (+ |t|^6/720 < 3.5e-17)
+  const float yc = BGB_FMINF(BGB_FMAXF(y.hi, -16000.0f), 16000.0f);
+  const float yh = y.hi != y.hi ? y.hi : yc;
+  const float tf = BGB_FMA(yh, 64.0f, 12582912.0f);
+  const int k = (int)bgb_float_as_uint(tf) - 0x4B400000;
+  const float kf = BGB_FSUB(tf, 12582912.0f);
+  n = (k + 32) >> 6;  // arithmetic shift: floor
+  const int j = k - (n << 6);
+  const df2 r = two_sum(BGB_FMA(-kf, 0.015625f, yh), y.lo);  // yh - k/64 is exact
   const df2 t = df_mul(r, df2{kLn2Hi, kLn2Lo});
   const float th = t.hi;
-  const float tail = BGB_FMUL(BGB_FMUL(BGB_FMUL(th, th), th),
-                              BGB_FMA(th, BGB_FMA(th, 1.0f / 120.0f, 1.0f / 24.0f), 1.0f / 6.0f));
   const float sq = BGB_FMUL(th, th);
-  const float sq_err = BGB_FMA(th, th, -sq);
-  df2 half_t2 = fast_two_sum(BGB_FMUL(sq, 0.5f), BGB_FMUL(BGB_FMA(2.0f * th, t.lo, sq_err), 0.5f));
-  df2 s = df_add(half_t2, df_make(tail));
-  s = df_add(t, s);
-  const df2 p = fast_two_sum(1.0f, s.hi);
-  const df2 e = fast_two_sum(p.hi, BGB_FADD(p.lo, s.lo));
+  const float sq_lo = BGB_FMA(2.0f * th, t.lo, BGB_FMA(th, th, -sq));  // t^2 = sq + sq_lo
+  const float tail = BGB_FMUL(BGB_FMUL(sq, th),
+                              BGB_FMA(th, BGB_FMA(th, 1.0f / 120.0f, 1.0f / 24.0f), 1.0f / 6.0f));
+  const df2 s1 = two_sum(th, BGB_FMUL(sq, 0.5f));  // t.hi + t^2/2 (hi part), exact
+  const df2 s = fast_two_sum(s1.hi, BGB_FADD(BGB_FADD(s1.lo, t.lo), BGB_FMA(sq_lo, 0.5f, tail)));
   const df2 T = {tab_hi[j + 32], tab_lo[j + 32]};
-  return df_mul(T, e);
+  return df_fma(T, s, T);
 }
 
 // 2^(float exponent) as a float, for n in [-126, 127]; 0 below.

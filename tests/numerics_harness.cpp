@@ -81,6 +81,19 @@ int main() {
     if (!same(i2d_bits(k), (double)k)) ++conv_mismatch;
   for (int k : {2147483647, -2147483647, 1 << 30, -(1 << 30)})
     if (!same(i2d_bits(k), (double)k)) ++conv_mismatch;
+  // df_exp2 outside the clamp: 2^y underflows / overflows in the callers, NaN propagates
+  long long edge_bad = 0;
+  for (float yv : {-1e30f, -1e6f, -20000.0f, 20000.0f, 1e6f, 1e30f, -INFINITY, INFINITY}) {
+    int n;
+    const df2 m = df_exp2(df2{yv, 0.0f}, n, kExp2TabHi, kExp2TabLo);
+    const double v = ((double)m.hi + m.lo) * std::ldexp(1.0, std::max(-1100, std::min(1100, n)));
+    if (!std::isfinite(m.hi) || (yv < 0 && v != 0.0) || (yv > 0 && !std::isinf(v))) ++edge_bad;
+  }
+  {
+    int n;
+    const df2 m = df_exp2(df2{NAN, 0.0f}, n, kExp2TabHi, kExp2TabLo);
+    if (!std::isnan(m.hi)) ++edge_bad;
+  }
   // d2f_trunc: below the float range 0, else within 2^-23 of the value
   double e_trunc = 0;
   for (int i = 0; i < 1000000; ++i) {
@@ -91,8 +104,8 @@ int main() {
   }
   std::printf("df_exp2 %.3e\nexp_tang %.3e\nexp_tang2048 %.3e\nexp_tang2048_ulp %.3f\ndf_exp_neg %.3e\n"
               "df_pow10 %.3e\nplanck_df %.3e\nconversion_mismatches %lld\nexp_tang2048_f %.3e\n"
-              "exp_tang2048_f_ulp %.3f\nd2f_trunc %.3e\n",
+              "exp_tang2048_f_ulp %.3f\nd2f_trunc %.3e\ndf_exp2_edge_failures %lld\n",
               e_exp2, e_tang, e_tang2048, ulp2048, e_expneg, e_pow10, e_planck, conv_mismatch, e_tang2048f,
-              ulp2048f, e_trunc);
+              ulp2048f, e_trunc, edge_bad);
   return 0;
 }

@@ -36,6 +36,7 @@ BOUNDS = {
     "exp_tang2048_f": 3.4e-16,
     "exp_tang2048_f_ulp": 1.5,
     "d2f_trunc": 1.2e-7,        # 2^-23
+    "df_exp2_edge_failures": 0,  # |y| beyond the clamp: 0 / infinite in the callers; NaN propagates
     "df_exp2": 5e-14,
     "df_pow10": 2e-12,          # |x| <= 40: 10^x from a 48-bit x log2(10)
     "df_exp_neg": 1e-12,        # d <= 60
