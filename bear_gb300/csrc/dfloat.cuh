@@ -28,6 +28,7 @@
 #define BGB_RINTF(x) std::rintf(x)
 #define BGB_FMINF(a, b) std::fmin((a), (b))
 #define BGB_FMAXF(a, b) std::fmax((a), (b))
+#define BGB_RCP_APPROX(x) (1.0f / (x))
 #define BGB_DMA(a, b, c) std::fma((a), (b), (c))
 static inline float bgb_int_as_float(int i) { float f; std::memcpy(&f, &i, 4); return f; }
 static inline long long bgb_double_as_ll(double d) { long long i; std::memcpy(&i, &d, 8); return i; }
@@ -44,6 +45,13 @@ static inline int bgb_clz(unsigned x) { return __builtin_clz(x); }
 #define BGB_RINTF(x) rintf(x)
 #define BGB_FMINF(a, b) fminf((a), (b))
 #define BGB_FMAXF(a, b) fmaxf((a), (b))
+#define BGB_RCP_APPROX(x) bgb_rcp_approx(x)
+// float reciprocal, relative error within 2^-23 (PTX rcp.approx; normal inputs)
+__device__ __forceinline__ float bgb_rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
 #define BGB_DMA(a, b, c) __fma_rn((a), (b), (c))
 #define bgb_int_as_float(i) __int_as_float(i)
 #define bgb_double_as_ll(d) __double_as_longlong(d)
@@ -142,6 +150,15 @@ BGB_HD df2 df_fma(df2 a, df2 b, df2 c) {
   e = BGB_FMA(a.lo, b.hi, e);
   const df2 s = two_sum(c.hi, p);
   return fast_two_sum(s.hi, BGB_FADD(s.lo, BGB_FADD(e, c.lo)));
+}
+
+// 1 / b for a double-float b whose hi part is a normal float: an approximate float
+// reciprocal r0 (relative error within 2^-23) refined by one Newton step with its square
+// term, r = r0 (1 + e + e^2), e = 1 - b r0 formed with FMA; relative error ~2^-45.
+BGB_HD df2 df_recip(df2 b) {
+  const float r0 = BGB_RCP_APPROX(b.hi);
+  const float e = BGB_FMA(-b.lo, r0, BGB_FMA(-b.hi, r0, 1.0f));
+  return fast_two_sum(r0, BGB_FMUL(r0, BGB_FMA(e, e, e)));
 }
 
 // a / b with three correction steps (quotient digits q1 + q2 + q3).

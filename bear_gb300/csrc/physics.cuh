@@ -25,7 +25,7 @@ BGB_HD double planck_df(df2 c1, df2 c2l, df2 invT, const float* tab_hi, const fl
   if (n < -60) return df_to_double(df_mul(c1, m)) * pow2d(n);  // 1 - u == 1 at this precision
   const df2 u = df_ldexp(m, n);
   const df2 d = df_sub(df_make(1.0f), u);
-  return df_to_double(df_div(df_mul(c1, u), d));
+  return df_to_double(df_mul(df_mul(c1, u), df_recip(d)));
 }
 
 // The same Planck function returned as a double-float (values below the float

@@ -176,7 +176,7 @@ __device__ __forceinline__ void emission_layer_tau_df(const LevelInfo* __restric
   if (narrow && t.hi > 1e-30f && t.hi < 1e30f) {
     d1 = df_to_double(df_mul(t, df2{kInvMuF[0][0], kInvMuF[0][1]}));
     d2 = df_to_double(df_mul(t, df2{kInvMuF[1][0], kInvMuF[1][1]}));
-    rtau = df_to_double(df_div(df_make(1.0f), t));
+    rtau = df_to_double(df_recip(t));
     if (OUT) {
       const df2 ksh = df_mul_f(df_add(kap.v, kap_prev.v), 0.5f);
       *tk = make_float4(t.hi, t.lo, ksh.hi, ksh.lo);

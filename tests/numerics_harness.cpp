@@ -94,6 +94,17 @@ int main() {
     const df2 m = df_exp2(df2{NAN, 0.0f}, n, kExp2TabHi, kExp2TabLo);
     if (!std::isnan(m.hi)) ++edge_bad;
   }
+  // df_recip over the ranges of 1/tau and 1/(1 - u) (host: correctly rounded float
+  // reciprocal; the device's approximate one is within 2^-23, which the Newton step with
+  // its square term absorbs)
+  double e_recip = 0;
+  for (int i = 0; i < 1000000; ++i) {
+    const double b = std::ldexp(1.0 + U(g), (int)(180.0 * U(g)) - 90);
+    const df2 bd = df_from_double(b);
+    const df2 r = df_recip(bd);
+    const long double ref = 1.0L / ((long double)bd.hi + bd.lo);
+    e_recip = std::fmax(e_recip, (double)fabsl(((long double)r.hi + r.lo) / ref - 1));
+  }
   // d2f_trunc: below the float range 0, else within 2^-23 of the value
   double e_trunc = 0;
   for (int i = 0; i < 1000000; ++i) {
@@ -104,8 +115,8 @@ int main() {
   }
   std::printf("df_exp2 %.3e\nexp_tang %.3e\nexp_tang2048 %.3e\nexp_tang2048_ulp %.3f\ndf_exp_neg %.3e\n"
               "df_pow10 %.3e\nplanck_df %.3e\nconversion_mismatches %lld\nexp_tang2048_f %.3e\n"
-              "exp_tang2048_f_ulp %.3f\nd2f_trunc %.3e\ndf_exp2_edge_failures %lld\n",
+              "exp_tang2048_f_ulp %.3f\nd2f_trunc %.3e\ndf_exp2_edge_failures %lld\ndf_recip %.3e\n",
               e_exp2, e_tang, e_tang2048, ulp2048, e_expneg, e_pow10, e_planck, conv_mismatch, e_tang2048f,
-              ulp2048f, e_trunc, edge_bad);
+              ulp2048f, e_trunc, edge_bad, e_recip);
   return 0;
 }

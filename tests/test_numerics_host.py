@@ -13,6 +13,7 @@ against long-double references over the argument ranges the kernels use:
 * d2f_trunc: float estimate of a double from its bits (2^-23);
 * df_exp2 / 10^x: double-float exponentials of the opacity assembly;
 * planck_df: the double-float Planck function;
+* df_recip: double-float reciprocal by one Newton step (1/tau, 1/(1 - u) of Planck);
 * df_exp_neg: the double-float exp(-delta) of the adjoint;
 * f2d_bits / i2d_bits: float and int to double built with integer operations
   (bit-identical to the conversions, checked on every exponent, zeros and subnormals).
@@ -36,6 +37,7 @@ BOUNDS = {
     "exp_tang2048_f": 3.4e-16,
     "exp_tang2048_f_ulp": 1.5,
     "d2f_trunc": 1.2e-7,        # 2^-23
+    "df_recip": 3e-14,          # one Newton step from a float reciprocal (~2^-45)
     "df_exp2_edge_failures": 0,  # |y| beyond the clamp: 0 / infinite in the callers; NaN propagates
     "df_exp2": 5e-14,
     "df_pow10": 2e-12,          # |x| <= 40: 10^x from a 48-bit x log2(10)
