@@ -21,11 +21,11 @@
 //                               cut-off indices staged in shared memory: d log L / d c_j =
 //                               sum_t g_tau_t G[t][j], d log L / d z_j (geometry and effective
 //                               height) and d log L / dR
-//   tr_adjoint_pass2b           per wavenumber, levels across warps: opacities recomputed for the
-//                               per-level sinks (log number densities of the table and Rayleigh
-//                               species, temperature, altitude, cloud extinction), warp
-//                               reduce-scatter, per-block partial sums
-//   tr_atmosphere_adjoint_kernel per evaluation: partial sums in a fixed order, forward-mode
+//   tr_adjoint_pass2b           per (evaluation, level), threads striding the wavenumbers: the
+//                               level sinks (log number densities of the table and Rayleigh
+//                               species, temperature, altitude, cloud extinction) from the stored
+//                               or recomputed opacity terms, one block reduction per level
+//   tr_atmosphere_adjoint_kernel per evaluation: the level sinks, forward-mode
 //                               tangents of the level physics (temperature, chemistry,
 //                               hydrostatic altitudes as prefix sums, cloud extinction),
 //                               planet and star radii
@@ -42,8 +42,6 @@
 
 namespace bgb {
 
-constexpr int kTrVPB = 32;  // wavenumbers per block of the transmission adjoint kernels
-constexpr int kTrTPN = 4;   // threads per wavenumber
 
 // d log L / d depth_k normalised (the seed): sum_r W_rk gS_r times the evaluation's normaliser
 __device__ __forceinline__ double tr_seed(const DeviceModel& dm, const double* __restrict__ gS,
@@ -242,132 +240,111 @@ __global__ void __launch_bounds__(128) tr_adjoint_pass2a(DeviceModel dm, TrArgs 
 }
 
 // ------------------------------------------------------------------ pass 2b
-// Block: 32 wavenumbers (lanes) x 4 warps; warp w takes levels w, w+4, ...
-// Dynamic shared memory: per-species terms float2 [S][128], double [S][128], then the
-// evaluation's Rayleigh number densities float2 [L][R].
-// partial[b][l][v][tile]: v = 0..S-1 d log L / d ln n_s (table species),
-// S..S+R-1 d log L / d ln n_r (Rayleigh species), S+R temperature, S+R+1 z_l,
-// S+R+2 cloud extinction of level l (all times the evaluation's seed normaliser).
+// Level sinks: one block per (evaluation, level). The kTrSinkThreads threads stride the
+// wavenumbers and accumulate, as double-floats in registers, v = 0..S-1 d log L / d ln n_s
+// (table species), S..S+R-1 d log L / d ln n_r (Rayleigh species), S+R temperature,
+// S+R+1 z_l and S+R+2 the cloud extinction of level l; one block reduction in a fixed order
+// (warp reduce-scatter, then the warps' sums in warp order) writes partial[b][l][v] (times
+// the evaluation's seed normaliser in the parameter pass). The opacity terms come from the
+// forward pass's stores (a.ts, a.dk) where present, else they are recomputed from the level
+// table in the same order (per-thread shared slots). Dynamic shared memory: float2 [S][T],
+// double [S][T] (T = kTrSinkThreads), then the level's Rayleigh number densities float2 [R].
+constexpr int kTrSinkThreads = 128;
+
 template <int VP>
-__global__ void __launch_bounds__(kTrTPN * kTrVPB, VP == 32 ? 4 : 6) tr_adjoint_pass2b(DeviceModel dm, TrArgs a) {
-  constexpr int G = 32 / VP;
+__global__ void __launch_bounds__(kTrSinkThreads, VP == 32 ? 4 : 6) tr_adjoint_pass2b(DeviceModel dm, TrArgs a) {
+  constexpr int G = 32 / VP, NW = kTrSinkThreads / 32;
   __shared__ ExpTables et;
+  __shared__ float2 red[NW][VP];
   extern __shared__ __align__(16) unsigned char tr2_smem[];
   const int S = dm.S, R = dm.R, L = dm.L;
-  float2* tdf = reinterpret_cast<float2*>(tr2_smem);
-  double* twd = reinterpret_cast<double*>(tr2_smem + (size_t)S * blockDim.x * sizeof(float2));
-  float2* rn_s = reinterpret_cast<float2*>(twd + (size_t)S * blockDim.x);  // [L][R] Rayleigh n as double-floats
+  const int b = blockIdx.x, l = blockIdx.y, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  float2* td = reinterpret_cast<float2*>(tr2_smem) + tid;                                  // [S][T]
+  double* tw = reinterpret_cast<double*>(tr2_smem + (size_t)S * kTrSinkThreads * sizeof(float2)) + tid;
+  float2* rn_s = reinterpret_cast<float2*>(tr2_smem + (size_t)S * kTrSinkThreads * (sizeof(float2) + sizeof(double)));
   load_exp_tables(et);
-  for (int idx = threadIdx.x; idx < L * R; idx += blockDim.x) {
-    const df2 d = df_from_double(__ldg(&a.ray_n[(size_t)blockIdx.x * L * R + idx]));
-    rn_s[idx] = make_float2(d.hi, d.lo);
+  for (int r = tid; r < R; r += kTrSinkThreads) {
+    const df2 d = df_from_double(__ldg(&a.ray_n[((size_t)b * L + l) * R + r]));
+    rn_s[r] = make_float2(d.hi, d.lo);
   }
   __syncthreads();
-  const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int kk = blockIdx.y * 32 + lane;
-  const bool active = kk < dm.N;
-  const int k = active ? kk : dm.N - 1;  // idle lanes repeat the last wavenumber with zero sinks
   const size_t N = dm.N;
-  const size_t col = (size_t)b * L * N + k;
-  const LevelSpeciesDF* sf = a.lsdf + (size_t)b * L * S;
-  const float2* dw = a.dwT + (size_t)b * L * S;
-  float2* td = tdf + tid;
-  double* tw = twd + tid;
-  for (int l = warp; l < L; l += blockDim.x / 32) {
+  const LevelSpeciesDF* sfl = a.lsdf + ((size_t)b * L + l) * S;
+  const float2* dwl = a.dwT + ((size_t)b * L + l) * S;
+  const size_t row = ((size_t)b * L + l) * N;  // [b][l][k] of k = 0
+  const float2* tsl = a.ts + ((size_t)b * L + l) * S * N;  // [s][N] (stored mode)
+  df2 v[VP];
+#pragma unroll
+  for (int q = 0; q < VP; ++q) v[q] = df2{0.0f, 0.0f};
+  for (int k = tid; k < (int)N; k += kTrSinkThreads) {
     // d log L / d chi_l (chi_l enters c_l and c_{l-1})
     df2 gx = {0.0f, 0.0f};
-    if (active) {
-      if (l <= L - 2) {
-        const float2 v = a.gc[col + (size_t)l * N];
-        gx = df2{v.x, v.y};
-      }
-      if (l >= 1) {
-        const float2 v = a.gc[col + (size_t)(l - 1) * N];
-        gx = df_add(gx, df2{v.x, v.y});
-      }
+    if (l <= L - 2) {
+      const float2 c0 = a.gc[row + k];
+      gx = df2{c0.x, c0.y};
     }
-    df2 gzl = {0.0f, 0.0f};
-    if (active) {
-      const float2 v = a.gz[col + (size_t)l * N];
-      gzl = df2{v.x, v.y};
+    if (l >= 1) {
+      const float2 c1 = a.gc[row - N + k];
+      gx = df_add(gx, df2{c1.x, c1.y});
     }
-    // opacity terms and their temperature slope (level-table values are log2 units): from the
-    // forward pass's stores where it kept them, else recomputed in the same order
+    const float2 gz = a.gz[row + k];
+    // opacity terms and their temperature slope (level-table values are log2 units)
     df2 dk = {0.0f, 0.0f};
     double dkw = 0.0;
     bool wide = false;
-    const float2 dks = a.ts ? a.dk[col + (size_t)l * N] : make_float2(__int_as_float(0x7fc00000), 0.0f);
+    const float2 dks = a.ts ? a.dk[row + k] : make_float2(__int_as_float(0x7fc00000), 0.0f);
     const bool stored = !isnan(dks.x);
-    const float2* tsl = a.ts + ((size_t)b * L + l) * S * N + k;  // [s][N] (stored mode)
     if (stored) {
       dk = df2{dks.x, dks.y};
     } else {
-      const float2* dwl = dw + (size_t)l * S;
-      level_kappa_df_cb<2>(dm.ltab, N, sf + (size_t)l * S, S, k, et,
-                           [&](int s, df2 t, double t_w, bool is_wide, df2 lo, df2 hi) {
-                             const float2 d = __ldg(dwl + s);
-                             td[(size_t)s * blockDim.x] = make_float2(t.hi, t.lo);
-                             tw[(size_t)s * blockDim.x] = t_w;
-                             if (d.x != 0.0f) {
-                               const df2 slope = df_mul(df_sub(hi, lo), df2{d.x, d.y});
-                               if (is_wide) dkw += t_w * df_to_double(slope);
-                               else dk = df_add(dk, df_mul(t, slope));
-                             }
-                             wide = wide || is_wide;
-                           });
+      level_kappa_df_cb<2>(dm.ltab, N, sfl, S, k, et, [&](int s, df2 t, double t_w, bool is_wide, df2 lo, df2 hi) {
+        const float2 d = __ldg(dwl + s);
+        td[(size_t)s * kTrSinkThreads] = make_float2(t.hi, t.lo);
+        tw[(size_t)s * kTrSinkThreads] = t_w;
+        if (d.x != 0.0f) {
+          const df2 slope = df_mul(df_sub(hi, lo), df2{d.x, d.y});
+          if (is_wide) dkw += t_w * df_to_double(slope);
+          else dk = df_add(dk, df_mul(t, slope));
+        }
+        wide = wide || is_wide;
+      });
     }
     df2 gT = df_mul(gx, df_mul(dk, df2{kLn2Hi, kLn2Lo}));
     if (wide) gT = df_add(gT, df_from_double(df_to_double(gx) * dkw * 0.693147180559945309));
-    const float2* rn = rn_s + (size_t)l * R;
-    df2 v[VP];
 #pragma unroll
     for (int q = 0; q < VP; ++q) {
       df2 x = {0.0f, 0.0f};
       if (q < S) {
-        const float2 t = stored ? __ldg(tsl + (size_t)q * N) : td[(size_t)q * blockDim.x];
+        const float2 t = stored ? __ldg(tsl + (size_t)q * N + k) : td[(size_t)q * kTrSinkThreads];
         x = df_mul(gx, df2{t.x, t.y});
-        if (wide) x = df_add(x, df_from_double(df_to_double(gx) * tw[(size_t)q * blockDim.x]));
+        if (wide) x = df_add(x, df_from_double(df_to_double(gx) * tw[(size_t)q * kTrSinkThreads]));
       } else if (q < S + R) {
         const float2 sr = __ldg(&dm.rayleigh_df[(size_t)(q - S) * N + k]);
-        const float2 nr = rn[q - S];
+        const float2 nr = rn_s[q - S];
         x = df_mul(gx, df_mul(df2{sr.x, sr.y}, df2{nr.x, nr.y}));
       } else if (q == S + R) {
         x = gT;
       } else if (q == S + R + 1) {
-        x = gzl;
+        x = df2{gz.x, gz.y};
       } else if (q == S + R + 2) {
         x = gx;
       }
-      v[q] = x;
+      v[q] = df_add(v[q], x);
     }
-    const df2 r = warp_reduce_scatter<VP>(v, lane);
-    const int idx = lane / G;
-    if (lane % G == 0 && idx < a.V)
-      a.partial[(((size_t)b * L + l) * a.V + idx) * gridDim.y + blockIdx.y] = df_to_double(r);
+  }
+  const df2 r = warp_reduce_scatter<VP>(v, lane);
+  if (lane % G == 0) red[warp][lane / G] = make_float2(r.hi, r.lo);
+  __syncthreads();
+  if (tid < a.V) {
+    df2 sum = {red[0][tid].x, red[0][tid].y};
+#pragma unroll
+    for (int w = 1; w < NW; ++w) sum = df_add(sum, df2{red[w][tid].x, red[w][tid].y});
+    a.partial[((size_t)b * L + l) * a.V + tid] = df_to_double(sum);
   }
 }
 
-// ------------------------------------------------------------------ partial-sum reduction
-// One warp per (evaluation, level, sink) row: the row's per-tile partial sums added in a
-// fixed order (lane-strided, then a warp tree), the total written over the row's first
-// entry. Grid: evaluations x row blocks of kReduceWarps rows.
-constexpr int kReduceWarps = 8;
-
-__global__ void __launch_bounds__(kReduceWarps * 32) tr_partial_reduce_kernel(double* __restrict__ partial, int rows,
-                                                                              int tiles) {
-  const int lane = threadIdx.x & 31;
-  const int row = blockIdx.y * kReduceWarps + (threadIdx.x >> 5);
-  if (row >= rows) return;
-  double* p = partial + ((size_t)blockIdx.x * rows + row) * tiles;
-  double s = 0.0;
-  for (int q = lane; q < tiles; q += 32) s += p[q];
-  s = warp_sum_d(s);
-  if (lane == 0) p[0] = s;
-}
-
 // ------------------------------------------------------------------ parameter tangents
-// One block per evaluation. sg[L][V] = the partial sums reduced over the tiles (by
-// tr_partial_reduce_kernel, first entry of each row); then
+// One block per evaluation. sg[L][V] = the level sinks of pass 2b (partial[b][l][v]); then
 // thread th < P forms d log L / d param_th = sum over levels of the sinks times the
 // tangents of ln n (table and Rayleigh species), T, z_l and the cloud extinction
 // chi_cloud,l = tau_layer(l-1) / (z_l - z_{l-1}) (CloudModel::convertOpticalDepth
@@ -493,7 +470,7 @@ size_t transmission_grad_bytes_per_eval(const Model& m, int V, bool store) {
   const size_t L = m.L, N = m.N;
   const size_t tiles = (N + 31) / 32;
   const size_t terms = store ? L * N * ((size_t)m.acfg.S + 1) * sizeof(float2) : 0;
-  return L * N * (6 * sizeof(float2) + sizeof(short)) + 3 * L * L * sizeof(float2) + L * (size_t)V * tiles * 8 +
+  return L * N * (6 * sizeof(float2) + sizeof(short)) + 3 * L * L * sizeof(float2) + L * (size_t)V * 8 +
          tiles * 8 + terms;
 }
 
@@ -515,7 +492,7 @@ void alloc_transmission_grad(Model& m, int chunk, int V, bool store) {
   BGB_CUDA(cudaMalloc(&g.tr_gc, n * sizeof(float2)));
   BGB_CUDA(cudaMalloc(&g.tr_gz, n * sizeof(float2)));
   BGB_CUDA(cudaMalloc(&g.tr_rp, B * tiles * sizeof(double)));
-  BGB_CUDA(cudaMalloc(&g.partial, B * L * (size_t)V * tiles * sizeof(double)));
+  BGB_CUDA(cudaMalloc(&g.partial, B * L * (size_t)V * sizeof(double)));
 }
 
 // The adjoint kernels of one chunk, after the storing forward pass and the likelihood adjoint.
@@ -536,11 +513,11 @@ void transmission_adjoint_chunk(Model& m, const double* params_chunk, int nb, cu
     BGB_CUDA(cudaFuncSetAttribute(tr_adjoint_pass2a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2a));
   tr_adjoint_pass2a<<<dim3(nb, tiles), 128, sm2a, st>>>(dm, a);
   BGB_CUDA(cudaGetLastError());
-  const size_t sm2 = (size_t)S * kTrTPN * kTrVPB * (sizeof(float2) + sizeof(double)) + (size_t)L * m.acfg.R * sizeof(float2);
+  const size_t sm2 = (size_t)S * kTrSinkThreads * (sizeof(float2) + sizeof(double)) + (size_t)m.acfg.R * sizeof(float2);
   const int VP = V <= 8 ? 8 : V <= 16 ? 16 : 32;
   auto go2 = [&](auto kernel) {
     if (sm2 > 48 * 1024) BGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));
-    kernel<<<dim3(nb, tiles), kTrTPN * kTrVPB, sm2, st>>>(dm, a);
+    kernel<<<dim3(nb, L), kTrSinkThreads, sm2, st>>>(dm, a);
   };
   if (VP == 8) go2(tr_adjoint_pass2b<8>);
   else if (VP == 16) go2(tr_adjoint_pass2b<16>);
@@ -549,10 +526,7 @@ void transmission_adjoint_chunk(Model& m, const double* params_chunk, int nb, cu
   const size_t sma = (size_t)L * V * sizeof(double);
   if (sma > 48 * 1024)
     BGB_CUDA(cudaFuncSetAttribute(tr_atmosphere_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sma));
-  tr_partial_reduce_kernel<<<dim3(nb, (L * V + kReduceWarps - 1) / kReduceWarps), kReduceWarps * 32, 0, st>>>(
-      g.partial, L * V, tiles);
-  BGB_CUDA(cudaGetLastError());
-  tr_atmosphere_adjoint_kernel<<<nb, 128, sma, st>>>(dm, params_chunk, P, w.lev, w.ev, g.partial, V, tiles, g.tr_rp,
+  tr_atmosphere_adjoint_kernel<<<nb, 128, sma, st>>>(dm, params_chunk, P, w.lev, w.ev, g.partial, V, 1, g.tr_rp,
                                                      tiles, g.seed, grad_chunk);
   BGB_CUDA(cudaGetLastError());
 }
