@@ -194,6 +194,17 @@ def fp64_peak_tflops(torch, device):
     return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
+def captured_traffic(workload, batch):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu capture of
+    this workload and batch (profiles/dram_traffic.json), or None."""
+    try:
+        with open(os.path.join(REPO, "profiles", "dram_traffic.json")) as f:
+            rec = json.load(f)[workload]
+    except (OSError, KeyError, ValueError):
+        return None
+    return rec["dram_bytes_per_launch"] if rec.get("batch") == batch else None
+
+
 def cpu_baseline(text, arrays, params, sample, threads, budget_s=12.0):
     """The FP64 C restatement of the reference path (a port) on the host cores:
     sequential evaluations of the batch's live points until ``budget_s`` seconds
@@ -703,7 +714,9 @@ def main():
             "roofline": {"bound": "hbm", "kernel": "emission_kernel" if kind == "emission" else
                          ("transmission_annuli_kernel" if args.workload in ANNULI else "transmission_kernel"),
                          "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                         "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": None,
+                         "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": captured_traffic(args.workload, B),
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch of the "
+                                           "tuned shape (profiles/dram_traffic.json; null where not captured)",
                          "peak_source": peak_kind, "kernel_ms": kern_ms, "algorithmic_bytes": alg_bytes,
                          "distinct_table_rows": rows},
             "stage_ms": {"atmosphere": stages[0], "radiative_transfer": stages[1],
