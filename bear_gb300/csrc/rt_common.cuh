@@ -51,6 +51,9 @@ __device__ __forceinline__ Kappa level_kappa_df_cb(const float2* __restrict__ lt
                                                    const LevelSpeciesDF* __restrict__ f, int S, int k,
                                                    const ExpTables& et, F&& term) {
   Kappa r = {{0.0f, 0.0f}, 0.0};
+  // the sum as an unnormalised pair: exact two-sum into hi, low parts added into lo,
+  // renormalised once at the end
+  float acc_hi = 0.0f, acc_lo = 0.0f;
   for (int s0 = 0; s0 < S; s0 += GRP) {
     int4 rw[GRP];
     float4 fb[GRP];
@@ -74,12 +77,15 @@ __device__ __forceinline__ Kappa level_kappa_df_cb(const float2* __restrict__ lt
         continue;
       }
       const df2 lo = {t0[g].x, t0[g].y}, hi = {t1[g].x, t1[g].y};
-      const df2 y = df_add(df_lerp(lo, hi, df2{fb[g].x, fb[g].y}), df2{fb[g].z, fb[g].w});
+      // lo + (hi - lo) wT + log2 n
+      const df2 y = df_fma(df_sub(hi, lo), df2{fb[g].x, fb[g].y}, df_add(lo, df2{fb[g].z, fb[g].w}));
       int n;
       const df2 m = df_exp2(y, n, et.hi, et.lo);
       if (n > -100 && n < 100) {
         const df2 t = df_ldexp(m, n);
-        r.v = df_add(r.v, t);
+        const df2 a = two_sum(acc_hi, t.hi);
+        acc_hi = a.hi;
+        acc_lo = BGB_FADD(acc_lo, BGB_FADD(a.lo, t.lo));
         term(s, t, 0.0, false, lo, hi);
       } else {
         const double w = df_to_double(m) * pow2d(n);
@@ -88,6 +94,7 @@ __device__ __forceinline__ Kappa level_kappa_df_cb(const float2* __restrict__ lt
       }
     }
   }
+  r.v = fast_two_sum(acc_hi, acc_lo);
   return r;
 }
 
