@@ -221,31 +221,10 @@ BGB_HD df2 df_ldexp(df2 a, int n) {
 // 2^n as a double for n in [-1022, 1023]; 0 below.
 BGB_HD double pow2d(int n) { return n < -1022 ? 0.0 : bgb_ll_as_double((long long)(n + 1023) << 52); }
 
-// exp(x) in FP64 by Tang's method: x = k ln2/64 + r (Cody-Waite with a two-part
-// ln2/64 and FMA), |r| <= ln2/128, degree-5 Taylor polynomial, table 2^(j/64)
-// (tab: 64 doubles, j = k mod 64), scaling by 2^(k div 64) in the exponent field.
-// Valid for x in [-700, 700]; about 1 ulp.
-BGB_HD double exp_tang(double x, const double* tab) {
-  const double shifter = 6755399441055744.0;  // 1.5 * 2^52: rounds to an integer
-  const double t = BGB_DMA(x, k64OverLn2, shifter);
-  const int k = (int)(bgb_double_as_ll(t) & 0xffffffff);
-  const double kd = i2d_bits(k);  // == t - shifter
-  double r = BGB_DMA(-kd, kLn2Over64Hi, x);
-  r = BGB_DMA(-kd, kLn2Over64Lo, r);
-  double p = BGB_DMA(r, 1.0 / 120.0, 1.0 / 24.0);
-  p = BGB_DMA(r, p, 1.0 / 6.0);
-  p = BGB_DMA(r, p, 0.5);
-  p = BGB_DMA(r * r, p, r);
-  const int j = k & 63;
-  const int m = k >> 6;  // arithmetic shift: floor(k / 64)
-  const double T = tab[j];
-  const double scaled = bgb_ll_as_double(bgb_double_as_ll(T) + ((long long)m << 52));
-  return BGB_DMA(scaled, p, scaled);
-}
-
-// The same method with a 2048-entry table (tab: 2^(j/2048), j = 0..2047): |r| <=
-// ln2/4096, so the degree-3 Taylor polynomial r + r^2/2 + r^3/6 suffices
-// (remainder r^4/24 < 3.5e-17): 8 FP64 operations instead of 10.
+// exp(x) in FP64 by Tang's method with a 2048-entry table (tab: 2^(j/2048), j = 0..2047):
+// x = k ln2/2048 + r (Cody-Waite with a two-part ln2/2048 and FMA), |r| <= ln2/4096, so the
+// degree-3 Taylor polynomial r + r^2/2 + r^3/6 suffices
+// (remainder r^4/24 < 3.5e-17): 8 FP64 operations.
 // Valid for x in [-700, 700]; about 1 ulp.
 BGB_HD double exp_tang2048(double x, const double* tab) {
   const double shifter = 6755399441055744.0;  // 1.5 * 2^52

@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(256) emission_kernel_fp64(DeviceModel dm, cons
     const double kap = kappa(l);
     const double B = c1 / (exp(c2 * __ldg(&lv[l].invT)) - 1.0);
     const double tau = __ldg(&lv[l - 1].dz) * (kap + kap_prev) / 2. + __ldg(&lv[l - 1].cloud) * csh;
-    sc_layer<false>(tau, B, B_prev, I1, I2, nullptr);
+    sc_layer(tau, B, B_prev, I1, I2);
     if (STORE) {
       Is[(size_t)l * 2 * N] = I1;
       Is[(size_t)l * 2 * N + N] = I2;

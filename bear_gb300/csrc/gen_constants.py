@@ -2,9 +2,8 @@
 computed to 60 digits with mpmath and split into (hi, lo) pairs.
 
   2^(j/64), j = -32..32  as float pairs   (double-float exp2, Tang's table method)
-  2^(j/64), j = 0..63    as doubles       (FP64 exp, Tang's table method)
   2^(j/2048), j = 0..2047 as doubles      (FP64 exp with a degree-3 polynomial)
-  ln 2, log2 10, log2 e  as float pairs; ln2/64 as a double pair (Cody-Waite)
+  ln 2, log2 10, log2 e  as float pairs; ln2/2048 as a double pair (Cody-Waite)
 
 Run: python bear_gb300/csrc/gen_constants.py > bear_gb300/csrc/dfconst.h
 """
@@ -43,16 +42,11 @@ print("namespace bgb {")
 print("// 2^(j/64) for j = -32..32 as (hi, lo) floats")
 print("BGB_CONST_MEM float kExp2TabHi[65] = {" + ", ".join(ff(split_f(mpmath.power(2, mpmath.mpf(j) / 64))[0]) for j in range(-32, 33)) + "};")
 print("BGB_CONST_MEM float kExp2TabLo[65] = {" + ", ".join(ff(split_f(mpmath.power(2, mpmath.mpf(j) / 64))[1]) for j in range(-32, 33)) + "};")
-print("// 2^(j/64) for j = 0..63 as doubles")
-print("BGB_CONST_MEM double kExp2TabD[64] = {" + ", ".join(float(mpmath.power(2, mpmath.mpf(j) / 64)).hex() for j in range(64)) + "};")
 print("// 2^(j/2048) for j = 0..2047 as doubles (global memory: blocks stage it in shared memory)")
 print("BGB_GLOBAL_MEM double kExp2TabD2048[2048] = {" + ", ".join(float(mpmath.power(2, mpmath.mpf(j) / 2048)).hex() for j in range(2048)) + "};")
 for name, val in (("Ln2", mpmath.log(2)), ("Log2_10", mpmath.log(10, 2)), ("Log2e", 1 / mpmath.log(2))):
     hi, lo = split_f(val)
     print(f"constexpr float k{name}Hi = {ff(hi)}, k{name}Lo = {ff(lo)};")
-hi, lo = split_d(mpmath.log(2) / 64)
-print(f"constexpr double kLn2Over64Hi = {hi.hex()}, kLn2Over64Lo = {lo.hex()};")
-print(f"constexpr double k64OverLn2 = {float(64 / mpmath.log(2)).hex()};")
 hi, lo = split_d(mpmath.log(2) / 2048)
 print(f"constexpr double kLn2Over2048Hi = {hi.hex()}, kLn2Over2048Lo = {lo.hex()};")
 print(f"constexpr double k2048OverLn2 = {float(2048 / mpmath.log(2)).hex()};")

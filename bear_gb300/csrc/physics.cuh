@@ -10,7 +10,6 @@ namespace bgb {
 struct ExpTables {
   float hi[65];
   float lo[65];
-  double d[64];
 };
 
 // Planck function B_nu(T) = 2 h c^2 nu^3 / (exp(h nu c / k T) - 1)

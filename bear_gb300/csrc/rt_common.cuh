@@ -23,7 +23,6 @@ __device__ __forceinline__ void load_exp_tables(ExpTables& t) {
     t.hi[i] = kExp2TabHi[i];
     t.lo[i] = kExp2TabLo[i];
   }
-  for (int i = threadIdx.x; i < 64; i += blockDim.x) t.d[i] = kExp2TabD[i];
 }
 
 // Level opacity as a double-float plus an FP64 part for terms outside the float
@@ -205,17 +204,14 @@ __device__ __forceinline__ void emission_layer_tau_df(const LevelInfo* __restric
 // One layer of the two-angle short-characteristics recurrence
 // (ShortCharacteristics::calcSpectrum src/radiative_transfer/short_characteristics.cpp:85-115):
 // delta = tau/mu, a = exp(-delta), I <- I a + (1 + (a-1)/delta) B_top + (-a - (a-1)/delta) B_bottom.
-template <bool TANG>
-__device__ __forceinline__ void sc_layer(double tau, double B, double B_prev, double& I1, double& I2,
-                                         const double* tab) {
+// All FP64 with the CUDA math library (the validation path).
+__device__ __forceinline__ void sc_layer(double tau, double B, double B_prev, double& I1, double& I2) {
   if (tau == 0) return;  // the reference skips exactly transparent layers only
   const double rtau = 1.0 / tau;
 #pragma unroll
   for (int i = 0; i < 2; ++i) {
     const double d = tau * kInvMu[i];
-    double a;
-    if (TANG) a = d > 700.0 ? 0.0 : exp_tang(-d, tab);
-    else a = exp(-d);
+    const double a = exp(-d);
     const double q = (a - 1.0) * (kMu[i] * rtau);
     double& I = i == 0 ? I1 : I2;
     I = I * a;

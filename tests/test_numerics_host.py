@@ -5,8 +5,8 @@ operation sequence in IEEE round-to-nearest host arithmetic, FMA where the
 device code uses FMA); tests/numerics_harness.cpp measures each routine
 against long-double references over the argument ranges the kernels use:
 
-* exp_tang / exp_tang2048: Tang's table-driven FP64 exp (64- and 2048-entry
-  tables; the FP64 reference forms of the recurrence's exponential);
+* exp_tang2048: Tang's table-driven FP64 exp (2048-entry table; the form with
+  the table index chosen in FP64);
 * exp_tang2048_f: the same with the table index chosen in FP32 from d2f_trunc,
   the exp(-delta) of the short-characteristics recurrence (ulp bound over
   delta <= 40, where a >= 4e-18; relative bound over delta <= 700);
@@ -31,7 +31,6 @@ import pytest
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 BOUNDS = {
-    "exp_tang": 3.4e-16,        # ~1.5 ulp
     "exp_tang2048": 3.4e-16,
     "exp_tang2048_ulp": 1.5,
     "exp_tang2048_f": 3.4e-16,
