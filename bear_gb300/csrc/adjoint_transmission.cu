@@ -12,8 +12,9 @@
 // Kernel chain for one chunk of evaluations (the likelihood adjoint and the seed
 // normaliser come from adjoint.cu):
 //   tr_geometry_adjoint_kernel  per evaluation, before the forward radiative transfer:
-//                               P[t][j] = dG[t][j-1]/dz_j = (R + z_j)/S_t(j),
-//                               Q[t][i] = dG[t][i]/dz_t, U[t][i] = dG[t][i]/dR
+//                               P[t][j] = dG[t][j-1]/dz_j = (R + z_j)/S_t(j) (stored as
+//                               [j][t]), Q[t][i] = dG[t][i]/dz_t, U[t][i] = dG[t][i]/dR, and
+//                               the path lengths G transposed ([j][t]) for pass 2a
 //   transmission_kernel<STORE>  (engine.cu) the forward pass itself also stores, per (level,
 //                               wavenumber), the ray transmission T_t, the cut-off index, the
 //                               pair sums c and the ray sums of c dG/dz_t and c dG/dR
@@ -55,13 +56,16 @@ __device__ __forceinline__ double tr_seed(const DeviceModel& dm, const double* _
 
 // ------------------------------------------------------------------ geometry derivatives
 __global__ void tr_geometry_adjoint_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
-                                           const EvalInfo* __restrict__ ev, float2* __restrict__ geo) {
+                                           const EvalInfo* __restrict__ ev, const float2* __restrict__ geom,
+                                           float2* __restrict__ geo) {
   const int b = blockIdx.x, L = dm.L;
   const LevelInfo* lv = lev + (size_t)b * L;
   const double R = ev[b].radius;
-  float2* P = geo + (size_t)b * 3 * L * L;
-  float2* Q = P + (size_t)L * L;
+  float2* PT = geo + (size_t)b * 4 * L * L;  // [j][t]: P transposed, for the per-level sums of pass 2a
+  float2* Q = PT + (size_t)L * L;
   float2* U = Q + (size_t)L * L;
+  float2* GT = U + (size_t)L * L;            // [j][t]: the forward path lengths G transposed
+  const float2* G = geom + (size_t)b * L * L;
   // 1 / S_t(j) for j > t (0 for j <= t or a degenerate zero path)
   auto rS = [&](int t, int j) -> double {
     if (j <= t) return 0.0;
@@ -77,7 +81,8 @@ __global__ void tr_geometry_adjoint_kernel(DeviceModel dm, const LevelInfo* __re
   for (int idx = blockIdx.y * blockDim.x + threadIdx.x; idx < L * L; idx += gridDim.y * blockDim.x) {
     const int t = idx / L, i = idx % L;
     const double zt = lv[t].z;
-    put(P + idx, (R + lv[i].z) * rS(t, i));
+    put(PT + (size_t)i * L + t, (R + lv[i].z) * rS(t, i));
+    GT[(size_t)i * L + t] = __ldg(&G[idx]);
     double q = 0.0, u = 0.0;
     if (i >= t && i < L - 1) {
       const double r0 = rS(t, i), r1 = rS(t, i + 1);
@@ -193,8 +198,9 @@ __global__ void __launch_bounds__(128) tr_adjoint_pass2a(DeviceModel dm, TrArgs 
   }
   __syncthreads();
   if (active) {
-    const float2* G = a.geom + (size_t)b * L * L;
-    const float2* P = a.geo + (size_t)b * 3 * L * L;
+    // per level j the rays' path lengths G[t][j] and P[t][j], contiguous in t
+    const float2* PT = a.geo + (size_t)b * 4 * L * L;
+    const float2* GT = PT + (size_t)3 * L * L;
     const df2 z = {0.0f, 0.0f};
     for (int j = grp; j < L; j += 4) {
       const df2 cj1 = j >= 1 ? ld(a.c, j - 1) : z;
@@ -208,7 +214,7 @@ __global__ void __launch_bounds__(128) tr_adjoint_pass2a(DeviceModel dm, TrArgs 
       const int t0 = (int)__reduce_min_sync(mask, (unsigned)m_s[j * 32 + lane]);
       for (int t = t0; t <= tmax; ++t) {
         const int I = I_s[t * 32 + lane];
-        const float2 g = __ldg(&G[(size_t)t * L + j]), p = __ldg(&P[(size_t)t * L + j]);
+        const float2 g = __ldg(&GT[(size_t)j * L + t]), p = __ldg(&PT[(size_t)j * L + t]);
         if (I < j - 1) continue;  // the ray of tangent level t stops below level j
         const df2 gtau = sm(gt_s, t * 32 + lane);
         const bool in_j = I >= j && j <= L - 2;
@@ -470,7 +476,7 @@ size_t transmission_grad_bytes_per_eval(const Model& m, int V, bool store) {
   const size_t L = m.L, N = m.N;
   const size_t tiles = (N + 31) / 32;
   const size_t terms = store ? L * N * ((size_t)m.acfg.S + 1) * sizeof(float2) : 0;
-  return L * N * (6 * sizeof(float2) + sizeof(short)) + 3 * L * L * sizeof(float2) + L * (size_t)V * 8 +
+  return L * N * (6 * sizeof(float2) + sizeof(short)) + 4 * L * L * sizeof(float2) + L * (size_t)V * 8 +
          tiles * 8 + terms;
 }
 
@@ -488,7 +494,7 @@ void alloc_transmission_grad(Model& m, int chunk, int V, bool store) {
   BGB_CUDA(cudaMalloc(&g.taps.tr_qs, n * sizeof(float2)));
   BGB_CUDA(cudaMalloc(&g.taps.tr_us, n * sizeof(float2)));
   BGB_CUDA(cudaMalloc(&g.taps.tr_I, n * sizeof(short)));
-  BGB_CUDA(cudaMalloc(&g.taps.tr_geo, B * 3 * L * L * sizeof(float2)));
+  BGB_CUDA(cudaMalloc(&g.taps.tr_geo, B * 4 * L * L * sizeof(float2)));
   BGB_CUDA(cudaMalloc(&g.tr_gc, n * sizeof(float2)));
   BGB_CUDA(cudaMalloc(&g.tr_gz, n * sizeof(float2)));
   BGB_CUDA(cudaMalloc(&g.tr_rp, B * tiles * sizeof(double)));

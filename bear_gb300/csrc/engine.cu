@@ -258,7 +258,8 @@ __global__ void transmission_geometry_kernel(DeviceModel dm, const LevelInfo* __
 constexpr int kTPN = 4;
 
 __global__ void tr_geometry_adjoint_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
-                                           const EvalInfo* __restrict__ ev, float2* __restrict__ geo);
+                                           const EvalInfo* __restrict__ ev, const float2* __restrict__ geom,
+                                           float2* __restrict__ geo);
 
 // Extinction abs + scat + cloud of every level of wavenumber k into the staged column
 // chi[l][VPB] (double-floats with DF, FP64 otherwise); thread j of the wavenumber's TPN
@@ -403,7 +404,7 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
       int last = L - 2;
       if (DF && STORE) {
         const float2* Gt = reinterpret_cast<const float2*>(geom) + (size_t)b * L * L + (size_t)t * L;
-        const float2* Qt = taps.tr_geo + (size_t)b * 3 * L * L + (size_t)L * L + (size_t)t * L;
+        const float2* Qt = taps.tr_geo + (size_t)b * 4 * L * L + (size_t)L * L + (size_t)t * L;
         const float2* Ut = Qt + (size_t)L * L;
         const float ch = dm.tau_cut_hi, cl = dm.tau_cut_lo;
         df2 ts = {0.0f, 0.0f};
@@ -1220,7 +1221,8 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
     if (taps) {
       // gradient pass: double-float kernel storing the ray data
       if (!df) throw Error(BEAR_ERR_UNSUPPORTED, "the transmission gradient runs in precision mode 0");
-      tr_geometry_adjoint_kernel<<<dim3(batch, (L * L + 255) / 256), 256, 0, st>>>(dm, w.lev, w.ev, taps->tr_geo);
+      tr_geometry_adjoint_kernel<<<dim3(batch, (L * L + 255) / 256), 256, 0, st>>>(
+          dm, w.lev, w.ev, reinterpret_cast<const float2*>(w.geom), taps->tr_geo);
       BGB_CUDA(cudaGetLastError());
       // the tuned wavenumbers per block when it is 64, else 32
       const int sv = vpb == 64 ? 64 : 32;
