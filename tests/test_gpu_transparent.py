@@ -1,7 +1,8 @@
 """Nearly transparent emission columns against the FP64 oracle: every line species at
-mixing ratios of 1e-30 .. 1e-14 and no collision-induced absorption, so the layer
-optical depths fall to 1e-25 .. 1e-9. There exp(-delta) rounds to 1 or to a few ulp
-below it, and the reference's q = (a - 1)/delta keeps only the rounding of a: the
+mixing ratios of 0 and 1e-30 .. 1e-14 and no collision-induced absorption, so the layer
+optical depths are exactly 0 (layers the reference skips) or fall to 1e-25 .. 1e-9.
+There exp(-delta) rounds to 1 or to a few ulp below it, and the reference's
+q = (a - 1)/delta keeps only the rounding of a: the
 engine's recurrence (carried as J = I - B with (a - 1) rounded where the reference
 rounds it) must reproduce those results, in the double-float and in the FP64 path."""
 
@@ -16,7 +17,7 @@ from bear_gb300.retrieval import Engine
 
 pytestmark = pytest.mark.gpu
 
-VMRS = [1e-30, 1e-24, 1e-20, 1e-17, 1e-14]
+VMRS = [0.0, 1e-30, 1e-24, 1e-20, 1e-17, 1e-14]  # 0: every layer has tau == 0 exactly (skipped)
 
 
 @pytest.fixture(scope="module")
