@@ -212,18 +212,28 @@ __global__ void __launch_bounds__(128) tr_adjoint_pass2a(DeviceModel dm, TrArgs 
       // from the lowest m(j) of the warp's wavenumbers, so the path-length loads stay uniform
       const unsigned mask = __activemask();
       const int t0 = (int)__reduce_min_sync(mask, (unsigned)m_s[j * 32 + lane]);
-      for (int t = t0; t <= tmax; ++t) {
-        const int I = I_s[t * 32 + lane];
-        const float2 g = __ldg(&GT[(size_t)j * L + t]), p = __ldg(&PT[(size_t)j * L + t]);
-        if (I < j - 1) continue;  // the ray of tangent level t stops below level j
-        const df2 gtau = sm(gt_s, t * 32 + lane);
+      auto ray = [&](int t, int I, float2 g, float2 p, float2 gt) {
+        if (I < j - 1) return;  // the ray of tangent level t stops below level j
+        const df2 gtau = {gt.x, gt.y};
         const bool in_j = I >= j && j <= L - 2;
         if (in_j) gc = df_fma(gtau, df2{g.x, g.y}, gc);
         if (t < j) {
           if (in_j) pin = df_fma(gtau, df2{p.x, p.y}, pin);
           else pend = df_fma(gtau, df2{p.x, p.y}, pend);  // j - 1 <= I_t holds here
         }
+      };
+      const float2* Gj = GT + (size_t)j * L;
+      const float2* Pj = PT + (size_t)j * L;
+      int t = t0;
+      // two rays per step, their loads issued together (same sums, same order)
+      for (; t + 1 <= tmax; t += 2) {
+        const int I0 = I_s[t * 32 + lane], I1 = I_s[(t + 1) * 32 + lane];
+        const float2 g0 = __ldg(&Gj[t]), g1 = __ldg(&Gj[t + 1]), p0 = __ldg(&Pj[t]), p1 = __ldg(&Pj[t + 1]);
+        const float2 q0 = gt_s[t * 32 + lane], q1 = gt_s[(t + 1) * 32 + lane];
+        ray(t, I0, g0, p0, q0);
+        ray(t + 1, I1, g1, p1, q1);
       }
+      if (t <= tmax) ray(t, I_s[t * 32 + lane], __ldg(&Gj[t]), __ldg(&Pj[t]), gt_s[t * 32 + lane]);
       const df2 gzp = df_fma(pin, dcc, df_mul(pend, cj1));
       // direct terms of the effective height: z1_j + g_h (A_{j-1} - A_{j+1}) (- A_0 at j = 0)
       df2 nb = z;
