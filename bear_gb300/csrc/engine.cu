@@ -408,18 +408,31 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
         const float2* Ut = Qt + (size_t)L * L;
         const float ch = dm.tau_cut_hi, cl = dm.tau_cut_lo;
         df2 ts = {0.0f, 0.0f};
-        for (int i = t; i < L - 1; ++i) {
-          const float2 g = __ldg(&Gt[i]), c = chi_f[i * VPB + v];
-          const float2 q = __ldg(&Qt[i]), u = __ldg(&Ut[i]);
+        bool cut = false;
+        // one segment of the three ray sums; true at the cut-off (tau > cut-off)
+        auto seg = [&](float2 g, float2 c, float2 q, float2 u) {
           const df2 cc = {c.x, c.y};
           ts = df_fma(df2{g.x, g.y}, cc, ts);
           qs = df_fma(df2{q.x, q.y}, cc, qs);
           us = df_fma(df2{u.x, u.y}, cc, us);
-          if (ts.hi > ch || (ts.hi == ch && ts.lo > cl)) {  // tau > cut-off
+          return ts.hi > ch || (ts.hi == ch && ts.lo > cl);
+        };
+        int i = t;
+        // two segments per step with their loads issued together (same sums, same break)
+        for (; i + 1 < L - 1 && !cut; i += 2) {
+          const float2 g0 = __ldg(&Gt[i]), g1 = __ldg(&Gt[i + 1]);
+          const float2 q0 = __ldg(&Qt[i]), q1 = __ldg(&Qt[i + 1]);
+          const float2 u0 = __ldg(&Ut[i]), u1 = __ldg(&Ut[i + 1]);
+          const float2 c0 = chi_f[i * VPB + v], c1 = chi_f[(i + 1) * VPB + v];
+          if (seg(g0, c0, q0, u0)) {
             last = i;
-            break;
+            cut = true;
+          } else if (seg(g1, c1, q1, u1)) {
+            last = i + 1;
+            cut = true;
           }
         }
+        if (i < L - 1 && !cut && seg(__ldg(&Gt[i]), chi_f[i * VPB + v], __ldg(&Qt[i]), __ldg(&Ut[i]))) last = i;
         tsd = ts;
       } else if (DF) {
         const float2* Gt = reinterpret_cast<const float2*>(geom) + (size_t)b * L * L + (size_t)t * L;
