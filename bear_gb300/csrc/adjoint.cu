@@ -449,9 +449,9 @@ __global__ void __launch_bounds__(kAdjThreads, DF ? 6 : 4) emission_adjoint_kern
       }
       df2 gB_m = z, gtau = z;
       if (opaque_layer) {
-        const df2 rt = t.hi > 1e-30f ? df_div(df_make(1.0f), t) : z;  // only used above delta = 1e-2
-        const df2 Ip1 = df_from_double(Is[(size_t)(l - 1) * 2 * N]);
-        const df2 Ip2 = df_from_double(Is[(size_t)(l - 1) * 2 * N + N]);
+        const df2 rt = t.hi > 1e-30f ? df_recip(t) : z;  // only used above delta = 1e-2
+        const df2 Ip1 = df_from_double_bits(Is[(size_t)(l - 1) * 2 * N]);
+        const df2 Ip2 = df_from_double_bits(Is[(size_t)(l - 1) * 2 * N + N]);
         sc_layer_adjoint_df(t, rt, B_l, B_m, Ip1, Ip2, lam1, lam2, gB_l, gB_m, gtau, et);
       }
       gK_l = df_add(gK_l, df_mul(gtau, dzh));
@@ -619,9 +619,9 @@ __global__ void __launch_bounds__(kAdjThreads) emission_adjoint_sweep_kernel(Dev
     const df2 dzh = {gz.x, gz.y};
     df2 gB_m = z, gtau = z;
     if (t.hi != 0.0f) {
-      const df2 rt = t.hi > 1e-30f ? df_div(df_make(1.0f), t) : z;  // only used above delta = 1e-2
-      const df2 Ip1 = df_from_double(Is[(size_t)(l - 1) * 2 * N]);
-      const df2 Ip2 = df_from_double(Is[(size_t)(l - 1) * 2 * N + N]);
+      const df2 rt = t.hi > 1e-30f ? df_recip(t) : z;  // only used above delta = 1e-2
+      const df2 Ip1 = df_from_double_bits(Is[(size_t)(l - 1) * 2 * N]);
+      const df2 Ip2 = df_from_double_bits(Is[(size_t)(l - 1) * 2 * N + N]);
       sc_layer_adjoint_df(t, rt, B_l, B_m, Ip1, Ip2, lam1, lam2, gB_l, gB_m, gtau, et);
     }
     gK_l = df_add(gK_l, df_mul(gtau, dzh));

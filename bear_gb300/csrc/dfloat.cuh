@@ -101,6 +101,21 @@ BGB_HD df2 df_from_double(double x) {
   return {hi, (float)(x - (double)hi)};
 }
 
+// The same split with integer operations for |x| in [2^-60, 2^101): hi = x truncated to
+// 24 significand bits, lo = the remaining 29 bits as a float (one int -> float conversion,
+// rounding them to 24 bits), so hi + lo is within 2^-48 |x| of x and |lo| < 2^-23 |hi|;
+// no FP64-pipe instruction. Zero and values outside that range take df_from_double.
+BGB_HD df2 df_from_double_bits(double x) {
+  const long long b = bgb_double_as_ll(x);
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e < 1023 - 60 || e >= 1023 + 101) return df_from_double(x);
+  const unsigned sign = (unsigned)((unsigned long long)b >> 32) & 0x80000000u;
+  const float hi = bgb_int_as_float((int)(sign | ((unsigned)(e - 896) << 23) | (unsigned)((b >> 29) & 0x7fffff)));
+  // the remaining bits times 2^(e - 1075) (a normal float power for e in range)
+  const float r = BGB_FMUL((float)(unsigned)(b & 0x1fffffff), bgb_int_as_float((e - 948) << 23));
+  return {hi, sign ? -r : r};
+}
+
 // hi + lo in FP64: the two conversions on the integer pipe, one FP64 add.
 BGB_HD double df_to_double(df2 a) { return f2d_bits(a.hi) + f2d_bits(a.lo); }
 

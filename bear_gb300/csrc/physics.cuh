@@ -36,7 +36,7 @@ BGB_HD df2 planck_df2(df2 c1, df2 c2l, df2 invT, const float* tab_hi, const floa
   if (n < -60) return df_ldexp(df_mul(c1, m), n);
   const df2 u = df_ldexp(m, n);
   const df2 d = df_sub(df_make(1.0f), u);
-  return df_div(df_mul(c1, u), d);
+  return df_mul(df_mul(c1, u), df_recip(d));
 }
 
 // exp(-d) for a double-float d >= 0 (0 for d > 700 and below the float range).

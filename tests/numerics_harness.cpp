@@ -104,6 +104,24 @@ int main() {
     const long double ref = 1.0L / ((long double)bd.hi + bd.lo);
     e_recip = std::fmax(e_recip, (double)fabsl(((long double)r.hi + r.lo) / ref - 1));
   }
+  // df_from_double_bits: within 2^-48 of the value in its range, df_from_double outside it
+  double e_split = 0;
+  long long split_fallback_bad = 0;
+  for (int i = 0; i < 2000000; ++i) {
+    double x = std::ldexp(1.0 + U(g), (int)(200.0 * U(g)) - 100);
+    if (i & 1) x = -x;
+    if (i % 1000 == 0) x = 0.0;
+    const df2 d = df_from_double_bits(x);
+    const int ex = std::ilogb(x);
+    if (x == 0.0 || ex < -60 || ex >= 101) {
+      const df2 r = df_from_double(x);
+      if (bgb_float_as_uint(d.hi) != bgb_float_as_uint(r.hi) || bgb_float_as_uint(d.lo) != bgb_float_as_uint(r.lo))
+        ++split_fallback_bad;
+    } else {
+      e_split = std::fmax(e_split, (double)fabsl(((long double)d.hi + d.lo) / (long double)x - 1));
+      if (std::fabs(d.lo) >= std::ldexp(std::fabs(d.hi), -23)) ++split_fallback_bad;
+    }
+  }
   // d2f_trunc: below the float range 0, else within 2^-23 of the value
   double e_trunc = 0;
   for (int i = 0; i < 1000000; ++i) {
@@ -114,8 +132,9 @@ int main() {
   }
   std::printf("df_exp2 %.3e\nexp_tang2048 %.3e\nexp_tang2048_ulp %.3f\ndf_exp_neg %.3e\n"
               "df_pow10 %.3e\nplanck_df %.3e\nconversion_mismatches %lld\nexp_tang2048_f %.3e\n"
-              "exp_tang2048_f_ulp %.3f\nd2f_trunc %.3e\ndf_exp2_edge_failures %lld\ndf_recip %.3e\n",
+              "exp_tang2048_f_ulp %.3f\nd2f_trunc %.3e\ndf_exp2_edge_failures %lld\ndf_recip %.3e\n"
+              "df_from_double_bits %.3e\ndf_from_double_bits_failures %lld\n",
               e_exp2, e_tang2048, ulp2048, e_expneg, e_pow10, e_planck, conv_mismatch, e_tang2048f,
-              ulp2048f, e_trunc, edge_bad, e_recip);
+              ulp2048f, e_trunc, edge_bad, e_recip, e_split, split_fallback_bad);
   return 0;
 }

@@ -37,6 +37,8 @@ BOUNDS = {
     "exp_tang2048_f_ulp": 1.5,
     "d2f_trunc": 1.2e-7,        # 2^-23
     "df_recip": 3e-14,          # one Newton step from a float reciprocal (~2^-45)
+    "df_from_double_bits": 3.6e-15,   # 2^-48
+    "df_from_double_bits_failures": 0,  # outside its range identical to df_from_double
     "df_exp2_edge_failures": 0,  # |y| beyond the clamp: 0 / infinite in the callers; NaN propagates
     "df_exp2": 5e-14,
     "df_pow10": 2e-12,          # |x| <= 40: 10^x from a 48-bit x log2(10)
