@@ -14,6 +14,8 @@ against long-double references over the argument ranges the kernels use:
 * df_exp2 / 10^x: double-float exponentials of the opacity assembly;
 * planck_df: the double-float Planck function;
 * df_recip: double-float reciprocal by one Newton step (1/tau, 1/(1 - u) of Planck);
+* df_from_double_bits: FP64 value split into a double-float with integer operations
+  (the adjoint's stored intensities), identical to df_from_double outside its range;
 * df_exp_neg: the double-float exp(-delta) of the adjoint;
 * f2d_bits / i2d_bits: float and int to double built with integer operations
   (bit-identical to the conversions, checked on every exponent, zeros and subnormals).
