@@ -698,16 +698,18 @@ __global__ void __launch_bounds__(kAdjThreads) emission_adjoint_sinks_kernel(Dev
         const float4 fb = __ldg(reinterpret_cast<const float4*>(sf + s) + 1);  // wT, log2 n
         if (fb.z == kNoSpecies) continue;
         const df2 lo = {t0[g].x, t0[g].y}, hi = {t1[g].x, t1[g].y};
-        const df2 y = df_add(df_lerp(lo, hi, df2{fb.x, fb.y}), df2{fb.z, fb.w});
+        // lo + (hi - lo) wT + log2 n, as the forward pass forms it (level_kappa_df_cb)
+        const df2 diff = df_sub(hi, lo);
+        const df2 y = df_fma(diff, df2{fb.x, fb.y}, df_add(lo, df2{fb.z, fb.w}));
         int n;
         const df2 m = df_exp2(y, n, et.hi, et.lo);
         const float2 d = __ldg(dwl + s);
         const bool narrow = n > -100 && n < 100;
-        const df2 slope = df_mul(df_sub(hi, lo), df2{d.x, d.y});
+        const df2 slope = df_mul(diff, df2{d.x, d.y});
         if (narrow) {
           const df2 t = df_ldexp(m, n);
-          acc[s] = df_add(acc[s], df_mul(gK, t));
-          if (d.x != 0.0f) dk = df_add(dk, df_mul(t, slope));
+          acc[s] = df_fma(gK, t, acc[s]);
+          if (d.x != 0.0f) dk = df_fma(t, slope, dk);
         } else {
           const double tw = df_to_double(m) * pow2d(n);
           if (gK64 == 0.0) gK64 = df_to_double(gK);
