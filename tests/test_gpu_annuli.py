@@ -2,8 +2,8 @@
 reference) on the GPU against the FP64 oracle's restatement of the same integral: every
 spectral and binned point within 1e-6 relative and log L within 1e-8 + 1e-12 |log L|, in
 the double-float and the FP64 paths, for a non-grey (KH) cloud case and a variable-gravity
-grey-cloud case. A = 1 gives the default kernel's results bit for bit; the gradient is
-refused for A > 1."""
+grey-cloud case. A = 1 gives the default kernel's results bit for bit; the captured,
+autotuned batch and every launch shape agree; the gradient is refused for A > 1."""
 
 import os
 
@@ -88,3 +88,30 @@ def test_annuli_gradient_is_refused(case):
     with pytest.raises(_lib.EngineError) as err:
         e.grad_batch(torch.tensor(c.params[:1], device="cuda"))
     assert err.value.code == 4  # BEAR_ERR_UNSUPPORTED
+
+
+def test_annuli_autotuned_graph_and_shapes(case):
+    """The captured, autotuned batch equals the uncaptured batch, and every launch shape
+    (threads per wavenumber x rays per group) gives log L within rounding of the default."""
+    import torch
+    from bear_gb300.retrieval import BatchEvaluator
+    c, e, om = case
+    P = torch.tensor(np.repeat(c.params, 3, axis=0), device="cuda")
+    ll_ref, ng_ref = e.loglike_batch(P)
+    ll_ref = ll_ref.cpu().numpy()
+    ev = BatchEvaluator(e, P)
+    try:
+        ll_g, ng_g = ev()
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(ng_g.cpu().numpy(), ng_ref.cpu().numpy())
+        shape_ll = {}
+        for rt in (16, 32, 64):
+            e.set_launch(rt, 0)
+            shape_ll[rt] = e.loglike_batch(P)[0].cpu().numpy()
+        e.set_launch(0, 0)
+        assert np.array_equal(ll_g.cpu().numpy(), shape_ll[ev.rt_threads if ev.rt_threads in shape_ll else 32])
+        for rt, ll in shape_ll.items():
+            ok = ~ng_ref.cpu().numpy().astype(bool)
+            assert np.all(np.abs(ll[ok] - ll_ref[ok]) <= 1e-9 + 1e-13 * np.abs(ll_ref[ok])), rt
+    finally:
+        ev.close()
