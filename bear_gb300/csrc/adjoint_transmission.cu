@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(128) tr_adjoint_pass2a(DeviceModel dm, TrArgs 
 // double [S][T] (T = kTrSinkThreads), then the level's Rayleigh number densities float2 [R].
 constexpr int kTrSinkThreads = 128;
 
-template <int VP>
+template <int VP, bool PAIRS>
 __global__ void __launch_bounds__(kTrSinkThreads, VP == 32 ? 4 : 6) tr_adjoint_pass2b(DeviceModel dm, TrArgs a) {
   constexpr int G = 32 / VP, NW = kTrSinkThreads / 32;
   __shared__ ExpTables et;
@@ -292,23 +292,13 @@ __global__ void __launch_bounds__(kTrSinkThreads, VP == 32 ? 4 : 6) tr_adjoint_p
   df2 v[VP];
 #pragma unroll
   for (int q = 0; q < VP; ++q) v[q] = df2{0.0f, 0.0f};
-  for (int k = tid; k < (int)N; k += kTrSinkThreads) {
-    // d log L / d chi_l (chi_l enters c_l and c_{l-1})
-    df2 gx = {0.0f, 0.0f};
-    if (l <= L - 2) {
-      const float2 c0 = a.gc[row + k];
-      gx = df2{c0.x, c0.y};
-    }
-    if (l >= 1) {
-      const float2 c1 = a.gc[row - N + k];
-      gx = df_add(gx, df2{c1.x, c1.y});
-    }
-    const float2 gz = a.gz[row + k];
+  // one wavenumber's contribution (the recompute path, and every wavenumber when the
+  // wavenumbers are not taken in pairs)
+  auto one = [&](int k, df2 gx, float2 gz, float2 dks) {
     // opacity terms and their temperature slope (level-table values are log2 units)
     df2 dk = {0.0f, 0.0f};
     double dkw = 0.0;
     bool wide = false;
-    const float2 dks = a.ts ? a.dk[row + k] : make_float2(__int_as_float(0x7fc00000), 0.0f);
     const bool stored = !isnan(dks.x);
     if (stored) {
       dk = df2{dks.x, dks.y};
@@ -346,6 +336,75 @@ __global__ void __launch_bounds__(kTrSinkThreads, VP == 32 ? 4 : 6) tr_adjoint_p
         x = gx;
       }
       v[q] = df_add(v[q], x);
+    }
+  };
+  auto load_gx = [&](int k) {
+    df2 gx = {0.0f, 0.0f};
+    if (l <= L - 2) {
+      const float2 c0 = a.gc[row + k];
+      gx = df2{c0.x, c0.y};
+    }
+    if (l >= 1) {
+      const float2 c1 = a.gc[row - N + k];
+      gx = df_add(gx, df2{c1.x, c1.y});
+    }
+    return gx;
+  };
+  const float2 no_store = make_float2(__int_as_float(0x7fc00000), 0.0f);
+  if (!PAIRS) {
+    for (int k = tid; k < (int)N; k += kTrSinkThreads)
+      one(k, load_gx(k), a.gz[row + k], a.ts ? a.dk[row + k] : no_store);
+  } else {
+    // N even: wavenumbers in adjacent pairs, every read 16 bytes; where both terms of a pair
+    // are stored they are combined directly (the same sums in the same order as one() twice)
+    auto ld4 = [](const float2* p) { return __ldg(reinterpret_cast<const float4*>(p)); };
+    for (int k0 = 2 * tid; k0 < (int)N; k0 += 2 * kTrSinkThreads) {
+      df2 gx0 = {0.0f, 0.0f}, gx1 = {0.0f, 0.0f};
+      if (l <= L - 2) {
+        const float4 c = ld4(a.gc + row + k0);
+        gx0 = df2{c.x, c.y};
+        gx1 = df2{c.z, c.w};
+      }
+      if (l >= 1) {
+        const float4 c = ld4(a.gc + row - N + k0);
+        gx0 = df_add(gx0, df2{c.x, c.y});
+        gx1 = df_add(gx1, df2{c.z, c.w});
+      }
+      const float4 gz = ld4(a.gz + row + k0);
+      const float4 dks = a.ts ? ld4(a.dk + row + k0) : make_float4(no_store.x, 0.0f, no_store.x, 0.0f);
+      if (isnan(dks.x) || isnan(dks.z)) {
+#pragma unroll 1
+        for (int w = 0; w < 2; ++w)
+          one(k0 + w, w ? gx1 : gx0, w ? make_float2(gz.z, gz.w) : make_float2(gz.x, gz.y),
+              w ? make_float2(dks.z, dks.w) : make_float2(dks.x, dks.y));
+        continue;
+      }
+      const df2 gT0 = df_mul(gx0, df_mul(df2{dks.x, dks.y}, df2{kLn2Hi, kLn2Lo}));
+      const df2 gT1 = df_mul(gx1, df_mul(df2{dks.z, dks.w}, df2{kLn2Hi, kLn2Lo}));
+#pragma unroll
+      for (int q = 0; q < VP; ++q) {
+        df2 x0 = {0.0f, 0.0f}, x1 = {0.0f, 0.0f};
+        if (q < S) {
+          const float4 t = ld4(tsl + (size_t)q * N + k0);
+          x0 = df_mul(gx0, df2{t.x, t.y});
+          x1 = df_mul(gx1, df2{t.z, t.w});
+        } else if (q < S + R) {
+          const float4 sr = ld4(dm.rayleigh_df + (size_t)(q - S) * N + k0);
+          const float2 nr = rn_s[q - S];
+          x0 = df_mul(gx0, df_mul(df2{sr.x, sr.y}, df2{nr.x, nr.y}));
+          x1 = df_mul(gx1, df_mul(df2{sr.z, sr.w}, df2{nr.x, nr.y}));
+        } else if (q == S + R) {
+          x0 = gT0;
+          x1 = gT1;
+        } else if (q == S + R + 1) {
+          x0 = df2{gz.x, gz.y};
+          x1 = df2{gz.z, gz.w};
+        } else if (q == S + R + 2) {
+          x0 = gx0;
+          x1 = gx1;
+        }
+        v[q] = df_add(df_add(v[q], x0), x1);
+      }
     }
   }
   const df2 r = warp_reduce_scatter<VP>(v, lane);
@@ -535,9 +594,11 @@ void transmission_adjoint_chunk(Model& m, const double* params_chunk, int nb, cu
     if (sm2 > 48 * 1024) BGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));
     kernel<<<dim3(nb, L), kTrSinkThreads, sm2, st>>>(dm, a);
   };
-  if (VP == 8) go2(tr_adjoint_pass2b<8>);
-  else if (VP == 16) go2(tr_adjoint_pass2b<16>);
-  else go2(tr_adjoint_pass2b<32>);
+  // wavenumbers in pairs (16-byte reads) when N is even
+  const bool pairs = (N % 2) == 0;
+  if (VP == 8) pairs ? go2(tr_adjoint_pass2b<8, true>) : go2(tr_adjoint_pass2b<8, false>);
+  else if (VP == 16) pairs ? go2(tr_adjoint_pass2b<16, true>) : go2(tr_adjoint_pass2b<16, false>);
+  else pairs ? go2(tr_adjoint_pass2b<32, true>) : go2(tr_adjoint_pass2b<32, false>);
   BGB_CUDA(cudaGetLastError());
   const size_t sma = (size_t)L * V * sizeof(double);
   if (sma > 48 * 1024)
