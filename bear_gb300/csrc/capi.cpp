@@ -40,6 +40,30 @@ void check_cuda(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw bgb::Error(BEAR_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// Makes the model's device current for the duration of a call and restores the
+// caller's device afterwards, so a call made while another GPU is current still
+// launches on the GPU that holds the model's buffers. cudaSetDevice is only
+// called when the devices differ.
+class DeviceScope {
+ public:
+  explicit DeviceScope(int device) {
+    check_cuda(cudaGetDevice(&previous_), "cudaGetDevice");
+    if (previous_ != device) {
+      check_cuda(cudaSetDevice(device), "cudaSetDevice");
+      switched_ = true;
+    }
+  }
+  ~DeviceScope() {
+    if (switched_) cudaSetDevice(previous_);
+  }
+  DeviceScope(const DeviceScope&) = delete;
+  DeviceScope& operator=(const DeviceScope&) = delete;
+
+ private:
+  int previous_ = 0;
+  bool switched_ = false;
+};
+
 void require_ready(const bear_model* h) {
   if (!h) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null model");
   if (!h->m.finalized) throw bgb::Error(BEAR_ERR_STATE, "model is not finalized");
@@ -121,6 +145,7 @@ int bear_model_finalize(bear_model* h) {
   return guarded([&] {
     if (!h) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null model");
     if (h->m.finalized) throw bgb::Error(BEAR_ERR_STATE, "model already finalized");
+    const DeviceScope on_model_device(h->m.device);
     if (!h->m.prepared) {
       bgb::finalize_host(h->m);
       h->m.prepared = true;
@@ -204,7 +229,12 @@ int bear_model_device_bytes(const bear_model* h, size_t* bytes) {
 
 void bear_model_destroy(bear_model* h) {
   if (!h) return;
-  if (h->m.finalized) bgb::release_model(h->m);
+  if (h->m.finalized) {
+    int previous = 0;
+    const bool have_previous = cudaGetDevice(&previous) == cudaSuccess;
+    bgb::release_model(h->m);
+    if (have_previous) cudaSetDevice(previous);
+  }
   delete h;
 }
 
@@ -280,6 +310,7 @@ int bear_model_table_info(const bear_model* h, int* levels, int* table_species, 
 int bear_model_stencil_rows(bear_model* h, int batch, long long* rows) {
   return guarded([&] {
     require_ready(h);
+    const DeviceScope on_model_device(h->m.device);
     if (!rows) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null output");
     *rows = bgb::stencil_rows(h->m, batch);
   });
@@ -289,6 +320,7 @@ int bear_forward(bear_model* h, const double* params, int nb_params, double* spe
                  double* const* obs_dev, int* neglect, void* stream) {
   return guarded([&] {
     require_ready(h);
+    const DeviceScope on_model_device(h->m.device);
     bgb::Model& m = h->m;
     cudaStream_t st = (cudaStream_t)stream;
     run_plain(h, params, nb_params, st);
@@ -311,6 +343,7 @@ int bear_compute_model(bear_model* h, const double* params, int nb_params, doubl
                        double* obs, int* neglect, void* stream) {
   return guarded([&] {
     require_ready(h);
+    const DeviceScope on_model_device(h->m.device);
     bgb::Model& m = h->m;
     cudaStream_t st = (cudaStream_t)stream;
     run_plain(h, params, nb_params, st);
@@ -339,6 +372,7 @@ int bear_compute_model(bear_model* h, const double* params, int nb_params, doubl
 int bear_loglike(bear_model* h, const double* params, int nb_params, double* loglike, void* stream) {
   return guarded([&] {
     require_ready(h);
+    const DeviceScope on_model_device(h->m.device);
     bgb::Model& m = h->m;
     cudaStream_t st = (cudaStream_t)stream;
     run_plain(h, params, nb_params, st);
@@ -353,6 +387,7 @@ int bear_loglike_batch(bear_model* h, const double* params_dev, int batch, int n
                        double* loglike_dev, uint8_t* neglect_dev, void* stream) {
   return guarded([&] {
     require_ready(h);
+    const DeviceScope on_model_device(h->m.device);
     require_params(h, nb_params);
     if (batch < 1) throw bgb::Error(BEAR_ERR_SIZE, "batch must be positive");
     if (!params_dev || !loglike_dev) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null device buffer");
@@ -364,6 +399,7 @@ int bear_loglike_noalloc(bear_model* h, const double* params_dev, int nb_params,
                          uint8_t* neglect_dev, void* stream) {
   return guarded([&] {
     require_ready(h);
+    const DeviceScope on_model_device(h->m.device);
     require_params(h, nb_params);
     if (!params_dev || !loglike_dev) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null device buffer");
     bgb::loglike_noalloc(h->m, params_dev, loglike_dev, neglect_dev, (cudaStream_t)stream);
@@ -374,6 +410,7 @@ int bear_contribution_functions(bear_model* h, const double* params, int nb_para
                                 double* cf_spectrum, void* stream) {
   return guarded([&] {
     require_ready(h);
+    const DeviceScope on_model_device(h->m.device);
     if (h->m.transmission)
       throw bgb::Error(BEAR_ERR_UNSUPPORTED, "contribution functions exist for emission and secondary-eclipse models");
     const cudaStream_t st = (cudaStream_t)stream;
@@ -386,6 +423,7 @@ int bear_model_set_priors(bear_model* h, int n, const int* type, const double* a
                           const double* unit, const int* link) {
   return guarded([&] {
     require_ready(h);
+    const DeviceScope on_model_device(h->m.device);
     if (n < 0 || (n > 0 && !type)) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null prior table");
     bgb::set_priors(h->m, n, type, a, b, unit, link);
   });
@@ -395,6 +433,7 @@ int bear_prior_transform_batch(bear_model* h, const double* cube_dev, int batch,
                                double* params_dev, void* stream) {
   return guarded([&] {
     require_ready(h);
+    const DeviceScope on_model_device(h->m.device);
     require_params(h, nb_params);
     if (batch < 1) throw bgb::Error(BEAR_ERR_SIZE, "batch must be positive");
     if (!cube_dev || !params_dev) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null device buffer");
@@ -406,6 +445,7 @@ int bear_loglike_cube_batch(bear_model* h, const double* cube_dev, int batch, in
                             double* loglike_dev, uint8_t* neglect_dev, void* stream) {
   return guarded([&] {
     require_ready(h);
+    const DeviceScope on_model_device(h->m.device);
     require_params(h, nb_params);
     if (batch < 1) throw bgb::Error(BEAR_ERR_SIZE, "batch must be positive");
     if (!cube_dev || !params_dev || !loglike_dev) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null device buffer");
@@ -420,6 +460,7 @@ int bear_loglike_grad_batch(bear_model* h, const double* params_dev, int batch, 
                             void* stream) {
   return guarded([&] {
     require_ready(h);
+    const DeviceScope on_model_device(h->m.device);
     require_params(h, nb_params);
     if (batch < 1) throw bgb::Error(BEAR_ERR_SIZE, "batch must be positive");
     if (!params_dev || !loglike_dev || !grad_dev) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null device buffer");
@@ -448,6 +489,7 @@ int bear_model_autotune(bear_model* h, const double* params_dev, int batch, int 
                         int* rt_threads_out) {
   return guarded([&] {
     require_ready(h);
+    const DeviceScope on_model_device(h->m.device);
     require_params(h, nb_params);
     if (batch < 2) throw bgb::Error(BEAR_ERR_SIZE, "autotuning needs a batch of at least 2");
     if (!params_dev) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null device buffer");
@@ -551,6 +593,7 @@ int bear_batch_graph_create(bear_model* h, const double* params_dev, int batch, 
                             double* loglike_dev, uint8_t* neglect_dev, bear_batch_graph** out) {
   return guarded([&] {
     require_ready(h);
+    const DeviceScope on_model_device(h->m.device);
     require_params(h, nb_params);
     if (batch < 1) throw bgb::Error(BEAR_ERR_SIZE, "batch must be positive");
     if (!params_dev || !loglike_dev || !out) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null buffer");
@@ -565,6 +608,7 @@ int bear_batch_graph_create_cube(bear_model* h, const double* cube_dev, int batc
                                  bear_batch_graph** out) {
   return guarded([&] {
     require_ready(h);
+    const DeviceScope on_model_device(h->m.device);
     require_params(h, nb_params);
     if (batch < 1) throw bgb::Error(BEAR_ERR_SIZE, "batch must be positive");
     if (!cube_dev || !params_dev || !loglike_dev || !out) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null buffer");
@@ -581,6 +625,7 @@ int bear_batch_graph_launch(bear_batch_graph* g, void* stream) {
     if (!g || !g->exec) throw bgb::Error(BEAR_ERR_INVALID_INPUT, "null graph");
     if (g->generation != g->h->m.ws_generation)
       throw bgb::Error(BEAR_ERR_STATE, "the model's work buffers were reallocated after the capture; recreate the graph");
+    const DeviceScope on_model_device(g->h->m.device);
     check_cuda(cudaGraphLaunch(g->exec, (cudaStream_t)stream), "cudaGraphLaunch");
   });
 }

@@ -1,21 +1,24 @@
 // Single-evaluation log-likelihood that allocates no memory at call time.
 //
-// Who needs this: callers that may not allocate device memory while they run --
-// code executing inside a CUDA stream capture (cudaMalloc is not capturable),
-// processes whose device memory is owned by another framework's pool or by a
-// strict budget, and real-time callbacks (for example a sampler's per-point
-// likelihood hook) that must not block on the allocator. The regular entry
-// points grow a per-model workspace with cudaMalloc the first time a batch size
-// is seen; this one instead keeps the per-evaluation work buffers (level and
-// stencil records, the high-resolution spectrum, the binned spectrum, the
-// transmission path lengths) in one fixed array in device memory declared below.
+// Who needs this: host applications that cannot call cudaMalloc while they run.
+// Some own all device memory through another framework's pool or a fixed budget
+// set at start-up, so an allocation made behind their back either fails or
+// breaks their accounting; others call the likelihood from a real-time callback
+// (for example a sampler's per-point likelihood hook) that must not block on the
+// allocator. The regular entry points grow a per-model workspace with cudaMalloc
+// the first time a batch size is seen; this one instead keeps the per-evaluation
+// work buffers (level and stencil records, the high-resolution spectrum, the
+// binned spectrum, the transmission path lengths) in one fixed array in device
+// memory declared below.
 //
 // The array is a file-scope __device__ variable, so every GPU that loads the
 // library holds kNoAllocScratchBytes of it until the process exits, whether or
 // not this entry point is used. Host code cannot use the array's name as a
 // device address; its address is looked up with cudaGetSymbolAddress once per
-// device (with that device current) on the first call made for a model on that
-// device. Make that first call before any stream capture starts.
+// device, with that device current, on the first call made for a model on that
+// device. Make that first call before any stream capture starts. The address is
+// kept for the life of the process: after cudaDeviceReset it is stale, and this
+// entry point must not be called again in that process.
 //
 // Every call on a device shares the same array, and each call overwrites what
 // the previous one left there: every element a call reads is written earlier in
@@ -84,18 +87,18 @@ size_t layout(const Model& m, unsigned char* base, Workspace* w) {
   return off;
 }
 
+// Address of the scratch array on `device`, which the caller has made current
+// (the C ABI switches to the model's device for the whole call).
 unsigned char* scratch_for_device(int device) {
   if (device < 0 || device >= kMaxDevices) throw Error(BEAR_ERR_INVALID_INPUT, "device index out of range");
   std::lock_guard<std::mutex> lock(g_scratch_mutex);
   if (!g_scratch_addr[device]) {
-    int previous = 0;
-    cudaError_t e = cudaGetDevice(&previous);
+    int current = -1;
+    cudaError_t e = cudaGetDevice(&current);
     if (e != cudaSuccess) throw Error(BEAR_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-    e = cudaSetDevice(device);
-    if (e != cudaSuccess) throw Error(BEAR_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+    if (current != device) throw Error(BEAR_ERR_STATE, "the model's device is not current");
     void* ptr = nullptr;
     e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-    cudaSetDevice(previous);
     if (e != cudaSuccess || !ptr)
       throw Error(BEAR_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
     g_scratch_addr[device] = ptr;

@@ -19,6 +19,11 @@
  * Threading: a model is used by one host thread / one stream at a time. Batch
  * calls are stream-ordered and allocate nothing once a batch size has been
  * seen (work buffers grow on first use of a larger batch).
+ *
+ * Devices: every call that touches the GPU makes the model's device (the one
+ * given to bear_model_create) current while it runs and restores the caller's
+ * current device before returning. Streams passed in must belong to the
+ * model's device.
  */
 #ifndef BEAR_GB300_H
 #define BEAR_GB300_H
@@ -254,17 +259,20 @@ int bear_model_set_precision(bear_model* m, int mode);
 int bear_model_set_launch(bear_model* m, int rt_threads, int obs_threads);
 
 /* Allocation-free log-likelihood of one parameter set. No counterpart in the
- * reference. For callers that cannot allocate device memory during the call:
- * inside a CUDA stream capture, under a foreign memory pool or budget, or in a
- * latency-bound per-point callback. params_dev: device, nb_params doubles;
- * loglike_dev: device, 1 double (-1e30 when neglected); neglect_dev: device,
- * 1 byte (NULL allowed). The per-evaluation work buffers live in a fixed
- * 2 MiB device array that every GPU loading the library holds until exit;
- * models needing more scratch than that are rejected with BEAR_ERR_SIZE. The
- * first call for a model's device looks up the array's address with
- * cudaGetSymbolAddress: make it before any stream capture. All calls on a
- * device share the array: calls that may overlap on the GPU race and must be
- * serialised by the caller. Stream-ordered; does not synchronise. */
+ * reference. For host applications that cannot call cudaMalloc during the call:
+ * those whose device memory belongs to another framework's pool or to a fixed
+ * budget set at start-up, and per-point sampler callbacks that must not block in
+ * the allocator. params_dev: device, nb_params doubles; loglike_dev: device,
+ * 1 double (-1e30 when neglected); neglect_dev: device, 1 byte (NULL allowed).
+ * The per-evaluation work buffers live in a fixed 2 MiB device array that every
+ * GPU loading the library holds until exit; models needing more scratch than
+ * that are rejected with BEAR_ERR_SIZE. The first call for a model's device
+ * looks up the array's address with cudaGetSymbolAddress (with the model's
+ * device current): make it before any stream capture. The address is kept for
+ * the life of the process, so the entry point must not be used after
+ * cudaDeviceReset. All calls on a device share the array: calls that may
+ * overlap on the GPU race and must be serialised by the caller. Stream-ordered;
+ * does not synchronise. */
 int bear_loglike_noalloc(bear_model* m, const double* params_dev, int nb_params,
                          double* loglike_dev, uint8_t* neglect_dev, void* stream);
 

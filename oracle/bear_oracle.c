@@ -605,18 +605,21 @@ static int load_rows(orc_model* m, opac_t* op, const char* folder) {
       if (fread(buf, sizeof(float), nd, df) != nd) { fclose(df); set_err("short read %s", path); return -1; }
       fclose(df);
       double* r = (double*)malloc(m->N * sizeof(double));
-      for (size_t k = 0; k < m->N; ++k) r[k] = 0.0;
-      for (size_t k = 0; k < m->N; ++k) {
-        if (m->index_list[k] > nd - 1) break;
-        double v = buf[m->index_list[k]];
-        if (logst) v = pow(10.0, v);
-        r[k] = v;
+      /* points past the end of the file keep 0 (then the 1e-200 floor) */
+      size_t kend = 0;
+      while (kend < m->N && m->index_list[kend] <= nd - 1) ++kend;
+      const long long nk = (long long)m->N;
+#pragma omp parallel for schedule(static)
+      for (long long k = 0; k < nk; ++k) {
+        double v = 0.0;
+        if ((size_t)k < kend) {
+          v = buf[m->index_list[k]];
+          if (logst) v = pow(10.0, v);
+        }
+        if (op->mass > 0) v *= op->mass / 6.022140857e23;
+        if (v < 1e-200) v = 1e-200;
+        r[k] = log10(v);
       }
-      for (size_t k = 0; k < m->N; ++k) {
-        if (op->mass > 0) r[k] *= op->mass / 6.022140857e23;
-        if (r[k] < 1e-200) r[k] = 1e-200;
-      }
-      for (size_t k = 0; k < m->N; ++k) r[k] = log10(r[k]);
       op->rows[t][q] = r;
     }
     free(idx);
@@ -1595,6 +1598,29 @@ int orc_obs_setup(const orc_model* m, int k, long* out, int cap) {
 }
 
 void orc_destroy(orc_model* m) {
-  /* the oracle lives for the length of a test; memory is returned to the OS at exit */
+  if (!m) return;
+  for (int i = 0; i < m->nopac; ++i) {
+    opac_t* op = &m->opac[i];
+    for (int t = 0; t < op->nT; ++t) {
+      if (op->rows && op->rows[t]) {
+        for (int q = 0; q < op->nP[t]; ++q) free(op->rows[t][q]);
+        free(op->rows[t]);
+      }
+      if (op->P) free(op->P[t]);
+      if (op->logP) free(op->logP[t]);
+    }
+    free(op->rows); free(op->P); free(op->logP); free(op->nP); free(op->T);
+    free(op->rayleigh); free(op->hm_bf);
+    for (int j = 1; j < 7; ++j) free(op->hm_ff[j]);
+  }
+  for (int i = 0; i < m->nobs; ++i) {
+    obs_t* o = &m->obs[i];
+    free(o->data); free(o->error); free(o->weight); free(o->fwhm); free(o->edges); free(o->centers);
+    free(o->edge_nu); free(o->edge_idx); free(o->sigma); free(o->conv); free(o->filter_wl);
+    free(o->filter_resp); free(o->filter_on_grid); free(o->filter_weight);
+  }
+  free(m->nu_full); free(m->wl_full); free(m->index_list); free(m->nu); free(m->wl); free(m->p);
+  free(m->pp_dof_vertices); free(m->pp_el_vert); free(m->star_flux); free(m->star_grid);
+  for (int a = 0; a < 3; ++a) free(m->star_axis[a]);
   free(m);
 }

@@ -58,6 +58,8 @@ def lib():
         L.orc_set_tau_cutoff.argtypes = [C.c_void_p, C.c_double]
         L.orc_obs_setup.restype = C.c_int
         L.orc_obs_setup.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_long), C.c_int]
+        L.orc_destroy.restype = None
+        L.orc_destroy.argtypes = [C.c_void_p]
         _lib = L
     return _lib
 
@@ -96,6 +98,18 @@ class OracleModel:
         self.N = L.orc_nb_spectral_points(h)
         self.M = L.orc_nb_obs_points(h)
         self.P = L.orc_nb_parameters(h)
+
+    def close(self) -> None:
+        """Frees the model's tables and operators (several GB at the largest workload)."""
+        if getattr(self, "h", None):
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
     def grid(self) -> np.ndarray:
         out = np.empty(self.N)

@@ -160,3 +160,59 @@ def test_transmission_gradient_neglect_and_precision(case):
             _grad(e, phys)
     finally:
         e.set_precision(0)
+
+
+@pytest.fixture(scope="module")
+def odd_case():
+    """The transmission edge-case set (60 levels, 16469 points: an odd count, so pass 2b
+    reads single wavenumbers instead of pairs), fitted mean molecular weight, error
+    inflation and a 3-knot temperature profile; constant gravity (the transmission
+    gradient rejects variable gravity)."""
+    c = goldenlib.Case(os.path.join(goldenlib.GOLDEN_DIR, "transmission_edges.npz"))
+    text = c.config_text().replace("variable_gravity 1", "variable_gravity 0")
+    obs = c.observations()
+    e = Engine(text, obs)
+    om = oracle.OracleModel(text, obs)
+    assert e.N % 2 == 1
+    yield c, e, om
+    e.close()
+
+
+def test_transmission_gradient_odd_point_count(odd_case):
+    """Odd N, with and without the stored opacity terms, against the FP64 oracle's
+    Richardson differences (cut-off disabled)."""
+    c, e, om = odd_case
+    phys = np.array(c.params[:3], dtype=np.float64)
+    e.set_tau_cutoff(float("inf"))
+    om.set_tau_cutoff(float("inf"))
+    try:
+        ll_s, g_s, ng = _grad(e, phys)                       # opacity terms stored
+        per_eval_without_terms = 60 * e.N * 50                # ray data of one evaluation (60 levels)
+        e.set_gradient_memory(int(2.4 * per_eval_without_terms))  # too small to store the terms
+        try:
+            ll_r, g_r, _ = _grad(e, phys)                    # opacity terms recomputed
+        finally:
+            e.set_gradient_memory(0)
+        assert np.array_equal(ll_s, ll_r) and np.array_equal(g_s, g_r)
+        worst = 0.0
+        for i in range(len(phys)):
+            assert not ng[i]
+            x = phys[i]
+            assert abs(ll_s[i] - om.loglike(x)) <= 1e-8 + 1e-12 * abs(ll_s[i])
+            d1 = np.array([_fd(om.loglike, x, j, 1e-5) for j in range(len(x))])
+            d2 = np.array([_fd(om.loglike, x, j, 5e-6) for j in range(len(x))])
+            fd = (4 * d2 - d1) / 3
+            sa, sf = x * g_s[i], x * fd
+            scale = np.max(np.abs(sf))
+            for j in range(len(x)):
+                err = abs(sa[j] - sf[j])
+                if j == 12:  # cloud-top pressure (held-fixed cloud layers): zero
+                    assert g_s[i][j] == 0.0
+                    continue
+                tol = 1e-6 * abs(sf[j]) + 1e-8 * scale + 2e-10 * abs(ll_s[i]) / 1e-5
+                assert err <= tol, (i, j, sa[j], sf[j], err, tol)
+                worst = max(worst, err / max(abs(sf[j]), 1e-300))
+        _record("odd_point_count_fd_worst_rel_err", worst)
+    finally:
+        e.set_tau_cutoff(10.0)
+        om.set_tau_cutoff(10.0)

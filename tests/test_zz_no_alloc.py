@@ -1,8 +1,9 @@
 """The allocation-free single-evaluation entry point, bear_loglike_noalloc.
 
-It exists for callers that must not allocate device memory while a likelihood
-is evaluated (inside a CUDA stream capture, under another framework's memory
-pool, in a per-point sampler callback). Its work buffers live in a fixed device
+It exists for host applications that cannot call cudaMalloc while a likelihood
+is evaluated: their device memory belongs to another framework's pool or to a
+fixed budget set at start-up, or they evaluate from a per-point sampler callback
+that must not block in the allocator. Its work buffers live in a fixed device
 array instead of the model's growable workspace. This file is collected last so
 that a run stopping at the first failure has run every other test first; it
 also passes on its own in a fresh process (the array's address is looked up on
@@ -38,17 +39,31 @@ def test_noalloc_matches_plain_loglike(name):
     stream = torch.cuda.current_stream().cuda_stream
     ll = torch.empty(1, dtype=torch.float64, device="cuda")
     ng = torch.empty(1, dtype=torch.uint8, device="cuda")
-    # two calls in a row on the shared scratch array, then the neglected parameter set
-    for i in (0, 1, len(case.params) - 1):
-        p = torch.tensor(case.params[i], dtype=torch.float64, device="cuda")
+    # two calls in a row on the shared scratch array, then the neglected parameter set;
+    # all device buffers exist before the first call
+    rows = (0, 1, len(case.params) - 1)
+    params = [torch.tensor(case.params[i], dtype=torch.float64, device="cuda") for i in rows]
+    got = []
+    free_after_first = model_bytes_after_first = None
+    for n, p in enumerate(params):
         ll.fill_(0.0)
         rc = _noalloc(eng, p, ll, ng, stream)
         assert rc == 0, _lib.load().bear_last_error().decode()
         torch.cuda.synchronize()
+        got.append((ll.item(), bool(ng.item())))
+        if n == 0:
+            # the first call on a device may load the library's device code (which holds
+            # the scratch array); every later call must leave device memory as it is
+            free_after_first = torch.cuda.mem_get_info()[0]
+            model_bytes_after_first = eng.device_bytes()
+        else:
+            assert torch.cuda.mem_get_info()[0] == free_after_first, "device memory changed across a call"
+            assert eng.device_bytes() == model_bytes_after_first, "the model's workspace grew"
+    for i, (value, neglect) in zip(rows, got):
         expected = eng.loglike(case.params[i])           # the existing entry point
-        assert bool(ng.item()) == bool(case.arrays["ref_neglect"][i])
-        assert abs(ll.item() - expected) <= 1e-8, (i, ll.item(), expected)
-        assert abs(ll.item() - case.arrays["ref_loglike"][i]) <= 1e-8 + 1e-12 * abs(expected)
+        assert neglect == bool(case.arrays["ref_neglect"][i])
+        assert abs(value - expected) <= 1e-8, (i, value, expected)
+        assert abs(value - case.arrays["ref_loglike"][i]) <= 1e-8 + 1e-12 * abs(expected)
     eng.close()
 
 
