@@ -87,3 +87,25 @@ def run_case(case_dir: str, repeat: int = 0, threads: int = 0) -> dict:
             out["seconds_per_eval"] = float(line.split()[1])
     out["stdout"] = res.stdout
     return out
+
+
+def run_priors(case_dir: str, config_text: str, observations, priors, cube: np.ndarray) -> dict:
+    """Retrieval::convertCubeParameters of the reference (harness --priors) for every row
+    of ``cube`` with the given prior list (bear_gb300.config.Prior: type, description,
+    parameter, unit) on the model of ``config_text`` / ``observations``."""
+    cube = np.atleast_2d(np.asarray(cube, dtype=np.float64))
+    write_case(case_dir, config_text, observations, cube)
+    with open(os.path.join(case_dir, "priors.txt"), "w") as f:
+        for p in priors:
+            vals = " ".join(repr(float(x)) for x in p.parameter)
+            f.write(f"{p.type} {p.description.replace(' ', '_')} {p.unit or '-'} {len(p.parameter)} {vals}\n")
+    with open(os.path.join(case_dir, "cube.txt"), "w") as f:
+        f.write(f"{cube.shape[1]} {cube.shape[0]}\n")
+        for row in cube:
+            f.write(" ".join(repr(float(x)) for x in row) + "\n")
+    res = subprocess.run([HARNESS, case_dir, "--priors"], capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"reference harness failed ({res.returncode}):\n{res.stdout[-3000:]}\n{res.stderr[-3000:]}")
+    S, P = cube.shape
+    return {"parameter": np.fromfile(os.path.join(case_dir, "ref_prior_parameter.bin"), dtype=np.float64).reshape(S, P),
+            "physical": np.fromfile(os.path.join(case_dir, "ref_prior_physical.bin"), dtype=np.float64).reshape(S, P)}

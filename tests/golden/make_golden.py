@@ -2,7 +2,9 @@
 CPU path (oracle/_ref/bear_ref_harness, built from the reference sources by
 oracle/ref/Makefile) on seeded synthetic inputs.
 
-    make -C oracle/ref && python tests/golden/make_golden.py
+    make -C oracle/ref REF=<reference sources> && python tests/golden/make_golden.py [case ...]
+
+The prior-transform case (tests/golden/priors.npz) is made with the argument "priors".
 
 Each case: tables from bear_gb300.synthetic (regenerated at test time), a
 config-text template, observations whose data are the reference model at a
@@ -78,9 +80,55 @@ def same(t):
     return t
 
 
+# prior list of the prior-transform case: one per parameter of the emission edge-case model
+# (log g, f, distance, H2O, CO, K, T, cloud tau, cloud top, bottom factor, shift, error
+# exponent), every type but the Gaussian (the reference's erf_inv comes from Boost.Math,
+# which is not in the image) and every unit; linked priors give the 1-based index they follow
+PRIOR_CASE = [
+    ("uniform", "log_g", [5.5, 4.5], ""),            # reversed bounds: swapped by the reference
+    ("log_uniform", "scaling_f", [0.5, 2.0], "Rs"),
+    ("delta", "distance", [10.0], "pc"),
+    ("log_uniform", "H2O", [1e-8, 1e-2], ""),
+    ("linked", "CO", [4.0], ""),                     # follows H2O's cube coordinate
+    ("log_uniform", "K", [1e-5, 1e-9], "Me"),        # reversed bounds
+    ("uniform", "T", [800.0, 2500.0], "Rj"),
+    ("uniform", "cloud_tau", [0.0, 10.0], "Mj"),
+    ("log_uniform", "cloud_top", [1e-3, 1.0], "Ms"),
+    ("linked", "bottom_factor", [7.0], ""),          # follows T's cube coordinate, without T's unit
+    ("uniform", "shift", [-1e-3, 1e-3], "ly"),
+    ("uniform", "error_exponent", [-40.0, -30.0], "Re"),
+]
+
+
+def make_priors():
+    """Retrieval::convertCubeParameters of the reference on seeded hypercube points (and the
+    corners 0, 1, 1/2) with PRIOR_CASE on the emission edge-case model."""
+    import json
+
+    from bear_gb300.config import Prior
+    from goldenlib import Case
+
+    base = Case(os.path.join(GOLDEN_DIR, "emission_edges.npz"))
+    pr = [Prior(t, d, list(p), u) for t, d, p, u in PRIOR_CASE]
+    P = len(pr)
+    cube = np.random.default_rng(20261212).uniform(size=(61, P))
+    cube = np.vstack([np.zeros(P), np.ones(P), np.full(P, 0.5), cube])
+    ref = refcase.run_priors(os.path.join("/tmp", "bear_golden_case_priors"), base.config_text(),
+                             base.observations(), pr, cube)
+    meta = {"base_case": "emission_edges", "priors": [list(x) for x in PRIOR_CASE]}
+    np.savez_compressed(os.path.join(GOLDEN_DIR, "priors.npz"), cube=cube, ref_parameter=ref["parameter"],
+                        ref_physical=ref["physical"],
+                        meta=np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8))
+
+
 def main():
     os.makedirs(GOLDEN_DIR, exist_ok=True)
     which = set(sys.argv[1:])
+
+    # prior transforms of the reference (the emission edge-case model must exist already)
+    if "priors" in which:
+        make_priors()
+        return
 
     # 1. plain emission, the 50-level / 6270-point benchmark workload
     if not which or "emission_plain" in which:

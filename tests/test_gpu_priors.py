@@ -101,3 +101,28 @@ def test_prior_errors(case):
     bad[3] = Prior("linked", "x", [len(pr) + 5])
     with pytest.raises(_lib.EngineError):
         e.set_priors(bad)                           # link out of range
+
+
+def test_device_transform_matches_the_reference_binary():
+    """bear_prior_transform_batch against Retrieval::convertCubeParameters of the reference
+    binary (tests/golden/priors.npz): uniform, log-uniform, delta and linked priors with
+    every unit, on the emission edge-case model (12 parameters), 64 hypercube points."""
+    import json
+    import os
+
+    import torch
+
+    z = np.load(os.path.join(goldenlib.GOLDEN_DIR, "priors.npz"))
+    meta = json.loads(bytes(z["meta"]).decode())
+    base = goldenlib.Case(os.path.join(goldenlib.GOLDEN_DIR, meta["base_case"] + ".npz"))
+    e = Engine(base.config_text(), base.observations())
+    try:
+        e.set_priors([Prior(t, d, p, u) for t, d, p, u in meta["priors"]])
+        dev = e.prior_transform_batch(torch.tensor(z["cube"], device="cuda")).cpu().numpy()
+    finally:
+        e.close()
+    ref = z["ref_physical"]
+    err = np.abs(dev - ref) / np.maximum(np.abs(ref), 1e-300)
+    # the log-uniform exponent a + u (b - a) is one FMA on the device: one rounding of it
+    # moves 10^x by ln(10) |x| 2^-53 relative (~2e-15 at x = -9)
+    assert err.max() < 1e-14, err.max()

@@ -48,3 +48,25 @@ def test_linked_prior_errors():
         Priors([Prior("uniform", "a", [0, 1]), Prior("linked", "b", [1]), Prior("linked", "c", [2])])
     with pytest.raises(ValueError, match="unknown"):
         Priors([Prior("cauchy", "a", [0, 1])])
+
+
+def _golden_priors():
+    import json
+    import os
+
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "priors.npz"))
+    meta = json.loads(bytes(z["meta"]).decode())
+    return [Prior(t, d, p, u) for t, d, p, u in meta["priors"]], z
+
+
+def test_host_transform_matches_the_reference_binary():
+    """Against Retrieval::convertCubeParameters of the reference itself
+    (tests/golden/priors.npz, made by tests/golden/make_golden.py priors): uniform,
+    log-uniform, delta and linked priors with every unit; the Gaussian prior is pinned only
+    to the published erfinv formula above, because the reference takes erf_inv from
+    Boost.Math, which is not available to build it here."""
+    pr, z = _golden_priors()
+    host = Priors(pr).cube_to_physical_batch(z["cube"])
+    ref = z["ref_physical"]
+    err = np.abs(host - ref) / np.maximum(np.abs(ref), 1e-300)
+    assert err.max() <= 4e-16, err.max()
