@@ -288,4 +288,48 @@ BGB_HD double exp_tang2048_f(double x, float xf, const double* tab) {
   return BGB_DMA(scaled, p, scaled);
 }
 
+// exp(-d) in FP64 for a double-float d with 0 <= d.hi <= 700, by Tang's method with the
+// table tab = 2^(j/2048): k = round(d 2048/ln2) is chosen in FP32 from d.hi (as in
+// exp_tang2048_f, |r| <= 0.75 ln2/2048), the reduced argument r = k ln2/2048 - d is formed as
+// a double-float from an error-free product and sum (ln2/2048 as the float pair
+// kLn2Over2048FHi + kLn2Over2048FLo) whose low part is rounded once, q = e^r - 1 =
+// r + r^2/2 + r^3/6 in double-float, and exp(-d) = 2^(-k/2048) (1 + q) with 2^(-k/2048) an
+// FP64 table value times 2^m: one conversion add and one FMA on the FP64 pipe. The rounding
+// of r's low part costs up to ~1e-14 d relative (~2^-47 d; d itself, a double-float product
+// of the layer depth, carries about as much); the polynomial's remainder is below r^4/24.
+// exp_neg_df_fp32 is the FP32 part (returns tf, the rounded index with its float shifter,
+// and q = qh + ql); exp_neg_df_finish the integer and FP64 part.
+BGB_HD void exp_neg_df_fp32(df2 d, float& tf, float& qh, float& ql) {
+  tf = BGB_FMA(d.hi, k2048OverLn2F, 12582912.0f);
+  const float kf = BGB_FSUB(tf, 12582912.0f);
+  const float p = BGB_FMUL(kf, kLn2Over2048FHi);
+  const float pe = BGB_FMA(kf, kLn2Over2048FHi, -p);  // k Ch = p + pe exactly
+  const df2 s = two_sum(p, -d.hi);
+  // the low parts (pe, d.lo ~ 2^-24 d) can reach a few percent of s.hi: renormalise
+  const df2 r = two_sum(s.hi, BGB_FADD(s.lo, BGB_FADD(pe, BGB_FMA(kf, kLn2Over2048FLo, -d.lo))));
+  const float rh = r.hi, rl = r.lo;
+  const float sq = BGB_FMUL(rh, rh);
+  const float sq_lo = BGB_FMA(BGB_FMUL(2.0f, rh), rl, BGB_FMA(rh, rh, -sq));  // r^2 = sq + sq_lo
+  const float t3 = BGB_FMUL(BGB_FMUL(sq, rh), 1.0f / 6.0f);
+  const df2 q1 = fast_two_sum(rh, BGB_FMUL(sq, 0.5f));
+  qh = q1.hi;
+  ql = BGB_FADD(q1.lo, BGB_FADD(rl, BGB_FMA(sq_lo, 0.5f, t3)));
+}
+
+BGB_HD double exp_neg_df_finish(float tf, float qh, float ql, const double* tab) {
+  const int K = 0x4B400000 - (int)bgb_float_as_uint(tf);  // -k
+  const int j = K & 2047;
+  const int m = K >> 11;  // floor(K / 2048)
+  const double T = tab[j];
+  const double S = bgb_ll_as_double(bgb_double_as_ll(T) + ((long long)m << 52));
+  const double q = f2d_bits(qh) + f2d_bits(ql);
+  return BGB_DMA(S, q, S);
+}
+
+BGB_HD double exp_neg_df(df2 d, const double* tab) {
+  float tf, qh, ql;
+  exp_neg_df_fp32(d, tf, qh, ql);
+  return exp_neg_df_finish(tf, qh, ql, tab);
+}
+
 }  // namespace bgb

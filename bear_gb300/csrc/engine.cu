@@ -43,6 +43,7 @@
 #include "model.h"
 #include "physics.cuh"
 #include "rt_common.cuh"
+#include "rt_pair.cuh"
 #include "star.cuh"
 
 namespace bgb {
@@ -100,7 +101,7 @@ __global__ void __launch_bounds__(256, 6) emission_kernel(DeviceModel dm, const 
   const df2 c1 = {c1f.x, c1f.y}, c2l = {c2f.x, c2f.y};
   auto planck = [&](int l) {
     const float2 it = __ldg(reinterpret_cast<const float2*>(&lv[l].invT_hi));
-    return planck_df(c1, c2l, df2{it.x, it.y}, et.hi, et.lo);
+    return planck_dd(c1, c2l, df2{it.x, it.y}, et.hi, et.lo);
   };
   auto kappa = [&](int l) {
     Kappa kp = level_kappa_df(dm.ltab, N, sf + (size_t)l * S, S, k, et);
@@ -118,34 +119,117 @@ __global__ void __launch_bounds__(256, 6) emission_kernel(DeviceModel dm, const 
   const double csh = (EXT && dm.cloud_kind) ? cloud_shape(dm, ev[b], k) : 1.0;
   const df2 csd = df_from_double(csh);
   Kappa kap_prev = kappa(0);
-  double B_prev = planck(0);
-  double J1 = 0.0, J2 = 0.0;  // I - B: the bottom boundary is I = B
+  PlanckD B_prev = planck(0);
+  double K1 = 0.0, K2 = 0.0;  // (I - B) / mu: the bottom boundary is I = B
   if (STORE) {
-    Is[0] = B_prev;
-    Is[N] = B_prev;
+    const double B0 = planck_value(B_prev);
+    Is[0] = B0;
+    Is[N] = B0;
   }
   for (int l = 1; l < L; ++l) {
     const Kappa kap = kappa(l);
-    const double B = planck(l);
-    double d1, d2, rtau;
+    const PlanckD B = planck(l);
     if (STORE) {
       float4 tk;
-      emission_layer_tau_df<EXT, true>(lv, l, kap, kap_prev, d1, d2, rtau, csh, csd, &tk);
+      emission_layer<EXT, true>(lv, l, kap, kap_prev, B, B_prev, K1, K2, tab2048, csh, csd, &tk);
       layer_store[((size_t)b * L + l) * N + k] = tk;
+      const double Bd = planck_value(B);
+      Is[(size_t)l * 2 * N] = fma(kMu[0], K1, Bd);
+      Is[(size_t)l * 2 * N + N] = fma(kMu[1], K2, Bd);
     } else {
-      emission_layer_tau_df<EXT>(lv, l, kap, kap_prev, d1, d2, rtau, csh, csd);
-    }
-    sc_layer_j(d1, d2, rtau, B, B_prev, J1, J2, tab2048);
-    if (STORE) {
-      Is[(size_t)l * 2 * N] = J1 + B;
-      Is[(size_t)l * 2 * N + N] = J2 + B;
+      emission_layer<EXT>(lv, l, kap, kap_prev, B, B_prev, K1, K2, tab2048, csh, csd);
     }
     kap_prev = kap;
     B_prev = B;
   }
-  const double I1 = J1 + B_prev, I2 = J2 + B_prev;
+  const double Bt = planck_value(B_prev);
+  const double I1 = fma(kMu[0], K1, Bt), I2 = fma(kMu[1], K2, Bt);
   const double flux = 2.0 * kPi * (I1 * kMu[0] * 0.5 + I2 * kMu[1] * 0.5) * 1e-3;
   spectrum[(size_t)b * N + k] = flux * __ldg(&ev[b].scaling);
+}
+
+// The same fused kernel with two wavenumbers per thread, k0 = 2 x (thread index) and
+// k0 + 1: the double-float opacity assembly, Planck function and layer recurrence of both
+// are issued as paired FP32 instructions (rt_pair.cuh), the FP64 steps run per
+// wavenumber. Each wavenumber's result is bit for bit emission_kernel<STORE>'s (with N odd,
+// the last thread's second element repeats k0 and is not written). Used for batches; models
+// with the H- continuum or a non-grey cloud use emission_kernel<false, true>.
+template <bool STORE>
+__global__ void __launch_bounds__(256, 2) emission_kernel_x2(DeviceModel dm, const LevelInfo* __restrict__ lev,
+                                                          const LevelSpeciesDF* __restrict__ lsdf,
+                                                          const EvalInfo* __restrict__ ev,
+                                                          double* __restrict__ spectrum, double* __restrict__ istore,
+                                                          float4* __restrict__ layer_store = nullptr) {
+  __shared__ ExpTables et;
+  __shared__ double tab2048[2048];
+  load_exp_tables(et);
+  for (int i = threadIdx.x; i < 2048; i += blockDim.x) tab2048[i] = kExp2TabD2048[i];
+  __syncthreads();
+  const int b = blockIdx.x;
+  const int k0 = 2 * (blockIdx.y * blockDim.x + threadIdx.x);
+  if (k0 >= dm.N) return;
+  const bool two = k0 + 1 < dm.N;
+  const int k1 = two ? k0 + 1 : k0;
+  const int L = dm.L, S = dm.S;
+  const size_t N = dm.N;
+  const LevelInfo* lv = lev + (size_t)b * L;
+  const LevelSpeciesDF* sf = lsdf + (size_t)b * L * S;
+  dfx c1, c2l;
+  {
+    const float2 a0 = __ldg(dm.planck_c1_df + k0), a1 = __ldg(dm.planck_c1_df + k1);
+    const float2 b0 = __ldg(dm.planck_c2l_df + k0), b1 = __ldg(dm.planck_c2l_df + k1);
+    c1 = {make_float2(a0.x, a1.x), make_float2(a0.y, a1.y)};
+    c2l = {make_float2(b0.x, b1.x), make_float2(b0.y, b1.y)};
+  }
+  auto inv_t = [&](int l) {
+    const float2 it = __ldg(reinterpret_cast<const float2*>(&lv[l].invT_hi));
+    return df2{it.x, it.y};
+  };
+  KappaX kap_prev = level_kappa_x(dm.ltab, N, sf, S, k0, k1, et);
+  PlanckX Bp = planck_x(c1, c2l, inv_t(0), et);
+  double K1[2] = {0.0, 0.0}, K2[2] = {0.0, 0.0};  // (I - B) / mu: the bottom boundary is I = B
+  double* Is0 = STORE ? istore + (size_t)b * L * 2 * N + k0 : nullptr;
+  double* Is1 = STORE ? istore + (size_t)b * L * 2 * N + k1 : nullptr;
+  if (STORE) {
+    const double B0 = planck_value(planck_get(Bp, 0)), B1 = planck_value(planck_get(Bp, 1));
+    Is0[0] = B0;
+    Is0[N] = B0;
+    if (two) {
+      Is1[0] = B1;
+      Is1[N] = B1;
+    }
+  }
+  for (int l = 1; l < L; ++l) {
+    const KappaX kap = level_kappa_x(dm.ltab, N, sf + (size_t)l * S, S, k0, k1, et);
+    const PlanckX B = planck_x(c1, c2l, inv_t(l), et);
+    if (STORE) {
+      float4 tk0, tk1;
+      emission_layer_x<true>(lv, l, kap, kap_prev, B, Bp, K1, K2, tab2048, &tk0, &tk1);
+      layer_store[((size_t)b * L + l) * N + k0] = tk0;
+      const double B0 = planck_value(planck_get(B, 0));
+      Is0[(size_t)l * 2 * N] = fma(kMu[0], K1[0], B0);
+      Is0[(size_t)l * 2 * N + N] = fma(kMu[1], K2[0], B0);
+      if (two) {
+        layer_store[((size_t)b * L + l) * N + k1] = tk1;
+        const double B1 = planck_value(planck_get(B, 1));
+        Is1[(size_t)l * 2 * N] = fma(kMu[0], K1[1], B1);
+        Is1[(size_t)l * 2 * N + N] = fma(kMu[1], K2[1], B1);
+      }
+    } else {
+      emission_layer_x(lv, l, kap, kap_prev, B, Bp, K1, K2, tab2048);
+    }
+    kap_prev = kap;
+    Bp = B;
+  }
+  const double scaling = __ldg(&ev[b].scaling);
+#pragma unroll
+  for (int e = 0; e < 2; ++e) {
+    if (e == 1 && !two) break;
+    const double Bt = planck_value(planck_get(Bp, e));
+    const double I1 = fma(kMu[0], K1[e], Bt), I2 = fma(kMu[1], K2[e], Bt);
+    const double flux = 2.0 * kPi * (I1 * kMu[0] * 0.5 + I2 * kMu[1] * 0.5) * 1e-3;
+    spectrum[(size_t)b * N + (e ? k1 : k0)] = flux * scaling;
+  }
 }
 
 // Validation path: every step in FP64 with the CUDA math library.
@@ -1180,10 +1264,17 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
   if (!m.transmission) {
     const int TB = rt > 0 ? rt : (batch == 1 ? 64 : 128);
     dim3 grid(batch, (dm.N + TB - 1) / TB);
+    // batches: two wavenumbers per thread (the single evaluation of the plain path keeps one
+    // per thread, which puts twice as many threads on its one spectrum)
+    const bool pair = batch >= 2;
+    const dim3 grid2(batch, (dm.N + 2 * TB - 1) / (2 * TB));
     const size_t hm_smem = m.hm ? (size_t)L * kHmTerms * sizeof(float2) : 0;
     if (taps && m.precision == 1)
       emission_kernel_fp64<true><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.ray_n, w.ev, w.spectrum, taps->istore);
-    else if (taps)  // the gradient rejects H- models
+    else if (taps && pair)  // the gradient rejects H- models
+      emission_kernel_x2<true><<<grid2, TB, 0, st>>>(dm, w.lev, w.lsdf, w.ev, w.spectrum, taps->istore,
+                                                     taps->em_layer);
+    else if (taps)
       emission_kernel<true><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.spectrum,
                                                 taps->istore, taps->em_layer);
     else if (m.precision == 1)
@@ -1191,6 +1282,8 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
     else if (m.hm || m.acfg.cloud_kind)
       emission_kernel<false, true><<<grid, TB, hm_smem, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev,
                                                              w.spectrum, nullptr);
+    else if (pair)
+      emission_kernel_x2<false><<<grid2, TB, 0, st>>>(dm, w.lev, w.lsdf, w.ev, w.spectrum, nullptr);
     else
       emission_kernel<false><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.spectrum, nullptr);
   } else if (m.annuli > 1) {

@@ -4,6 +4,7 @@ computed to 60 digits with mpmath and split into (hi, lo) pairs.
   2^(j/64), j = -32..32  as float pairs   (double-float exp2, Tang's table method)
   2^(j/2048), j = 0..2047 as doubles      (FP64 exp with a degree-3 polynomial)
   ln 2, log2 10, log2 e  as float pairs; ln2/2048 as a double pair (Cody-Waite)
+  ln2/2048               as a float pair (argument reduction in double-float)
 
 Run: python bear_gb300/csrc/gen_constants.py > bear_gb300/csrc/dfconst.h
 """
@@ -50,4 +51,6 @@ for name, val in (("Ln2", mpmath.log(2)), ("Log2_10", mpmath.log(10, 2)), ("Log2
 hi, lo = split_d(mpmath.log(2) / 2048)
 print(f"constexpr double kLn2Over2048Hi = {hi.hex()}, kLn2Over2048Lo = {lo.hex()};")
 print(f"constexpr double k2048OverLn2 = {float(2048 / mpmath.log(2)).hex()};")
+hi, lo = split_f(mpmath.log(2) / 2048)
+print(f"constexpr float kLn2Over2048FHi = {ff(hi)}, kLn2Over2048FLo = {ff(lo)};")
 print("}  // namespace bgb")

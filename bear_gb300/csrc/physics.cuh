@@ -27,6 +27,38 @@ BGB_HD double planck_df(df2 c1, df2 c2l, df2 invT, const float* tab_hi, const fl
   return df_to_double(df_mul(df_mul(c1, u), df_recip(d)));
 }
 
+// The Planck function of planck_df kept as a double-float for the emission recurrence,
+// which forms (B - B') / tau in double-float. tiny: u = exp(-h nu c / k T) < 2^-60, where
+// the double-float can leave the float range; then d holds B in FP64 (as planck_df returns
+// it) and the recurrence takes its FP64 path for the layers next to this level.
+struct PlanckD {
+  df2 v;
+  double d;
+  bool tiny;
+};
+
+BGB_HD PlanckD planck_dd(df2 c1, df2 c2l, df2 invT, const float* tab_hi, const float* tab_lo) {
+  const df2 y = df_neg(df_mul(c2l, invT));
+  int n;
+  const df2 m = df_exp2(y, n, tab_hi, tab_lo);  // u = m 2^n, n <= 0
+  PlanckD r;
+  if (n < -60) {
+    r.v = df2{0.0f, 0.0f};
+    r.d = df_to_double(df_mul(c1, m)) * pow2d(n);  // 1 - u == 1 at this precision
+    r.tiny = true;
+    return r;
+  }
+  const df2 u = df_ldexp(m, n);
+  const df2 d = df_sub(df_make(1.0f), u);
+  r.v = df_mul(df_mul(c1, u), df_recip(d));
+  r.d = 0.0;
+  r.tiny = false;
+  return r;
+}
+
+// B in FP64 (the value planck_df returns).
+BGB_HD double planck_value(const PlanckD& b) { return b.tiny ? b.d : df_to_double(b.v); }
+
 // The same Planck function returned as a double-float (values below the float
 // range flush to zero); used by the adjoint, whose arithmetic is double-float.
 BGB_HD df2 planck_df2(df2 c1, df2 c2l, df2 invT, const float* tab_hi, const float* tab_lo) {

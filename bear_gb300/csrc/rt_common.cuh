@@ -154,52 +154,11 @@ __device__ __forceinline__ double cloud_shape(const DeviceModel& dm, const EvalI
   return e.cs[3] / (e.cs[0] * pow(x, -e.cs[1]) + pow(x, 0.2));
 }
 
-// Optical depth of emission layer l (between levels l-1 and l),
-// dz (k_l + k_{l-1}) / 2 + cloud, and its reciprocal, in double-float; FP64 when
-// an opacity has a term outside the float range or the depth is outside the
-// comfortable float range.
-// SHAPE: the cloud depth is scaled by the non-grey cloud factor (csh, FP64, and its
-// double-float split csd).
-// OUT (gradient pass): tk receives the layer optical depth as a double-float (FP64 values
-// clamped to 1e37) and (k_l + k_{l-1}) / 2, as the adjoint uses them.
-// The per-angle optical depths delta_i = tau / mu_i as FP64 values of double-float products
-// (one conversion add each) and 1 / tau.
+// 1/mu_i of the Gauss angles as double-floats.
 constexpr float kInvMuF[2][2] = {{(float)(1.0 / 0.211324865405187),
                                   (float)(1.0 / 0.211324865405187 - (double)(float)(1.0 / 0.211324865405187))},
                                  {(float)(1.0 / 0.788675134594813),
                                   (float)(1.0 / 0.788675134594813 - (double)(float)(1.0 / 0.788675134594813))}};
-
-template <bool SHAPE = false, bool OUT = false>
-__device__ __forceinline__ void emission_layer_tau_df(const LevelInfo* __restrict__ lv, int l, const Kappa& kap,
-                                                      const Kappa& kap_prev, double& d1, double& d2, double& rtau,
-                                                      double csh = 1.0, df2 csd = df2{1.0f, 0.0f},
-                                                      float4* tk = nullptr) {
-  const float4 g = __ldg(reinterpret_cast<const float4*>(&lv[l - 1].dzh_hi));  // dzh, cloud
-  const df2 cl = SHAPE ? df_mul(df2{g.z, g.w}, csd) : df2{g.z, g.w};
-  const df2 t = df_add(df_mul(df2{g.x, g.y}, df_add(kap.v, kap_prev.v)), cl);
-  // both wide parts zero (+-0), tested on the bits to stay off the FP64 pipe
-  const bool narrow = ((__double_as_longlong(kap.wide) | __double_as_longlong(kap_prev.wide)) << 1) == 0;
-  if (narrow && t.hi > 1e-30f && t.hi < 1e30f) {
-    d1 = df_to_double(df_mul(t, df2{kInvMuF[0][0], kInvMuF[0][1]}));
-    d2 = df_to_double(df_mul(t, df2{kInvMuF[1][0], kInvMuF[1][1]}));
-    rtau = df_to_double(df_recip(t));
-    if (OUT) {
-      const df2 ksh = df_mul_f(df_add(kap.v, kap_prev.v), 0.5f);
-      *tk = make_float4(t.hi, t.lo, ksh.hi, ksh.lo);
-    }
-  } else {
-    const double ks = (df_to_double(kap.v) + kap.wide) + (df_to_double(kap_prev.v) + kap_prev.wide);
-    const double tau =
-        __ldg(&lv[l - 1].dz) * ks / 2. + (SHAPE ? __ldg(&lv[l - 1].cloud) * csh : __ldg(&lv[l - 1].cloud));
-    d1 = tau * kInvMu[0];
-    d2 = tau * kInvMu[1];
-    rtau = 1.0 / tau;
-    if (OUT) {
-      const df2 td = df_from_double(fmin(tau, 1e37)), kd = df_from_double(fmin(0.5 * ks, 1e37));
-      *tk = make_float4(td.hi, td.lo, kd.hi, kd.lo);
-    }
-  }
-}
 
 // One layer of the two-angle short-characteristics recurrence
 // (ShortCharacteristics::calcSpectrum src/radiative_transfer/short_characteristics.cpp:85-115):
@@ -219,32 +178,89 @@ __device__ __forceinline__ void sc_layer(double tau, double B, double B_prev, do
   }
 }
 
-// The same layer in fewer FP64 operations, used by the default kernel, carried as
-// J = I - B (the intensity less the source function of the level just passed):
-// I = a (I' - B') + B + q (B - B'), q = (a - 1) / delta, becomes J = a J' + (a - 1) w with
-// w = mu u, u = (B - B') / tau (shared by the angles): four FP64 operations per angle.
-// (a - 1) w is rounded as the reference rounds q (B - B'); in particular a layer thin
-// enough that a rounds to 1 leaves J unchanged, as the reference leaves I - B.
-// delta_i = tau / mu_i and 1 / tau come from the caller (double-float products); the
-// exponential (exp_tang2048_f, table index chosen in FP32; tab2048 = 2^(j/2048)) and
-// the recurrence are FP64. An exactly transparent layer (tau == 0) is skipped as in the
-// reference: I stays, so J moves by B' - B.
-__device__ __forceinline__ void sc_layer_j(double d1, double d2, double rtau, double B, double B_prev, double& J1,
-                                           double& J2, const double* tab2048) {
-  if ((__double_as_longlong(d1) << 1) == 0) {  // tau == 0 (bit test)
-    const double s = B_prev - B;
-    J1 += s;
-    J2 += s;
+// The FP64 form of emission_layer below (the CUDA-free table exponential exp_tang2048):
+// layers with an opacity term outside the float range or a depth outside the comfortable
+// float range, layers next to a level whose Planck function is below the float range, and
+// exactly transparent layers (tau == 0, which the reference skips: I stays, so K_i moves by
+// (B' - B) / mu_i). tau_df: tau as the double-float path formed it (when `narrow`).
+template <bool SHAPE, bool OUT>
+__device__ __noinline__ void emission_layer_fp64(const LevelInfo* __restrict__ lv, int l, const Kappa& kap,
+                                                 const Kappa& kap_prev, bool narrow, df2 tau_df, df2 ks,
+                                                 double B, double Bp, double& K1, double& K2,
+                                                 const double* tab2048, double csh, float4* tk) {
+  double tau;
+  if (narrow) {
+    tau = df_to_double(tau_df);
+    if (OUT) {
+      const df2 ksh = df_mul_f(ks, 0.5f);
+      *tk = make_float4(tau_df.hi, tau_df.lo, ksh.hi, ksh.lo);
+    }
+  } else {
+    const double ks64 = (df_to_double(kap.v) + kap.wide) + (df_to_double(kap_prev.v) + kap_prev.wide);
+    tau = __ldg(&lv[l - 1].dz) * ks64 / 2. + (SHAPE ? __ldg(&lv[l - 1].cloud) * csh : __ldg(&lv[l - 1].cloud));
+    if (OUT) {
+      const df2 td = df_from_double(fmin(tau, 1e37)), kd = df_from_double(fmin(0.5 * ks64, 1e37));
+      *tk = make_float4(td.hi, td.lo, kd.hi, kd.lo);
+    }
+  }
+  if (tau == 0) {  // the reference skips exactly transparent layers only
+    const double dB = Bp - B;
+    K1 += dB * kInvMu[0];
+    K2 += dB * kInvMu[1];
     return;
   }
-  const double u = (B - B_prev) * rtau;
+  const double u = (B - Bp) * (1.0 / tau);
 #pragma unroll
   for (int i = 0; i < 2; ++i) {
-    const double d = i == 0 ? d1 : d2;
-    const double a = __double_as_longlong(d) > kBits700 ? 0.0 : exp_tang2048_f(-d, -d2f_trunc(d), tab2048);
-    const double w = kMu[i] * u;
-    double& J = i == 0 ? J1 : J2;
-    J = fma(a, J, (a - 1.0) * w);
+    const double d = tau * kInvMu[i];
+    const double a = __double_as_longlong(d) > kBits700 ? 0.0 : exp_tang2048(-d, tab2048);
+    double& K = i == 0 ? K1 : K2;
+    K = fma(a, K, fma(a, u, -u));
+  }
+}
+
+// One emission layer (between levels l-1 and l) of the two-angle short-characteristics
+// recurrence, carried as K_i = (I_i - B) / mu_i, B the Planck function of the level just
+// passed:
+//   K_i <- a_i K_i + (a_i - 1) u,   u = (B - B') / tau,   a_i = exp(-tau / mu_i),
+// which is ShortCharacteristics::calcSpectrum's update I <- I a + (1 + q) B + (-a - q) B'
+// with q = (a - 1) / delta (src/radiative_transfer/short_characteristics.cpp:85-115) with B
+// subtracted and divided by mu_i. tau = dz (kappa_l + kappa_{l-1}) / 2 + cloud, 1 / tau, u
+// and the angles' depths tau / mu_i are double-floats, a_i comes from exp_neg_df, and
+// (a_i - 1) u is one FMA (a_i u - u, rounded once; a_i == 1 leaves K_i unchanged, as the
+// reference leaves I - B): nine FP64 operations per layer (u's conversion; per angle the
+// conversion add and FMA of exp_neg_df and two FMAs). Other layers take emission_layer_fp64.
+// SHAPE: the cloud depth is scaled by the non-grey cloud factor (csh, FP64, and its
+// double-float split csd). OUT (gradient pass): tk receives tau and (k_l + k_{l-1}) / 2 as
+// double-floats (FP64 values clamped to 1e37), which the adjoint sweep reads back.
+template <bool SHAPE = false, bool OUT = false>
+__device__ __forceinline__ void emission_layer(const LevelInfo* __restrict__ lv, int l, const Kappa& kap,
+                                               const Kappa& kap_prev, const PlanckD& B, const PlanckD& Bp,
+                                               double& K1, double& K2, const double* tab2048, double csh = 1.0,
+                                               df2 csd = df2{1.0f, 0.0f}, float4* tk = nullptr) {
+  const float4 g = __ldg(reinterpret_cast<const float4*>(&lv[l - 1].dzh_hi));  // dzh, cloud
+  const df2 cl = SHAPE ? df_mul(df2{g.z, g.w}, csd) : df2{g.z, g.w};
+  const df2 ks = df_add(kap.v, kap_prev.v);
+  const df2 t = df_add(df_mul(df2{g.x, g.y}, ks), cl);
+  // both wide parts zero (+-0), tested on the bits to stay off the FP64 pipe
+  const bool narrow = ((__double_as_longlong(kap.wide) | __double_as_longlong(kap_prev.wide)) << 1) == 0 &&
+                      t.hi > 1e-30f && t.hi < 1e30f;
+  if (!narrow || B.tiny || Bp.tiny) {
+    emission_layer_fp64<SHAPE, OUT>(lv, l, kap, kap_prev, narrow, t, ks, planck_value(B), planck_value(Bp), K1,
+                                    K2, tab2048, csh, tk);
+    return;
+  }
+  if (OUT) {
+    const df2 ksh = df_mul_f(ks, 0.5f);
+    *tk = make_float4(t.hi, t.lo, ksh.hi, ksh.lo);
+  }
+  const double u = df_to_double(df_mul(df_sub(B.v, Bp.v), df_recip(t)));
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const df2 d = df_mul(t, i == 0 ? df2{kInvMuF[0][0], kInvMuF[0][1]} : df2{kInvMuF[1][0], kInvMuF[1][1]});
+    const double a = d.hi > 700.0f ? 0.0 : exp_neg_df(d, tab2048);
+    double& K = i == 0 ? K1 : K2;
+    K = fma(a, K, fma(a, u, -u));
   }
 }
 

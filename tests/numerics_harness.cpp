@@ -16,7 +16,7 @@ int main() {
   std::mt19937_64 g(20261203);
   std::uniform_real_distribution<double> U(0.0, 1.0);
   double e_exp2 = 0, e_tang2048 = 0, e_pow10 = 0, e_planck = 0, e_expneg = 0, ulp2048 = 0;
-  double e_tang2048f = 0, ulp2048f = 0;
+  double e_tang2048f = 0, ulp2048f = 0, e_negdf_scaled = 0, ulp_negdf = 0;
   for (int i = 0; i < 2000000; ++i) {
     // double-float 2^y over the exponent range of the opacity terms
     const double y = -140.0 + 180.0 * U(g);
@@ -38,6 +38,24 @@ int main() {
     e_tang2048f = std::fmax(e_tang2048f, (double)fabsl(bf / rx - 1));
     if (x >= -40.0)  // a >= 4e-18: the range where a's last bits can reach the intensities
       ulp2048f = std::fmax(ulp2048f, (double)fabsl(((long double)bf - rx) / (std::nextafter(rd, 1e308) - rd)));
+    // exp(-d) in FP64 from a double-float d (the recurrence's a = exp(-tau/mu)), against the
+    // exact exponential of the double-float input: the reduction rounds its low part once, an
+    // error ~1e-14 d relative (about what d carries as a double-float product); thin layers, where
+    // a - 1 is what matters, are oversampled and held to the ulp
+    {
+      double xd = 40.0 * U(g);
+      if (i % 3 == 0) xd = 1e-3 * U(g);
+      if (i % 7 == 0) xd = 40.0 + 660.0 * U(g);
+      const df2 dd = df_from_double(xd);
+      const double ad = exp_neg_df(dd, kExp2TabD2048);
+      const long double ra = expl(-((long double)dd.hi + (long double)dd.lo));
+      const double rel = (double)fabsl(ad / ra - 1);
+      e_negdf_scaled = std::fmax(e_negdf_scaled, rel / std::fmax(xd, 1.0));
+      if (xd < 1e-3) {
+        const double rr = (double)ra;
+        ulp_negdf = std::fmax(ulp_negdf, (double)fabsl(((long double)ad - ra) / (std::nextafter(rr, 1e308) - rr)));
+      }
+    }
     // double-float exp(-d) of the adjoint
     const double d = 60.0 * U(g);
     const df2 en = df_exp_neg(df_from_double(d), kExp2TabHi, kExp2TabLo);
@@ -133,8 +151,9 @@ int main() {
   std::printf("df_exp2 %.3e\nexp_tang2048 %.3e\nexp_tang2048_ulp %.3f\ndf_exp_neg %.3e\n"
               "df_pow10 %.3e\nplanck_df %.3e\nconversion_mismatches %lld\nexp_tang2048_f %.3e\n"
               "exp_tang2048_f_ulp %.3f\nd2f_trunc %.3e\ndf_exp2_edge_failures %lld\ndf_recip %.3e\n"
-              "df_from_double_bits %.3e\ndf_from_double_bits_failures %lld\n",
+              "df_from_double_bits %.3e\ndf_from_double_bits_failures %lld\n"
+              "exp_neg_df_per_d %.3e\nexp_neg_df_thin_ulp %.3f\n",
               e_exp2, e_tang2048, ulp2048, e_expneg, e_pow10, e_planck, conv_mismatch, e_tang2048f,
-              ulp2048f, e_trunc, edge_bad, e_recip, e_split, split_fallback_bad);
+              ulp2048f, e_trunc, edge_bad, e_recip, e_split, split_fallback_bad, e_negdf_scaled, ulp_negdf);
   return 0;
 }

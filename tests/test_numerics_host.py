@@ -17,6 +17,9 @@ against long-double references over the argument ranges the kernels use:
 * df_from_double_bits: FP64 value split into a double-float with integer operations
   (the adjoint's stored intensities), identical to df_from_double outside its range;
 * df_exp_neg: the double-float exp(-delta) of the adjoint;
+* exp_neg_df: the FP64 exp(-delta) of the recurrence from a double-float delta (argument
+  reduction in double-float, one FP64 conversion add and FMA), relative error per unit of
+  delta (the reduction's low part is rounded once: ~2^-47 delta) and ulp for thin layers;
 * f2d_bits / i2d_bits: float and int to double built with integer operations
   (bit-identical to the conversions, checked on every exponent, zeros and subnormals).
 
@@ -47,6 +50,10 @@ BOUNDS = {
     "df_exp_neg": 1e-12,        # d <= 60
     "planck_df": 1e-11,         # x = h nu c / k T up to 690: ~x 2^-48 from the 48-bit exponent
     "conversion_mismatches": 0,  # float / int -> double on the integer pipe: bit-identical
+    "exp_neg_df_per_d": 1.5e-14,  # relative error / max(delta, 1), delta <= 700: the rounding of the
+                                  # reduced argument's low part (~2^-47 delta); the double-float delta
+                                  # (a product of the layer depth) carries about as much
+    "exp_neg_df_thin_ulp": 1.5,  # delta < 1e-3
 }
 
 
