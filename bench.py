@@ -77,11 +77,11 @@ CONFIG_RECORDS = (
     ("3_emission_adjoint", "emission_adjoint", 256, None),
     ("4_joint_large", "joint_large", 1024, None),
 )
-# FP64-pipe instructions per wavenumber and layer of emission_kernel, counted from the
-# source: the double-float -> double conversions of delta_1, delta_2, 1/tau and B_nu, one
-# FP64 add each (the float -> double steps run on the integer pipe); (B - B') / tau (2); per
-# Gauss angle exp_tang2048_f (6), mu u (1), a - 1 (1), (a - 1) w (1) and the update (1).
-EMISSION_FP64_OPS_PER_POINT_LAYER = 4 + 2 + 2 * (6 + 1 + 1 + 1 + 1)
+# FP64-pipe instructions per wavenumber and layer of the emission kernels' recurrence
+# (emission_layer), counted from the source: the conversion add of u = (B - B') / tau (formed
+# in double-float; the float -> double steps run on the integer pipe), and per Gauss angle
+# the conversion add and FMA of exp_neg_df, (a - 1) u as one FMA and the update FMA.
+EMISSION_FP64_OPS_PER_POINT_LAYER = 1 + 2 * (2 + 1 + 1)
 FLUSH_BYTES = 512 * 1024 * 1024
 
 
