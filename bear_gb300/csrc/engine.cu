@@ -154,8 +154,13 @@ __global__ void __launch_bounds__(256, 6) emission_kernel(DeviceModel dm, const 
 // wavenumber. Each wavenumber's result is bit for bit emission_kernel<STORE>'s (with N odd,
 // the last thread's second element repeats k0 and is not written). Used for batches; models
 // with the H- continuum or a non-grey cloud use emission_kernel<false, true>.
+// Launch bound: at most 128 threads per block and 8 resident blocks, which caps the kernel
+// at 64 registers (a few bytes spill): the kernel waits mostly on level-table reads from L2,
+// and 32 resident warps per SM hide them better than 24 at the 83 registers it would take
+// (measured 17.9 against 19.9 ms for the 512-evaluation batch).
+constexpr int kPairThreads = 128;
 template <bool STORE>
-__global__ void __launch_bounds__(256, 2) emission_kernel_x2(DeviceModel dm, const LevelInfo* __restrict__ lev,
+__global__ void __launch_bounds__(kPairThreads, 8) emission_kernel_x2(DeviceModel dm, const LevelInfo* __restrict__ lev,
                                                           const LevelSpeciesDF* __restrict__ lsdf,
                                                           const EvalInfo* __restrict__ ev,
                                                           double* __restrict__ spectrum, double* __restrict__ istore,
@@ -1267,12 +1272,13 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
     // batches: two wavenumbers per thread (the single evaluation of the plain path keeps one
     // per thread, which puts twice as many threads on its one spectrum)
     const bool pair = batch >= 2;
-    const dim3 grid2(batch, (dm.N + 2 * TB - 1) / (2 * TB));
+    const int TB2 = std::min(TB, kPairThreads);  // launch bound of the two-wavenumber kernel
+    const dim3 grid2(batch, (dm.N + 2 * TB2 - 1) / (2 * TB2));
     const size_t hm_smem = m.hm ? (size_t)L * kHmTerms * sizeof(float2) : 0;
     if (taps && m.precision == 1)
       emission_kernel_fp64<true><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.ray_n, w.ev, w.spectrum, taps->istore);
     else if (taps && pair)  // the gradient rejects H- models
-      emission_kernel_x2<true><<<grid2, TB, 0, st>>>(dm, w.lev, w.lsdf, w.ev, w.spectrum, taps->istore,
+      emission_kernel_x2<true><<<grid2, TB2, 0, st>>>(dm, w.lev, w.lsdf, w.ev, w.spectrum, taps->istore,
                                                      taps->em_layer);
     else if (taps)
       emission_kernel<true><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.spectrum,
@@ -1283,7 +1289,7 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
       emission_kernel<false, true><<<grid, TB, hm_smem, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev,
                                                              w.spectrum, nullptr);
     else if (pair)
-      emission_kernel_x2<false><<<grid2, TB, 0, st>>>(dm, w.lev, w.lsdf, w.ev, w.spectrum, nullptr);
+      emission_kernel_x2<false><<<grid2, TB2, 0, st>>>(dm, w.lev, w.lsdf, w.ev, w.spectrum, nullptr);
     else
       emission_kernel<false><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.spectrum, nullptr);
   } else if (m.annuli > 1) {
