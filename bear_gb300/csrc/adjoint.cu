@@ -45,6 +45,7 @@
 #include "level_physics.cuh"
 #include "model.h"
 #include "rt_common.cuh"
+#include "dfloat2x.cuh"
 #include "star.cuh"
 
 namespace bgb {
@@ -648,6 +649,7 @@ struct SinkArgs {
 };
 
 constexpr int kSinkKPT = 4;  // wavenumbers per thread of the sink kernel
+constexpr int kSinkGrp = 2;  // species whose table reads the sink kernel issues together
 
 template <int VP>
 __global__ void __launch_bounds__(kAdjThreads) emission_adjoint_sinks_kernel(DeviceModel dm, SinkArgs a) {
@@ -667,60 +669,98 @@ __global__ void __launch_bounds__(kAdjThreads) emission_adjoint_sinks_kernel(Dev
   df2 acc[VP];
 #pragma unroll
   for (int j = 0; j < VP; ++j) acc[j] = z;
+  // the thread's wavenumbers in pairs (j, j + 1) = (ka, ka + kAdjThreads): the species terms
+  // and slopes of both are formed with paired FP32 instructions (dfloat2x.cuh, per element bit
+  // for bit the single-wavenumber arithmetic), and each accumulator receives the pair's
+  // contributions in wavenumber order, as one wavenumber per step would add them
 #pragma unroll 1
-  for (int j = 0; j < kSinkKPT; ++j) {
-    const int k = (blockIdx.z * kSinkKPT + j) * kAdjThreads + tid;
-    if (k >= dm.N) break;
-    const float2 gk = gKl[k];
-    if (gk.x == 0.0f) continue;
-    const df2 gK = {gk.x, gk.y};
-    double gK64 = 0.0;
-    df2 dk = z;
-    double dkw = 0.0;
-    // species in groups of four: a group's table reads are issued before its arithmetic
+  for (int j = 0; j < kSinkKPT; j += 2) {
+    const int ka = (blockIdx.z * kSinkKPT + j) * kAdjThreads + tid;
+    if (ka >= dm.N) break;
+    const bool hb = ka + kAdjThreads < dm.N;
+    const int kb = hb ? ka + kAdjThreads : ka;
+    const float2 gka = gKl[ka];
+    const float2 gkb = hb ? gKl[kb] : make_float2(0.0f, 0.0f);
+    const bool use_a = gka.x != 0.0f, use_b = gkb.x != 0.0f;  // zero seeds add nothing
+    if (!use_a && !use_b) continue;
+    const df2 gKa = {gka.x, gka.y}, gKb = {gkb.x, gkb.y};
+    double gK64a = 0.0, gK64b = 0.0;
+    dfx dk = {f2(0.0f), f2(0.0f)};
+    double dkwa = 0.0, dkwb = 0.0;
+    // species in groups of kSinkGrp: a group's table reads are issued before its arithmetic
 #pragma unroll
-    for (int s0 = 0; s0 < VP - 1; s0 += 4) {
+    for (int s0 = 0; s0 < VP - 1; s0 += kSinkGrp) {
       if (s0 >= S) break;
-      float2 t0[4], t1[4];
+      float2 t0a[kSinkGrp], t0b[kSinkGrp], t1a[kSinkGrp], t1b[kSinkGrp];
 #pragma unroll
-      for (int g = 0; g < 4; ++g) {
+      for (int g = 0; g < kSinkGrp; ++g) {
         const int s = s0 + g;
         if (s >= S || s >= VP - 1) break;
         const int4 rw = __ldg(reinterpret_cast<const int4*>(sf + s));
-        t0[g] = __ldg(dm.ltab + (size_t)rw.x * N + k);
-        t1[g] = __ldg(dm.ltab + (size_t)rw.y * N + k);
+        const float2* r0 = dm.ltab + (size_t)rw.x * N;
+        const float2* r1 = dm.ltab + (size_t)rw.y * N;
+        t0a[g] = __ldg(r0 + ka);
+        t0b[g] = __ldg(r0 + kb);
+        t1a[g] = __ldg(r1 + ka);
+        t1b[g] = __ldg(r1 + kb);
       }
 #pragma unroll
-      for (int g = 0; g < 4; ++g) {
+      for (int g = 0; g < kSinkGrp; ++g) {
         const int s = s0 + g;
         if (s >= S || s >= VP - 1) break;
         // species term 2^y of the level opacity (level_kappa_df_cb) and its temperature slope
         const float4 fb = __ldg(reinterpret_cast<const float4*>(sf + s) + 1);  // wT, log2 n
         if (fb.z == kNoSpecies) continue;
-        const df2 lo = {t0[g].x, t0[g].y}, hi = {t1[g].x, t1[g].y};
+        const dfx lo = {make_float2(t0a[g].x, t0b[g].x), make_float2(t0a[g].y, t0b[g].y)};
+        const dfx hi = {make_float2(t1a[g].x, t1b[g].x), make_float2(t1a[g].y, t1b[g].y)};
         // lo + (hi - lo) wT + log2 n, as the forward pass forms it (level_kappa_df_cb)
-        const df2 diff = df_sub(hi, lo);
-        const df2 y = df_fma(diff, df2{fb.x, fb.y}, df_add(lo, df2{fb.z, fb.w}));
-        int n;
-        const df2 m = df_exp2(y, n, et.hi, et.lo);
+        const dfx diff = dfx_sub(hi, lo);
+        const dfx y = dfx_fma(diff, dfx_bcast(df2{fb.x, fb.y}), dfx_add(lo, dfx_bcast(df2{fb.z, fb.w})));
+        int2 n;
+        const dfx m = dfx_exp2(y, n, et.hi, et.lo);
         const float2 d = __ldg(dwl + s);
-        const bool narrow = n > -100 && n < 100;
-        const df2 slope = df_mul(diff, df2{d.x, d.y});
-        if (narrow) {
-          const df2 t = df_ldexp(m, n);
-          acc[s] = df_fma(gK, t, acc[s]);
-          if (d.x != 0.0f) dk = df_fma(t, slope, dk);
+        const dfx slope = dfx_mul(diff, dfx_bcast(df2{d.x, d.y}));
+        const bool nar_a = n.x > -100 && n.x < 100, nar_b = n.y > -100 && n.y < 100;
+        if (nar_a && nar_b) {
+          const dfx t = dfx_ldexp_normal(m, n);
+          if (use_a) acc[s] = df_fma(gKa, dfx_get(t, 0), acc[s]);
+          if (use_b) acc[s] = df_fma(gKb, dfx_get(t, 1), acc[s]);
+          if (d.x != 0.0f) dk = dfx_fma(t, slope, dk);
         } else {
-          const double tw = df_to_double(m) * pow2d(n);
-          if (gK64 == 0.0) gK64 = df_to_double(gK);
-          acc[s] = df_add(acc[s], df_from_double(gK64 * tw));
-          if (d.x != 0.0f) dkw += tw * df_to_double(slope);
+          // a term outside the float exponent range: the single-wavenumber steps per element
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            if (!(e ? use_b : use_a)) continue;
+            const df2 me = dfx_get(m, e), se = dfx_get(slope, e), gKe = e ? gKb : gKa;
+            const int ne = e ? n.y : n.x;
+            if (ne > -100 && ne < 100) {
+              const df2 t = df_ldexp(me, ne);
+              acc[s] = df_fma(gKe, t, acc[s]);
+              if (d.x != 0.0f) {
+                const df2 dke = df_fma(t, se, dfx_get(dk, e));
+                (e ? dk.hi.y : dk.hi.x) = dke.hi;
+                (e ? dk.lo.y : dk.lo.x) = dke.lo;
+              }
+            } else {
+              const double tw = df_to_double(me) * pow2d(ne);
+              double& g64 = e ? gK64b : gK64a;
+              if (g64 == 0.0) g64 = df_to_double(gKe);
+              acc[s] = df_add(acc[s], df_from_double(g64 * tw));
+              if (d.x != 0.0f) (e ? dkwb : dkwa) += tw * df_to_double(se);
+            }
+          }
         }
       }
     }
     // opacity part of d log L / dT: gK d kappa / dT (level-table values are log2: d 2^y / dy = 2^y ln 2)
-    acc[VP - 1] = df_add(acc[VP - 1], df_mul(gK, df_mul(dk, df2{kLn2Hi, kLn2Lo})));
-    if (dkw != 0.0) acc[VP - 1] = df_add(acc[VP - 1], df_from_double(df_to_double(gK) * dkw * 0.693147180559945309));
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      if (!(e ? use_b : use_a)) continue;
+      const df2 gKe = e ? gKb : gKa;
+      acc[VP - 1] = df_add(acc[VP - 1], df_mul(gKe, df_mul(dfx_get(dk, e), df2{kLn2Hi, kLn2Lo})));
+      const double dkw = e ? dkwb : dkwa;
+      if (dkw != 0.0) acc[VP - 1] = df_add(acc[VP - 1], df_from_double(df_to_double(gKe) * dkw * 0.693147180559945309));
+    }
   }
   const df2 r = warp_reduce_scatter<VP>(acc, lane);
   if (lane % G == 0) red[warp][lane / G] = df_to_double(r);
