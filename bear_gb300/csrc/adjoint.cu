@@ -45,7 +45,7 @@
 #include "level_physics.cuh"
 #include "model.h"
 #include "rt_common.cuh"
-#include "dfloat2x.cuh"
+#include "rt_pair.cuh"
 #include "star.cuh"
 
 namespace bgb {
@@ -282,6 +282,85 @@ __device__ __forceinline__ void sc_layer_adjoint_df(df2 t, df2 rt, df2 B, df2 Bp
     const df2 gd = df_sub(df_mul(dq, df_mul(lam, dB)), df_mul(a, df_mul(lam, df_sub(Ip, Bp))));
     gtau = df_add(gtau, df_mul(gd, invmu));
     lam = df_mul(lam, a);
+  }
+}
+
+// ------------------------------------------------------------------ two wavenumbers per thread
+// The double-float steps above for two wavenumbers with paired FP32 instructions
+// (dfloat2x.cuh): element e of every result is bit for bit the single-wavenumber result for
+// element e's inputs.
+
+// planck_df2 (physics.cuh) per element, c1 and c2l per element, 1/T shared
+__device__ __forceinline__ dfx planck_dfx(dfx c1, dfx c2l, df2 invT, const ExpTables& et) {
+  const dfx y = dfx_neg(dfx_mul(c2l, dfx_bcast(invT)));
+  int2 n;
+  const dfx m = dfx_exp2(y, n, et.hi, et.lo);
+  if (n.x >= -60 && n.y >= -60) {
+    const dfx u = dfx_ldexp_normal(m, n);
+    const dfx d = dfx_sub(dfx_bcast(df_make(1.0f)), u);
+    return dfx_mul(dfx_mul(c1, u), dfx_recip(d));
+  }
+  dfx r;
+#pragma unroll
+  for (int e = 0; e < 2; ++e) {
+    const df2 me = dfx_get(m, e), c1e = dfx_get(c1, e);
+    const int ne = e ? n.y : n.x;
+    df2 v;
+    if (ne < -60) {
+      v = df_ldexp(df_mul(c1e, me), ne);
+    } else {
+      const df2 u = df_ldexp(me, ne);
+      v = df_mul(df_mul(c1e, u), df_recip(df_sub(df_make(1.0f), u)));
+    }
+    dfx_set(r, e, v);
+  }
+  return r;
+}
+
+// sc_layer_adjoint_df per element, both elements with a nonzero layer depth; rt is the
+// reciprocal depth where t.hi > 1e-30 and zero elsewhere. Where the elements fall on
+// different sides of delta = 1e-2, both branches are formed and each element keeps its own.
+__device__ __forceinline__ void sc_layer_adjoint_x(dfx t, dfx rt, dfx B, dfx Bp, dfx Ip1, dfx Ip2, dfx& lam1,
+                                                   dfx& lam2, dfx& gB, dfx& gBp, dfx& gtau, const ExpTables& et) {
+  const dfx dB = dfx_sub(B, Bp);
+  const dfx one = dfx_bcast(df_make(1.0f)), half = dfx_bcast(df_make(0.5f));
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const dfx invmu = dfx_bcast(i == 0 ? df2{kInvMuHi0, kInvMuLo0} : df2{kInvMuHi1, kInvMuLo1});
+    const dfx mu = dfx_bcast(i == 0 ? df2{kMuHi0, kMuLo0} : df2{kMuHi1, kMuLo1});
+    const dfx d = dfx_mul(t, invmu);
+    const dfx a = dfx_exp_neg(d, et.hi, et.lo);
+    const bool sm0 = d.hi.x < 1e-2f, sm1 = d.hi.y < 1e-2f;
+    const dfx z = {f2(0.0f), f2(0.0f)};
+    dfx s1 = z, nq = z, dq = z;
+    if (sm0 || sm1) {
+      const float2 dh = f2neg(d.hi);
+      const float2 p1 = f2fma(dh, f2fma(dh, f2(1.0f / 720.0f), f2(1.0f / 120.0f)), f2(1.0f / 24.0f));
+      dfx P = dfx_sub(dfx_bcast(df2{kSixthHi, kSixthLo}), dfx_mul_f(d, p1));
+      P = dfx_sub(half, dfx_mul(d, P));
+      s1 = dfx_mul(d, P);
+      const float2 p2 = f2fma(dh, f2fma(dh, f2(1.0f / 144.0f), f2(1.0f / 30.0f)), f2(0.125f));
+      const dfx Q = dfx_sub(dfx_bcast(df2{kThirdHi, kThirdLo}), dfx_mul_f(d, p2));
+      dq = dfx_sub(half, dfx_mul(d, Q));
+      nq = dfx_mul(d, dq);
+    }
+    if (!(sm0 && sm1)) {
+      const dfx rd = dfx_mul(rt, mu);  // 1 / delta
+      const dfx q = dfx_mul(dfx_sub(a, one), rd);
+      const dfx s1n = dfx_add(one, q);
+      const dfx nqn = dfx_neg(dfx_add(a, q));
+      const dfx dqn = dfx_mul(nqn, rd);
+      s1 = dfx_select(sm0, sm1, s1, s1n);
+      nq = dfx_select(sm0, sm1, nq, nqn);
+      dq = dfx_select(sm0, sm1, dq, dqn);
+    }
+    dfx& lam = i == 0 ? lam1 : lam2;
+    const dfx Ip = i == 0 ? Ip1 : Ip2;
+    gB = dfx_add(gB, dfx_mul(lam, s1));
+    gBp = dfx_add(gBp, dfx_mul(lam, nq));
+    const dfx gd = dfx_sub(dfx_mul(dq, dfx_mul(lam, dB)), dfx_mul(a, dfx_mul(lam, dfx_sub(Ip, Bp))));
+    gtau = dfx_add(gtau, dfx_mul(gd, invmu));
+    lam = dfx_mul(lam, a);
   }
 }
 
@@ -529,7 +608,7 @@ __global__ void __launch_bounds__(kAdjThreads, DF ? 6 : 4) emission_adjoint_kern
 // The default gradient splits the emission adjoint in two kernels so that the
 // opacity recomputation and the per-level reductions run with full occupancy:
 //
-// emission_adjoint_sweep_kernel   one thread per (evaluation, wavenumber): the reverse
+// emission_adjoint_sweep_kernel   one thread per (evaluation, two wavenumbers): the reverse
 //     short-characteristics recurrence from the forward's stored intensities, layer
 //     optical depths and half opacity sums (so no opacities are recomputed here), the
 //     Planck function recomputed per level; writes d log L / d kappa of every level and
@@ -554,48 +633,65 @@ struct SweepArgs {
   int V, tiles_total;
 };
 
-__global__ void __launch_bounds__(kAdjThreads) emission_adjoint_sweep_kernel(DeviceModel dm, SweepArgs a) {
+// Two wavenumbers per thread: ka = tile 2 kAdjThreads + tid (element 0) and ka + kAdjThreads
+// (element 1), each with its own seed; an element past the grid repeats the last
+// wavenumber with a zero seed. The recurrence of each element is the single-wavenumber
+// double-float recurrence bit for bit; the block sums of the level sinks add the thread's
+// two elements first.
+// Five blocks per SM (96 registers, a few spilled): 55.7 ms for the gradient of 512
+// evaluations of 80 levels x 10257 points, against 56.7 ms at 128 registers and 58.7 ms
+// unbounded (152 registers, three blocks per SM).
+__global__ void __launch_bounds__(kAdjThreads, 5) emission_adjoint_sweep_kernel(DeviceModel dm, SweepArgs a) {
   constexpr int NW = kAdjThreads / 32;
   __shared__ ExpTables et;
   __shared__ double red[NW][4];
   load_exp_tables(et);
   __syncthreads();
-  const int S = dm.S, L = dm.L;
+  const int L = dm.L;
   const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int kk = blockIdx.y * kAdjThreads + tid;
-  const bool active = kk < dm.N;
-  const int k = active ? kk : dm.N - 1;  // idle lanes repeat the last wavenumber with a zero seed
   const size_t N = dm.N;
   const LevelInfo* lv = a.lev + (size_t)b * L;
-  const double* Is = a.istore + (size_t)b * L * 2 * N + k;
-  const float4* lay = a.layer + (size_t)b * L * N + k;
-  float2* gKo = a.gK + (size_t)b * L * N + k;
-
-  // seed: d log L / dF_k = sum_r W_rk gS_r, F = scaling 2 pi 1e-3 (mu1 I1 + mu2 I2) / 2
-  double gF = 0.0;
-  {
+  const double* Is[2];
+  const float4* lay[2];
+  float2* gKo[2];
+  bool act[2];
+  double sd[2];
+  dfx c1, c2l, c2, rc1;
+#pragma unroll
+  for (int e = 0; e < 2; ++e) {
+    const int kk = blockIdx.y * 2 * kAdjThreads + e * kAdjThreads + tid;
+    act[e] = kk < dm.N;
+    const int k = act[e] ? kk : dm.N - 1;
+    Is[e] = a.istore + (size_t)b * L * 2 * N + k;
+    lay[e] = a.layer + (size_t)b * L * N + k;
+    gKo[e] = a.gK + (size_t)b * L * N + k;
+    // seed: d log L / dF_k = sum_r W_rk gS_r, F = scaling 2 pi 1e-3 (mu1 I1 + mu2 I2) / 2
+    double gF = 0.0;
     const double* g = a.gS + (size_t)b * dm.M;
     const int e1 = __ldg(&dm.col_ptr[k + 1]);
-    for (int e = __ldg(&dm.col_ptr[k]); e < e1; ++e) gF = fma(__ldg(&dm.col_w[e]), g[__ldg(&dm.col_row[e])], gF);
+    for (int j = __ldg(&dm.col_ptr[k]); j < e1; ++j) gF = fma(__ldg(&dm.col_w[j]), g[__ldg(&dm.col_row[j])], gF);
+    sd[e] = act[e] ? gF * a.seed[b * 3] * __ldg(&a.ev[b].scaling) * (kPi * 1e-3) : 0.0;
+    const float2 c1f = __ldg(dm.planck_c1_df + k), c2f = __ldg(dm.planck_c2l_df + k);
+    const df2 c1e = {c1f.x, c1f.y}, c2le = {c2f.x, c2f.y};
+    dfx_set(c1, e, c1e);
+    dfx_set(c2l, e, c2le);
+    dfx_set(c2, e, df_mul(c2le, df2{kLn2Hi, kLn2Lo}));  // h nu c / k
+    dfx_set(rc1, e, df_div(df_make(1.0f), c1e));
   }
-  const double sd = active ? gF * a.seed[b * 3] * __ldg(&a.ev[b].scaling) * (kPi * 1e-3) : 0.0;
-
-  const float2 c1f = __ldg(dm.planck_c1_df + k), c2f = __ldg(dm.planck_c2l_df + k);
-  const df2 c1 = {c1f.x, c1f.y}, c2l = {c2f.x, c2f.y};
-  const df2 c2 = df_mul(c2l, df2{kLn2Hi, kLn2Lo});  // h nu c / k
-  const df2 rc1 = df_div(df_make(1.0f), c1);
   auto invT = [&](int l) {
     const float2 it = __ldg(reinterpret_cast<const float2*>(&lv[l].invT_hi));
     return df2{it.x, it.y};
   };
+  const dfx one = dfx_bcast(df_make(1.0f));
   // dB/dT = B (1 + B / c1) x / T with x = c2 / T
-  auto dplanck = [&](int l, df2 B) {
-    const df2 it = invT(l);
-    return df_mul(df_mul(B, df_add(df_make(1.0f), df_mul(B, rc1))), df_mul(df_mul(c2, it), it));
+  auto dplanck = [&](int l, dfx B) {
+    const dfx it = dfx_bcast(invT(l));
+    return dfx_mul(dfx_mul(B, dfx_add(one, dfx_mul(B, rc1))), dfx_mul(dfx_mul(c2, it), it));
   };
-  // the three opacity-free sinks of level l, reduced over the block
-  auto emit3 = [&](int l, df2 gBT, df2 gdz, df2 gcl) {
-    df2 v[4] = {gBT, gdz, gcl, df2{0.0f, 0.0f}};
+  // the three opacity-free sinks of level l, the thread's two elements added, reduced over the block
+  auto emit3 = [&](int l, dfx gBT, dfx gdz, dfx gcl) {
+    df2 v[4] = {df_add(dfx_get(gBT, 0), dfx_get(gBT, 1)), df_add(dfx_get(gdz, 0), dfx_get(gdz, 1)),
+                df_add(dfx_get(gcl, 0), dfx_get(gcl, 1)), df2{0.0f, 0.0f}};
     const df2 r = warp_reduce_scatter<4>(v, lane);
     if ((lane & 7) == 0) red[warp][lane >> 3] = df_to_double(r);
     __syncthreads();
@@ -603,41 +699,65 @@ __global__ void __launch_bounds__(kAdjThreads) emission_adjoint_sweep_kernel(Dev
       double sum = 0.0;
 #pragma unroll
       for (int w = 0; w < NW; ++w) sum += red[w][tid];
-      a.partial[(((size_t)b * L + l) * a.V + S + tid) * a.tiles_total + blockIdx.y] = sum;
+      a.partial[(((size_t)b * L + l) * a.V + dm.S + tid) * a.tiles_total + blockIdx.y] = sum;
     }
     __syncthreads();
   };
 
   const df2 z = {0.0f, 0.0f};
-  df2 lam1 = df_from_double(sd * kMu[0]), lam2 = df_from_double(sd * kMu[1]);
-  df2 B_l = planck_df2(c1, c2l, invT(L - 1), et.hi, et.lo);
-  df2 gB_l = z, gK_l = z, gdz_l = z, gcl_l = z;
+  const dfx zx = dfx_bcast(z);
+  dfx lam1 = dfx_make(df_from_double(sd[0] * kMu[0]), df_from_double(sd[1] * kMu[0]));
+  dfx lam2 = dfx_make(df_from_double(sd[0] * kMu[1]), df_from_double(sd[1] * kMu[1]));
+  dfx B_l = planck_dfx(c1, c2l, invT(L - 1), et);
+  dfx gB_l = zx, gK_l = zx, gdz_l = zx, gcl_l = zx;
   for (int l = L - 1; l >= 1; --l) {
-    const df2 B_m = planck_df2(c1, c2l, invT(l - 1), et.hi, et.lo);
-    const float4 tk = lay[(size_t)l * N];
-    const df2 t = {tk.x, tk.y}, ksh = {tk.z, tk.w};
+    const dfx B_m = planck_dfx(c1, c2l, invT(l - 1), et);
+    const float4 ta = lay[0][(size_t)l * N], tb = lay[1][(size_t)l * N];
+    const dfx t = {make_float2(ta.x, tb.x), make_float2(ta.y, tb.y)};
+    const dfx ksh = {make_float2(ta.z, tb.z), make_float2(ta.w, tb.w)};
     const float2 gz = __ldg(reinterpret_cast<const float2*>(&lv[l - 1].dzh_hi));
-    const df2 dzh = {gz.x, gz.y};
-    df2 gB_m = z, gtau = z;
-    if (t.hi != 0.0f) {
-      const df2 rt = t.hi > 1e-30f ? df_recip(t) : z;  // only used above delta = 1e-2
-      const df2 Ip1 = df_from_double_bits(Is[(size_t)(l - 1) * 2 * N]);
-      const df2 Ip2 = df_from_double_bits(Is[(size_t)(l - 1) * 2 * N + N]);
-      sc_layer_adjoint_df(t, rt, B_l, B_m, Ip1, Ip2, lam1, lam2, gB_l, gB_m, gtau, et);
+    const dfx dzh = dfx_bcast(df2{gz.x, gz.y});
+    dfx gB_m = zx, gtau = zx;
+    const bool nz0 = t.hi.x != 0.0f, nz1 = t.hi.y != 0.0f;
+    if (nz0 || nz1) {
+      const size_t ip = (size_t)(l - 1) * 2 * N;
+      const dfx Ip1 = dfx_make(df_from_double_bits(Is[0][ip]), df_from_double_bits(Is[1][ip]));
+      const dfx Ip2 = dfx_make(df_from_double_bits(Is[0][ip + N]), df_from_double_bits(Is[1][ip + N]));
+      if (nz0 && nz1) {
+        // the reciprocal depth is only used above delta = 1e-2
+        const dfx rt = dfx_select(t.hi.x > 1e-30f, t.hi.y > 1e-30f, dfx_recip(t), zx);
+        sc_layer_adjoint_x(t, rt, B_l, B_m, Ip1, Ip2, lam1, lam2, gB_l, gB_m, gtau, et);
+      } else {
+        // one element's layer has zero depth (its sweep passes the layer unchanged): the
+        // single-wavenumber steps for the other
+        const int e = nz0 ? 0 : 1;
+        const df2 te = dfx_get(t, e);
+        const df2 rt = te.hi > 1e-30f ? df_recip(te) : z;
+        df2 l1 = dfx_get(lam1, e), l2 = dfx_get(lam2, e), gb = dfx_get(gB_l, e), gbm = z, gt = z;
+        sc_layer_adjoint_df(te, rt, dfx_get(B_l, e), dfx_get(B_m, e), dfx_get(Ip1, e), dfx_get(Ip2, e), l1, l2, gb,
+                            gbm, gt, et);
+        dfx_set(lam1, e, l1);
+        dfx_set(lam2, e, l2);
+        dfx_set(gB_l, e, gb);
+        dfx_set(gB_m, e, gbm);
+        dfx_set(gtau, e, gt);
+      }
     }
-    gK_l = df_add(gK_l, df_mul(gtau, dzh));
-    if (active) gKo[(size_t)l * N] = make_float2(gK_l.hi, gK_l.lo);
-    emit3(l, df_mul(gB_l, dplanck(l, B_l)), gdz_l, gcl_l);
+    gK_l = dfx_add(gK_l, dfx_mul(gtau, dzh));
+    if (act[0]) gKo[0][(size_t)l * N] = make_float2(gK_l.hi.x, gK_l.lo.x);
+    if (act[1]) gKo[1][(size_t)l * N] = make_float2(gK_l.hi.y, gK_l.lo.y);
+    emit3(l, dfx_mul(gB_l, dplanck(l, B_l)), gdz_l, gcl_l);
     // layer l's own sinks belong to lev[l-1] (its dz and cloud)
-    gdz_l = df_mul(gtau, ksh);
+    gdz_l = dfx_mul(gtau, ksh);
     gcl_l = gtau;
-    gK_l = df_mul(gtau, dzh);
+    gK_l = dfx_mul(gtau, dzh);
     gB_l = gB_m;
     B_l = B_m;
   }
-  gB_l = df_add(gB_l, df_add(lam1, lam2));  // both angles start from I = B at the bottom level
-  if (active) gKo[0] = make_float2(gK_l.hi, gK_l.lo);
-  emit3(0, df_mul(gB_l, dplanck(0, B_l)), gdz_l, gcl_l);
+  gB_l = dfx_add(gB_l, dfx_add(lam1, lam2));  // both angles start from I = B at the bottom level
+  if (act[0]) gKo[0][0] = make_float2(gK_l.hi.x, gK_l.lo.x);
+  if (act[1]) gKo[1][0] = make_float2(gK_l.hi.y, gK_l.lo.y);
+  emit3(0, dfx_mul(gB_l, dplanck(0, B_l)), gdz_l, gcl_l);
 }
 
 struct SinkArgs {
@@ -1036,9 +1156,10 @@ void launch_gradient(Model& m, const double* params_dev, int batch, cudaStream_t
   if (V > 32) throw Error(BEAR_ERR_UNSUPPORTED, "the gradient supports at most 29 table species");
   if (P > kAdjThreads) throw Error(BEAR_ERR_UNSUPPORTED, "the gradient supports at most 128 parameters");
   const bool df = m.precision == 0;
-  // tile slots of the partial sums: the fused / sweep kernel's (128 wavenumbers each), then
+  // tile slots of the partial sums: the fused kernel's (128 wavenumbers each) or the sweep
+  // kernel's (256 wavenumbers each), then
   // in the double-float path the sink kernel's (kSinkKPT x 128 wavenumbers each)
-  const int tiles_a = (int)((m.N + kAdjThreads - 1) / kAdjThreads);
+  const int tiles_a = (int)((m.N + (df ? 2 : 1) * kAdjThreads - 1) / ((df ? 2 : 1) * kAdjThreads));
   const int tiles_b = df ? (int)((m.N + kSinkKPT * kAdjThreads - 1) / (kSinkKPT * kAdjThreads)) : 0;
   const int tiles = tiles_a + tiles_b;
   const size_t per_eval = grad_bytes_per_eval(m, tiles, V, df);

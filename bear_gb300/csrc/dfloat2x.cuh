@@ -118,4 +118,30 @@ __device__ __forceinline__ dfx dfx_ldexp_normal(dfx m, int2 n) {
   return {f2mul(m.hi, s), f2mul(m.lo, s)};
 }
 
+// df_ldexp for any n <= 127 per element: the two-step scaling of its second branch, with
+// the second factor 1 (an exact multiplication) for an element in the first branch's range.
+__device__ __forceinline__ dfx dfx_ldexp(dfx m, int2 n) {
+  const bool w0 = n.x >= -126, w1 = n.y >= -126;
+  const float2 s1 = make_float2(pow2f(w0 ? n.x : -126), pow2f(w1 ? n.y : -126));
+  const float2 s2 = make_float2(w0 ? 1.0f : pow2f(n.x + 126), w1 ? 1.0f : pow2f(n.y + 126));
+  return {f2mul(f2mul(m.hi, s1), s2), f2mul(f2mul(m.lo, s1), s2)};
+}
+
+// element e of a where c_e holds, of b elsewhere
+__device__ __forceinline__ dfx dfx_select(bool c0, bool c1, dfx a, dfx b) {
+  return {make_float2(c0 ? a.hi.x : b.hi.x, c1 ? a.hi.y : b.hi.y),
+          make_float2(c0 ? a.lo.x : b.lo.x, c1 ? a.lo.y : b.lo.y)};
+}
+
+// element e replaced by the double-float v
+__device__ __forceinline__ void dfx_set(dfx& a, int e, df2 v) {
+  if (e) {
+    a.hi.y = v.hi;
+    a.lo.y = v.lo;
+  } else {
+    a.hi.x = v.hi;
+    a.lo.x = v.lo;
+  }
+}
+
 }  // namespace bgb

@@ -345,6 +345,12 @@ __global__ void transmission_geometry_kernel(DeviceModel dm, const LevelInfo* __
 // last index inside the cut-off and the sums of c_i dG[t][i]/dz_t and c_i dG[t][i]/dR
 // over each ray (taps.tr_*; dG from taps.tr_geo, computed before this kernel).
 constexpr int kTPN = 4;
+// The effective-height sum sum_t rw_t (1 - T_t) is formed as kHeightGroups partial sums,
+// group g holding the rays t = L - 2 - g - kHeightGroups m in descending order, added in
+// group order; every transmission kernel with one tangent level per ray keeps this order,
+// whatever its threads per wavenumber (4: two groups per thread; 8: one), so all of them
+// give the same bits.
+constexpr int kHeightGroups = 8;
 
 __global__ void tr_geometry_adjoint_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
                                            const EvalInfo* __restrict__ ev, const float2* __restrict__ geom,
@@ -439,7 +445,6 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
   extern __shared__ double chi_s[];  // [L][VPB]
   float2* chi_f = reinterpret_cast<float2*>(chi_s);
   __shared__ ExpTables et;
-  __shared__ double h_part[TPN][VPB];
   const int v = threadIdx.x % VPB, j = threadIdx.x / VPB;
   const int b = blockIdx.x;
   const int k = blockIdx.y * VPB + v;
@@ -479,7 +484,7 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
     }
   }
   __syncthreads();
-  double h = 0.0;
+  double h = 0.0, h_other = 0.0;  // height groups j and j + TPN
   const double Rp = ev[b].radius;
   const double* rw = rays + (size_t)b * 2 * L + L;  // effective-height weights
   const size_t col = (size_t)b * L * N + k;  // [b][level][k] of level 0 (gradient pass stores)
@@ -579,18 +584,193 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
         omt = 1. - exp(-tau);
       }
       h = fma(__ldg(&rw[t]), omt, h);
+      // the next ray (t - TPN) belongs to the other height group of this thread
+      const double x = h;
+      h = h_other;
+      h_other = x;
     }
   }
-  h_part[j][v] = h;
+  // after an even number of rays h holds group j again, after an odd number group j + TPN;
+  // the group sums [kHeightGroups][VPB] take the place of the extinction column
+  const bool odd = j <= L - 2 && (((L - 2 - j) / TPN) & 1) == 0;
+  double* h_part = chi_s;
+  __syncthreads();
+  h_part[j * VPB + v] = odd ? h_other : h;
+  h_part[(j + TPN) * VPB + v] = odd ? h : h_other;
   __syncthreads();
   if (active && j == 0) {
     double hs = 0.0;
 #pragma unroll
-    for (int q = 0; q < TPN; ++q) hs += h_part[q][v];
+    for (int q = 0; q < kHeightGroups; ++q) hs += h_part[q * VPB + v];
     hs = sqrt(hs + Rp * Rp) - Rp;
     const double rp = hs + Rp;
     const double Rs = ev[b].star_radius;
     spectrum[(size_t)b * N + k] = rp * rp / Rs / Rs * 1e6;
+  }
+}
+
+// transmission_kernel's double-float forward path with two wavenumbers per thread group:
+// a block covers VP pairs (k, k + VP), 2 VP wavenumbers, with TPN threads per pair (4 or 8).
+// Every double-float step is that kernel's step issued once for both wavenumbers with
+// paired FP32 instructions (dfloat2x.cuh), and the effective-height sums run in the same
+// groups and order (kHeightGroups), so each transit depth is bit for bit
+// transmission_kernel's. A tangent sum runs paired until either wavenumber passes the
+// cut-off; the other one finishes alone. The level-table reads of GRP species are issued
+// together. Dynamic shared memory: the extinction column chi[L][VP] as paired
+// double-floats (hi0, hi1, lo0, lo1), then the evaluation's Rayleigh number densities [L][R]
+// as double-floats; after the tangent sums the kHeightGroups partial sums take its place.
+// Measured on 64 evaluations of 100 levels x 33976 points (10 tables, 2 Rayleigh species):
+// <16, 8, 8, 2> (63 registers, 7 blocks = 28 warps per SM) 14.76 ms, against 16.28 ms for
+// transmission_kernel at 64 wavenumbers per block; 4 threads per pair (16 warps per SM) took
+// 19.8 ms, and issuing the next species' table reads ahead of the current arithmetic
+// 15.5-16.9 ms. About two thirds of the time is the extinction column.
+template <int VP, int TPN, int MINB, int GRP>
+__global__ void __launch_bounds__(TPN * VP, MINB) transmission_kernel_x2(DeviceModel dm, const LevelInfo* __restrict__ lev,
+                                                                  const LevelSpeciesDF* __restrict__ lsdf,
+                                                                  const double* __restrict__ ray_n,
+                                                                  const EvalInfo* __restrict__ ev,
+                                                                  const double* __restrict__ geom,
+                                                                  const double* __restrict__ rays,
+                                                                  double* __restrict__ spectrum) {
+  static_assert(TPN == 4 || TPN == 8, "4 or 8 threads per pair");
+  constexpr int NG = kHeightGroups / TPN;  // height groups per thread
+  extern __shared__ float4 chi_x[];  // [L][VP]
+  __shared__ ExpTables et;
+  const int v = threadIdx.x % VP, j = threadIdx.x / VP;
+  const int b = blockIdx.x;
+  const int ka = blockIdx.y * 2 * VP + v, kb = ka + VP;
+  const int L = dm.L, S = dm.S, R = dm.R;
+  const size_t N = dm.N;
+  const bool act0 = ka < dm.N, act1 = kb < dm.N;  // act1 implies act0
+  const int k0 = act0 ? ka : dm.N - 1, k1 = act1 ? kb : dm.N - 1;
+  const LevelInfo* lv = lev + (size_t)b * L;
+  const LevelSpeciesDF* sf = lsdf + (size_t)b * L * S;
+  float2* rn_s = reinterpret_cast<float2*>(chi_x + (size_t)L * VP);  // [L][R]
+  // non-grey cloud: the extinction of every level scaled by the wavelength factor
+  double csh0 = 1.0, csh1 = 1.0;
+  if (dm.cloud_kind && act0) {
+    csh0 = cloud_shape(dm, ev[b], k0);
+    csh1 = cloud_shape(dm, ev[b], k1);
+  }
+  load_exp_tables(et);
+  for (int idx = threadIdx.x; idx < L * R; idx += blockDim.x) {
+    const df2 d = df_from_double(__ldg(&ray_n[(size_t)b * L * R + idx]));
+    rn_s[idx] = make_float2(d.hi, d.lo);
+  }
+  __syncthreads();
+  // extinction abs + scat + cloud of every level (the TPN threads take every TPN-th level)
+  if (act0) {
+    for (int l = j; l < L; l += TPN) {
+      const KappaX kp = level_kappa_x<GRP>(dm.ltab, N, sf + (size_t)l * S, S, k0, k1, et);
+      dfx x = kp.v;
+      if ((__double_as_longlong(kp.wide0) << 1) != 0) dfx_set(x, 0, df_add(dfx_get(x, 0), df_from_double(kp.wide0)));
+      if ((__double_as_longlong(kp.wide1) << 1) != 0) dfx_set(x, 1, df_add(dfx_get(x, 1), df_from_double(kp.wide1)));
+      for (int r = 0; r < R; ++r) {
+        const float2 s0 = __ldg(&dm.rayleigh_df[(size_t)r * N + k0]), s1 = __ldg(&dm.rayleigh_df[(size_t)r * N + k1]);
+        const float2 nr = rn_s[l * R + r];
+        x = dfx_fma(dfx{make_float2(s0.x, s1.x), make_float2(s0.y, s1.y)}, dfx_bcast(df2{nr.x, nr.y}), x);
+      }
+      const float2 cl = __ldg(reinterpret_cast<const float2*>(&lv[l].cloud_hi));
+      x = dm.cloud_kind ? dfx_fma(dfx_bcast(df2{cl.x, cl.y}), dfx_make(df_from_double(csh0), df_from_double(csh1)), x)
+                        : dfx_add(x, dfx_bcast(df2{cl.x, cl.y}));
+      chi_x[l * VP + v] = make_float4(x.hi.x, x.hi.y, x.lo.x, x.lo.y);
+    }
+  }
+  // neighbour sums chi_i + chi_{i+1}, the bracket of every trapezoid term: thread j takes a
+  // run of levels and reads the value after its run before any thread writes
+  const int run = (L - 1 + TPN - 1) / TPN;
+  const int i0 = j * run, i1 = min(i0 + run, L - 1);
+  __syncthreads();
+  float4 after = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (act0 && i0 < i1) after = chi_x[i1 * VP + v];
+  __syncthreads();
+  if (act0 && i0 < i1) {
+    float4 cur = chi_x[i0 * VP + v];
+    for (int i = i0; i < i1; ++i) {
+      const float4 nx = i + 1 < i1 ? chi_x[(i + 1) * VP + v] : after;
+      const dfx s2 = dfx_add(dfx{make_float2(cur.x, cur.y), make_float2(cur.z, cur.w)},
+                             dfx{make_float2(nx.x, nx.y), make_float2(nx.z, nx.w)});
+      chi_x[i * VP + v] = make_float4(s2.hi.x, s2.hi.y, s2.lo.x, s2.lo.y);
+      cur = nx;
+    }
+  }
+  __syncthreads();
+  double h0 = 0.0, h1 = 0.0, h0o = 0.0, h1o = 0.0;  // groups j (and j + TPN when NG = 2)
+  const double* rw = rays + (size_t)b * 2 * L + L;  // effective-height weights
+  if (act0) {
+    const float ch = dm.tau_cut_hi, cl = dm.tau_cut_lo;
+    for (int t = L - 2 - j; t >= 0; t -= TPN) {
+      const float2* Gt = reinterpret_cast<const float2*>(geom) + (size_t)b * L * L + (size_t)t * L;
+      dfx ts = {f2(0.0f), f2(0.0f)};
+      bool cut0 = false, cut1 = false;
+      int i = t;
+      for (; i < L - 1; ++i) {
+        const float2 g = __ldg(&Gt[i]);
+        const float4 c = chi_x[i * VP + v];
+        ts = dfx_fma(dfx_bcast(df2{g.x, g.y}), dfx{make_float2(c.x, c.y), make_float2(c.z, c.w)}, ts);
+        if (ts.hi.x >= ch || ts.hi.y >= ch) {  // tau > cut-off needs hi >= the cut-off's hi
+          cut0 = ts.hi.x > ch || (ts.hi.x == ch && ts.lo.x > cl);
+          cut1 = ts.hi.y > ch || (ts.hi.y == ch && ts.lo.y > cl);
+          if (cut0 || cut1) {
+            ++i;
+            break;
+          }
+        }
+      }
+      if (cut0 != cut1) {
+        // one wavenumber is past the cut-off: the other one's remaining terms alone
+        const int e = cut0 ? 1 : 0;
+        df2 te = dfx_get(ts, e);
+        for (; i < L - 1; ++i) {
+          const float2 g = __ldg(&Gt[i]);
+          const float4 c = chi_x[i * VP + v];
+          te = df_fma(df2{g.x, g.y}, e ? df2{c.y, c.w} : df2{c.x, c.z}, te);
+          if (te.hi > ch || (te.hi == ch && te.lo > cl)) break;
+        }
+        dfx_set(ts, e, te);
+      }
+      // 1 - T with T = exp(-tau) in double-float
+      const dfx omt = dfx_sub(dfx_bcast(df_make(1.0f)), dfx_exp_neg(ts, et.hi, et.lo));
+      const double w = __ldg(&rw[t]);
+      h0 = fma(w, df_to_double(dfx_get(omt, 0)), h0);
+      h1 = fma(w, df_to_double(dfx_get(omt, 1)), h1);
+      if (NG == 2) {  // the next ray belongs to the thread's other group
+        double x = h0;
+        h0 = h0o;
+        h0o = x;
+        x = h1;
+        h1 = h1o;
+        h1o = x;
+      }
+    }
+  }
+  // the group sums [kHeightGroups][2][VP] take the place of the extinction column
+  double* h_part = reinterpret_cast<double*>(chi_x);
+  __syncthreads();
+  if (NG == 2) {
+    // after an odd number of rays the other group's sums are current
+    const bool odd = j <= L - 2 && (((L - 2 - j) / TPN) & 1) == 0;
+    h_part[(2 * j) * VP + v] = odd ? h0o : h0;
+    h_part[(2 * j + 1) * VP + v] = odd ? h1o : h1;
+    h_part[(2 * (j + TPN)) * VP + v] = odd ? h0 : h0o;
+    h_part[(2 * (j + TPN) + 1) * VP + v] = odd ? h1 : h1o;
+  } else {
+    h_part[(2 * j) * VP + v] = h0;
+    h_part[(2 * j + 1) * VP + v] = h1;
+  }
+  __syncthreads();
+  if (j == 0) {
+    const double Rp = ev[b].radius, Rs = ev[b].star_radius;
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      if (!(e ? act1 : act0)) continue;
+      double hs = 0.0;
+#pragma unroll
+      for (int q = 0; q < kHeightGroups; ++q) hs += h_part[(2 * q + e) * VP + v];
+      hs = sqrt(hs + Rp * Rp) - Rp;
+      const double rp = hs + Rp;
+      spectrum[(size_t)b * N + (e ? k1 : k0)] = rp * rp / Rs / Rs * 1e6;
+    }
   }
 }
 
@@ -1200,6 +1380,8 @@ void upload_model(Model& m) {
     BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<false, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<true, 32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<true, 64, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel_x2<16, 8, 8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel_x2<32, 8, 3, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_annuli_kernel<true, 32, 4, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_annuli_kernel<true, 32, 8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_annuli_kernel<true, 32, 8, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
@@ -1320,11 +1502,16 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
     const dim3 ggrid(batch, (L * L + 255) / 256);
     if (m.precision == 1) transmission_geometry_kernel<false><<<ggrid, 256, 0, st>>>(dm, w.lev, w.ev, w.geom, w.rays);
     else transmission_geometry_kernel<true><<<ggrid, 256, 0, st>>>(dm, w.lev, w.ev, w.geom, w.rays);
-    // the launch shape selects the wavenumbers per block: 16, 32 (default) or 64, 4 threads each
+    // the launch shape: 16, 32 or 64 wavenumbers per block with 4 threads each; 160 (the
+    // double-float default) or 192: 32 or 64 wavenumbers per block in pairs, 8 threads per pair.
+    // The FP64 path and the gradient's storing pass take 32 for 160 and 192.
     const int vpb = (rt == 16 || rt == 64) ? rt : 32;
     dim3 grid(batch, (dm.N + vpb - 1) / vpb);
     const bool df = m.precision != 1;
-    const size_t sm = (size_t)L * vpb * sizeof(double) + (df ? (size_t)L * dm.R * sizeof(float2) : 0);
+    const int pairs = (rt == 16 || rt == 32 || rt == 64) ? 0 : (rt == 192 ? 32 : 16);
+    // extinction column and Rayleigh densities, at least the height-group sums that reuse them
+    const size_t sm = std::max((size_t)L * vpb * sizeof(double) + (df ? (size_t)L * dm.R * sizeof(float2) : 0),
+                               (size_t)kHeightGroups * vpb * sizeof(double));
     if (sm > kTransmissionDynSmem) throw Error(BEAR_ERR_UNSUPPORTED, "too many levels for the transmission kernel");
     const ForwardTaps none{};
     auto go = [&](auto kernel) {
@@ -1339,13 +1526,24 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
       // the tuned wavenumbers per block when it is 64, else 32
       const int sv = vpb == 64 ? 64 : 32;
       const dim3 gs(batch, (dm.N + sv - 1) / sv);
-      const size_t sms = (size_t)L * sv * sizeof(double) + (size_t)L * dm.R * sizeof(float2);
+      const size_t sms = std::max((size_t)L * sv * sizeof(double) + (size_t)L * dm.R * sizeof(float2),
+                                  (size_t)kHeightGroups * sv * sizeof(double));
       if (sv == 64)
         transmission_kernel<true, 64, true><<<gs, kTPN * 64, sms, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev,
                                                                         w.geom, w.rays, w.spectrum, *taps);
       else
         transmission_kernel<true, 32, true><<<gs, kTPN * 32, sms, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev,
                                                                         w.geom, w.rays, w.spectrum, *taps);
+    } else if (df && pairs) {
+      const size_t smx = std::max((size_t)L * pairs * sizeof(float4) + (size_t)L * dm.R * sizeof(float2),
+                                  (size_t)kHeightGroups * 2 * pairs * sizeof(double));
+      if (smx > kTransmissionDynSmem) throw Error(BEAR_ERR_UNSUPPORTED, "too many levels for the transmission kernel");
+      const dim3 gx(batch, (dm.N + 2 * pairs - 1) / (2 * pairs));
+      auto gox = [&](auto kernel, int tpn) {
+        kernel<<<gx, tpn * pairs, smx, st>>>(dm, w.lev, w.lsdf, w.ray_n, w.ev, w.geom, w.rays, w.spectrum);
+      };
+      if (pairs == 32) gox(transmission_kernel_x2<32, 8, 3, 2>, 8);
+      else gox(transmission_kernel_x2<16, 8, 8, 2>, 8);
     } else if (vpb == 16) df ? go(transmission_kernel<true, 16>) : go(transmission_kernel<false, 16>);
     else if (vpb == 64) df ? go(transmission_kernel<true, 64>) : go(transmission_kernel<false, 64>);
     else df ? go(transmission_kernel<true, 32>) : go(transmission_kernel<false, 32>);

@@ -20,53 +20,79 @@ struct KappaX {
 };
 
 // level_kappa_df for wavenumbers k0 and k1: the sum over table species of 2^y n with
-// y = lo + (hi - lo) wT + log2 n (level-table values, log2 units).
+// y = lo + (hi - lo) wT + log2 n (level-table values, log2 units). The level-table reads
+// of GRP species are issued before their arithmetic (the order of the sum is unchanged).
+template <int GRP = 1>
 __device__ __forceinline__ KappaX level_kappa_x(const float2* __restrict__ ltab, size_t N,
                                                 const LevelSpeciesDF* __restrict__ f, int S, int k0, int k1,
                                                 const ExpTables& et) {
   KappaX r;
   r.wide0 = r.wide1 = 0.0;
   float2 acc_hi = f2(0.0f), acc_lo = f2(0.0f);
-  for (int s = 0; s < S; ++s) {
-    const int4 rw = __ldg(reinterpret_cast<const int4*>(f + s));
-    const float4 fb = __ldg(reinterpret_cast<const float4*>(f + s) + 1);  // wT, log2 n
-    if (fb.z == kNoSpecies) continue;  // zero number density: the species adds nothing
-    const float2* r0 = ltab + (size_t)rw.x * N;
-    const float2* r1 = ltab + (size_t)rw.y * N;
-    const float2 a0 = __ldg(r0 + k0), a1 = __ldg(r0 + k1), b0 = __ldg(r1 + k0), b1 = __ldg(r1 + k1);
-    const dfx lo = {make_float2(a0.x, a1.x), make_float2(a0.y, a1.y)};
-    const dfx hi = {make_float2(b0.x, b1.x), make_float2(b0.y, b1.y)};
-    const dfx y = dfx_fma(dfx_sub(hi, lo), dfx_bcast(df2{fb.x, fb.y}), dfx_add(lo, dfx_bcast(df2{fb.z, fb.w})));
-    int2 n;
-    const dfx m = dfx_exp2(y, n, et.hi, et.lo);
-    const bool nar0 = n.x > -100 && n.x < 100, nar1 = n.y > -100 && n.y < 100;
-    if (nar0 && nar1) {
-      const dfx t = dfx_ldexp_normal(m, n);
-      const dfx a = two_sum_x(acc_hi, t.hi);
-      acc_hi = a.hi;
-      acc_lo = f2add(acc_lo, f2add(a.lo, t.lo));
-    } else {
-      // one or both terms outside the float exponent range: the scalar steps per element
-      if (nar0) {
-        const df2 t = df_ldexp(dfx_get(m, 0), n.x);
-        const df2 a = two_sum(acc_hi.x, t.hi);
-        acc_hi.x = a.hi;
-        acc_lo.x = BGB_FADD(acc_lo.x, BGB_FADD(a.lo, t.lo));
-      } else {
-        r.wide0 += df_to_double(dfx_get(m, 0)) * pow2d(n.x);
+  for (int s0 = 0; s0 < S; s0 += GRP) {
+    float4 fb[GRP];
+    float2 a0[GRP], a1[GRP], b0[GRP], b1[GRP];
+#pragma unroll
+    for (int g = 0; g < GRP; ++g) {
+      if (s0 + g >= S) break;
+      const int4 rw = __ldg(reinterpret_cast<const int4*>(f + s0 + g));
+      fb[g] = __ldg(reinterpret_cast<const float4*>(f + s0 + g) + 1);  // wT, log2 n
+      if (fb[g].z != kNoSpecies) {
+        const float2* r0 = ltab + (size_t)rw.x * N;
+        const float2* r1 = ltab + (size_t)rw.y * N;
+        a0[g] = __ldg(r0 + k0);
+        a1[g] = __ldg(r0 + k1);
+        b0[g] = __ldg(r1 + k0);
+        b1[g] = __ldg(r1 + k1);
       }
-      if (nar1) {
-        const df2 t = df_ldexp(dfx_get(m, 1), n.y);
-        const df2 a = two_sum(acc_hi.y, t.hi);
-        acc_hi.y = a.hi;
-        acc_lo.y = BGB_FADD(acc_lo.y, BGB_FADD(a.lo, t.lo));
+    }
+#pragma unroll
+    for (int g = 0; g < GRP; ++g) {
+      if (s0 + g >= S) break;
+      if (fb[g].z == kNoSpecies) continue;  // zero number density: the species adds nothing
+      const dfx lo = {make_float2(a0[g].x, a1[g].x), make_float2(a0[g].y, a1[g].y)};
+      const dfx hi = {make_float2(b0[g].x, b1[g].x), make_float2(b0[g].y, b1[g].y)};
+      const dfx y =
+          dfx_fma(dfx_sub(hi, lo), dfx_bcast(df2{fb[g].x, fb[g].y}), dfx_add(lo, dfx_bcast(df2{fb[g].z, fb[g].w})));
+      int2 n;
+      const dfx m = dfx_exp2(y, n, et.hi, et.lo);
+      const bool nar0 = n.x > -100 && n.x < 100, nar1 = n.y > -100 && n.y < 100;
+      if (nar0 && nar1) {
+        const dfx t = dfx_ldexp_normal(m, n);
+        const dfx a = two_sum_x(acc_hi, t.hi);
+        acc_hi = a.hi;
+        acc_lo = f2add(acc_lo, f2add(a.lo, t.lo));
       } else {
-        r.wide1 += df_to_double(dfx_get(m, 1)) * pow2d(n.y);
+        // one or both terms outside the float exponent range: the scalar steps per element
+        if (nar0) {
+          const df2 t = df_ldexp(dfx_get(m, 0), n.x);
+          const df2 a = two_sum(acc_hi.x, t.hi);
+          acc_hi.x = a.hi;
+          acc_lo.x = BGB_FADD(acc_lo.x, BGB_FADD(a.lo, t.lo));
+        } else {
+          r.wide0 += df_to_double(dfx_get(m, 0)) * pow2d(n.x);
+        }
+        if (nar1) {
+          const df2 t = df_ldexp(dfx_get(m, 1), n.y);
+          const df2 a = two_sum(acc_hi.y, t.hi);
+          acc_hi.y = a.hi;
+          acc_lo.y = BGB_FADD(acc_lo.y, BGB_FADD(a.lo, t.lo));
+        } else {
+          r.wide1 += df_to_double(dfx_get(m, 1)) * pow2d(n.y);
+        }
       }
     }
   }
   r.v = fast_two_sum_x(acc_hi, acc_lo);
   return r;
+}
+
+// df_exp_neg (physics.cuh) for two double-floats
+__device__ __forceinline__ dfx dfx_exp_neg(dfx d, const float* tab_hi, const float* tab_lo) {
+  int2 n;
+  const dfx m = dfx_exp2(dfx_neg(dfx_mul(d, dfx_bcast(df2{kLog2eHi, kLog2eLo}))), n, tab_hi, tab_lo);
+  const dfx z = {f2(0.0f), f2(0.0f)};
+  return dfx_select(d.hi.x > 700.0f, d.hi.y > 700.0f, z, dfx_ldexp(m, n));
 }
 
 // planck_dd (physics.cuh) for two wavenumbers.

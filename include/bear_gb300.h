@@ -218,7 +218,7 @@ int bear_model_set_gradient_memory(bear_model* m, long long bytes);
 /* --------------------------------------------------------------- autotuner and captured batches
  * No reference counterpart. bear_model_autotune times the radiative-transfer
  * kernel's launch shapes (emission: 64 / 128 / 256 threads per block;
- * transmission: 16 / 32 / 64 wavenumbers per block) on this batch with CUDA events,
+ * transmission: 160, 192, 32, 64, see bear_model_set_launch) on this batch with CUDA events,
  * keeps the fastest for later batched calls (an explicit bear_model_set_launch
  * takes precedence) and reports it. Synchronous; results do not depend on the
  * choice (each wavenumber is computed by the same code). */
@@ -252,10 +252,12 @@ int bear_batch_graph_destroy(bear_batch_graph* g);
 int bear_model_set_precision(bear_model* m, int mode);
 
 /* Launch shape of the radiative-transfer kernel (emission: threads =
- * wavenumbers per block, 64 / 128 / 256; transmission: wavenumbers per block,
- * 16 / 32 / 64, four threads each; 0 = default or the autotuned shape) and threads
- * per block of the observation + likelihood kernel (0 = 256). An explicit
- * setting overrides bear_model_autotune. */
+ * wavenumbers per block, 64 / 128 / 256; transmission: 16 / 32 / 64 wavenumbers
+ * per block with four threads each, or 160 / 192 for 32 / 64 wavenumbers per block
+ * in pairs, eight threads per pair, any other value the default 160; the FP64
+ * path runs 32 in place of 160 and 192; 0 = default or the autotuned shape) and
+ * threads per block of the observation + likelihood kernel (0 = 256). An explicit
+ * setting overrides bear_model_autotune. Every shape gives the same bits. */
 int bear_model_set_launch(bear_model* m, int rt_threads, int obs_threads);
 
 /* Allocation-free log-likelihood of one parameter set. No counterpart in the
