@@ -624,14 +624,17 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
 // transmission_kernel at 64 wavenumbers per block; 4 threads per pair (16 warps per SM) took
 // 19.8 ms, and issuing the next species' table reads ahead of the current arithmetic
 // 15.5-16.9 ms. About two thirds of the time is the extinction column.
-template <int VP, int TPN, int MINB, int GRP>
+// With STORE (the gradient's forward pass) it also writes transmission_kernel<STORE>'s
+// stores: the opacity terms and temperature-slope sums, the pair sums c, and per ray T_t,
+// the cut-off index and the ray sums of c dG/dz_t and c dG/dR.
+template <int VP, int TPN, int MINB, int GRP, bool STORE = false>
 __global__ void __launch_bounds__(TPN * VP, MINB) transmission_kernel_x2(DeviceModel dm, const LevelInfo* __restrict__ lev,
                                                                   const LevelSpeciesDF* __restrict__ lsdf,
                                                                   const double* __restrict__ ray_n,
                                                                   const EvalInfo* __restrict__ ev,
                                                                   const double* __restrict__ geom,
                                                                   const double* __restrict__ rays,
-                                                                  double* __restrict__ spectrum) {
+                                                                  double* __restrict__ spectrum, ForwardTaps taps) {
   static_assert(TPN == 4 || TPN == 8, "4 or 8 threads per pair");
   constexpr int NG = kHeightGroups / TPN;  // height groups per thread
   extern __shared__ float4 chi_x[];  // [L][VP]
@@ -660,8 +663,45 @@ __global__ void __launch_bounds__(TPN * VP, MINB) transmission_kernel_x2(DeviceM
   __syncthreads();
   // extinction abs + scat + cloud of every level (the TPN threads take every TPN-th level)
   if (act0) {
+    const dfx zero = {f2(0.0f), f2(0.0f)};
     for (int l = j; l < L; l += TPN) {
-      const KappaX kp = level_kappa_x<GRP>(dm.ltab, N, sf + (size_t)l * S, S, k0, k1, et);
+      KappaX kp;
+      if (STORE && taps.tr_ts) {
+        // each species' term and the temperature-slope sum sum_s term_s (hi_s - lo_s) dwT_s/dT
+        // (tr_extinction_terms per element)
+        const float2* dwl = taps.dwT + ((size_t)b * L + l) * S;
+        float2* tso = taps.tr_ts + ((size_t)b * L + l) * S * N;
+        dfx dk = zero;
+        bool wide0 = false, wide1 = false;
+        kp = level_kappa_x_cb<GRP>(dm.ltab, N, sf + (size_t)l * S, S, k0, k1, et,
+                                   [&](int s, const dfx& t, bool w0, bool w1, const dfx& lo, const dfx& hi) {
+                                     tso[(size_t)s * N + k0] = make_float2(t.hi.x, t.lo.x);
+                                     if (act1) tso[(size_t)s * N + k1] = make_float2(t.hi.y, t.lo.y);
+                                     const float2 d = __ldg(dwl + s);
+                                     if (d.x != 0.0f) {
+                                       if (!w0 && !w1) {
+                                         dk = dfx_add(dk, dfx_mul(t, dfx_mul(dfx_sub(hi, lo), dfx_bcast(df2{d.x, d.y}))));
+                                       } else {
+#pragma unroll
+                                         for (int e = 0; e < 2; ++e) {
+                                           if (e ? w1 : w0) continue;
+                                           dfx_set(dk, e, df_add(dfx_get(dk, e),
+                                                                 df_mul(dfx_get(t, e),
+                                                                        df_mul(df_sub(dfx_get(hi, e), dfx_get(lo, e)),
+                                                                               df2{d.x, d.y}))));
+                                         }
+                                       }
+                                     }
+                                     wide0 = wide0 || w0;
+                                     wide1 = wide1 || w1;
+                                   });
+        const float2 nan2 = make_float2(__int_as_float(0x7fc00000), 0.0f);
+        float2* dko = taps.tr_dk + ((size_t)b * L + l) * N;
+        dko[k0] = wide0 ? nan2 : make_float2(dk.hi.x, dk.lo.x);
+        if (act1) dko[k1] = wide1 ? nan2 : make_float2(dk.hi.y, dk.lo.y);
+      } else {
+        kp = level_kappa_x<GRP>(dm.ltab, N, sf + (size_t)l * S, S, k0, k1, et);
+      }
       dfx x = kp.v;
       if ((__double_as_longlong(kp.wide0) << 1) != 0) dfx_set(x, 0, df_add(dfx_get(x, 0), df_from_double(kp.wide0)));
       if ((__double_as_longlong(kp.wide1) << 1) != 0) dfx_set(x, 1, df_add(dfx_get(x, 1), df_from_double(kp.wide1)));
@@ -691,6 +731,10 @@ __global__ void __launch_bounds__(TPN * VP, MINB) transmission_kernel_x2(DeviceM
       const dfx s2 = dfx_add(dfx{make_float2(cur.x, cur.y), make_float2(cur.z, cur.w)},
                              dfx{make_float2(nx.x, nx.y), make_float2(nx.z, nx.w)});
       chi_x[i * VP + v] = make_float4(s2.hi.x, s2.hi.y, s2.lo.x, s2.lo.y);
+      if (STORE) {
+        taps.tr_c[((size_t)b * L + i) * N + k0] = make_float2(s2.hi.x, s2.lo.x);
+        if (act1) taps.tr_c[((size_t)b * L + i) * N + k1] = make_float2(s2.hi.y, s2.lo.y);
+      }
       cur = nx;
     }
   }
@@ -701,17 +745,29 @@ __global__ void __launch_bounds__(TPN * VP, MINB) transmission_kernel_x2(DeviceM
     const float ch = dm.tau_cut_hi, cl = dm.tau_cut_lo;
     for (int t = L - 2 - j; t >= 0; t -= TPN) {
       const float2* Gt = reinterpret_cast<const float2*>(geom) + (size_t)b * L * L + (size_t)t * L;
-      dfx ts = {f2(0.0f), f2(0.0f)};
+      // STORE: the ray sums of c dG/dz_t (Q) and c dG/dR (U) beside the optical depth
+      const float2* Qt = STORE ? taps.tr_geo + (size_t)b * 4 * L * L + (size_t)L * L + (size_t)t * L : nullptr;
+      const float2* Ut = STORE ? Qt + (size_t)L * L : nullptr;
+      dfx ts = {f2(0.0f), f2(0.0f)}, qs = ts, us = ts;
       bool cut0 = false, cut1 = false;
+      int last0 = L - 2, last1 = L - 2;  // the last index inside the cut-off
       int i = t;
       for (; i < L - 1; ++i) {
         const float2 g = __ldg(&Gt[i]);
         const float4 c = chi_x[i * VP + v];
-        ts = dfx_fma(dfx_bcast(df2{g.x, g.y}), dfx{make_float2(c.x, c.y), make_float2(c.z, c.w)}, ts);
+        const dfx cc = {make_float2(c.x, c.y), make_float2(c.z, c.w)};
+        ts = dfx_fma(dfx_bcast(df2{g.x, g.y}), cc, ts);
+        if (STORE) {
+          const float2 q = __ldg(&Qt[i]), u = __ldg(&Ut[i]);
+          qs = dfx_fma(dfx_bcast(df2{q.x, q.y}), cc, qs);
+          us = dfx_fma(dfx_bcast(df2{u.x, u.y}), cc, us);
+        }
         if (ts.hi.x >= ch || ts.hi.y >= ch) {  // tau > cut-off needs hi >= the cut-off's hi
           cut0 = ts.hi.x > ch || (ts.hi.x == ch && ts.lo.x > cl);
           cut1 = ts.hi.y > ch || (ts.hi.y == ch && ts.lo.y > cl);
           if (cut0 || cut1) {
+            if (cut0) last0 = i;
+            if (cut1) last1 = i;
             ++i;
             break;
           }
@@ -720,17 +776,42 @@ __global__ void __launch_bounds__(TPN * VP, MINB) transmission_kernel_x2(DeviceM
       if (cut0 != cut1) {
         // one wavenumber is past the cut-off: the other one's remaining terms alone
         const int e = cut0 ? 1 : 0;
-        df2 te = dfx_get(ts, e);
+        df2 te = dfx_get(ts, e), qe = dfx_get(qs, e), ue = dfx_get(us, e);
         for (; i < L - 1; ++i) {
           const float2 g = __ldg(&Gt[i]);
           const float4 c = chi_x[i * VP + v];
-          te = df_fma(df2{g.x, g.y}, e ? df2{c.y, c.w} : df2{c.x, c.z}, te);
-          if (te.hi > ch || (te.hi == ch && te.lo > cl)) break;
+          const df2 ce = e ? df2{c.y, c.w} : df2{c.x, c.z};
+          te = df_fma(df2{g.x, g.y}, ce, te);
+          if (STORE) {
+            const float2 q = __ldg(&Qt[i]), u = __ldg(&Ut[i]);
+            qe = df_fma(df2{q.x, q.y}, ce, qe);
+            ue = df_fma(df2{u.x, u.y}, ce, ue);
+          }
+          if (te.hi > ch || (te.hi == ch && te.lo > cl)) {
+            (e ? last1 : last0) = i;
+            break;
+          }
         }
         dfx_set(ts, e, te);
+        dfx_set(qs, e, qe);
+        dfx_set(us, e, ue);
+      }
+      const dfx T = dfx_exp_neg(ts, et.hi, et.lo);
+      if (STORE) {
+        const size_t at = ((size_t)b * L + t) * N;
+        taps.tr_T[at + k0] = make_float2(T.hi.x, T.lo.x);
+        taps.tr_qs[at + k0] = make_float2(qs.hi.x, qs.lo.x);
+        taps.tr_us[at + k0] = make_float2(us.hi.x, us.lo.x);
+        taps.tr_I[at + k0] = (short)last0;
+        if (act1) {
+          taps.tr_T[at + k1] = make_float2(T.hi.y, T.lo.y);
+          taps.tr_qs[at + k1] = make_float2(qs.hi.y, qs.lo.y);
+          taps.tr_us[at + k1] = make_float2(us.hi.y, us.lo.y);
+          taps.tr_I[at + k1] = (short)last1;
+        }
       }
       // 1 - T with T = exp(-tau) in double-float
-      const dfx omt = dfx_sub(dfx_bcast(df_make(1.0f)), dfx_exp_neg(ts, et.hi, et.lo));
+      const dfx omt = dfx_sub(dfx_bcast(df_make(1.0f)), T);
       const double w = __ldg(&rw[t]);
       h0 = fma(w, df_to_double(dfx_get(omt, 0)), h0);
       h1 = fma(w, df_to_double(dfx_get(omt, 1)), h1);
@@ -1382,6 +1463,8 @@ void upload_model(Model& m) {
     BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<true, 64, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_kernel_x2<16, 8, 8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_kernel_x2<32, 8, 3, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel_x2<16, 8, 8, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel_x2<16, 8, 6, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_annuli_kernel<true, 32, 4, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_annuli_kernel<true, 32, 8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_annuli_kernel<true, 32, 8, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
@@ -1523,6 +1606,27 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
       tr_geometry_adjoint_kernel<<<dim3(batch, (L * L + 255) / 256), 256, 0, st>>>(
           dm, w.lev, w.ev, reinterpret_cast<const float2*>(w.geom), taps->tr_geo);
       BGB_CUDA(cudaGetLastError());
+      if (pairs) {
+        // the paired kernel, 32 wavenumbers per block, whatever the paired shape
+        const size_t smx = std::max((size_t)L * 16 * sizeof(float4) + (size_t)L * dm.R * sizeof(float2),
+                                    (size_t)kHeightGroups * 2 * 16 * sizeof(double));
+        if (smx > kTransmissionDynSmem) throw Error(BEAR_ERR_UNSUPPORTED, "too many levels for the transmission kernel");
+        const dim3 gx(batch, (dm.N + 31) / 32);
+        if (rt == 192)
+          transmission_kernel_x2<16, 8, 6, 2, true><<<gx, 128, smx, st>>>(dm, w.lev, w.lsdf, w.ray_n, w.ev, w.geom,
+                                                                          w.rays, w.spectrum, *taps);
+        else
+          transmission_kernel_x2<16, 8, 8, 2, true><<<gx, 128, smx, st>>>(dm, w.lev, w.lsdf, w.ray_n, w.ev, w.geom,
+                                                                          w.rays, w.spectrum, *taps);
+        BGB_CUDA(cudaGetLastError());
+        if (profile) BGB_CUDA(cudaEventRecord(m.ev[2], st));
+        const int OTx = m.obs_threads > 0 ? m.obs_threads : 256;
+        obs_loglike_kernel<<<batch, OTx, 0, st>>>(dm, w.spectrum, params_dev, dm.P, w.ev, w.obs, loglike_dev,
+                                                 neglect_dev, m.precision == 1);
+        BGB_CUDA(cudaGetLastError());
+        if (profile) BGB_CUDA(cudaEventRecord(m.ev[3], st));
+        return;
+      }
       // the tuned wavenumbers per block when it is 64, else 32
       const int sv = vpb == 64 ? 64 : 32;
       const dim3 gs(batch, (dm.N + sv - 1) / sv);
@@ -1540,7 +1644,7 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
       if (smx > kTransmissionDynSmem) throw Error(BEAR_ERR_UNSUPPORTED, "too many levels for the transmission kernel");
       const dim3 gx(batch, (dm.N + 2 * pairs - 1) / (2 * pairs));
       auto gox = [&](auto kernel, int tpn) {
-        kernel<<<gx, tpn * pairs, smx, st>>>(dm, w.lev, w.lsdf, w.ray_n, w.ev, w.geom, w.rays, w.spectrum);
+        kernel<<<gx, tpn * pairs, smx, st>>>(dm, w.lev, w.lsdf, w.ray_n, w.ev, w.geom, w.rays, w.spectrum, none);
       };
       if (pairs == 32) gox(transmission_kernel_x2<32, 8, 3, 2>, 8);
       else gox(transmission_kernel_x2<16, 8, 8, 2>, 8);

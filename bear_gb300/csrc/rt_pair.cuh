@@ -19,16 +19,20 @@ struct KappaX {
   double wide0, wide1;
 };
 
-// level_kappa_df for wavenumbers k0 and k1: the sum over table species of 2^y n with
+// level_kappa_df_cb for wavenumbers k0 and k1: the sum over table species of 2^y n with
 // y = lo + (hi - lo) wT + log2 n (level-table values, log2 units). The level-table reads
 // of GRP species are issued before their arithmetic (the order of the sum is unchanged).
-template <int GRP = 1>
-__device__ __forceinline__ KappaX level_kappa_x(const float2* __restrict__ ltab, size_t N,
-                                                const LevelSpeciesDF* __restrict__ f, int S, int k0, int k1,
-                                                const ExpTables& et) {
+// term(s, t, wide0, wide1, lo, hi) receives each species' term of both wavenumbers (zero
+// for an element whose term lies outside the float range, flagged wide, and for a species
+// of zero number density).
+template <int GRP = 1, class F>
+__device__ __forceinline__ KappaX level_kappa_x_cb(const float2* __restrict__ ltab, size_t N,
+                                                   const LevelSpeciesDF* __restrict__ f, int S, int k0, int k1,
+                                                   const ExpTables& et, F&& term) {
   KappaX r;
   r.wide0 = r.wide1 = 0.0;
   float2 acc_hi = f2(0.0f), acc_lo = f2(0.0f);
+  const dfx zero = {f2(0.0f), f2(0.0f)};
   for (int s0 = 0; s0 < S; s0 += GRP) {
     float4 fb[GRP];
     float2 a0[GRP], a1[GRP], b0[GRP], b1[GRP];
@@ -48,8 +52,12 @@ __device__ __forceinline__ KappaX level_kappa_x(const float2* __restrict__ ltab,
     }
 #pragma unroll
     for (int g = 0; g < GRP; ++g) {
-      if (s0 + g >= S) break;
-      if (fb[g].z == kNoSpecies) continue;  // zero number density: the species adds nothing
+      const int s = s0 + g;
+      if (s >= S) break;
+      if (fb[g].z == kNoSpecies) {  // zero number density: the species adds nothing
+        term(s, zero, false, false, zero, zero);
+        continue;
+      }
       const dfx lo = {make_float2(a0[g].x, a1[g].x), make_float2(a0[g].y, a1[g].y)};
       const dfx hi = {make_float2(b0[g].x, b1[g].x), make_float2(b0[g].y, b1[g].y)};
       const dfx y =
@@ -62,13 +70,16 @@ __device__ __forceinline__ KappaX level_kappa_x(const float2* __restrict__ ltab,
         const dfx a = two_sum_x(acc_hi, t.hi);
         acc_hi = a.hi;
         acc_lo = f2add(acc_lo, f2add(a.lo, t.lo));
+        term(s, t, false, false, lo, hi);
       } else {
         // one or both terms outside the float exponent range: the scalar steps per element
+        dfx tt = zero;
         if (nar0) {
           const df2 t = df_ldexp(dfx_get(m, 0), n.x);
           const df2 a = two_sum(acc_hi.x, t.hi);
           acc_hi.x = a.hi;
           acc_lo.x = BGB_FADD(acc_lo.x, BGB_FADD(a.lo, t.lo));
+          dfx_set(tt, 0, t);
         } else {
           r.wide0 += df_to_double(dfx_get(m, 0)) * pow2d(n.x);
         }
@@ -77,14 +88,24 @@ __device__ __forceinline__ KappaX level_kappa_x(const float2* __restrict__ ltab,
           const df2 a = two_sum(acc_hi.y, t.hi);
           acc_hi.y = a.hi;
           acc_lo.y = BGB_FADD(acc_lo.y, BGB_FADD(a.lo, t.lo));
+          dfx_set(tt, 1, t);
         } else {
           r.wide1 += df_to_double(dfx_get(m, 1)) * pow2d(n.y);
         }
+        term(s, tt, !nar0, !nar1, lo, hi);
       }
     }
   }
   r.v = fast_two_sum_x(acc_hi, acc_lo);
   return r;
+}
+
+template <int GRP = 1>
+__device__ __forceinline__ KappaX level_kappa_x(const float2* __restrict__ ltab, size_t N,
+                                                const LevelSpeciesDF* __restrict__ f, int S, int k0, int k1,
+                                                const ExpTables& et) {
+  return level_kappa_x_cb<GRP>(ltab, N, f, S, k0, k1, et,
+                               [](int, const dfx&, bool, bool, const dfx&, const dfx&) {});
 }
 
 // df_exp_neg (physics.cuh) for two double-floats

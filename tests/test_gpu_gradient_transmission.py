@@ -145,6 +145,31 @@ def test_transmission_gradient_chunked_and_reproducible(case):
     assert np.array_equal(ll0, ll2) and np.array_equal(g0, g2)
 
 
+def test_transmission_gradient_storing_shapes_are_bit_identical(case):
+    """The storing forward pass with two wavenumbers per thread group (the default and the
+    paired launch shapes) and with one (launch shape 32) stores the same opacity terms, pair
+    sums and ray data, so the gradients are equal bit for bit; and the level sinks summed
+    from the stored terms streamed through shared memory (even N) equal those recomputed
+    from the level table (a gradient memory budget too small to store the terms)."""
+    spec, e, om, pr = case
+    phys = _points(spec, pr, 10, 27)
+    ll0, g0, ng0 = _grad(e, phys)
+    try:
+        for rt in (32, 192, 160):
+            e.set_launch(rt, 0)
+            ll1, g1, ng1 = _grad(e, phys)
+            assert np.array_equal(ll0, ll1) and np.array_equal(g0, g1) and np.array_equal(ng0, ng1), rt
+    finally:
+        e.set_launch(0, 0)
+    assert e.N % 2 == 0
+    e.set_gradient_memory(int(2.4 * 100 * e.N * 50))  # ray data of two evaluations, no opacity terms
+    try:
+        ll2, g2, ng2 = _grad(e, phys)
+    finally:
+        e.set_gradient_memory(0)
+    assert np.array_equal(ll0, ll2) and np.array_equal(g0, g2) and np.array_equal(ng0, ng2)
+
+
 def test_transmission_gradient_neglect_and_precision(case):
     spec, e, om, pr = case
     phys = _points(spec, pr, 3, 24)
