@@ -408,8 +408,14 @@ def measure_engine(ctx, workload, batch, steps, warmup, args, cpu_budget_s):
     alg_bytes = rows * N * 8 + B * L * S * 32 + B * N * 8
     peaks, peak_kind = measured_peaks()
     achieved_gbs = alg_bytes / (kern_ms * 1e-3) / 1e9
-    kernel = "emission_kernel" if kind == "emission" else (
-        "transmission_annuli_kernel" if workload in ANNULI else "transmission_kernel")
+    rec_k = kernel_counters(workload, B)
+    if rec_k:
+        kernel = rec_k["kernel"].split(" grid")[0]
+    elif kind == "emission":
+        kernel = "emission_kernel_x2<0>" if B >= 2 else "emission_kernel<0, 0>"
+    else:
+        kernel = "transmission_annuli_kernel" if workload in ANNULI else "transmission_kernel_x2<16, 8, 8, 2, 0>"
+
     rec = {
         "workload": workload, "batch": B, "levels": L, "spectral_points": N, "bins": M, "table_species": S,
         "annuli_per_layer": ANNULI.get(workload, 1), "steps": steps, "ms_per_step": total_ms / steps,
@@ -558,7 +564,7 @@ def measure_joint(ctx, batch, steps, warmup, args, cpu_budget_s):
         "gpu_launches": 7 * steps,
         "batched_path": {"api": "two bear_batch_graph_launch per step", "autotuned_rt_threads":
                          [ev.em.rt_threads, ev.tr.rt_threads]},
-        "roofline": {"bound": "hbm", "kernel": "emission_kernel + transmission_kernel", "achieved": achieved,
+        "roofline": {"bound": "hbm", "kernel": "emission_kernel_x2<0> + transmission_kernel_x2<16, 8, 8, 2, 0>", "achieved": achieved,
                      "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
                      "peak_source": peak_kind, "kernel_ms": kern_ms, "algorithmic_bytes": alg,
                      "distinct_table_rows": rows_e + rows_t},

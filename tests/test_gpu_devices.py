@@ -11,6 +11,14 @@ import pytest
 import goldenlib
 from bear_gb300.retrieval import BatchEvaluator, Engine
 
+
+def _device_count():
+    try:
+        import torch
+        return torch.cuda.device_count()
+    except Exception:
+        return 0
+
 pytestmark = pytest.mark.gpu
 
 
@@ -36,7 +44,7 @@ def test_calls_keep_the_current_device():
     e.close()
 
 
-@pytest.mark.skipif("torch.cuda.device_count() < 2", reason="needs two GPUs")
+@pytest.mark.skipif(_device_count() < 2, reason="needs two GPUs")
 def test_model_on_another_device():
     import torch
 
