@@ -555,8 +555,10 @@ void alloc_transmission_grad(Model& m, int chunk, int V, bool store) {
   const size_t B = chunk, L = m.L, N = m.N;
   g.tr_store = store;
   if (store) {
-    BGB_CUDA(cudaMalloc(&g.taps.tr_ts, B * L * (size_t)m.acfg.S * N * sizeof(float2)));
-    BGB_CUDA(cudaMalloc(&g.taps.tr_dk, B * L * N * sizeof(float2)));
+    // two spare entries at the end of the arrays the level-sink pass streams (whole 16-byte
+    // units of an odd-length last row)
+    BGB_CUDA(cudaMalloc(&g.taps.tr_ts, (B * L * (size_t)m.acfg.S * N + 2) * sizeof(float2)));
+    BGB_CUDA(cudaMalloc(&g.taps.tr_dk, (B * L * N + 2) * sizeof(float2)));
   }
   const size_t n = B * L * N, tiles = (N + 31) / 32;
   BGB_CUDA(cudaMalloc(&g.taps.tr_c, n * sizeof(float2)));
@@ -565,20 +567,23 @@ void alloc_transmission_grad(Model& m, int chunk, int V, bool store) {
   BGB_CUDA(cudaMalloc(&g.taps.tr_us, n * sizeof(float2)));
   BGB_CUDA(cudaMalloc(&g.taps.tr_I, n * sizeof(short)));
   BGB_CUDA(cudaMalloc(&g.taps.tr_geo, B * 4 * L * L * sizeof(float2)));
-  BGB_CUDA(cudaMalloc(&g.tr_gc, n * sizeof(float2)));
-  BGB_CUDA(cudaMalloc(&g.tr_gz, n * sizeof(float2)));
+  BGB_CUDA(cudaMalloc(&g.tr_gc, (n + 2) * sizeof(float2)));
+  BGB_CUDA(cudaMalloc(&g.tr_gz, (n + 2) * sizeof(float2)));
   BGB_CUDA(cudaMalloc(&g.tr_rp, B * tiles * sizeof(double)));
   BGB_CUDA(cudaMalloc(&g.partial, B * L * (size_t)V * sizeof(double)));
 }
 
 // ------------------------------------------------------------------ pass 2b, streamed
-// tr_adjoint_pass2b's sums (its stored-terms path with wavenumbers in pairs, N even) with the
-// rows it reads streamed through shared memory by bulk asynchronous copies: per
-// (evaluation, level) block and tile of kStreamTile wavenumbers the S opacity-term rows, the
-// R Rayleigh cross-section rows, g_z, the temperature-slope sums and the two g_c rows
-// (kStreamStages tiles in flight). Thread tid takes the pair k0 + 2 tid, k0 + 2 tid + 1 of
-// each tile, so every sum receives the same terms in the same order as in
-// tr_adjoint_pass2b<VP, true>, and the partial sums are equal bit for bit. A pair with a
+// tr_adjoint_pass2b's sums (its stored-terms path) with the rows it reads streamed through
+// shared memory by bulk asynchronous copies: per (evaluation, level) block and tile of
+// kStreamTile wavenumbers the S opacity-term rows, the R Rayleigh cross-section rows, g_z,
+// the temperature-slope sums and the two g_c rows (STAGES tiles in flight: three where two
+// blocks per SM fit, else two). With PAIRS (N even) thread tid takes the pair k0 + 2 tid,
+// k0 + 2 tid + 1 of each tile, as tr_adjoint_pass2b<VP, true> does; otherwise the single
+// wavenumbers k0 + tid and k0 + 128 + tid, as tr_adjoint_pass2b<VP, false> does (rows of odd
+// length start on 8-byte boundaries: each copy starts at the 16-byte unit holding its first
+// entry, and the arrays end with a spare 16-byte unit). Every sum receives the same terms
+// in the same order as in that kernel, so the partial sums are equal bit for bit. A pair with a
 // term outside the float range (no stored slope) recomputes its terms from the level table
 // as that kernel does. If a copy does not complete within the bounded wait, the block's
 // partial sums are set to NaN (the gradient of that evaluation reads NaN) and the block
@@ -590,7 +595,7 @@ void alloc_transmission_grad(Model& m, int chunk, int V, bool store) {
 // register-streamed tr_adjoint_pass2b took 9.3 ms and a version refilling stages after a
 // block barrier 8.2 ms.
 constexpr int kStreamTile = 256;  // wavenumbers per tile (128 pairs, one per thread)
-constexpr int kStreamStages = 3;
+constexpr int kStreamMaxSeg = 40;  // segments per tile: S + R + 4 with S + R <= 36
 
 // level_kappa_df_cb's term of one species (same arithmetic): t (zero if outside the float
 // range, then w holds it in FP64 and wide is set), lo and hi the level-table values
@@ -619,58 +624,108 @@ __device__ __forceinline__ void species_term_df(const float2* __restrict__ ltab,
   }
 }
 
-template <int VP>
+// tr_adjoint_pass2b's one() for a wavenumber without a stored slope sum (a term outside the
+// float range): the S species contributions gx t_s (+ the FP64 part) into xs, and the
+// temperature contribution returned; kept out of line so that the streamed kernel's
+// common path carries no per-species arrays.
+__device__ __noinline__ df2 tr_sink_recompute(const DeviceModel& dm, const LevelSpeciesDF* __restrict__ sfl,
+                                              const float2* __restrict__ dwl, int k, const ExpTables& et, df2 gx,
+                                              df2* xs) {
+  const int S = dm.S;
+  const size_t N = dm.N;
+  df2 dk = {0.0f, 0.0f};
+  double dkw = 0.0;
+  bool wide = false;
+  double tw[32];
+  for (int q = 0; q < S; ++q) {
+    bool is_wide;
+    df2 lo, hi;
+    species_term_df(dm.ltab, N, sfl + q, k, et, xs[q], tw[q], is_wide, lo, hi);
+    const float2 d = __ldg(dwl + q);
+    if (d.x != 0.0f) {
+      const df2 slope = df_mul(df_sub(hi, lo), df2{d.x, d.y});
+      if (is_wide) dkw += tw[q] * df_to_double(slope);
+      else dk = df_add(dk, df_mul(xs[q], slope));
+    }
+    wide = wide || is_wide;
+  }
+  df2 gT = df_mul(gx, df_mul(dk, df2{kLn2Hi, kLn2Lo}));
+  if (wide) gT = df_add(gT, df_from_double(df_to_double(gx) * dkw * 0.693147180559945309));
+  for (int q = 0; q < S; ++q) {
+    df2 x = df_mul(gx, xs[q]);
+    if (wide) x = df_add(x, df_from_double(df_to_double(gx) * tw[q]));
+    xs[q] = x;
+  }
+  return gT;
+}
+
+template <int VP, int STAGES, bool PAIRS>
 __global__ void __launch_bounds__(kTrSinkThreads + 32, 2) tr_adjoint_pass2b_stream(DeviceModel dm, TrArgs a, int nseg) {
-  static_assert(kStreamTile == 2 * kTrSinkThreads, "one pair per thread and tile");
+  static_assert(kStreamTile == 2 * kTrSinkThreads, "two wavenumbers per thread and tile");
   constexpr int G = 32 / VP, NW = kTrSinkThreads / 32;
+  constexpr int SEG = kStreamTile + 2;  // entries per staged segment (one spare 16-byte unit)
   __shared__ ExpTables et;
   __shared__ float2 red[NW][VP];
-  __shared__ __align__(8) uint64_t full[kStreamStages], empty[kStreamStages];
+  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES];
   __shared__ float2 rn_s[32];
   __shared__ volatile int abort_s, issued_s;
+  __shared__ const float2* seg_src[kStreamMaxSeg];  // 16-byte unit holding the row's first entry
+  __shared__ int seg_sh[kStreamMaxSeg];             // entries before the row's first in that unit
   extern __shared__ __align__(16) unsigned char tr2s_smem[];
-  float2* stage = reinterpret_cast<float2*>(tr2s_smem);  // [kStreamStages][nseg][kStreamTile]
+  float2* stage = reinterpret_cast<float2*>(tr2s_smem);  // [STAGES][nseg][SEG]
   const int S = dm.S, R = dm.R, L = dm.L;
   const int b = blockIdx.x, l = blockIdx.y, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const size_t N = dm.N;
-  const size_t row = ((size_t)b * L + l) * N;  // [b][l][k] of k = 0
-  const LevelSpeciesDF* sfl = a.lsdf + ((size_t)b * L + l) * S;
-  const float2* dwl = a.dwT + ((size_t)b * L + l) * S;
-  const float2* tsl = a.ts + ((size_t)b * L + l) * S * N;
+  const size_t bl = (size_t)b * L + l;
+  const size_t row = bl * N;  // [b][l][k] of k = 0
+  const LevelSpeciesDF* sfl = a.lsdf + bl * S;
+  const float2* dwl = a.dwT + bl * S;
   // segment order: S term rows, R Rayleigh rows, g_z, slope sums, g_c of levels l and l - 1
   const int sGZ = S + R, sDK = S + R + 1, sC0 = S + R + 2, sC1 = S + R + 3;
   const bool has_c0 = l <= L - 2, has_c1 = l >= 1;
   const int ntiles = (int)((N + kStreamTile - 1) / kStreamTile);
+  // first entry of each segment's row in its array (tiles start at even offsets)
+  auto row_start = [&](int seg) -> size_t {
+    if (seg < S) return (bl * S + seg) * N;
+    if (seg < S + R) return (size_t)(seg - S) * N;
+    if (seg == sC1) return row - N;
+    return row;
+  };
+  auto array_of = [&](int seg) -> const float2* {
+    if (seg < S) return a.ts;
+    if (seg < S + R) return dm.rayleigh_df;
+    if (seg == sGZ) return a.gz;
+    if (seg == sDK) return a.dk;
+    return a.gc;
+  };
+  auto used = [&](int seg) { return !((seg == sC0 && !has_c0) || (seg == sC1 && !has_c1)); };
   load_exp_tables(et);
   for (int r = tid; r < R; r += blockDim.x) {
-    const df2 d = df_from_double(__ldg(&a.ray_n[((size_t)b * L + l) * R + r]));
+    const df2 d = df_from_double(__ldg(&a.ray_n[bl * R + r]));
     rn_s[r] = make_float2(d.hi, d.lo);
   }
   if (tid == 0) {
     abort_s = 0;
     issued_s = 0;
-    for (int s = 0; s < kStreamStages; ++s) {
+    for (int s = 0; s < STAGES; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], NW);
     }
     fence_barrier_init();
   }
+  for (int seg = tid; seg < nseg; seg += blockDim.x) {
+    const size_t o = row_start(seg);
+    seg_sh[seg] = (int)(o & 1);
+    seg_src[seg] = array_of(seg) + (o & ~(size_t)1);
+  }
   __syncthreads();
-  auto src_of = [&](int seg, size_t k0) -> const float2* {
-    if (seg < S) return tsl + (size_t)seg * N + k0;
-    if (seg < S + R) return dm.rayleigh_df + (size_t)(seg - S) * N + k0;
-    if (seg == sGZ) return a.gz + row + k0;
-    if (seg == sDK) return a.dk + row + k0;
-    if (seg == sC0) return a.gc + row + k0;
-    return a.gc + row - N + k0;
-  };
   if (warp == NW) {
     // producer warp (one lane): refill each stage once the consumer warps released it
     if (lane == 0) {
       for (int it = 0; it < ntiles; ++it) {
-        const int st = it % kStreamStages;
-        if (it >= kStreamStages) {
-          if (!mbar_wait_bounded(&empty[st], (uint32_t)((it / kStreamStages - 1) & 1))) {
+        const int st = it % STAGES;
+        if (it >= STAGES) {
+          if (!mbar_wait_bounded(&empty[st], (uint32_t)((it / STAGES - 1) & 1))) {
             abort_s = 1;
             break;
           }
@@ -678,149 +733,147 @@ __global__ void __launch_bounds__(kTrSinkThreads + 32, 2) tr_adjoint_pass2b_stre
         }
         if (abort_s) break;
         const size_t k0 = (size_t)it * kStreamTile;
-        const uint32_t bytes = (uint32_t)(min((size_t)kStreamTile, N - k0) * sizeof(float2));
-        const int used = nseg - (has_c0 ? 0 : 1) - (has_c1 ? 0 : 1);
-        mbar_expect_tx(&full[st], bytes * (uint32_t)used);
-        float2* base = stage + (size_t)st * nseg * kStreamTile;
+        const int len = (int)min((size_t)kStreamTile, N - k0);
+        // each copy: whole 16-byte units from the one holding the tile's first entry
+        uint32_t total = 0;
+        for (int seg = 0; seg < nseg; ++seg)
+          if (used(seg)) total += (uint32_t)((seg_sh[seg] + len + 1) & ~1) * (uint32_t)sizeof(float2);
+        mbar_expect_tx(&full[st], total);
+        float2* base = stage + (size_t)st * nseg * SEG;
         for (int seg = 0; seg < nseg; ++seg) {
-          if ((seg == sC0 && !has_c0) || (seg == sC1 && !has_c1)) continue;
-          bulk_g2s(base + (size_t)seg * kStreamTile, src_of(seg, k0), bytes, &full[st]);
+          if (!used(seg)) continue;
+          const uint32_t bytes = (uint32_t)((seg_sh[seg] + len + 1) & ~1) * (uint32_t)sizeof(float2);
+          bulk_g2s(base + (size_t)seg * SEG, seg_src[seg] + k0, bytes, &full[st]);
         }
         issued_s = it + 1;
       }
     }
   } else {
-  df2 v[VP];
+    df2 v[VP];
 #pragma unroll
-  for (int q = 0; q < VP; ++q) v[q] = df2{0.0f, 0.0f};
-  const df2 z = {0.0f, 0.0f};
-  for (int it = 0; it < ntiles; ++it) {
-    const int st = it % kStreamStages;
-    if (!mbar_wait_bounded(&full[st], (uint32_t)((it / kStreamStages) & 1))) abort_s = 1;
-    if (abort_s) break;
-    const float2* base = stage + (size_t)st * nseg * kStreamTile;
-    auto sg4 = [&](int seg) { return reinterpret_cast<const float4*>(base + (size_t)seg * kStreamTile)[tid]; };
-    const int k0 = it * kStreamTile + 2 * tid;
-    if (k0 < (int)N) {
-      df2 gx0 = z, gx1 = z;
-      if (has_c0) {
-        const float4 c = sg4(sC0);
-        gx0 = df2{c.x, c.y};
-        gx1 = df2{c.z, c.w};
-      }
-      if (has_c1) {
-        const float4 c = sg4(sC1);
-        gx0 = df_add(gx0, df2{c.x, c.y});
-        gx1 = df_add(gx1, df2{c.z, c.w});
-      }
-      const float4 gz = sg4(sGZ);
-      const float4 dks = sg4(sDK);
-      if (isnan(dks.x) || isnan(dks.z)) {
-        // per wavenumber, in order; an element without a stored slope recomputes its terms
-#pragma unroll 1
-        for (int e = 0; e < 2; ++e) {
-          const int k = k0 + e;
-          const df2 gx = e ? gx1 : gx0;
-          const float2 dke = e ? make_float2(dks.z, dks.w) : make_float2(dks.x, dks.y);
-          const bool stored = !isnan(dke.x);
-          df2 dk = z, tq[VP];
-          double dkw = 0.0, twq[VP];
-          bool wide = false;
+    for (int q = 0; q < VP; ++q) v[q] = df2{0.0f, 0.0f};
+    const df2 z = {0.0f, 0.0f};
+    for (int it = 0; it < ntiles; ++it) {
+      const int st = it % STAGES;
+      if (!mbar_wait_bounded(&full[st], (uint32_t)((it / STAGES) & 1))) abort_s = 1;
+      if (abort_s) break;
+      const float2* base = stage + (size_t)st * nseg * SEG;
+      const int k0 = it * kStreamTile;
+      // entry idx of the tile in segment seg (past the copy's leading entry, if any)
+      auto sg2 = [&](int seg, int idx) { return base[seg * SEG + seg_sh[seg] + idx]; };
+      // one wavenumber (tr_adjoint_pass2b's one(), stored or recomputed terms)
+      auto single = [&](int k, int idx) {
+        df2 gx = z;
+        if (has_c0) {
+          const float2 c = sg2(sC0, idx);
+          gx = df2{c.x, c.y};
+        }
+        if (has_c1) {
+          const float2 c = sg2(sC1, idx);
+          gx = df_add(gx, df2{c.x, c.y});
+        }
+        const float2 gz = sg2(sGZ, idx), dke = sg2(sDK, idx);
+        const bool stored = !isnan(dke.x);
+        df2 xs[32];  // recomputed species contributions (rare path)
+        const df2 gT = stored ? df_mul(gx, df_mul(df2{dke.x, dke.y}, df2{kLn2Hi, kLn2Lo}))
+                              : tr_sink_recompute(dm, sfl, dwl, k, et, gx, xs);
 #pragma unroll
-          for (int q = 0; q < VP; ++q) {
-            tq[q] = z;
-            twq[q] = 0.0;
-            if (q >= S) continue;
+        for (int q = 0; q < VP; ++q) {
+          df2 x = z;
+          if (q < S) {
             if (stored) {
-              const float4 t = sg4(q);
-              tq[q] = e ? df2{t.z, t.w} : df2{t.x, t.y};
-              continue;
+              const float2 t = sg2(q, idx);
+              x = df_mul(gx, df2{t.x, t.y});
+            } else {
+              x = xs[q];
             }
-            bool is_wide;
-            df2 lo, hi;
-            species_term_df(dm.ltab, N, sfl + q, k, et, tq[q], twq[q], is_wide, lo, hi);
-            const float2 d = __ldg(dwl + q);
-            if (d.x != 0.0f) {
-              const df2 slope = df_mul(df_sub(hi, lo), df2{d.x, d.y});
-              if (is_wide) dkw += twq[q] * df_to_double(slope);
-              else dk = df_add(dk, df_mul(tq[q], slope));
-            }
-            wide = wide || is_wide;
+          } else if (q < S + R) {
+            const float2 sr = sg2(q, idx);
+            const float2 nr = rn_s[q - S];
+            x = df_mul(gx, df_mul(df2{sr.x, sr.y}, df2{nr.x, nr.y}));
+          } else if (q == S + R) {
+            x = gT;
+          } else if (q == S + R + 1) {
+            x = df2{gz.x, gz.y};
+          } else if (q == S + R + 2) {
+            x = gx;
           }
-          if (stored) dk = df2{dke.x, dke.y};
-          df2 gT = df_mul(gx, df_mul(dk, df2{kLn2Hi, kLn2Lo}));
-          if (wide) gT = df_add(gT, df_from_double(df_to_double(gx) * dkw * 0.693147180559945309));
+          v[q] = df_add(v[q], x);
+        }
+      };
+      if (!PAIRS) {
+        if (k0 + tid < (int)N) single(k0 + tid, tid);
+        if (k0 + kTrSinkThreads + tid < (int)N) single(k0 + kTrSinkThreads + tid, kTrSinkThreads + tid);
+      } else if (k0 + 2 * tid < (int)N) {
+        auto sg4 = [&](int seg) { return reinterpret_cast<const float4*>(base + (size_t)seg * SEG)[tid]; };
+        const float4 dks = sg4(sDK);
+        if (isnan(dks.x) || isnan(dks.z)) {
+          // a term outside the float range: per wavenumber, in order
+          single(k0 + 2 * tid, 2 * tid);
+          single(k0 + 2 * tid + 1, 2 * tid + 1);
+        } else {
+          df2 gx0 = z, gx1 = z;
+          if (has_c0) {
+            const float4 c = sg4(sC0);
+            gx0 = df2{c.x, c.y};
+            gx1 = df2{c.z, c.w};
+          }
+          if (has_c1) {
+            const float4 c = sg4(sC1);
+            gx0 = df_add(gx0, df2{c.x, c.y});
+            gx1 = df_add(gx1, df2{c.z, c.w});
+          }
+          const float4 gz = sg4(sGZ);
+          const df2 gT0 = df_mul(gx0, df_mul(df2{dks.x, dks.y}, df2{kLn2Hi, kLn2Lo}));
+          const df2 gT1 = df_mul(gx1, df_mul(df2{dks.z, dks.w}, df2{kLn2Hi, kLn2Lo}));
 #pragma unroll
           for (int q = 0; q < VP; ++q) {
-            df2 x = z;
+            df2 x0 = z, x1 = z;
             if (q < S) {
-              x = df_mul(gx, tq[q]);
-              if (wide) x = df_add(x, df_from_double(df_to_double(gx) * twq[q]));
+              const float4 t = sg4(q);
+              x0 = df_mul(gx0, df2{t.x, t.y});
+              x1 = df_mul(gx1, df2{t.z, t.w});
             } else if (q < S + R) {
               const float4 sr = sg4(q);
               const float2 nr = rn_s[q - S];
-              x = df_mul(gx, df_mul(e ? df2{sr.z, sr.w} : df2{sr.x, sr.y}, df2{nr.x, nr.y}));
+              x0 = df_mul(gx0, df_mul(df2{sr.x, sr.y}, df2{nr.x, nr.y}));
+              x1 = df_mul(gx1, df_mul(df2{sr.z, sr.w}, df2{nr.x, nr.y}));
             } else if (q == S + R) {
-              x = gT;
+              x0 = gT0;
+              x1 = gT1;
             } else if (q == S + R + 1) {
-              x = e ? df2{gz.z, gz.w} : df2{gz.x, gz.y};
+              x0 = df2{gz.x, gz.y};
+              x1 = df2{gz.z, gz.w};
             } else if (q == S + R + 2) {
-              x = gx;
+              x0 = gx0;
+              x1 = gx1;
             }
-            v[q] = df_add(v[q], x);
+            v[q] = df_add(df_add(v[q], x0), x1);
           }
-        }
-      } else {
-        const df2 gT0 = df_mul(gx0, df_mul(df2{dks.x, dks.y}, df2{kLn2Hi, kLn2Lo}));
-        const df2 gT1 = df_mul(gx1, df_mul(df2{dks.z, dks.w}, df2{kLn2Hi, kLn2Lo}));
-#pragma unroll
-        for (int q = 0; q < VP; ++q) {
-          df2 x0 = z, x1 = z;
-          if (q < S) {
-            const float4 t = sg4(q);
-            x0 = df_mul(gx0, df2{t.x, t.y});
-            x1 = df_mul(gx1, df2{t.z, t.w});
-          } else if (q < S + R) {
-            const float4 sr = sg4(q);
-            const float2 nr = rn_s[q - S];
-            x0 = df_mul(gx0, df_mul(df2{sr.x, sr.y}, df2{nr.x, nr.y}));
-            x1 = df_mul(gx1, df_mul(df2{sr.z, sr.w}, df2{nr.x, nr.y}));
-          } else if (q == S + R) {
-            x0 = gT0;
-            x1 = gT1;
-          } else if (q == S + R + 1) {
-            x0 = df2{gz.x, gz.y};
-            x1 = df2{gz.z, gz.w};
-          } else if (q == S + R + 2) {
-            x0 = gx0;
-            x1 = gx1;
-          }
-          v[q] = df_add(df_add(v[q], x0), x1);
         }
       }
+      // this warp is done with the stage
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[st]);
     }
-    // this warp is done with the stage
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[st]);
-  }
-  const df2 r = warp_reduce_scatter<VP>(v, lane);
-  if (lane % G == 0) red[warp][lane / G] = make_float2(r.hi, r.lo);
+    const df2 r = warp_reduce_scatter<VP>(v, lane);
+    if (lane % G == 0) red[warp][lane / G] = make_float2(r.hi, r.lo);
   }
   __syncthreads();
   if (abort_s) {
     // wait (bounded) for the copies still in flight, then mark the block's sums invalid
     if (tid == 0)
-      for (int it = max(0, issued_s - kStreamStages); it < issued_s; ++it)
-        mbar_wait_bounded(&full[it % kStreamStages], (uint32_t)((it / kStreamStages) & 1));
+      for (int it = max(0, issued_s - STAGES); it < issued_s; ++it)
+        mbar_wait_bounded(&full[it % STAGES], (uint32_t)((it / STAGES) & 1));
     __syncthreads();
-    if (tid < a.V) a.partial[((size_t)b * L + l) * a.V + tid] = __longlong_as_double(0x7ff8000000000000LL);
+    if (tid < a.V) a.partial[bl * a.V + tid] = __longlong_as_double(0x7ff8000000000000LL);
     return;
   }
   if (tid < a.V) {
     df2 sum = {red[0][tid].x, red[0][tid].y};
 #pragma unroll
     for (int w = 1; w < NW; ++w) sum = df_add(sum, df2{red[w][tid].x, red[w][tid].y});
-    a.partial[((size_t)b * L + l) * a.V + tid] = df_to_double(sum);
+    a.partial[bl * a.V + tid] = df_to_double(sum);
   }
 }
 
@@ -851,16 +904,25 @@ void transmission_adjoint_chunk(Model& m, const double* params_chunk, int nb, cu
   // wavenumbers in pairs (16-byte reads) when N is even; with the opacity terms stored, the
   // rows streamed through shared memory by bulk copies (16-byte aligned rows need N even)
   const bool pairs = (N % 2) == 0;
+  // three stages of tiles in flight where two blocks per SM still fit, else two
   const int nseg = S + m.acfg.R + 4;
-  const size_t sms = (size_t)kStreamStages * nseg * kStreamTile * sizeof(float2);
-  if (pairs && tp.tr_ts && m.acfg.R <= 32 && sms <= 200 * 1024) {
+  const size_t stage_bytes = (size_t)nseg * (kStreamTile + 2) * sizeof(float2);
+  const int stages = 3 * stage_bytes <= 110 * 1024 ? 3 : 2;
+  const size_t sms = stages * stage_bytes;
+  if (tp.tr_ts && m.acfg.R <= 32 && nseg <= kStreamMaxSeg && sms <= 200 * 1024) {
     auto gos = [&](auto kernel) {
       BGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sms));
       kernel<<<dim3(nb, L), kTrSinkThreads + 32, sms, st>>>(dm, a, nseg);
     };
-    if (VP == 8) gos(tr_adjoint_pass2b_stream<8>);
-    else if (VP == 16) gos(tr_adjoint_pass2b_stream<16>);
-    else gos(tr_adjoint_pass2b_stream<32>);
+    if (stages == 3) {
+      if (VP == 8) pairs ? gos(tr_adjoint_pass2b_stream<8, 3, true>) : gos(tr_adjoint_pass2b_stream<8, 3, false>);
+      else if (VP == 16) pairs ? gos(tr_adjoint_pass2b_stream<16, 3, true>) : gos(tr_adjoint_pass2b_stream<16, 3, false>);
+      else pairs ? gos(tr_adjoint_pass2b_stream<32, 3, true>) : gos(tr_adjoint_pass2b_stream<32, 3, false>);
+    } else {
+      if (VP == 8) pairs ? gos(tr_adjoint_pass2b_stream<8, 2, true>) : gos(tr_adjoint_pass2b_stream<8, 2, false>);
+      else if (VP == 16) pairs ? gos(tr_adjoint_pass2b_stream<16, 2, true>) : gos(tr_adjoint_pass2b_stream<16, 2, false>);
+      else pairs ? gos(tr_adjoint_pass2b_stream<32, 2, true>) : gos(tr_adjoint_pass2b_stream<32, 2, false>);
+    }
   } else if (VP == 8) pairs ? go2(tr_adjoint_pass2b<8, true>) : go2(tr_adjoint_pass2b<8, false>);
   else if (VP == 16) pairs ? go2(tr_adjoint_pass2b<16, true>) : go2(tr_adjoint_pass2b<16, false>);
   else pairs ? go2(tr_adjoint_pass2b<32, true>) : go2(tr_adjoint_pass2b<32, false>);

@@ -1381,7 +1381,9 @@ void upload_model(Model& m) {
   dm.cloud_kind = m.acfg.cloud_kind;
   dm.rayleigh = dev_upload(m, ray);
   {
-    std::vector<float2> rdf(ray.size());
+    // two zero entries past the last row: whole 16-byte units of the last row can be
+    // bulk-copied when the row length is odd
+    std::vector<float2> rdf(ray.size() + 2, make_float2(0.0f, 0.0f));
     for (size_t i = 0; i < ray.size(); ++i) rdf[i] = split_df(ray[i]);
     dm.rayleigh_df = dev_upload(m, rdf);
   }
