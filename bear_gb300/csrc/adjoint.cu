@@ -641,6 +641,11 @@ struct SweepArgs {
 // Five blocks per SM (96 registers, a few spilled): 55.7 ms for the gradient of 512
 // evaluations of 80 levels x 10257 points, against 56.7 ms at 128 registers and 58.7 ms
 // unbounded (152 registers, three blocks per SM).
+// CLOUD (power-law and KH clouds): the layer's cloud depth is cloud_l f_k with the
+// wavelength factor f_k of the evaluation's cloud parameters, so the cloud sink of level l
+// is sum_k g_tau f_k, and value S + 3 + c of level 0 receives
+// sum_k (sum_l g_tau cloud_l) df_k/dtheta_c for the NC shape parameters theta_c.
+template <bool CLOUD>
 __global__ void __launch_bounds__(kAdjThreads, 5) emission_adjoint_sweep_kernel(DeviceModel dm, SweepArgs a) {
   constexpr int NW = kAdjThreads / 32;
   __shared__ ExpTables et;
@@ -706,6 +711,14 @@ __global__ void __launch_bounds__(kAdjThreads, 5) emission_adjoint_sweep_kernel(
 
   const df2 z = {0.0f, 0.0f};
   const dfx zx = dfx_bcast(z);
+  // non-grey cloud: the wavelength factors as the forward pass forms them, and the
+  // per-wavenumber sum of g_tau cloud_l over the layers
+  dfx csx = zx, wc = zx;
+  if (CLOUD) {
+    const int k0 = min((int)(blockIdx.y * 2 * kAdjThreads + tid), dm.N - 1);
+    const int k1 = min((int)(blockIdx.y * 2 * kAdjThreads + kAdjThreads + tid), dm.N - 1);
+    csx = dfx_make(df_from_double(cloud_shape(dm, a.ev[b], k0)), df_from_double(cloud_shape(dm, a.ev[b], k1)));
+  }
   dfx lam1 = dfx_make(df_from_double(sd[0] * kMu[0]), df_from_double(sd[1] * kMu[0]));
   dfx lam2 = dfx_make(df_from_double(sd[0] * kMu[1]), df_from_double(sd[1] * kMu[1]));
   dfx B_l = planck_dfx(c1, c2l, invT(L - 1), et);
@@ -715,7 +728,7 @@ __global__ void __launch_bounds__(kAdjThreads, 5) emission_adjoint_sweep_kernel(
     const float4 ta = lay[0][(size_t)l * N], tb = lay[1][(size_t)l * N];
     const dfx t = {make_float2(ta.x, tb.x), make_float2(ta.y, tb.y)};
     const dfx ksh = {make_float2(ta.z, tb.z), make_float2(ta.w, tb.w)};
-    const float2 gz = __ldg(reinterpret_cast<const float2*>(&lv[l - 1].dzh_hi));
+    const float4 gz = __ldg(reinterpret_cast<const float4*>(&lv[l - 1].dzh_hi));  // dzh, cloud
     const dfx dzh = dfx_bcast(df2{gz.x, gz.y});
     dfx gB_m = zx, gtau = zx;
     const bool nz0 = t.hi.x != 0.0f, nz1 = t.hi.y != 0.0f;
@@ -749,7 +762,8 @@ __global__ void __launch_bounds__(kAdjThreads, 5) emission_adjoint_sweep_kernel(
     emit3(l, dfx_mul(gB_l, dplanck(l, B_l)), gdz_l, gcl_l);
     // layer l's own sinks belong to lev[l-1] (its dz and cloud)
     gdz_l = dfx_mul(gtau, ksh);
-    gcl_l = gtau;
+    gcl_l = CLOUD ? dfx_mul(gtau, csx) : gtau;
+    if (CLOUD && gz.z != 0.0f) wc = dfx_fma(gtau, dfx_bcast(df2{gz.z, gz.w}), wc);
     gK_l = dfx_mul(gtau, dzh);
     gB_l = gB_m;
     B_l = B_m;
@@ -758,6 +772,31 @@ __global__ void __launch_bounds__(kAdjThreads, 5) emission_adjoint_sweep_kernel(
   if (act[0]) gKo[0][0] = make_float2(gK_l.hi.x, gK_l.lo.x);
   if (act[1]) gKo[1][0] = make_float2(gK_l.hi.y, gK_l.lo.y);
   emit3(0, dfx_mul(gB_l, dplanck(0, B_l)), gdz_l, gcl_l);
+  if (CLOUD) {
+    // sum_k w_k df_k/dtheta_c over the block, into value S + 3 + c of level 0
+    const int nc = dm.cloud_kind == 1 ? 1 : 3;
+    double v[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      if (!act[e]) continue;
+      const int k = blockIdx.y * 2 * kAdjThreads + e * kAdjThreads + tid;
+      double d[3];
+      cloud_shape_tangent(dm, a.ev[b], k, d);
+      const double w = df_to_double(dfx_get(wc, e));
+      for (int c = 0; c < nc; ++c) v[c] = fma(w, d[c], v[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) v[c] = warp_sum_d(v[c]);
+    if (lane == 0)
+      for (int c = 0; c < 3; ++c) red[warp][c] = v[c];
+    __syncthreads();
+    if (tid < nc) {
+      double sum = 0.0;
+#pragma unroll
+      for (int w = 0; w < NW; ++w) sum += red[w][tid];
+      a.partial[(((size_t)b * L + 0) * a.V + dm.S + 3 + tid) * a.tiles_total + blockIdx.y] = sum;
+    }
+  }
 }
 
 struct SinkArgs {
@@ -1011,6 +1050,11 @@ __global__ void __launch_bounds__(kAdjThreads) atmosphere_adjoint_kernel(
           l < L - 1)
         acc = fma(sgl[S + 2], cloud_d, acc);
     }
+    // non-grey cloud shape parameters (after the optical depth): value S + 3 + c of level 0
+    if (ch == 0 && c.cloud && c.cloud_kind) {
+      const int cs = th - ci - 1;
+      if (cs >= 0 && cs < (c.cloud_kind == 1 ? 1 : 3)) acc += sg[S + 3 + cs];
+    }
     // radius-distance scaling (R_J / d)^2 f, once (chunk 0); the secondary eclipse has
     // none (its R_p / R_s and stellar derivatives come from the likelihood adjoint)
     if (ch == 0 && dm.star_model == 0) {
@@ -1146,13 +1190,17 @@ static void launch_gradient_transmission(Model& m, const double* params_dev, int
 void launch_gradient(Model& m, const double* params_dev, int batch, cudaStream_t st, double* loglike_dev,
                      double* grad_dev, uint8_t* neglect_dev) {
   if (m.hm) throw Error(BEAR_ERR_UNSUPPORTED, "no gradient for models with the H- continuum");
-  if (m.acfg.cloud_kind) throw Error(BEAR_ERR_UNSUPPORTED, "no gradient for the power-law and KH clouds");
+  if (m.acfg.cloud_kind && (m.transmission || m.precision != 0))
+    throw Error(BEAR_ERR_UNSUPPORTED, "power-law and KH cloud gradients: emission models, precision mode 0");
   if (m.transmission) {
     launch_gradient_transmission(m, params_dev, batch, st, loglike_dev, grad_dev, neglect_dev);
     return;
   }
   const int S = m.acfg.S, L = m.L, P = m.acfg.nparam_total;
-  const int V = S + 3;
+  // level values: species, temperature, layer thickness, cloud, then (level 0 only) the
+  // derivatives along the non-grey cloud's shape parameters
+  const int NC = m.acfg.cloud_kind == 1 ? 1 : m.acfg.cloud_kind == 2 ? 3 : 0;
+  const int V = S + 3 + NC;
   if (V > 32) throw Error(BEAR_ERR_UNSUPPORTED, "the gradient supports at most 29 table species");
   if (P > kAdjThreads) throw Error(BEAR_ERR_UNSUPPORTED, "the gradient supports at most 128 parameters");
   const bool df = m.precision == 0;
@@ -1190,7 +1238,8 @@ void launch_gradient(Model& m, const double* params_dev, int batch, cudaStream_t
     if (df) {
       BGB_CUDA(cudaMemsetAsync(g.partial, 0, (size_t)nb * L * V * tiles * sizeof(double), st));
       SweepArgs sa{w.lev, w.ev, g.taps.istore, g.taps.em_layer, g.gS, g.seed, g.em_gK, g.partial, V, tiles};
-      emission_adjoint_sweep_kernel<<<grid, kAdjThreads, 0, st>>>(m.dm, sa);
+      if (m.acfg.cloud_kind) emission_adjoint_sweep_kernel<true><<<grid, kAdjThreads, 0, st>>>(m.dm, sa);
+      else emission_adjoint_sweep_kernel<false><<<grid, kAdjThreads, 0, st>>>(m.dm, sa);
       BGB_CUDA(cudaGetLastError());
       if (S > 0) {
         SinkArgs ka{w.lsdf, g.taps.dwT, g.em_gK, g.partial, V, tiles, tiles_a};

@@ -154,6 +154,31 @@ __device__ __forceinline__ double cloud_shape(const DeviceModel& dm, const EvalI
   return e.cs[3] / (e.cs[0] * pow(x, -e.cs[1]) + pow(x, 0.2));
 }
 
+// Derivatives of cloud_shape along the cloud's shape parameters, FP64: power law
+// d/d a of (wl / wl_ref)^a; KH d/d q0, d/d a0, d/d r of Q_ref / Q with
+// Q = q0 x^-a0 + x^0.2, x = 2 pi r / wl (Q_ref at the reference wavelength).
+__device__ __forceinline__ void cloud_shape_tangent(const DeviceModel& dm, const EvalInfo& e, int k, double d[3]) {
+  const double wl = __ldg(&dm.wl[k]);
+  const double wl_ref = dm.cfg->cloud_ref_wl;
+  d[0] = d[1] = d[2] = 0.0;
+  if (dm.cloud_kind == 1) {
+    d[0] = pow(wl, e.cs[0]) / e.cs[3] * (log(wl) - log(wl_ref));
+    return;
+  }
+  const double q0 = e.cs[0], a0 = e.cs[1], tpr = e.cs[2];
+  const double x = tpr / wl, xr = tpr / wl_ref;
+  const double xa = pow(x, -a0), xra = pow(xr, -a0);
+  const double Q = q0 * xa + pow(x, 0.2), Qr = e.cs[3];
+  const double f = Qr / Q;
+  // dQ/dr = dQ/dx dx/dr with dQ/dx = (-a0 q0 x^-a0 + 0.2 x^0.2) / x and dx/dr = x / r
+  const double r = tpr / (2.0 * kPi);
+  const double dQ_dr = (-a0 * q0 * xa + 0.2 * pow(x, 0.2)) / r;
+  const double dQr_dr = (-a0 * q0 * xra + 0.2 * pow(xr, 0.2)) / r;
+  d[0] = f * (xra / Qr - xa / Q);                                  // q0
+  d[1] = f * (-q0 * xra * log(xr) / Qr + q0 * xa * log(x) / Q);    // a0
+  d[2] = f * (dQr_dr / Qr - dQ_dr / Q);                            // r
+}
+
 // 1/mu_i of the Gauss angles as double-floats.
 constexpr float kInvMuF[2][2] = {{(float)(1.0 / 0.211324865405187),
                                   (float)(1.0 / 0.211324865405187 - (double)(float)(1.0 / 0.211324865405187))},

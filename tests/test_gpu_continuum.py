@@ -1,7 +1,8 @@
 """H- continuum (bound-free + free-free) in the batched emission workload (80 levels,
 6 line species, 11001 points at 1 cm^-1 from 0.8 um, H, H- and e- in the chemistry)
 against the FP64 oracle, and the double-float path against the FP64 path. Models
-with the H- continuum or a power-law / KH cloud have no gradient (BEAR_ERR_UNSUPPORTED)."""
+with the H- continuum, and transmission models with a power-law / KH cloud, have no gradient
+(BEAR_ERR_UNSUPPORTED)."""
 
 import dataclasses
 
@@ -91,9 +92,11 @@ def test_hminus_gradient_is_rejected(case):
     assert ei.value.code == 4
 
 
-def test_non_grey_cloud_gradient_is_rejected():
+def test_transmission_non_grey_cloud_gradient_is_rejected():
+    """The non-grey clouds have an adjoint for emission models (test_gpu_gradient_cloud.py);
+    the transmission adjoint rejects them."""
     import torch
-    c = [goldenlib.Case(p) for p in goldenlib.golden_cases() if p.endswith("emission_powerlaw_cloud.npz")][0]
+    c = [goldenlib.Case(p) for p in goldenlib.golden_cases() if p.endswith("transmission_kh_cloud.npz")][0]
     e = Engine(c.config_text(), c.observations())
     try:
         with pytest.raises(_lib.EngineError) as ei:
