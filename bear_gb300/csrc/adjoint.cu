@@ -805,6 +805,7 @@ struct SinkArgs {
   const float2* gK;
   double* partial;
   int V, tiles_total, tile0;  // this kernel's slots start at tile0
+  int hm_v0;                  // H- continuum: the value of its first coefficient (0: none)
 };
 
 constexpr int kSinkKPT = 4;  // wavenumbers per thread of the sink kernel
@@ -911,6 +912,18 @@ __global__ void __launch_bounds__(kAdjThreads) emission_adjoint_sinks_kernel(Dev
         }
       }
     }
+    // H- continuum: d log L / d (level coefficient c) = sum_k gK row_c (the rows after the
+    // Rayleigh rows), accumulators S .. S + kHmTerms - 1
+    if (a.hm_v0) {
+#pragma unroll
+      for (int j = 0; j < VP - 1; ++j) {  // compile-time accumulator index j = S + c
+        if (j < S || j >= S + kHmTerms) continue;
+        const float2* row = dm.rayleigh_df + (size_t)(dm.R_ray + j - S) * N;
+        const float2 ra = __ldg(row + ka), rb = __ldg(row + kb);
+        if (use_a) acc[j] = df_fma(gKa, df2{ra.x, ra.y}, acc[j]);
+        if (use_b) acc[j] = df_fma(gKb, df2{rb.x, rb.y}, acc[j]);
+      }
+    }
     // opacity part of d log L / dT: gK d kappa / dT (level-table values are log2: d 2^y / dy = 2^y ln 2)
 #pragma unroll
     for (int e = 0; e < 2; ++e) {
@@ -924,12 +937,14 @@ __global__ void __launch_bounds__(kAdjThreads) emission_adjoint_sinks_kernel(Dev
   const df2 r = warp_reduce_scatter<VP>(acc, lane);
   if (lane % G == 0) red[warp][lane / G] = df_to_double(r);
   __syncthreads();
-  // value slot j < S: species j; slot VP-1: temperature (value S of the partial sums)
-  if (tid < VP && (tid < S || tid == VP - 1)) {
+  // value slot j < S: species j; S .. S + 6 with the H- continuum: its coefficients (values
+  // hm_v0 ..); slot VP-1: temperature (value S of the partial sums)
+  const bool hm_slot = a.hm_v0 && tid >= S && tid < S + kHmTerms;
+  if (tid < VP && (tid < S || tid == VP - 1 || hm_slot)) {
     double sum = 0.0;
 #pragma unroll
     for (int w = 0; w < NW; ++w) sum += red[w][tid];
-    const int v = tid < S ? tid : S;
+    const int v = tid < S ? tid : hm_slot ? a.hm_v0 + tid - S : S;
     a.partial[(((size_t)b * L + l) * a.V + v) * a.tiles_total + a.tile0 + blockIdx.z] = sum;
   }
 }
@@ -1036,6 +1051,23 @@ __global__ void __launch_bounds__(kAdjThreads) atmosphere_adjoint_kernel(
       for (int s = 0; s < S; ++s)
         if (np[s] >= 0) acc = fma(sgl[s], dlnX[s] - np[s] * dlnT, acc);
       acc = fma(sgl[S], dT, acc);
+      if (c.hm) {
+        // H- continuum coefficients (atmosphere_kernel): h_0 = n(H-), h_i = (5040/T)^((i+1)/2)
+        // n(e-) k T n(H) for i >= 1 (zero, and held there, when n(H-) = 0); n_j = X_j p / (k T)
+        const double* sh = sgl + S + 3 + (c.cloud_kind == 1 ? 1 : c.cloud_kind == 2 ? 3 : 0);
+        const double nt = dm.pressure[l] * 1.e6 / kBoltzmann / T, dnt = -nt * dlnT;
+        const double nHm = X[SP_Hm] * nt, ne = X[SP_e] * nt, nH = X[SP_H] * nt;
+        const double dnHm = dX[SP_Hm] * nt + X[SP_Hm] * dnt;
+        const double dne = dX[SP_e] * nt + X[SP_e] * dnt, dnH = dX[SP_H] * nt + X[SP_H] * dnt;
+        acc = fma(sh[0], dnHm, acc);
+        if (nHm != 0.0)
+          for (int i = 1; i < kHmTerms; ++i) {
+            const double ex = (i + 1) / 2.0;
+            const double f = pow(5040.0 / T, ex);
+            const double dh = kBoltzmann * (f * (dne * T * nH + ne * dT * nH + ne * T * dnH) - ex * f * dlnT * ne * T * nH);
+            acc = fma(sh[i], dh, acc);
+          }
+      }
       // layer thickness Delta_l = 0.5 (p_{l-1} - p_l) 1e6 (u_l + u_{l-1}) / g (lev[l-1].dz)
       const double u = kGasConst * T / (mmw * dm.pressure[l] * 1e6);
       const double du = u * (dlnT - dmmw / mmw);
@@ -1189,7 +1221,8 @@ static void launch_gradient_transmission(Model& m, const double* params_dev, int
 
 void launch_gradient(Model& m, const double* params_dev, int batch, cudaStream_t st, double* loglike_dev,
                      double* grad_dev, uint8_t* neglect_dev) {
-  if (m.hm) throw Error(BEAR_ERR_UNSUPPORTED, "no gradient for models with the H- continuum");
+  if (m.hm && (m.transmission || m.precision != 0))
+    throw Error(BEAR_ERR_UNSUPPORTED, "H- continuum gradients: emission models, precision mode 0");
   if (m.acfg.cloud_kind && (m.transmission || m.precision != 0))
     throw Error(BEAR_ERR_UNSUPPORTED, "power-law and KH cloud gradients: emission models, precision mode 0");
   if (m.transmission) {
@@ -1200,7 +1233,7 @@ void launch_gradient(Model& m, const double* params_dev, int batch, cudaStream_t
   // level values: species, temperature, layer thickness, cloud, then (level 0 only) the
   // derivatives along the non-grey cloud's shape parameters
   const int NC = m.acfg.cloud_kind == 1 ? 1 : m.acfg.cloud_kind == 2 ? 3 : 0;
-  const int V = S + 3 + NC;
+  const int V = S + 3 + NC + (m.hm ? kHmTerms : 0);  // the H- coefficients last
   if (V > 32) throw Error(BEAR_ERR_UNSUPPORTED, "the gradient supports at most 29 table species");
   if (P > kAdjThreads) throw Error(BEAR_ERR_UNSUPPORTED, "the gradient supports at most 128 parameters");
   const bool df = m.precision == 0;
@@ -1225,7 +1258,7 @@ void launch_gradient(Model& m, const double* params_dev, int batch, cudaStream_t
     BGB_CUDA(cudaFuncSetAttribute(atmosphere_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem_atm));
   const int VP = value_slots(V);
-  const int VPB = value_slots(S + 1);
+  const int VPB = value_slots(S + 1 + (m.hm ? kHmTerms : 0));
   for (int c0 = 0; c0 < batch; c0 += chunk) {
     const int nb = std::min(chunk, batch - c0);
     const double* pc = params_dev + (size_t)c0 * P;
@@ -1242,7 +1275,7 @@ void launch_gradient(Model& m, const double* params_dev, int batch, cudaStream_t
       else emission_adjoint_sweep_kernel<false><<<grid, kAdjThreads, 0, st>>>(m.dm, sa);
       BGB_CUDA(cudaGetLastError());
       if (S > 0) {
-        SinkArgs ka{w.lsdf, g.taps.dwT, g.em_gK, g.partial, V, tiles, tiles_a};
+        SinkArgs ka{w.lsdf, g.taps.dwT, g.em_gK, g.partial, V, tiles, tiles_a, m.hm ? S + 3 + NC : 0};
         const dim3 gridb(nb, L, tiles_b);
         if (VPB == 8) emission_adjoint_sinks_kernel<8><<<gridb, kAdjThreads, 0, st>>>(m.dm, ka);
         else if (VPB == 16) emission_adjoint_sinks_kernel<16><<<gridb, kAdjThreads, 0, st>>>(m.dm, ka);

@@ -1544,7 +1544,7 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
     const size_t hm_smem = m.hm ? (size_t)L * kHmTerms * sizeof(float2) : 0;
     if (taps && m.precision == 1)
       emission_kernel_fp64<true><<<grid, TB, 0, st>>>(dm, w.lev, w.ls, w.ray_n, w.ev, w.spectrum, taps->istore);
-    else if (taps && m.acfg.cloud_kind)  // non-grey cloud (the gradient rejects H- models)
+    else if (taps && (m.acfg.cloud_kind || m.hm))  // non-grey cloud or H- continuum
       emission_kernel<true, true><<<grid, TB, hm_smem, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.spectrum,
                                                             taps->istore, taps->em_layer);
     else if (taps && pair)

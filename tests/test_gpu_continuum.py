@@ -1,8 +1,8 @@
 """H- continuum (bound-free + free-free) in the batched emission workload (80 levels,
 6 line species, 11001 points at 1 cm^-1 from 0.8 um, H, H- and e- in the chemistry)
-against the FP64 oracle, and the double-float path against the FP64 path. Models
-with the H- continuum, and transmission models with a power-law / KH cloud, have no gradient
-(BEAR_ERR_UNSUPPORTED)."""
+against the FP64 oracle, the double-float path against the FP64 path, and the emission
+gradient with the H- continuum against the oracle's differences. Transmission models with
+the H- continuum or a power-law / KH cloud have no gradient (BEAR_ERR_UNSUPPORTED)."""
 
 import dataclasses
 
@@ -84,12 +84,54 @@ def test_hminus_double_float_against_fp64(case):
     assert np.all(d <= 1e-8 + 1e-12 * ll_64.abs().cpu().numpy()), d.max()
 
 
-def test_hminus_gradient_is_rejected(case):
+def _fd(f, x, j, rel):
+    h = rel * abs(x[j])
+    xp, xm = x.copy(), x.copy()
+    xp[j] += h
+    xm[j] -= h
+    return (f(xp) - f(xm)) / (2 * h)
+
+
+def test_hminus_gradient_against_oracle(case):
+    """The emission adjoint with the H- continuum: the level sinks of its seven
+    coefficients (sum over wavenumbers of d log L / d kappa times the coefficient rows)
+    mapped through the coefficients' tangents (n(H-), n(e-) k T n(H) (5040/T)^((i+1)/2)),
+    every parameter against the oracle's Richardson central differences; at the point
+    without H- the free-free terms are held at zero."""
     import torch
     e, om, truth, ns = case
-    with pytest.raises(_lib.EngineError) as ei:
-        e.grad_batch(torch.tensor(truth[None, :], device="cuda"))
-    assert ei.value.code == 4
+    phys = _points(truth, ns, 3, 7)
+    phys[0] = truth
+    ll, g, ng = e.grad_batch(torch.tensor(phys, device="cuda"))
+    ll, g = ll.cpu().numpy(), g.cpu().numpy()
+    for i in range(len(phys)):
+        assert not ng[i]
+        x = phys[i]
+        assert abs(ll[i] - om.loglike(x)) <= 1e-8 + 1e-12 * abs(ll[i])
+        fd = np.zeros(len(x))
+        for j in range(len(x)):
+            if x[j] == 0.0:
+                continue  # a zero H- abundance: no relative step
+            fd[j] = (4 * _fd(om.loglike, x, j, 5e-6) - _fd(om.loglike, x, j, 1e-5)) / 3
+        sa, sf = x * g[i], x * fd
+        scale = np.max(np.abs(sf))
+        for j in range(len(x)):
+            err = abs(sa[j] - sf[j])
+            tol = 1e-6 * abs(sf[j]) + 1e-8 * scale + 2e-10 * abs(ll[i]) / 1e-5
+            assert err <= tol, (i, j, sa[j], sf[j], err, tol)
+
+
+def test_hminus_transmission_gradient_is_rejected():
+    """The transmission adjoint rejects models with the H- continuum."""
+    import torch
+    c = [goldenlib.Case(p) for p in goldenlib.golden_cases() if p.endswith("transmission_hminus.npz")][0]
+    e = Engine(c.config_text(), c.observations())
+    try:
+        with pytest.raises(_lib.EngineError) as ei:
+            e.grad_batch(torch.tensor(c.params[:1], device="cuda"))
+        assert ei.value.code == 4
+    finally:
+        e.close()
 
 
 def test_transmission_non_grey_cloud_gradient_is_rejected():
