@@ -1221,8 +1221,7 @@ static void launch_gradient_transmission(Model& m, const double* params_dev, int
 
 void launch_gradient(Model& m, const double* params_dev, int batch, cudaStream_t st, double* loglike_dev,
                      double* grad_dev, uint8_t* neglect_dev) {
-  if (m.hm && (m.transmission || m.precision != 0))
-    throw Error(BEAR_ERR_UNSUPPORTED, "H- continuum gradients: emission models, precision mode 0");
+  if (m.hm && m.precision != 0) throw Error(BEAR_ERR_UNSUPPORTED, "H- continuum gradients run in precision mode 0");
   if (m.acfg.cloud_kind && (m.transmission || m.precision != 0))
     throw Error(BEAR_ERR_UNSUPPORTED, "power-law and KH cloud gradients: emission models, precision mode 0");
   if (m.transmission) {

@@ -511,9 +511,19 @@ __global__ void __launch_bounds__(128) tr_atmosphere_adjoint_kernel(
     const double* sgl = sg + (size_t)l * V;
     for (int s = 0; s < S; ++s)
       if (np[s] >= 0) acc = fma(sgl[s], dlnX[s] - np[s] * dlnT, acc);
-    for (int r = 0; r < R; ++r) {
+    for (int r = 0; r < c.R_ray; ++r) {
       const int jr = c.ray_index[r];
       if (X[jr] != 0.0) acc = fma(sgl[S + r], dX[jr] / X[jr] - dlnT, acc);
+    }
+    if (c.hm && X[SP_Hm] != 0.0) {
+      // H- continuum: values S + R_ray + i are d log L / d ln h_i for the coefficients
+      // h_0 = n(H-) and h_i = (5040/T)^((i+1)/2) n(e-) k T n(H) (atmosphere_kernel); n_j = X_j p / (k T).
+      // A zero H or e- abundance makes h_i (i >= 1) zero, and its derivative is taken as zero.
+      acc = fma(sgl[S + c.R_ray], dX[SP_Hm] / X[SP_Hm] - dlnT, acc);
+      if (X[SP_e] != 0.0 && X[SP_H] != 0.0) {
+        const double dln = dX[SP_e] / X[SP_e] + dX[SP_H] / X[SP_H];
+        for (int i = 1; i < kHmTerms; ++i) acc = fma(sgl[S + c.R_ray + i], dln - (1.0 + (i + 1) / 2.0) * dlnT, acc);
+      }
     }
     acc = fma(sgl[S + R], dT, acc);
     // z_l = z_{l-1} + Delta_l, Delta_l = 0.5 (p_{l-1} - p_l) 1e6 (u_l + u_{l-1}) / g, u = R T / (mmw p 1e6)

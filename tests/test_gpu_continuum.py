@@ -2,7 +2,8 @@
 6 line species, 11001 points at 1 cm^-1 from 0.8 um, H, H- and e- in the chemistry)
 against the FP64 oracle, the double-float path against the FP64 path, and the emission
 gradient with the H- continuum against the oracle's differences. Transmission models with
-the H- continuum or a power-law / KH cloud have no gradient (BEAR_ERR_UNSUPPORTED)."""
+a power-law / KH cloud have no gradient (BEAR_ERR_UNSUPPORTED); with the H- continuum they
+do, checked against the oracle's differences."""
 
 import dataclasses
 
@@ -121,16 +122,40 @@ def test_hminus_gradient_against_oracle(case):
             assert err <= tol, (i, j, sa[j], sf[j], err, tol)
 
 
-def test_hminus_transmission_gradient_is_rejected():
-    """The transmission adjoint rejects models with the H- continuum."""
+def test_hminus_transmission_gradient_against_oracle():
+    """The transmission adjoint with the H- continuum (its seven coefficients are linear
+    opacity terms after the Rayleigh rows, so the level sinks already cover them; the
+    per-evaluation tangents map them), against the oracle's Richardson differences with
+    the tau > 10 cut-off disabled in both, at the golden points (one without H-)."""
     import torch
     c = [goldenlib.Case(p) for p in goldenlib.golden_cases() if p.endswith("transmission_hminus.npz")][0]
-    e = Engine(c.config_text(), c.observations())
+    text = c.config_text().replace("variable_gravity 1", "variable_gravity 0")
+    obs = c.observations()
+    e = Engine(text, obs)
+    om = oracle.OracleModel(text, obs)
+    e.set_tau_cutoff(float("inf"))
+    om.set_tau_cutoff(float("inf"))
     try:
-        with pytest.raises(_lib.EngineError) as ei:
-            e.grad_batch(torch.tensor(c.params[:1], device="cuda"))
-        assert ei.value.code == 4
+        phys = np.array(c.params, dtype=np.float64)
+        ll, g, ng = e.grad_batch(torch.tensor(phys, device="cuda"))
+        ll, g = ll.cpu().numpy(), g.cpu().numpy()
+        for i in range(len(phys)):
+            assert not ng[i]
+            x = phys[i]
+            assert abs(ll[i] - om.loglike(x)) <= 1e-8 + 1e-12 * abs(ll[i])
+            fd = np.zeros(len(x))
+            for j in range(len(x)):
+                if x[j] != 0.0:
+                    fd[j] = (4 * _fd(om.loglike, x, j, 5e-6) - _fd(om.loglike, x, j, 1e-5)) / 3
+            sa, sf = x * g[i], x * fd
+            scale = np.max(np.abs(sf))
+            for j in range(len(x)):
+                err = abs(sa[j] - sf[j])
+                tol = 1e-6 * abs(sf[j]) + 1e-8 * scale + 2e-10 * abs(ll[i]) / 1e-5
+                assert err <= tol, (i, j, sa[j], sf[j], err, tol)
     finally:
+        e.set_tau_cutoff(10.0)
+        om.close()
         e.close()
 
 
