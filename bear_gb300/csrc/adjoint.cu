@@ -1125,6 +1125,7 @@ void free_grad_workspace(Model& m) {
   cudaFree(g.tr_gc);
   cudaFree(g.tr_gz);
   cudaFree(g.tr_rp);
+  cudaFree(g.tr_cs);
   g = GradWorkspace{};
 }
 
@@ -1182,7 +1183,10 @@ static void launch_gradient_transmission(Model& m, const double* params_dev, int
   if (m.var_g) throw Error(BEAR_ERR_UNSUPPORTED, "the transmission gradient does not support variable gravity");
   if (m.annuli > 1) throw Error(BEAR_ERR_UNSUPPORTED, "the transmission gradient needs one impact parameter per level");
   const int S = m.acfg.S, R = m.acfg.R, L = m.L, P = m.acfg.nparam_total;
-  const int V = S + R + 3;
+  // level values: species, Rayleigh / H- terms, temperature, altitude, cloud extinction, then
+  // the sums along the non-grey cloud's shape parameters
+  const int NC = m.acfg.cloud_kind == 1 ? 1 : m.acfg.cloud_kind == 2 ? 3 : 0;
+  const int V = S + R + 3 + NC;
   if (V > 32) throw Error(BEAR_ERR_UNSUPPORTED, "the gradient supports at most 29 table and Rayleigh species");
   if (P > 128) throw Error(BEAR_ERR_UNSUPPORTED, "the gradient supports at most 128 parameters");
   if (L > 32767) throw Error(BEAR_ERR_UNSUPPORTED, "too many levels");
@@ -1222,8 +1226,8 @@ static void launch_gradient_transmission(Model& m, const double* params_dev, int
 void launch_gradient(Model& m, const double* params_dev, int batch, cudaStream_t st, double* loglike_dev,
                      double* grad_dev, uint8_t* neglect_dev) {
   if (m.hm && m.precision != 0) throw Error(BEAR_ERR_UNSUPPORTED, "H- continuum gradients run in precision mode 0");
-  if (m.acfg.cloud_kind && (m.transmission || m.precision != 0))
-    throw Error(BEAR_ERR_UNSUPPORTED, "power-law and KH cloud gradients: emission models, precision mode 0");
+  if (m.acfg.cloud_kind && m.precision != 0)
+    throw Error(BEAR_ERR_UNSUPPORTED, "power-law and KH cloud gradients run in precision mode 0");
   if (m.transmission) {
     launch_gradient_transmission(m, params_dev, batch, st, loglike_dev, grad_dev, neglect_dev);
     return;

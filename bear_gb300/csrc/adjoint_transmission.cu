@@ -118,7 +118,35 @@ struct TrArgs {
   int V;
   const float2* ts;  // stored opacity terms (nullptr: recompute them)
   const float2* dk;  // stored temperature-slope sums
+  const double* cs;  // non-grey cloud: per evaluation the wavelength factor and its NC shape derivatives
+  int nc;            // NC (0: grey cloud or none)
 };
+
+// The cloud values of level l at wavenumber k from g_x = d log L / d chi_l: value q0 = 0 (the
+// cloud extinction) is g_x times the wavelength factor of a non-grey cloud (g_x itself for
+// the grey one), values q0 = 1 .. NC the sums along the shape parameters,
+// g_x cloud_l df_k / dtheta (cloud_l the level's grey-part cloud extinction).
+__device__ __forceinline__ df2 tr_cloud_value(const TrArgs& a, int q0, int b, size_t N, int k, df2 gx,
+                                              double cloud_l) {
+  if (!a.cs) return q0 == 0 ? gx : df2{0.0f, 0.0f};
+  const double* row = a.cs + (size_t)b * (1 + a.nc) * N + (size_t)q0 * N + k;
+  if (q0 == 0) return df_mul(gx, df_from_double(__ldg(row)));
+  return df_from_double(df_to_double(gx) * cloud_l * __ldg(row));
+}
+
+// The wavelength factor of the evaluation's non-grey cloud and its derivatives along the
+// shape parameters at every wavenumber (the forward pass's cloud_shape, FP64).
+__global__ void tr_cloud_shape_kernel(DeviceModel dm, const EvalInfo* __restrict__ ev, double* __restrict__ cs,
+                                      int nc) {
+  const int b = blockIdx.x, k = blockIdx.y * blockDim.x + threadIdx.x;
+  if (k >= dm.N) return;
+  const size_t N = dm.N;
+  double* row = cs + (size_t)b * (1 + nc) * N;
+  row[k] = cloud_shape(dm, ev[b], k);
+  double d[3];
+  cloud_shape_tangent(dm, ev[b], k, d);
+  for (int c = 0; c < nc; ++c) row[(size_t)(1 + c) * N + k] = d[c];
+}
 
 // Block: 32 wavenumbers (lanes) x 4 groups; group w takes levels j = w, w+4, ...
 // From the forward pass's stores, with g_h = d log L / dh (the normalised seed times
@@ -268,7 +296,9 @@ __global__ void __launch_bounds__(128) tr_adjoint_pass2a(DeviceModel dm, TrArgs 
 // double [S][T] (T = kTrSinkThreads), then the level's Rayleigh number densities float2 [R].
 constexpr int kTrSinkThreads = 128;
 
-template <int VP, bool PAIRS>
+// CLOUD: a non-grey cloud (the cloud value weighted by the wavelength factor, and the
+// values along its shape parameters; tr_cloud_value).
+template <int VP, bool PAIRS, bool CLOUD = false>
 __global__ void __launch_bounds__(kTrSinkThreads, VP == 32 ? 4 : 6) tr_adjoint_pass2b(DeviceModel dm, TrArgs a) {
   constexpr int G = 32 / VP, NW = kTrSinkThreads / 32;
   __shared__ ExpTables et;
@@ -290,6 +320,7 @@ __global__ void __launch_bounds__(kTrSinkThreads, VP == 32 ? 4 : 6) tr_adjoint_p
   const float2* dwl = a.dwT + ((size_t)b * L + l) * S;
   const size_t row = ((size_t)b * L + l) * N;  // [b][l][k] of k = 0
   const float2* tsl = a.ts + ((size_t)b * L + l) * S * N;  // [s][N] (stored mode)
+  const double cloud_l = CLOUD ? __ldg(&a.lev[(size_t)b * L + l].cloud) : 0.0;
   df2 v[VP];
 #pragma unroll
   for (int q = 0; q < VP; ++q) v[q] = df2{0.0f, 0.0f};
@@ -333,8 +364,8 @@ __global__ void __launch_bounds__(kTrSinkThreads, VP == 32 ? 4 : 6) tr_adjoint_p
         x = gT;
       } else if (q == S + R + 1) {
         x = df2{gz.x, gz.y};
-      } else if (q == S + R + 2) {
-        x = gx;
+      } else if (CLOUD ? q >= S + R + 2 && q <= S + R + 2 + a.nc : q == S + R + 2) {
+        x = CLOUD ? tr_cloud_value(a, q - S - R - 2, b, N, k, gx, cloud_l) : gx;
       }
       v[q] = df_add(v[q], x);
     }
@@ -400,9 +431,9 @@ __global__ void __launch_bounds__(kTrSinkThreads, VP == 32 ? 4 : 6) tr_adjoint_p
         } else if (q == S + R + 1) {
           x0 = df2{gz.x, gz.y};
           x1 = df2{gz.z, gz.w};
-        } else if (q == S + R + 2) {
-          x0 = gx0;
-          x1 = gx1;
+        } else if (CLOUD ? q >= S + R + 2 && q <= S + R + 2 + a.nc : q == S + R + 2) {
+          x0 = CLOUD ? tr_cloud_value(a, q - S - R - 2, b, N, k0, gx0, cloud_l) : gx0;
+          x1 = CLOUD ? tr_cloud_value(a, q - S - R - 2, b, N, k0 + 1, gx1, cloud_l) : gx1;
         }
         v[q] = df_add(df_add(v[q], x0), x1);
       }
@@ -546,6 +577,12 @@ __global__ void __launch_bounds__(128) tr_atmosphere_adjoint_kernel(
       acc = fma(sgl[S + R + 2], d, acc);
     }
   }
+  // non-grey cloud shape parameters (after the optical depth): values S + R + 3 + c summed over levels
+  if (c.cloud && c.cloud_kind) {
+    const int cs = th - ci - 1;
+    if (cs >= 0 && cs < (c.cloud_kind == 1 ? 1 : 3))
+      for (int l = 0; l < L; ++l) acc += sg[(size_t)l * V + S + R + 3 + cs];
+  }
   if (th == 1) acc += s_rp;                                      // planet radius
   if (th == 2) acc += -2.0 / e.star_radius * seed[b * 3 + 2];    // stellar radius
   grad[(size_t)b * P + th] += acc;
@@ -556,8 +593,9 @@ size_t transmission_grad_bytes_per_eval(const Model& m, int V, bool store) {
   const size_t L = m.L, N = m.N;
   const size_t tiles = (N + 31) / 32;
   const size_t terms = store ? L * N * ((size_t)m.acfg.S + 1) * sizeof(float2) : 0;
+  const size_t cs = m.acfg.cloud_kind ? (m.acfg.cloud_kind == 1 ? 2 : 4) * N * sizeof(double) : 0;
   return L * N * (6 * sizeof(float2) + sizeof(short)) + 4 * L * L * sizeof(float2) + L * (size_t)V * 8 +
-         tiles * 8 + terms;
+         tiles * 8 + terms + cs;
 }
 
 void alloc_transmission_grad(Model& m, int chunk, int V, bool store) {
@@ -581,6 +619,10 @@ void alloc_transmission_grad(Model& m, int chunk, int V, bool store) {
   BGB_CUDA(cudaMalloc(&g.tr_gz, (n + 2) * sizeof(float2)));
   BGB_CUDA(cudaMalloc(&g.tr_rp, B * tiles * sizeof(double)));
   BGB_CUDA(cudaMalloc(&g.partial, B * L * (size_t)V * sizeof(double)));
+  if (m.acfg.cloud_kind) {
+    const size_t nc = m.acfg.cloud_kind == 1 ? 1 : 3;
+    BGB_CUDA(cudaMalloc(&g.tr_cs, B * (1 + nc) * N * sizeof(double)));
+  }
 }
 
 // ------------------------------------------------------------------ pass 2b, streamed
@@ -899,7 +941,11 @@ void transmission_adjoint_chunk(Model& m, const double* params_chunk, int nb, cu
   const int tiles = (int)((N + 31) / 32);
   TrArgs a{w.lev, w.lsdf, w.ray_n, w.ev, reinterpret_cast<const float2*>(w.geom), tp.tr_geo, tp.dwT, g.gS,
            g.seed, tp.tr_c, tp.tr_T, tp.tr_qs, tp.tr_us, tp.tr_I, g.tr_gc, g.tr_gz, g.tr_rp, g.partial, V,
-           tp.tr_ts, tp.tr_dk};
+           tp.tr_ts, tp.tr_dk, g.tr_cs, m.acfg.cloud_kind == 1 ? 1 : m.acfg.cloud_kind == 2 ? 3 : 0};
+  if (g.tr_cs) {
+    tr_cloud_shape_kernel<<<dim3(nb, (unsigned)((N + 255) / 256)), 256, 0, st>>>(dm, w.ev, g.tr_cs, a.nc);
+    BGB_CUDA(cudaGetLastError());
+  }
   const size_t sm2a = (size_t)L * 32 * (sizeof(float2) + 2 * sizeof(short)) + (size_t)3 * L * sizeof(float2);
   if (sm2a > 48 * 1024)
     BGB_CUDA(cudaFuncSetAttribute(tr_adjoint_pass2a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2a));
@@ -919,7 +965,7 @@ void transmission_adjoint_chunk(Model& m, const double* params_chunk, int nb, cu
   const size_t stage_bytes = (size_t)nseg * (kStreamTile + 2) * sizeof(float2);
   const int stages = 3 * stage_bytes <= 110 * 1024 ? 3 : 2;
   const size_t sms = stages * stage_bytes;
-  if (tp.tr_ts && m.acfg.R <= 32 && nseg <= kStreamMaxSeg && sms <= 200 * 1024) {
+  if (!g.tr_cs && tp.tr_ts && m.acfg.R <= 32 && nseg <= kStreamMaxSeg && sms <= 200 * 1024) {
     auto gos = [&](auto kernel) {
       BGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sms));
       kernel<<<dim3(nb, L), kTrSinkThreads + 32, sms, st>>>(dm, a, nseg);
@@ -933,6 +979,10 @@ void transmission_adjoint_chunk(Model& m, const double* params_chunk, int nb, cu
       else if (VP == 16) pairs ? gos(tr_adjoint_pass2b_stream<16, 2, true>) : gos(tr_adjoint_pass2b_stream<16, 2, false>);
       else pairs ? gos(tr_adjoint_pass2b_stream<32, 2, true>) : gos(tr_adjoint_pass2b_stream<32, 2, false>);
     }
+  } else if (g.tr_cs) {  // non-grey cloud
+    if (VP == 8) pairs ? go2(tr_adjoint_pass2b<8, true, true>) : go2(tr_adjoint_pass2b<8, false, true>);
+    else if (VP == 16) pairs ? go2(tr_adjoint_pass2b<16, true, true>) : go2(tr_adjoint_pass2b<16, false, true>);
+    else pairs ? go2(tr_adjoint_pass2b<32, true, true>) : go2(tr_adjoint_pass2b<32, false, true>);
   } else if (VP == 8) pairs ? go2(tr_adjoint_pass2b<8, true>) : go2(tr_adjoint_pass2b<8, false>);
   else if (VP == 16) pairs ? go2(tr_adjoint_pass2b<16, true>) : go2(tr_adjoint_pass2b<16, false>);
   else pairs ? go2(tr_adjoint_pass2b<32, true>) : go2(tr_adjoint_pass2b<32, false>);

@@ -254,6 +254,7 @@ struct GradWorkspace {
   float2* tr_gc = nullptr;    // d log L / d (chi_j + chi_{j+1})
   float2* tr_gz = nullptr;    // d log L / d z_j
   double* tr_rp = nullptr;    // per (evaluation, tile) partial d log L / d R_p
+  double* tr_cs = nullptr;    // non-grey cloud: B x (1 + NC) x N wavelength factor and its shape derivatives
   bool tr_store = false;      // the forward pass stores the opacity terms (taps.tr_ts, tr_dk)
 };
 

@@ -1,9 +1,8 @@
 """H- continuum (bound-free + free-free) in the batched emission workload (80 levels,
 6 line species, 11001 points at 1 cm^-1 from 0.8 um, H, H- and e- in the chemistry)
 against the FP64 oracle, the double-float path against the FP64 path, and the emission
-gradient with the H- continuum against the oracle's differences. Transmission models with
-a power-law / KH cloud have no gradient (BEAR_ERR_UNSUPPORTED); with the H- continuum they
-do, checked against the oracle's differences."""
+gradient with the H- continuum against the oracle's differences, and the transmission
+gradient with the H- continuum and with the KH cloud likewise."""
 
 import dataclasses
 
@@ -159,15 +158,45 @@ def test_hminus_transmission_gradient_against_oracle():
         e.close()
 
 
-def test_transmission_non_grey_cloud_gradient_is_rejected():
-    """The non-grey clouds have an adjoint for emission models (test_gpu_gradient_cloud.py);
-    the transmission adjoint rejects them."""
+def test_transmission_kh_cloud_gradient_against_oracle():
+    """The transmission adjoint with the KH cloud: the level's cloud sink weighted by the
+    wavelength factor, and the sums along q0, a0 and the particle size (the factor's
+    derivatives per wavenumber, tr_cloud_shape_kernel), against the oracle's Richardson
+    differences with the tau > 10 cut-off disabled; the cloud-top pressure places whole
+    layers (zero gradient). The golden set's first point is left out: there the cloud bottom
+    (one scale height below the top) moves by a level within the difference step in T, and
+    the differences of the grey cloud at that point miss the adjoint by the same 2 %."""
     import torch
     c = [goldenlib.Case(p) for p in goldenlib.golden_cases() if p.endswith("transmission_kh_cloud.npz")][0]
-    e = Engine(c.config_text(), c.observations())
+    text = c.config_text().replace("variable_gravity 1", "variable_gravity 0")
+    obs = c.observations()
+    e = Engine(text, obs)
+    om = oracle.OracleModel(text, obs)
+    e.set_tau_cutoff(float("inf"))
+    om.set_tau_cutoff(float("inf"))
     try:
-        with pytest.raises(_lib.EngineError) as ei:
-            e.grad_batch(torch.tensor(c.params[:1], device="cuda"))
-        assert ei.value.code == 4
+        phys = np.array(c.params[1:], dtype=np.float64)
+        top = phys.shape[1] - 1  # cloud-top pressure (the bottom follows the scale height)
+        ll, g, ng = e.grad_batch(torch.tensor(phys, device="cuda"))
+        ll, g = ll.cpu().numpy(), g.cpu().numpy()
+        for i in range(len(phys)):
+            assert not ng[i]
+            x = phys[i]
+            assert abs(ll[i] - om.loglike(x)) <= 1e-8 + 1e-12 * abs(ll[i])
+            assert g[i][top] == 0.0
+            fd = np.zeros(len(x))
+            for j in range(len(x)):
+                if x[j] != 0.0 and j != top:
+                    fd[j] = (4 * _fd(om.loglike, x, j, 5e-6) - _fd(om.loglike, x, j, 1e-5)) / 3
+            sa, sf = x * g[i], x * fd
+            scale = np.max(np.abs(sf))
+            for j in range(len(x)):
+                if j == top:
+                    continue
+                err = abs(sa[j] - sf[j])
+                tol = 1e-6 * abs(sf[j]) + 1e-8 * scale + 2e-10 * abs(ll[i]) / 1e-5
+                assert err <= tol, (i, j, sa[j], sf[j], err, tol)
     finally:
+        e.set_tau_cutoff(10.0)
+        om.close()
         e.close()
