@@ -498,7 +498,7 @@ int bear_model_autotune(bear_model* h, const double* params_dev, int batch, int 
     // emission: threads (wavenumbers) per block; transmission: wavenumbers per block
     const std::vector<int> cand = !m.transmission ? std::vector<int>{64, 128, 256}
                                   : m.annuli > 1  ? std::vector<int>{32, 16, 64}
-                                                  : std::vector<int>{160, 192, 32, 64};
+                                                  : std::vector<int>{160, 176, 208, 192, 224, 32, 64};
     const int saved_rt = m.rt_threads;
     const bool saved_prof = m.profiling;
     m.rt_threads = 0;

@@ -1465,6 +1465,9 @@ void upload_model(Model& m) {
     BGB_CUDA(cudaFuncSetAttribute(transmission_kernel<true, 64, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_kernel_x2<16, 8, 8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_kernel_x2<32, 8, 3, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel_x2<16, 8, 8, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel_x2<16, 8, 7, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_kernel_x2<16, 4, 16, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_kernel_x2<16, 8, 8, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_kernel_x2<16, 8, 6, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_annuli_kernel<true, 32, 4, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
@@ -1590,13 +1593,16 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
     const dim3 ggrid(batch, (L * L + 255) / 256);
     if (m.precision == 1) transmission_geometry_kernel<false><<<ggrid, 256, 0, st>>>(dm, w.lev, w.ev, w.geom, w.rays);
     else transmission_geometry_kernel<true><<<ggrid, 256, 0, st>>>(dm, w.lev, w.ev, w.geom, w.rays);
-    // the launch shape: 16, 32 or 64 wavenumbers per block with 4 threads each; 160 (the
-    // double-float default) or 192: 32 or 64 wavenumbers per block in pairs, 8 threads per pair.
-    // The FP64 path and the gradient's storing pass take 32 for 160 and 192.
+    // the launch shape: 16, 32 or 64 wavenumbers per block with 4 threads each; paired
+    // wavenumbers: 160 (the double-float default; 32 wavenumbers per block, 8 threads per pair,
+    // table reads of two species issued together), 176 (one species per group), 208 (four),
+    // 224 (4 threads per pair: twice the levels per thread), 192 (64 wavenumbers per block).
+    // The FP64 path takes 32 for the paired shapes.
     const int vpb = (rt == 16 || rt == 64) ? rt : 32;
     dim3 grid(batch, (dm.N + vpb - 1) / vpb);
     const bool df = m.precision != 1;
     const int pairs = (rt == 16 || rt == 32 || rt == 64) ? 0 : (rt == 192 ? 32 : 16);
+    const int tpn_x = rt == 224 ? 4 : 8;  // threads per pair (levels per thread: L / tpn_x)
     // extinction column and Rayleigh densities, at least the height-group sums that reuse them
     const size_t sm = std::max((size_t)L * vpb * sizeof(double) + (df ? (size_t)L * dm.R * sizeof(float2) : 0),
                                (size_t)kHeightGroups * vpb * sizeof(double));
@@ -1652,6 +1658,9 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
         kernel<<<gx, tpn * pairs, smx, st>>>(dm, w.lev, w.lsdf, w.ray_n, w.ev, w.geom, w.rays, w.spectrum, none);
       };
       if (pairs == 32) gox(transmission_kernel_x2<32, 8, 3, 2>, 8);
+      else if (rt == 176) gox(transmission_kernel_x2<16, 8, 8, 1>, 8);   // one species per table-read group
+      else if (rt == 208) gox(transmission_kernel_x2<16, 8, 7, 4>, 8);   // four species per group
+      else if (rt == 224) gox(transmission_kernel_x2<16, 4, 16, 2>, tpn_x);  // 4 threads per pair
       else gox(transmission_kernel_x2<16, 8, 8, 2>, 8);
     } else if (vpb == 16) df ? go(transmission_kernel<true, 16>) : go(transmission_kernel<false, 16>);
     else if (vpb == 64) df ? go(transmission_kernel<true, 64>) : go(transmission_kernel<false, 64>);

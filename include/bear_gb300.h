@@ -218,7 +218,8 @@ int bear_model_set_gradient_memory(bear_model* m, long long bytes);
 /* --------------------------------------------------------------- autotuner and captured batches
  * No reference counterpart. bear_model_autotune times the radiative-transfer
  * kernel's launch shapes (emission: 64 / 128 / 256 threads per block;
- * transmission: 160, 192, 32, 64, see bear_model_set_launch) on this batch with CUDA events,
+ * transmission: 160, 176, 208, 192, 224, 32, 64, see bear_model_set_launch: wavenumbers
+ * per block, levels per thread and species per table-read group) on this batch with CUDA events,
  * keeps the fastest for later batched calls (an explicit bear_model_set_launch
  * takes precedence) and reports it. Synchronous; results do not depend on the
  * choice (each wavenumber is computed by the same code). */
@@ -253,9 +254,12 @@ int bear_model_set_precision(bear_model* m, int mode);
 
 /* Launch shape of the radiative-transfer kernel (emission: threads =
  * wavenumbers per block, 64 / 128 / 256; transmission: 16 / 32 / 64 wavenumbers
- * per block with four threads each, or 160 / 192 for 32 / 64 wavenumbers per block
- * in pairs, eight threads per pair, any other value the default 160; the FP64
- * path runs 32 in place of 160 and 192; 0 = default or the autotuned shape) and
+ * per block with four threads each, or two wavenumbers per thread group: 160 (32
+ * wavenumbers per block, eight threads per pair, two species per table-read group),
+ * 176 (one species per group), 208 (four), 224 (four threads per pair: twice the
+ * levels per thread), 192 (64 wavenumbers per block); any other value the default
+ * 160; the FP64 path runs 32 in place of the paired shapes; 0 = default or the
+ * autotuned shape) and
  * threads per block of the observation + likelihood kernel (0 = 256). An explicit
  * setting overrides bear_model_autotune. Every shape gives the same bits. */
 int bear_model_set_launch(bear_model* m, int rt_threads, int obs_threads);

@@ -49,7 +49,7 @@ def test_graph_replay_equals_batched_path(name, kind):
         P0 = _live(spec, kind, 48, 1)
         ref0, ng0 = e.loglike_batch(P0)
         ev = BatchEvaluator(e, P0, autotune=True)
-        assert ev.rt_threads in ((16, 32, 64, 160, 192) if kind == "transmission" else (64, 128, 256))
+        assert ev.rt_threads in ((16, 32, 64, 160, 176, 192, 208, 224) if kind == "transmission" else (64, 128, 256))
         ll, ng = ev()
         torch.cuda.synchronize()
         assert torch.equal(ll, ref0) and torch.equal(ng, ng0)
@@ -89,7 +89,7 @@ def test_transmission_launch_shapes_are_bit_identical():
         P = _live(spec, "transmission", 24, 5)
         p3 = P[3].cpu().numpy()
         ref = None
-        for rt in (32, 16, 64, 160, 192, 0):
+        for rt in (32, 16, 64, 160, 176, 192, 208, 224, 0):
             e.set_launch(rt, 0)
             ll, ng = e.loglike_batch(P)
             sp, binned, _ = e.compute_model(p3)
