@@ -168,8 +168,10 @@ __global__ void __launch_bounds__(128) tr_adjoint_pass2a(DeviceModel dm, TrArgs 
   float2* ff_s = fw_s + L;                                             // [L]: (R + z_t) wz_t
   short* I_s = reinterpret_cast<short*>(ff_s + L);                     // [L][32]
   short* m_s = I_s + (size_t)L * 32;                                   // [L][32]
-  const int b = blockIdx.x, lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
-  const int kk = blockIdx.y * 32 + lane;
+  // grid (tiles, evaluations): the blocks an SM runs together mostly share one evaluation, so
+  // its path-length rows stay in L1
+  const int b = blockIdx.y, lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
+  const int kk = blockIdx.x * 32 + lane;
   const bool active = kk < dm.N;
   const int k = active ? kk : dm.N - 1;
   const size_t N = dm.N;
@@ -280,7 +282,7 @@ __global__ void __launch_bounds__(128) tr_adjoint_pass2a(DeviceModel dm, TrArgs 
   if (threadIdx.x == 0) {
     double s = 0.0;
     for (int q = 0; q < 128; ++q) s += df_to_double(sm(rp_part, q));
-    a.rp[(size_t)b * gridDim.y + blockIdx.y] = s;
+    a.rp[(size_t)b * gridDim.x + blockIdx.x] = s;
   }
 }
 
@@ -949,7 +951,7 @@ void transmission_adjoint_chunk(Model& m, const double* params_chunk, int nb, cu
   const size_t sm2a = (size_t)L * 32 * (sizeof(float2) + 2 * sizeof(short)) + (size_t)3 * L * sizeof(float2);
   if (sm2a > 48 * 1024)
     BGB_CUDA(cudaFuncSetAttribute(tr_adjoint_pass2a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2a));
-  tr_adjoint_pass2a<<<dim3(nb, tiles), 128, sm2a, st>>>(dm, a);
+  tr_adjoint_pass2a<<<dim3(tiles, nb), 128, sm2a, st>>>(dm, a);
   BGB_CUDA(cudaGetLastError());
   const size_t sm2 = (size_t)S * kTrSinkThreads * (sizeof(float2) + sizeof(double)) + (size_t)m.acfg.R * sizeof(float2);
   const int VP = V <= 8 ? 8 : V <= 16 ? 16 : 32;
