@@ -152,7 +152,9 @@ __global__ void tr_cloud_shape_kernel(DeviceModel dm, const EvalInfo* __restrict
 // From the forward pass's stores, with g_h = d log L / dh (the normalised seed times
 // 1e6 / R_s^2) and F_t = (R + z_t) wz_t:
 //   g_tau_t = g_h F_t T_t                 staged with the cut-off indices in shared
-//                                          memory (float2 [L][32] then short [L][32])
+//                                          memory (float2 [L][32] then short [L][32]; 24
+//                                          warps per SM at 100 levels: 14.8 -> ~12.5 ms at
+//                                          B = 64 once m(j) no longer took a third array)
 //   g_c_j   = sum_{t <= j <= I_t} g_tau_t G[t][j]                      (j <= L-2)
 //   g_z_j   = sum_{t < j} g_tau_t P[t][j] (c_{j-1} [j-1 <= I_t] - c_j [j <= I_t])
 //           + g_h (1 - T_j) wz_j + g_tau_j qs_j + g_h (A_{j-1} - A_{j+1}) (- A_0 at j = 0),
@@ -167,7 +169,6 @@ __global__ void __launch_bounds__(128) tr_adjoint_pass2a(DeviceModel dm, TrArgs 
   float2* fw_s = fz_s + L;                                             // [L]: wz_t
   float2* ff_s = fw_s + L;                                             // [L]: (R + z_t) wz_t
   short* I_s = reinterpret_cast<short*>(ff_s + L);                     // [L][32]
-  short* m_s = I_s + (size_t)L * 32;                                   // [L][32]
   // grid (tiles, evaluations): the blocks an SM runs together mostly share one evaluation, so
   // its path-length rows stay in L1
   const int b = blockIdx.y, lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
@@ -217,18 +218,13 @@ __global__ void __launch_bounds__(128) tr_adjoint_pass2a(DeviceModel dm, TrArgs 
   }
   if (grp == 0) rp = df_add(rp, df_mul(gh, df_from_double(2.0 * Rp)));  // depth = (h + R^2) / R_s^2
   __syncthreads();
-  // m(j): the lowest tangent level whose ray reaches level j. Ray t covers levels
-  // t..I_t + 1 (I_t >= t), so in ascending t the covered levels form a growing prefix.
-  if (grp == 0) {
-    int cov = -1;
-    for (int t = 0; t < L - 1; ++t) {
-      const int hi = min((int)I_s[t * 32 + lane] + 1, L - 1);
-      for (int j = cov + 1; j <= hi; ++j) m_s[j * 32 + lane] = (short)t;
-      cov = max(cov, hi);
-    }
-  }
   __syncthreads();
   if (active) {
+    // m(j): the lowest tangent level whose ray reaches level j. Ray t covers levels
+    // t..I_t + 1 (I_t >= t), so in ascending t the covered levels form a growing prefix
+    // (reaching L - 1 at t = L - 2 at the latest); m(j) is the t whose ray first extends it
+    // to j, found while the thread's levels j ascend
+    int tp = 0, cov = -1, mcur = 0;
     // per level j the rays' path lengths G[t][j] and P[t][j], contiguous in t
     const float2* PT = a.geo + (size_t)b * 4 * L * L;
     const float2* GT = PT + (size_t)3 * L * L;
@@ -240,9 +236,13 @@ __global__ void __launch_bounds__(128) tr_adjoint_pass2a(DeviceModel dm, TrArgs 
       // g_z part: sum over rays through j of g_tau P (x dcc), over rays ending at j - 1 (x c_{j-1})
       df2 gc = z, pin = z, pend = z;
       const int tmax = min(j, L - 2);
+      while (cov < j && tp <= L - 2) {
+        cov = max(cov, min((int)I_s[tp * 32 + lane] + 1, L - 1));
+        mcur = tp++;
+      }
       // from the lowest m(j) of the warp's wavenumbers, so the path-length loads stay uniform
       const unsigned mask = __activemask();
-      const int t0 = (int)__reduce_min_sync(mask, (unsigned)m_s[j * 32 + lane]);
+      const int t0 = (int)__reduce_min_sync(mask, (unsigned)mcur);
       auto ray = [&](int t, int I, float2 g, float2 p, float2 gt) {
         if (I < j - 1) return;  // the ray of tangent level t stops below level j
         const df2 gtau = {gt.x, gt.y};
@@ -948,7 +948,7 @@ void transmission_adjoint_chunk(Model& m, const double* params_chunk, int nb, cu
     tr_cloud_shape_kernel<<<dim3(nb, (unsigned)((N + 255) / 256)), 256, 0, st>>>(dm, w.ev, g.tr_cs, a.nc);
     BGB_CUDA(cudaGetLastError());
   }
-  const size_t sm2a = (size_t)L * 32 * (sizeof(float2) + 2 * sizeof(short)) + (size_t)3 * L * sizeof(float2);
+  const size_t sm2a = (size_t)L * 32 * (sizeof(float2) + sizeof(short)) + (size_t)3 * L * sizeof(float2);
   if (sm2a > 48 * 1024)
     BGB_CUDA(cudaFuncSetAttribute(tr_adjoint_pass2a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2a));
   tr_adjoint_pass2a<<<dim3(tiles, nb), 128, sm2a, st>>>(dm, a);
