@@ -480,8 +480,14 @@ __global__ void __launch_bounds__(128) tr_atmosphere_adjoint_kernel(
     if (lane == 0) s_rp = s * inv;
   }
   __syncthreads();
-  if (tid >= P) return;
-  const int th = tid;
+  // thread (th, ch): parameter th over the levels of chunk ch; the altitude tangent, a prefix
+  // sum over levels, starts each chunk from the chunks below it (two passes), and the chunk
+  // sums are added in chunk order
+  __shared__ double part[128];
+  const int nch = max(1, (int)blockDim.x / P);
+  const int th = tid % P, ch = tid / P;
+  const bool work = ch < nch;
+  const int l0 = ch * L / nch, l1 = (ch + 1) * L / nch;
   const double* par = params + (size_t)b * P;
   const double* gen = par;
   const int ng = c.nparam_general, nc = c.nparam_chem, nt = c.nparam_temp;
@@ -535,11 +541,45 @@ __global__ void __launch_bounds__(128) tr_atmosphere_adjoint_kernel(
     dlnX[s] = v;
     np[s] = zero ? -1 : n;
   }
-  double acc = 0.0, u_prev = 0.0, du_prev = 0.0, dz_prev = 0.0, dz = 0.0;
-  for (int l = 0; l < L; ++l) {
+  auto dT_at = [&](int l) -> double {
+    if (!temp_theta) return 0.0;
+    return c.temp_poly ? poly_value(c, ddof, dm.log10p[l]) : (tm == 0 ? 1.0 : 0.0);
+  };
+  // u = R T / (mmw p 1e6) and its tangent at level l
+  auto u_at = [&](int l, double& du) {
+    const double T = lev[(size_t)b * L + l].T;
+    const double u = kGasConst * T / (mmw * dm.pressure[l] * 1e6);
+    du = u * (dT_at(l) / T - dmmw / mmw);
+    return u;
+  };
+  // Delta_l tangent (layer l - 1 -> l): 0.5 (p_{l-1} - p_l) 1e6 ((du_l + du_{l-1}) - (u_l + u_{l-1}) d ln g) / g
+  auto ddelta = [&](int l, double u, double du, double u_prev, double du_prev) {
+    const double pf = 0.5 * (dm.pressure[l - 1] * 1e6 - dm.pressure[l] * 1e6) / g;
+    return pf * ((du + du_prev) - (u + u_prev) * dlng);
+  };
+  // pass 1: the chunk's altitude-tangent increment
+  double u_prev = 0.0, du_prev = 0.0;
+  if (work) {
+    double inc = 0.0;
+    if (l0 >= 1) u_prev = u_at(l0 - 1, du_prev);
+    double up = u_prev, dup = du_prev;
+    for (int l = l0; l < l1; ++l) {
+      double du;
+      const double u = u_at(l, du);
+      if (l >= 1) inc += ddelta(l, u, du, up, dup);
+      up = u;
+      dup = du;
+    }
+    part[tid] = inc;
+  }
+  __syncthreads();
+  double dz = 0.0, dz_prev = 0.0, acc = 0.0;
+  if (work)
+    for (int q = 0; q < ch; ++q) dz += part[q * P + th];
+  __syncthreads();
+  for (int l = l0; work && l < l1; ++l) {
     const LevelInfo li = lev[(size_t)b * L + l];
-    double dT = 0.0;
-    if (temp_theta) dT = c.temp_poly ? poly_value(c, ddof, dm.log10p[l]) : (tm == 0 ? 1.0 : 0.0);
+    const double dT = dT_at(l);
     const double dlnT = dT / li.T;
     const double* sgl = sg + (size_t)l * V;
     for (int s = 0; s < S; ++s)
@@ -560,13 +600,10 @@ __global__ void __launch_bounds__(128) tr_atmosphere_adjoint_kernel(
     }
     acc = fma(sgl[S + R], dT, acc);
     // z_l = z_{l-1} + Delta_l, Delta_l = 0.5 (p_{l-1} - p_l) 1e6 (u_l + u_{l-1}) / g, u = R T / (mmw p 1e6)
-    const double u = kGasConst * li.T / (mmw * dm.pressure[l] * 1e6);
-    const double du = u * (dlnT - dmmw / mmw);
+    double du;
+    const double u = u_at(l, du);
     dz_prev = dz;
-    if (l >= 1) {
-      const double pf = 0.5 * (dm.pressure[l - 1] * 1e6 - dm.pressure[l] * 1e6) / g;
-      dz += pf * ((du + du_prev) - (u + u_prev) * dlng);
-    }
+    if (l >= 1) dz += ddelta(l, u, du, u_prev, du_prev);
     u_prev = u;
     du_prev = du;
     acc = fma(sgl[S + R + 1], dz, acc);
@@ -580,14 +617,22 @@ __global__ void __launch_bounds__(128) tr_atmosphere_adjoint_kernel(
     }
   }
   // non-grey cloud shape parameters (after the optical depth): values S + R + 3 + c summed over levels
-  if (c.cloud && c.cloud_kind) {
+  if (work && c.cloud && c.cloud_kind) {
     const int cs = th - ci - 1;
     if (cs >= 0 && cs < (c.cloud_kind == 1 ? 1 : 3))
-      for (int l = 0; l < L; ++l) acc += sg[(size_t)l * V + S + R + 3 + cs];
+      for (int l = l0; l < l1; ++l) acc += sg[(size_t)l * V + S + R + 3 + cs];
   }
-  if (th == 1) acc += s_rp;                                      // planet radius
-  if (th == 2) acc += -2.0 / e.star_radius * seed[b * 3 + 2];    // stellar radius
-  grad[(size_t)b * P + th] += acc;
+  if (work && ch == 0) {
+    if (th == 1) acc += s_rp;                                      // planet radius
+    if (th == 2) acc += -2.0 / e.star_radius * seed[b * 3 + 2];    // stellar radius
+  }
+  part[tid] = acc;
+  __syncthreads();
+  if (tid < P) {
+    double tot = 0.0;
+    for (int q = 0; q < nch; ++q) tot += part[q * P + tid];
+    grad[(size_t)b * P + tid] += tot;
+  }
 }
 
 // ------------------------------------------------------------------ host side
