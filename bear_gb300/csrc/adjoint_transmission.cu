@@ -41,6 +41,7 @@
 
 #include "adjoint_common.cuh"
 #include "bulk_copy.cuh"
+#include "dfloat2x.cuh"
 
 namespace bgb {
 
@@ -160,23 +161,31 @@ __global__ void tr_cloud_shape_kernel(DeviceModel dm, const EvalInfo* __restrict
 //           + g_h (1 - T_j) wz_j + g_tau_j qs_j + g_h (A_{j-1} - A_{j+1}) (- A_0 at j = 0),
 //             A_t = (R + z_t)(1 - T_t)   (wz_t = z_{t+1} - z_{t-1}; z_1 - z_0 at t = 0)
 //   dlogL/dR += g_h (1 - T_j) wz_j + g_tau_j us_j (+ 2 R g_h once: depth = (h + R^2) / R_s^2)
-__global__ void __launch_bounds__(128) tr_adjoint_pass2a(DeviceModel dm, TrArgs a) {
+// Two wavenumbers per lane (k and k + 32 of a 64-wavenumber tile) with paired FP32
+// double-float instructions (dfloat2x.cuh), eight groups of levels: every per-element step is
+// the one-wavenumber step, and a ray that does not reach level j (or a sum it does not enter)
+// contributes a zeroed g_tau, which leaves a double-float sum unchanged, so each wavenumber's
+// g_c and g_z equal the one-wavenumber results.
+constexpr int kPass2aGroups = 8;
+
+__global__ void __launch_bounds__(32 * kPass2aGroups, 3) tr_adjoint_pass2a(DeviceModel dm, TrArgs a) {
+  constexpr int NG = kPass2aGroups;
   extern __shared__ __align__(16) unsigned char tr2a_smem[];
-  __shared__ float2 rp_part[128];
+  __shared__ float2 rp_part[32 * NG];
   const int L = dm.L;
-  float2* gt_s = reinterpret_cast<float2*>(tr2a_smem);               // [L][32]
-  float2* fz_s = gt_s + (size_t)L * 32;                                // [L]: R + z_t
+  float4* gt_s = reinterpret_cast<float4*>(tr2a_smem);                // [L][32] paired g_tau
+  float2* fz_s = reinterpret_cast<float2*>(gt_s + (size_t)L * 32);     // [L]: R + z_t
   float2* fw_s = fz_s + L;                                             // [L]: wz_t
   float2* ff_s = fw_s + L;                                             // [L]: (R + z_t) wz_t
-  short* I_s = reinterpret_cast<short*>(ff_s + L);                     // [L][32]
+  short2* I_s = reinterpret_cast<short2*>(ff_s + L);                   // [L][32] paired cut-off indices
   // grid (tiles, evaluations): the blocks an SM runs together mostly share one evaluation, so
   // its path-length rows stay in L1
   const int b = blockIdx.y, lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
-  const int kk = blockIdx.x * 32 + lane;
-  const bool active = kk < dm.N;
-  const int k = active ? kk : dm.N - 1;
+  const int kk0 = blockIdx.x * 64 + lane, kk1 = kk0 + 32;
+  const bool act0 = kk0 < dm.N, act1 = kk1 < dm.N;
+  const int k0 = act0 ? kk0 : dm.N - 1, k1 = act1 ? kk1 : dm.N - 1;
   const size_t N = dm.N;
-  const size_t col = (size_t)b * L * N + k;
+  const size_t col0 = (size_t)b * L * N + k0, col1 = (size_t)b * L * N + k1;
   const LevelInfo* lv = a.lev + (size_t)b * L;
   const double Rp = a.ev[b].radius, Rs = a.ev[b].star_radius;
   // per-level geometry factors of the effective height (FP64 once per block)
@@ -189,68 +198,79 @@ __global__ void __launch_bounds__(128) tr_adjoint_pass2a(DeviceModel dm, TrArgs 
     ff_s[t] = make_float2(f.hi, f.lo);
   }
   __syncthreads();
-  const df2 gh = df_from_double(active ? tr_seed(dm, a.gS, a.seed, b, k) * 1e6 / (Rs * Rs) : 0.0);
-  const df2 one = df_make(1.0f);
+  const dfx gh = dfx_make(df_from_double(act0 ? tr_seed(dm, a.gS, a.seed, b, k0) * 1e6 / (Rs * Rs) : 0.0),
+                          df_from_double(act1 ? tr_seed(dm, a.gS, a.seed, b, k1) * 1e6 / (Rs * Rs) : 0.0));
+  const dfx zx = {f2(0.0f), f2(0.0f)};
+  const dfx one = dfx_bcast(df_make(1.0f));
+  // both elements of a per-(level, wavenumber) array at level t
   auto ld = [&](const float2* arr, int t) {
-    const float2 v = arr[col + (size_t)t * N];
-    return df2{v.x, v.y};
+    const float2 v0 = arr[col0 + (size_t)t * N], v1 = arr[col1 + (size_t)t * N];
+    return dfx{make_float2(v0.x, v1.x), make_float2(v0.y, v1.y)};
+  };
+  auto st = [&](float2* arr, int t, const dfx& v) {
+    if (act0) arr[col0 + (size_t)t * N] = make_float2(v.hi.x, v.lo.x);
+    if (act1) arr[col1 + (size_t)t * N] = make_float2(v.hi.y, v.lo.y);
   };
   auto sm = [](const float2* arr, int i) {
     const float2 v = arr[i];
-    return df2{v.x, v.y};
+    return dfx_bcast(df2{v.x, v.y});
   };
   // per tangent level: g_tau_t = g_h F_t T_t (staged), A_t = (R + z_t)(1 - T_t) and the direct
   // sink z1_t = g_h (1 - T_t) wz_t + g_tau_t qs_t, written over the ray sums they replace
-  df2 rp = {0.0f, 0.0f};
-  for (int t = grp; t < L - 1; t += 4) {
-    const df2 T = ld(a.T, t), omT = df_sub(one, T);
-    const df2 gt = df_mul(df_mul(gh, sm(ff_s, t)), T);
-    const df2 base = df_mul(df_mul(gh, omT), sm(fw_s, t));
-    const df2 z1 = df_add(base, df_mul(gt, ld(a.qs, t)));
-    rp = df_add(rp, df_add(base, df_mul(gt, ld(a.us, t))));
-    const df2 A = df_mul(sm(fz_s, t), omT);
-    gt_s[t * 32 + lane] = make_float2(gt.hi, gt.lo);
-    I_s[t * 32 + lane] = a.I[col + (size_t)t * N];
-    if (active) {
-      a.qs[col + (size_t)t * N] = make_float2(z1.hi, z1.lo);
-      a.us[col + (size_t)t * N] = make_float2(A.hi, A.lo);
-    }
+  dfx rp = zx;
+  for (int t = grp; t < L - 1; t += NG) {
+    const dfx T = ld(a.T, t), omT = dfx_sub(one, T);
+    const dfx gt = dfx_mul(dfx_mul(gh, sm(ff_s, t)), T);
+    const dfx base = dfx_mul(dfx_mul(gh, omT), sm(fw_s, t));
+    const dfx z1 = dfx_add(base, dfx_mul(gt, ld(a.qs, t)));
+    rp = dfx_add(rp, dfx_add(base, dfx_mul(gt, ld(a.us, t))));
+    const dfx A = dfx_mul(sm(fz_s, t), omT);
+    gt_s[t * 32 + lane] = make_float4(gt.hi.x, gt.hi.y, gt.lo.x, gt.lo.y);
+    I_s[t * 32 + lane] = make_short2(a.I[col0 + (size_t)t * N], a.I[col1 + (size_t)t * N]);
+    st(a.qs, t, z1);
+    st(a.us, t, A);
   }
-  if (grp == 0) rp = df_add(rp, df_mul(gh, df_from_double(2.0 * Rp)));  // depth = (h + R^2) / R_s^2
+  if (grp == 0) rp = dfx_add(rp, dfx_mul(gh, dfx_bcast(df_from_double(2.0 * Rp))));  // depth = (h + R^2) / R_s^2
   __syncthreads();
-  __syncthreads();
-  if (active) {
+  if (act0) {
     // m(j): the lowest tangent level whose ray reaches level j. Ray t covers levels
     // t..I_t + 1 (I_t >= t), so in ascending t the covered levels form a growing prefix
     // (reaching L - 1 at t = L - 2 at the latest); m(j) is the t whose ray first extends it
-    // to j, found while the thread's levels j ascend
-    int tp = 0, cov = -1, mcur = 0;
+    // to j, found per element while the thread's levels j ascend
+    int tp0 = 0, cov0 = -1, m0 = 0, tp1 = 0, cov1 = -1, m1 = 0;
     // per level j the rays' path lengths G[t][j] and P[t][j], contiguous in t
     const float2* PT = a.geo + (size_t)b * 4 * L * L;
     const float2* GT = PT + (size_t)3 * L * L;
-    const df2 z = {0.0f, 0.0f};
-    for (int j = grp; j < L; j += 4) {
-      const df2 cj1 = j >= 1 ? ld(a.c, j - 1) : z;
-      const df2 cj = j <= L - 2 ? ld(a.c, j) : z;
-      const df2 dcc = df_sub(cj1, cj);
+    for (int j = grp; j < L; j += NG) {
+      const dfx cj1 = j >= 1 ? ld(a.c, j - 1) : zx;
+      const dfx cj = j <= L - 2 ? ld(a.c, j) : zx;
+      const dfx dcc = dfx_sub(cj1, cj);
       // g_z part: sum over rays through j of g_tau P (x dcc), over rays ending at j - 1 (x c_{j-1})
-      df2 gc = z, pin = z, pend = z;
+      dfx gc = zx, pin = zx, pend = zx;
       const int tmax = min(j, L - 2);
-      while (cov < j && tp <= L - 2) {
-        cov = max(cov, min((int)I_s[tp * 32 + lane] + 1, L - 1));
-        mcur = tp++;
+      while (cov0 < j && tp0 <= L - 2) {
+        cov0 = max(cov0, min((int)I_s[tp0 * 32 + lane].x + 1, L - 1));
+        m0 = tp0++;
+      }
+      while (cov1 < j && tp1 <= L - 2) {
+        cov1 = max(cov1, min((int)I_s[tp1 * 32 + lane].y + 1, L - 1));
+        m1 = tp1++;
       }
       // from the lowest m(j) of the warp's wavenumbers, so the path-length loads stay uniform
       const unsigned mask = __activemask();
-      const int t0 = (int)__reduce_min_sync(mask, (unsigned)mcur);
-      auto ray = [&](int t, int I, float2 g, float2 p, float2 gt) {
-        if (I < j - 1) return;  // the ray of tangent level t stops below level j
-        const df2 gtau = {gt.x, gt.y};
-        const bool in_j = I >= j && j <= L - 2;
-        if (in_j) gc = df_fma(gtau, df2{g.x, g.y}, gc);
+      const int t0 = (int)__reduce_min_sync(mask, (unsigned)min(m0, m1));
+      auto ray = [&](int t, short2 I, float2 g, float2 p, float4 q) {
+        // per element: the ray of tangent level t reaches level j (I >= j - 1); it passes
+        // through j (sum g_c and P "in") or ends at j - 1 (P "end")
+        const bool r0 = I.x >= j - 1, r1 = I.y >= j - 1;
+        const bool in0 = r0 && I.x >= j && j <= L - 2, in1 = r1 && I.y >= j && j <= L - 2;
+        const dfx gtau = {make_float2(q.x, q.y), make_float2(q.z, q.w)};
+        if (in0 || in1) gc = dfx_fma(dfx_select(in0, in1, gtau, zx), dfx_bcast(df2{g.x, g.y}), gc);
         if (t < j) {
-          if (in_j) pin = df_fma(gtau, df2{p.x, p.y}, pin);
-          else pend = df_fma(gtau, df2{p.x, p.y}, pend);  // j - 1 <= I_t holds here
+          const bool e0 = r0 && !in0, e1 = r1 && !in1;
+          const dfx pp = dfx_bcast(df2{p.x, p.y});
+          if (in0 || in1) pin = dfx_fma(dfx_select(in0, in1, gtau, zx), pp, pin);
+          if (e0 || e1) pend = dfx_fma(dfx_select(e0, e1, gtau, zx), pp, pend);
         }
       };
       const float2* Gj = GT + (size_t)j * L;
@@ -258,30 +278,31 @@ __global__ void __launch_bounds__(128) tr_adjoint_pass2a(DeviceModel dm, TrArgs 
       int t = t0;
       // two rays per step, their loads issued together (same sums, same order)
       for (; t + 1 <= tmax; t += 2) {
-        const int I0 = I_s[t * 32 + lane], I1 = I_s[(t + 1) * 32 + lane];
+        const short2 I0 = I_s[t * 32 + lane], I1 = I_s[(t + 1) * 32 + lane];
         const float2 g0 = __ldg(&Gj[t]), g1 = __ldg(&Gj[t + 1]), p0 = __ldg(&Pj[t]), p1 = __ldg(&Pj[t + 1]);
-        const float2 q0 = gt_s[t * 32 + lane], q1 = gt_s[(t + 1) * 32 + lane];
+        const float4 q0 = gt_s[t * 32 + lane], q1 = gt_s[(t + 1) * 32 + lane];
         ray(t, I0, g0, p0, q0);
         ray(t + 1, I1, g1, p1, q1);
       }
       if (t <= tmax) ray(t, I_s[t * 32 + lane], __ldg(&Gj[t]), __ldg(&Pj[t]), gt_s[t * 32 + lane]);
-      const df2 gzp = df_fma(pin, dcc, df_mul(pend, cj1));
+      const dfx gzp = dfx_fma(pin, dcc, dfx_mul(pend, cj1));
       // direct terms of the effective height: z1_j + g_h (A_{j-1} - A_{j+1}) (- A_0 at j = 0)
-      df2 nb = z;
+      dfx nb = zx;
       if (j >= 1) nb = ld(a.us, j - 1);
-      if (j + 1 <= L - 2) nb = df_sub(nb, ld(a.us, j + 1));
-      if (j == 0) nb = df_sub(nb, ld(a.us, 0));
-      df2 gzt = df_fma(gh, nb, gzp);
-      if (j <= L - 2) gzt = df_add(gzt, ld(a.qs, j));
-      a.gc[col + (size_t)j * N] = make_float2(gc.hi, gc.lo);
-      a.gz[col + (size_t)j * N] = make_float2(gzt.hi, gzt.lo);
+      if (j + 1 <= L - 2) nb = dfx_sub(nb, ld(a.us, j + 1));
+      if (j == 0) nb = dfx_sub(nb, ld(a.us, 0));
+      dfx gzt = dfx_fma(gh, nb, gzp);
+      if (j <= L - 2) gzt = dfx_add(gzt, ld(a.qs, j));
+      st(a.gc, j, gc);
+      st(a.gz, j, gzt);
     }
   }
-  rp_part[threadIdx.x] = make_float2(rp.hi, rp.lo);
+  const df2 rps = df_add(dfx_get(rp, 0), dfx_get(rp, 1));
+  rp_part[threadIdx.x] = make_float2(rps.hi, rps.lo);
   __syncthreads();
   if (threadIdx.x == 0) {
     double s = 0.0;
-    for (int q = 0; q < 128; ++q) s += df_to_double(sm(rp_part, q));
+    for (int q = 0; q < 32 * NG; ++q) s += df_to_double(df2{rp_part[q].x, rp_part[q].y});
     a.rp[(size_t)b * gridDim.x + blockIdx.x] = s;
   }
 }
@@ -986,6 +1007,7 @@ void transmission_adjoint_chunk(Model& m, const double* params_chunk, int nb, cu
   const int L = m.L, S = m.acfg.S, P = m.acfg.nparam_total;
   const size_t N = m.N;
   const int tiles = (int)((N + 31) / 32);
+  const int tiles2a = (int)((N + 63) / 64);  // pass 2a: 64 wavenumbers per block (the d log L / dR partials)
   TrArgs a{w.lev, w.lsdf, w.ray_n, w.ev, reinterpret_cast<const float2*>(w.geom), tp.tr_geo, tp.dwT, g.gS,
            g.seed, tp.tr_c, tp.tr_T, tp.tr_qs, tp.tr_us, tp.tr_I, g.tr_gc, g.tr_gz, g.tr_rp, g.partial, V,
            tp.tr_ts, tp.tr_dk, g.tr_cs, m.acfg.cloud_kind == 1 ? 1 : m.acfg.cloud_kind == 2 ? 3 : 0};
@@ -993,10 +1015,10 @@ void transmission_adjoint_chunk(Model& m, const double* params_chunk, int nb, cu
     tr_cloud_shape_kernel<<<dim3(nb, (unsigned)((N + 255) / 256)), 256, 0, st>>>(dm, w.ev, g.tr_cs, a.nc);
     BGB_CUDA(cudaGetLastError());
   }
-  const size_t sm2a = (size_t)L * 32 * (sizeof(float2) + sizeof(short)) + (size_t)3 * L * sizeof(float2);
+  const size_t sm2a = (size_t)L * 32 * (sizeof(float4) + sizeof(short2)) + (size_t)3 * L * sizeof(float2);
   if (sm2a > 48 * 1024)
     BGB_CUDA(cudaFuncSetAttribute(tr_adjoint_pass2a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2a));
-  tr_adjoint_pass2a<<<dim3(tiles, nb), 128, sm2a, st>>>(dm, a);
+  tr_adjoint_pass2a<<<dim3(tiles2a, nb), 32 * kPass2aGroups, sm2a, st>>>(dm, a);
   BGB_CUDA(cudaGetLastError());
   const size_t sm2 = (size_t)S * kTrSinkThreads * (sizeof(float2) + sizeof(double)) + (size_t)m.acfg.R * sizeof(float2);
   const int VP = V <= 8 ? 8 : V <= 16 ? 16 : 32;
@@ -1038,7 +1060,7 @@ void transmission_adjoint_chunk(Model& m, const double* params_chunk, int nb, cu
   if (sma > 48 * 1024)
     BGB_CUDA(cudaFuncSetAttribute(tr_atmosphere_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sma));
   tr_atmosphere_adjoint_kernel<<<nb, 128, sma, st>>>(dm, params_chunk, P, w.lev, w.ev, g.partial, V, 1, g.tr_rp,
-                                                     tiles, g.seed, grad_chunk);
+                                                     tiles2a, g.seed, grad_chunk);
   BGB_CUDA(cudaGetLastError());
 }
 
