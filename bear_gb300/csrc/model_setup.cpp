@@ -849,7 +849,11 @@ static void setup_atmosphere(Model& m) {
   a.cloud_kind = m.cloud ? m.cloud_kind : 0;
   a.cloud_ref_wl = m.cloud_ref_wl;
   a.fit_mmw = m.fit_mmw;
-  a.var_g = m.var_g;
+  // variable gravity applies to transmission models only: the emission and secondary-eclipse
+  // models compute their structure with constant gravity (EmissionModel::calcAtmosphereStructure
+  // src/forward_model/emission/emission.cpp:178-185, OccultationModel::calcAtmosphereStructure
+  // src/forward_model/secondary_eclipse/secondary_eclipse.cpp:165-172 pass false)
+  a.var_g = m.var_g && m.transmission;
   // table species: temperature nodes and the (parameter-independent) pressure bracket of
   // every level for every temperature row (OpacitySpecies::findClosestDataPoints
   // src/transport_coeff/opacity_species.cpp:204-269)

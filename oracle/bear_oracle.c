@@ -1069,7 +1069,8 @@ static int atmosphere(const orc_model* m, const double* tparam, const double* cp
   a->z[0] = 0.0;
   for (int i = 1; i < L; ++i) {
     double gi = g;
-    if (m->var_g) { const double lr = bottom_radius + a->z[i - 1]; gi = g * pow(bottom_radius / lr, 2.0); }
+    /* transmission models only (emission.cpp:178-185 and secondary_eclipse.cpp:165-172 pass false) */
+    if (m->var_g && m->transmission) { const double lr = bottom_radius + a->z[i - 1]; gi = g * pow(bottom_radius / lr, 2.0); }
     double dz = (1.0 / (rho[i] * gi) + 1.0 / (rho[i - 1] * gi)) * 0.5 * (m->p[i - 1] * 1e6 - m->p[i] * 1e6);
     a->z[i] = a->z[i - 1] + dz;
   }

@@ -195,3 +195,19 @@ def test_double_float_path_against_fp64_path(name, kind):
     assert np.all(d <= tol), (d.max(), tol.min())
     assert rel_spec < 1e-9
     e.close()
+
+
+def test_variable_gravity_is_ignored_by_emission_models():
+    """As in the reference (EmissionModel::calcAtmosphereStructure
+    src/forward_model/emission/emission.cpp:178-185 passes constant gravity), the engine's
+    emission model gives the same log L with the variable-gravity key on."""
+    c = goldenlib.Case(os.path.join(goldenlib.GOLDEN_DIR, "emission_edges.npz"))
+    obs = c.observations()
+    e0 = Engine(c.config_text(), obs)
+    e1 = Engine(c.config_text() + "variable_gravity 1\n", obs)
+    try:
+        for p in c.params[:2]:
+            assert e1.loglike(p) == e0.loglike(p)
+    finally:
+        e0.close()
+        e1.close()
