@@ -1180,7 +1180,6 @@ void transmission_adjoint_chunk(Model& m, const double* params_chunk, int nb, cu
 static void launch_gradient_transmission(Model& m, const double* params_dev, int batch, cudaStream_t st,
                                          double* loglike_dev, double* grad_dev, uint8_t* neglect_dev) {
   if (m.precision != 0) throw Error(BEAR_ERR_UNSUPPORTED, "the transmission gradient runs in precision mode 0");
-  if (m.var_g) throw Error(BEAR_ERR_UNSUPPORTED, "the transmission gradient does not support variable gravity");
   if (m.annuli > 1) throw Error(BEAR_ERR_UNSUPPORTED, "the transmission gradient needs one impact parameter per level");
   const int S = m.acfg.S, R = m.acfg.R, L = m.L, P = m.acfg.nparam_total;
   // level values: species, Rayleigh / H- terms, temperature, altitude, cloud extinction, then

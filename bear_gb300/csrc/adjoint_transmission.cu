@@ -573,30 +573,50 @@ __global__ void __launch_bounds__(128) tr_atmosphere_adjoint_kernel(
     du = u * (dT_at(l) / T - dmmw / mmw);
     return u;
   };
-  // Delta_l tangent (layer l - 1 -> l): 0.5 (p_{l-1} - p_l) 1e6 ((du_l + du_{l-1}) - (u_l + u_{l-1}) d ln g) / g
-  auto ddelta = [&](int l, double u, double du, double u_prev, double du_prev) {
-    const double pf = 0.5 * (dm.pressure[l - 1] * 1e6 - dm.pressure[l] * 1e6) / g;
-    return pf * ((du + du_prev) - (u + u_prev) * dlng);
+  // The altitude tangent dz_l = dz_{l-1} + A_l + B_l dz_{l-1} for the layer l - 1 -> l:
+  // constant gravity (Delta_l = 0.5 (p_{l-1} - p_l) 1e6 (u_l + u_{l-1}) / g): B_l = 0,
+  // A_l = 0.5 (p_{l-1} - p_l) 1e6 ((du_l + du_{l-1}) - (u_l + u_{l-1}) d ln g) / g; variable
+  // gravity (g_l = g R^2 / (R + z_{l-1})^2, Atmosphere::calcAltitudeVariableGravity
+  // src/forward_model/atmosphere/atmosphere.cpp:311-334, R the planet radius): with the
+  // forward's Delta_l = z_l - z_{l-1}, B_l = 2 Delta_l / (R + z_{l-1}) and
+  // A_l = Delta_l ((du_l + du_{l-1}) / (u_l + u_{l-1}) - d ln g - 2 dR / R + 2 dR / (R + z_{l-1})).
+  const double R0 = gen[1], dR0 = th == 1 ? 1.0 : 0.0;
+  auto ddelta = [&](int l, double u, double du, double u_prev, double du_prev, double& B) {
+    if (!c.var_g) {
+      B = 0.0;
+      const double pf = 0.5 * (dm.pressure[l - 1] * 1e6 - dm.pressure[l] * 1e6) / g;
+      return pf * ((du + du_prev) - (u + u_prev) * dlng);
+    }
+    const double zp = lev[(size_t)b * L + l - 1].z, dzv = lev[(size_t)b * L + l].z - zp;
+    B = 2.0 * dzv / (R0 + zp);
+    return dzv * ((du + du_prev) / (u + u_prev) - dlng - 2.0 * dR0 / R0 + 2.0 * dR0 / (R0 + zp));
   };
-  // pass 1: the chunk's altitude-tangent increment
+  // pass 1: the chunk's affine map of the altitude tangent, dz_end = M dz_start + C
+  __shared__ double part_m[128];
   double u_prev = 0.0, du_prev = 0.0;
   if (work) {
-    double inc = 0.0;
+    double Mc = 1.0, Cc = 0.0;
     if (l0 >= 1) u_prev = u_at(l0 - 1, du_prev);
     double up = u_prev, dup = du_prev;
     for (int l = l0; l < l1; ++l) {
       double du;
       const double u = u_at(l, du);
-      if (l >= 1) inc += ddelta(l, u, du, up, dup);
+      if (l >= 1) {
+        double B;
+        const double A = ddelta(l, u, du, up, dup, B);
+        Cc = c.var_g ? fma(1.0 + B, Cc, A) : Cc + A;
+        Mc *= 1.0 + B;
+      }
       up = u;
       dup = du;
     }
-    part[tid] = inc;
+    part[tid] = Cc;
+    part_m[tid] = Mc;
   }
   __syncthreads();
   double dz = 0.0, dz_prev = 0.0, acc = 0.0;
   if (work)
-    for (int q = 0; q < ch; ++q) dz += part[q * P + th];
+    for (int q = 0; q < ch; ++q) dz = c.var_g ? fma(part_m[q * P + th], dz, part[q * P + th]) : dz + part[q * P + th];
   __syncthreads();
   for (int l = l0; work && l < l1; ++l) {
     const LevelInfo li = lev[(size_t)b * L + l];
@@ -624,7 +644,11 @@ __global__ void __launch_bounds__(128) tr_atmosphere_adjoint_kernel(
     double du;
     const double u = u_at(l, du);
     dz_prev = dz;
-    if (l >= 1) dz += ddelta(l, u, du, u_prev, du_prev);
+    if (l >= 1) {
+      double B;
+      const double A = ddelta(l, u, du, u_prev, du_prev, B);
+      dz = c.var_g ? fma(1.0 + B, dz, A) : dz + A;
+    }
     u_prev = u;
     du_prev = du;
     acc = fma(sgl[S + R + 1], dz, acc);

@@ -187,26 +187,31 @@ def test_transmission_gradient_neglect_and_precision(case):
         e.set_precision(0)
 
 
-@pytest.fixture(scope="module")
-def odd_case():
+@pytest.fixture(scope="module", params=[0, 1], ids=["constant_gravity", "variable_gravity"])
+def odd_case(request):
     """The transmission edge-case set (60 levels, 16469 points: an odd count, so pass 2b
     reads single wavenumbers instead of pairs), fitted mean molecular weight, error
-    inflation and a 3-knot temperature profile; constant gravity (the transmission
-    gradient rejects variable gravity)."""
+    inflation and a 3-knot temperature profile; constant gravity, and the variable gravity
+    of Atmosphere::calcAltitudeVariableGravity (src/forward_model/atmosphere/atmosphere.cpp:311-334),
+    whose altitude tangent carries d z_{l-1} and the planet radius into each layer."""
     c = goldenlib.Case(os.path.join(goldenlib.GOLDEN_DIR, "transmission_edges.npz"))
-    text = c.config_text().replace("variable_gravity 1", "variable_gravity 0")
+    text = c.config_text()
+    assert "variable_gravity 1" in text
+    if request.param == 0:
+        text = text.replace("variable_gravity 1", "variable_gravity 0")
     obs = c.observations()
     e = Engine(text, obs)
     om = oracle.OracleModel(text, obs)
     assert e.N % 2 == 1
-    yield c, e, om
+    yield c, e, om, ("variable_gravity" if request.param else "constant_gravity")
+    om.close()
     e.close()
 
 
 def test_transmission_gradient_odd_point_count(odd_case):
     """Odd N, with and without the stored opacity terms, against the FP64 oracle's
     Richardson differences (cut-off disabled)."""
-    c, e, om = odd_case
+    c, e, om, tag = odd_case
     phys = np.array(c.params[:3], dtype=np.float64)
     e.set_tau_cutoff(float("inf"))
     om.set_tau_cutoff(float("inf"))
@@ -237,7 +242,7 @@ def test_transmission_gradient_odd_point_count(odd_case):
                 tol = 1e-6 * abs(sf[j]) + 1e-8 * scale + 2e-10 * abs(ll_s[i]) / 1e-5
                 assert err <= tol, (i, j, sa[j], sf[j], err, tol)
                 worst = max(worst, err / max(abs(sf[j]), 1e-300))
-        _record("odd_point_count_fd_worst_rel_err", worst)
+        _record("odd_point_count_fd_worst_rel_err_" + tag, worst)
     finally:
         e.set_tau_cutoff(10.0)
         om.set_tau_cutoff(10.0)
