@@ -13,11 +13,11 @@
 // normaliser come from adjoint.cu):
 //   tr_geometry_adjoint_kernel  per evaluation, before the forward radiative transfer:
 //                               P[t][j] = dG[t][j-1]/dz_j = (R + z_j)/S_t(j) (stored as
-//                               [j][t]), Q[t][i] = dG[t][i]/dz_t, U[t][i] = dG[t][i]/dR, and
-//                               the path lengths G transposed ([j][t]) for pass 2a
+//                               [j][t]), Q[t][i] = dG[t][i]/dz_t and the path lengths G
+//                               transposed ([j][t]) for pass 2a
 //   transmission_kernel<STORE>  (engine.cu) the forward pass itself also stores, per (level,
 //                               wavenumber), the ray transmission T_t, the cut-off index, the
-//                               pair sums c and the ray sums of c dG/dz_t and c dG/dR
+//                               pair sums c and the ray sum of c dG/dz_t
 //   tr_adjoint_pass2a           per (level j, wavenumber), g_tau_t = d log L / d tau_t and the
 //                               cut-off indices staged in shared memory: d log L / d c_j =
 //                               sum_t g_tau_t G[t][j], d log L / d z_j (geometry and effective
@@ -63,10 +63,9 @@ __global__ void tr_geometry_adjoint_kernel(DeviceModel dm, const LevelInfo* __re
   const int b = blockIdx.x, L = dm.L;
   const LevelInfo* lv = lev + (size_t)b * L;
   const double R = ev[b].radius;
-  float2* PT = geo + (size_t)b * 4 * L * L;  // [j][t]: P transposed, for the per-level sums of pass 2a
+  float2* PT = geo + (size_t)b * 3 * L * L;  // [j][t]: P transposed, for the per-level sums of pass 2a
   float2* Q = PT + (size_t)L * L;
-  float2* U = Q + (size_t)L * L;
-  float2* GT = U + (size_t)L * L;            // [j][t]: the forward path lengths G transposed
+  float2* GT = Q + (size_t)L * L;            // [j][t]: the forward path lengths G transposed
   const float2* G = geom + (size_t)b * L * L;
   // 1 / S_t(j) for j > t (0 for j <= t or a degenerate zero path)
   auto rS = [&](int t, int j) -> double {
@@ -85,14 +84,9 @@ __global__ void tr_geometry_adjoint_kernel(DeviceModel dm, const LevelInfo* __re
     const double zt = lv[t].z;
     put(PT + (size_t)i * L + t, (R + lv[i].z) * rS(t, i));
     GT[(size_t)i * L + t] = __ldg(&G[idx]);
-    double q = 0.0, u = 0.0;
-    if (i >= t && i < L - 1) {
-      const double r0 = rS(t, i), r1 = rS(t, i + 1);
-      q = (R + zt) * (r0 - r1);
-      u = (lv[i + 1].z - zt) * r1 - (lv[i].z - zt) * r0;
-    }
+    double q = 0.0;
+    if (i >= t && i < L - 1) q = (R + zt) * (rS(t, i) - rS(t, i + 1));
     put(Q + idx, q);
-    put(U + idx, u);
   }
 }
 
@@ -110,7 +104,7 @@ struct TrArgs {
   const float2* c;
   const float2* T;
   float2* qs;  // read, then overwritten with the direct altitude sink z1_t
-  float2* us;  // read, then overwritten with A_t = (R + z_t)(1 - T_t)
+  float2* us;  // written with A_t = (R + z_t)(1 - T_t)
   const short* I;
   float2* gc;
   float2* gz;
@@ -160,7 +154,9 @@ __global__ void tr_cloud_shape_kernel(DeviceModel dm, const EvalInfo* __restrict
 //   g_z_j   = sum_{t < j} g_tau_t P[t][j] (c_{j-1} [j-1 <= I_t] - c_j [j <= I_t])
 //           + g_h (1 - T_j) wz_j + g_tau_j qs_j + g_h (A_{j-1} - A_{j+1}) (- A_0 at j = 0),
 //             A_t = (R + z_t)(1 - T_t)   (wz_t = z_{t+1} - z_{t-1}; z_1 - z_0 at t = 0)
-//   dlogL/dR += g_h (1 - T_j) wz_j + g_tau_j us_j (+ 2 R g_h once: depth = (h + R^2) / R_s^2)
+//   dlogL/dR = sum_j g_z_j + 2 R g_h (depth = (h + R^2) / R_s^2): every radius in the path
+//             lengths and the effective-height weights is R + z_j, so their derivative along R
+//             is the sum of their derivatives along the z_j
 // Two wavenumbers per lane (k and k + 32 of a 64-wavenumber tile) with paired FP32
 // double-float instructions (dfloat2x.cuh), eight groups of levels: every per-element step is
 // the one-wavenumber step, and a ray that does not reach level j (or a sum it does not enter)
@@ -216,14 +212,13 @@ __global__ void __launch_bounds__(32 * kPass2aGroups, 3) tr_adjoint_pass2a(Devic
     return dfx_bcast(df2{v.x, v.y});
   };
   // per tangent level: g_tau_t = g_h F_t T_t (staged), A_t = (R + z_t)(1 - T_t) and the direct
-  // sink z1_t = g_h (1 - T_t) wz_t + g_tau_t qs_t, written over the ray sums they replace
+  // sink z1_t = g_h (1 - T_t) wz_t + g_tau_t qs_t, written over the ray sum qs_t and into a.us
   dfx rp = zx;
   for (int t = grp; t < L - 1; t += NG) {
     const dfx T = ld(a.T, t), omT = dfx_sub(one, T);
     const dfx gt = dfx_mul(dfx_mul(gh, sm(ff_s, t)), T);
     const dfx base = dfx_mul(dfx_mul(gh, omT), sm(fw_s, t));
     const dfx z1 = dfx_add(base, dfx_mul(gt, ld(a.qs, t)));
-    rp = dfx_add(rp, dfx_add(base, dfx_mul(gt, ld(a.us, t))));
     const dfx A = dfx_mul(sm(fz_s, t), omT);
     gt_s[t * 32 + lane] = make_float4(gt.hi.x, gt.hi.y, gt.lo.x, gt.lo.y);
     I_s[t * 32 + lane] = make_short2(a.I[col0 + (size_t)t * N], a.I[col1 + (size_t)t * N]);
@@ -239,8 +234,8 @@ __global__ void __launch_bounds__(32 * kPass2aGroups, 3) tr_adjoint_pass2a(Devic
     // to j, found per element while the thread's levels j ascend
     int tp0 = 0, cov0 = -1, m0 = 0, tp1 = 0, cov1 = -1, m1 = 0;
     // per level j the rays' path lengths G[t][j] and P[t][j], contiguous in t
-    const float2* PT = a.geo + (size_t)b * 4 * L * L;
-    const float2* GT = PT + (size_t)3 * L * L;
+    const float2* PT = a.geo + (size_t)b * 3 * L * L;
+    const float2* GT = PT + (size_t)2 * L * L;
     for (int j = grp; j < L; j += NG) {
       const dfx cj1 = j >= 1 ? ld(a.c, j - 1) : zx;
       const dfx cj = j <= L - 2 ? ld(a.c, j) : zx;
@@ -295,6 +290,8 @@ __global__ void __launch_bounds__(32 * kPass2aGroups, 3) tr_adjoint_pass2a(Devic
       if (j <= L - 2) gzt = dfx_add(gzt, ld(a.qs, j));
       st(a.gc, j, gc);
       st(a.gz, j, gzt);
+      // (an element past N reads wavenumber N - 1's stored sinks: left out)
+      rp = dfx_add(rp, dfx_select(true, act1, gzt, zx));
     }
   }
   const df2 rps = df_add(dfx_get(rp, 0), dfx_get(rp, 1));
@@ -686,7 +683,7 @@ size_t transmission_grad_bytes_per_eval(const Model& m, int V, bool store) {
   const size_t tiles = (N + 31) / 32;
   const size_t terms = store ? L * N * ((size_t)m.acfg.S + 1) * sizeof(float2) : 0;
   const size_t cs = m.acfg.cloud_kind ? (m.acfg.cloud_kind == 1 ? 2 : 4) * N * sizeof(double) : 0;
-  return L * N * (6 * sizeof(float2) + sizeof(short)) + 4 * L * L * sizeof(float2) + L * (size_t)V * 8 +
+  return L * N * (6 * sizeof(float2) + sizeof(short)) + 3 * L * L * sizeof(float2) + L * (size_t)V * 8 +
          tiles * 8 + terms + cs;
 }
 
@@ -706,7 +703,7 @@ void alloc_transmission_grad(Model& m, int chunk, int V, bool store) {
   BGB_CUDA(cudaMalloc(&g.taps.tr_qs, n * sizeof(float2)));
   BGB_CUDA(cudaMalloc(&g.taps.tr_us, n * sizeof(float2)));
   BGB_CUDA(cudaMalloc(&g.taps.tr_I, n * sizeof(short)));
-  BGB_CUDA(cudaMalloc(&g.taps.tr_geo, B * 4 * L * L * sizeof(float2)));
+  BGB_CUDA(cudaMalloc(&g.taps.tr_geo, B * 3 * L * L * sizeof(float2)));
   BGB_CUDA(cudaMalloc(&g.tr_gc, (n + 2) * sizeof(float2)));
   BGB_CUDA(cudaMalloc(&g.tr_gz, (n + 2) * sizeof(float2)));
   BGB_CUDA(cudaMalloc(&g.tr_rp, B * tiles * sizeof(double)));

@@ -342,8 +342,8 @@ __global__ void transmission_geometry_kernel(DeviceModel dm, const LevelInfo* __
 // evaluation's Rayleigh number densities [L][R] as double-floats.
 // With STORE (double-float path, gradient pass) the kernel also writes, per
 // (evaluation, level, wavenumber), the pair sums c, the ray transmissions T_t, the
-// last index inside the cut-off and the sums of c_i dG[t][i]/dz_t and c_i dG[t][i]/dR
-// over each ray (taps.tr_*; dG from taps.tr_geo, computed before this kernel).
+// last index inside the cut-off and the sum of c_i dG[t][i]/dz_t over each ray (taps.tr_*;
+// dG/dz_t from taps.tr_geo, computed before this kernel).
 constexpr int kTPN = 4;
 // The effective-height sum sum_t rw_t (1 - T_t) is formed as kHeightGroups partial sums,
 // group g holding the rays t = L - 2 - g - kHeightGroups m in descending order, added in
@@ -494,21 +494,19 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
     for (int t = L - 2 - j; t >= 0; t -= TPN) {
       double tau = 0.0;
       df2 tsd = {0.0f, 0.0f};  // the tangent sum as a double-float (DF)
-      df2 qs = {0.0f, 0.0f}, us = {0.0f, 0.0f};
+      df2 qs = {0.0f, 0.0f};
       int last = L - 2;
       if (DF && STORE) {
         const float2* Gt = reinterpret_cast<const float2*>(geom) + (size_t)b * L * L + (size_t)t * L;
-        const float2* Qt = taps.tr_geo + (size_t)b * 4 * L * L + (size_t)L * L + (size_t)t * L;
-        const float2* Ut = Qt + (size_t)L * L;
+        const float2* Qt = taps.tr_geo + (size_t)b * 3 * L * L + (size_t)L * L + (size_t)t * L;
         const float ch = dm.tau_cut_hi, cl = dm.tau_cut_lo;
         df2 ts = {0.0f, 0.0f};
         bool cut = false;
-        // one segment of the three ray sums; true at the cut-off (tau > cut-off)
-        auto seg = [&](float2 g, float2 c, float2 q, float2 u) {
+        // one segment of the two ray sums; true at the cut-off (tau > cut-off)
+        auto seg = [&](float2 g, float2 c, float2 q) {
           const df2 cc = {c.x, c.y};
           ts = df_fma(df2{g.x, g.y}, cc, ts);
           qs = df_fma(df2{q.x, q.y}, cc, qs);
-          us = df_fma(df2{u.x, u.y}, cc, us);
           return ts.hi > ch || (ts.hi == ch && ts.lo > cl);
         };
         int i = t;
@@ -516,17 +514,16 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
         for (; i + 1 < L - 1 && !cut; i += 2) {
           const float2 g0 = __ldg(&Gt[i]), g1 = __ldg(&Gt[i + 1]);
           const float2 q0 = __ldg(&Qt[i]), q1 = __ldg(&Qt[i + 1]);
-          const float2 u0 = __ldg(&Ut[i]), u1 = __ldg(&Ut[i + 1]);
           const float2 c0 = chi_f[i * VPB + v], c1 = chi_f[(i + 1) * VPB + v];
-          if (seg(g0, c0, q0, u0)) {
+          if (seg(g0, c0, q0)) {
             last = i;
             cut = true;
-          } else if (seg(g1, c1, q1, u1)) {
+          } else if (seg(g1, c1, q1)) {
             last = i + 1;
             cut = true;
           }
         }
-        if (i < L - 1 && !cut && seg(__ldg(&Gt[i]), chi_f[i * VPB + v], __ldg(&Qt[i]), __ldg(&Ut[i]))) last = i;
+        if (i < L - 1 && !cut && seg(__ldg(&Gt[i]), chi_f[i * VPB + v], __ldg(&Qt[i]))) last = i;
         tsd = ts;
       } else if (DF) {
         const float2* Gt = reinterpret_cast<const float2*>(geom) + (size_t)b * L * L + (size_t)t * L;
@@ -576,7 +573,6 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
           const size_t at = col + (size_t)t * N;
           taps.tr_T[at] = make_float2(T.hi, T.lo);
           taps.tr_qs[at] = make_float2(qs.hi, qs.lo);
-          taps.tr_us[at] = make_float2(us.hi, us.lo);
           taps.tr_I[at] = (short)last;
         }
         omt = df_to_double(df_sub(df_make(1.0f), T));
@@ -626,7 +622,7 @@ __global__ void __launch_bounds__(kTPN * VPB) transmission_kernel(DeviceModel dm
 // 15.5-16.9 ms. About two thirds of the time is the extinction column.
 // With STORE (the gradient's forward pass) it also writes transmission_kernel<STORE>'s
 // stores: the opacity terms and temperature-slope sums, the pair sums c, and per ray T_t,
-// the cut-off index and the ray sums of c dG/dz_t and c dG/dR.
+// the cut-off index and the ray sum of c dG/dz_t.
 template <int VP, int TPN, int MINB, int GRP, bool STORE = false>
 __global__ void __launch_bounds__(TPN * VP, MINB) transmission_kernel_x2(DeviceModel dm, const LevelInfo* __restrict__ lev,
                                                                   const LevelSpeciesDF* __restrict__ lsdf,
@@ -745,10 +741,9 @@ __global__ void __launch_bounds__(TPN * VP, MINB) transmission_kernel_x2(DeviceM
     const float ch = dm.tau_cut_hi, cl = dm.tau_cut_lo;
     for (int t = L - 2 - j; t >= 0; t -= TPN) {
       const float2* Gt = reinterpret_cast<const float2*>(geom) + (size_t)b * L * L + (size_t)t * L;
-      // STORE: the ray sums of c dG/dz_t (Q) and c dG/dR (U) beside the optical depth
-      const float2* Qt = STORE ? taps.tr_geo + (size_t)b * 4 * L * L + (size_t)L * L + (size_t)t * L : nullptr;
-      const float2* Ut = STORE ? Qt + (size_t)L * L : nullptr;
-      dfx ts = {f2(0.0f), f2(0.0f)}, qs = ts, us = ts;
+      // STORE: the ray sum of c dG/dz_t (Q) beside the optical depth
+      const float2* Qt = STORE ? taps.tr_geo + (size_t)b * 3 * L * L + (size_t)L * L + (size_t)t * L : nullptr;
+      dfx ts = {f2(0.0f), f2(0.0f)}, qs = ts;
       bool cut0 = false, cut1 = false;
       int last0 = L - 2, last1 = L - 2;  // the last index inside the cut-off
       int i = t;
@@ -758,9 +753,8 @@ __global__ void __launch_bounds__(TPN * VP, MINB) transmission_kernel_x2(DeviceM
         const dfx cc = {make_float2(c.x, c.y), make_float2(c.z, c.w)};
         ts = dfx_fma(dfx_bcast(df2{g.x, g.y}), cc, ts);
         if (STORE) {
-          const float2 q = __ldg(&Qt[i]), u = __ldg(&Ut[i]);
+          const float2 q = __ldg(&Qt[i]);
           qs = dfx_fma(dfx_bcast(df2{q.x, q.y}), cc, qs);
-          us = dfx_fma(dfx_bcast(df2{u.x, u.y}), cc, us);
         }
         if (ts.hi.x >= ch || ts.hi.y >= ch) {  // tau > cut-off needs hi >= the cut-off's hi
           cut0 = ts.hi.x > ch || (ts.hi.x == ch && ts.lo.x > cl);
@@ -776,16 +770,15 @@ __global__ void __launch_bounds__(TPN * VP, MINB) transmission_kernel_x2(DeviceM
       if (cut0 != cut1) {
         // one wavenumber is past the cut-off: the other one's remaining terms alone
         const int e = cut0 ? 1 : 0;
-        df2 te = dfx_get(ts, e), qe = dfx_get(qs, e), ue = dfx_get(us, e);
+        df2 te = dfx_get(ts, e), qe = dfx_get(qs, e);
         for (; i < L - 1; ++i) {
           const float2 g = __ldg(&Gt[i]);
           const float4 c = chi_x[i * VP + v];
           const df2 ce = e ? df2{c.y, c.w} : df2{c.x, c.z};
           te = df_fma(df2{g.x, g.y}, ce, te);
           if (STORE) {
-            const float2 q = __ldg(&Qt[i]), u = __ldg(&Ut[i]);
+            const float2 q = __ldg(&Qt[i]);
             qe = df_fma(df2{q.x, q.y}, ce, qe);
-            ue = df_fma(df2{u.x, u.y}, ce, ue);
           }
           if (te.hi > ch || (te.hi == ch && te.lo > cl)) {
             (e ? last1 : last0) = i;
@@ -794,19 +787,16 @@ __global__ void __launch_bounds__(TPN * VP, MINB) transmission_kernel_x2(DeviceM
         }
         dfx_set(ts, e, te);
         dfx_set(qs, e, qe);
-        dfx_set(us, e, ue);
       }
       const dfx T = dfx_exp_neg(ts, et.hi, et.lo);
       if (STORE) {
         const size_t at = ((size_t)b * L + t) * N;
         taps.tr_T[at + k0] = make_float2(T.hi.x, T.lo.x);
         taps.tr_qs[at + k0] = make_float2(qs.hi.x, qs.lo.x);
-        taps.tr_us[at + k0] = make_float2(us.hi.x, us.lo.x);
         taps.tr_I[at + k0] = (short)last0;
         if (act1) {
           taps.tr_T[at + k1] = make_float2(T.hi.y, T.lo.y);
           taps.tr_qs[at + k1] = make_float2(qs.hi.y, qs.lo.y);
-          taps.tr_us[at + k1] = make_float2(us.hi.y, us.lo.y);
           taps.tr_I[at + k1] = (short)last1;
         }
       }

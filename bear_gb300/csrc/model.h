@@ -228,12 +228,12 @@ struct ForwardTaps {
   float4* em_layer = nullptr;  // emission, B x L x N: layer optical depth and (k_l + k_{l-1}) / 2
                                // as double-floats (layer l between levels l-1 and l; l = 0 unused)
   // transmission, per (evaluation, level, wavenumber) as double-floats unless noted
-  float2* tr_geo = nullptr;  // per evaluation 4 x L x L: dG/dz_j (P, transposed), dG/dz_t (Q),
-                             // dG/dR (U), the path lengths G transposed
+  float2* tr_geo = nullptr;  // per evaluation 3 x L x L: dG/dz_j (P, transposed), dG/dz_t (Q),
+                             // the path lengths G transposed
   float2* tr_c = nullptr;    // extinction pair sums chi_i + chi_{i+1}
   float2* tr_T = nullptr;    // tangent-ray transmission T_t
   float2* tr_qs = nullptr;   // sum_i c_i Q[t][i] over the ray's terms
-  float2* tr_us = nullptr;   // sum_i c_i U[t][i]
+  float2* tr_us = nullptr;   // pass 2a: A_t = (R + z_t)(1 - T_t)
   short* tr_I = nullptr;     // last level index inside the cut-off
   // transmission, when the gradient's memory budget allows (else the adjoint recomputes them):
   float2* tr_ts = nullptr;   // B x L x S x N: each table species' opacity term n_s sigma_s
