@@ -1126,6 +1126,8 @@ void free_grad_workspace(Model& m) {
   cudaFree(g.tr_gz);
   cudaFree(g.tr_rp);
   cudaFree(g.tr_cs);
+  cudaFree(g.taps.tr_d);
+  cudaFree(g.tr_gd);
   g = GradWorkspace{};
 }
 
@@ -1180,7 +1182,6 @@ void transmission_adjoint_chunk(Model& m, const double* params_chunk, int nb, cu
 static void launch_gradient_transmission(Model& m, const double* params_dev, int batch, cudaStream_t st,
                                          double* loglike_dev, double* grad_dev, uint8_t* neglect_dev) {
   if (m.precision != 0) throw Error(BEAR_ERR_UNSUPPORTED, "the transmission gradient runs in precision mode 0");
-  if (m.annuli > 1) throw Error(BEAR_ERR_UNSUPPORTED, "the transmission gradient needs one impact parameter per level");
   const int S = m.acfg.S, R = m.acfg.R, L = m.L, P = m.acfg.nparam_total;
   // level values: species, Rayleigh / H- terms, temperature, altitude, cloud extinction, then
   // the sums along the non-grey cloud's shape parameters
@@ -1194,7 +1195,8 @@ static void launch_gradient_transmission(Model& m, const double* params_dev, int
   // min(batch, 8) evaluations still fit the memory budget; else the adjoint recomputes them
   const size_t extra = L * S1 * sizeof(float2) + M * 8 + 3 * 8;
   const size_t per_store = transmission_grad_bytes_per_eval(m, V, true) + extra;
-  const bool store = m.grad_budget / per_store >= std::min<size_t>((size_t)batch, 8);
+  // (with A > 1 impact parameters per layer the adjoint always recomputes them)
+  const bool store = m.annuli <= 1 && m.grad_budget / per_store >= std::min<size_t>((size_t)batch, 8);
   const size_t per_eval = store ? per_store : transmission_grad_bytes_per_eval(m, V, false) + extra;
   const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)batch, m.grad_budget / per_eval));
   BGB_CUDA(cudaSetDevice(m.device));

@@ -90,6 +90,46 @@ __global__ void tr_geometry_adjoint_kernel(DeviceModel dm, const LevelInfo* __re
   }
 }
 
+// With A impact parameters per layer (ray k = t A + jj of layer t, impact radius
+// b_k = R + zb_k, zb_k = z_t + (z_{t+1} - z_t) jj / A, path lengths G_k[i] = s_{i+1} - s_i,
+// s_i = sqrt((R + z_i)^2 - b_k^2), the first segment G_k[t] = s_{t+1}): per evaluation
+//   PT[j][k] = ds_j / dz_j = (R + z_j) / s_j  (j > t, else 0)
+//   GT[j][k] = G_k[j]                          (t <= j <= L - 2, else 0)
+//   Q[t][i][jj] = dG_k[i] / db_k = b_k (1 / s_i [i > t] - 1 / s_{i+1})   (the forward's layout)
+__global__ void tr_geometry_adjoint_annuli_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
+                                                  const EvalInfo* __restrict__ ev, const float2* __restrict__ geom,
+                                                  const double* __restrict__ rays, float2* __restrict__ geo) {
+  const int b = blockIdx.x, L = dm.L, A = dm.annuli, K = (L - 1) * A;
+  const LevelInfo* lv = lev + (size_t)b * L;
+  const double R = ev[b].radius;
+  const double* zb = rays + (size_t)b * 2 * (K + 1);
+  float2* PT = geo + (size_t)b * 3 * L * K;
+  float2* GT = PT + (size_t)L * K;
+  float2* Q = GT + (size_t)L * K;
+  const float2* G = geom + (size_t)b * (L - 1) * L * A;
+  auto put = [](float2* p, double v) {
+    const df2 d = df_from_double(v);
+    *p = make_float2(d.hi, d.lo);
+  };
+  for (size_t idx = (size_t)blockIdx.y * blockDim.x + threadIdx.x; idx < (size_t)K * L;
+       idx += (size_t)gridDim.y * blockDim.x) {
+    const int kr = (int)(idx / L), i = (int)(idx % L);
+    const int t = kr / A, jj = kr - t * A;
+    const double bt = R + zb[kr], bb = __dmul_rn(bt, bt);
+    auto rS = [&](int j) -> double {  // 1 / s_j (0 at and below the tangent layer's base)
+      if (j <= t) return 0.0;
+      const double a = R + lv[j].z;
+      const double sj = sqrt(__dsub_rn(__dmul_rn(a, a), bb));
+      return sj > 0.0 ? 1.0 / sj : 0.0;
+    };
+    put(PT + (size_t)i * K + kr, i > t ? (R + lv[i].z) * rS(i) : 0.0);
+    const size_t at = ((size_t)t * L + i) * A + jj;
+    const bool seg = i >= t && i < L - 1;
+    GT[(size_t)i * K + kr] = seg ? G[at] : make_float2(0.0f, 0.0f);
+    put(Q + at, seg ? bt * (rS(i) - rS(i + 1)) : 0.0);
+  }
+}
+
 // ------------------------------------------------------------------ pass 2a
 struct TrArgs {
   const LevelInfo* lev;
@@ -115,6 +155,11 @@ struct TrArgs {
   const float2* dk;  // stored temperature-slope sums
   const double* cs;  // non-grey cloud: per evaluation the wavelength factor and its NC shape derivatives
   int nc;            // NC (0: grey cloud or none)
+  // A > 1 impact parameters per layer: the rays' altitudes and weights (the forward
+  // geometry's), the extinction differences and d log L / d of them
+  const double* rays = nullptr;
+  const float2* d = nullptr;
+  float2* gd = nullptr;
 };
 
 // The cloud values of level l at wavenumber k from g_x = d log L / d chi_l: value q0 = 0 (the
@@ -304,6 +349,149 @@ __global__ void __launch_bounds__(32 * kPass2aGroups, 3) tr_adjoint_pass2a(Devic
   }
 }
 
+// Pass 2a with A impact parameters per layer (K = (L - 1) A rays; geometry in
+// tr_geometry_adjoint_annuli_kernel). Ray k of layer t_k with weight w_k = jj / A has
+//   tau_k = G_k[t] (c_t + w_k d_t) + sum_{i = t+1}^{I_k} G_k[i] c_i,  d_t = chi_{t+1} - chi_t,
+//   h = sum_k rw_k (1 - T_k),  rw_k = (R + zb_k)((zb_{k+1} - zb_k) + (zb_k - zb_{k-1})).
+// Block: 64 wavenumbers (two per lane, paired double-floats) x 8 warps, three phases:
+//   1. per ray: g_tau_k = g_h rw_k T_k (over T_k), A_k = (R + zb_k)(1 - T_k), and
+//      z1_k = g_h (1 - T_k) wz_k + g_tau_k qs_k (over qs_k; qs_k = dtau_k / db_k)
+//   2. per ray: D_k = d log L / d zb_k = z1_k + g_h (A_{k-1} - A_{k+1}) (- A_0 at k = 0)
+//   3. per level j, over the rays that reach it (from the lowest one, as in tr_adjoint_pass2a):
+//      g_c_j = sum g_tau_k G_k[j] (segment j in the ray), g_d_j = sum_{t_k = j} g_tau_k w_k G_k[j],
+//      g_z_j = sum_{t_k < j} g_tau_k P_k[j] (c'_{j-1} [j-1 <= I_k] - c_j [j <= I_k])
+//              + sum_{t_k = j} (1 - w_k) D_k + sum_{t_k = j-1} w_k D_k (+ g_h A_{K-1} at j = L - 1),
+//      c'_{j-1} = c_{j-1} + w_k d_{j-1} for the rays of layer j - 1 (their first segment);
+//      d log L / dR = sum_j g_z_j + 2 R g_h as in tr_adjoint_pass2a.
+// The per-ray arrays are [b][k][N]; lanes past N work on wavenumber N - 1 with a zero seed
+// and store nothing.
+__global__ void __launch_bounds__(32 * kPass2aGroups, 2) tr_adjoint_pass2a_annuli(DeviceModel dm, TrArgs a) {
+  constexpr int NG = kPass2aGroups;
+  __shared__ float2 rp_part[32 * NG];
+  const int L = dm.L, A = dm.annuli, K = (L - 1) * A;
+  const int b = blockIdx.y, lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
+  const int kk0 = blockIdx.x * 64 + lane, kk1 = kk0 + 32;
+  const bool act0 = kk0 < dm.N, act1 = kk1 < dm.N;
+  const int k0 = act0 ? kk0 : dm.N - 1, k1 = act1 ? kk1 : dm.N - 1;
+  const size_t N = dm.N;
+  const size_t col0 = (size_t)b * L * N + k0, col1 = (size_t)b * L * N + k1;    // per-level rows
+  const size_t rcol0 = (size_t)b * K * N + k0, rcol1 = (size_t)b * K * N + k1;  // per-ray rows
+  const double Rp = a.ev[b].radius, Rs = a.ev[b].star_radius;
+  const double* zb = a.rays + (size_t)b * 2 * (K + 1);
+  const double* rw = zb + (K + 1);
+  const dfx gh = dfx_make(df_from_double(act0 ? tr_seed(dm, a.gS, a.seed, b, k0) * 1e6 / (Rs * Rs) : 0.0),
+                          df_from_double(act1 ? tr_seed(dm, a.gS, a.seed, b, k1) * 1e6 / (Rs * Rs) : 0.0));
+  const dfx zx = {f2(0.0f), f2(0.0f)};
+  const dfx one = dfx_bcast(df_make(1.0f));
+  auto pair = [](float2 v0, float2 v1) { return dfx{make_float2(v0.x, v1.x), make_float2(v0.y, v1.y)}; };
+  auto ld = [&](const float2* arr, int t) { return pair(arr[col0 + (size_t)t * N], arr[col1 + (size_t)t * N]); };
+  auto ldr = [&](const float2* arr, int k) { return pair(arr[rcol0 + (size_t)k * N], arr[rcol1 + (size_t)k * N]); };
+  auto put = [&](float2* arr, size_t c0, size_t c1, const dfx& v) {
+    if (act0) arr[c0] = make_float2(v.hi.x, v.lo.x);
+    if (act1) arr[c1] = make_float2(v.hi.y, v.lo.y);
+  };
+  auto bc = [](double x) { return dfx_bcast(df_from_double(x)); };
+  // the per-ray stores are rewritten in place: T -> g_tau, us -> A, qs -> z1, then qs -> D
+  float2* gtau_r = const_cast<float2*>(a.T);
+  for (int kr = grp; kr < K; kr += NG) {
+    const dfx T = ldr(a.T, kr), omT = dfx_sub(one, T);
+    const double z = zb[kr];
+    const double wz = (zb[kr + 1] - z) + (kr >= 1 ? z - zb[kr - 1] : 0.0);
+    const dfx gt = dfx_mul(dfx_mul(gh, bc(rw[kr])), T);
+    const dfx z1 = dfx_add(dfx_mul(dfx_mul(gh, omT), bc(wz)), dfx_mul(gt, ldr(a.qs, kr)));
+    const size_t o = (size_t)kr * N;
+    put(gtau_r, rcol0 + o, rcol1 + o, gt);
+    put(a.us, rcol0 + o, rcol1 + o, dfx_mul(bc(Rp + z), omT));
+    put(a.qs, rcol0 + o, rcol1 + o, z1);
+  }
+  __syncthreads();
+  for (int kr = grp; kr < K; kr += NG) {
+    dfx nb = zx;
+    if (kr >= 1) nb = ldr(a.us, kr - 1);
+    if (kr + 1 <= K - 1) nb = dfx_sub(nb, ldr(a.us, kr + 1));
+    if (kr == 0) nb = dfx_sub(nb, ldr(a.us, 0));
+    const size_t o = (size_t)kr * N;
+    put(a.qs, rcol0 + o, rcol1 + o, dfx_fma(gh, nb, ldr(a.qs, kr)));
+  }
+  __syncthreads();
+  const float2* PT = a.geo + (size_t)b * 3 * L * K;
+  const float2* GT = PT + (size_t)L * K;
+  dfx rp = zx;
+  // the lowest ray reaching level j, per element (ray k covers levels t_k .. I_k + 1)
+  int tp0 = 0, cov0 = -1, m0 = 0, tp1 = 0, cov1 = -1, m1 = 0;
+  for (int j = grp; j < L; j += NG) {
+    const dfx cj1 = j >= 1 ? ld(a.c, j - 1) : zx;
+    const dfx cj = j <= L - 2 ? ld(a.c, j) : zx;
+    const dfx dj1 = j >= 1 ? ld(a.d, j - 1) : zx;
+    dfx gc = zx, gd = zx, pin = zx, pend = zx, pw = zx, dd = zx;
+    while (cov0 < j && tp0 <= K - 1) {
+      cov0 = max(cov0, min((int)a.I[rcol0 + (size_t)tp0 * N] + 1, L - 1));
+      m0 = tp0++;
+    }
+    while (cov1 < j && tp1 <= K - 1) {
+      cov1 = max(cov1, min((int)a.I[rcol1 + (size_t)tp1 * N] + 1, L - 1));
+      m1 = tp1++;
+    }
+    const int kmin = (int)__reduce_min_sync(0xffffffffu, (unsigned)min(m0, m1));
+    const int kmax = j <= L - 2 ? min((j + 1) * A, K) - 1 : K - 1;
+    const float2* Gj = GT + (size_t)j * K;
+    const float2* Pj = PT + (size_t)j * K;
+    for (int kr = kmin; kr <= kmax; ++kr) {
+      const int t = kr / A;
+      const short I0 = a.I[rcol0 + (size_t)kr * N], I1 = a.I[rcol1 + (size_t)kr * N];
+      const dfx gtau = ldr(gtau_r, kr);
+      // segment j in the ray (and j <= L - 2), segment j - 1 in the ray
+      const bool in0 = I0 >= j && j <= L - 2, in1 = I1 >= j && j <= L - 2;
+      if (in0 || in1) {
+        const float2 g = __ldg(&Gj[kr]);
+        gc = dfx_fma(dfx_select(in0, in1, gtau, zx), dfx_bcast(df2{g.x, g.y}), gc);
+      }
+      if (t < j) {
+        const bool e0 = I0 >= j - 1 && !in0, e1 = I1 >= j - 1 && !in1;
+        const float2 p = __ldg(&Pj[kr]);
+        const dfx pp = dfx_bcast(df2{p.x, p.y});
+        if (in0 || in1) pin = dfx_fma(dfx_select(in0, in1, gtau, zx), pp, pin);
+        if (e0 || e1) pend = dfx_fma(dfx_select(e0, e1, gtau, zx), pp, pend);
+      }
+    }
+    // the first segments: rays of layer j (g_d, and (1 - w) D) and of layer j - 1 (w P, w D)
+    if (j <= L - 2)
+      for (int jj = 0; jj < A; ++jj) {
+        const int kr = j * A + jj;
+        const double w = (double)jj / A;
+        const dfx gtau = ldr(gtau_r, kr);
+        const float2 g = __ldg(&Gj[kr]);
+        gd = dfx_fma(dfx_mul(gtau, bc(w)), dfx_bcast(df2{g.x, g.y}), gd);
+        dd = dfx_fma(bc(1.0 - w), ldr(a.qs, kr), dd);
+      }
+    if (j >= 1)
+      for (int jj = 0; jj < A; ++jj) {
+        const int kr = (j - 1) * A + jj;
+        const double w = (double)jj / A;
+        const float2 p = __ldg(&Pj[kr]);
+        pw = dfx_fma(dfx_mul(ldr(gtau_r, kr), bc(w)), dfx_bcast(df2{p.x, p.y}), pw);
+        dd = dfx_fma(bc(w), ldr(a.qs, kr), dd);
+      }
+    if (j == L - 1) dd = dfx_fma(gh, ldr(a.us, K - 1), dd);  // zb_K = z_{L-1}
+    const dfx gz = dfx_add(dfx_add(dfx_fma(pin, dfx_sub(cj1, cj), dfx_mul(pend, cj1)), dfx_mul(pw, dj1)), dd);
+    if (j <= L - 2) {
+      put(a.gc, col0 + (size_t)j * N, col1 + (size_t)j * N, gc);
+      put(a.gd, col0 + (size_t)j * N, col1 + (size_t)j * N, gd);
+    }
+    put(a.gz, col0 + (size_t)j * N, col1 + (size_t)j * N, gz);
+    rp = dfx_add(rp, dfx_select(act0, act1, gz, zx));
+  }
+  if (grp == 0) rp = dfx_add(rp, dfx_mul(gh, bc(2.0 * Rp)));  // depth = (h + R^2) / R_s^2
+  const df2 rps = df_add(dfx_get(rp, 0), dfx_get(rp, 1));
+  rp_part[threadIdx.x] = make_float2(rps.hi, rps.lo);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int q = 0; q < 32 * NG; ++q) s += df_to_double(df2{rp_part[q].x, rp_part[q].y});
+    a.rp[(size_t)b * gridDim.x + blockIdx.x] = s;
+  }
+}
+
 // ------------------------------------------------------------------ pass 2b
 // Level sinks: one block per (evaluation, level). The kTrSinkThreads threads stride the
 // wavenumbers and accumulate, as double-floats in registers, v = 0..S-1 d log L / d ln n_s
@@ -400,6 +588,16 @@ __global__ void __launch_bounds__(kTrSinkThreads, VP == 32 ? 4 : 6) tr_adjoint_p
       const float2 c1 = a.gc[row - N + k];
       gx = df_add(gx, df2{c1.x, c1.y});
     }
+    if (a.gd) {  // A > 1: the first segments' c_t + w d_t, d_t = chi_{t+1} - chi_t
+      if (l >= 1) {
+        const float2 d1 = a.gd[row - N + k];
+        gx = df_add(gx, df2{d1.x, d1.y});
+      }
+      if (l <= L - 2) {
+        const float2 d0 = a.gd[row + k];
+        gx = df_sub(gx, df2{d0.x, d0.y});
+      }
+    }
     return gx;
   };
   const float2 no_store = make_float2(__int_as_float(0x7fc00000), 0.0f);
@@ -421,6 +619,18 @@ __global__ void __launch_bounds__(kTrSinkThreads, VP == 32 ? 4 : 6) tr_adjoint_p
         const float4 c = ld4(a.gc + row - N + k0);
         gx0 = df_add(gx0, df2{c.x, c.y});
         gx1 = df_add(gx1, df2{c.z, c.w});
+      }
+      if (a.gd) {
+        if (l >= 1) {
+          const float4 c = ld4(a.gd + row - N + k0);
+          gx0 = df_add(gx0, df2{c.x, c.y});
+          gx1 = df_add(gx1, df2{c.z, c.w});
+        }
+        if (l <= L - 2) {
+          const float4 c = ld4(a.gd + row + k0);
+          gx0 = df_sub(gx0, df2{c.x, c.y});
+          gx1 = df_sub(gx1, df2{c.z, c.w});
+        }
       }
       const float4 gz = ld4(a.gz + row + k0);
       const float4 dks = a.ts ? ld4(a.dk + row + k0) : make_float4(no_store.x, 0.0f, no_store.x, 0.0f);
@@ -679,12 +889,15 @@ __global__ void __launch_bounds__(128) tr_atmosphere_adjoint_kernel(
 
 // ------------------------------------------------------------------ host side
 size_t transmission_grad_bytes_per_eval(const Model& m, int V, bool store) {
-  const size_t L = m.L, N = m.N;
+  const size_t L = m.L, N = m.N, K = transmission_rays(m);
   const size_t tiles = (N + 31) / 32;
   const size_t terms = store ? L * N * ((size_t)m.acfg.S + 1) * sizeof(float2) : 0;
   const size_t cs = m.acfg.cloud_kind ? (m.acfg.cloud_kind == 1 ? 2 : 4) * N * sizeof(double) : 0;
-  return L * N * (6 * sizeof(float2) + sizeof(short)) + 3 * L * L * sizeof(float2) + L * (size_t)V * 8 +
-         tiles * 8 + terms + cs;
+  // per ray T, qs, us, I; per level c, g_c, g_z (and with A > 1 d, g_d)
+  const size_t rays = std::max(K, L);
+  const size_t levels = (m.annuli > 1 ? 5 : 3) * L * N * sizeof(float2);
+  return rays * N * (3 * sizeof(float2) + sizeof(short)) + levels + 3 * L * rays * sizeof(float2) +
+         L * (size_t)V * 8 + tiles * 8 + terms + cs;
 }
 
 void alloc_transmission_grad(Model& m, int chunk, int V, bool store) {
@@ -697,15 +910,20 @@ void alloc_transmission_grad(Model& m, int chunk, int V, bool store) {
     BGB_CUDA(cudaMalloc(&g.taps.tr_ts, (B * L * (size_t)m.acfg.S * N + 2) * sizeof(float2)));
     BGB_CUDA(cudaMalloc(&g.taps.tr_dk, (B * L * N + 2) * sizeof(float2)));
   }
-  const size_t n = B * L * N, tiles = (N + 31) / 32;
+  // per-ray arrays: one row per level (rays at the levels) or per ray (A > 1)
+  const size_t n = B * L * N, tiles = (N + 31) / 32, nr = B * std::max<size_t>(transmission_rays(m), L) * N;
   BGB_CUDA(cudaMalloc(&g.taps.tr_c, n * sizeof(float2)));
-  BGB_CUDA(cudaMalloc(&g.taps.tr_T, n * sizeof(float2)));
-  BGB_CUDA(cudaMalloc(&g.taps.tr_qs, n * sizeof(float2)));
-  BGB_CUDA(cudaMalloc(&g.taps.tr_us, n * sizeof(float2)));
-  BGB_CUDA(cudaMalloc(&g.taps.tr_I, n * sizeof(short)));
-  BGB_CUDA(cudaMalloc(&g.taps.tr_geo, B * 3 * L * L * sizeof(float2)));
+  BGB_CUDA(cudaMalloc(&g.taps.tr_T, nr * sizeof(float2)));
+  BGB_CUDA(cudaMalloc(&g.taps.tr_qs, nr * sizeof(float2)));
+  BGB_CUDA(cudaMalloc(&g.taps.tr_us, nr * sizeof(float2)));
+  BGB_CUDA(cudaMalloc(&g.taps.tr_I, nr * sizeof(short)));
+  BGB_CUDA(cudaMalloc(&g.taps.tr_geo, nr / N * 3 * L * sizeof(float2)));
   BGB_CUDA(cudaMalloc(&g.tr_gc, (n + 2) * sizeof(float2)));
   BGB_CUDA(cudaMalloc(&g.tr_gz, (n + 2) * sizeof(float2)));
+  if (m.annuli > 1) {
+    BGB_CUDA(cudaMalloc(&g.taps.tr_d, n * sizeof(float2)));
+    BGB_CUDA(cudaMalloc(&g.tr_gd, (n + 2) * sizeof(float2)));
+  }
   BGB_CUDA(cudaMalloc(&g.tr_rp, B * tiles * sizeof(double)));
   BGB_CUDA(cudaMalloc(&g.partial, B * L * (size_t)V * sizeof(double)));
   if (m.acfg.cloud_kind) {
@@ -1027,19 +1245,25 @@ void transmission_adjoint_chunk(Model& m, const double* params_chunk, int nb, cu
   const ForwardTaps& tp = g.taps;
   const int L = m.L, S = m.acfg.S, P = m.acfg.nparam_total;
   const size_t N = m.N;
-  const int tiles = (int)((N + 31) / 32);
   const int tiles2a = (int)((N + 63) / 64);  // pass 2a: 64 wavenumbers per block (the d log L / dR partials)
   TrArgs a{w.lev, w.lsdf, w.ray_n, w.ev, reinterpret_cast<const float2*>(w.geom), tp.tr_geo, tp.dwT, g.gS,
            g.seed, tp.tr_c, tp.tr_T, tp.tr_qs, tp.tr_us, tp.tr_I, g.tr_gc, g.tr_gz, g.tr_rp, g.partial, V,
            tp.tr_ts, tp.tr_dk, g.tr_cs, m.acfg.cloud_kind == 1 ? 1 : m.acfg.cloud_kind == 2 ? 3 : 0};
+  a.rays = w.rays;
+  a.d = tp.tr_d;
+  a.gd = g.tr_gd;
   if (g.tr_cs) {
     tr_cloud_shape_kernel<<<dim3(nb, (unsigned)((N + 255) / 256)), 256, 0, st>>>(dm, w.ev, g.tr_cs, a.nc);
     BGB_CUDA(cudaGetLastError());
   }
-  const size_t sm2a = (size_t)L * 32 * (sizeof(float4) + sizeof(short2)) + (size_t)3 * L * sizeof(float2);
-  if (sm2a > 48 * 1024)
-    BGB_CUDA(cudaFuncSetAttribute(tr_adjoint_pass2a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2a));
-  tr_adjoint_pass2a<<<dim3(tiles2a, nb), 32 * kPass2aGroups, sm2a, st>>>(dm, a);
+  if (m.annuli > 1) {
+    tr_adjoint_pass2a_annuli<<<dim3(tiles2a, nb), 32 * kPass2aGroups, 0, st>>>(dm, a);
+  } else {
+    const size_t sm2a = (size_t)L * 32 * (sizeof(float4) + sizeof(short2)) + (size_t)3 * L * sizeof(float2);
+    if (sm2a > 48 * 1024)
+      BGB_CUDA(cudaFuncSetAttribute(tr_adjoint_pass2a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2a));
+    tr_adjoint_pass2a<<<dim3(tiles2a, nb), 32 * kPass2aGroups, sm2a, st>>>(dm, a);
+  }
   BGB_CUDA(cudaGetLastError());
   const size_t sm2 = (size_t)S * kTrSinkThreads * (sizeof(float2) + sizeof(double)) + (size_t)m.acfg.R * sizeof(float2);
   const int VP = V <= 8 ? 8 : V <= 16 ? 16 : 32;

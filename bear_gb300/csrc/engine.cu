@@ -355,6 +355,9 @@ constexpr int kHeightGroups = 8;
 __global__ void tr_geometry_adjoint_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
                                            const EvalInfo* __restrict__ ev, const float2* __restrict__ geom,
                                            float2* __restrict__ geo);
+__global__ void tr_geometry_adjoint_annuli_kernel(DeviceModel dm, const LevelInfo* __restrict__ lev,
+                                                  const EvalInfo* __restrict__ ev, const float2* __restrict__ geom,
+                                                  const double* __restrict__ rays, float2* __restrict__ geo);
 
 // Extinction abs + scat + cloud of every level of wavenumber k into the staged column
 // chi[l][VPB] (double-floats with DF, FP64 otherwise); thread j of the wavenumber's TPN
@@ -915,11 +918,17 @@ inline size_t annuli_dyn_smem(int L, int R, bool df) {
   return 2 * (size_t)L * 32 * sizeof(double) + (df ? (size_t)L * R * sizeof(float2) : 0);
 }
 
-template <bool DF, int VPB, int TPN, int RG>
+// With STORE (double-float path, the gradient's forward pass) the kernel also writes, per
+// (evaluation, level, wavenumber), the pair sums c_i and differences d_i = chi_{i+1} - chi_i,
+// and per (evaluation, ray, wavenumber) the ray transmission, the last segment inside the
+// cut-off and the ray sum of the extinction times dG/db (b = R + zb the impact radius; dG/db
+// from taps.tr_geo, computed before this kernel).
+template <bool DF, int VPB, int TPN, int RG, bool STORE = false>
 __global__ void __launch_bounds__(TPN * VPB, 4) transmission_annuli_kernel(
     DeviceModel dm, const LevelInfo* __restrict__ lev, const LevelSpecies* __restrict__ ls,
     const LevelSpeciesDF* __restrict__ lsdf, const double* __restrict__ ray_n, const EvalInfo* __restrict__ ev,
-    const double* __restrict__ geom, const double* __restrict__ rays, double* __restrict__ spectrum) {
+    const double* __restrict__ geom, const double* __restrict__ rays, double* __restrict__ spectrum,
+    ForwardTaps taps) {
   extern __shared__ double chi_s[];
   const int L = dm.L, S = dm.S, R = dm.R, A = dm.annuli, K = (L - 1) * A;
   float2* chi_f = reinterpret_cast<float2*>(chi_s);
@@ -961,6 +970,11 @@ __global__ void __launch_bounds__(TPN * VPB, 4) transmission_annuli_kernel(
         const df2 s2 = df_add(x0, x1), d2 = df_sub(x1, x0);
         chi_f[i * VPB + v] = make_float2(s2.hi, s2.lo);
         dif_f[i * VPB + v] = make_float2(d2.hi, d2.lo);
+        if (STORE) {
+          const size_t at = ((size_t)b * L + i) * N + k;
+          taps.tr_c[at] = make_float2(s2.hi, s2.lo);
+          taps.tr_d[at] = make_float2(d2.hi, d2.lo);
+        }
       } else {
         const double c0 = chi_s[i * VPB + v], c1 = chi_s[(i + 1) * VPB + v];
         chi_s[i * VPB + v] = c0 + c1;
@@ -986,24 +1000,38 @@ __global__ void __launch_bounds__(TPN * VPB, 4) transmission_annuli_kernel(
           const float ch = dm.tau_cut_hi, cl = dm.tau_cut_lo;
           auto over = [ch, cl](df2 x) { return x.hi > ch || (x.hi == ch && x.lo > cl); };  // tau > cut-off
           const float2 c0 = chi_f[t * VPB + v], d0 = dif_f[t * VPB + v];
-          df2 ts[RG];
+          df2 ts[RG], qs[RG];
+          int last[RG];
           unsigned live = 0;
+          // STORE: dG/db of the group's rays, in the layout of the path lengths
+          const float2* Qt =
+              STORE ? taps.tr_geo + (size_t)b * 3 * L * K + (size_t)2 * L * K + (size_t)t * L * A + a0 : nullptr;
 #pragma unroll
           for (int u = 0; u < RG; ++u) {
             ts[u] = df2{0.0f, 0.0f};
+            qs[u] = df2{0.0f, 0.0f};
+            last[u] = L - 2;
             if (u < na) {
               const float2 g = __ldg(&Gt[(size_t)t * A + u]), w = wj_s[a0 + u];
               const df2 seg = df_add(df2{c0.x, c0.y}, df_mul(df2{w.x, w.y}, df2{d0.x, d0.y}));
               ts[u] = df_mul(df2{g.x, g.y}, seg);
+              if (STORE) {
+                const float2 q = __ldg(&Qt[(size_t)t * A + u]);
+                qs[u] = df_mul(df2{q.x, q.y}, seg);
+              }
               if (!over(ts[u])) live |= 1u << u;
+              else last[u] = t;
             }
           }
           for (int i = t + 1; i < L - 1 && live; ++i) {
             const float2 c = chi_f[i * VPB + v];
-            float2 g[RG];
+            float2 g[RG], q[RG];
 #pragma unroll
             for (int u = 0; u < RG; ++u)
-              if (u < na) g[u] = __ldg(&Gt[(size_t)i * A + u]);
+              if (u < na) {
+                g[u] = __ldg(&Gt[(size_t)i * A + u]);
+                if (STORE) q[u] = __ldg(&Qt[(size_t)i * A + u]);
+              }
             // branch-free over the group (a finished ray's sum is kept, not advanced), so
             // that the group's independent sums overlap
 #pragma unroll
@@ -1013,6 +1041,12 @@ __global__ void __launch_bounds__(TPN * VPB, 4) transmission_annuli_kernel(
                 const bool l = (live >> u) & 1u;
                 ts[u].hi = l ? n.hi : ts[u].hi;
                 ts[u].lo = l ? n.lo : ts[u].lo;
+                if (STORE) {
+                  const df2 nq = df_fma(df2{q[u].x, q[u].y}, df2{c.x, c.y}, qs[u]);
+                  qs[u].hi = l ? nq.hi : qs[u].hi;
+                  qs[u].lo = l ? nq.lo : qs[u].lo;
+                  if (l && over(n)) last[u] = i;
+                }
                 live &= ~((unsigned)(l && over(n)) << u);
               }
           }
@@ -1021,6 +1055,12 @@ __global__ void __launch_bounds__(TPN * VPB, 4) transmission_annuli_kernel(
           for (int u = 0; u < RG; ++u)
             if (u < na) {
               const df2 T = df_exp_neg(ts[u], et.hi, et.lo);
+              if (STORE) {
+                const size_t at = ((size_t)b * K + t * A + a0 + u) * N + k;
+                taps.tr_T[at] = make_float2(T.hi, T.lo);
+                taps.tr_qs[at] = make_float2(qs[u].hi, qs[u].lo);
+                taps.tr_I[at] = (short)last[u];
+              }
               h = fma(__ldg(&rw[t * A + a0 + u]), df_to_double(df_sub(df_make(1.0f), T)), h);
             }
         } else {
@@ -1464,6 +1504,7 @@ void upload_model(Model& m) {
     BGB_CUDA(cudaFuncSetAttribute(transmission_annuli_kernel<true, 32, 8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_annuli_kernel<true, 32, 8, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     BGB_CUDA(cudaFuncSetAttribute(transmission_annuli_kernel<false, 32, 4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    BGB_CUDA(cudaFuncSetAttribute(transmission_annuli_kernel<true, 32, 4, 4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
   }
 }
 
@@ -1559,16 +1600,28 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
     // A impact parameters per layer: 32 wavenumbers per block, extinction sums and
     // differences staged; the launch shape selects threads per wavenumber x rays summed
     // together: 16 -> 4 x 4, 32 (default) -> 8 x 4, 64 -> 8 x 8 (FP64 path: 4 threads)
-    if (taps) throw Error(BEAR_ERR_UNSUPPORTED, "the transmission gradient needs one impact parameter per level");
     const bool df = m.precision != 1;
     const size_t sm = annuli_dyn_smem(L, dm.R, df);
     if (sm > kTransmissionDynSmem) throw Error(BEAR_ERR_UNSUPPORTED, "too many levels for the transmission kernel");
     const dim3 grid(batch, (dm.N + 31) / 32);
-    const dim3 ggrid(batch, (transmission_rays(m) + 1 + 127) / 128);  // one thread per ray + the top level
+    const int K = transmission_rays(m);
+    const dim3 ggrid(batch, (K + 1 + 127) / 128);  // one thread per ray + the top level
     auto go = [&](auto kernel, int tpn) {
-      kernel<<<grid, tpn * 32, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.rays, w.spectrum);
+      kernel<<<grid, tpn * 32, sm, st>>>(dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.rays, w.spectrum,
+                                         ForwardTaps{});
     };
-    if (df) {
+    if (taps) {
+      // gradient pass: the double-float kernel storing the ray data (4 threads per wavenumber,
+      // 4 rays per group)
+      if (!df) throw Error(BEAR_ERR_UNSUPPORTED, "the transmission gradient runs in precision mode 0");
+      transmission_annuli_geometry_kernel<true><<<ggrid, 128, 0, st>>>(dm, w.lev, w.ev, w.geom, w.rays);
+      BGB_CUDA(cudaGetLastError());
+      tr_geometry_adjoint_annuli_kernel<<<dim3(batch, ((size_t)K * L + 255) / 256), 256, 0, st>>>(
+          dm, w.lev, w.ev, reinterpret_cast<const float2*>(w.geom), w.rays, taps->tr_geo);
+      BGB_CUDA(cudaGetLastError());
+      transmission_annuli_kernel<true, 32, 4, 4, true><<<grid, 4 * 32, sm, st>>>(
+          dm, w.lev, w.ls, w.lsdf, w.ray_n, w.ev, w.geom, w.rays, w.spectrum, *taps);
+    } else if (df) {
       transmission_annuli_geometry_kernel<true><<<ggrid, 128, 0, st>>>(dm, w.lev, w.ev, w.geom, w.rays);
       BGB_CUDA(cudaGetLastError());
       if (rt == 16) go(transmission_annuli_kernel<true, 32, 4, 4>, 4);

@@ -235,6 +235,9 @@ struct ForwardTaps {
   float2* tr_qs = nullptr;   // sum_i c_i Q[t][i] over the ray's terms
   float2* tr_us = nullptr;   // pass 2a: A_t = (R + z_t)(1 - T_t)
   short* tr_I = nullptr;     // last level index inside the cut-off
+  // (with A impact parameters per layer tr_T, tr_qs, tr_us and tr_I hold one row per ray,
+  // K = (L - 1) A rows, and tr_geo 3 x L x K per evaluation)
+  float2* tr_d = nullptr;    // A > 1: extinction differences chi_{i+1} - chi_i
   // transmission, when the gradient's memory budget allows (else the adjoint recomputes them):
   float2* tr_ts = nullptr;   // B x L x S x N: each table species' opacity term n_s sigma_s
   float2* tr_dk = nullptr;   // B x L x N: sum_s term_s (hi_s - lo_s) d wT_s / dT; x = NaN where a
@@ -253,6 +256,7 @@ struct GradWorkspace {
   // transmission adjoint, per (evaluation, level, wavenumber), double-floats
   float2* tr_gc = nullptr;    // d log L / d (chi_j + chi_{j+1})
   float2* tr_gz = nullptr;    // d log L / d z_j
+  float2* tr_gd = nullptr;    // A > 1: d log L / d (chi_{j+1} - chi_j) (the first, partial ray segments)
   double* tr_rp = nullptr;    // per (evaluation, tile) partial d log L / d R_p
   double* tr_cs = nullptr;    // non-grey cloud: B x (1 + NC) x N wavelength factor and its shape derivatives
   bool tr_store = false;      // the forward pass stores the opacity terms (taps.tr_ts, tr_dk)

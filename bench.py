@@ -13,8 +13,7 @@ captured graph); ``e2e`` = the same through the host API with the parameter
 upload and the log-likelihood download inside the timed region; ``plain_path`` =
 one evaluation per bear_loglike call (host in, host out). The adjoint gradient
 of the same batch is timed as well (``gradient``: evals/s and the ratio of its
-time to the forward batch), except for transmission_annuli (10 impact parameters
-per layer, which the adjoint does not cover). L2 is flushed between timed steps
+time to the forward batch). L2 is flushed between timed steps
 (a 512 MiB write) outside the per-step event pair.
 
 The default run (no --workload) adds ``configs``: the same record for the other
@@ -378,9 +377,7 @@ def measure_engine(ctx, workload, batch, steps, warmup, args, cpu_budget_s):
 
     # adjoint gradient: log L and d log L / d params for the batch
     grad = None
-    if workload in ANNULI:
-        grad = {"unavailable": "the adjoint covers one tangent ray per level"}
-    elif not args.no_gradient:
+    if not args.no_gradient:
         G = torch.empty(B, eng.P, dtype=torch.float64, device=ctx.device)
 
         def grad_step():
@@ -393,7 +390,7 @@ def measure_engine(ctx, workload, batch, steps, warmup, args, cpu_budget_s):
         fwd_ms = total_ms / steps
         grad = {"evals_per_s": B / (grad_ms * 1e-3), "ms_per_batch": grad_ms, "forward_ms_per_batch": fwd_ms,
                 "grad_over_forward": grad_ms / fwd_ms, "parameters": eng.P, "steps": n_grad,
-                "kernels_per_batch": 6 if kind == "emission" else 10,
+                "kernels_per_batch": 6 if kind == "emission" else 9 if workload in ANNULI else 10,
                 "api": "bear_loglike_grad_batch (adjoint; forward pass included in the time)"}
         del G
 

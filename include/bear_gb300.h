@@ -199,10 +199,9 @@ int bear_loglike_cube_batch(bear_model* m, const double* cube_dev, int batch, in
  * Discrete choices of the model (table brackets, cloud layer indices, the
  * transmission tau cut-off indices) are held fixed, so d/d cloud-top pressure
  * is 0. Emission, secondary-eclipse and transmission models (grey, power-law and
- * KH clouds, the H- continuum, variable gravity); transmission, H- and non-grey
- * cloud gradients run in precision mode 0, and a transmission model with more
- * than one impact parameter per layer has none (BEAR_ERR_UNSUPPORTED).
- * Stream-ordered. Evaluations run in chunks whose work buffers fit the gradient
+ * KH clouds, the H- continuum, variable gravity, A impact parameters per
+ * layer); transmission, H- and non-grey cloud gradients run in precision mode 0
+ * (else BEAR_ERR_UNSUPPORTED). Stream-ordered. Evaluations run in chunks whose work buffers fit the gradient
  * memory budget. */
 int bear_loglike_grad_batch(bear_model* m, const double* params_dev, int batch, int nb_params,
                             double* loglike_dev, double* grad_dev, uint8_t* neglect_dev,
