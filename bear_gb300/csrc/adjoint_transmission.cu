@@ -436,24 +436,37 @@ __global__ void __launch_bounds__(32 * kPass2aGroups, 2) tr_adjoint_pass2a_annul
     const int kmax = j <= L - 2 ? min((j + 1) * A, K) - 1 : K - 1;
     const float2* Gj = GT + (size_t)j * K;
     const float2* Pj = PT + (size_t)j * K;
-    for (int kr = kmin; kr <= kmax; ++kr) {
-      const int t = kr / A;
-      const short I0 = a.I[rcol0 + (size_t)kr * N], I1 = a.I[rcol1 + (size_t)kr * N];
-      const dfx gtau = ldr(gtau_r, kr);
+    auto ray = [&](int t, short I0, short I1, const dfx& gtau, float2 g, float2 p) {
       // segment j in the ray (and j <= L - 2), segment j - 1 in the ray
       const bool in0 = I0 >= j && j <= L - 2, in1 = I1 >= j && j <= L - 2;
-      if (in0 || in1) {
-        const float2 g = __ldg(&Gj[kr]);
-        gc = dfx_fma(dfx_select(in0, in1, gtau, zx), dfx_bcast(df2{g.x, g.y}), gc);
-      }
+      if (in0 || in1) gc = dfx_fma(dfx_select(in0, in1, gtau, zx), dfx_bcast(df2{g.x, g.y}), gc);
       if (t < j) {
         const bool e0 = I0 >= j - 1 && !in0, e1 = I1 >= j - 1 && !in1;
-        const float2 p = __ldg(&Pj[kr]);
         const dfx pp = dfx_bcast(df2{p.x, p.y});
         if (in0 || in1) pin = dfx_fma(dfx_select(in0, in1, gtau, zx), pp, pin);
         if (e0 || e1) pend = dfx_fma(dfx_select(e0, e1, gtau, zx), pp, pend);
       }
+    };
+    // two rays per step, their loads issued together (same sums, same order); t and jj of
+    // ray kr kept as counters
+    int t = kmin / A, jj = kmin - t * A;
+    int kr = kmin;
+    for (; kr + 1 <= kmax; kr += 2) {
+      const size_t o0 = (size_t)kr * N, o1 = o0 + N;
+      const short Ia0 = a.I[rcol0 + o0], Ia1 = a.I[rcol1 + o0], Ib0 = a.I[rcol0 + o1], Ib1 = a.I[rcol1 + o1];
+      const dfx ga = ldr(gtau_r, kr), gb = ldr(gtau_r, kr + 1);
+      const float2 g0 = __ldg(&Gj[kr]), g1 = __ldg(&Gj[kr + 1]), p0 = __ldg(&Pj[kr]), p1 = __ldg(&Pj[kr + 1]);
+      const int tb = jj + 1 == A ? t + 1 : t;
+      ray(t, Ia0, Ia1, ga, g0, p0);
+      ray(tb, Ib0, Ib1, gb, g1, p1);
+      jj += 2;
+      while (jj >= A) {
+        jj -= A;
+        ++t;
+      }
     }
+    if (kr <= kmax)
+      ray(t, a.I[rcol0 + (size_t)kr * N], a.I[rcol1 + (size_t)kr * N], ldr(gtau_r, kr), __ldg(&Gj[kr]), __ldg(&Pj[kr]));
     // the first segments: rays of layer j (g_d, and (1 - w) D) and of layer j - 1 (w P, w D)
     if (j <= L - 2)
       for (int jj = 0; jj < A; ++jj) {
