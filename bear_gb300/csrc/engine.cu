@@ -1616,7 +1616,8 @@ static void launch_stages(Model& m, const double* params_dev, int batch, const W
       if (!df) throw Error(BEAR_ERR_UNSUPPORTED, "the transmission gradient runs in precision mode 0");
       transmission_annuli_geometry_kernel<true><<<ggrid, 128, 0, st>>>(dm, w.lev, w.ev, w.geom, w.rays);
       BGB_CUDA(cudaGetLastError());
-      tr_geometry_adjoint_annuli_kernel<<<dim3(batch, ((size_t)K * L + 255) / 256), 256, 0, st>>>(
+      tr_geometry_adjoint_annuli_kernel<<<dim3(batch, (unsigned)std::min<size_t>(((size_t)K * L + 255) / 256, 65535)),
+                                          256, 0, st>>>(
           dm, w.lev, w.ev, reinterpret_cast<const float2*>(w.geom), w.rays, taps->tr_geo);
       BGB_CUDA(cudaGetLastError());
       transmission_annuli_kernel<true, 32, 4, 4, true><<<grid, 4 * 32, sm, st>>>(
