@@ -142,7 +142,7 @@ struct TrArgs {
   const double* gS;
   const double* seed;
   const float2* c;
-  const float2* T;
+  float2* T;  // ray transmissions (rewritten in place with d log L / d tau by the annuli pass 2a)
   float2* qs;  // read, then overwritten with the direct altitude sink z1_t
   float2* us;  // written with A_t = (R + z_t)(1 - T_t)
   const short* I;
@@ -392,7 +392,7 @@ __global__ void __launch_bounds__(32 * kPass2aGroups, 2) tr_adjoint_pass2a_annul
   };
   auto bc = [](double x) { return dfx_bcast(df_from_double(x)); };
   // the per-ray stores are rewritten in place: T -> g_tau, us -> A, qs -> z1, then qs -> D
-  float2* gtau_r = const_cast<float2*>(a.T);
+  float2* gtau_r = a.T;
   for (int kr = grp; kr < K; kr += NG) {
     const dfx T = ldr(a.T, kr), omT = dfx_sub(one, T);
     const double z = zb[kr];
